@@ -1,0 +1,239 @@
+/*
+ * mpflow_gb300.h -- C ABI of the GB300-native EIT hot path.
+ *
+ * One shared library, libmpflow_gb300.so, built for sm_103a.  Every entry
+ * point returns an int status (MPF_OK on success); no C++ exception crosses
+ * this boundary.  mpf_last_error() gives the message of the last failure on
+ * the calling thread.  Device pointers are plain CUDA device addresses owned
+ * by the caller; the library owns only the opaque model objects and their
+ * workspaces.  All device work is ordered on the stream passed in (a
+ * cudaStream_t; NULL is the legacy default stream) and no entry point
+ * synchronises the host unless its comment says so.
+ *
+ * Each declaration names the reference (pgebhardt/mpflow) interface it
+ * replaces, as path:line within that project.
+ */
+#ifndef MPFLOW_GB300_H
+#define MPFLOW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* mpf_stream_t; /* == cudaStream_t */
+
+enum mpf_status {
+    MPF_OK = 0,
+    MPF_EINVAL = 1,      /* bad argument: the reference throws std::invalid_argument */
+    MPF_ENOMEM = 2,      /* device or host allocation failed (std::runtime_error) */
+    MPF_ECUDA = 3,       /* a CUDA call failed */
+    MPF_ENOCONV = 4,     /* an iterative solve hit its iteration cap */
+    MPF_EBREAKDOWN = 5,  /* non-positive pivot / curvature (Cholesky info > 0) */
+    MPF_ETIMEOUT = 6,    /* a bounded device-side wait ran out */
+    MPF_EFULL = 7,       /* ELL row has more than 32 entries (std::logic_error) */
+    MPF_ENOTSUP = 8      /* valid request this build does not implement */
+};
+
+/* Source types, include/mpflow/fem/sources.h:31-34 (Sources::Type). */
+enum mpf_source_type { MPF_SOURCE_OPEN = 0, MPF_SOURCE_FIXED = 1 };
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* mpf_last_error(void);
+/* Library version string (src/version.cpp:23-25 analogue). */
+const char* mpf_version(void);
+
+/* ======================================================================== */
+/* Host-side mesh and FEM setup (no GPU needed)                             */
+/* ======================================================================== */
+
+/* Padded row count of a dense matrix: src/numeric/matrix.cpp:49-55 with
+ * math::roundTo, include/mpflow/mathematics.h:42-44. */
+uint32_t mpf_data_rows(uint32_t rows);
+
+/* Concentric-ring disk mesh: ring i (1..rings) carries 6i nodes, so
+ * nodes = 1 + 3 rings (rings+1), elements = 6 rings^2.  Replaces the
+ * distmesh branch of IrregularMesh::fromConfig
+ * (src/numeric/irregular_mesh.cpp:87-122), whose library is not available.
+ * nodes: n x 2 row-major; elements: e x 3 row-major, counter-clockwise. */
+int mpf_ring_mesh_counts(int32_t rings, int32_t* n_nodes, int32_t* n_elements);
+int mpf_ring_mesh(int32_t rings, double radius, double* nodes, int32_t* elements);
+
+/* Edge table, element->edge map and boundary edge list.  Replaces
+ * distmesh::utils::findUniqueEdges / getTriangulationEdgeIndices /
+ * fixBoundaryEdgeOrientation / boundEdges used at
+ * src/numeric/irregular_mesh.cpp:25-46.  Numbering: elements in order, local
+ * edges (0,1),(1,2),(2,0); interior edges stored (min,max); boundary edges
+ * oriented counter-clockwise around the domain.  edges: cap 3e x 2,
+ * element_edges: e x 3, boundary: cap 3e. */
+int mpf_mesh_edges(int32_t n_nodes, int32_t n_elements, const double* nodes,
+                   const int32_t* elements, int32_t* edges, int32_t* element_edges,
+                   int32_t* boundary, int32_t* n_edges, int32_t* n_boundary);
+
+/* Electrode (port) edge sets on a circular boundary: FEM::Ports::circularBoundary,
+ * src/fem/ports.cpp:32-77.  port_edges: count x cap row-major, -1 padded;
+ * *max_port_edges receives the widest port. */
+int mpf_ports_circular(int32_t n_nodes, const double* nodes, int32_t n_elements,
+                       const int32_t* elements, const int32_t* edges, int32_t n_boundary,
+                       const int32_t* boundary, int32_t count, double width, double offset,
+                       int32_t clockwise, int32_t* port_edges, int32_t cap,
+                       int32_t* max_port_edges);
+
+/* P1 elemental stiffness int grad phi_i . grad phi_j and mass int phi_i phi_j,
+ * e x 3 x 3 row-major each: basis::Linear::integralA / integralB,
+ * src/fem/basis_linear.cpp:72-91. */
+int mpf_p1_elemental(int32_t n_elements, const double* nodes, const int32_t* elements,
+                     double* stiffness, double* mass);
+
+/* Reference ELL layout of the FEM system matrix: column ids (dataRows x 32,
+ * row-major, 0xFFFFFFFF padding) and density, exactly as
+ * Equation::initElementalMatrices leaves sMatrix/rMatrix/systemMatrix
+ * (src/fem/equation.cpp:131-144, src/numeric/sparse_matrix.cpp:396-423). */
+int mpf_ell_layout(int32_t n_nodes, int32_t n_elements, const int32_t* elements,
+                   uint32_t* column_ids, uint32_t* density);
+
+/* Excitation matrix (n x ports, column-major, leading dimension ld):
+ * Equation::initExcitationMatrix, src/fem/equation.cpp:183-215. */
+int mpf_excitation_matrix(int32_t n_nodes, const double* nodes, const int32_t* edges,
+                          int32_t ports, const int32_t* port_edges, int32_t cap, double* exc,
+                          int32_t ld);
+
+/* ======================================================================== */
+/* EIT model: mesh + ports + sources + 2.5D setup, resident on one GPU       */
+/* ======================================================================== */
+
+typedef struct mpf_eit* mpf_eit_t;
+
+/* Constructor arguments of models::EIT (include/mpflow/models/eit.h:38-42,
+ * src/models/eit.cpp:29-95) and of FEM::Sources (src/fem/sources.cpp:27-75).
+ * Patterns are ports x count, column-major (the reference's Matrix<int>). */
+typedef struct mpf_eit_desc {
+    int32_t n_nodes;
+    int32_t n_elements;
+    const double* nodes;        /* n x 2 row-major */
+    const int32_t* elements;    /* e x 3 row-major */
+    const int32_t* edges;       /* edge table from mpf_mesh_edges, n_edges x 2 */
+    int32_t n_edges;
+    int32_t ports;
+    const int32_t* port_edges;  /* ports x port_edges_cap row-major, -1 padded */
+    int32_t port_edges_cap;
+    int32_t drive_count;
+    int32_t meas_count;
+    const double* drive_pattern;  /* ports x drive_count, column-major */
+    const double* meas_pattern;   /* ports x meas_count, column-major */
+    const double* source_values;  /* drive_count values */
+    int32_t source_type;          /* enum mpf_source_type */
+    double reference_value;
+    int32_t logarithmic;          /* 1: sigma = ref * 10^(v/10) */
+    int32_t components;           /* 2.5D harmonics */
+    double height;
+    double port_height;
+    int32_t device;               /* CUDA device ordinal */
+} mpf_eit_desc;
+
+/* Sizes a caller needs to shape its buffers. */
+typedef struct mpf_eit_info {
+    int32_t n_nodes, n_elements, data_rows;  /* data_rows: padded node count */
+    int32_t ports, drive_count, meas_count;
+    int32_t drive_cols_pad, meas_cols_pad;   /* pattern dataCols (multiples of 16) */
+    int32_t jacobian_rows;                   /* drive_cols_pad * meas_cols_pad */
+    int32_t elements_pad;                    /* element count padded to 64 */
+    int32_t density, levels;
+    int32_t unique_columns;                  /* distinct excitation vectors solved */
+    int32_t components, active_components;   /* harmonics with a nonzero excitation */
+} mpf_eit_info;
+
+int mpf_eit_create(const mpf_eit_desc* desc, mpf_eit_t* model);
+int mpf_eit_destroy(mpf_eit_t model);
+int mpf_eit_get_info(mpf_eit_t model, mpf_eit_info* info);
+
+/* Options of the iterative forward solve. */
+typedef struct mpf_solve_opts {
+    double tol;            /* relative residual of every system (per right-hand side) */
+    int32_t max_iter;      /* 0: 10 * n_nodes, the reference default */
+    double refine_tol;     /* > 0: FP64-residual iterative refinement to this level */
+    int32_t max_refine;    /* outer refinement steps (default 6) */
+    int32_t warm_start;    /* 1: start from the fields left by the previous call */
+    int32_t check_every;   /* iterations between host convergence checks (default 16) */
+} mpf_solve_opts;
+
+typedef struct mpf_solve_stats {
+    int32_t iterations;        /* CG iterations of the slowest system, summed over refinements */
+    int32_t refinements;
+    int32_t not_converged;     /* systems that hit max_iter */
+    double max_rel_residual;   /* largest final relative residual (FP64 when refining) */
+    double seconds;            /* host wall time of the call (synchronised) */
+} mpf_solve_stats;
+
+/* sigma -> stiffness S and mass R slot values in the reference ELL layout
+ * (dataRows x 32 row-major per frame), i.e. Equation::update's two
+ * updateMatrix launches (src/fem/equation.cpp:261-274,
+ * src/fem/equation_kernel.cu:60-82).  gamma: frames x n_elements.
+ * s_values / r_values: frames x data_rows x 32 floats. */
+int mpf_eit_assemble(mpf_eit_t model, int32_t frames, const float* gamma, float* s_values,
+                     float* r_values, mpf_stream_t stream);
+
+/* Forward solve of all frames x harmonics x excitations in one batch:
+ * EIT::solve (src/models/eit.cpp:139-213) for current sources.
+ *   gamma:    frames x n_elements (device, float)
+ *   voltages: frames x meas_count x drive_count, column-major per frame
+ *             (the reference's result Matrix, Mm x Md) or NULL
+ *   jacobian: frames x jacobian_rows x n_elements, column-major per frame
+ *             (the reference's jacobian Matrix) or NULL
+ * Synchronises the stream (convergence is checked on the host every
+ * opts->check_every iterations). */
+int mpf_eit_forward(mpf_eit_t model, int32_t frames, const float* gamma, float* voltages,
+                    float* jacobian, const mpf_solve_opts* opts, mpf_solve_stats* stats,
+                    mpf_stream_t stream);
+
+/* Potential fields of the last forward solve in the reference layout
+ * (EIT::fields): component c of frame f as a data_rows x (drive+meas)
+ * column-major float matrix.  fields: frames x components x data_rows x
+ * (drive_count + meas_count). */
+int mpf_eit_fields(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t stream);
+
+/* ======================================================================== */
+/* Regularised Gauss-Newton                                                  */
+/* ======================================================================== */
+
+/* One Gauss-Newton step per frame, solveAbsolute (src/solver/solver.cpp:196-225)
+ * with Inverse::updateJacobian + solve (src/solver/inverse.cpp:60-238) for
+ * R = I, in dual form:
+ *   dgamma = J^T (J J^T + mu I)^{-1} (v_meas - V(gamma)),  mu = (ref*lambda)^2
+ * J J^T from split hi+lo BF16 tcgen05 products, FP64 Cholesky.
+ *   gamma:     frames x n_elements, updated in place
+ *   v_meas:    frames x meas_count x drive_count (column-major per frame)
+ *   residual:  frames doubles, ||v_meas - V(gamma_in)|| / ||v_meas|| (or NULL)
+ * Synchronises the stream. */
+int mpf_gn_step(mpf_eit_t model, int32_t frames, float* gamma, const float* v_meas, double lambda,
+                const mpf_solve_opts* opts, double* residual, mpf_solve_stats* stats,
+                mpf_stream_t stream);
+
+/* ======================================================================== */
+/* Dense building blocks                                                     */
+/* ======================================================================== */
+
+/* C = A A^T for batch row-major FP32 matrices A (rows x cols, leading
+ * dimension lda >= cols, lda % 8 == 0) with split hi+lo BF16 products
+ * (hi.hi + hi.lo + lo.hi) on the tcgen05 tensor cores, FP32 accumulation;
+ * C is rows x rows row-major (symmetric).  rows % 128 == 0, cols % 64 == 0.
+ * The replaced reference product is the cuBLAS J^T J of
+ * src/solver/inverse.cpp:136-156 (taken here in its dual orientation). */
+int mpf_gram_split_bf16(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda,
+                        float* C, mpf_stream_t stream);
+
+/* Batched FP64 Cholesky solve of (A + shift I) X = B, A n x n symmetric
+ * (row-major == column-major), B n x nrhs column-major, per batch entry.
+ * A is overwritten by its factor.  info[batch] (device ints) receives 0 or
+ * the 1-based index of the first non-positive pivot.  Replaces the dense CG
+ * of Inverse::solve (src/solver/inverse.cpp:213-238). */
+int mpf_cholesky_solve_f64(int32_t batch, int32_t n, double* A, double shift, double* B,
+                           int32_t nrhs, int32_t* info, mpf_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPFLOW_GB300_H */

@@ -1,0 +1,229 @@
+// extern "C" entry points of libmpflow_gb300 (declared in include/mpflow_gb300.h).
+// Every entry catches C++ exceptions so none crosses the ABI, and records a
+// thread-local message for mpf_last_error().
+#include <cuda_runtime.h>
+
+#include <exception>
+#include <new>
+
+#include "model.h"
+
+namespace mpf {
+
+static thread_local std::string g_error;
+
+void set_error(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_error = buf;
+}
+
+int fail(int status, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return status;
+}
+
+const char* last_error() { return g_error.c_str(); }
+
+int eit_create(const mpf_eit_desc* d, mpf_eit** out);
+int eit_assemble_export(mpf_eit* m, int F, const float* gamma, float* sOut, float* rOut, cudaStream_t s);
+int eit_forward(mpf_eit* m, int F, const float* gamma, float* V, float* Jref, const mpf_solve_opts* o,
+                mpf_solve_stats* stats, cudaStream_t s);
+int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s);
+int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, const mpf_solve_opts* o,
+            double* residual, mpf_solve_stats* stats, cudaStream_t s);
+void eit_info(const mpf_eit* m, mpf_eit_info* i);
+void eit_destroy(mpf_eit* m);
+
+}  // namespace mpf
+
+#define MPF_GUARD(...)                                                         \
+    try {                                                                      \
+        mpf::set_error("%s", "");                                              \
+        __VA_ARGS__                                                            \
+    } catch (const std::bad_alloc&) {                                          \
+        return mpf::fail(MPF_ENOMEM, "host allocation failed");                \
+    } catch (const std::exception& ex) {                                       \
+        return mpf::fail(MPF_EINVAL, "%s", ex.what());                         \
+    } catch (...) {                                                            \
+        return mpf::fail(MPF_EINVAL, "unknown C++ exception");                 \
+    }
+
+extern "C" {
+
+const char* mpf_last_error(void) { return mpf::last_error(); }
+
+const char* mpf_version(void) { return "mpflow_gb300 0.1.0 (sm_103a)"; }
+
+uint32_t mpf_data_rows(uint32_t rows) { return mpf::data_rows(rows); }
+
+int mpf_ring_mesh_counts(int32_t rings, int32_t* n_nodes, int32_t* n_elements) {
+    MPF_GUARD({
+        MPF_CHECK(rings >= 1 && rings <= 2000 && n_nodes && n_elements, MPF_EINVAL,
+                  "mpf_ring_mesh_counts: rings must be in [1, 2000]");
+        *n_nodes = 1 + 3 * rings * (rings + 1);
+        *n_elements = 6 * rings * rings;
+        return MPF_OK;
+    })
+}
+
+int mpf_ring_mesh(int32_t rings, double radius, double* nodes, int32_t* elements) {
+    MPF_GUARD({
+        MPF_CHECK(nodes && elements, MPF_EINVAL, "mpf_ring_mesh: null output");
+        return mpf::ring_mesh(rings, radius, nodes, elements);
+    })
+}
+
+int mpf_mesh_edges(int32_t n_nodes, int32_t n_elements, const double* nodes, const int32_t* elements,
+                   int32_t* edges, int32_t* element_edges, int32_t* boundary, int32_t* n_edges,
+                   int32_t* n_boundary) {
+    MPF_GUARD({
+        MPF_CHECK(nodes && elements && edges && element_edges && boundary && n_edges && n_boundary, MPF_EINVAL,
+                  "mpf_mesh_edges: null argument");
+        return mpf::mesh_edges(n_nodes, n_elements, nodes, elements, edges, element_edges, boundary, n_edges,
+                               n_boundary);
+    })
+}
+
+int mpf_ports_circular(int32_t n_nodes, const double* nodes, int32_t n_elements, const int32_t* elements,
+                       const int32_t* edges, int32_t n_boundary, const int32_t* boundary, int32_t count, double width,
+                       double offset, int32_t clockwise, int32_t* port_edges, int32_t cap, int32_t* max_port_edges) {
+    MPF_GUARD({
+        MPF_CHECK(nodes && elements && edges && boundary && port_edges && max_port_edges, MPF_EINVAL,
+                  "mpf_ports_circular: null argument");
+        return mpf::ports_circular(n_nodes, nodes, n_elements, elements, edges, n_boundary, boundary, count, width,
+                                   offset, clockwise, port_edges, cap, max_port_edges);
+    })
+}
+
+int mpf_p1_elemental(int32_t n_elements, const double* nodes, const int32_t* elements, double* stiffness,
+                     double* mass) {
+    MPF_GUARD({
+        MPF_CHECK(n_elements > 0 && nodes && elements && stiffness && mass, MPF_EINVAL,
+                  "mpf_p1_elemental: bad arguments");
+        mpf::p1_elemental(n_elements, nodes, elements, stiffness, mass);
+        return MPF_OK;
+    })
+}
+
+int mpf_ell_layout(int32_t n_nodes, int32_t n_elements, const int32_t* elements, uint32_t* column_ids,
+                   uint32_t* density) {
+    MPF_GUARD({
+        MPF_CHECK(elements && column_ids && density, MPF_EINVAL, "mpf_ell_layout: null argument");
+        mpf::FemStructure fs;
+        MPF_TRY(mpf::build_structure(n_nodes, n_elements, elements, fs));
+        std::copy(fs.refColIds.begin(), fs.refColIds.end(), column_ids);
+        *density = (uint32_t)fs.density;
+        return MPF_OK;
+    })
+}
+
+int mpf_excitation_matrix(int32_t n_nodes, const double* nodes, const int32_t* edges, int32_t ports,
+                          const int32_t* port_edges, int32_t cap, double* exc, int32_t ld) {
+    MPF_GUARD({
+        MPF_CHECK(nodes && edges && port_edges && exc && ld >= n_nodes && ports > 0, MPF_EINVAL,
+                  "mpf_excitation_matrix: bad arguments");
+        mpf::excitation_matrix(n_nodes, nodes, edges, ports, port_edges, cap, exc, ld);
+        return MPF_OK;
+    })
+}
+
+int mpf_eit_create(const mpf_eit_desc* desc, mpf_eit_t* model) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_create: model == nullptr");
+        *model = nullptr;
+        return mpf::eit_create(desc, model);
+    })
+}
+
+int mpf_eit_destroy(mpf_eit_t model) {
+    MPF_GUARD({
+        mpf::eit_destroy(model);
+        return MPF_OK;
+    })
+}
+
+int mpf_eit_get_info(mpf_eit_t model, mpf_eit_info* info) {
+    MPF_GUARD({
+        MPF_CHECK(model && info, MPF_EINVAL, "mpf_eit_get_info: null argument");
+        mpf::eit_info(model, info);
+        return MPF_OK;
+    })
+}
+
+int mpf_eit_assemble(mpf_eit_t model, int32_t frames, const float* gamma, float* s_values, float* r_values,
+                     mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_assemble: model == nullptr");
+        return mpf::eit_assemble_export(model, frames, gamma, s_values, r_values, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_forward(mpf_eit_t model, int32_t frames, const float* gamma, float* voltages, float* jacobian,
+                    const mpf_solve_opts* opts, mpf_solve_stats* stats, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_forward: model == nullptr");
+        return mpf::eit_forward(model, frames, gamma, voltages, jacobian, opts, stats, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_fields(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_fields: model == nullptr");
+        return mpf::eit_fields(model, frames, fields, (cudaStream_t)stream);
+    })
+}
+
+int mpf_gn_step(mpf_eit_t model, int32_t frames, float* gamma, const float* v_meas, double lambda,
+                const mpf_solve_opts* opts, double* residual, mpf_solve_stats* stats, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_gn_step: model == nullptr");
+        MPF_CHECK(lambda >= 0.0, MPF_EINVAL, "mpf_gn_step: lambda < 0");
+        return mpf::gn_step(model, frames, gamma, v_meas, lambda, opts, residual, stats, (cudaStream_t)stream);
+    })
+}
+
+int mpf_gram_split_bf16(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda, float* C,
+                        mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(batch >= 1 && A && C && lda >= cols, MPF_EINVAL, "mpf_gram_split_bf16: bad arguments");
+        MPF_CHECK(rows % 128 == 0 && cols % 64 == 0 && lda % 8 == 0, MPF_EINVAL,
+                  "mpf_gram_split_bf16: rows %% 128, cols %% 64 and lda %% 8 must be 0");
+        cudaStream_t s = (cudaStream_t)stream;
+        mpf::DevBuf<__nv_bfloat16> hi, lo;
+        mpf::DevBuf<float> work;
+        MPF_TRY(hi.alloc((size_t)batch * rows * lda));
+        MPF_TRY(lo.alloc((size_t)batch * rows * lda));
+        MPF_TRY(work.alloc(mpf::dense_gram_work_floats(batch, rows, cols)));
+        MPF_TRY(mpf::dense_split_bf16(batch, rows, cols, A, lda, hi.ptr, lo.ptr, s));
+        MPF_TRY(mpf::dense_gram_split_bf16(batch, rows, cols, hi.ptr, lo.ptr, lda, C, work.ptr, work.count, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        bool aborted = false;
+        MPF_TRY(mpf::dense_gram_check_abort(&aborted));
+        MPF_CHECK(!aborted, MPF_ETIMEOUT, "gram kernel: a pipeline wait timed out");
+        return MPF_OK;
+    })
+}
+
+int mpf_cholesky_solve_f64(int32_t batch, int32_t n, double* A, double shift, double* B, int32_t nrhs,
+                           int32_t* info, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(batch >= 1 && n >= 1 && A && B && info && nrhs >= 1, MPF_EINVAL,
+                  "mpf_cholesky_solve_f64: bad arguments");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (shift != 0.0) MPF_TRY(mpf::dense_add_shift(batch, n, A, shift, s));
+        MPF_TRY(mpf::dense_cholesky_f64(batch, n, A, info, s));
+        MPF_TRY(mpf::dense_cholesky_solve_f64(batch, n, A, B, nrhs, s));
+        return MPF_OK;
+    })
+}
+
+}  // extern "C"

@@ -1,0 +1,546 @@
+// Batched Jacobi-preconditioned conjugate gradient for the EIT systems.
+//
+// Restates src/numeric/conjugate_gradient.cpp:61-161 (per-column scalars,
+// Jacobi preconditioner of src/numeric/preconditioner_kernel.cu:63-83, the
+// zero-denominator guards of src/numeric/conjugate_gradient_kernel.cu:77-89)
+// for many independent systems at once: every (frame, harmonic) group has
+// KP right-hand sides that share one matrix S + alpha_c R, and every group
+// runs its own iteration with per-right-hand-side convergence masks.
+//
+// One CG iteration is three launches, each a single pass over the vectors:
+//   k_spmm_dot   q = (S + alpha R) p,  pq = p.q
+//   k_update     x += a p, r -= a q, z = D^-1 r, rz' = r.z  (+ convergence)
+//   k_direction  p = D^-1 r + b p
+// The SpMM fuses S + alpha R (the system matrix is never materialised), reads
+// ELL columns/values once per row (warp-uniform broadcast) and gathers the KP
+// right-hand sides of a neighbour node as one contiguous 128-bit-aligned
+// segment.  Inner products: each thread sums at most 16 products with an
+// error-free (TwoProduct/TwoSum) float pair, everything above that level is
+// FP64; the per-block partials are combined by the last block of the group in
+// a fixed order, so results are deterministic.
+#include "model.h"
+
+namespace mpf {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kRowsPerWarp = kRowTile / kWarps;  // 16
+
+template <int KP>
+struct Shape {
+    static constexpr int LPR = KP >= 32 ? 32 : KP;  // lanes per row
+    static constexpr int VEC = KP / LPR;            // floats per lane
+    static constexpr int SUB = 32 / LPR;            // rows per warp step
+    static constexpr int STEPS = kRowsPerWarp / SUB;
+};
+
+template <int V>
+__device__ __forceinline__ void ldv(const float* p, float (&v)[V]) {
+    if constexpr (V == 1) {
+        v[0] = *p;
+    } else if constexpr (V == 2) {
+        float2 t = *reinterpret_cast<const float2*>(p);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+        float4 t = *reinterpret_cast<const float4*>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+}
+template <int V>
+__device__ __forceinline__ void stv(float* p, const float (&v)[V]) {
+    if constexpr (V == 1) {
+        *p = v[0];
+    } else if constexpr (V == 2) {
+        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    } else {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+// Error-free accumulation of a*b into a float pair (Knuth TwoSum + FMA
+// TwoProduct); value() is exact to about 2^-48 relative per thread.
+struct DotAcc {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float a, float b) {
+        float p = __fmul_rn(a, b);
+        float pe = __fmaf_rn(a, b, -p);
+        float t = __fadd_rn(s, p);
+        float z = __fsub_rn(t, s);
+        float te = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(te, pe));
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+__device__ __forceinline__ float diag_inv(const float* S, const float* R, const int32_t* diagSlot,
+                                          int npad, int row, float alpha) {
+    int ds = __ldg(&diagSlot[row]);
+    float d = __ldg(&S[(size_t)ds * npad + row]) + alpha * __ldg(&R[(size_t)ds * npad + row]);
+    return d != 0.f ? 1.f / d : 0.f;
+}
+
+// Block-level reduction of per-thread partials into part[g][blk][KP]; returns
+// true in every thread of the block that finishes the group last (that block
+// then sees all partials of the group).
+template <int KP, int NDOT>
+__device__ __forceinline__ bool block_partials(const DotAcc (&acc)[NDOT][Shape<KP>::VEC],
+                                               double* const (&part)[NDOT], int g, int nblk,
+                                               unsigned* counter) {
+    using Sh = Shape<KP>;
+    __shared__ double red[NDOT][kWarps * Sh::SUB][KP];
+    __shared__ bool amLast;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+#pragma unroll
+    for (int d = 0; d < NDOT; ++d)
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) red[d][warp * Sh::SUB + sub][j0 + v] = acc[d][v].value();
+    __syncthreads();
+    if (threadIdx.x < KP) {
+#pragma unroll
+        for (int d = 0; d < NDOT; ++d) {
+            double s = 0.0;
+            for (int w = 0; w < kWarps * Sh::SUB; ++w) s += red[d][w][threadIdx.x];
+            part[d][((size_t)g * nblk + blockIdx.x) * KP + threadIdx.x] = s;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) amLast = atomicAdd(&counter[g], 1u) == (unsigned)(nblk - 1);
+    __syncthreads();
+    if (amLast) __threadfence();
+    return amLast;
+}
+
+// Fixed-order sum of the block partials of group g, right-hand side j.
+__device__ __forceinline__ double sum_partials(const double* part, int g, int nblk, int KP, int j) {
+    double s = 0.0;
+    const double* p = part + (size_t)g * nblk * KP + j;
+    for (int b = 0; b < nblk; ++b) s += __ldcg(p + (size_t)b * KP);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// r = b - A x (or r = b), z = D^-1 r, p = z, rz = r.z, bz = b.D^-1 b
+template <int KP>
+__global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
+    using Sh = Shape<KP>;
+    const int g = blockIdx.y;
+    const int f = g / P.Ca, ci = g % P.Ca;
+    const float alpha = P.alpha[ci];
+    const float* S = P.S + (size_t)f * P.W * P.npad;
+    const float* R = P.R + (size_t)f * P.W * P.npad;
+    const size_t vb = (size_t)g * P.npad * KP;
+    const float* b = P.b + (P.bPerGroup ? vb : (size_t)ci * P.npad * KP);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+    DotAcc acc[2][Sh::VEC];
+    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
+    for (int st = 0; st < Sh::STEPS; ++st) {
+        const int row = rowBase + st * Sh::SUB + sub;
+        float bv[Sh::VEC], rv[Sh::VEC];
+        ldv<Sh::VEC>(b + (size_t)row * KP + j0, bv);
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) rv[v] = bv[v];
+        if (!zeroGuess) {
+            const float* x = P.x + vb;
+            float y[Sh::VEC] = {};
+            for (int k = 0; k < P.W; ++k) {
+                const int col = __ldg(&P.cols[(size_t)k * P.npad + row]);
+                const float a = __ldg(&S[(size_t)k * P.npad + row]) + alpha * __ldg(&R[(size_t)k * P.npad + row]);
+                float xv[Sh::VEC];
+                ldv<Sh::VEC>(x + (size_t)col * KP + j0, xv);
+#pragma unroll
+                for (int v = 0; v < Sh::VEC; ++v) y[v] = fmaf(a, xv[v], y[v]);
+            }
+#pragma unroll
+            for (int v = 0; v < Sh::VEC; ++v) rv[v] = bv[v] - y[v];
+        } else {
+            float zv[Sh::VEC] = {};
+            stv<Sh::VEC>(P.x + vb + (size_t)row * KP + j0, zv);
+        }
+        const float di = diag_inv(S, R, P.diagSlot, P.npad, row, alpha);
+        float zv[Sh::VEC];
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) {
+            zv[v] = di * rv[v];
+            acc[0][v].add(rv[v], zv[v]);
+            acc[1][v].add(bv[v], di * bv[v]);
+        }
+        stv<Sh::VEC>(P.r + vb + (size_t)row * KP + j0, rv);
+        stv<Sh::VEC>(P.p + vb + (size_t)row * KP + j0, zv);
+    }
+    double* const parts[2] = {P.partA, P.partB};
+    if (block_partials<KP, 2>(acc, parts, g, P.nblk, P.counter)) {
+        int notConv = 0;
+        if (threadIdx.x < KP) {
+            const int j = threadIdx.x;
+            double rz = sum_partials(P.partA, g, P.nblk, KP, j);
+            double bz = sum_partials(P.partB, g, P.nblk, KP, j);
+            P.rz[(size_t)g * KP + j] = rz;
+            P.bz[(size_t)g * KP + j] = bz;
+            P.beta[(size_t)g * KP + j] = 0.0;
+            int c = rz <= P.tol2 * bz;
+            P.conv[(size_t)g * KP + j] = c;
+            notConv = !c;
+        }
+        int any = __syncthreads_or(notConv);
+        if (threadIdx.x == 0) {
+            P.active[g] = any;
+            P.iters[g] = 0;
+            P.counter[g] = 0;
+        }
+    }
+}
+
+// q = (S + alpha R) p, pq = p.q
+template <int KP>
+__global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
+    using Sh = Shape<KP>;
+    const int g = blockIdx.y;
+    if (!P.active[g]) return;
+    const int f = g / P.Ca, ci = g % P.Ca;
+    const float alpha = P.alpha[ci];
+    const float* S = P.S + (size_t)f * P.W * P.npad;
+    const float* R = P.R + (size_t)f * P.W * P.npad;
+    const size_t vb = (size_t)g * P.npad * KP;
+    const float* p = P.p + vb;
+    float* q = P.q + vb;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+    DotAcc acc[1][Sh::VEC];
+    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
+    for (int st = 0; st < Sh::STEPS; ++st) {
+        const int row = rowBase + st * Sh::SUB + sub;
+        float y[Sh::VEC] = {};
+        for (int k = 0; k < P.W; ++k) {
+            const int col = __ldg(&P.cols[(size_t)k * P.npad + row]);
+            const float a = __ldg(&S[(size_t)k * P.npad + row]) + alpha * __ldg(&R[(size_t)k * P.npad + row]);
+            float xv[Sh::VEC];
+            ldv<Sh::VEC>(p + (size_t)col * KP + j0, xv);
+#pragma unroll
+            for (int v = 0; v < Sh::VEC; ++v) y[v] = fmaf(a, xv[v], y[v]);
+        }
+        stv<Sh::VEC>(q + (size_t)row * KP + j0, y);
+        float pv[Sh::VEC];
+        ldv<Sh::VEC>(p + (size_t)row * KP + j0, pv);
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) acc[0][v].add(pv[v], y[v]);
+    }
+    double* const parts[1] = {P.partA};
+    if (block_partials<KP, 1>(acc, parts, g, P.nblk, P.counter)) {
+        if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, P.nblk, KP, threadIdx.x);
+        if (threadIdx.x == 0) P.counter[g] = 0;
+    }
+}
+
+// x += a p, r -= a q, z = D^-1 r, rz' = r.z; the last block updates the
+// scalars, the convergence mask and the group's active flag.
+template <int KP>
+__global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
+    using Sh = Shape<KP>;
+    const int g = blockIdx.y;
+    if (!P.active[g]) return;
+    const int f = g / P.Ca, ci = g % P.Ca;
+    const float alpha = P.alpha[ci];
+    const float* S = P.S + (size_t)f * P.W * P.npad;
+    const float* R = P.R + (size_t)f * P.W * P.npad;
+    const size_t vb = (size_t)g * P.npad * KP;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+    float a[Sh::VEC];
+#pragma unroll
+    for (int v = 0; v < Sh::VEC; ++v) {
+        const size_t s = (size_t)g * KP + j0 + v;
+        const double pq = P.pq[s];
+        a[v] = (!P.conv[s] && pq != 0.0) ? (float)(P.rz[s] / pq) : 0.f;
+    }
+    DotAcc acc[1][Sh::VEC];
+    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
+    for (int st = 0; st < Sh::STEPS; ++st) {
+        const int row = rowBase + st * Sh::SUB + sub;
+        const size_t o = vb + (size_t)row * KP + j0;
+        float xv[Sh::VEC], rv[Sh::VEC], pv[Sh::VEC], qv[Sh::VEC];
+        ldv<Sh::VEC>(P.x + o, xv);
+        ldv<Sh::VEC>(P.r + o, rv);
+        ldv<Sh::VEC>(P.p + o, pv);
+        ldv<Sh::VEC>(P.q + o, qv);
+        const float di = diag_inv(S, R, P.diagSlot, P.npad, row, alpha);
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) {
+            xv[v] = fmaf(a[v], pv[v], xv[v]);
+            rv[v] = fmaf(-a[v], qv[v], rv[v]);
+            acc[0][v].add(rv[v], di * rv[v]);
+        }
+        stv<Sh::VEC>(P.x + o, xv);
+        stv<Sh::VEC>(P.r + o, rv);
+    }
+    double* const parts[1] = {P.partA};
+    if (block_partials<KP, 1>(acc, parts, g, P.nblk, P.counter)) {
+        int notConv = 0;
+        if (threadIdx.x < KP) {
+            const size_t s = (size_t)g * KP + threadIdx.x;
+            if (!P.conv[s]) {
+                const double rzn = sum_partials(P.partA, g, P.nblk, KP, threadIdx.x);
+                const double rzo = P.rz[s];
+                P.beta[s] = rzo != 0.0 ? rzn / rzo : 0.0;
+                P.rz[s] = rzn;
+                const int c = rzn <= P.tol2 * P.bz[s];
+                P.conv[s] = c;
+                notConv = !c;
+            }
+        }
+        int any = __syncthreads_or(notConv);
+        if (threadIdx.x == 0) {
+            P.active[g] = any;
+            P.iters[g] += 1;
+            P.counter[g] = 0;
+        }
+    }
+}
+
+// p = D^-1 r + beta p on the right-hand sides still iterating
+template <int KP>
+__global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
+    using Sh = Shape<KP>;
+    const int g = blockIdx.y;
+    if (!P.active[g]) return;
+    const int f = g / P.Ca, ci = g % P.Ca;
+    const float alpha = P.alpha[ci];
+    const float* S = P.S + (size_t)f * P.W * P.npad;
+    const float* R = P.R + (size_t)f * P.W * P.npad;
+    const size_t vb = (size_t)g * P.npad * KP;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+    float be[Sh::VEC];
+    bool live[Sh::VEC];
+#pragma unroll
+    for (int v = 0; v < Sh::VEC; ++v) {
+        const size_t s = (size_t)g * KP + j0 + v;
+        live[v] = !P.conv[s];
+        be[v] = (float)P.beta[s];
+    }
+    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
+    for (int st = 0; st < Sh::STEPS; ++st) {
+        const int row = rowBase + st * Sh::SUB + sub;
+        const size_t o = vb + (size_t)row * KP + j0;
+        float rv[Sh::VEC], pv[Sh::VEC];
+        ldv<Sh::VEC>(P.r + o, rv);
+        ldv<Sh::VEC>(P.p + o, pv);
+        const float di = diag_inv(S, R, P.diagSlot, P.npad, row, alpha);
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) pv[v] = live[v] ? fmaf(be[v], pv[v], di * rv[v]) : pv[v];
+        stv<Sh::VEC>(P.p + o, pv);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 refinement: r64 = b64 - (S64 + alpha R64) x64, written as the float
+// right-hand side of the next inner solve; rr = |r64|^2, bb = |b64|^2.
+template <int KP>
+__global__ void __launch_bounds__(kThreads) k_residual64(CgProblem P, const double* S64, const double* R64,
+                                                         const double* x64, const double* b64,
+                                                         float* rOut, double* partR, double* partB,
+                                                         double* rr, double* bb) {
+    using Sh = Shape<KP>;
+    const int g = blockIdx.y;
+    const int f = g / P.Ca, ci = g % P.Ca;
+    const double alpha = (double)P.alpha[ci];
+    const double* S = S64 + (size_t)f * P.W * P.npad;
+    const double* R = R64 + (size_t)f * P.W * P.npad;
+    const size_t vb = (size_t)g * P.npad * KP;
+    b64 += (size_t)ci * P.npad * KP;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+    double accR[Sh::VEC] = {}, accB[Sh::VEC] = {};
+    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
+    for (int st = 0; st < Sh::STEPS; ++st) {
+        const int row = rowBase + st * Sh::SUB + sub;
+        double y[Sh::VEC] = {};
+        for (int k = 0; k < P.W; ++k) {
+            const int col = __ldg(&P.cols[(size_t)k * P.npad + row]);
+            const double a = S[(size_t)k * P.npad + row] + alpha * R[(size_t)k * P.npad + row];
+#pragma unroll
+            for (int v = 0; v < Sh::VEC; ++v) y[v] = fma(a, x64[vb + (size_t)col * KP + j0 + v], y[v]);
+        }
+        float ro[Sh::VEC];
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) {
+            const double bv = b64[(size_t)row * KP + j0 + v];
+            const double rv = bv - y[v];
+            ro[v] = (float)rv;
+            accR[v] = fma(rv, rv, accR[v]);
+            accB[v] = fma(bv, bv, accB[v]);
+        }
+        stv<Sh::VEC>(rOut + vb + (size_t)row * KP + j0, ro);
+    }
+    __shared__ double red[2][kWarps * Sh::SUB][KP];
+    __shared__ bool amLast;
+#pragma unroll
+    for (int v = 0; v < Sh::VEC; ++v) {
+        red[0][warp * Sh::SUB + sub][j0 + v] = accR[v];
+        red[1][warp * Sh::SUB + sub][j0 + v] = accB[v];
+    }
+    __syncthreads();
+    if (threadIdx.x < KP) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int w = 0; w < kWarps * Sh::SUB; ++w) {
+            s0 += red[0][w][threadIdx.x];
+            s1 += red[1][w][threadIdx.x];
+        }
+        partR[((size_t)g * P.nblk + blockIdx.x) * KP + threadIdx.x] = s0;
+        partB[((size_t)g * P.nblk + blockIdx.x) * KP + threadIdx.x] = s1;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) amLast = atomicAdd(&P.counter[g], 1u) == (unsigned)(P.nblk - 1);
+    __syncthreads();
+    if (amLast) {
+        __threadfence();
+        if (threadIdx.x < KP) {
+            rr[(size_t)g * KP + threadIdx.x] = sum_partials(partR, g, P.nblk, KP, threadIdx.x);
+            bb[(size_t)g * KP + threadIdx.x] = sum_partials(partB, g, P.nblk, KP, threadIdx.x);
+        }
+        if (threadIdx.x == 0) P.counter[g] = 0;
+    }
+}
+
+__global__ void k_accumulate64(size_t count, const float* x, double* x64) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        x64[i] += (double)x[i];
+}
+
+__global__ void k_to_float(size_t count, const double* x64, float* x) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        x[i] = (float)x64[i];
+}
+
+// Neumann (dcFree) harmonics: the iteration runs on the singular stiffness
+// matrix with a zero-sum right-hand side; the reference's solution of
+// (A + 1 1^T) x = b is the zero-mean solution plus (1^T b / n^2) 1.
+__global__ void __launch_bounds__(kThreads) k_mean_sum(CgProblem P, double* part, double* sums) {
+    const int g = blockIdx.y;
+    if (!P.dcFree[g % P.Ca]) return;
+    const size_t vb = (size_t)g * P.npad * P.KP;
+    __shared__ double red[kThreads];
+    __shared__ bool amLast;
+    const int rows = kRowTile;
+    // thread t handles right-hand side j = t % KP over a strided set of rows
+    const int j = threadIdx.x % P.KP, lanes = kThreads / P.KP > 0 ? kThreads / P.KP : 1;
+    const int r0 = threadIdx.x / P.KP;
+    double s = 0.0;
+    if (threadIdx.x < lanes * P.KP)
+        for (int r = r0; r < rows; r += lanes) {
+            const int row = blockIdx.x * kRowTile + r;
+            if (row < P.n) s += (double)P.x[vb + (size_t)row * P.KP + j];
+        }
+    red[threadIdx.x] = threadIdx.x < lanes * P.KP ? s : 0.0;
+    __syncthreads();
+    if (threadIdx.x < P.KP) {
+        double t = 0.0;
+        for (int l = 0; l < lanes; ++l) t += red[l * P.KP + threadIdx.x];
+        part[((size_t)g * P.nblk + blockIdx.x) * P.KP + threadIdx.x] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) amLast = atomicAdd(&P.counter[g], 1u) == (unsigned)(P.nblk - 1);
+    __syncthreads();
+    if (amLast) {
+        __threadfence();
+        if (threadIdx.x < P.KP) sums[(size_t)g * P.KP + threadIdx.x] = sum_partials(part, g, P.nblk, P.KP, threadIdx.x);
+        if (threadIdx.x == 0) P.counter[g] = 0;
+    }
+}
+
+__global__ void k_mean_apply(CgProblem P, const double* shift, const double* sums) {
+    const int g = blockIdx.y;
+    if (!P.dcFree[g % P.Ca]) return;
+    const size_t vb = (size_t)g * P.npad * P.KP;
+    const size_t count = (size_t)P.n * P.KP;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(i % P.KP);
+        const double m = sums[(size_t)g * P.KP + j] / (double)P.n;
+        P.x[vb + i] = (float)((double)P.x[vb + i] - m + shift[j]);
+    }
+}
+
+template <template <int> class Launcher, class... Args>
+int dispatch_kp(int KP, Args&&... args) {
+    switch (KP) {
+        case 16: return Launcher<16>::run(args...);
+        case 32: return Launcher<32>::run(args...);
+        case 64: return Launcher<64>::run(args...);
+        case 128: return Launcher<128>::run(args...);
+        default: return fail(MPF_EINVAL, "unsupported right-hand-side width %d", KP);
+    }
+}
+
+template <int KP>
+struct InitL {
+    static int run(const CgProblem& P, bool zeroGuess, cudaStream_t s) {
+        k_init<KP><<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P, zeroGuess ? 1 : 0);
+        MPF_CUDA(cudaGetLastError());
+        return MPF_OK;
+    }
+};
+template <int KP>
+struct IterL {
+    static int run(const CgProblem& P, cudaStream_t s) {
+        dim3 grid(P.nblk, P.G);
+        k_spmm_dot<KP><<<grid, kThreads, 0, s>>>(P);
+        k_update<KP><<<grid, kThreads, 0, s>>>(P);
+        k_direction<KP><<<grid, kThreads, 0, s>>>(P);
+        MPF_CUDA(cudaGetLastError());
+        return MPF_OK;
+    }
+};
+template <int KP>
+struct Res64L {
+    static int run(const CgProblem& P, const double* S64, const double* R64, const double* x64,
+                   const double* b64, double* partR, double* partB, double* rr, double* bb,
+                   cudaStream_t s) {
+        k_residual64<KP><<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P, S64, R64, x64, b64, P.r, partR, partB,
+                                                                 rr, bb);
+        MPF_CUDA(cudaGetLastError());
+        return MPF_OK;
+    }
+};
+
+}  // namespace
+
+int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s) {
+    return dispatch_kp<InitL>(P.KP, P, zeroGuess, s);
+}
+
+int cg_launch_iteration(const CgProblem& P, cudaStream_t s) { return dispatch_kp<IterL>(P.KP, P, s); }
+
+int cg_launch_residual64(const CgProblem& P, const double* S64, const double* R64, const double* x64,
+                         const double* b64, double* partR, double* partB, double* rr, double* bb,
+                         cudaStream_t s) {
+    return dispatch_kp<Res64L>(P.KP, P, S64, R64, x64, b64, partR, partB, rr, bb, s);
+}
+
+int cg_launch_accumulate64(const CgProblem& P, double* x64, cudaStream_t s) {
+    size_t count = (size_t)P.G * P.npad * P.KP;
+    k_accumulate64<<<1216, 256, 0, s>>>(count, P.x, x64);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s) {
+    size_t count = (size_t)P.G * P.npad * P.KP;
+    k_to_float<<<1216, 256, 0, s>>>(count, x64, P.x);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int cg_launch_mean_fix(const CgProblem& P, const double* shift, double* part, double* sums, cudaStream_t s) {
+    k_mean_sum<<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P, part, sums);
+    k_mean_apply<<<dim3(64, P.G), 256, 0, s>>>(P, shift, sums);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+}  // namespace mpf

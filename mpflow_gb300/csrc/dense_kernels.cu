@@ -1,0 +1,552 @@
+// Dense kernels of the Gauss-Newton step.
+//
+//  * k_gram_tc   C = A A^T from split hi+lo BF16 operands on the 5th-gen tensor
+//                cores: TMA (128B-swizzled tiles) -> shared memory -> tcgen05.mma
+//                (kind::f16, FP32 accumulator in tensor memory) -> tcgen05.ld
+//                epilogue.  Only tiles on or above the diagonal are computed
+//                and the K (element) dimension is split over CTAs; a second
+//                kernel reduces the splits in a fixed order and mirrors the
+//                result.  hi.hi + hi.lo + lo.hi is accumulated per k-block.
+//  * Cholesky    blocked right-looking FP64 factorisation (32x32 blocks:
+//                diagonal factor, panel solve, trailing update) and the two
+//                triangular solves, batched over frames.
+// The GEMM replaces the cuBLAS J^T J of src/solver/inverse.cpp:136-156 (taken
+// in dual orientation, J J^T); the factorisation replaces the dense CG of
+// src/solver/inverse.cpp:213-238.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "model.h"
+
+namespace mpf {
+namespace {
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t global_timer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after ~2 s, raising the abort flag instead of hanging.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abortFlag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_timer();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abortFlag) return false;
+        if (global_timer() - t0 > 2000000000ull) {
+            *abortFlag = 1;
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            dst),
+        "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
+        : "memory");
+}
+// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
+// core-matrix groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);      // start address
+    d |= (uint64_t)1 << 16;                      // leading byte offset (unused for SW128 K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;            // stride byte offset
+    d |= (uint64_t)1 << 46;                      // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;                      // 128-byte swizzle
+    return d;
+}
+// instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M=128, N=128
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            dtmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%"
+        "20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---------------------------------------------------------------------------
+constexpr int kTile = 128;                       // M = N tile
+constexpr int kBK = 64;                          // K block (128 bytes of BF16)
+constexpr int kStages = 3;
+constexpr int kTileBytes = kTile * kBK * 2;      // 16 KB
+constexpr int kStageBytes = 4 * kTileBytes;      // A_hi, A_lo, B_hi, B_lo
+constexpr int kGramSmem = kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
+
+struct GramArgs {
+    int rows;        // rows per batch entry (multiple of 128)
+    int kblocks;     // K blocks (cols / 64)
+    int tiles;       // upper-triangular tile count per batch entry
+    int nt;          // tiles per dimension
+    int splits;      // K splits
+    float* work;     // [batch][splits][tiles][128][128]
+    int* abortFlag;  // device flag raised by a timed-out wait
+};
+
+// One CTA = one (batch, upper tile, K split).  Warp 0 lane 0 issues TMA,
+// warp 1 lane 0 issues the MMAs, all four warps drain TMEM.
+__global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUtensorMap mapHi,
+                                                    const __grid_constant__ CUtensorMap mapLo, GramArgs ga) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + kStages * kStageBytes);
+    __shared__ uint32_t tmemBase;
+    __shared__ int localAbort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.z;
+    const int split = blockIdx.y;
+    // tile index -> (tm, tn) with tm <= tn
+    int t = blockIdx.x, tm = 0;
+    while (t >= ga.nt - tm) {
+        t -= ga.nt - tm;
+        ++tm;
+    }
+    const int tn = tm + t;
+    const int kb0 = (int)((long)ga.kblocks * split / ga.splits);
+    const int kb1 = (int)((long)ga.kblocks * (split + 1) / ga.splits);
+    const int nk = kb1 - kb0;
+
+    const uint32_t fullBar = smem_u32(&bars[0]);
+    const uint32_t emptyBar = smem_u32(&bars[kStages]);
+    const uint32_t doneBar = smem_u32(&bars[2 * kStages]);
+
+    if (threadIdx.x == 0) {
+        localAbort = 0;
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(fullBar + 8 * s, 1);
+            mbar_init(emptyBar + 8 * s, 1);
+        }
+        mbar_init(doneBar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmemBase)),
+                     "r"(128));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmemBase;
+    volatile int* abortFlag = &localAbort;
+
+    const int rowA = b * ga.rows + tm * kTile;
+    const int rowB = b * ga.rows + tn * kTile;
+    const uint32_t smemBase = smem_u32(smem);
+
+    if (warp == 0 && lane == 0) {
+        // producer
+        for (int i = 0; i < nk; ++i) {
+            const int s = i % kStages, round = i / kStages;
+            if (round > 0 && !mbar_wait(emptyBar + 8 * s, (round - 1) & 1, abortFlag)) break;
+            const uint32_t st = smemBase + s * kStageBytes;
+            mbar_expect_tx(fullBar + 8 * s, kStageBytes);
+            const int x = (kb0 + i) * kBK;
+            tma_load_2d(st, &mapHi, fullBar + 8 * s, x, rowA);
+            tma_load_2d(st + kTileBytes, &mapLo, fullBar + 8 * s, x, rowA);
+            tma_load_2d(st + 2 * kTileBytes, &mapHi, fullBar + 8 * s, x, rowB);
+            tma_load_2d(st + 3 * kTileBytes, &mapLo, fullBar + 8 * s, x, rowB);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        for (int i = 0; i < nk; ++i) {
+            const int s = i % kStages, round = i / kStages;
+            if (!mbar_wait(fullBar + 8 * s, round & 1, abortFlag)) break;
+            tc_fence_after();
+            const uint32_t st = smemBase + s * kStageBytes;
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; ++kk) {
+                const uint32_t off = kk * 32;
+                const uint64_t aHi = sw128_desc(st + off), aLo = sw128_desc(st + kTileBytes + off);
+                const uint64_t bHi = sw128_desc(st + 2 * kTileBytes + off), bLo = sw128_desc(st + 3 * kTileBytes + off);
+                mma_bf16(tmem, aHi, bHi, (i > 0 || kk > 0) ? 1u : 0u);
+                mma_bf16(tmem, aHi, bLo, 1u);
+                mma_bf16(tmem, aLo, bHi, 1u);
+            }
+            mma_commit(emptyBar + 8 * s);
+        }
+        mma_commit(doneBar);
+    }
+    __syncwarp();
+    // epilogue: every warp drains its 32 TMEM lanes
+    const bool waited = nk > 0 && mbar_wait(doneBar, 0, abortFlag);
+    const bool ok = __all_sync(0xffffffffu, waited && !*abortFlag);
+    tc_fence_after();
+    const int row = warp * 32 + lane;
+    float* out = ga.work + ((((size_t)b * ga.splits + split) * ga.tiles + blockIdx.x) * kTile + row) * kTile;
+    if (ok) {
+#pragma unroll 1
+        for (int c = 0; c < kTile; c += 32) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+#pragma unroll
+            for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4*>(out + c + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+        }
+    } else {
+        for (int c = 0; c < kTile; ++c) out[c] = 0.f;
+        if (threadIdx.x == 0 && nk > 0) atomicExch(ga.abortFlag, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128));
+    }
+}
+
+// Sum the K splits in order and write the full symmetric matrix, either FP32
+// (C) or FP64 with a diagonal shift (A64).
+__global__ void k_gram_reduce(int rows, int tiles, int nt, int splits, const float* __restrict__ work,
+                              float* __restrict__ C, double* __restrict__ A64, double shift) {
+    const int b = blockIdx.z, tile = blockIdx.y;
+    int t = tile, tm = 0;
+    while (t >= nt - tm) {
+        t -= nt - tm;
+        ++tm;
+    }
+    const int tn = tm + t;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kTile * kTile; i += gridDim.x * blockDim.x) {
+        const int r = i / kTile, c = i % kTile;
+        float s = 0.f;
+        for (int sp = 0; sp < splits; ++sp) s += work[(((size_t)b * splits + sp) * tiles + tile) * kTile * kTile + i];
+        const int gr = tm * kTile + r, gc = tn * kTile + c;
+        if (C) {
+            C[(size_t)b * rows * rows + (size_t)gr * rows + gc] = s;
+            C[(size_t)b * rows * rows + (size_t)gc * rows + gr] = s;
+        }
+        if (A64) {
+            const double v = (double)s + (gr == gc ? shift : 0.0);
+            A64[(size_t)b * rows * rows + (size_t)gr * rows + gc] = v;
+            A64[(size_t)b * rows * rows + (size_t)gc * rows + gr] = v;
+        }
+    }
+}
+
+__global__ void k_split_bf16(int batch, int rows, int cols, const float* __restrict__ A, int lda,
+                             __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+    const size_t total = (size_t)batch * rows * lda;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int c = (int)(i % lda);
+        const float v = c < cols ? A[i] : 0.f;
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[i] = h;
+        lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 Cholesky, 32x32 blocks, column-major (lower triangle holds L).
+constexpr int NB = 32;
+
+__global__ void k_potrf_diag(int n, double* A, int k, int* info) {
+    __shared__ double a[NB][NB + 1];
+    __shared__ int bad;
+    double* M = A + (size_t)blockIdx.x * n * n;
+    const int o = k * NB;
+    for (int i = threadIdx.x; i < NB * NB; i += blockDim.x) {
+        const int r = i % NB, c = i / NB;
+        a[r][c] = M[(size_t)(o + r) + (size_t)(o + c) * n];
+    }
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int j = 0; j < NB; ++j) {
+        if (threadIdx.x == 0) {
+            const double d = a[j][j];
+            if (!(d > 0.0)) {
+                if (!bad && info[blockIdx.x] == 0) info[blockIdx.x] = o + j + 1;
+                bad = 1;
+                a[j][j] = 1.0;
+            } else {
+                a[j][j] = sqrt(d);
+            }
+        }
+        __syncthreads();
+        for (int i = j + 1 + threadIdx.x; i < NB; i += blockDim.x) a[i][j] /= a[j][j];
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+            const int i = idx % NB, l = idx / NB;
+            if (l > j && i >= l) a[i][l] -= a[i][j] * a[l][j];
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < NB * NB; i += blockDim.x) {
+        const int r = i % NB, c = i / NB;
+        if (r >= c) M[(size_t)(o + r) + (size_t)(o + c) * n] = a[r][c];
+    }
+}
+
+// L_ik = A_ik L_kk^-T for the block rows below the diagonal block k
+__global__ void k_trsm(int n, double* A, int k) {
+    __shared__ double L[NB][NB + 1];
+    __shared__ double X[NB][NB + 1];
+    double* M = A + (size_t)blockIdx.y * n * n;
+    const int o = k * NB, ro = (k + 1 + blockIdx.x) * NB;
+    for (int i = threadIdx.x; i < NB * NB; i += blockDim.x) {
+        const int r = i % NB, c = i / NB;
+        L[r][c] = M[(size_t)(o + r) + (size_t)(o + c) * n];
+        X[r][c] = M[(size_t)(ro + r) + (size_t)(o + c) * n];
+    }
+    __syncthreads();
+    if (threadIdx.x < NB) {
+        const int r = threadIdx.x;
+        for (int j = 0; j < NB; ++j) {
+            double s = X[r][j];
+            for (int l = 0; l < j; ++l) s -= X[r][l] * L[j][l];
+            X[r][j] = s / L[j][j];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < NB * NB; i += blockDim.x) {
+        const int r = i % NB, c = i / NB;
+        M[(size_t)(ro + r) + (size_t)(o + c) * n] = X[r][c];
+    }
+}
+
+// A_ij -= L_ik L_jk^T for k < j <= i
+__global__ void k_syrk(int n, double* A, int k) {
+    __shared__ double Li[NB][NB + 1];
+    __shared__ double Lj[NB][NB + 1];
+    double* M = A + (size_t)blockIdx.y * n * n;
+    int t = blockIdx.x, bi = 0;
+    while (t > bi) {
+        t -= bi + 1;
+        ++bi;
+    }
+    const int bj = t;  // bj <= bi, both relative to k+1
+    const int o = k * NB, io = (k + 1 + bi) * NB, jo = (k + 1 + bj) * NB;
+    for (int i = threadIdx.x; i < NB * NB; i += blockDim.x) {
+        const int r = i % NB, c = i / NB;
+        Li[r][c] = M[(size_t)(io + r) + (size_t)(o + c) * n];
+        Lj[r][c] = M[(size_t)(jo + r) + (size_t)(o + c) * n];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
+        const int r = idx % NB, c = idx / NB;
+        double s = 0.0;
+#pragma unroll 8
+        for (int l = 0; l < NB; ++l) s = fma(Li[r][l], Lj[c][l], s);
+        M[(size_t)(io + r) + (size_t)(jo + c) * n] -= s;
+    }
+}
+
+// Forward then backward substitution with L (column-major lower), one block
+// per (batch, right-hand side).
+__global__ void k_chol_solve(int n, const double* __restrict__ Lall, double* __restrict__ Ball, int nrhs) {
+    extern __shared__ double x[];
+    const int b = blockIdx.x / nrhs, c = blockIdx.x % nrhs;
+    const double* L = Lall + (size_t)b * n * n;
+    double* B = Ball + ((size_t)b * nrhs + c) * n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = B[i];
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        const double xj = x[j] / L[(size_t)j + (size_t)j * n];
+        __syncthreads();
+        if (threadIdx.x == 0) x[j] = xj;
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) x[i] -= L[(size_t)i + (size_t)j * n] * xj;
+        __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {
+        const double xj = x[j] / L[(size_t)j + (size_t)j * n];
+        __syncthreads();
+        if (threadIdx.x == 0) x[j] = xj;
+        for (int i = threadIdx.x; i < j; i += blockDim.x) x[i] -= L[(size_t)j + (size_t)i * n] * xj;
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) B[i] = x[i];
+}
+
+__global__ void k_add_shift(int n, double* A, double shift) {
+    double* M = A + (size_t)blockIdx.y * n * n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) M[(size_t)i * n + i] += shift;
+}
+
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int get_encoder(EncodeTiledFn* out) {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    static int status = MPF_OK;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+            status = fail(MPF_ECUDA, "cuTensorMapEncodeTiled unavailable");
+            return;
+        }
+        fn = (EncodeTiledFn)p;
+    });
+    *out = fn;
+    return fn ? MPF_OK : status;
+}
+
+int make_map(CUtensorMap* map, const __nv_bfloat16* base, int totalRows, int ld) {
+    EncodeTiledFn enc;
+    MPF_TRY(get_encoder(&enc));
+    cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)totalRows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kTile};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    MPF_CHECK(r == CUDA_SUCCESS, MPF_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return MPF_OK;
+}
+
+int gram_splits(int tiles, int kblocks) {
+    int s = 148 / tiles;
+    s = std::max(1, std::min(s, kblocks / 8));
+    return std::max(1, std::min(s, kblocks));
+}
+
+int* abort_flag_device() {
+    static int* flag = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) {
+            flag = nullptr;
+            return;
+        }
+        cudaMemset(flag, 0, sizeof(int));
+    });
+    return flag;
+}
+
+}  // namespace
+
+size_t dense_gram_work_floats(int batch, int rows, int cols) {
+    const int nt = rows / kTile, tiles = nt * (nt + 1) / 2, kblocks = cols / kBK;
+    return (size_t)batch * gram_splits(tiles, kblocks) * tiles * kTile * kTile;
+}
+
+static int gram_run(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo, int ld,
+                    float* C, double* A64, double shift, float* work, size_t workFloats, cudaStream_t s) {
+    MPF_CHECK(rows % kTile == 0 && cols % kBK == 0 && ld % 8 == 0 && ld >= cols, MPF_EINVAL,
+              "gram: rows %% 128, cols %% 64 and ld %% 8 must be 0 (rows=%d cols=%d ld=%d)", rows, cols, ld);
+    const int nt = rows / kTile, tiles = nt * (nt + 1) / 2, kblocks = cols / kBK;
+    const int splits = gram_splits(tiles, kblocks);
+    MPF_CHECK(workFloats >= (size_t)batch * splits * tiles * kTile * kTile, MPF_EINVAL, "gram: workspace too small");
+    CUtensorMap mHi, mLo;
+    MPF_TRY(make_map(&mHi, hi, batch * rows, ld));
+    MPF_TRY(make_map(&mLo, lo, batch * rows, ld));
+    int* flag = abort_flag_device();
+    MPF_CHECK(flag != nullptr, MPF_ENOMEM, "gram: abort flag allocation failed");
+    static bool attr = false;
+    if (!attr) {
+        MPF_CUDA(cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmem));
+        attr = true;
+    }
+    GramArgs ga{rows, kblocks, tiles, nt, splits, work, flag};
+    k_gram_tc<<<dim3(tiles, splits, batch), 128, kGramSmem, s>>>(mHi, mLo, ga);
+    MPF_CUDA(cudaGetLastError());
+    k_gram_reduce<<<dim3(16, tiles, batch), 256, 0, s>>>(rows, tiles, nt, splits, work, C, A64, shift);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int dense_gram_split_bf16(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo, int ld,
+                          float* C, float* work, size_t workFloats, cudaStream_t s) {
+    return gram_run(batch, rows, cols, hi, lo, ld, C, nullptr, 0.0, work, workFloats, s);
+}
+
+int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo, int ld,
+                         double shift, double* A64, float* work, size_t workFloats, cudaStream_t s) {
+    return gram_run(batch, rows, cols, hi, lo, ld, nullptr, A64, shift, work, workFloats, s);
+}
+
+int dense_gram_check_abort(bool* aborted) {
+    int* flag = abort_flag_device();
+    int h = 0;
+    MPF_CUDA(cudaMemcpy(&h, flag, sizeof(int), cudaMemcpyDeviceToHost));
+    *aborted = h != 0;
+    if (h) MPF_CUDA(cudaMemset(flag, 0, sizeof(int)));
+    return MPF_OK;
+}
+
+int dense_split_bf16(int batch, int rows, int cols, const float* A, int lda, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                     cudaStream_t s) {
+    k_split_bf16<<<2048, 256, 0, s>>>(batch, rows, cols, A, lda, hi, lo);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s) {
+    MPF_CHECK(n % NB == 0, MPF_EINVAL, "cholesky: n must be a multiple of %d (got %d)", NB, n);
+    MPF_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * batch, s));
+    const int nb = n / NB;
+    for (int k = 0; k < nb; ++k) {
+        k_potrf_diag<<<batch, 256, 0, s>>>(n, A, k, info);
+        const int m = nb - k - 1;
+        if (m > 0) {
+            k_trsm<<<dim3(m, batch), 64, 0, s>>>(n, A, k);
+            k_syrk<<<dim3(m * (m + 1) / 2, batch), 256, 0, s>>>(n, A, k);
+        }
+    }
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s) {
+    MPF_CHECK((size_t)n * sizeof(double) <= 48 * 1024, MPF_EINVAL, "cholesky solve: n too large (%d)", n);
+    k_chol_solve<<<batch * nrhs, 512, n * sizeof(double), s>>>(n, L, B, nrhs);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s) {
+    k_add_shift<<<dim3((n + 255) / 256, batch), 256, 0, s>>>(n, A, shift);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+}  // namespace mpf

@@ -1,0 +1,393 @@
+// FEM kernels of the EIT hot path: assembly, electrode voltages, Jacobian,
+// layout exports and the Gauss-Newton residual / parameter update.
+#include <cuda_bf16.h>
+
+#include "model.h"
+
+namespace mpf {
+namespace {
+
+// src/fem/equation_kernel.cu:35-53: linear or dB-like logarithmic parameter.
+__device__ __forceinline__ float mat_param(float ref, float v, int logarithmic) {
+    return logarithmic ? ref * expf(2.302585093f * v / 10.f) : ref * v;
+}
+__device__ __forceinline__ double mat_param64(double ref, double v, int logarithmic) {
+    return logarithmic ? ref * exp(2.302585092994046 * v / 10.0) : ref * v;
+}
+__device__ __forceinline__ float mat_param_deriv(float ref, float v, int logarithmic) {
+    return logarithmic ? (2.302585093f / 10.f) * ref * expf(2.302585093f * v / 10.f) : ref;
+}
+
+// Assembly, restating updateMatrixKernel (src/fem/equation_kernel.cu:60-82):
+// every slot sums its element contributions K_e[ij] * p(gamma_e) in element
+// order, which is the reference's level order.  One thread per slot; the
+// output is slot-major so the SpMM reads it coalesced.
+__global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ cptr,
+                           const int32_t* __restrict__ contrib, const float* __restrict__ Kf,
+                           const float* __restrict__ Mf, const double* __restrict__ Kd,
+                           const double* __restrict__ Md, const float* __restrict__ gamma, float ref,
+                           int logarithmic, float* __restrict__ S, float* __restrict__ R,
+                           double* __restrict__ S64, double* __restrict__ R64) {
+    const int f = blockIdx.y;
+    const size_t slots = (size_t)W * npad;
+    const float* gf = gamma + (size_t)f * E;
+    for (size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x; s < slots; s += (size_t)gridDim.x * blockDim.x) {
+        const int c0 = __ldg(&cptr[s]), c1 = __ldg(&cptr[s + 1]);
+        float vs = 0.f, vr = 0.f;
+        double ds = 0.0, dr = 0.0;
+        for (int c = c0; c < c1; ++c) {
+            const int code = __ldg(&contrib[c]);
+            const float g = __ldg(&gf[code / 9]);
+            const float pg = mat_param(ref, g, logarithmic);
+            vs = fmaf(__ldg(&Kf[code]), pg, vs);
+            vr = fmaf(__ldg(&Mf[code]), pg, vr);
+            if (S64) {
+                const double pg64 = mat_param64((double)ref, (double)g, logarithmic);
+                ds = fma(Kd[code], pg64, ds);
+                dr = fma(Md[code], pg64, dr);
+            }
+        }
+        S[(size_t)f * slots + s] = vs;
+        R[(size_t)f * slots + s] = vr;
+        if (S64) {
+            S64[(size_t)f * slots + s] = ds;
+            R64[(size_t)f * slots + s] = dr;
+        }
+    }
+}
+
+// slot-major [W][npad] -> reference ELL [dataRows][32] (same slot order)
+__global__ void k_export_ell(int W, int npad, int n, int dataRows, const float* __restrict__ src,
+                             float* __restrict__ dst) {
+    const int f = blockIdx.y;
+    const size_t total = (size_t)dataRows * kEllWidth;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int row = (int)(i / kEllWidth), slot = (int)(i % kEllWidth);
+        float v = 0.f;
+        if (row < n && slot < W) v = src[(size_t)f * W * npad + (size_t)slot * npad + row];
+        dst[(size_t)f * total + i] = v;
+    }
+}
+
+// Gm[g][u][v] = sum_n B0[n][u] * X[g][n][v] over the nonzeros of B0 (the
+// excitation vectors only touch electrode nodes).
+__global__ void k_gram_meas(int KP, int npad, int nnz, const int32_t* __restrict__ nzPtr,
+                            const int32_t* __restrict__ nzNode, const double* __restrict__ nzVal,
+                            const float* __restrict__ X, double* __restrict__ Gm) {
+    const int g = blockIdx.x;
+    const float* Xg = X + (size_t)g * npad * KP;
+    for (int pair = threadIdx.x; pair < KP * KP; pair += blockDim.x) {
+        const int u = pair / KP, v = pair % KP;
+        double s = 0.0;
+        for (int c = nzPtr[u]; c < nzPtr[u + 1]; ++c) s += nzVal[c] * (double)Xg[(size_t)nzNode[c] * KP + v];
+        Gm[(size_t)g * KP * KP + pair] = s;
+    }
+    (void)nnz;
+}
+
+// V[f](m, d) = sum_c beta_c * sd * sm * Gm[f,c](um(m), ud(d)): the
+// applyMeasurementPattern GEMM of src/models/eit.cpp:220-245 summed over the
+// harmonics, on the unique excitation columns.
+__global__ void k_voltages(int F, int Ca, int KP, int Mm, int Md, const double* __restrict__ Gm,
+                           const float* __restrict__ beta, const int32_t* __restrict__ measU,
+                           const float* __restrict__ measScale, const int32_t* __restrict__ driveU,
+                           const float* __restrict__ driveScale, float* __restrict__ V) {
+    const int total = F * Mm * Md;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int f = i / (Mm * Md), r = i % (Mm * Md);
+        const int m = r % Mm, d = r / Mm;
+        const int um = measU[m], ud = driveU[d];
+        double s = 0.0;
+        for (int ci = 0; ci < Ca; ++ci)
+            s += (double)beta[ci] * Gm[((size_t)(f * Ca + ci) * KP + um) * KP + ud];
+        V[i] = (float)(s * (double)measScale[m] * (double)driveScale[d]);
+    }
+}
+
+// Jacobian, restating calcJacobianKernel (src/fem/equation_kernel.cu:197-245)
+// for all harmonics at once:
+//   J[d*MP + m][e] = -h p'(gamma_e) sd sm sum_c beta_c^2
+//                    sum_ij Y_c[n_i][ud] K_e[i+3j] Y_c[n_j][um]
+// A block owns 32 consecutive elements (one per lane); warp w owns drive rows
+// [w*DPT, (w+1)*DPT) and all MP measurement rows.  Fields of the 3 element
+// nodes are staged through shared memory per harmonic; the output rows of a
+// warp are 32 consecutive elements, i.e. coalesced 128-byte stores.
+template <int KP, int MP, int DPT>
+__global__ void __launch_bounds__(512) k_jacobian(JacPlan jp, int npad, const float* __restrict__ X,
+                                                  const float* __restrict__ gamma, float* __restrict__ J,
+                                                  __nv_bfloat16* __restrict__ Jhi,
+                                                  __nv_bfloat16* __restrict__ Jlo) {
+    extern __shared__ float jsm[];
+    float(*Ys)[KP][33] = reinterpret_cast<float(*)[KP][33]>(jsm);
+    float(*Ts)[KP][33] = reinterpret_cast<float(*)[KP][33]>(jsm + 3 * KP * 33);
+    float(*Ks)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33);
+    const int f = blockIdx.y;
+    const int e0 = blockIdx.x * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nthreads = blockDim.x;
+    const int e = e0 + lane;
+    for (int i = threadIdx.x; i < 32 * 9; i += nthreads) {
+        const int el = i / 9, k = i % 9;
+        Ks[el][k] = (e0 + el < jp.E) ? jp.Kf[(size_t)(e0 + el) * 9 + k] : 0.f;
+    }
+    float acc[DPT][MP];
+#pragma unroll
+    for (int a = 0; a < DPT; ++a)
+#pragma unroll
+        for (int m = 0; m < MP; ++m) acc[a][m] = 0.f;
+    const int dBase = warp * DPT;
+    const int drives = jp.rowsJ / MP;
+    for (int ci = 0; ci < jp.Ca; ++ci) {
+        const float* Xg = X + ((size_t)f * jp.Ca + ci) * npad * KP;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 32 * 3 * KP; i += nthreads) {
+            const int u = i % KP, l = (i / KP) % 3, el = i / (3 * KP);
+            float v = 0.f;
+            if (e0 + el < jp.E) v = Xg[(size_t)jp.elements[(size_t)(e0 + el) * 3 + l] * KP + u];
+            Ys[l][u][el] = v;
+        }
+        __syncthreads();
+        const float b2 = jp.beta2[ci];
+        for (int i = threadIdx.x; i < 32 * 3 * KP; i += nthreads) {
+            const int el = i % 32, u = (i / 32) % KP, jj = i / (32 * KP);
+            // T_j[u] = sum_i Y[n_i][u] K[i + 3j] (stiffness stored row-major [i][j])
+            Ts[jj][u][el] = b2 * (Ys[0][u][el] * Ks[el][0 * 3 + jj] + Ys[1][u][el] * Ks[el][1 * 3 + jj] +
+                                  Ys[2][u][el] * Ks[el][2 * 3 + jj]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+            float ym[MP];
+#pragma unroll
+            for (int m = 0; m < MP; ++m) {
+                const int um = jp.rowM[m];
+                ym[m] = um >= 0 ? Ys[jj][um][lane] : 0.f;
+            }
+#pragma unroll
+            for (int a = 0; a < DPT; ++a) {
+                const int ud = (dBase + a) < drives ? jp.rowD[(dBase + a) * MP] : -1;
+                const float td = ud >= 0 ? Ts[jj][ud][lane] : 0.f;
+#pragma unroll
+                for (int m = 0; m < MP; ++m) acc[a][m] = fmaf(td, ym[m], acc[a][m]);
+            }
+        }
+    }
+    const bool valid = e < jp.E;
+    const float deriv = valid ? -jp.height * mat_param_deriv(jp.ref, gamma[(size_t)f * jp.E + e], jp.logarithmic) : 0.f;
+    const size_t base = (size_t)f * jp.rowsJ * jp.Epad;
+#pragma unroll
+    for (int a = 0; a < DPT; ++a) {
+#pragma unroll
+        for (int m = 0; m < MP; ++m) {
+            const int row = (dBase + a) * MP + m;
+            if (row >= jp.rowsJ) continue;
+            const float v = valid ? deriv * jp.rowScale[row] * acc[a][m] : 0.f;
+            const size_t o = base + (size_t)row * jp.Epad + e;
+            J[o] = v;
+            if (Jhi) {
+                const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                Jhi[o] = h;
+                Jlo[o] = __float2bfloat16_rn(v - __bfloat162float(h));
+            }
+        }
+    }
+}
+
+// J [rowsJ][Epad] -> reference layout [E][rowsJ] (column-major rowsJ x E)
+__global__ void k_transpose(int rowsJ, int Epad, int E, const float* __restrict__ J, float* __restrict__ Jref) {
+    __shared__ float tile[32][33];
+    const int f = blockIdx.z;
+    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+    const float* src = J + (size_t)f * rowsJ * Epad;
+    float* dst = Jref + (size_t)f * rowsJ * E;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int r = r0 + i, c = c0 + threadIdx.x;
+        tile[i][threadIdx.x] = (r < rowsJ && c < E) ? src[(size_t)r * Epad + c] : 0.f;
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int c = c0 + i, r = r0 + threadIdx.x;
+        if (c < E && r < rowsJ) dst[(size_t)c * rowsJ + r] = tile[threadIdx.x][i];
+    }
+}
+
+// Fields in the reference layout: out[f][c] is dataRows x (Md + Mm)
+// column-major; column col of harmonic c is beta_c * scale_col * Y[u(col)].
+__global__ void k_fields_export(int F, int Ca, int C, const int32_t* __restrict__ compOf, int npad, int KP,
+                                int dataRows, int cols, const int32_t* __restrict__ colU,
+                                const float* __restrict__ colScale, const float* __restrict__ betaC,
+                                const float* __restrict__ X, float* __restrict__ out, int n) {
+    const size_t per = (size_t)dataRows * cols;
+    const size_t total = (size_t)F * C * per;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int f = (int)(i / ((size_t)C * per));
+        const int c = (int)((i / per) % C);
+        const size_t r = i % per;
+        const int node = (int)(r % dataRows), col = (int)(r / dataRows);
+        const int ci = compOf[c];
+        float v = 0.f;
+        if (ci >= 0 && node < n)
+            v = betaC[c] * colScale[col] * X[(((size_t)f * Ca + ci) * npad + node) * KP + colU[col]];
+        out[i] = v;
+    }
+}
+
+// y = vec(v_meas - V) in the Jacobian's row order (d * MP + m), res = |y|/|v_meas|
+__global__ void k_residual(int rowsJ, int Mm, int Md, int MP, const float* __restrict__ vMeas,
+                           const float* __restrict__ V, double* __restrict__ y, double* __restrict__ res) {
+    const int f = blockIdx.x;
+    __shared__ double sy[256], sm[256];
+    double ay = 0.0, am = 0.0;
+    for (int row = threadIdx.x; row < rowsJ; row += blockDim.x) {
+        const int m = row % MP, d = row / MP;
+        double v = 0.0;
+        if (m < Mm && d < Md) {
+            const double meas = vMeas[(size_t)f * Mm * Md + m + (size_t)d * Mm];
+            v = meas - (double)V[(size_t)f * Mm * Md + m + (size_t)d * Mm];
+            am += meas * meas;
+        }
+        y[(size_t)f * rowsJ + row] = v;
+        ay += v * v;
+    }
+    sy[threadIdx.x] = ay;
+    sm[threadIdx.x] = am;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sy[threadIdx.x] += sy[threadIdx.x + s];
+            sm[threadIdx.x] += sm[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) res[f] = sm[0] > 0.0 ? sqrt(sy[0] / sm[0]) : sqrt(sy[0]);
+}
+
+// gamma[e] += sum_r J[r][e] w[r]  (J^T w of the dual Gauss-Newton step,
+// src/solver/inverse.cpp:198-204 then src/solver/solver.cpp:222)
+__global__ void k_update_gamma(int rowsJ, int Epad, int E, const float* __restrict__ J,
+                               const double* __restrict__ w, float* __restrict__ gamma) {
+    extern __shared__ float ws[];
+    const int f = blockIdx.y;
+    for (int r = threadIdx.x; r < rowsJ; r += blockDim.x) ws[r] = (float)w[(size_t)f * rowsJ + r];
+    __syncthreads();
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const float* Jf = J + (size_t)f * rowsJ * Epad;
+    float s = 0.f, c = 0.f;
+    for (int r = 0; r < rowsJ; ++r) {
+        // compensated float sum of J[r][e] * w[r]
+        const float a = __ldg(&Jf[(size_t)r * Epad + e]), b = ws[r];
+        const float p = __fmul_rn(a, b), pe = __fmaf_rn(a, b, -p);
+        const float t = __fadd_rn(s, p), z = __fsub_rn(t, s);
+        const float te = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(te, pe));
+    }
+    gamma[(size_t)f * E + e] += (float)((double)s + (double)c);
+}
+
+}  // namespace
+
+int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
+                        const float* Kf, const float* Mf, const double* Kd, const double* Md,
+                        const float* gamma, float ref, int logarithmic, float* S, float* R,
+                        double* S64, double* R64, cudaStream_t s) {
+    const size_t slots = (size_t)W * npad;
+    int blocks = (int)std::min<size_t>((slots + 255) / 256, 4096);
+    k_assemble<<<dim3(blocks, F), 256, 0, s>>>(W, npad, E, cptr, contrib, Kf, Mf, Kd, Md, gamma, ref,
+                                               logarithmic, S, R, S64, R64);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float* slotMajor,
+                          float* refLayout, cudaStream_t s) {
+    int blocks = (int)std::min<size_t>(((size_t)dataRows * kEllWidth + 255) / 256, 4096);
+    k_export_ell<<<dim3(blocks, F), 256, 0, s>>>(W, npad, n, dataRows, slotMajor, refLayout);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int fem_launch_gram_meas(int G, int KP, int npad, const MeasPlan& mp, const float* X, double* Gm,
+                         cudaStream_t s) {
+    k_gram_meas<<<G, 256, 0, s>>>(KP, npad, mp.nnz, mp.nzPtr, mp.nzNode, mp.nzVal, X, Gm);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int fem_launch_voltages(int F, int Ca, int KP, int Mm, int Md, const double* Gm, const float* beta,
+                        const int32_t* measU, const float* measScale, const int32_t* driveU,
+                        const float* driveScale, float* V, cudaStream_t s) {
+    int total = F * Mm * Md;
+    k_voltages<<<(total + 255) / 256, 256, 0, s>>>(F, Ca, KP, Mm, Md, Gm, beta, measU, measScale, driveU,
+                                                   driveScale, V);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+template <int KP, int MP, int DPT>
+static int launch_jac(int F, const JacPlan& jp, int npad, const float* X, const float* gamma, float* J,
+                      __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s) {
+    const int warps = (jp.rowsJ / MP + DPT - 1) / DPT;
+    MPF_CHECK(warps >= 1 && warps <= 16, MPF_ENOTSUP, "jacobian: %d drive rows not supported", jp.rowsJ / MP);
+    dim3 grid(jp.Epad / 32, F);
+    const size_t smem = sizeof(float) * (6 * KP * 33 + 32 * 9);
+    if (smem > 48 * 1024)
+        MPF_CUDA(cudaFuncSetAttribute(k_jacobian<KP, MP, DPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_jacobian<KP, MP, DPT><<<grid, warps * 32, smem, s>>>(jp, npad, X, gamma, J, Jhi, Jlo);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int fem_launch_jacobian(int F, const JacPlan& jp, int MP, int npad, const float* X, const float* gamma,
+                               float* J, __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s) {
+    const int drives = jp.rowsJ / MP;
+#define MPF_JAC(KPv, MPv, DPTv) \
+    if (jp.KP == KPv && MP == MPv && (drives + DPTv - 1) / DPTv <= 16 && (DPTv == 1 || drives > 16 * (DPTv / 2))) \
+        return launch_jac<KPv, MPv, DPTv>(F, jp, npad, X, gamma, J, Jhi, Jlo, s);
+    MPF_JAC(16, 16, 1)
+    MPF_JAC(32, 16, 1)
+    MPF_JAC(32, 32, 1)
+    MPF_JAC(32, 32, 2)
+    MPF_JAC(64, 32, 1)
+    MPF_JAC(64, 32, 2)
+    MPF_JAC(64, 64, 1)
+    MPF_JAC(64, 64, 2)
+    MPF_JAC(64, 64, 4)
+#undef MPF_JAC
+    return fail(MPF_ENOTSUP, "jacobian: unsupported shape KP=%d MP=%d drives=%d", jp.KP, MP, drives);
+}
+
+int fem_launch_transpose_jacobian(int F, int rowsJ, int Epad, int E, const float* J, float* Jref,
+                                  cudaStream_t s) {
+    dim3 grid((E + 31) / 32, (rowsJ + 31) / 32, F);
+    k_transpose<<<grid, dim3(32, 8), 0, s>>>(rowsJ, Epad, E, J, Jref);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int npad, int KP, int dataRows,
+                               int cols, int n, const int32_t* colU, const float* colScale,
+                               const float* betaC, const float* X, float* out, cudaStream_t s) {
+    k_fields_export<<<2048, 256, 0, s>>>(F, Ca, C, compOf, npad, KP, dataRows, cols, colU, colScale, betaC, X,
+                                         out, n);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, const float* V, double* y,
+                        double* res, cudaStream_t s) {
+    const int MP = rowsJ / (int)data_rows((uint32_t)Md);
+    k_residual<<<F, 256, 0, s>>>(rowsJ, Mm, Md, MP, vMeas, V, y, res);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, const double* w, float* gamma,
+                            cudaStream_t s) {
+    dim3 grid((E + 255) / 256, F);
+    k_update_gamma<<<grid, 256, rowsJ * sizeof(float), s>>>(rowsJ, Epad, E, J, w, gamma);
+    MPF_CUDA(cudaGetLastError());
+    return MPF_OK;
+}
+
+}  // namespace mpf

@@ -1,0 +1,617 @@
+// EIT model: host-side setup of the device-resident structure and the
+// orchestration of the forward solve (EIT::solve, src/models/eit.cpp:139-213)
+// and of one regularised Gauss-Newton step (Solver::solveAbsolute,
+// src/solver/solver.cpp:196-225 with Inverse, src/solver/inverse.cpp:60-238).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+
+#include "model.h"
+
+struct mpf_eit {
+    // sizes
+    int n = 0, E = 0, dataRows = 0, npad = 0, nblk = 0, W = 0, levels = 0;
+    int L = 0, Md = 0, Mm = 0, MdPad = 0, MmPad = 0, rowsJ = 0, Epad = 0;
+    int K = 0, KP = 0, C = 0, Ca = 0;
+    int sourceType = 0, logarithmic = 0, device = 0;
+    float ref = 1.f;
+    double height = 1.0, portHeight = 1.0;
+    // host copies
+    mpf::FemStructure fs;
+    std::vector<int> compOf;          // component -> active index or -1
+    std::vector<float> alphaH, betaH; // per active component
+    std::vector<double> betaAll;      // per component
+    // device: static structure
+    mpf::DevBuf<int32_t> cols, diagSlot, cptr, contrib, elements;
+    mpf::DevBuf<float> Kf, Mf;
+    mpf::DevBuf<double> Kd, Md64;
+    mpf::DevBuf<float> Bc;            // [Ca][npad][KP] right-hand sides per active harmonic
+    mpf::DevBuf<double> Bc64;
+    mpf::DevBuf<float> alpha, beta, beta2, betaC;
+    mpf::DevBuf<int32_t> dcFree, compOfD;
+    mpf::DevBuf<int32_t> nzPtr, nzNode;
+    mpf::DevBuf<double> nzVal;
+    mpf::DevBuf<int32_t> driveU, measU, rowD, rowM, colU;
+    mpf::DevBuf<float> driveScale, measScale, rowScale, colScale;
+    mpf::DevBuf<double> meanShift;    // [KP]
+    int anyDcFree = 0;
+    // workspace, grown on demand
+    int capF = 0, capF64 = 0, capFJ = 0;
+    mpf::DevBuf<float> S, R, X, Rv, Pv, Qv;
+    mpf::DevBuf<double> S64, R64, X64;
+    mpf::DevBuf<double> partA, partB, rz, pq, bz, betaW, rr, bb, Gm, meanPart, meanSums;
+    mpf::DevBuf<int> conv, active, iters;
+    mpf::DevBuf<unsigned> counter;
+    mpf::DevBuf<float> V, J, gramWork;
+    mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
+    mpf::DevBuf<double> A64, y, res;
+    mpf::DevBuf<int> info;
+    std::vector<int> activeHost, itersHost;
+    int* pinnedActive = nullptr;
+    bool fieldsValid = false;
+    int lastFrames = 0;
+    // captured CG iteration chunks keyed by the problem bytes
+    std::map<std::string, cudaGraphExec_t> graphs;
+
+    ~mpf_eit() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        if (pinnedActive) cudaFreeHost(pinnedActive);
+    }
+};
+
+namespace mpf {
+namespace {
+
+int check_device(mpf_eit* m) {
+    MPF_CUDA(cudaSetDevice(m->device));
+    return MPF_OK;
+}
+
+// first nonzero entry of a pattern column, 0 for an all-zero column
+double lead(const double* col, int L) {
+    for (int i = 0; i < L; ++i)
+        if (col[i] != 0.0) return col[i];
+    return 0.0;
+}
+
+}  // namespace
+
+int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
+    MPF_CHECK(d && out, MPF_EINVAL, "mpf_eit_create: null argument");
+    MPF_CHECK(d->n_nodes > 0 && d->n_elements > 0 && d->nodes && d->elements && d->edges && d->port_edges,
+              MPF_EINVAL, "mpf_eit_create: mesh == nullptr");
+    MPF_CHECK(d->ports > 0 && d->drive_count > 1 && d->meas_count > 1, MPF_EINVAL,
+              "mpf_eit_create: need ports > 0 and at least two drive and measurement patterns");
+    MPF_CHECK(d->drive_pattern && d->meas_pattern && d->source_values, MPF_EINVAL,
+              "mpf_eit_create: pattern == nullptr");
+    MPF_CHECK(d->components >= 1, MPF_EINVAL, "mpflow::models::EIT::EIT: components < 1");
+    MPF_CHECK(d->height > 0.0, MPF_EINVAL, "mpFlow::models::EIT::EIT: height <= 0.0");
+    MPF_CHECK(d->port_height > 0.0, MPF_EINVAL, "mpFlow::models::EIT::EIT: portHeight <= 0.0");
+    MPF_CHECK(d->source_type == MPF_SOURCE_OPEN, MPF_ENOTSUP,
+              "mpf_eit_create: voltage (fixed) sources are not implemented in this build");
+    auto m = std::make_unique<mpf_eit>();
+    m->device = d->device;
+    MPF_TRY(check_device(m.get()));
+    m->n = d->n_nodes;
+    m->E = d->n_elements;
+    m->L = d->ports;
+    m->Md = d->drive_count;
+    m->Mm = d->meas_count;
+    m->MdPad = (int)data_rows((uint32_t)m->Md);
+    m->MmPad = (int)data_rows((uint32_t)m->Mm);
+    m->rowsJ = m->MdPad * m->MmPad;
+    m->Epad = round_up(m->E, kElemTile);
+    m->sourceType = d->source_type;
+    m->ref = (float)d->reference_value;
+    m->logarithmic = d->logarithmic ? 1 : 0;
+    m->C = d->components;
+    m->height = d->height;
+    m->portHeight = d->port_height;
+
+    // ---- FEM structure and elemental integrals
+    MPF_TRY(build_structure(m->n, m->E, d->elements, m->fs));
+    m->dataRows = m->fs.dataRows;
+    m->npad = m->fs.npad;
+    m->nblk = m->npad / kRowTile;
+    m->W = m->fs.density;
+    m->levels = m->fs.levels;
+    std::vector<double> K((size_t)m->E * 9), M((size_t)m->E * 9);
+    p1_elemental(m->E, d->nodes, d->elements, K.data(), M.data());
+    std::vector<float> Kf(K.begin(), K.end()), Mf(M.begin(), M.end());
+
+    // ---- excitation matrix and unique right-hand sides
+    std::vector<double> exc((size_t)m->n * m->L);
+    excitation_matrix(m->n, d->nodes, d->edges, m->L, d->port_edges, d->port_edges_cap, exc.data(), m->n);
+    const int L = m->L, Md = m->Md, Mm = m->Mm;
+    std::vector<std::vector<double>> canon;  // canonical pattern columns
+    auto unique_of = [&](const std::vector<double>& col, int& u, float& scale) {
+        double c = lead(col.data(), L);
+        if (c == 0.0) {
+            u = -1;
+            scale = 0.f;
+            return;
+        }
+        std::vector<double> nc(L);
+        for (int i = 0; i < L; ++i) nc[i] = col[i] / c;
+        for (size_t k = 0; k < canon.size(); ++k)
+            if (canon[k] == nc) {
+                u = (int)k;
+                scale = (float)c;
+                return;
+            }
+        canon.push_back(nc);
+        u = (int)canon.size() - 1;
+        scale = (float)c;
+    };
+    std::vector<int32_t> dU(Md), mU(Mm);
+    std::vector<float> dS(Md), mS(Mm);
+    for (int j = 0; j < Md; ++j) {
+        std::vector<double> col(L);
+        for (int i = 0; i < L; ++i) col[i] = d->source_values[j] * d->drive_pattern[i + (size_t)j * L];
+        unique_of(col, dU[j], dS[j]);
+    }
+    for (int j = 0; j < Mm; ++j) {
+        std::vector<double> col(L);
+        for (int i = 0; i < L; ++i) col[i] = d->meas_pattern[i + (size_t)j * L];
+        unique_of(col, mU[j], mS[j]);
+    }
+    if (canon.empty()) canon.push_back(std::vector<double>(L, 0.0));
+    for (auto& u : dU) u = u < 0 ? 0 : u;
+    for (auto& u : mU) u = u < 0 ? 0 : u;
+    m->K = (int)canon.size();
+    m->KP = m->K <= 16 ? 16 : m->K <= 32 ? 32 : m->K <= 64 ? 64 : m->K <= 128 ? 128 : 0;
+    MPF_CHECK(m->KP > 0, MPF_ENOTSUP, "mpf_eit_create: %d distinct excitation patterns (max 128)", m->K);
+    const int KP = m->KP, P = m->npad;
+    std::vector<double> B0((size_t)P * KP, 0.0);
+    for (int u = 0; u < m->K; ++u)
+        for (int nd = 0; nd < m->n; ++nd) {
+            double s = 0.0;
+            for (int i = 0; i < L; ++i) s += exc[nd + (size_t)i * m->n] * canon[u][i];
+            B0[(size_t)nd * KP + u] = s;
+        }
+    // measurement plan: nonzeros of B0 by column
+    std::vector<int32_t> nzPtr(KP + 1, 0), nzNode;
+    std::vector<double> nzVal;
+    for (int u = 0; u < KP; ++u) {
+        for (int nd = 0; nd < m->n; ++nd) {
+            double v = B0[(size_t)nd * KP + u];
+            if (v != 0.0) {
+                nzNode.push_back(nd);
+                nzVal.push_back(v);
+            }
+        }
+        nzPtr[u + 1] = (int32_t)nzNode.size();
+    }
+    if (nzNode.empty()) {
+        nzNode.push_back(0);
+        nzVal.push_back(0.0);
+    }
+
+    // ---- 2.5D components (src/models/eit.cpp:154-157)
+    m->compOf.assign(m->C, -1);
+    m->betaAll.assign(m->C, 0.0);
+    std::vector<int32_t> dcf;
+    double beta0 = 1.0 / m->height;
+    for (int c = 0; c < m->C; ++c) {
+        double alpha = std::pow(2.0 * c * M_PI / m->height, 2);
+        double beta = c == 0 ? 1.0 / m->height
+                             : 2.0 * std::sin(c * M_PI * m->portHeight / m->height) / (c * M_PI * m->portHeight);
+        m->betaAll[c] = beta;
+        // a harmonic whose excitation vanishes to rounding contributes nothing
+        if (std::fabs(beta) <= 1e-12 * std::fabs(beta0)) continue;
+        m->compOf[c] = (int)m->alphaH.size();
+        m->alphaH.push_back((float)alpha);
+        m->betaH.push_back((float)beta);
+        dcf.push_back(c == 0 ? 1 : 0);
+    }
+    m->Ca = (int)m->alphaH.size();
+    m->anyDcFree = dcf.size() && dcf[0] ? 1 : 0;
+    // per active harmonic right-hand sides (the Neumann one projected to zero sum)
+    std::vector<double> Bc((size_t)m->Ca * P * KP, 0.0), shift(KP, 0.0);
+    for (int ci = 0; ci < m->Ca; ++ci) {
+        double* dst = Bc.data() + (size_t)ci * P * KP;
+        std::memcpy(dst, B0.data(), sizeof(double) * (size_t)P * KP);
+        if (dcf[ci]) {
+            for (int u = 0; u < KP; ++u) {
+                double s = 0.0;
+                for (int nd = 0; nd < m->n; ++nd) s += B0[(size_t)nd * KP + u];
+                shift[u] = s / ((double)m->n * (double)m->n);
+                double mean = s / (double)m->n;
+                for (int nd = 0; nd < m->n; ++nd) dst[(size_t)nd * KP + u] -= mean;
+            }
+        }
+    }
+    std::vector<float> Bcf(Bc.begin(), Bc.end());
+
+    // ---- Jacobian row tables and field export tables
+    std::vector<int32_t> rowD(m->rowsJ, -1), rowM(m->rowsJ, -1);
+    std::vector<float> rowS(m->rowsJ, 0.f);
+    for (int dd = 0; dd < m->MdPad; ++dd)
+        for (int mm = 0; mm < m->MmPad; ++mm) {
+            int row = dd * m->MmPad + mm;
+            if (dd < Md && mm < Mm) {
+                rowD[row] = dU[dd];
+                rowM[row] = mU[mm];
+                rowS[row] = dS[dd] * mS[mm];
+            } else {
+                rowD[row] = dd < Md ? dU[dd] : -1;
+                rowM[row] = mm < Mm ? mU[mm] : -1;
+                rowS[row] = 0.f;
+            }
+        }
+    std::vector<int32_t> colU(Md + Mm);
+    std::vector<float> colS(Md + Mm);
+    for (int j = 0; j < Md; ++j) { colU[j] = dU[j]; colS[j] = dS[j]; }
+    for (int j = 0; j < Mm; ++j) { colU[Md + j] = mU[j]; colS[Md + j] = mS[j]; }
+    std::vector<float> beta2(m->Ca), betaC(m->C);
+    for (int ci = 0; ci < m->Ca; ++ci) beta2[ci] = m->betaH[ci] * m->betaH[ci];
+    for (int c = 0; c < m->C; ++c) betaC[c] = m->compOf[c] >= 0 ? (float)m->betaAll[c] : 0.f;
+    std::vector<int32_t> elems(d->elements, d->elements + (size_t)3 * m->E);
+
+    // ---- upload
+    MPF_TRY(m->cols.upload(m->fs.cols));
+    MPF_TRY(m->diagSlot.upload(m->fs.diagSlot));
+    MPF_TRY(m->cptr.upload(m->fs.contribPtr));
+    MPF_TRY(m->contrib.upload(m->fs.contrib));
+    MPF_TRY(m->elements.upload(elems));
+    MPF_TRY(m->Kf.upload(Kf));
+    MPF_TRY(m->Mf.upload(Mf));
+    MPF_TRY(m->Kd.upload(K));
+    MPF_TRY(m->Md64.upload(M));
+    MPF_TRY(m->Bc.upload(Bcf));
+    MPF_TRY(m->Bc64.upload(Bc));
+    MPF_TRY(m->alpha.upload(m->alphaH));
+    MPF_TRY(m->beta.upload(m->betaH));
+    MPF_TRY(m->beta2.upload(beta2));
+    MPF_TRY(m->betaC.upload(betaC));
+    MPF_TRY(m->dcFree.upload(dcf));
+    MPF_TRY(m->compOfD.upload(m->compOf));
+    MPF_TRY(m->nzPtr.upload(nzPtr));
+    MPF_TRY(m->nzNode.upload(nzNode));
+    MPF_TRY(m->nzVal.upload(nzVal));
+    MPF_TRY(m->driveU.upload(dU));
+    MPF_TRY(m->measU.upload(mU));
+    MPF_TRY(m->driveScale.upload(dS));
+    MPF_TRY(m->measScale.upload(mS));
+    MPF_TRY(m->rowD.upload(rowD));
+    MPF_TRY(m->rowM.upload(rowM));
+    MPF_TRY(m->rowScale.upload(rowS));
+    MPF_TRY(m->colU.upload(colU));
+    MPF_TRY(m->colScale.upload(colS));
+    MPF_TRY(m->meanShift.upload(shift));
+    MPF_CUDA(cudaMallocHost(&m->pinnedActive, sizeof(int) * 4096));
+    *out = m.release();
+    return MPF_OK;
+}
+
+static int ensure_workspace(mpf_eit* m, int F, bool refine, bool jacobian) {
+    const size_t G = (size_t)F * m->Ca;
+    const size_t vec = G * m->npad * m->KP;
+    if (F > m->capF) {
+        const size_t slots = (size_t)F * m->W * m->npad;
+        MPF_TRY(m->S.alloc(slots));
+        MPF_TRY(m->R.alloc(slots));
+        // fields survive growth only if the old contents are copied; simpler to invalidate
+        m->X.release();
+        MPF_TRY(m->X.alloc(vec));
+        MPF_CUDA(cudaMemset(m->X.ptr, 0, vec * sizeof(float)));
+        MPF_TRY(m->Rv.alloc(vec));
+        MPF_TRY(m->Pv.alloc(vec));
+        MPF_TRY(m->Qv.alloc(vec));
+        const size_t parts = G * m->nblk * m->KP, sc = G * m->KP;
+        MPF_TRY(m->partA.alloc(parts));
+        MPF_TRY(m->partB.alloc(parts));
+        MPF_TRY(m->meanPart.alloc(parts));
+        MPF_TRY(m->rz.alloc(sc));
+        MPF_TRY(m->pq.alloc(sc));
+        MPF_TRY(m->bz.alloc(sc));
+        MPF_TRY(m->betaW.alloc(sc));
+        MPF_TRY(m->rr.alloc(sc));
+        MPF_TRY(m->bb.alloc(sc));
+        MPF_TRY(m->meanSums.alloc(sc));
+        MPF_TRY(m->conv.alloc(sc));
+        MPF_TRY(m->active.alloc(G));
+        MPF_TRY(m->iters.alloc(G));
+        MPF_TRY(m->counter.alloc(G));
+        MPF_CUDA(cudaMemset(m->counter.ptr, 0, G * sizeof(unsigned)));
+        MPF_TRY(m->Gm.alloc(G * m->KP * m->KP));
+        MPF_TRY(m->V.alloc((size_t)F * m->Mm * m->Md));
+        m->activeHost.resize(G);
+        m->itersHost.resize(G);
+        MPF_CHECK(G <= 4096, MPF_EINVAL, "too many (frame, harmonic) groups in one call: %zu (max 4096)", G);
+        m->capF = F;
+        m->fieldsValid = false;
+        for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+        m->graphs.clear();
+    }
+    if (refine && F > m->capF64) {
+        const size_t slots = (size_t)F * m->W * m->npad;
+        MPF_TRY(m->S64.alloc(slots));
+        MPF_TRY(m->R64.alloc(slots));
+        MPF_TRY(m->X64.alloc(vec));
+        m->capF64 = F;
+    }
+    if (jacobian && F > m->capFJ) {
+        const size_t jsz = (size_t)F * m->rowsJ * m->Epad;
+        MPF_TRY(m->J.alloc(jsz));
+        MPF_TRY(m->Jhi.alloc(jsz));
+        MPF_TRY(m->Jlo.alloc(jsz));
+        MPF_TRY(m->gramWork.alloc(dense_gram_work_floats(F, m->rowsJ, m->Epad)));
+        MPF_TRY(m->A64.alloc((size_t)F * m->rowsJ * m->rowsJ));
+        MPF_TRY(m->y.alloc((size_t)F * m->rowsJ));
+        MPF_TRY(m->res.alloc((size_t)F));
+        MPF_TRY(m->info.alloc((size_t)F));
+        m->capFJ = F;
+    }
+    return MPF_OK;
+}
+
+static CgProblem make_problem(mpf_eit* m, int F, double tol) {
+    CgProblem P{};
+    P.n = m->n;
+    P.npad = m->npad;
+    P.W = m->W;
+    P.KP = m->KP;
+    P.G = F * m->Ca;
+    P.Ca = m->Ca;
+    P.nblk = m->nblk;
+    P.cols = m->cols.ptr;
+    P.diagSlot = m->diagSlot.ptr;
+    P.S = m->S.ptr;
+    P.R = m->R.ptr;
+    P.alpha = m->alpha.ptr;
+    P.x = m->X.ptr;
+    P.r = m->Rv.ptr;
+    P.p = m->Pv.ptr;
+    P.q = m->Qv.ptr;
+    P.b = m->Bc.ptr;
+    P.bPerGroup = 0;
+    P.dcFree = m->dcFree.ptr;
+    P.partA = m->partA.ptr;
+    P.partB = m->partB.ptr;
+    P.rz = m->rz.ptr;
+    P.pq = m->pq.ptr;
+    P.bz = m->bz.ptr;
+    P.beta = m->betaW.ptr;
+    P.conv = m->conv.ptr;
+    P.active = m->active.ptr;
+    P.iters = m->iters.ptr;
+    P.counter = m->counter.ptr;
+    P.tol2 = tol * tol;
+    return P;
+}
+
+// Runs CG iterations until every group converged or max_iter; returns the
+// iteration count of the slowest group and the number of unconverged groups.
+static int run_cg(mpf_eit* m, const CgProblem& P, int maxIter, int checkEvery, cudaStream_t s, int* itersOut,
+                  int* notConverged) {
+    const int G = P.G;
+    std::string key(reinterpret_cast<const char*>(&P), sizeof(P));
+    key += std::to_string(checkEvery);
+    cudaGraphExec_t exec = nullptr;
+    auto it = m->graphs.find(key);
+    if (it != m->graphs.end()) {
+        exec = it->second;
+    } else {
+        cudaStream_t cap;
+        MPF_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t graph;
+        MPF_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        int st = MPF_OK;
+        for (int i = 0; i < checkEvery && st == MPF_OK; ++i) st = cg_launch_iteration(P, cap);
+        cudaError_t e = cudaStreamEndCapture(cap, &graph);
+        cudaStreamDestroy(cap);
+        if (st != MPF_OK) return st;
+        MPF_CHECK(e == cudaSuccess, MPF_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        MPF_CHECK(e == cudaSuccess, MPF_ECUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+        m->graphs[key] = exec;
+    }
+    int done = 0;
+    bool anyActive = true;
+    while (done < maxIter) {
+        MPF_CUDA(cudaGraphLaunch(exec, s));
+        done += checkEvery;
+        MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.active, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        anyActive = false;
+        for (int g = 0; g < G; ++g) anyActive |= m->pinnedActive[g] != 0;
+        if (!anyActive) break;
+    }
+    MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.iters, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    int mx = 0;
+    for (int g = 0; g < G; ++g) mx = std::max(mx, m->pinnedActive[g]);
+    *itersOut = mx;
+    if (anyActive) {
+        MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.active, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        int nc = 0;
+        for (int g = 0; g < G; ++g) nc += m->pinnedActive[g] != 0;
+        *notConverged = nc;
+    } else {
+        *notConverged = 0;
+    }
+    return MPF_OK;
+}
+
+static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
+    o.tol = 1e-6;
+    o.max_iter = 0;
+    o.refine_tol = 0.0;
+    o.max_refine = 6;
+    o.warm_start = 0;
+    o.check_every = 16;
+    if (in) o = *in;
+    if (o.tol <= 0.0) o.tol = 1e-6;
+    if (o.max_iter <= 0) o.max_iter = 10 * n;
+    if (o.max_refine <= 0) o.max_refine = 6;
+    if (o.check_every <= 0) o.check_every = 16;
+}
+
+int eit_assemble(mpf_eit* m, int F, const float* gamma, bool fp64, cudaStream_t s) {
+    return fem_launch_assemble(F, m->W, m->npad, m->E, m->cptr.ptr, m->contrib.ptr, m->Kf.ptr, m->Mf.ptr,
+                               m->Kd.ptr, m->Md64.ptr, gamma, m->ref, m->logarithmic, m->S.ptr, m->R.ptr,
+                               fp64 ? m->S64.ptr : nullptr, fp64 ? m->R64.ptr : nullptr, s);
+}
+
+int eit_assemble_export(mpf_eit* m, int F, const float* gamma, float* sOut, float* rOut, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma, MPF_EINVAL, "mpf_eit_assemble: bad arguments");
+    MPF_TRY(ensure_workspace(m, F, false, false));
+    MPF_TRY(eit_assemble(m, F, gamma, false, s));
+    if (sOut) MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->S.ptr, sOut, s));
+    if (rOut) MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->R.ptr, rOut, s));
+    return MPF_OK;
+}
+
+// Forward solve into the workspace (fields X, voltages V, optional J).
+int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_solve_opts* optsIn,
+                   mpf_solve_stats* stats, cudaStream_t s) {
+    auto t0 = std::chrono::steady_clock::now();
+    mpf_solve_opts o;
+    fill_defaults(optsIn, o, m->n);
+    const bool refine = o.refine_tol > 0.0;
+    MPF_TRY(ensure_workspace(m, F, refine, wantJ));
+    const bool warm = o.warm_start && m->fieldsValid && m->lastFrames == F;
+    MPF_TRY(eit_assemble(m, F, gamma, refine, s));
+    CgProblem P = make_problem(m, F, o.tol);
+    int totalIters = 0, notConv = 0, refinements = 0;
+    double maxRel = 0.0;
+    if (!refine) {
+        MPF_TRY(cg_launch_init(P, !warm, s));
+        MPF_TRY(run_cg(m, P, o.max_iter, o.check_every, s, &totalIters, &notConv));
+    } else {
+        const size_t vec = (size_t)P.G * m->npad * m->KP;
+        if (warm) {
+            // X64 = X (float fields of the previous call)
+            std::vector<char> dummy;
+            (void)dummy;
+            MPF_CUDA(cudaMemsetAsync(m->X64.ptr, 0, vec * sizeof(double), s));
+            MPF_TRY(cg_launch_accumulate64(P, m->X64.ptr, s));
+        } else {
+            MPF_CUDA(cudaMemsetAsync(m->X64.ptr, 0, vec * sizeof(double), s));
+        }
+        std::vector<double> rrH((size_t)P.G * m->KP), bbH((size_t)P.G * m->KP);
+        CgProblem Pin = P;
+        Pin.b = m->Rv.ptr;  // inner right-hand side: the float image of the FP64 residual
+        Pin.bPerGroup = 1;
+        for (int outer = 0; outer <= o.max_refine; ++outer) {
+            MPF_TRY(cg_launch_residual64(P, m->S64.ptr, m->R64.ptr, m->X64.ptr, m->Bc64.ptr, m->partA.ptr,
+                                         m->partB.ptr, m->rr.ptr, m->bb.ptr, s));
+            MPF_CUDA(cudaMemcpyAsync(rrH.data(), m->rr.ptr, sizeof(double) * rrH.size(), cudaMemcpyDeviceToHost, s));
+            MPF_CUDA(cudaMemcpyAsync(bbH.data(), m->bb.ptr, sizeof(double) * bbH.size(), cudaMemcpyDeviceToHost, s));
+            MPF_CUDA(cudaStreamSynchronize(s));
+            maxRel = 0.0;
+            for (size_t i = 0; i < rrH.size(); ++i)
+                if (bbH[i] > 0.0) maxRel = std::max(maxRel, std::sqrt(rrH[i] / bbH[i]));
+            if (maxRel <= o.refine_tol || outer == o.max_refine) break;
+            int it = 0, nc = 0;
+            MPF_TRY(cg_launch_init(Pin, true, s));
+            MPF_TRY(run_cg(m, Pin, o.max_iter, o.check_every, s, &it, &nc));
+            totalIters += it;
+            notConv = std::max(notConv, nc);
+            ++refinements;
+            MPF_TRY(cg_launch_accumulate64(P, m->X64.ptr, s));
+        }
+        MPF_TRY(cg_launch_to_float(P, m->X64.ptr, s));
+        if (maxRel > o.refine_tol) notConv = std::max(notConv, 1);
+    }
+    if (m->anyDcFree) MPF_TRY(cg_launch_mean_fix(P, m->meanShift.ptr, m->meanPart.ptr, m->meanSums.ptr, s));
+    m->fieldsValid = true;
+    m->lastFrames = F;
+    MeasPlan mp{(int)m->nzNode.count, m->nzNode.ptr, nullptr, m->nzVal.ptr, m->nzPtr.ptr};
+    MPF_TRY(fem_launch_gram_meas(P.G, m->KP, m->npad, mp, m->X.ptr, m->Gm.ptr, s));
+    MPF_TRY(fem_launch_voltages(F, m->Ca, m->KP, m->Mm, m->Md, m->Gm.ptr, m->beta.ptr, m->measU.ptr,
+                                m->measScale.ptr, m->driveU.ptr, m->driveScale.ptr, m->V.ptr, s));
+    if (wantJ) {
+        JacPlan jp{m->rowsJ, m->Epad, m->E, m->KP, m->Ca, m->rowD.ptr, m->rowM.ptr, m->rowScale.ptr,
+                   m->beta2.ptr, m->elements.ptr, m->Kf.ptr, m->ref, (float)m->height, m->logarithmic};
+        MPF_TRY(fem_launch_jacobian(F, jp, m->MmPad, m->npad, m->X.ptr, gamma, m->J.ptr, m->Jhi.ptr, m->Jlo.ptr, s));
+    }
+    MPF_CUDA(cudaStreamSynchronize(s));
+    MPF_CUDA(cudaGetLastError());
+    if (stats) {
+        stats->iterations = totalIters;
+        stats->refinements = refinements;
+        stats->not_converged = notConv;
+        stats->max_rel_residual = maxRel;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return notConv ? fail(MPF_ENOCONV, "forward solve: %d systems did not converge", notConv) : MPF_OK;
+}
+
+int eit_forward(mpf_eit* m, int F, const float* gamma, float* V, float* Jref, const mpf_solve_opts* o,
+                mpf_solve_stats* stats, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma, MPF_EINVAL, "mpFlow::models::EIT::solve: materialDistribution == nullptr");
+    int st = eit_forward_ws(m, F, gamma, Jref != nullptr, o, stats, s);
+    if (st != MPF_OK && st != MPF_ENOCONV) return st;
+    if (V) MPF_CUDA(cudaMemcpyAsync(V, m->V.ptr, sizeof(float) * (size_t)F * m->Mm * m->Md, cudaMemcpyDeviceToDevice, s));
+    if (Jref) MPF_TRY(fem_launch_transpose_jacobian(F, m->rowsJ, m->Epad, m->E, m->J.ptr, Jref, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    return st;
+}
+
+int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(m->fieldsValid && F >= 1 && F <= m->lastFrames && out, MPF_EINVAL,
+              "mpf_eit_fields: no forward solve with that many frames");
+    MPF_TRY(fem_launch_fields_export(F, m->Ca, m->C, m->compOfD.ptr, m->npad, m->KP, m->dataRows, m->Md + m->Mm,
+                                     m->n, m->colU.ptr, m->colScale.ptr, m->betaC.ptr, m->X.ptr, out, s));
+    return MPF_OK;
+}
+
+int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, const mpf_solve_opts* o,
+            double* residual, mpf_solve_stats* stats, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma && vMeas, MPF_EINVAL, "mpFlow::solver::Solver::solveAbsolute: bad arguments");
+    int st = eit_forward_ws(m, F, gamma, true, o, stats, s);
+    if (st != MPF_OK && st != MPF_ENOCONV) return st;
+    MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
+    const double mu = (double)m->ref * lambda * (double)m->ref * lambda;
+    MPF_TRY(dense_gram_f64_shift(F, m->rowsJ, m->Epad, m->Jhi.ptr, m->Jlo.ptr, m->Epad, mu, m->A64.ptr,
+                                 m->gramWork.ptr, m->gramWork.count, s));
+    MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s));
+    MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s));
+    MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->J.ptr, m->y.ptr, gamma, s));
+    if (residual) MPF_CUDA(cudaMemcpyAsync(residual, m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
+    std::vector<int> info(F);
+    MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    bool aborted = false;
+    MPF_TRY(dense_gram_check_abort(&aborted));
+    MPF_CHECK(!aborted, MPF_ETIMEOUT, "gram kernel: a pipeline wait timed out");
+    for (int f = 0; f < F; ++f)
+        MPF_CHECK(info[f] == 0, MPF_EBREAKDOWN, "Cholesky of (J J^T + mu I) failed at pivot %d (frame %d)", info[f], f);
+    return st;
+}
+
+void eit_destroy(mpf_eit* m) {
+    if (!m) return;
+    cudaSetDevice(m->device);
+    delete m;
+}
+
+void eit_info(const mpf_eit* m, mpf_eit_info* i) {
+    i->n_nodes = m->n;
+    i->n_elements = m->E;
+    i->data_rows = m->dataRows;
+    i->ports = m->L;
+    i->drive_count = m->Md;
+    i->meas_count = m->Mm;
+    i->drive_cols_pad = m->MdPad;
+    i->meas_cols_pad = m->MmPad;
+    i->jacobian_rows = m->rowsJ;
+    i->elements_pad = m->Epad;
+    i->density = m->W;
+    i->levels = m->levels;
+    i->unique_columns = m->K;
+    i->components = m->C;
+    i->active_components = m->Ca;
+}
+
+}  // namespace mpf

@@ -1,0 +1,115 @@
+// Device-resident EIT model and the launch interfaces of its kernels.
+//
+// Data layout in HBM (one mesh, `frames` conductivity frames per call):
+//   cols      [W][npad]            int32  slot-major ELL columns, W = density
+//   S, R      [F][W][npad]         float  stiffness / mass slot values of each frame
+//   S64, R64  [F][W][npad]         double same in FP64 (refinement residual only)
+//   X         [F][Ca][npad][KP]    float  fields: node-major, the KP right-hand
+//                                         sides of a node are contiguous, so one
+//                                         ELL gather moves KP*4 contiguous bytes
+//   J         [F][rowsJ][Epad]     float  Jacobian, element index contiguous
+//   Jhi, Jlo  [F][rowsJ][Epad]     bf16   split of J for the tensor-core Gram
+// A "group" g = f*Ca + ci is one (frame, active harmonic) pair; all KP
+// right-hand sides of a group share one matrix S + alpha_c R.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "mpf_internal.h"
+
+namespace mpf {
+
+// Per-launch view of a batched CG problem.
+struct CgProblem {
+    int n, npad, W, KP, G, Ca, nblk;  // nblk = npad / kRowTile
+    const int32_t* cols;
+    const int32_t* diagSlot;
+    const float* S;      // [F][W][npad]
+    const float* R;
+    const float* alpha;  // [Ca] per active harmonic
+    // vectors [G][npad][KP]
+    float *x, *r, *p, *q;
+    const float* b;      // right-hand side: [Ca][npad][KP] per harmonic, or [G][npad][KP]
+    int bPerGroup;
+    const int* dcFree;   // [Ca] 1 if the harmonic's matrix is singular (c == 0, open sources)
+    // reduction state
+    double* partA;       // [G][nblk][KP]
+    double* partB;
+    double* rz;          // [G][KP]
+    double* pq;
+    double* bz;
+    double* beta;
+    int* conv;           // [G][KP]
+    int* active;         // [G]
+    int* iters;          // [G]
+    unsigned* counter;   // [G] last-block-done counters (kept at zero between launches)
+    double tol2;
+};
+
+// cg_kernels.cu
+int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
+int cg_launch_iteration(const CgProblem& P, cudaStream_t s);
+int cg_launch_residual64(const CgProblem& P, const double* S64, const double* R64, const double* x64,
+                         const double* b64, double* partR, double* partB, double* rr, double* bb,
+                         cudaStream_t s);
+int cg_launch_accumulate64(const CgProblem& P, double* x64, cudaStream_t s);
+int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s);
+int cg_launch_mean_fix(const CgProblem& P, const double* shift /*[KP]*/, double* part, double* sums,
+                       cudaStream_t s);
+
+// fem_kernels.cu
+int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
+                        const float* Kf, const float* Mf, const double* Kd, const double* Md,
+                        const float* gamma, float ref, int logarithmic, float* S, float* R,
+                        double* S64, double* R64, cudaStream_t s);
+int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float* slotMajor,
+                          float* refLayout, cudaStream_t s);
+struct MeasPlan {
+    int nnz;                 // nonzeros of the unique excitation columns
+    const int32_t* nzNode;   // [nnz]
+    const int32_t* nzCol;    // [nnz]
+    const double* nzVal;     // [nnz]
+    const int32_t* nzPtr;    // [KP+1] CSR by column
+};
+int fem_launch_gram_meas(int G, int KP, int npad, const MeasPlan& mp, const float* X, double* Gm,
+                         cudaStream_t s);
+int fem_launch_voltages(int F, int Ca, int KP, int Mm, int Md, const double* Gm, const float* beta,
+                        const int32_t* measU, const float* measScale, const int32_t* driveU,
+                        const float* driveScale, float* V, cudaStream_t s);
+struct JacPlan {
+    int rowsJ, Epad, E, KP, Ca;
+    const int32_t* rowD;     // [rowsJ] unique column of the drive field, -1 for padding
+    const int32_t* rowM;     // [rowsJ] unique column of the measurement field
+    const float* rowScale;   // [rowsJ] drive scale * measurement scale
+    const float* beta2;      // [Ca] beta_c^2
+    const int32_t* elements; // [E][3]
+    const float* Kf;         // [E][9]
+    float ref, height;       // J *= -height (open sources)
+    int logarithmic;
+};
+int fem_launch_jacobian(int F, const JacPlan& jp, int MP, int npad, const float* X, const float* gamma,
+                        float* J, __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s);
+int fem_launch_transpose_jacobian(int F, int rowsJ, int Epad, int E, const float* J, float* Jref,
+                                  cudaStream_t s);
+int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int npad, int KP,
+                             int dataRows, int cols, int n, const int32_t* colU, const float* colScale,
+                             const float* betaC, const float* X, float* out, cudaStream_t s);
+int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, const float* V,
+                        double* y, double* res, cudaStream_t s);
+int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, const double* w,
+                            float* gamma, cudaStream_t s);
+
+// dense_kernels.cu
+int dense_gram_split_bf16(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo,
+                          int ld, float* C, float* work, size_t workFloats, cudaStream_t s);
+size_t dense_gram_work_floats(int batch, int rows, int cols);
+int dense_split_bf16(int batch, int rows, int cols, const float* A, int lda, __nv_bfloat16* hi,
+                     __nv_bfloat16* lo, cudaStream_t s);
+int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo,
+                         int ld, double shift, double* A64, float* work, size_t workFloats, cudaStream_t s);
+int dense_gram_check_abort(bool* aborted);
+int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s);
+int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s);
+int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s);
+
+}  // namespace mpf

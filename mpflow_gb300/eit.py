@@ -1,0 +1,272 @@
+"""Host-side mirror of mpFlow's EIT interface over the C ABI.
+
+Class and method names follow the reference (pgebhardt/mpflow):
+
+* :class:`IrregularMesh`  -- numeric::IrregularMesh (include/mpflow/numeric/irregular_mesh.h:27-61)
+* :class:`Ports`          -- FEM::Ports (include/mpflow/fem/ports.h:26-46)
+* :class:`Sources`        -- FEM::Sources (include/mpflow/fem/sources.h:31-113)
+* :class:`EIT`            -- models::EIT (include/mpflow/models/eit.h:31-81)
+
+All numerics run in libmpflow_gb300.so on the GPU; this module only shapes
+arguments.  Device buffers are torch CUDA tensors (used as plain device
+memory); the stream is torch's current stream.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import check, lib, ptr
+
+OPEN, FIXED = 0, 1
+
+
+def data_rows(n: int) -> int:
+    """Padded row count of a reference dense matrix (src/numeric/matrix.cpp:49-55)."""
+    return int(lib().mpf_data_rows(int(n)))
+
+
+class IrregularMesh:
+    """Triangle mesh with edge table and boundary (numeric::IrregularMesh)."""
+
+    def __init__(self, nodes: np.ndarray, elements: np.ndarray):
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        self.elements = np.ascontiguousarray(elements, dtype=np.int32)
+        if self.nodes.ndim != 2 or self.nodes.shape[1] != 2:
+            raise ValueError("mpFlow::numeric::IrregularMesh::IrregularMesh: nodes.cols() != 2")
+        if self.elements.shape[0] == 0:
+            raise ValueError("mpFlow::numeric::IrregularMesh::IrregularMesh: elements.rows() == 0")
+        N, E = self.nodes.shape[0], self.elements.shape[0]
+        edges = np.zeros((3 * E, 2), np.int32)
+        element_edges = np.zeros((E, 3), np.int32)
+        boundary = np.zeros(3 * E, np.int32)
+        ne, nb = ctypes.c_int32(0), ctypes.c_int32(0)
+        check(lib().mpf_mesh_edges(N, E, ptr(self.nodes), ptr(self.elements), ptr(edges),
+                                   ptr(element_edges), ptr(boundary), ctypes.byref(ne),
+                                   ctypes.byref(nb)))
+        self.edges = edges[:ne.value].copy()
+        self.elementEdges = element_edges
+        self.boundary = boundary[:nb.value].copy()
+
+    @staticmethod
+    def ring(rings: int, radius: float = 1.0) -> "IrregularMesh":
+        """Disk of `rings` concentric rings, ring i carrying 6i nodes."""
+        n, e = ctypes.c_int32(0), ctypes.c_int32(0)
+        check(lib().mpf_ring_mesh_counts(int(rings), ctypes.byref(n), ctypes.byref(e)))
+        nodes = np.zeros((n.value, 2))
+        elements = np.zeros((e.value, 3), np.int32)
+        check(lib().mpf_ring_mesh(int(rings), float(radius), ptr(nodes), ptr(elements)))
+        return IrregularMesh(nodes, elements)
+
+    def elementNodes(self, element: int) -> np.ndarray:
+        return self.nodes[self.elements[element]]
+
+    def edgeNodes(self, edge: int) -> np.ndarray:
+        return self.nodes[self.edges[edge]]
+
+
+class Ports:
+    """Electrode edge sets (FEM::Ports)."""
+
+    def __init__(self, edges: np.ndarray):
+        self.edges = np.ascontiguousarray(edges, dtype=np.int32)
+        if self.edges.shape[0] == 0:
+            raise ValueError("mpFlow::FEM::Ports::Ports: edges == 0")
+        self.count = self.edges.shape[0]
+
+    @staticmethod
+    def circularBoundary(count: int, width: float, mesh: IrregularMesh, offset: float = 0.0,
+                         clockwise: bool = False, cap: int = 512) -> "Ports":
+        out = np.full((count, cap), -1, np.int32)
+        mx = ctypes.c_int32(0)
+        check(lib().mpf_ports_circular(mesh.nodes.shape[0], ptr(mesh.nodes), mesh.elements.shape[0],
+                                       ptr(mesh.elements), ptr(mesh.edges), mesh.boundary.shape[0],
+                                       ptr(mesh.boundary), int(count), float(width), float(offset),
+                                       int(bool(clockwise)), ptr(out), cap, ctypes.byref(mx)))
+        return Ports(out[:, :max(mx.value, 1)].copy())
+
+
+def adjacent_pattern(count: int) -> np.ndarray:
+    """Adjacent (+1 on port j, -1 on port j+1) pattern, ports x count."""
+    p = np.zeros((count, count))
+    for j in range(count):
+        p[j, j] = 1.0
+        p[(j + 1) % count, j] = -1.0
+    return p
+
+
+class Sources:
+    """Excitation description (FEM::Sources): type, values and patterns."""
+
+    Open, Fixed = OPEN, FIXED
+
+    def __init__(self, type_: int, values, ports: Ports, drivePattern: np.ndarray,
+                 measurementPattern: np.ndarray):
+        if ports is None:
+            raise ValueError("mpFlow::FEM::Sources::Sources: ports == nullptr")
+        self.type = int(type_)
+        self.ports = ports
+        self.drivePattern = np.asfortranarray(drivePattern, dtype=np.float64)
+        self.measurementPattern = np.asfortranarray(measurementPattern, dtype=np.float64)
+        vals = np.atleast_1d(np.asarray(values, dtype=np.float64))
+        if vals.size == 1:
+            vals = np.full(self.drivePattern.shape[1], vals[0])
+        if vals.size != self.drivePattern.shape[1]:
+            raise ValueError("mpFlow::FEM::Sources::Sources: invalid size of values vector")
+        self.values = vals
+
+    @property
+    def pattern(self) -> np.ndarray:
+        """[values * drive | measurement] (src/fem/sources.cpp:58-71)."""
+        return np.concatenate([self.drivePattern * self.values[None, :], self.measurementPattern], axis=1)
+
+
+class SolveOptions:
+    def __init__(self, tol=1e-6, max_iter=0, refine_tol=0.0, max_refine=6, warm_start=False,
+                 check_every=16):
+        self.tol, self.max_iter, self.refine_tol = tol, max_iter, refine_tol
+        self.max_refine, self.warm_start, self.check_every = max_refine, warm_start, check_every
+
+    def c(self) -> _ffi.SolveOpts:
+        return _ffi.SolveOpts(float(self.tol), int(self.max_iter), float(self.refine_tol),
+                              int(self.max_refine), int(bool(self.warm_start)), int(self.check_every))
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class EIT:
+    """2.5D EIT forward model resident on one GPU (models::EIT).
+
+    ``solve`` takes a (frames x elements) float32 CUDA tensor of material
+    values and returns the (frames x meas x drive) electrode voltages."""
+
+    def __init__(self, mesh: IrregularMesh, sources: Sources, referenceValue: float = 1.0,
+                 components: int = 1, height: float = 1.0, portHeight: float = 1.0,
+                 logarithmic: bool = False, device: int = 0):
+        self.mesh, self.sources = mesh, sources
+        self.referenceValue = float(referenceValue)
+        self.components, self.height, self.portHeight = int(components), float(height), float(portHeight)
+        self.logarithmic = bool(logarithmic)
+        self.device = int(device)
+        self._keep = [mesh.nodes, mesh.elements, mesh.edges, sources.ports.edges,
+                      sources.drivePattern, sources.measurementPattern, sources.values]
+        d = _ffi.EitDesc(
+            mesh.nodes.shape[0], mesh.elements.shape[0], ptr(mesh.nodes).value, ptr(mesh.elements).value,
+            ptr(mesh.edges).value, mesh.edges.shape[0], sources.ports.count,
+            ptr(sources.ports.edges).value, sources.ports.edges.shape[1],
+            sources.drivePattern.shape[1], sources.measurementPattern.shape[1],
+            ptr(sources.drivePattern).value, ptr(sources.measurementPattern).value,
+            ptr(sources.values).value, sources.type, self.referenceValue, int(self.logarithmic),
+            self.components, self.height, self.portHeight, self.device)
+        h = ctypes.c_void_p()
+        check(lib().mpf_eit_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        info = _ffi.EitInfo()
+        check(lib().mpf_eit_get_info(h, ctypes.byref(info)))
+        self.info = {name: getattr(info, name) for name, _ in _ffi.EitInfo._fields_}
+        self.last_stats = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().mpf_eit_destroy(h)
+            self._h = None
+
+    # -- shapes
+    @property
+    def jacobian_rows(self) -> int:
+        return self.info["jacobian_rows"]
+
+    def _frames(self, gamma):
+        import torch
+        if not (isinstance(gamma, torch.Tensor) and gamma.is_cuda and gamma.dtype == torch.float32):
+            raise TypeError("materialDistribution must be a float32 CUDA tensor")
+        g = gamma.reshape(-1, self.mesh.elements.shape[0]).contiguous()
+        return g, g.shape[0]
+
+    def assemble(self, gamma):
+        """Stiffness and mass slot values in the reference ELL layout."""
+        import torch
+        g, F = self._frames(gamma)
+        dr = self.info["data_rows"]
+        S = torch.empty((F, dr, 32), dtype=torch.float32, device=g.device)
+        R = torch.empty_like(S)
+        check(lib().mpf_eit_assemble(self._h, F, ptr(g), ptr(S), ptr(R), _stream()))
+        return S, R
+
+    def solve(self, materialDistribution, options: SolveOptions | None = None, jacobian: bool = False):
+        """Forward solve; returns V (frames x Mm x Md) and, if asked, J
+        (frames x rowsJ x E, the reference's column-major jacobian as its
+        transpose view)."""
+        import torch
+        g, F = self._frames(materialDistribution)
+        Mm, Md = self.info["meas_count"], self.info["drive_count"]
+        V = torch.empty((F, Md, Mm), dtype=torch.float32, device=g.device)
+        J = None
+        if jacobian:
+            J = torch.empty((F, self.mesh.elements.shape[0], self.jacobian_rows), dtype=torch.float32,
+                            device=g.device)
+        st = _ffi.SolveStats()
+        o = (options or SolveOptions()).c()
+        check(lib().mpf_eit_forward(self._h, F, ptr(g), ptr(V), ptr(J), ctypes.byref(o), ctypes.byref(st),
+                                    _stream()))
+        self.last_stats = st
+        Vm = V.transpose(1, 2)  # (F, Mm, Md): column-major Mm x Md per frame
+        if jacobian:
+            return Vm, J.transpose(1, 2)
+        return Vm
+
+    def fields(self, frames: int):
+        """Potentials of the last solve: (frames, components, Md+Mm, data_rows)."""
+        import torch
+        dr = self.info["data_rows"]
+        cols = self.info["drive_count"] + self.info["meas_count"]
+        out = torch.empty((frames, self.components, cols, dr), dtype=torch.float32, device="cuda")
+        check(lib().mpf_eit_fields(self._h, frames, ptr(out), _stream()))
+        return out
+
+    def gn_step(self, gamma, v_meas, lam: float, options: SolveOptions | None = None):
+        """One regularised Gauss-Newton step in place on gamma; returns the
+        relative data residual of each frame before the step."""
+        import torch
+        g, F = self._frames(gamma)
+        if g.data_ptr() != gamma.data_ptr():
+            raise ValueError("gamma must be contiguous")
+        vm = v_meas.reshape(F, -1).contiguous()
+        res = np.zeros(F)
+        st = _ffi.SolveStats()
+        o = (options or SolveOptions()).c()
+        check(lib().mpf_gn_step(self._h, F, ptr(g), ptr(vm), float(lam), ctypes.byref(o), ptr(res),
+                                ctypes.byref(st), _stream()))
+        self.last_stats = st
+        return res
+
+
+def gram_split_bf16(A):
+    """C = A A^T (rows x rows) for a batch of row-major float32 CUDA matrices."""
+    import torch
+    if A.dim() == 2:
+        A = A[None]
+    B, rows, cols = A.shape
+    A = A.contiguous()
+    C = torch.empty((B, rows, rows), dtype=torch.float32, device=A.device)
+    check(lib().mpf_gram_split_bf16(B, rows, cols, ptr(A), cols, ptr(C), _stream()))
+    return C
+
+
+def cholesky_solve_f64(A, Bm, shift: float = 0.0):
+    """Solve (A + shift I) X = B for batches of float64 CUDA matrices (A overwritten)."""
+    import torch
+    if A.dim() == 2:
+        A, Bm = A[None], Bm[None]
+    batch, n, _ = A.shape
+    nrhs = Bm.shape[1] if Bm.dim() == 3 else 1
+    info = torch.zeros(batch, dtype=torch.int32, device=A.device)
+    check(lib().mpf_cholesky_solve_f64(batch, n, ptr(A), float(shift), ptr(Bm), nrhs, ptr(info), _stream()))
+    return info

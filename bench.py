@@ -1,0 +1,401 @@
+#!/usr/bin/env python3
+"""EIT reconstruction benchmark on GB300 (and the CPU reference arm).
+
+Workload (one "step"): reconstruct a batch of conductivity frames on the
+20k-node disk (80 rings: 19441 nodes, 38400 triangles), 32 electrodes with
+adjacent drive / adjacent measurement (1024 voltages per frame), 2.5D model
+with 8 axial harmonics (height 4, k_j = j*pi/2), logarithmic (dB)
+conductivity, by batched regularised Gauss-Newton until every frame's relative
+data residual ||V_meas - V(sigma)|| / ||V_meas|| is at most 1e-3.  Synthetic,
+seeded data: 1-3 circular inclusions (radius U(0.05, 0.3), contrast
+log-uniform in [0.1, 10]) on a 1 S/m background; V_meas from the forward
+model with FP64 refinement to 1e-9 (noise-free).  The metric is frames/s
+(frames that reach the target per second); the line also carries the CG SpMM
+bandwidth, the roofline of the dominant kernel and the CPU baseline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "EIT frames/s to 1e-3 rel residual: learned+batched vs plain GN; SpMV GB/s"
+UNIT = "frames/s"
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--frames", type=int, default=32, help="frames per step per GPU")
+    p.add_argument("--rings", type=int, default=80)
+    p.add_argument("--electrodes", type=int, default=32)
+    p.add_argument("--components", type=int, default=8)
+    p.add_argument("--height", type=float, default=4.0)
+    p.add_argument("--target", type=float, default=1e-3)
+    p.add_argument("--lam-rel", type=float, default=2e-2,
+                   help="Tikhonov lambda relative to the RMS row norm of J at the reference")
+    p.add_argument("--max-gn", type=int, default=10)
+    p.add_argument("--tol", type=float, default=1e-5, help="CG relative tolerance of the GN forward solves")
+    p.add_argument("--cpu-threads", type=int, default=0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def synthetic_frames(centroids: np.ndarray, count: int, seed: int) -> np.ndarray:
+    """Log-conductivity frames in dB (v = 10 log10(sigma / 1 S/m))."""
+    rng = np.random.default_rng(seed)
+    v = np.zeros((count, centroids.shape[0]), np.float32)
+    for f in range(count):
+        for _ in range(int(rng.integers(1, 4))):
+            r = rng.uniform(0.05, 0.3)
+            rc = rng.uniform(0.0, 0.95 - r)
+            th = rng.uniform(0.0, 2 * np.pi)
+            c = np.array([rc * np.cos(th), rc * np.sin(th)])
+            contrast = np.exp(rng.uniform(np.log(0.1), np.log(10.0)))
+            v[f, np.linalg.norm(centroids - c, axis=1) < r] = 10.0 * np.log10(contrast)
+    return v
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per SpMM launch per (frame, harmonic) group from the committed
+    ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "cg_spmm_dot_R80.md")
+    try:
+        with open(path) as fh:
+            for line in fh:
+                if line.startswith("dram_bytes_per_group_launch:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+def build_problem(a):
+    import mpflow_gb300 as mp
+    mesh = mp.IrregularMesh.ring(a.rings)
+    ports = mp.Ports.circularBoundary(a.electrodes, 0.1, mesh)
+    pat = mp.adjacent_pattern(a.electrodes)
+    src = mp.Sources(mp.OPEN, 1e-3, ports, pat, pat)
+    return mesh, ports, pat, src
+
+
+def cpu_baseline(a, mesh, ports, pat, frames_v, gn_iters_mean):
+    """One Gauss-Newton iteration of one frame with the FP64 oracle (the
+    reference's routines restated in C) on all host cores; frames/s =
+    1 / (seconds per GN iteration * (mean GN updates + 1 forward check))."""
+    import oracle
+    if a.cpu_threads > 0:
+        oracle.set_threads(a.cpu_threads)
+    s = oracle.Setup(mesh.nodes, mesh.elements, mesh.edges, mesh.boundary, ports.edges, pat, pat,
+                     np.full(a.electrodes, 1e-3), ref=1.0, logarithmic=True, components=a.components,
+                     height=a.height)
+    v = frames_v[0].astype(np.float64)
+    t0 = time.perf_counter()
+    Vm, _, _ = oracle.eit_forward(s, v, tol=a.tol, want_jacobian=False, exact=True)
+    t1 = time.perf_counter()
+    v0 = np.zeros_like(v)
+    V0, J0, _ = oracle.eit_forward(s, v0, tol=a.tol, exact=True)
+    t2 = time.perf_counter()
+    y = oracle.flatten_measurement(Vm, s) - oracle.flatten_measurement(V0, s)
+    lam = a.lam_rel * np.linalg.norm(J0) / np.sqrt(J0.shape[0])
+    oracle.inverse_dual(J0, y, 1.0, lam)
+    t3 = time.perf_counter()
+    forward_s = t1 - t0
+    gn_iter_s = t3 - t1
+    per_frame = gn_iter_s * gn_iters_mean + forward_s
+    return {
+        "value": 1.0 / per_frame,
+        "unit": UNIT,
+        "cores": oracle.num_threads(),
+        "kind": "port",
+        "sample": (f"1 frame: FP64 forward ({forward_s:.2f} s) + 1 GN iteration = forward+Jacobian+dual "
+                   f"Cholesky step ({gn_iter_s:.2f} s), scaled to {gn_iters_mean:.2f} GN updates + 1 forward "
+                   "check per frame (GPU-measured mean)"),
+    }
+
+
+def run_reference(a):
+    """--impl reference: the reference's numerics (FP64 oracle port, all host
+    threads) on the same workload, one bounded frame per step."""
+    rank, world, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
+    mesh, ports, pat, src = build_problem(a)
+    cent = mesh.nodes[mesh.elements].mean(axis=1)
+    import oracle
+    if a.cpu_threads > 0:
+        oracle.set_threads(a.cpu_threads)
+    s = oracle.Setup(mesh.nodes, mesh.elements, mesh.edges, mesh.boundary, ports.edges, pat, pat,
+                     np.full(a.electrodes, 1e-3), ref=1.0, logarithmic=True, components=a.components,
+                     height=a.height)
+    times, iters = [], []
+    for step in range(a.warmup + a.steps):
+        v_true = synthetic_frames(cent, 1, seed=10_000 + step)[0].astype(np.float64)
+        Vm, _, _ = oracle.eit_forward(s, v_true, tol=1e-9, want_jacobian=False, exact=True)
+        vm = oracle.flatten_measurement(Vm, s)
+        t0 = time.perf_counter()
+        v = np.zeros_like(v_true)
+        n_up = 0
+        lam = None
+        for it in range(a.max_gn + 1):
+            V, J, _ = oracle.eit_forward(s, v, tol=a.tol, exact=True)
+            y = vm - oracle.flatten_measurement(V, s)
+            if np.linalg.norm(y) / np.linalg.norm(vm) <= a.target or it == a.max_gn:
+                break
+            if lam is None:
+                lam = a.lam_rel * np.linalg.norm(J) / np.sqrt(J.shape[0])
+            v = v + oracle.inverse_dual(J, y, 1.0, lam)
+            n_up += 1
+        dt = time.perf_counter() - t0
+        if step >= a.warmup:
+            times.append(dt)
+            iters.append(n_up)
+    value = len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded inclusion frames, noise-free)",
+        "config": workload_config(a, frames=1),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"1 frame per step, full GN to target ({np.mean(iters):.2f} updates mean)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(a, frames):
+    return {"workload": (f"EIT 2.5D GN reconstruction: ring mesh {a.rings} rings (19441 nodes, 38400 "
+                         f"triangles at 80), {a.electrodes} electrodes adjacent/adjacent, "
+                         f"{a.components} harmonics (height {a.height}), log-conductivity"),
+            "frames_per_step_per_gpu": frames, "target_rel_residual": a.target,
+            "lambda_rel": a.lam_rel, "cg_tol": a.tol, "jacobian": "exact 2.5D derivative",
+            "l2": "CG working set > L2 (129 MB) at >= 8 frames per step"}
+
+
+def run_gb300(a):
+    import torch
+    import torch.distributed as dist
+    import mpflow_gb300 as mp
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group(backend="nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    mesh, ports, pat, src = build_problem(a)
+    E = mesh.elements.shape[0]
+    cent = mesh.nodes[mesh.elements].mean(axis=1)
+    model = mp.EIT(mesh, src, 1.0, components=a.components, height=a.height, logarithmic=True,
+                   device=local, exact_jacobian=True)
+    F = a.frames
+    nsteps = a.warmup + a.steps
+    # synthetic truth and measurements per step (untimed)
+    truth = [synthetic_frames(cent, F, seed=1000 * (rank + 1) + s) for s in range(nsteps)]
+    vmeas = []
+    ref_opts = mp.SolveOptions(tol=1e-5, refine_tol=1e-9, max_iter=6000)
+    for s in range(nsteps):
+        V = model.solve(torch.tensor(truth[s], device=dev), ref_opts)
+        vmeas.append(V.contiguous())
+    # regularisation from the Jacobian at the reference conductivity
+    _, J0 = model.solve(torch.zeros((1, E), device=dev), mp.SolveOptions(tol=a.tol), jacobian=True)
+    lam = a.lam_rel * float(J0.norm() / np.sqrt(J0.shape[1]))
+    del J0
+    opts = mp.SolveOptions(tol=a.tol, max_iter=6000)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timing: V_meas already in HBM
+    stream = torch.cuda.current_stream()
+    frames_done, gn_updates, times_ms = 0, [], []
+    launches0 = None
+    with ClockSampler(local) as clocks:
+        for s in range(nsteps):
+            g = torch.zeros((F, E), device=dev)
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            iters, res, st = model.gn_solve(g, vmeas[s], lam, target=a.target, max_iters=a.max_gn, options=opts)
+            e1.record(stream)
+            barrier()
+            if s >= a.warmup:
+                times_ms.append(e0.elapsed_time(e1))
+                frames_done += int(st.frames_converged)
+                gn_updates.extend(iters.tolist())
+    step_ms = float(np.mean(times_ms))
+    total_ms = float(np.sum(times_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        n = torch.tensor([frames_done], device=dev, dtype=torch.float64)
+        dist.all_reduce(n)
+        frames_all = float(n.item())
+    else:
+        frames_all = float(frames_done)
+    value = frames_all / (total_ms / 1e3)
+
+    # ---- end to end through the public API: host V_meas in, host sigma out
+    host_v = [v.cpu().pin_memory() for v in vmeas]
+    host_out = torch.empty((F, E), dtype=torch.float32).pin_memory()
+    e2e_ms, e2e_frames = [], 0
+    for s in range(nsteps):
+        barrier()
+        t0 = time.perf_counter()
+        vm = host_v[s].to(dev, non_blocking=True)
+        g = torch.zeros((F, E), device=dev)
+        _, _, st = model.gn_solve(g, vm, lam, target=a.target, max_iters=a.max_gn, options=opts)
+        host_out.copy_(g, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) * 1e3
+        if s >= a.warmup:
+            e2e_ms.append(dt)
+            e2e_frames += int(st.frames_converged)
+    e2e_value = e2e_frames * world / (sum(e2e_ms) / 1e3)
+
+    # ---- roofline of the CG kernels (CUDA events on the launching stream)
+    ms, by = model.profile_cg(torch.tensor(truth[0], device=dev), reps=10)
+    gbs = by / ms / 1e6
+    dom = int(np.argmax(ms))
+    names = ["k_spmm_dot", "k_update", "k_direction"]
+    peak, peak_kind = measured_peaks()
+    groups = F * model.info["active_components"]
+    traffic_per_group = profiled_traffic()
+    roofline = {"kernel": names[dom], "bound": "hbm", "achieved": float(gbs[dom]), "peak": peak,
+                "unit": "GB/s", "frac": float(gbs[dom] / peak), "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": (traffic_per_group * groups if (traffic_per_group and dom == 0) else None),
+                "algorithmic_bytes": float(by[dom]), "launch_ms": float(ms[dom])}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not a.no_cpu_baseline:
+        cpu = cpu_baseline(a, mesh, ports, pat, truth[0], float(np.mean(gn_updates)))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 inner products / refinement / Cholesky, split-BF16 J J^T)",
+        "data": "synthetic (seeded inclusion frames, noise-free; V_meas from the FP64-refined forward model)",
+        "config": workload_config(a, F),
+        "method": "plain batched GN (homogeneous start)",
+        "gn_updates_mean": float(np.mean(gn_updates)),
+        "frames_converged_fraction": frames_all / (F * world * a.steps),
+        "spmv_gbs": float(gbs[0]),
+        "cg_kernel_ms": {k: float(v) for k, v in zip(names, ms)},
+        "cg_kernel_gbs": {k: float(v) for k, v in zip(names, gbs)},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(vmeas[0].numel() * 4), "d2h_bytes_per_step": int(F * E * 4)},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse_args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -44,6 +44,10 @@ enum mpf_source_type { MPF_SOURCE_OPEN = 0, MPF_SOURCE_FIXED = 1 };
 const char* mpf_last_error(void);
 /* Library version string (src/version.cpp:23-25 analogue). */
 const char* mpf_version(void);
+/* Number of CUDA kernels this library has launched in the process so far
+ * (kernels inside replayed CUDA graphs included).  No reference counterpart
+ * (measurement support). */
+long long mpf_kernel_launches(void);
 
 /* ======================================================================== */
 /* Host-side mesh and FEM setup (no GPU needed)                             */
@@ -131,6 +135,11 @@ typedef struct mpf_eit_desc {
     double height;
     double port_height;
     int32_t device;               /* CUDA device ordinal */
+    /* 0: the reference's 2.5D Jacobian (stiffness term only, harmonic weight
+     *    height*beta_c^2; src/fem/equation.cpp:240-247, src/models/eit.cpp:180-205);
+     * 1: exact derivative of the 2.5D voltages (adds alpha_c * mass, weight beta_c).
+     * Identical for a single harmonic. */
+    int32_t jacobian_mode;
 } mpf_eit_desc;
 
 /* Sizes a caller needs to shape its buffers. */
@@ -210,6 +219,38 @@ int mpf_eit_fields(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t 
 int mpf_gn_step(mpf_eit_t model, int32_t frames, float* gamma, const float* v_meas, double lambda,
                 const mpf_solve_opts* opts, double* residual, mpf_solve_stats* stats,
                 mpf_stream_t stream);
+
+typedef struct mpf_gn_stats {
+    int32_t gn_iterations;    /* Gauss-Newton updates applied (slowest frame) */
+    int32_t cg_iterations;    /* CG iterations summed over the forward solves (slowest group) */
+    int32_t frames_converged; /* frames whose residual reached the target */
+    double seconds;           /* host wall time of the call (synchronised) */
+} mpf_gn_stats;
+
+/* Batched Gauss-Newton reconstruction: repeats mpf_gn_step on every frame
+ * whose relative data residual ||v_meas - V(gamma)|| / ||v_meas|| is above
+ * `target`, for at most max_gn_iters updates; frames that reach the target
+ * are frozen.  The reference leaves this outer loop to its caller
+ * (src/solver/solver.cpp:196-225 is one step).  Forward solves after the
+ * first start from the previous fields.
+ *   iterations: host, frames ints (updates per frame) or NULL
+ *   residual:   host, frames doubles (final residual per frame) or NULL */
+int mpf_gn_solve(mpf_eit_t model, int32_t frames, float* gamma, const float* v_meas, double lambda,
+                 double target, int32_t max_gn_iters, const mpf_solve_opts* opts, int32_t* iterations,
+                 double* residual, mpf_gn_stats* stats, mpf_stream_t stream);
+
+/* Kernel timing hook: runs `reps` CG iterations on the systems of `gamma`
+ * and reports, for the SpMM, update and direction kernels, the mean CUDA-
+ * event time of one launch (ms[3]) and its algorithmic bytes (bytes[3]).
+ * No reference counterpart (measurement support). */
+int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int32_t reps, double* ms,
+                       double* bytes, mpf_stream_t stream);
+
+/* CG iterations of every (frame, harmonic) group in the last inner solve of
+ * the last forward call, group g = frame * active_components + harmonic.
+ * Writes min(count, cap) entries; *count receives the group count.  The
+ * reference returns one summed count (src/models/eit.cpp:207-210). */
+int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, int32_t* count);
 
 /* ======================================================================== */
 /* Dense building blocks                                                     */

@@ -38,7 +38,7 @@ class EitDesc(ctypes.Structure):
         ("source_values", ctypes.c_void_p), ("source_type", ctypes.c_int32),
         ("reference_value", ctypes.c_double), ("logarithmic", ctypes.c_int32),
         ("components", ctypes.c_int32), ("height", ctypes.c_double), ("port_height", ctypes.c_double),
-        ("device", ctypes.c_int32),
+        ("device", ctypes.c_int32), ("jacobian_mode", ctypes.c_int32),
     ]
 
 
@@ -61,6 +61,11 @@ class SolveStats(ctypes.Structure):
                 ("seconds", ctypes.c_double)]
 
 
+class GnStats(ctypes.Structure):
+    _fields_ = [("gn_iterations", ctypes.c_int32), ("cg_iterations", ctypes.c_int32),
+                ("frames_converged", ctypes.c_int32), ("seconds", ctypes.c_double)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int32
 _D = ctypes.c_double
@@ -69,6 +74,7 @@ _D = ctypes.c_double
 SIGNATURES = {
     "mpf_last_error": (ctypes.c_char_p, []),
     "mpf_version": (ctypes.c_char_p, []),
+    "mpf_kernel_launches": (ctypes.c_longlong, []),
     "mpf_data_rows": (ctypes.c_uint32, [ctypes.c_uint32]),
     "mpf_ring_mesh_counts": (_I, [_I, _P, _P]),
     "mpf_ring_mesh": (_I, [_I, _D, _P, _P]),
@@ -84,6 +90,10 @@ SIGNATURES = {
     "mpf_eit_forward": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P]),
     "mpf_eit_fields": (_I, [_P, _I, _P, _P]),
     "mpf_gn_step": (_I, [_P, _I, _P, _P, _D, ctypes.POINTER(SolveOpts), _P, ctypes.POINTER(SolveStats), _P]),
+    "mpf_gn_solve": (_I, [_P, _I, _P, _P, _D, _D, _I, ctypes.POINTER(SolveOpts), _P, _P,
+                          ctypes.POINTER(GnStats), _P]),
+    "mpf_eit_profile_cg": (_I, [_P, _I, _P, _I, _P, _P, _P]),
+    "mpf_eit_group_iterations": (_I, [_P, _P, _I, _P]),
     "mpf_gram_split_bf16": (_I, [_I, _I, _I, _P, _I, _P, _P]),
     "mpf_cholesky_solve_f64": (_I, [_I, _I, _P, _D, _P, _I, _P, _P]),
 }

@@ -3,6 +3,7 @@
 // thread-local message for mpf_last_error().
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <exception>
 #include <new>
 
@@ -11,6 +12,10 @@
 namespace mpf {
 
 static thread_local std::string g_error;
+static std::atomic<long long> g_launches{0};
+
+void add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches() { return g_launches.load(std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
     char buf[1024];
@@ -42,6 +47,10 @@ int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, 
             double* residual, mpf_solve_stats* stats, cudaStream_t s);
 void eit_info(const mpf_eit* m, mpf_eit_info* i);
 void eit_destroy(mpf_eit* m);
+int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, double target, int maxIters,
+             const mpf_solve_opts* o, int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s);
+int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
+int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 
 }  // namespace mpf
 
@@ -62,6 +71,8 @@ extern "C" {
 const char* mpf_last_error(void) { return mpf::last_error(); }
 
 const char* mpf_version(void) { return "mpflow_gb300 0.1.0 (sm_103a)"; }
+
+long long mpf_kernel_launches(void) { return mpf::launches(); }
 
 uint32_t mpf_data_rows(uint32_t rows) { return mpf::data_rows(rows); }
 
@@ -188,6 +199,32 @@ int mpf_gn_step(mpf_eit_t model, int32_t frames, float* gamma, const float* v_me
         MPF_CHECK(model, MPF_EINVAL, "mpf_gn_step: model == nullptr");
         MPF_CHECK(lambda >= 0.0, MPF_EINVAL, "mpf_gn_step: lambda < 0");
         return mpf::gn_step(model, frames, gamma, v_meas, lambda, opts, residual, stats, (cudaStream_t)stream);
+    })
+}
+
+int mpf_gn_solve(mpf_eit_t model, int32_t frames, float* gamma, const float* v_meas, double lambda, double target,
+                 int32_t max_gn_iters, const mpf_solve_opts* opts, int32_t* iterations, double* residual,
+                 mpf_gn_stats* stats, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_gn_solve: model == nullptr");
+        MPF_CHECK(lambda >= 0.0 && target >= 0.0, MPF_EINVAL, "mpf_gn_solve: lambda and target must be >= 0");
+        return mpf::gn_solve(model, frames, gamma, v_meas, lambda, target, max_gn_iters, opts, iterations, residual,
+                             stats, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int32_t reps, double* ms, double* bytes,
+                       mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_profile_cg: model == nullptr");
+        return mpf::profile_cg(model, frames, gamma, reps, ms, bytes, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, int32_t* count) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_group_iterations: model == nullptr");
+        return mpf::group_iterations(model, iterations, cap, count);
     })
 }
 

@@ -123,12 +123,22 @@ __device__ __forceinline__ double sum_partials(const double* part, int g, int nb
 }
 
 // ---------------------------------------------------------------------------
-// r = b - A x (or r = b), z = D^-1 r, p = z, rz = r.z, bz = b.D^-1 b
+// Neumann (dcFree) harmonics: the reference regularises the singular
+// stiffness matrix as (A + 1 1^T) x = b (src/numeric/conjugate_gradient.cpp:
+// 85-89,115-119).  That rank-one term puts an eigenvalue n on the constant
+// vector, which in FP32 amplifies rounding in that direction ~n-fold, so the
+// iteration here uses (A + c' 1 1^T) with c' = mean(diag A) / n (eigenvalue
+// ~1 after Jacobi scaling); both systems have the same zero-mean solution
+// and k_dc_shift adds the exact constant difference afterwards.  The
+// rank-one term needs sum(p), which k_direction reduces for the next SpMM.
+
+// r = b - A x - sum(x) (or r = b), z = D^-1 r, p = z, rz = r.z, bz = b.D^-1 b, sum(p)
 template <int KP>
 __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
     using Sh = Shape<KP>;
     const int g = blockIdx.y;
     const int f = g / P.Ca, ci = g % P.Ca;
+    const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
     const float* S = P.S + (size_t)f * P.W * P.npad;
     const float* R = P.R + (size_t)f * P.W * P.npad;
@@ -136,10 +146,16 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
     const float* b = P.b + (P.bPerGroup ? vb : (size_t)ci * P.npad * KP);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
-    DotAcc acc[2][Sh::VEC];
+    float sx[Sh::VEC] = {};
+    if (dc && !zeroGuess && P.sumX0) {
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) sx[v] = (float)((double)P.dcScale * P.sumX0[(size_t)g * KP + j0 + v]);
+    }
+    DotAcc acc[3][Sh::VEC];
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
     for (int st = 0; st < Sh::STEPS; ++st) {
         const int row = rowBase + st * Sh::SUB + sub;
+        const bool real = row < P.n;
         float bv[Sh::VEC], rv[Sh::VEC];
         ldv<Sh::VEC>(b + (size_t)row * KP + j0, bv);
 #pragma unroll
@@ -156,7 +172,7 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
                 for (int v = 0; v < Sh::VEC; ++v) y[v] = fmaf(a, xv[v], y[v]);
             }
 #pragma unroll
-            for (int v = 0; v < Sh::VEC; ++v) rv[v] = bv[v] - y[v];
+            for (int v = 0; v < Sh::VEC; ++v) rv[v] = bv[v] - y[v] - (real ? sx[v] : 0.f);
         } else {
             float zv[Sh::VEC] = {};
             stv<Sh::VEC>(P.x + vb + (size_t)row * KP + j0, zv);
@@ -168,17 +184,19 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
             zv[v] = di * rv[v];
             acc[0][v].add(rv[v], zv[v]);
             acc[1][v].add(bv[v], di * bv[v]);
+            if (dc && real) acc[2][v].add(zv[v], 1.f);
         }
         stv<Sh::VEC>(P.r + vb + (size_t)row * KP + j0, rv);
         stv<Sh::VEC>(P.p + vb + (size_t)row * KP + j0, zv);
     }
-    double* const parts[2] = {P.partA, P.partB};
-    if (block_partials<KP, 2>(acc, parts, g, P.nblk, P.counter)) {
+    double* const parts[3] = {P.partA, P.partB, P.partC};
+    if (block_partials<KP, 3>(acc, parts, g, P.nblk, P.counter)) {
         int notConv = 0;
         if (threadIdx.x < KP) {
             const int j = threadIdx.x;
             double rz = sum_partials(P.partA, g, P.nblk, KP, j);
             double bz = sum_partials(P.partB, g, P.nblk, KP, j);
+            P.sumP[(size_t)g * KP + j] = dc ? sum_partials(P.partC, g, P.nblk, KP, j) : 0.0;
             P.rz[(size_t)g * KP + j] = rz;
             P.bz[(size_t)g * KP + j] = bz;
             P.beta[(size_t)g * KP + j] = 0.0;
@@ -195,13 +213,14 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
     }
 }
 
-// q = (S + alpha R) p, pq = p.q
+// q = (S + alpha R) p (+ sum(p) on Neumann harmonics), pq = p.q
 template <int KP>
 __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
     using Sh = Shape<KP>;
     const int g = blockIdx.y;
     if (!P.active[g]) return;
     const int f = g / P.Ca, ci = g % P.Ca;
+    const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
     const float* S = P.S + (size_t)f * P.W * P.npad;
     const float* R = P.R + (size_t)f * P.W * P.npad;
@@ -210,6 +229,11 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
     float* q = P.q + vb;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+    float sp[Sh::VEC] = {};
+    if (dc) {
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) sp[v] = (float)((double)P.dcScale * P.sumP[(size_t)g * KP + j0 + v]);
+    }
     DotAcc acc[1][Sh::VEC];
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
     for (int st = 0; st < Sh::STEPS; ++st) {
@@ -222,6 +246,10 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
             ldv<Sh::VEC>(p + (size_t)col * KP + j0, xv);
 #pragma unroll
             for (int v = 0; v < Sh::VEC; ++v) y[v] = fmaf(a, xv[v], y[v]);
+        }
+        if (row < P.n) {
+#pragma unroll
+            for (int v = 0; v < Sh::VEC; ++v) y[v] += sp[v];
         }
         stv<Sh::VEC>(q + (size_t)row * KP + j0, y);
         float pv[Sh::VEC];
@@ -301,13 +329,15 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
     }
 }
 
-// p = D^-1 r + beta p on the right-hand sides still iterating
+// p = D^-1 r + beta p on the right-hand sides still iterating; Neumann
+// harmonics also reduce sum(p) for the next SpMM.
 template <int KP>
 __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
     using Sh = Shape<KP>;
     const int g = blockIdx.y;
     if (!P.active[g]) return;
     const int f = g / P.Ca, ci = g % P.Ca;
+    const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
     const float* S = P.S + (size_t)f * P.W * P.npad;
     const float* R = P.R + (size_t)f * P.W * P.npad;
@@ -322,6 +352,7 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
         live[v] = !P.conv[s];
         be[v] = (float)P.beta[s];
     }
+    DotAcc acc[1][Sh::VEC];
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
     for (int st = 0; st < Sh::STEPS; ++st) {
         const int row = rowBase + st * Sh::SUB + sub;
@@ -331,22 +362,33 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
         ldv<Sh::VEC>(P.p + o, pv);
         const float di = diag_inv(S, R, P.diagSlot, P.npad, row, alpha);
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) pv[v] = live[v] ? fmaf(be[v], pv[v], di * rv[v]) : pv[v];
+        for (int v = 0; v < Sh::VEC; ++v) {
+            pv[v] = live[v] ? fmaf(be[v], pv[v], di * rv[v]) : pv[v];
+            if (dc && row < P.n) acc[0][v].add(pv[v], 1.f);
+        }
         stv<Sh::VEC>(P.p + o, pv);
+    }
+    if (!dc) return;
+    double* const parts[1] = {P.partA};
+    if (block_partials<KP, 1>(acc, parts, g, P.nblk, P.counter)) {
+        if (threadIdx.x < KP) P.sumP[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, P.nblk, KP, threadIdx.x);
+        if (threadIdx.x == 0) P.counter[g] = 0;
     }
 }
 
 // ---------------------------------------------------------------------------
-// FP64 refinement: r64 = b64 - (S64 + alpha R64) x64, written as the float
-// right-hand side of the next inner solve; rr = |r64|^2, bb = |b64|^2.
+// FP64 refinement: r64 = b64 - (S64 + alpha R64) x64 (- sum(x64) on Neumann
+// harmonics), written as the float right-hand side of the next inner solve;
+// rr = |r64|^2, bb = |b64|^2.
 template <int KP>
 __global__ void __launch_bounds__(kThreads) k_residual64(CgProblem P, const double* S64, const double* R64,
                                                          const double* x64, const double* b64,
-                                                         float* rOut, double* partR, double* partB,
-                                                         double* rr, double* bb) {
+                                                         const double* sumX64, float* rOut, double* partR,
+                                                         double* partB, double* rr, double* bb) {
     using Sh = Shape<KP>;
     const int g = blockIdx.y;
     const int f = g / P.Ca, ci = g % P.Ca;
+    const bool dc = P.dcFree[ci] != 0;
     const double alpha = (double)P.alpha[ci];
     const double* S = S64 + (size_t)f * P.W * P.npad;
     const double* R = R64 + (size_t)f * P.W * P.npad;
@@ -354,6 +396,11 @@ __global__ void __launch_bounds__(kThreads) k_residual64(CgProblem P, const doub
     b64 += (size_t)ci * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+    double sx[Sh::VEC] = {};
+    if (dc) {
+#pragma unroll
+        for (int v = 0; v < Sh::VEC; ++v) sx[v] = (double)P.dcScale * sumX64[(size_t)g * KP + j0 + v];
+    }
     double accR[Sh::VEC] = {}, accB[Sh::VEC] = {};
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
     for (int st = 0; st < Sh::STEPS; ++st) {
@@ -369,7 +416,7 @@ __global__ void __launch_bounds__(kThreads) k_residual64(CgProblem P, const doub
 #pragma unroll
         for (int v = 0; v < Sh::VEC; ++v) {
             const double bv = b64[(size_t)row * KP + j0 + v];
-            const double rv = bv - y[v];
+            const double rv = bv - y[v] - (row < P.n ? sx[v] : 0.0);
             ro[v] = (float)rv;
             accR[v] = fma(rv, rv, accR[v]);
             accB[v] = fma(bv, bv, accB[v]);
@@ -417,52 +464,38 @@ __global__ void k_to_float(size_t count, const double* x64, float* x) {
         x[i] = (float)x64[i];
 }
 
-// Neumann (dcFree) harmonics: the iteration runs on the singular stiffness
-// matrix with a zero-sum right-hand side; the reference's solution of
-// (A + 1 1^T) x = b is the zero-mean solution plus (1^T b / n^2) 1.
-__global__ void __launch_bounds__(kThreads) k_mean_sum(CgProblem P, double* part, double* sums) {
-    const int g = blockIdx.y;
-    if (!P.dcFree[g % P.Ca]) return;
-    const size_t vb = (size_t)g * P.npad * P.KP;
-    __shared__ double red[kThreads];
-    __shared__ bool amLast;
-    const int rows = kRowTile;
-    // thread t handles right-hand side j = t % KP over a strided set of rows
-    const int j = threadIdx.x % P.KP, lanes = kThreads / P.KP > 0 ? kThreads / P.KP : 1;
-    const int r0 = threadIdx.x / P.KP;
-    double s = 0.0;
-    if (threadIdx.x < lanes * P.KP)
-        for (int r = r0; r < rows; r += lanes) {
-            const int row = blockIdx.x * kRowTile + r;
-            if (row < P.n) s += (double)P.x[vb + (size_t)row * P.KP + j];
-        }
-    red[threadIdx.x] = threadIdx.x < lanes * P.KP ? s : 0.0;
-    __syncthreads();
-    if (threadIdx.x < P.KP) {
-        double t = 0.0;
-        for (int l = 0; l < lanes; ++l) t += red[l * P.KP + threadIdx.x];
-        part[((size_t)g * P.nblk + blockIdx.x) * P.KP + threadIdx.x] = t;
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) amLast = atomicAdd(&P.counter[g], 1u) == (unsigned)(P.nblk - 1);
-    __syncthreads();
-    if (amLast) {
-        __threadfence();
-        if (threadIdx.x < P.KP) sums[(size_t)g * P.KP + threadIdx.x] = sum_partials(part, g, P.nblk, P.KP, threadIdx.x);
-        if (threadIdx.x == 0) P.counter[g] = 0;
-    }
-}
-
-__global__ void k_mean_apply(CgProblem P, const double* shift, const double* sums) {
+// x += sign * shift[j] on the real rows of every Neumann group: converts
+// between the solution of (A + c' 1 1^T) x = b and the reference's
+// (A + 1 1^T) x = b, which differ only by (sum(b) / n^2)(1 - 1/c') 1.
+__global__ void k_dc_shift(CgProblem P, const double* shift, float sign) {
     const int g = blockIdx.y;
     if (!P.dcFree[g % P.Ca]) return;
     const size_t vb = (size_t)g * P.npad * P.KP;
     const size_t count = (size_t)P.n * P.KP;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
-        const int j = (int)(i % P.KP);
-        const double m = sums[(size_t)g * P.KP + j] / (double)P.n;
-        P.x[vb + i] = (float)((double)P.x[vb + i] - m + shift[j]);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        P.x[vb + i] += sign * (float)shift[i % P.KP];
+}
+
+// Column sums over the real rows of every Neumann group (0 elsewhere); one
+// block per group, fixed summation order.
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_colsum(int n, int npad, int KP, int Ca, const int* dcFree,
+                                                     const T* x, double* sums) {
+    const int g = blockIdx.x;
+    __shared__ double red[kThreads];
+    const int lanes = kThreads / KP;
+    const int j = threadIdx.x % KP, r0 = threadIdx.x / KP;
+    double s = 0.0;
+    if (dcFree[g % Ca]) {
+        const T* xg = x + (size_t)g * npad * KP;
+        for (int r = r0; r < n; r += lanes) s += (double)xg[(size_t)r * KP + j];
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < KP) {
+        double t = 0.0;
+        for (int l = 0; l < lanes; ++l) t += red[l * KP + threadIdx.x];
+        sums[(size_t)g * KP + threadIdx.x] = t;
     }
 }
 
@@ -481,7 +514,7 @@ template <int KP>
 struct InitL {
     static int run(const CgProblem& P, bool zeroGuess, cudaStream_t s) {
         k_init<KP><<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P, zeroGuess ? 1 : 0);
-        MPF_CUDA(cudaGetLastError());
+        MPF_LAUNCHED(1);
         return MPF_OK;
     }
 };
@@ -492,18 +525,30 @@ struct IterL {
         k_spmm_dot<KP><<<grid, kThreads, 0, s>>>(P);
         k_update<KP><<<grid, kThreads, 0, s>>>(P);
         k_direction<KP><<<grid, kThreads, 0, s>>>(P);
+        // recorded into a CUDA graph; its launches are counted per replay
         MPF_CUDA(cudaGetLastError());
+        return MPF_OK;
+    }
+};
+template <int KP>
+struct OneL {
+    static int run(const CgProblem& P, int which, cudaStream_t s) {
+        dim3 grid(P.nblk, P.G);
+        if (which == 0) k_spmm_dot<KP><<<grid, kThreads, 0, s>>>(P);
+        else if (which == 1) k_update<KP><<<grid, kThreads, 0, s>>>(P);
+        else k_direction<KP><<<grid, kThreads, 0, s>>>(P);
+        MPF_LAUNCHED(1);
         return MPF_OK;
     }
 };
 template <int KP>
 struct Res64L {
     static int run(const CgProblem& P, const double* S64, const double* R64, const double* x64,
-                   const double* b64, double* partR, double* partB, double* rr, double* bb,
-                   cudaStream_t s) {
-        k_residual64<KP><<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P, S64, R64, x64, b64, P.r, partR, partB,
-                                                                 rr, bb);
-        MPF_CUDA(cudaGetLastError());
+                   const double* b64, const double* sumX64, double* partR, double* partB, double* rr,
+                   double* bb, cudaStream_t s) {
+        k_residual64<KP><<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P, S64, R64, x64, b64, sumX64, P.r, partR,
+                                                                 partB, rr, bb);
+        MPF_LAUNCHED(1);
         return MPF_OK;
     }
 };
@@ -516,30 +561,40 @@ int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s) {
 
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s) { return dispatch_kp<IterL>(P.KP, P, s); }
 
+int cg_launch_kernel(const CgProblem& P, int which, cudaStream_t s) { return dispatch_kp<OneL>(P.KP, P, which, s); }
+
 int cg_launch_residual64(const CgProblem& P, const double* S64, const double* R64, const double* x64,
-                         const double* b64, double* partR, double* partB, double* rr, double* bb,
-                         cudaStream_t s) {
-    return dispatch_kp<Res64L>(P.KP, P, S64, R64, x64, b64, partR, partB, rr, bb, s);
+                         const double* b64, const double* sumX64, double* partR, double* partB, double* rr,
+                         double* bb, cudaStream_t s) {
+    return dispatch_kp<Res64L>(P.KP, P, S64, R64, x64, b64, sumX64, partR, partB, rr, bb, s);
 }
 
 int cg_launch_accumulate64(const CgProblem& P, double* x64, cudaStream_t s) {
     size_t count = (size_t)P.G * P.npad * P.KP;
     k_accumulate64<<<1216, 256, 0, s>>>(count, P.x, x64);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
 int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s) {
     size_t count = (size_t)P.G * P.npad * P.KP;
     k_to_float<<<1216, 256, 0, s>>>(count, x64, P.x);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
-int cg_launch_mean_fix(const CgProblem& P, const double* shift, double* part, double* sums, cudaStream_t s) {
-    k_mean_sum<<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P, part, sums);
-    k_mean_apply<<<dim3(64, P.G), 256, 0, s>>>(P, shift, sums);
-    MPF_CUDA(cudaGetLastError());
+int cg_launch_dc_shift(const CgProblem& P, const double* shift, float sign, cudaStream_t s) {
+    k_dc_shift<<<dim3(64, P.G), 256, 0, s>>>(P, shift, sign);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int cg_launch_colsum(const CgProblem& P, const float* x, const double* x64, double* sums, cudaStream_t s) {
+    if (x64)
+        k_colsum<double><<<P.G, kThreads, 0, s>>>(P.n, P.npad, P.KP, P.Ca, P.dcFree, x64, sums);
+    else
+        k_colsum<float><<<P.G, kThreads, 0, s>>>(P.n, P.npad, P.KP, P.Ca, P.dcFree, x, sums);
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 

@@ -488,9 +488,9 @@ static int gram_run(int batch, int rows, int cols, const __nv_bfloat16* hi, cons
     }
     GramArgs ga{rows, kblocks, tiles, nt, splits, work, flag};
     k_gram_tc<<<dim3(tiles, splits, batch), 128, kGramSmem, s>>>(mHi, mLo, ga);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     k_gram_reduce<<<dim3(16, tiles, batch), 256, 0, s>>>(rows, tiles, nt, splits, work, C, A64, shift);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
@@ -516,7 +516,7 @@ int dense_gram_check_abort(bool* aborted) {
 int dense_split_bf16(int batch, int rows, int cols, const float* A, int lda, __nv_bfloat16* hi, __nv_bfloat16* lo,
                      cudaStream_t s) {
     k_split_bf16<<<2048, 256, 0, s>>>(batch, rows, cols, A, lda, hi, lo);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
@@ -532,20 +532,20 @@ int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s) {
             k_syrk<<<dim3(m * (m + 1) / 2, batch), 256, 0, s>>>(n, A, k);
         }
     }
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(3 * nb - 2);
     return MPF_OK;
 }
 
 int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s) {
     MPF_CHECK((size_t)n * sizeof(double) <= 48 * 1024, MPF_EINVAL, "cholesky solve: n too large (%d)", n);
     k_chol_solve<<<batch * nrhs, 512, n * sizeof(double), s>>>(n, L, B, nrhs);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
 int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s) {
     k_add_shift<<<dim3((n + 255) / 256, batch), 256, 0, s>>>(n, A, shift);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 

@@ -121,13 +121,17 @@ __global__ void __launch_bounds__(512) k_jacobian(JacPlan jp, int npad, const fl
     float(*Ys)[KP][33] = reinterpret_cast<float(*)[KP][33]>(jsm);
     float(*Ts)[KP][33] = reinterpret_cast<float(*)[KP][33]>(jsm + 3 * KP * 33);
     float(*Ks)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33);
+    float(*Ms)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33 + 32 * 9);
+    float(*Ke)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33 + 2 * 32 * 9);
     const int f = blockIdx.y;
     const int e0 = blockIdx.x * 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nthreads = blockDim.x;
     const int e = e0 + lane;
     for (int i = threadIdx.x; i < 32 * 9; i += nthreads) {
         const int el = i / 9, k = i % 9;
-        Ks[el][k] = (e0 + el < jp.E) ? jp.Kf[(size_t)(e0 + el) * 9 + k] : 0.f;
+        const bool in = e0 + el < jp.E;
+        Ks[el][k] = in ? jp.Kf[(size_t)(e0 + el) * 9 + k] : 0.f;
+        Ms[el][k] = (in && jp.exact) ? jp.Mf[(size_t)(e0 + el) * 9 + k] : 0.f;
     }
     float acc[DPT][MP];
 #pragma unroll
@@ -145,13 +149,20 @@ __global__ void __launch_bounds__(512) k_jacobian(JacPlan jp, int npad, const fl
             if (e0 + el < jp.E) v = Xg[(size_t)jp.elements[(size_t)(e0 + el) * 3 + l] * KP + u];
             Ys[l][u][el] = v;
         }
+        // element matrix of this harmonic: K (reference mode) or K + alpha_c M
+        // (exact derivative of the 2.5D system matrix)
+        const float mc = jp.massCoef[ci];
+        for (int i = threadIdx.x; i < 32 * 9; i += nthreads) {
+            const int el = i / 9, k = i % 9;
+            Ke[el][k] = Ks[el][k] + mc * Ms[el][k];
+        }
         __syncthreads();
         const float b2 = jp.beta2[ci];
         for (int i = threadIdx.x; i < 32 * 3 * KP; i += nthreads) {
             const int el = i % 32, u = (i / 32) % KP, jj = i / (32 * KP);
-            // T_j[u] = sum_i Y[n_i][u] K[i + 3j] (stiffness stored row-major [i][j])
-            Ts[jj][u][el] = b2 * (Ys[0][u][el] * Ks[el][0 * 3 + jj] + Ys[1][u][el] * Ks[el][1 * 3 + jj] +
-                                  Ys[2][u][el] * Ks[el][2 * 3 + jj]);
+            // T_j[u] = sum_i Y[n_i][u] K[i + 3j] (element matrices stored row-major [i][j])
+            Ts[jj][u][el] = b2 * (Ys[0][u][el] * Ke[el][0 * 3 + jj] + Ys[1][u][el] * Ke[el][1 * 3 + jj] +
+                                  Ys[2][u][el] * Ke[el][2 * 3 + jj]);
         }
         __syncthreads();
 #pragma unroll
@@ -264,9 +275,11 @@ __global__ void k_residual(int rowsJ, int Mm, int Md, int MP, const float* __res
 // gamma[e] += sum_r J[r][e] w[r]  (J^T w of the dual Gauss-Newton step,
 // src/solver/inverse.cpp:198-204 then src/solver/solver.cpp:222)
 __global__ void k_update_gamma(int rowsJ, int Epad, int E, const float* __restrict__ J,
-                               const double* __restrict__ w, float* __restrict__ gamma) {
+                               const double* __restrict__ w, const int* __restrict__ frameActive,
+                               float* __restrict__ gamma) {
     extern __shared__ float ws[];
     const int f = blockIdx.y;
+    if (frameActive && !frameActive[f]) return;
     for (int r = threadIdx.x; r < rowsJ; r += blockDim.x) ws[r] = (float)w[(size_t)f * rowsJ + r];
     __syncthreads();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -295,7 +308,7 @@ int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, cons
     int blocks = (int)std::min<size_t>((slots + 255) / 256, 4096);
     k_assemble<<<dim3(blocks, F), 256, 0, s>>>(W, npad, E, cptr, contrib, Kf, Mf, Kd, Md, gamma, ref,
                                                logarithmic, S, R, S64, R64);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
@@ -303,14 +316,14 @@ int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const flo
                           float* refLayout, cudaStream_t s) {
     int blocks = (int)std::min<size_t>(((size_t)dataRows * kEllWidth + 255) / 256, 4096);
     k_export_ell<<<dim3(blocks, F), 256, 0, s>>>(W, npad, n, dataRows, slotMajor, refLayout);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
 int fem_launch_gram_meas(int G, int KP, int npad, const MeasPlan& mp, const float* X, double* Gm,
                          cudaStream_t s) {
     k_gram_meas<<<G, 256, 0, s>>>(KP, npad, mp.nnz, mp.nzPtr, mp.nzNode, mp.nzVal, X, Gm);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
@@ -320,7 +333,7 @@ int fem_launch_voltages(int F, int Ca, int KP, int Mm, int Md, const double* Gm,
     int total = F * Mm * Md;
     k_voltages<<<(total + 255) / 256, 256, 0, s>>>(F, Ca, KP, Mm, Md, Gm, beta, measU, measScale, driveU,
                                                    driveScale, V);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
@@ -330,11 +343,11 @@ static int launch_jac(int F, const JacPlan& jp, int npad, const float* X, const 
     const int warps = (jp.rowsJ / MP + DPT - 1) / DPT;
     MPF_CHECK(warps >= 1 && warps <= 16, MPF_ENOTSUP, "jacobian: %d drive rows not supported", jp.rowsJ / MP);
     dim3 grid(jp.Epad / 32, F);
-    const size_t smem = sizeof(float) * (6 * KP * 33 + 32 * 9);
+    const size_t smem = sizeof(float) * (6 * KP * 33 + 3 * 32 * 9);
     if (smem > 48 * 1024)
         MPF_CUDA(cudaFuncSetAttribute(k_jacobian<KP, MP, DPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_jacobian<KP, MP, DPT><<<grid, warps * 32, smem, s>>>(jp, npad, X, gamma, J, Jhi, Jlo);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
@@ -361,7 +374,7 @@ int fem_launch_transpose_jacobian(int F, int rowsJ, int Epad, int E, const float
                                   cudaStream_t s) {
     dim3 grid((E + 31) / 32, (rowsJ + 31) / 32, F);
     k_transpose<<<grid, dim3(32, 8), 0, s>>>(rowsJ, Epad, E, J, Jref);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
@@ -370,7 +383,7 @@ int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int np
                                const float* betaC, const float* X, float* out, cudaStream_t s) {
     k_fields_export<<<2048, 256, 0, s>>>(F, Ca, C, compOf, npad, KP, dataRows, cols, colU, colScale, betaC, X,
                                          out, n);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
@@ -378,15 +391,15 @@ int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, co
                         double* res, cudaStream_t s) {
     const int MP = rowsJ / (int)data_rows((uint32_t)Md);
     k_residual<<<F, 256, 0, s>>>(rowsJ, Mm, Md, MP, vMeas, V, y, res);
-    MPF_CUDA(cudaGetLastError());
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
-int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, const double* w, float* gamma,
-                            cudaStream_t s) {
+int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, const double* w,
+                            const int* frameActive, float* gamma, cudaStream_t s) {
     dim3 grid((E + 255) / 256, F);
-    k_update_gamma<<<grid, 256, rowsJ * sizeof(float), s>>>(rowsJ, Epad, E, J, w, gamma);
-    MPF_CUDA(cudaGetLastError());
+    k_update_gamma<<<grid, 256, rowsJ * sizeof(float), s>>>(rowsJ, Epad, E, J, w, frameActive, gamma);
+    MPF_LAUNCHED(1);
     return MPF_OK;
 }
 

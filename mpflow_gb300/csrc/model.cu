@@ -29,25 +29,28 @@ struct mpf_eit {
     mpf::DevBuf<double> Kd, Md64;
     mpf::DevBuf<float> Bc;            // [Ca][npad][KP] right-hand sides per active harmonic
     mpf::DevBuf<double> Bc64;
-    mpf::DevBuf<float> alpha, beta, beta2, betaC;
+    mpf::DevBuf<float> alpha, beta, beta2, betaC, massCoef;
+    int exactJacobian = 0;
     mpf::DevBuf<int32_t> dcFree, compOfD;
     mpf::DevBuf<int32_t> nzPtr, nzNode;
     mpf::DevBuf<double> nzVal;
     mpf::DevBuf<int32_t> driveU, measU, rowD, rowM, colU;
     mpf::DevBuf<float> driveScale, measScale, rowScale, colScale;
-    mpf::DevBuf<double> meanShift;    // [KP]
     int anyDcFree = 0;
+    float dcScale = 1.f;              // c' of the Neumann rank-one term
+    mpf::DevBuf<double> dcShift;      // [KP] constant difference to the reference's solution
     // workspace, grown on demand
     int capF = 0, capF64 = 0, capFJ = 0;
     mpf::DevBuf<float> S, R, X, Rv, Pv, Qv;
     mpf::DevBuf<double> S64, R64, X64;
-    mpf::DevBuf<double> partA, partB, rz, pq, bz, betaW, rr, bb, Gm, meanPart, meanSums;
+    mpf::DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, rr, bb, Gm, sumP, sumX;
     mpf::DevBuf<int> conv, active, iters;
     mpf::DevBuf<unsigned> counter;
     mpf::DevBuf<float> V, J, gramWork;
     mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
     mpf::DevBuf<double> A64, y, res;
-    mpf::DevBuf<int> info;
+    mpf::DevBuf<int> info, frameMask;
+    long long nnz = 0;                // used ELL slots (matrix nonzeros)
     std::vector<int> activeHost, itersHost;
     int* pinnedActive = nullptr;
     bool fieldsValid = false;
@@ -117,6 +120,7 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     m->nblk = m->npad / kRowTile;
     m->W = m->fs.density;
     m->levels = m->fs.levels;
+    for (uint32_t c : m->fs.refColIds) m->nnz += c != kInvalid;
     std::vector<double> K((size_t)m->E * 9), M((size_t)m->E * 9);
     p1_elemental(m->E, d->nodes, d->elements, K.data(), M.data());
     std::vector<float> Kf(K.begin(), K.end()), Mf(M.begin(), M.end());
@@ -208,22 +212,28 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     }
     m->Ca = (int)m->alphaH.size();
     m->anyDcFree = dcf.size() && dcf[0] ? 1 : 0;
-    // per active harmonic right-hand sides (the Neumann one projected to zero sum)
-    std::vector<double> Bc((size_t)m->Ca * P * KP, 0.0), shift(KP, 0.0);
-    for (int ci = 0; ci < m->Ca; ++ci) {
-        double* dst = Bc.data() + (size_t)ci * P * KP;
-        std::memcpy(dst, B0.data(), sizeof(double) * (size_t)P * KP);
-        if (dcf[ci]) {
-            for (int u = 0; u < KP; ++u) {
-                double s = 0.0;
-                for (int nd = 0; nd < m->n; ++nd) s += B0[(size_t)nd * KP + u];
-                shift[u] = s / ((double)m->n * (double)m->n);
-                double mean = s / (double)m->n;
-                for (int nd = 0; nd < m->n; ++nd) dst[(size_t)nd * KP + u] -= mean;
-            }
-        }
-    }
+    // right-hand sides per active harmonic (all equal to the unique excitations)
+    std::vector<double> Bc((size_t)m->Ca * P * KP, 0.0);
+    for (int ci = 0; ci < m->Ca; ++ci)
+        std::memcpy(Bc.data() + (size_t)ci * P * KP, B0.data(), sizeof(double) * (size_t)P * KP);
     std::vector<float> Bcf(Bc.begin(), Bc.end());
+    // rank-one scale c' = mean diagonal of S(ref) / n and the constant that
+    // turns the (A + c' 1 1^T) solution into the reference's (A + 1 1^T) one
+    {
+        double diagSum = 0.0;
+        for (int e = 0; e < m->E; ++e)
+            for (int i = 0; i < 3; ++i) diagSum += K[(size_t)e * 9 + i * 3 + i] * d->reference_value;
+        const double n = (double)m->n;
+        const double c = diagSum / n / n;
+        m->dcScale = (float)c;
+        std::vector<double> shift(KP, 0.0);
+        for (int u = 0; u < KP; ++u) {
+            double s = 0.0;
+            for (int nd = 0; nd < m->n; ++nd) s += B0[(size_t)nd * KP + u];
+            shift[u] = s / (n * n) * (1.0 - 1.0 / c);
+        }
+        MPF_TRY(m->dcShift.upload(shift));
+    }
 
     // ---- Jacobian row tables and field export tables
     std::vector<int32_t> rowD(m->rowsJ, -1), rowM(m->rowsJ, -1);
@@ -246,7 +256,13 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     for (int j = 0; j < Md; ++j) { colU[j] = dU[j]; colS[j] = dS[j]; }
     for (int j = 0; j < Mm; ++j) { colU[Md + j] = mU[j]; colS[Md + j] = mS[j]; }
     std::vector<float> beta2(m->Ca), betaC(m->C);
-    for (int ci = 0; ci < m->Ca; ++ci) beta2[ci] = m->betaH[ci] * m->betaH[ci];
+    std::vector<float> massCoef(m->Ca, 0.f);
+    m->exactJacobian = d->jacobian_mode == 1 ? 1 : 0;
+    for (int ci = 0; ci < m->Ca; ++ci) {
+        // reference: -h sum_c beta_c^2 (Y K Y); exact: -sum_c beta_c (Y (K + alpha_c M) Y)
+        beta2[ci] = m->exactJacobian ? (float)(m->betaH[ci] / m->height) : m->betaH[ci] * m->betaH[ci];
+        massCoef[ci] = m->exactJacobian ? m->alphaH[ci] : 0.f;
+    }
     for (int c = 0; c < m->C; ++c) betaC[c] = m->compOf[c] >= 0 ? (float)m->betaAll[c] : 0.f;
     std::vector<int32_t> elems(d->elements, d->elements + (size_t)3 * m->E);
 
@@ -265,6 +281,7 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     MPF_TRY(m->alpha.upload(m->alphaH));
     MPF_TRY(m->beta.upload(m->betaH));
     MPF_TRY(m->beta2.upload(beta2));
+    MPF_TRY(m->massCoef.upload(massCoef));
     MPF_TRY(m->betaC.upload(betaC));
     MPF_TRY(m->dcFree.upload(dcf));
     MPF_TRY(m->compOfD.upload(m->compOf));
@@ -280,7 +297,6 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     MPF_TRY(m->rowScale.upload(rowS));
     MPF_TRY(m->colU.upload(colU));
     MPF_TRY(m->colScale.upload(colS));
-    MPF_TRY(m->meanShift.upload(shift));
     MPF_CUDA(cudaMallocHost(&m->pinnedActive, sizeof(int) * 4096));
     *out = m.release();
     return MPF_OK;
@@ -303,14 +319,15 @@ static int ensure_workspace(mpf_eit* m, int F, bool refine, bool jacobian) {
         const size_t parts = G * m->nblk * m->KP, sc = G * m->KP;
         MPF_TRY(m->partA.alloc(parts));
         MPF_TRY(m->partB.alloc(parts));
-        MPF_TRY(m->meanPart.alloc(parts));
+        MPF_TRY(m->partC.alloc(parts));
         MPF_TRY(m->rz.alloc(sc));
         MPF_TRY(m->pq.alloc(sc));
         MPF_TRY(m->bz.alloc(sc));
         MPF_TRY(m->betaW.alloc(sc));
         MPF_TRY(m->rr.alloc(sc));
         MPF_TRY(m->bb.alloc(sc));
-        MPF_TRY(m->meanSums.alloc(sc));
+        MPF_TRY(m->sumP.alloc(sc));
+        MPF_TRY(m->sumX.alloc(sc));
         MPF_TRY(m->conv.alloc(sc));
         MPF_TRY(m->active.alloc(G));
         MPF_TRY(m->iters.alloc(G));
@@ -371,6 +388,10 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol) {
     P.dcFree = m->dcFree.ptr;
     P.partA = m->partA.ptr;
     P.partB = m->partB.ptr;
+    P.partC = m->partC.ptr;
+    P.sumP = m->sumP.ptr;
+    P.sumX0 = nullptr;
+    P.dcScale = m->dcScale;
     P.rz = m->rz.ptr;
     P.pq = m->pq.ptr;
     P.bz = m->bz.ptr;
@@ -414,6 +435,7 @@ static int run_cg(mpf_eit* m, const CgProblem& P, int maxIter, int checkEvery, c
     bool anyActive = true;
     while (done < maxIter) {
         MPF_CUDA(cudaGraphLaunch(exec, s));
+        add_launches(3LL * checkEvery);
         done += checkEvery;
         MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.active, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
         MPF_CUDA(cudaStreamSynchronize(s));
@@ -424,6 +446,7 @@ static int run_cg(mpf_eit* m, const CgProblem& P, int maxIter, int checkEvery, c
     MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.iters, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
     MPF_CUDA(cudaStreamSynchronize(s));
     int mx = 0;
+    m->itersHost.assign(m->pinnedActive, m->pinnedActive + G);
     for (int g = 0; g < G; ++g) mx = std::max(mx, m->pinnedActive[g]);
     *itersOut = mx;
     if (anyActive) {
@@ -481,15 +504,20 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     CgProblem P = make_problem(m, F, o.tol);
     int totalIters = 0, notConv = 0, refinements = 0;
     double maxRel = 0.0;
+    // fields are kept in the reference's convention; the iteration works on
+    // the c'-scaled Neumann system (see cg_kernels.cu)
+    if (warm && m->anyDcFree) MPF_TRY(cg_launch_dc_shift(P, m->dcShift.ptr, -1.f, s));
     if (!refine) {
+        if (warm && m->anyDcFree) {
+            MPF_TRY(cg_launch_colsum(P, m->X.ptr, nullptr, m->sumX.ptr, s));
+            P.sumX0 = m->sumX.ptr;
+        }
         MPF_TRY(cg_launch_init(P, !warm, s));
         MPF_TRY(run_cg(m, P, o.max_iter, o.check_every, s, &totalIters, &notConv));
     } else {
         const size_t vec = (size_t)P.G * m->npad * m->KP;
         if (warm) {
             // X64 = X (float fields of the previous call)
-            std::vector<char> dummy;
-            (void)dummy;
             MPF_CUDA(cudaMemsetAsync(m->X64.ptr, 0, vec * sizeof(double), s));
             MPF_TRY(cg_launch_accumulate64(P, m->X64.ptr, s));
         } else {
@@ -499,16 +527,20 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
         CgProblem Pin = P;
         Pin.b = m->Rv.ptr;  // inner right-hand side: the float image of the FP64 residual
         Pin.bPerGroup = 1;
+        double prevRel = 1e300;
         for (int outer = 0; outer <= o.max_refine; ++outer) {
-            MPF_TRY(cg_launch_residual64(P, m->S64.ptr, m->R64.ptr, m->X64.ptr, m->Bc64.ptr, m->partA.ptr,
-                                         m->partB.ptr, m->rr.ptr, m->bb.ptr, s));
+            if (m->anyDcFree) MPF_TRY(cg_launch_colsum(P, nullptr, m->X64.ptr, m->sumX.ptr, s));
+            MPF_TRY(cg_launch_residual64(P, m->S64.ptr, m->R64.ptr, m->X64.ptr, m->Bc64.ptr, m->sumX.ptr,
+                                         m->partA.ptr, m->partB.ptr, m->rr.ptr, m->bb.ptr, s));
             MPF_CUDA(cudaMemcpyAsync(rrH.data(), m->rr.ptr, sizeof(double) * rrH.size(), cudaMemcpyDeviceToHost, s));
             MPF_CUDA(cudaMemcpyAsync(bbH.data(), m->bb.ptr, sizeof(double) * bbH.size(), cudaMemcpyDeviceToHost, s));
             MPF_CUDA(cudaStreamSynchronize(s));
             maxRel = 0.0;
             for (size_t i = 0; i < rrH.size(); ++i)
                 if (bbH[i] > 0.0) maxRel = std::max(maxRel, std::sqrt(rrH[i] / bbH[i]));
-            if (maxRel <= o.refine_tol || outer == o.max_refine) break;
+            // stop when converged, out of steps, or no longer gaining (FP32 inner limit)
+            if (maxRel <= o.refine_tol || outer == o.max_refine || maxRel > 0.5 * prevRel) break;
+            prevRel = maxRel;
             int it = 0, nc = 0;
             MPF_TRY(cg_launch_init(Pin, true, s));
             MPF_TRY(run_cg(m, Pin, o.max_iter, o.check_every, s, &it, &nc));
@@ -520,7 +552,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
         MPF_TRY(cg_launch_to_float(P, m->X64.ptr, s));
         if (maxRel > o.refine_tol) notConv = std::max(notConv, 1);
     }
-    if (m->anyDcFree) MPF_TRY(cg_launch_mean_fix(P, m->meanShift.ptr, m->meanPart.ptr, m->meanSums.ptr, s));
+    if (m->anyDcFree) MPF_TRY(cg_launch_dc_shift(P, m->dcShift.ptr, 1.f, s));
     m->fieldsValid = true;
     m->lastFrames = F;
     MeasPlan mp{(int)m->nzNode.count, m->nzNode.ptr, nullptr, m->nzVal.ptr, m->nzPtr.ptr};
@@ -529,7 +561,8 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
                                 m->measScale.ptr, m->driveU.ptr, m->driveScale.ptr, m->V.ptr, s));
     if (wantJ) {
         JacPlan jp{m->rowsJ, m->Epad, m->E, m->KP, m->Ca, m->rowD.ptr, m->rowM.ptr, m->rowScale.ptr,
-                   m->beta2.ptr, m->elements.ptr, m->Kf.ptr, m->ref, (float)m->height, m->logarithmic};
+                   m->beta2.ptr, m->massCoef.ptr, m->elements.ptr, m->Kf.ptr, m->Mf.ptr, m->exactJacobian,
+                   m->ref, (float)m->height, m->logarithmic};
         MPF_TRY(fem_launch_jacobian(F, jp, m->MmPad, m->npad, m->X.ptr, gamma, m->J.ptr, m->Jhi.ptr, m->Jlo.ptr, s));
     }
     MPF_CUDA(cudaStreamSynchronize(s));
@@ -565,20 +598,19 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
     return MPF_OK;
 }
 
-int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, const mpf_solve_opts* o,
-            double* residual, mpf_solve_stats* stats, cudaStream_t s) {
-    MPF_TRY(check_device(m));
-    MPF_CHECK(F >= 1 && gamma && vMeas, MPF_EINVAL, "mpFlow::solver::Solver::solveAbsolute: bad arguments");
-    int st = eit_forward_ws(m, F, gamma, true, o, stats, s);
-    if (st != MPF_OK && st != MPF_ENOCONV) return st;
-    MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
+// J J^T + mu I (split-BF16 tensor cores) -> FP64 Cholesky -> w -> gamma += J^T w
+// for the frames in frameActive (all if null); y holds the residual on entry.
+static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* frameActive, cudaStream_t s) {
     const double mu = (double)m->ref * lambda * (double)m->ref * lambda;
     MPF_TRY(dense_gram_f64_shift(F, m->rowsJ, m->Epad, m->Jhi.ptr, m->Jlo.ptr, m->Epad, mu, m->A64.ptr,
                                  m->gramWork.ptr, m->gramWork.count, s));
     MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s));
     MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s));
-    MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->J.ptr, m->y.ptr, gamma, s));
-    if (residual) MPF_CUDA(cudaMemcpyAsync(residual, m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
+    MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->J.ptr, m->y.ptr, frameActive, gamma, s));
+    return MPF_OK;
+}
+
+static int gn_check(mpf_eit* m, int F, cudaStream_t s) {
     std::vector<int> info(F);
     MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
     MPF_CUDA(cudaStreamSynchronize(s));
@@ -587,7 +619,112 @@ int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, 
     MPF_CHECK(!aborted, MPF_ETIMEOUT, "gram kernel: a pipeline wait timed out");
     for (int f = 0; f < F; ++f)
         MPF_CHECK(info[f] == 0, MPF_EBREAKDOWN, "Cholesky of (J J^T + mu I) failed at pivot %d (frame %d)", info[f], f);
+    return MPF_OK;
+}
+
+int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, const mpf_solve_opts* o,
+            double* residual, mpf_solve_stats* stats, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma && vMeas, MPF_EINVAL, "mpFlow::solver::Solver::solveAbsolute: bad arguments");
+    int st = eit_forward_ws(m, F, gamma, true, o, stats, s);
+    if (st != MPF_OK && st != MPF_ENOCONV) return st;
+    MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
+    MPF_TRY(gn_update(m, F, gamma, lambda, nullptr, s));
+    if (residual) MPF_CUDA(cudaMemcpyAsync(residual, m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
+    MPF_TRY(gn_check(m, F, s));
     return st;
+}
+
+// Gauss-Newton iterations until every frame's relative data residual is at
+// most `target` (frames that reach it are frozen) or maxIters updates.
+int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, double target, int maxIters,
+             const mpf_solve_opts* oIn, int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma && vMeas && maxIters >= 0, MPF_EINVAL, "mpf_gn_solve: bad arguments");
+    auto t0 = std::chrono::steady_clock::now();
+    mpf_solve_opts o;
+    fill_defaults(oIn, o, m->n);
+    MPF_TRY(m->frameMask.alloc((size_t)F));
+    std::vector<int> mask(F, 1), iters(F, 0);
+    std::vector<double> res(F, 0.0);
+    int cgTotal = 0, gnIters = 0;
+    for (int it = 0;; ++it) {
+        mpf_solve_stats fs{};
+        mpf_solve_opts oi = o;
+        oi.warm_start = it > 0 ? 1 : o.warm_start;
+        int st = eit_forward_ws(m, F, gamma, true, &oi, &fs, s);
+        if (st != MPF_OK && st != MPF_ENOCONV) return st;
+        cgTotal += fs.iterations;
+        MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
+        MPF_CUDA(cudaMemcpyAsync(res.data(), m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        int live = 0;
+        for (int f = 0; f < F; ++f) {
+            if (mask[f] && res[f] <= target) mask[f] = 0;
+            live += mask[f];
+        }
+        if (live == 0 || it == maxIters) break;
+        for (int f = 0; f < F; ++f) iters[f] += mask[f];
+        MPF_CUDA(cudaMemcpyAsync(m->frameMask.ptr, mask.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+        MPF_TRY(gn_update(m, F, gamma, lambda, m->frameMask.ptr, s));
+        MPF_TRY(gn_check(m, F, s));
+        ++gnIters;
+    }
+    int converged = 0;
+    for (int f = 0; f < F; ++f) converged += res[f] <= target;
+    if (itersOut) std::copy(iters.begin(), iters.end(), itersOut);
+    if (resOut) std::copy(res.begin(), res.end(), resOut);
+    if (stats) {
+        stats->gn_iterations = gnIters;
+        stats->cg_iterations = cgTotal;
+        stats->frames_converged = converged;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return MPF_OK;
+}
+
+// Times the three CG kernels of one iteration with CUDA events on `s`
+// (tolerance 0, so no group retires during the measurement).
+int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma && reps >= 1 && ms && bytes, MPF_EINVAL, "mpf_eit_profile_cg: bad arguments");
+    MPF_TRY(ensure_workspace(m, F, false, false));
+    MPF_TRY(eit_assemble(m, F, gamma, false, s));
+    CgProblem P = make_problem(m, F, 0.0);
+    MPF_TRY(cg_launch_init(P, true, s));
+    cudaEvent_t ev[4];
+    for (auto& e : ev) MPF_CUDA(cudaEventCreate(&e));
+    double acc[3] = {0, 0, 0};
+    for (int r = 0; r < reps; ++r) {
+        MPF_CUDA(cudaEventRecord(ev[0], s));
+        MPF_TRY(cg_launch_kernel(P, 0, s));
+        MPF_CUDA(cudaEventRecord(ev[1], s));
+        MPF_TRY(cg_launch_kernel(P, 1, s));
+        MPF_CUDA(cudaEventRecord(ev[2], s));
+        MPF_TRY(cg_launch_kernel(P, 2, s));
+        MPF_CUDA(cudaEventRecord(ev[3], s));
+        MPF_CUDA(cudaEventSynchronize(ev[3]));
+        for (int k = 0; k < 3; ++k) {
+            float t = 0.f;
+            MPF_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+            acc[k] += t;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    const double G = (double)F * m->Ca, n = m->n, K = m->K;
+    for (int k = 0; k < 3; ++k) ms[k] = acc[k] / reps;
+    bytes[0] = G * ((double)m->nnz * 12.0 + 2.0 * K * n * 4.0);   // S, R, column + p gather + q
+    bytes[1] = G * (6.0 * K * n * 4.0 + 2.0 * n * 4.0);            // x, r rw; p, q read; diagonal
+    bytes[2] = G * (3.0 * K * n * 4.0 + 2.0 * n * 4.0);            // r, p read; p write; diagonal
+    return MPF_OK;
+}
+
+int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count) {
+    MPF_CHECK(out && count, MPF_EINVAL, "mpf_eit_group_iterations: null argument");
+    const int n = (int)m->itersHost.size();
+    for (int i = 0; i < n && i < cap; ++i) out[i] = m->itersHost[i];
+    *count = n;
+    return MPF_OK;
 }
 
 void eit_destroy(mpf_eit* m) {

@@ -35,6 +35,10 @@ struct CgProblem {
     // reduction state
     double* partA;       // [G][nblk][KP]
     double* partB;
+    double* partC;
+    double* sumP;        // [G][KP] sum(p) of Neumann groups (the 1 1^T term)
+    const double* sumX0; // [G][KP] sum(x0) for a warm start, or null
+    float dcScale;       // c' of the rank-one term c' 1 1^T (see model.cu)
     double* rz;          // [G][KP]
     double* pq;
     double* bz;
@@ -49,13 +53,14 @@ struct CgProblem {
 // cg_kernels.cu
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s);
+int cg_launch_kernel(const CgProblem& P, int which /*0 spmm, 1 update, 2 direction*/, cudaStream_t s);
 int cg_launch_residual64(const CgProblem& P, const double* S64, const double* R64, const double* x64,
-                         const double* b64, double* partR, double* partB, double* rr, double* bb,
-                         cudaStream_t s);
+                         const double* b64, const double* sumX64, double* partR, double* partB, double* rr,
+                         double* bb, cudaStream_t s);
+int cg_launch_colsum(const CgProblem& P, const float* x, const double* x64, double* sums, cudaStream_t s);
+int cg_launch_dc_shift(const CgProblem& P, const double* shift, float sign, cudaStream_t s);
 int cg_launch_accumulate64(const CgProblem& P, double* x64, cudaStream_t s);
 int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s);
-int cg_launch_mean_fix(const CgProblem& P, const double* shift /*[KP]*/, double* part, double* sums,
-                       cudaStream_t s);
 
 // fem_kernels.cu
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
@@ -81,9 +86,12 @@ struct JacPlan {
     const int32_t* rowD;     // [rowsJ] unique column of the drive field, -1 for padding
     const int32_t* rowM;     // [rowsJ] unique column of the measurement field
     const float* rowScale;   // [rowsJ] drive scale * measurement scale
-    const float* beta2;      // [Ca] beta_c^2
+    const float* beta2;      // [Ca] harmonic weight: beta_c^2 (reference) or beta_c / h (exact)
+    const float* massCoef;   // [Ca] alpha_c in exact mode, 0 in reference mode
     const int32_t* elements; // [E][3]
     const float* Kf;         // [E][9]
+    const float* Mf;         // [E][9] (read only in exact mode)
+    int exact;
     float ref, height;       // J *= -height (open sources)
     int logarithmic;
 };
@@ -97,7 +105,7 @@ int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int np
 int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, const float* V,
                         double* y, double* res, cudaStream_t s);
 int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, const double* w,
-                            float* gamma, cudaStream_t s);
+                            const int* frameActive, float* gamma, cudaStream_t s);
 
 // dense_kernels.cu
 int dense_gram_split_bf16(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo,

@@ -20,6 +20,10 @@ constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr int kRowTile = 128;             // internal node padding (CTA row tile)
 constexpr int kElemTile = 64;             // internal element padding (GEMM K block)
 
+// ---- kernel launch accounting (read by mpf_kernel_launches) -------------
+void add_launches(long long n);
+long long launches();
+
 // ---- error reporting ----------------------------------------------------
 void set_error(const char* fmt, ...);
 int fail(int status, const char* fmt, ...);
@@ -31,6 +35,13 @@ const char* last_error();
         if (mpf_e_ != cudaSuccess)                                                        \
             return ::mpf::fail(MPF_ECUDA, "%s: %s (%s:%d)", #call,                       \
                                cudaGetErrorString(mpf_e_), __FILE__, __LINE__);          \
+    } while (0)
+
+// after a kernel launch: count it and surface launch errors
+#define MPF_LAUNCHED(n)                         \
+    do {                                        \
+        ::mpf::add_launches(n);                 \
+        MPF_CUDA(cudaGetLastError());           \
     } while (0)
 
 #define MPF_CHECK(cond, status, ...)                       \

@@ -148,7 +148,7 @@ class EIT:
 
     def __init__(self, mesh: IrregularMesh, sources: Sources, referenceValue: float = 1.0,
                  components: int = 1, height: float = 1.0, portHeight: float = 1.0,
-                 logarithmic: bool = False, device: int = 0):
+                 logarithmic: bool = False, device: int = 0, exact_jacobian: bool = False):
         self.mesh, self.sources = mesh, sources
         self.referenceValue = float(referenceValue)
         self.components, self.height, self.portHeight = int(components), float(height), float(portHeight)
@@ -163,7 +163,7 @@ class EIT:
             sources.drivePattern.shape[1], sources.measurementPattern.shape[1],
             ptr(sources.drivePattern).value, ptr(sources.measurementPattern).value,
             ptr(sources.values).value, sources.type, self.referenceValue, int(self.logarithmic),
-            self.components, self.height, self.portHeight, self.device)
+            self.components, self.height, self.portHeight, self.device, int(bool(exact_jacobian)))
         h = ctypes.c_void_p()
         check(lib().mpf_eit_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h
@@ -200,10 +200,12 @@ class EIT:
         check(lib().mpf_eit_assemble(self._h, F, ptr(g), ptr(S), ptr(R), _stream()))
         return S, R
 
-    def solve(self, materialDistribution, options: SolveOptions | None = None, jacobian: bool = False):
+    def solve(self, materialDistribution, options: SolveOptions | None = None, jacobian: bool = False,
+              raise_on_noconv: bool = True):
         """Forward solve; returns V (frames x Mm x Md) and, if asked, J
         (frames x rowsJ x E, the reference's column-major jacobian as its
-        transpose view)."""
+        transpose view).  With raise_on_noconv=False an iteration-cap hit is
+        only recorded in last_stats.not_converged."""
         import torch
         g, F = self._frames(materialDistribution)
         Mm, Md = self.info["meas_count"], self.info["drive_count"]
@@ -214,9 +216,11 @@ class EIT:
                             device=g.device)
         st = _ffi.SolveStats()
         o = (options or SolveOptions()).c()
-        check(lib().mpf_eit_forward(self._h, F, ptr(g), ptr(V), ptr(J), ctypes.byref(o), ctypes.byref(st),
-                                    _stream()))
+        status = lib().mpf_eit_forward(self._h, F, ptr(g), ptr(V), ptr(J), ctypes.byref(o), ctypes.byref(st),
+                                       _stream())
         self.last_stats = st
+        if status != _ffi.MPF_OK and (raise_on_noconv or status != 4):
+            check(status)
         Vm = V.transpose(1, 2)  # (F, Mm, Md): column-major Mm x Md per frame
         if jacobian:
             return Vm, J.transpose(1, 2)
@@ -246,6 +250,39 @@ class EIT:
                                 ctypes.byref(st), _stream()))
         self.last_stats = st
         return res
+
+    def gn_solve(self, gamma, v_meas, lam: float, target: float = 1e-3, max_iters: int = 10,
+                 options: SolveOptions | None = None):
+        """Gauss-Newton until every frame's relative data residual <= target
+        (mpf_gn_solve); gamma is updated in place.  Returns (updates per
+        frame, final residual per frame, GnStats)."""
+        g, F = self._frames(gamma)
+        if g.data_ptr() != gamma.data_ptr():
+            raise ValueError("gamma must be contiguous")
+        vm = v_meas.reshape(F, -1).contiguous()
+        iters = np.zeros(F, np.int32)
+        res = np.zeros(F)
+        st = _ffi.GnStats()
+        o = (options or SolveOptions()).c()
+        check(lib().mpf_gn_solve(self._h, F, ptr(g), ptr(vm), float(lam), float(target), int(max_iters),
+                                 ctypes.byref(o), ptr(iters), ptr(res), ctypes.byref(st), _stream()))
+        return iters, res, st
+
+    def group_iterations(self) -> np.ndarray:
+        """CG iterations per (frame, active harmonic) group of the last inner solve."""
+        out = np.zeros(65536, np.int32)
+        cnt = ctypes.c_int32(0)
+        check(lib().mpf_eit_group_iterations(self._h, ptr(out), out.size, ctypes.byref(cnt)))
+        return out[:cnt.value].copy()
+
+    def profile_cg(self, gamma, reps: int = 20):
+        """Mean CUDA-event time (ms) and algorithmic bytes of one launch of the
+        SpMM, update and direction kernels (mpf_eit_profile_cg)."""
+        g, F = self._frames(gamma)
+        ms = np.zeros(3)
+        by = np.zeros(3)
+        check(lib().mpf_eit_profile_cg(self._h, F, ptr(g), int(reps), ptr(ms), ptr(by), _stream()))
+        return ms, by
 
 
 def gram_split_bf16(A):

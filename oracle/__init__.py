@@ -321,12 +321,14 @@ class Setup:
 
 
 def eit_forward(s: Setup, gamma: np.ndarray, tol: float = 1e-12, want_jacobian: bool = True,
-                max_iter: int = 0):
+                max_iter: int = 0, exact: bool = False):
     """Restatement of EIT::solve for current (Open) sources.
 
     Returns (V, J, fields): V is Mm x Md, J is rowsJ x E column-major (row =
     drive * roundMeas + meas), fields is a list of n x (Md+Mm) arrays per
-    component."""
+    component.  exact=True replaces the reference's 2.5D Jacobian (stiffness
+    term only, weight height*beta_c^2) by the exact derivative of V (element
+    matrix K + alpha_c M, weight beta_c); both agree for one harmonic."""
     n = s.nodes.shape[0]
     pattern = np.concatenate([s.drive * s.values[None, :], s.meas], axis=1)
     att = (s.meas.T @ s.exc.T)                       # Mm x N  (eit.cpp:93-94)
@@ -341,9 +343,13 @@ def eit_forward(s: Setup, gamma: np.ndarray, tol: float = 1e-12, want_jacobian: 
         excitation = (s.exc @ pattern) * beta
         x, _ = pcg(s.layout, sysv, excitation, tol=tol, max_iter=max_iter, dc_free=(c == 0))
         fields.append(x)
-        if want_jacobian:
+        if want_jacobian and not exact:
             calc_jacobian(s.elements, s.K, x, s.Md, s.Mm, gamma, s.ref, s.logarithmic, s.rowsJ,
                           J=J, additive=(c > 0))
+        elif want_jacobian and abs(beta) > 1e-12 / s.height:
+            Jc = calc_jacobian(s.elements, s.K + alpha * s.M, x, s.Md, s.Mm, gamma, s.ref,
+                               s.logarithmic, s.rowsJ)
+            J += Jc / (beta * s.height)
         V += att @ x[:, :s.Md]
     if want_jacobian:
         J *= s.height

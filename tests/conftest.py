@@ -39,13 +39,14 @@ def pytest_collection_modifyitems(config, items):
             item.add_marker(skip)
 
 
-def make_setup(rings=12, ports=16, width=0.1, components=1, height=1.0, port_height=1.0, current=1e-3,
+def make_setup(rings=16, ports=16, width=0.1, components=1, height=1.0, port_height=1.0, current=1e-3,
                logarithmic=False, ref=1.0):
     """Mesh + adjacent drive/measurement sources for both the library and the oracle."""
     import mpflow_gb300 as mp
     import oracle
     mesh = mp.IrregularMesh.ring(rings)
     pr = mp.Ports.circularBoundary(ports, width, mesh)
+    assert (pr.edges >= 0).sum(axis=1).min() >= 1, "mesh too coarse: a port has no boundary edge"
     pat = mp.adjacent_pattern(ports)
     src = mp.Sources(mp.OPEN, current, pr, pat, pat)
     orc = oracle.Setup(mesh.nodes, mesh.elements, mesh.edges, mesh.boundary, pr.edges, pat, pat,

@@ -1,0 +1,56 @@
+"""The C-ABI library loads without a GPU and exports every entry point that
+include/*.h declares (no compute calls)."""
+import ctypes
+import glob
+import os
+import re
+
+import mpflow_gb300
+from mpflow_gb300 import _ffi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for header in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(header).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(mpf_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert {"mpf_eit_create", "mpf_eit_forward", "mpf_gn_step", "mpf_gram_split_bf16",
+            "mpf_cholesky_solve_f64"} <= names
+
+
+def test_library_exports_all_declared_symbols():
+    L = ctypes.CDLL(_ffi.LIB_PATH)
+    missing = [n for n in sorted(declared_functions()) if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header():
+    assert declared_functions() <= set(_ffi.SIGNATURES)
+
+
+def test_host_only_calls_work_without_gpu():
+    L = mpflow_gb300.lib()
+    assert L.mpf_version().startswith(b"mpflow_gb300")
+    assert L.mpf_data_rows(19441) == 19456
+    n, e = ctypes.c_int32(), ctypes.c_int32()
+    assert L.mpf_ring_mesh_counts(80, ctypes.byref(n), ctypes.byref(e)) == 0
+    assert (n.value, e.value) == (19441, 38400)
+    assert L.mpf_ring_mesh_counts(0, ctypes.byref(n), ctypes.byref(e)) == 1
+    assert b"rings" in L.mpf_last_error()
+
+
+def test_invalid_model_arguments_are_rejected():
+    L = mpflow_gb300.lib()
+    h = ctypes.c_void_p()
+    assert L.mpf_eit_create(None, ctypes.byref(h)) == 1
+    assert L.mpf_eit_forward(None, 1, None, None, None, None, None, None) == 1
+    assert b"model == nullptr" in L.mpf_last_error()

@@ -20,7 +20,7 @@ def test_assembly_matches_oracle():
     import oracle
     import mpflow_gb300 as mp
     torch = _torch()
-    mesh, src, orc = make_setup(rings=14)
+    mesh, src, orc = make_setup(rings=16)
     g = inclusion_sigma(mesh, seed=3)
     model = mp.EIT(mesh, src, 1.0)
     S, R = model.assemble(torch.tensor(g, dtype=torch.float32, device="cuda"))
@@ -69,14 +69,17 @@ def test_forward_2p5d_refined():
     assert rel_err(J[0].cpu().numpy(), Jo) < 1e-4
     F = model.fields(1)[0].cpu().numpy()  # (C, Md+Mm, dataRows)
     n = mesh.nodes.shape[0]
+    scale = np.abs(Fo[0]).max()
     for c in range(8):
-        assert rel_err(F[c][:, :n].T, Fo[c]) < 1e-5, c
+        # harmonic 4 has beta = 2 sin(pi)/(4 pi) ~ 1e-17: its field is rounding noise
+        err = np.abs(F[c][:, :n].T - Fo[c]).max() / scale
+        assert err < 1e-6, (c, err)
 
 
 def test_batched_frames_match_single():
     import mpflow_gb300 as mp
     torch = _torch()
-    mesh, src, orc = make_setup(rings=12, ports=16, components=3, height=2.0)
+    mesh, src, orc = make_setup(rings=16, ports=16, components=3, height=2.0)
     gs = np.stack([inclusion_sigma(mesh, seed=s) for s in range(4)])
     model = mp.EIT(mesh, src, 1.0, components=3, height=2.0)
     opts = mp.SolveOptions(tol=1e-7, refine_tol=1e-10)
@@ -136,3 +139,105 @@ def test_gn_step_matches_oracle_dual():
     d = gt[0].cpu().numpy() - 1.0
     assert abs(res[0] - np.linalg.norm(y) / np.linalg.norm(oracle.flatten_measurement(Vmeas, orc))) < 1e-5
     assert rel_err(d, d_ref) < 2e-3, rel_err(d, d_ref)
+
+
+def test_exact_jacobian_2p5d_matches_oracle():
+    import oracle
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=16, ports=16, components=4, height=2.0)
+    rng = np.random.default_rng(3)
+    g = np.exp(0.3 * rng.standard_normal(mesh.elements.shape[0]))
+    Vo, Jo, _ = oracle.eit_forward(orc, g, tol=1e-13, exact=True)
+    model = mp.EIT(mesh, src, 1.0, components=4, height=2.0, exact_jacobian=True)
+    V, J = model.solve(torch.tensor(g, dtype=torch.float32, device="cuda"),
+                       mp.SolveOptions(tol=1e-5, refine_tol=1e-10), jacobian=True)
+    assert rel_err(V[0].cpu().numpy(), Vo) < 1e-5
+    assert rel_err(J[0].cpu().numpy(), Jo) < 1e-4
+
+
+def test_identity_measurement_pattern_constant_mode():
+    """Identity measurement patterns are not zero-sum, so the voltages see the
+    constant mode of the Neumann harmonic (the reference's (A + 1 1^T) system)."""
+    import oracle
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh = mp.IrregularMesh.ring(16)
+    pr = mp.Ports.circularBoundary(16, 0.1, mesh)
+    drive = mp.adjacent_pattern(16)
+    meas = np.eye(16)
+    src = mp.Sources(mp.OPEN, 1e-3, pr, drive, meas)
+    orc = oracle.Setup(mesh.nodes, mesh.elements, mesh.edges, mesh.boundary, pr.edges, drive, meas,
+                       np.full(16, 1e-3), components=2, height=2.0)
+    g = inclusion_sigma(mesh, seed=5)
+    Vo, Jo, _ = oracle.eit_forward(orc, g, tol=1e-13)
+    model = mp.EIT(mesh, src, 1.0, components=2, height=2.0)
+    V, J = model.solve(torch.tensor(g, dtype=torch.float32, device="cuda"),
+                       mp.SolveOptions(tol=1e-5, refine_tol=1e-10), jacobian=True)
+    assert model.info["unique_columns"] == 32
+    assert rel_err(V[0].cpu().numpy(), Vo) < 1e-5
+    assert rel_err(J[0].cpu().numpy(), Jo) < 1e-4
+
+
+def test_warm_start_reproduces_cold_solve():
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=24, ports=16, components=3, height=2.0)
+    gs = torch.tensor(np.stack([inclusion_sigma(mesh, seed=s) for s in range(3)]), dtype=torch.float32,
+                      device="cuda")
+    model = mp.EIT(mesh, src, 1.0, components=3, height=2.0)
+    V1 = model.solve(gs, mp.SolveOptions(tol=1e-7)).cpu().numpy()
+    cold = model.last_stats.iterations
+    V2 = model.solve(gs * 1.01, mp.SolveOptions(tol=1e-7, warm_start=True)).cpu().numpy()
+    warm = model.last_stats.iterations
+    # linear parametrisation: V scales as 1/sigma
+    assert rel_err(V2 * 1.01, V1) < 1e-5
+    assert warm < cold
+
+
+def test_iteration_cap_is_reported():
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=16)
+    model = mp.EIT(mesh, src, 1.0)
+    g = torch.ones((1, mesh.elements.shape[0]), device="cuda")
+    with pytest.raises(mp.MpfError) as ei:
+        model.solve(g, mp.SolveOptions(tol=1e-7, max_iter=2, check_every=1))
+    assert ei.value.status == 4
+    model.solve(g, mp.SolveOptions(tol=1e-7, max_iter=2, check_every=1), raise_on_noconv=False)
+    assert model.last_stats.not_converged > 0
+
+
+def test_gn_solve_reaches_target():
+    import oracle
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=24, ports=16, logarithmic=True)
+    E = mesh.elements.shape[0]
+    model = mp.EIT(mesh, src, 1.0, logarithmic=True)
+    vt = np.stack([10 * np.log10(inclusion_sigma(mesh, seed=s, value=v)) for s, v in ((0, 0.2), (1, 5.0))])
+    Vm = model.solve(torch.tensor(vt, dtype=torch.float32, device="cuda"), mp.SolveOptions(tol=1e-6, refine_tol=1e-10))
+    _, J0 = model.solve(torch.zeros((1, E), device="cuda"), mp.SolveOptions(tol=1e-6), jacobian=True)
+    lam = 2e-2 * float(J0.norm() / np.sqrt(J0.shape[1]))
+    g = torch.zeros((2, E), device="cuda")
+    iters, res, st = model.gn_solve(g, Vm, lam, target=5e-4, max_iters=10, options=mp.SolveOptions(tol=1e-6))
+    assert st.frames_converged == 2 and (res <= 5e-4).all()
+    assert (iters >= 1).all()
+    # the first GN update agrees with the oracle's dual step from the same start
+    g1 = torch.zeros((1, E), device="cuda")
+    model.gn_step(g1, Vm[0:1], lam, mp.SolveOptions(tol=1e-7, refine_tol=1e-10))
+    V0, Jo, _ = oracle.eit_forward(orc, np.zeros(E), tol=1e-13)
+    y = Vm[0].cpu().numpy().astype(np.float64).T.reshape(-1) - oracle.flatten_measurement(V0, orc)
+    d_ref = oracle.inverse_dual(Jo, y, 1.0, lam)
+    assert rel_err(g1[0].cpu().numpy(), d_ref) < 5e-3
+
+
+def test_profile_cg_reports_bandwidth():
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=24)
+    model = mp.EIT(mesh, src, 1.0)
+    n0 = mp.lib().mpf_kernel_launches()
+    ms, by = model.profile_cg(torch.ones((2, mesh.elements.shape[0]), device="cuda"), reps=3)
+    assert (ms > 0).all() and (by > 0).all()
+    assert mp.lib().mpf_kernel_launches() - n0 >= 10

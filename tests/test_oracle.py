@@ -1,0 +1,121 @@
+"""Known-answer checks of the FP64 oracle (CPU only).
+
+The reference ships no tests or golden vectors, so the oracle is pinned by
+properties that the reference's mathematics must satisfy and by the committed
+fixtures in tests/golden (generated from this oracle by make_golden.py).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import inclusion_sigma, make_setup
+
+import oracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_padding_rule():
+    # src/numeric/matrix.cpp:49-55 with roundTo (mathematics.h:42-44)
+    assert [oracle.data_rows(n) for n in (1, 2, 15, 16, 17, 32, 2791, 19441)] == \
+        [1, 16, 16, 16, 32, 32, 2800, 19456]
+
+
+def test_p1_integrals_analytic():
+    mesh, _, orc = make_setup(rings=6, ports=4, width=0.5)
+    K, M = orc.K, orc.M
+    # rows of the stiffness matrix sum to zero (constants are in the kernel)
+    assert np.abs(K.sum(axis=2)).max() < 1e-13
+    # mass integrates to the triangle area; total = area of the 36-gon
+    assert abs(M.sum() - 0.5 * 36 * np.sin(2 * np.pi / 36)) < 1e-13
+    # stiffness is symmetric positive semidefinite per element
+    assert np.abs(K - K.transpose(0, 2, 1)).max() < 1e-14
+    assert np.linalg.eigvalsh(K).min() > -1e-13
+
+
+def test_ell_layout_insertion_order():
+    mesh, _, orc = make_setup(rings=5, ports=4, width=0.5)
+    lay = orc.layout
+    # every used slot of a row holds a distinct neighbour; the diagonal is present
+    for row in range(mesh.nodes.shape[0]):
+        ids = lay.colIds[row][lay.colIds[row] != oracle.INVALID]
+        assert len(set(ids.tolist())) == len(ids)
+        assert row in ids
+    # the first element's nodes were inserted first (src/fem/equation.cpp:133-138)
+    e0 = mesh.elements[0]
+    for i in range(3):
+        assert list(lay.colIds[e0[i]][:3]) == list(e0)
+
+
+def test_forward_reciprocity_and_conservation():
+    mesh, _, orc = make_setup(rings=16)
+    g = inclusion_sigma(mesh, seed=2)
+    V, J, _ = oracle.eit_forward(orc, g, tol=1e-13)
+    # adjacent drive == adjacent measurement: V is symmetric up to the current value
+    Vs = V / 1e-3
+    assert np.abs(Vs - Vs.T).max() / np.abs(Vs).max() < 1e-10
+    # measurements around the ring sum to zero for every drive
+    assert np.abs(V.sum(axis=0)).max() / np.abs(V).max() < 1e-12
+
+
+def test_jacobian_homogeneity_and_fd():
+    mesh, _, orc = make_setup(rings=16)
+    rng = np.random.default_rng(0)
+    g = 1.0 + 0.5 * rng.random(mesh.elements.shape[0])
+    V, J, _ = oracle.eit_forward(orc, g, tol=1e-13)
+    Vf = oracle.flatten_measurement(V, orc)
+    # linear parametrisation, one harmonic: V is homogeneous of degree -1 in sigma
+    assert np.abs(J @ g + Vf).max() / np.abs(Vf).max() < 1e-10
+    d = rng.standard_normal(g.size) * 1e-4
+    Vp, _, _ = oracle.eit_forward(orc, g + d, tol=1e-13, want_jacobian=False)
+    Vm, _, _ = oracle.eit_forward(orc, g - d, tol=1e-13, want_jacobian=False)
+    fd = (oracle.flatten_measurement(Vp, orc) - oracle.flatten_measurement(Vm, orc)) / 2
+    assert np.abs(fd - J @ d).max() / np.abs(fd).max() < 1e-6
+
+
+def test_exact_jacobian_matches_fd_in_2p5d():
+    mesh, _, orc = make_setup(rings=8, width=0.2, components=4, height=2.0)
+    rng = np.random.default_rng(1)
+    g = 1.0 + 0.3 * rng.random(mesh.elements.shape[0])
+    _, J, _ = oracle.eit_forward(orc, g, tol=1e-13, exact=True)
+    d = rng.standard_normal(g.size) * 1e-4
+    Vp, _, _ = oracle.eit_forward(orc, g + d, tol=1e-13, want_jacobian=False)
+    Vm, _, _ = oracle.eit_forward(orc, g - d, tol=1e-13, want_jacobian=False)
+    fd = (oracle.flatten_measurement(Vp, orc) - oracle.flatten_measurement(Vm, orc)) / 2
+    assert np.abs(fd - J @ d).max() / np.abs(fd).max() < 1e-6
+    # the reference's 2.5D Jacobian keeps only the stiffness term and is not the FD derivative
+    _, Jr, _ = oracle.eit_forward(orc, g, tol=1e-13, exact=False)
+    assert np.abs(fd - Jr @ d).max() / np.abs(fd).max() > 1e-2
+
+
+def test_inverse_primal_equals_dual():
+    mesh, _, orc = make_setup(rings=16)
+    g = inclusion_sigma(mesh, seed=4)
+    V, J, _ = oracle.eit_forward(orc, np.ones(mesh.elements.shape[0]), tol=1e-13)
+    Vt, _, _ = oracle.eit_forward(orc, g, tol=1e-13, want_jacobian=False)
+    y = oracle.flatten_measurement(Vt, orc) - oracle.flatten_measurement(V, orc)
+    dp = oracle.inverse_primal(J, y, 1.0, 1e-2)
+    dd = oracle.inverse_dual(J, y, 1.0, 1e-2)
+    assert np.abs(dp - dd).max() / np.abs(dd).max() < 1e-9
+
+
+def test_cholesky_reports_breakdown():
+    A = np.array([[1.0, 2.0], [2.0, 1.0]], order="F")
+    assert oracle.lib().orc_cholesky(2, oracle._p(A)) == 2
+
+
+@pytest.mark.parametrize("name", ["config1_small"])
+def test_golden_fixture(name):
+    """The oracle reproduces the committed fixture (regression pin)."""
+    path = os.path.join(GOLDEN, f"{name}.npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated")
+    z = np.load(path)
+    mesh, _, orc = make_setup(rings=int(z["rings"]), ports=int(z["ports"]))
+    V, J, _ = oracle.eit_forward(orc, z["sigma"], tol=1e-13)
+    assert np.abs(V - z["V"]).max() / np.abs(z["V"]).max() < 1e-10
+    Jp = J @ z["probes"]
+    assert np.abs(Jp - z["J_probe"]).max() / np.abs(z["J_probe"]).max() < 1e-9
+    assert np.array_equal(orc.layout.colIds, z["colIds"])
+    assert np.array_equal(orc.portEdges, z["portEdges"])

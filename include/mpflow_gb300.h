@@ -265,6 +265,21 @@ int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, 
 int mpf_gram_split_bf16(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda,
                         float* C, mpf_stream_t stream);
 
+/* mpf_gram_split_bf16 without any device allocation.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory after start-up
+ * (a real-time loop that must not stall on cudaMalloc's implicit device
+ * synchronisation, or a host framework whose allocator owns the device): the
+ * BF16 hi/lo copies, split-K partials and abort flag live in fixed device
+ * arrays inside the library (12 MB per GPU that loads it, kept until exit)
+ * instead of per-call buffers.  Same arguments and result as
+ * mpf_gram_split_bf16; limits batch*rows*lda <= 2,097,152 elements and a
+ * split-K workspace <= 1,048,576 floats, larger requests return MPF_EINVAL.
+ * All calls share the arrays: calls that overlap on the GPU race and corrupt
+ * each other's results.  The first call on a device resolves the arrays'
+ * addresses; make it before any stream capture.  Synchronises the stream. */
+int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda,
+                                float* C, mpf_stream_t stream);
+
 /* Batched FP64 Cholesky solve of (A + shift I) X = B, A n x n symmetric
  * (row-major == column-major), B n x nrhs column-major, per batch entry.
  * A is overwritten by its factor.  info[batch] (device ints) receives 0 or

@@ -250,6 +250,14 @@ int mpf_gram_split_bf16(int32_t batch, int32_t rows, int32_t cols, const float* 
     })
 }
 
+int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda, float* C,
+                                mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(A && C, MPF_EINVAL, "mpf_gram_split_bf16_noalloc: null argument");
+        return mpf::dense_gram_split_bf16_noalloc(batch, rows, cols, A, lda, C, (cudaStream_t)stream);
+    })
+}
+
 int mpf_cholesky_solve_f64(int32_t batch, int32_t n, double* A, double shift, double* B, int32_t nrhs,
                            int32_t* info, mpf_stream_t stream) {
     MPF_GUARD({

@@ -470,7 +470,8 @@ size_t dense_gram_work_floats(int batch, int rows, int cols) {
 }
 
 static int gram_run(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo, int ld,
-                    float* C, double* A64, double shift, float* work, size_t workFloats, cudaStream_t s) {
+                    float* C, double* A64, double shift, float* work, size_t workFloats, cudaStream_t s,
+                    int* flagOverride = nullptr) {
     MPF_CHECK(rows % kTile == 0 && cols % kBK == 0 && ld % 8 == 0 && ld >= cols, MPF_EINVAL,
               "gram: rows %% 128, cols %% 64 and ld %% 8 must be 0 (rows=%d cols=%d ld=%d)", rows, cols, ld);
     const int nt = rows / kTile, tiles = nt * (nt + 1) / 2, kblocks = cols / kBK;
@@ -479,7 +480,7 @@ static int gram_run(int batch, int rows, int cols, const __nv_bfloat16* hi, cons
     CUtensorMap mHi, mLo;
     MPF_TRY(make_map(&mHi, hi, batch * rows, ld));
     MPF_TRY(make_map(&mLo, lo, batch * rows, ld));
-    int* flag = abort_flag_device();
+    int* flag = flagOverride ? flagOverride : abort_flag_device();
     MPF_CHECK(flag != nullptr, MPF_ENOMEM, "gram: abort flag allocation failed");
     static bool attr = false;
     if (!attr) {
@@ -517,6 +518,90 @@ int dense_split_bf16(int batch, int rows, int cols, const float* A, int lda, __n
                      cudaStream_t s) {
     k_split_bf16<<<2048, 256, 0, s>>>(batch, rows, cols, A, lda, hi, lo);
     MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free Gram (mpf_gram_split_bf16_noalloc).
+//
+// Some callers of this library cannot allocate device memory once they are
+// running: applications that size all GPU memory at start-up (a real-time
+// reconstruction loop that must not stall on cudaMalloc's implicit device
+// synchronisation, or a host framework whose own allocator owns the whole
+// device and forbids allocations from libraries).  For them the split-BF16
+// Gram has a variant whose scratch memory -- the BF16 hi/lo copies of A, the
+// split-K partial sums and the pipeline abort flag -- lives in the fixed
+// file-scope arrays below instead of buffers allocated per call.
+//
+// Limits: batch * rows * lda <= kNoAllocElems (2,097,152 elements) and the
+// split-K workspace <= kNoAllocWork floats (1,048,576), i.e. 12 MB of device
+// memory that every GPU loading this library keeps until the process exits.
+// All calls share these arrays, which keep the contents of the last call:
+// each call rewrites the parts it reads (the abort flag is cleared at the
+// start of every call), and two calls that overlap on the GPU (different
+// streams, no ordering between them) race on the arrays and corrupt each
+// other's results.  The first call on a device resolves the arrays' device
+// addresses (cudaGetSymbolAddress); make that first call before any stream
+// capture on that device.
+namespace {
+constexpr size_t kNoAllocElems = size_t(1) << 21;
+constexpr size_t kNoAllocWork = size_t(1) << 20;
+static __device__ __align__(256) __nv_bfloat16 g_noallocHi[kNoAllocElems];
+static __device__ __align__(256) __nv_bfloat16 g_noallocLo[kNoAllocElems];
+static __device__ __align__(256) float g_noallocWork[kNoAllocWork];
+static __device__ __align__(256) int g_noallocFlag[64];
+
+struct NoAllocScratch {
+    __nv_bfloat16* hi = nullptr;
+    __nv_bfloat16* lo = nullptr;
+    float* work = nullptr;
+    int* flag = nullptr;
+    bool ready = false;
+};
+
+// Device addresses of the scratch arrays, resolved once per device with that
+// device current (the host-side names are stand-ins, not device addresses).
+int noalloc_scratch(NoAllocScratch* out) {
+    static std::mutex mu;
+    static NoAllocScratch perDevice[64];
+    int dev = 0;
+    MPF_CUDA(cudaGetDevice(&dev));
+    MPF_CHECK(dev >= 0 && dev < 64, MPF_EINVAL, "gram (no-alloc): device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(mu);
+    NoAllocScratch& s = perDevice[dev];
+    if (!s.ready) {
+        MPF_CUDA(cudaGetSymbolAddress((void**)&s.hi, g_noallocHi));
+        MPF_CUDA(cudaGetSymbolAddress((void**)&s.lo, g_noallocLo));
+        MPF_CUDA(cudaGetSymbolAddress((void**)&s.work, g_noallocWork));
+        MPF_CUDA(cudaGetSymbolAddress((void**)&s.flag, g_noallocFlag));
+        s.ready = true;
+    }
+    *out = s;
+    return MPF_OK;
+}
+}  // namespace
+
+int dense_gram_split_bf16_noalloc(int batch, int rows, int cols, const float* A, int lda, float* C, cudaStream_t s) {
+    MPF_CHECK(batch >= 1 && rows % kTile == 0 && cols % kBK == 0 && lda % 8 == 0 && lda >= cols, MPF_EINVAL,
+              "mpf_gram_split_bf16_noalloc: rows %% 128, cols %% 64 and lda %% 8 must be 0 (rows=%d cols=%d lda=%d)",
+              rows, cols, lda);
+    const size_t elems = (size_t)batch * rows * lda;
+    MPF_CHECK(elems <= kNoAllocElems, MPF_EINVAL,
+              "mpf_gram_split_bf16_noalloc: batch*rows*lda = %zu exceeds the fixed scratch of %zu elements", elems,
+              kNoAllocElems);
+    const size_t work = dense_gram_work_floats(batch, rows, cols);
+    MPF_CHECK(work <= kNoAllocWork, MPF_EINVAL,
+              "mpf_gram_split_bf16_noalloc: split-K workspace of %zu floats exceeds the fixed scratch of %zu floats",
+              work, kNoAllocWork);
+    NoAllocScratch sc;
+    MPF_TRY(noalloc_scratch(&sc));
+    MPF_CUDA(cudaMemsetAsync(sc.flag, 0, sizeof(int), s));
+    MPF_TRY(dense_split_bf16(batch, rows, cols, A, lda, sc.hi, sc.lo, s));
+    MPF_TRY(gram_run(batch, rows, cols, sc.hi, sc.lo, lda, C, nullptr, 0.0, sc.work, kNoAllocWork, s, sc.flag));
+    int aborted = 0;
+    MPF_CUDA(cudaMemcpyAsync(&aborted, sc.flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    MPF_CHECK(!aborted, MPF_ETIMEOUT, "mpf_gram_split_bf16_noalloc: a pipeline wait timed out");
     return MPF_OK;
 }
 

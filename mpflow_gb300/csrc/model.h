@@ -116,6 +116,7 @@ int dense_split_bf16(int batch, int rows, int cols, const float* A, int lda, __n
 int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo,
                          int ld, double shift, double* A64, float* work, size_t workFloats, cudaStream_t s);
 int dense_gram_check_abort(bool* aborted);
+int dense_gram_split_bf16_noalloc(int batch, int rows, int cols, const float* A, int lda, float* C, cudaStream_t s);
 int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s);
 int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s);
 int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s);

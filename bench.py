@@ -54,6 +54,8 @@ def parse_args():
     p.add_argument("--tol", type=float, default=1e-5, help="CG relative tolerance of the GN forward solves")
     p.add_argument("--cpu-threads", type=int, default=0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile-only", action="store_true",
+                   help="only time the CG kernels (all groups active) on --frames frames; for ncu captures")
     return p.parse_args()
 
 
@@ -282,6 +284,15 @@ def run_gb300(a):
                    device=local, exact_jacobian=True)
     F = a.frames
     nsteps = a.warmup + a.steps
+    if a.profile_only:
+        v = torch.tensor(synthetic_frames(cent, F, seed=7), device=dev)
+        ms, by = model.profile_cg(v, reps=max(a.steps, 1))
+        names = ["k_spmm_dot", "k_update", "k_direction"]
+        print(json.dumps({"profile_only": True, "frames": F, "groups": F * model.info["active_components"],
+                          "ms": dict(zip(names, ms.tolist())),
+                          "gbs": dict(zip(names, (by / ms / 1e6).tolist())),
+                          "algorithmic_bytes": dict(zip(names, by.tolist()))}), flush=True)
+        return
     # synthetic truth and measurements per step (untimed)
     truth = [synthetic_frames(cent, F, seed=1000 * (rank + 1) + s) for s in range(nsteps)]
     vmeas = []
@@ -303,17 +314,19 @@ def run_gb300(a):
     # ---- device-resident timing: V_meas already in HBM
     stream = torch.cuda.current_stream()
     frames_done, gn_updates, times_ms = 0, [], []
-    launches0 = None
+    launches = 0
     with ClockSampler(local) as clocks:
         for s in range(nsteps):
             g = torch.zeros((F, E), device=dev)
             barrier()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = mp.lib().mpf_kernel_launches()
             e0.record(stream)
             iters, res, st = model.gn_solve(g, vmeas[s], lam, target=a.target, max_iters=a.max_gn, options=opts)
             e1.record(stream)
             barrier()
             if s >= a.warmup:
+                launches += mp.lib().mpf_kernel_launches() - l0
                 times_ms.append(e0.elapsed_time(e1))
                 frames_done += int(st.frames_converged)
                 gn_updates.extend(iters.tolist())
@@ -383,6 +396,8 @@ def run_gb300(a):
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(vmeas[0].numel() * 4), "d2h_bytes_per_step": int(F * E * 4)},
         "clocks": clocks.summary(),
+        "gpu_launches": int(launches),
+        "cg_variants": model.cg_variants(F).tolist(),
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -252,6 +252,19 @@ int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int3
  * reference returns one summed count (src/models/eit.cpp:207-210). */
 int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, int32_t* count);
 
+/* CG kernel variants of the SpMM, update and direction kernels.  Variant
+ * v = 3 * i + k runs {4, 2, 1}[i] floats per lane and keeps {1, 2, 4}[k] row
+ * steps in flight per warp.  By default the first cold solve with a given
+ * frame count times every variant on the model's own systems and keeps the
+ * fastest (the reference's fixed launch shape is src/sparse/
+ * sparse_matrix.cpp:222-240).
+ *   set: host, 3 ints, each a variant or -1 (autotune), or NULL to leave as is
+ *   get: host, 3 ints receiving the variants a solve with `frames` frames
+ *        uses, or NULL
+ * Fails with MPF_EINVAL for a variant that the right-hand-side width does
+ * not allow.  No reference counterpart. */
+int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int32_t* get);
+
 /* ======================================================================== */
 /* Dense building blocks                                                     */
 /* ======================================================================== */

@@ -51,6 +51,7 @@ int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda,
              const mpf_solve_opts* o, int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s);
 int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
 int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
+int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
 
 }  // namespace mpf
 
@@ -225,6 +226,13 @@ int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, 
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_group_iterations: model == nullptr");
         return mpf::group_iterations(model, iterations, cap, count);
+    })
+}
+
+int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int32_t* get) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_cg_variants: model == nullptr");
+        return mpf::cg_variants(model, set, frames, get);
     })
 }
 

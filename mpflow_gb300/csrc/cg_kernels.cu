@@ -11,13 +11,17 @@
 //   k_spmm_dot   q = (S + alpha R) p,  pq = p.q
 //   k_update     x += a p, r -= a q, z = D^-1 r, rz' = r.z  (+ convergence)
 //   k_direction  p = D^-1 r + b p
-// The SpMM fuses S + alpha R (the system matrix is never materialised), reads
-// ELL columns/values once per row (warp-uniform broadcast) and gathers the KP
-// right-hand sides of a neighbour node as one contiguous 128-bit-aligned
-// segment.  Inner products: each thread sums at most 16 products with an
-// error-free (TwoProduct/TwoSum) float pair, everything above that level is
-// FP64; the per-block partials are combined by the last block of the group in
-// a fixed order, so results are deterministic.
+// Memory access: a lane moves VEC consecutive floats, so KP/VEC lanes cover
+// one node's right-hand sides and one warp instruction serves 32*VEC/KP
+// rows; each warp keeps RB row steps in flight.  VEC and RB are template
+// parameters chosen per model by the autotuner in model.cu (CUDA-event
+// timings of every variant on the model's own systems).  An ELL slot is one
+// packed float4 {S, R, column, 0} read as a broadcast; the SpMM fuses
+// S + alpha R (the system matrix is never materialised) and unrolls up to
+// kWFast slots.  Inner products: each thread sums at most 16 products with
+// an error-free (TwoProduct/TwoSum) float pair, everything above that level
+// is FP64; the per-block partials are combined by the last block of the group
+// in a fixed order, so results are deterministic.
 #include "model.h"
 
 namespace mpf {
@@ -26,13 +30,15 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kRowsPerWarp = kRowTile / kWarps;  // 16
+constexpr int kWFast = 8;                         // ELL slots unrolled at compile time
 
-template <int KP>
+template <int KP, int VEC_>
 struct Shape {
-    static constexpr int LPR = KP >= 32 ? 32 : KP;  // lanes per row
-    static constexpr int VEC = KP / LPR;            // floats per lane
-    static constexpr int SUB = 32 / LPR;            // rows per warp step
-    static constexpr int STEPS = kRowsPerWarp / SUB;
+    static constexpr int VEC = VEC_;                 // floats per lane
+    static constexpr int LPR = KP / VEC;             // lanes per row
+    static constexpr int SUB = 32 / LPR;             // rows per warp instruction
+    static constexpr int STEPS = kRowsPerWarp / SUB; // warp steps per 16 rows
+    static_assert(LPR >= 1 && LPR <= 32 && 32 % LPR == 0, "invalid lane mapping");
 };
 
 template <int V>
@@ -40,10 +46,10 @@ __device__ __forceinline__ void ldv(const float* p, float (&v)[V]) {
     if constexpr (V == 1) {
         v[0] = *p;
     } else if constexpr (V == 2) {
-        float2 t = *reinterpret_cast<const float2*>(p);
+        const float2 t = *reinterpret_cast<const float2*>(p);
         v[0] = t.x; v[1] = t.y;
     } else {
-        float4 t = *reinterpret_cast<const float4*>(p);
+        const float4 t = *reinterpret_cast<const float4*>(p);
         v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
     }
 }
@@ -74,29 +80,29 @@ struct DotAcc {
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
-__device__ __forceinline__ float diag_inv(const float* S, const float* R, const int32_t* diagSlot,
-                                          int npad, int row, float alpha) {
-    int ds = __ldg(&diagSlot[row]);
-    float d = __ldg(&S[(size_t)ds * npad + row]) + alpha * __ldg(&R[(size_t)ds * npad + row]);
+__device__ __forceinline__ float diag_inv(const float4* SR, const int32_t* diagSlot, int npad, int row,
+                                          float alpha) {
+    const int ds = __ldg(&diagSlot[row]);
+    const float4 e = __ldg(&SR[(size_t)ds * npad + row]);
+    const float d = e.x + alpha * e.y;
     return d != 0.f ? 1.f / d : 0.f;
 }
 
 // Block-level reduction of per-thread partials into part[g][blk][KP]; returns
 // true in every thread of the block that finishes the group last (that block
 // then sees all partials of the group).
-template <int KP, int NDOT>
-__device__ __forceinline__ bool block_partials(const DotAcc (&acc)[NDOT][Shape<KP>::VEC],
-                                               double* const (&part)[NDOT], int g, int nblk,
-                                               unsigned* counter) {
-    using Sh = Shape<KP>;
+template <int KP, int VEC, int NDOT>
+__device__ __forceinline__ bool block_partials(const DotAcc (&acc)[NDOT][VEC], double* const (&part)[NDOT], int g,
+                                               int nblk, unsigned* counter) {
+    using Sh = Shape<KP, VEC>;
     __shared__ double red[NDOT][kWarps * Sh::SUB][KP];
     __shared__ bool amLast;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
 #pragma unroll
     for (int d = 0; d < NDOT; ++d)
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) red[d][warp * Sh::SUB + sub][j0 + v] = acc[d][v].value();
+        for (int v = 0; v < VEC; ++v) red[d][warp * Sh::SUB + sub][j0 + v] = acc[d][v].value();
     __syncthreads();
     if (threadIdx.x < KP) {
 #pragma unroll
@@ -122,6 +128,43 @@ __device__ __forceinline__ double sum_partials(const double* part, int g, int nb
     return s;
 }
 
+// y[i] = (S + alpha R) x over the rows row[i] (kWFast slots unrolled, rest looped)
+template <int KP, int VEC, int RB>
+__device__ __forceinline__ void spmm_rows(const float4* SR, int W, int npad, float alpha, const float* x, int j0,
+                                          const int (&row)[RB], float (&y)[RB][VEC]) {
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) y[i][v] = 0.f;
+#pragma unroll
+    for (int k = 0; k < kWFast; ++k) {
+        if (k < W) {
+            float4 e[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i) e[i] = __ldg(&SR[(size_t)k * npad + row[i]]);
+#pragma unroll
+            for (int i = 0; i < RB; ++i) {
+                float xv[VEC];
+                ldv<VEC>(x + (size_t)__float_as_int(e[i].z) * KP + j0, xv);
+                const float a = e[i].x + alpha * e[i].y;
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(a, xv[v], y[i][v]);
+            }
+        }
+    }
+    for (int k = kWFast; k < W; ++k) {
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+            const float4 e = __ldg(&SR[(size_t)k * npad + row[i]]);
+            float xv[VEC];
+            ldv<VEC>(x + (size_t)__float_as_int(e.z) * KP + j0, xv);
+            const float a = e.x + alpha * e.y;
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(a, xv[v], y[i][v]);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Neumann (dcFree) harmonics: the reference regularises the singular
 // stiffness matrix as (A + 1 1^T) x = b (src/numeric/conjugate_gradient.cpp:
@@ -132,65 +175,63 @@ __device__ __forceinline__ double sum_partials(const double* part, int g, int nb
 // and k_dc_shift adds the exact constant difference afterwards.  The
 // rank-one term needs sum(p), which k_direction reduces for the next SpMM.
 
-// r = b - A x - sum(x) (or r = b), z = D^-1 r, p = z, rz = r.z, bz = b.D^-1 b, sum(p)
+// r = b - A x - c' sum(x) (or r = b), z = D^-1 r, p = z, rz = r.z, bz = b.D^-1 b, sum(p)
 template <int KP>
 __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
-    using Sh = Shape<KP>;
+    constexpr int VEC = KP >= 32 ? 4 : 2;
+    using Sh = Shape<KP, VEC>;
+    constexpr int RB = Sh::STEPS < 2 ? Sh::STEPS : 2;
     const int g = blockIdx.y;
     const int f = g / P.Ca, ci = g % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
-    const float* S = P.S + (size_t)f * P.W * P.npad;
-    const float* R = P.R + (size_t)f * P.W * P.npad;
+    const float4* SR = P.SR + (size_t)f * P.W * P.npad;
     const size_t vb = (size_t)g * P.npad * KP;
     const float* b = P.b + (P.bPerGroup ? vb : (size_t)ci * P.npad * KP);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
-    float sx[Sh::VEC] = {};
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    float sx[VEC] = {};
     if (dc && !zeroGuess && P.sumX0) {
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) sx[v] = (float)((double)P.dcScale * P.sumX0[(size_t)g * KP + j0 + v]);
+        for (int v = 0; v < VEC; ++v) sx[v] = (float)((double)P.dcScale * P.sumX0[(size_t)g * KP + j0 + v]);
     }
-    DotAcc acc[3][Sh::VEC];
+    DotAcc acc[3][VEC];
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
-    for (int st = 0; st < Sh::STEPS; ++st) {
-        const int row = rowBase + st * Sh::SUB + sub;
-        const bool real = row < P.n;
-        float bv[Sh::VEC], rv[Sh::VEC];
-        ldv<Sh::VEC>(b + (size_t)row * KP + j0, bv);
+    for (int st = 0; st < Sh::STEPS; st += RB) {
+        int row[RB];
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) rv[v] = bv[v];
+        for (int i = 0; i < RB; ++i) row[i] = rowBase + (st + i) * Sh::SUB + sub;
+        float y[RB][VEC];
         if (!zeroGuess) {
-            const float* x = P.x + vb;
-            float y[Sh::VEC] = {};
-            for (int k = 0; k < P.W; ++k) {
-                const int col = __ldg(&P.cols[(size_t)k * P.npad + row]);
-                const float a = __ldg(&S[(size_t)k * P.npad + row]) + alpha * __ldg(&R[(size_t)k * P.npad + row]);
-                float xv[Sh::VEC];
-                ldv<Sh::VEC>(x + (size_t)col * KP + j0, xv);
-#pragma unroll
-                for (int v = 0; v < Sh::VEC; ++v) y[v] = fmaf(a, xv[v], y[v]);
-            }
-#pragma unroll
-            for (int v = 0; v < Sh::VEC; ++v) rv[v] = bv[v] - y[v] - (real ? sx[v] : 0.f);
+            spmm_rows<KP, VEC, RB>(SR, P.W, P.npad, alpha, P.x + vb, j0, row, y);
         } else {
-            float zv[Sh::VEC] = {};
-            stv<Sh::VEC>(P.x + vb + (size_t)row * KP + j0, zv);
-        }
-        const float di = diag_inv(S, R, P.diagSlot, P.npad, row, alpha);
-        float zv[Sh::VEC];
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) {
-            zv[v] = di * rv[v];
-            acc[0][v].add(rv[v], zv[v]);
-            acc[1][v].add(bv[v], di * bv[v]);
-            if (dc && real) acc[2][v].add(zv[v], 1.f);
+            for (int i = 0; i < RB; ++i) {
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) y[i][v] = 0.f;
+                stv<VEC>(P.x + vb + (size_t)row[i] * KP + j0, y[i]);
+            }
         }
-        stv<Sh::VEC>(P.r + vb + (size_t)row * KP + j0, rv);
-        stv<Sh::VEC>(P.p + vb + (size_t)row * KP + j0, zv);
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+            const bool real = row[i] < P.n;
+            float bv[VEC], rv[VEC], zv[VEC];
+            ldv<VEC>(b + (size_t)row[i] * KP + j0, bv);
+            const float di = diag_inv(SR, P.diagSlot, P.npad, row[i], alpha);
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                rv[v] = zeroGuess ? bv[v] : bv[v] - y[i][v] - (real ? sx[v] : 0.f);
+                zv[v] = di * rv[v];
+                acc[0][v].add(rv[v], zv[v]);
+                acc[1][v].add(bv[v], di * bv[v]);
+                if (dc && real) acc[2][v].add(zv[v], 1.f);
+            }
+            stv<VEC>(P.r + vb + (size_t)row[i] * KP + j0, rv);
+            stv<VEC>(P.p + vb + (size_t)row[i] * KP + j0, zv);
+        }
     }
     double* const parts[3] = {P.partA, P.partB, P.partC};
-    if (block_partials<KP, 3>(acc, parts, g, P.nblk, P.counter)) {
+    if (block_partials<KP, VEC, 3>(acc, parts, g, P.nblk, P.counter)) {
         int notConv = 0;
         if (threadIdx.x < KP) {
             const int j = threadIdx.x;
@@ -213,52 +254,49 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
     }
 }
 
-// q = (S + alpha R) p (+ sum(p) on Neumann harmonics), pq = p.q
-template <int KP>
+// q = (S + alpha R) p (+ c' sum(p) on Neumann harmonics), pq = p.q
+template <int KP, int VEC, int RB>
 __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
-    using Sh = Shape<KP>;
+    using Sh = Shape<KP, VEC>;
     const int g = blockIdx.y;
     if (!P.active[g]) return;
     const int f = g / P.Ca, ci = g % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
-    const float* S = P.S + (size_t)f * P.W * P.npad;
-    const float* R = P.R + (size_t)f * P.W * P.npad;
+    const float4* SR = P.SR + (size_t)f * P.W * P.npad;
     const size_t vb = (size_t)g * P.npad * KP;
     const float* p = P.p + vb;
     float* q = P.q + vb;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
-    float sp[Sh::VEC] = {};
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    float sp[VEC] = {};
     if (dc) {
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) sp[v] = (float)((double)P.dcScale * P.sumP[(size_t)g * KP + j0 + v]);
+        for (int v = 0; v < VEC; ++v) sp[v] = (float)((double)P.dcScale * P.sumP[(size_t)g * KP + j0 + v]);
     }
-    DotAcc acc[1][Sh::VEC];
+    DotAcc acc[1][VEC];
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
-    for (int st = 0; st < Sh::STEPS; ++st) {
-        const int row = rowBase + st * Sh::SUB + sub;
-        float y[Sh::VEC] = {};
-        for (int k = 0; k < P.W; ++k) {
-            const int col = __ldg(&P.cols[(size_t)k * P.npad + row]);
-            const float a = __ldg(&S[(size_t)k * P.npad + row]) + alpha * __ldg(&R[(size_t)k * P.npad + row]);
-            float xv[Sh::VEC];
-            ldv<Sh::VEC>(p + (size_t)col * KP + j0, xv);
+    for (int st = 0; st < Sh::STEPS; st += RB) {
+        int row[RB];
 #pragma unroll
-            for (int v = 0; v < Sh::VEC; ++v) y[v] = fmaf(a, xv[v], y[v]);
+        for (int i = 0; i < RB; ++i) row[i] = rowBase + (st + i) * Sh::SUB + sub;
+        float y[RB][VEC];
+        spmm_rows<KP, VEC, RB>(SR, P.W, P.npad, alpha, p, j0, row, y);
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+            if (row[i] < P.n) {
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) y[i][v] += sp[v];
+            }
+            stv<VEC>(q + (size_t)row[i] * KP + j0, y[i]);
+            float pv[VEC];
+            ldv<VEC>(p + (size_t)row[i] * KP + j0, pv);
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) acc[0][v].add(pv[v], y[i][v]);
         }
-        if (row < P.n) {
-#pragma unroll
-            for (int v = 0; v < Sh::VEC; ++v) y[v] += sp[v];
-        }
-        stv<Sh::VEC>(q + (size_t)row * KP + j0, y);
-        float pv[Sh::VEC];
-        ldv<Sh::VEC>(p + (size_t)row * KP + j0, pv);
-#pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) acc[0][v].add(pv[v], y[v]);
     }
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, 1>(acc, parts, g, P.nblk, P.counter)) {
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.nblk, P.counter)) {
         if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, P.nblk, KP, threadIdx.x);
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
@@ -266,47 +304,53 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
 
 // x += a p, r -= a q, z = D^-1 r, rz' = r.z; the last block updates the
 // scalars, the convergence mask and the group's active flag.
-template <int KP>
+template <int KP, int VEC, int RB>
 __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
-    using Sh = Shape<KP>;
+    using Sh = Shape<KP, VEC>;
     const int g = blockIdx.y;
     if (!P.active[g]) return;
     const int f = g / P.Ca, ci = g % P.Ca;
     const float alpha = P.alpha[ci];
-    const float* S = P.S + (size_t)f * P.W * P.npad;
-    const float* R = P.R + (size_t)f * P.W * P.npad;
+    const float4* SR = P.SR + (size_t)f * P.W * P.npad;
     const size_t vb = (size_t)g * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
-    float a[Sh::VEC];
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    float a[VEC];
 #pragma unroll
-    for (int v = 0; v < Sh::VEC; ++v) {
+    for (int v = 0; v < VEC; ++v) {
         const size_t s = (size_t)g * KP + j0 + v;
         const double pq = P.pq[s];
         a[v] = (!P.conv[s] && pq != 0.0) ? (float)(P.rz[s] / pq) : 0.f;
     }
-    DotAcc acc[1][Sh::VEC];
+    DotAcc acc[1][VEC];
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
-    for (int st = 0; st < Sh::STEPS; ++st) {
-        const int row = rowBase + st * Sh::SUB + sub;
-        const size_t o = vb + (size_t)row * KP + j0;
-        float xv[Sh::VEC], rv[Sh::VEC], pv[Sh::VEC], qv[Sh::VEC];
-        ldv<Sh::VEC>(P.x + o, xv);
-        ldv<Sh::VEC>(P.r + o, rv);
-        ldv<Sh::VEC>(P.p + o, pv);
-        ldv<Sh::VEC>(P.q + o, qv);
-        const float di = diag_inv(S, R, P.diagSlot, P.npad, row, alpha);
+    for (int st = 0; st < Sh::STEPS; st += RB) {
+        float xv[RB][VEC], rv[RB][VEC], pv[RB][VEC], qv[RB][VEC], di[RB];
+        size_t o[RB];
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) {
-            xv[v] = fmaf(a[v], pv[v], xv[v]);
-            rv[v] = fmaf(-a[v], qv[v], rv[v]);
-            acc[0][v].add(rv[v], di * rv[v]);
+        for (int i = 0; i < RB; ++i) {
+            const int row = rowBase + (st + i) * Sh::SUB + sub;
+            o[i] = vb + (size_t)row * KP + j0;
+            ldv<VEC>(P.x + o[i], xv[i]);
+            ldv<VEC>(P.r + o[i], rv[i]);
+            ldv<VEC>(P.p + o[i], pv[i]);
+            ldv<VEC>(P.q + o[i], qv[i]);
+            di[i] = diag_inv(SR, P.diagSlot, P.npad, row, alpha);
         }
-        stv<Sh::VEC>(P.x + o, xv);
-        stv<Sh::VEC>(P.r + o, rv);
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                xv[i][v] = fmaf(a[v], pv[i][v], xv[i][v]);
+                rv[i][v] = fmaf(-a[v], qv[i][v], rv[i][v]);
+                acc[0][v].add(rv[i][v], di[i] * rv[i][v]);
+            }
+            stv<VEC>(P.x + o[i], xv[i]);
+            stv<VEC>(P.r + o[i], rv[i]);
+        }
     }
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, 1>(acc, parts, g, P.nblk, P.counter)) {
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.nblk, P.counter)) {
         int notConv = 0;
         if (threadIdx.x < KP) {
             const size_t s = (size_t)g * KP + threadIdx.x;
@@ -331,61 +375,68 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
 
 // p = D^-1 r + beta p on the right-hand sides still iterating; Neumann
 // harmonics also reduce sum(p) for the next SpMM.
-template <int KP>
+template <int KP, int VEC, int RB>
 __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
-    using Sh = Shape<KP>;
+    using Sh = Shape<KP, VEC>;
     const int g = blockIdx.y;
     if (!P.active[g]) return;
     const int f = g / P.Ca, ci = g % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
-    const float* S = P.S + (size_t)f * P.W * P.npad;
-    const float* R = P.R + (size_t)f * P.W * P.npad;
+    const float4* SR = P.SR + (size_t)f * P.W * P.npad;
     const size_t vb = (size_t)g * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
-    float be[Sh::VEC];
-    bool live[Sh::VEC];
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    float be[VEC];
+    bool live[VEC];
 #pragma unroll
-    for (int v = 0; v < Sh::VEC; ++v) {
+    for (int v = 0; v < VEC; ++v) {
         const size_t s = (size_t)g * KP + j0 + v;
         live[v] = !P.conv[s];
         be[v] = (float)P.beta[s];
     }
-    DotAcc acc[1][Sh::VEC];
+    DotAcc acc[1][VEC];
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
-    for (int st = 0; st < Sh::STEPS; ++st) {
-        const int row = rowBase + st * Sh::SUB + sub;
-        const size_t o = vb + (size_t)row * KP + j0;
-        float rv[Sh::VEC], pv[Sh::VEC];
-        ldv<Sh::VEC>(P.r + o, rv);
-        ldv<Sh::VEC>(P.p + o, pv);
-        const float di = diag_inv(S, R, P.diagSlot, P.npad, row, alpha);
+    for (int st = 0; st < Sh::STEPS; st += RB) {
+        float rv[RB][VEC], pv[RB][VEC], di[RB];
+        int row[RB];
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) {
-            pv[v] = live[v] ? fmaf(be[v], pv[v], di * rv[v]) : pv[v];
-            if (dc && row < P.n) acc[0][v].add(pv[v], 1.f);
+        for (int i = 0; i < RB; ++i) {
+            row[i] = rowBase + (st + i) * Sh::SUB + sub;
+            const size_t o = vb + (size_t)row[i] * KP + j0;
+            ldv<VEC>(P.r + o, rv[i]);
+            ldv<VEC>(P.p + o, pv[i]);
+            di[i] = diag_inv(SR, P.diagSlot, P.npad, row[i], alpha);
         }
-        stv<Sh::VEC>(P.p + o, pv);
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                pv[i][v] = live[v] ? fmaf(be[v], pv[i][v], di[i] * rv[i][v]) : pv[i][v];
+                if (dc && row[i] < P.n) acc[0][v].add(pv[i][v], 1.f);
+            }
+            stv<VEC>(P.p + vb + (size_t)row[i] * KP + j0, pv[i]);
+        }
     }
     if (!dc) return;
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, 1>(acc, parts, g, P.nblk, P.counter)) {
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.nblk, P.counter)) {
         if (threadIdx.x < KP) P.sumP[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, P.nblk, KP, threadIdx.x);
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
 }
 
 // ---------------------------------------------------------------------------
-// FP64 refinement: r64 = b64 - (S64 + alpha R64) x64 (- sum(x64) on Neumann
-// harmonics), written as the float right-hand side of the next inner solve;
-// rr = |r64|^2, bb = |b64|^2.
+// FP64 refinement: r64 = b64 - (S64 + alpha R64) x64 (- c' sum(x64) on
+// Neumann harmonics), written as the float right-hand side of the next inner
+// solve; rr = |r64|^2, bb = |b64|^2.
 template <int KP>
 __global__ void __launch_bounds__(kThreads) k_residual64(CgProblem P, const double* S64, const double* R64,
                                                          const double* x64, const double* b64,
                                                          const double* sumX64, float* rOut, double* partR,
                                                          double* partB, double* rr, double* bb) {
-    using Sh = Shape<KP>;
+    constexpr int VEC = KP >= 32 ? 4 : 2;
+    using Sh = Shape<KP, VEC>;
     const int g = blockIdx.y;
     const int f = g / P.Ca, ci = g % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
@@ -395,38 +446,38 @@ __global__ void __launch_bounds__(kThreads) k_residual64(CgProblem P, const doub
     const size_t vb = (size_t)g * P.npad * KP;
     b64 += (size_t)ci * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * Sh::VEC;
-    double sx[Sh::VEC] = {};
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    double sx[VEC] = {};
     if (dc) {
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) sx[v] = (double)P.dcScale * sumX64[(size_t)g * KP + j0 + v];
+        for (int v = 0; v < VEC; ++v) sx[v] = (double)P.dcScale * sumX64[(size_t)g * KP + j0 + v];
     }
-    double accR[Sh::VEC] = {}, accB[Sh::VEC] = {};
+    double accR[VEC] = {}, accB[VEC] = {};
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
     for (int st = 0; st < Sh::STEPS; ++st) {
         const int row = rowBase + st * Sh::SUB + sub;
-        double y[Sh::VEC] = {};
+        double y[VEC] = {};
         for (int k = 0; k < P.W; ++k) {
             const int col = __ldg(&P.cols[(size_t)k * P.npad + row]);
             const double a = S[(size_t)k * P.npad + row] + alpha * R[(size_t)k * P.npad + row];
 #pragma unroll
-            for (int v = 0; v < Sh::VEC; ++v) y[v] = fma(a, x64[vb + (size_t)col * KP + j0 + v], y[v]);
+            for (int v = 0; v < VEC; ++v) y[v] = fma(a, x64[vb + (size_t)col * KP + j0 + v], y[v]);
         }
-        float ro[Sh::VEC];
+        float ro[VEC];
 #pragma unroll
-        for (int v = 0; v < Sh::VEC; ++v) {
+        for (int v = 0; v < VEC; ++v) {
             const double bv = b64[(size_t)row * KP + j0 + v];
             const double rv = bv - y[v] - (row < P.n ? sx[v] : 0.0);
             ro[v] = (float)rv;
             accR[v] = fma(rv, rv, accR[v]);
             accB[v] = fma(bv, bv, accB[v]);
         }
-        stv<Sh::VEC>(rOut + vb + (size_t)row * KP + j0, ro);
+        stv<VEC>(rOut + vb + (size_t)row * KP + j0, ro);
     }
     __shared__ double red[2][kWarps * Sh::SUB][KP];
     __shared__ bool amLast;
 #pragma unroll
-    for (int v = 0; v < Sh::VEC; ++v) {
+    for (int v = 0; v < VEC; ++v) {
         red[0][warp * Sh::SUB + sub][j0 + v] = accR[v];
         red[1][warp * Sh::SUB + sub][j0 + v] = accB[v];
     }
@@ -499,6 +550,59 @@ __global__ void __launch_bounds__(kThreads) k_colsum(int n, int npad, int KP, in
     }
 }
 
+// ---------------------------------------------------------------------------
+// Variant table: variant v = vecIdx * 3 + rbIdx with VEC in {4, 2, 1} and
+// RB in {1, 2, 4}; entries whose lane mapping or step count does not fit the
+// right-hand-side width are null.
+using CgKernel = void (*)(CgProblem);
+
+template <int KP, int VEC, int RB>
+constexpr bool valid_variant() {
+    return KP / VEC <= 32 && (kRowsPerWarp / (32 / (KP / VEC))) % RB == 0 && (kRowsPerWarp / (32 / (KP / VEC))) >= RB;
+}
+
+template <int KP, int VEC, int RB>
+void fill_variant(CgKernel (&t)[3][kCgVariants], int v) {
+    if constexpr (KP / VEC <= 32) {
+        if constexpr (valid_variant<KP, VEC, RB>()) {
+            t[0][v] = k_spmm_dot<KP, VEC, RB>;
+            t[1][v] = k_update<KP, VEC, RB>;
+            t[2][v] = k_direction<KP, VEC, RB>;
+        }
+    }
+}
+
+template <int KP>
+struct VariantTable {
+    CgKernel k[3][kCgVariants] = {};
+    VariantTable() {
+        fill_variant<KP, 4, 1>(k, 0);
+        fill_variant<KP, 4, 2>(k, 1);
+        fill_variant<KP, 4, 4>(k, 2);
+        fill_variant<KP, 2, 1>(k, 3);
+        fill_variant<KP, 2, 2>(k, 4);
+        fill_variant<KP, 2, 4>(k, 5);
+        fill_variant<KP, 1, 1>(k, 6);
+        fill_variant<KP, 1, 2>(k, 7);
+        fill_variant<KP, 1, 4>(k, 8);
+    }
+};
+
+CgKernel variant_kernel(int KP, int which, int v) {
+    static const VariantTable<16> t16;
+    static const VariantTable<32> t32;
+    static const VariantTable<64> t64;
+    static const VariantTable<128> t128;
+    if (v < 0 || v >= kCgVariants || which < 0 || which > 2) return nullptr;
+    switch (KP) {
+        case 16: return t16.k[which][v];
+        case 32: return t32.k[which][v];
+        case 64: return t64.k[which][v];
+        case 128: return t128.k[which][v];
+        default: return nullptr;
+    }
+}
+
 template <template <int> class Launcher, class... Args>
 int dispatch_kp(int KP, Args&&... args) {
     switch (KP) {
@@ -519,29 +623,6 @@ struct InitL {
     }
 };
 template <int KP>
-struct IterL {
-    static int run(const CgProblem& P, cudaStream_t s) {
-        dim3 grid(P.nblk, P.G);
-        k_spmm_dot<KP><<<grid, kThreads, 0, s>>>(P);
-        k_update<KP><<<grid, kThreads, 0, s>>>(P);
-        k_direction<KP><<<grid, kThreads, 0, s>>>(P);
-        // recorded into a CUDA graph; its launches are counted per replay
-        MPF_CUDA(cudaGetLastError());
-        return MPF_OK;
-    }
-};
-template <int KP>
-struct OneL {
-    static int run(const CgProblem& P, int which, cudaStream_t s) {
-        dim3 grid(P.nblk, P.G);
-        if (which == 0) k_spmm_dot<KP><<<grid, kThreads, 0, s>>>(P);
-        else if (which == 1) k_update<KP><<<grid, kThreads, 0, s>>>(P);
-        else k_direction<KP><<<grid, kThreads, 0, s>>>(P);
-        MPF_LAUNCHED(1);
-        return MPF_OK;
-    }
-};
-template <int KP>
 struct Res64L {
     static int run(const CgProblem& P, const double* S64, const double* R64, const double* x64,
                    const double* b64, const double* sumX64, double* partR, double* partB, double* rr,
@@ -555,13 +636,36 @@ struct Res64L {
 
 }  // namespace
 
+bool cg_variant_valid(int KP, int which, int v) { return variant_kernel(KP, which, v) != nullptr; }
+
+int cg_default_variant(int KP) { return KP <= 64 ? 1 : 0; }  // VEC 4, RB 2 (KP 128: RB 1)
+
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s) {
     return dispatch_kp<InitL>(P.KP, P, zeroGuess, s);
 }
 
-int cg_launch_iteration(const CgProblem& P, cudaStream_t s) { return dispatch_kp<IterL>(P.KP, P, s); }
+// One CG iteration with the problem's chosen variants; `count` says whether
+// the launches are real (false while recording a CUDA graph, whose replays
+// are counted by the caller).
+static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count) {
+    const int v = which == 0 ? P.variantSpmm : which == 1 ? P.variantUpdate : P.variantDirection;
+    CgKernel k = variant_kernel(P.KP, which, v);
+    MPF_CHECK(k != nullptr, MPF_EINVAL, "CG kernel variant %d not available for %d right-hand sides", v, P.KP);
+    k<<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P);
+    if (count) {
+        MPF_LAUNCHED(1);
+    } else {
+        MPF_CUDA(cudaGetLastError());
+    }
+    return MPF_OK;
+}
 
-int cg_launch_kernel(const CgProblem& P, int which, cudaStream_t s) { return dispatch_kp<OneL>(P.KP, P, which, s); }
+int cg_launch_iteration(const CgProblem& P, cudaStream_t s) {
+    for (int which = 0; which < 3; ++which) MPF_TRY(launch_one(P, which, s, false));
+    return MPF_OK;
+}
+
+int cg_launch_kernel(const CgProblem& P, int which, cudaStream_t s) { return launch_one(P, which, s, true); }
 
 int cg_launch_residual64(const CgProblem& P, const double* S64, const double* R64, const double* x64,
                          const double* b64, const double* sumX64, double* partR, double* partB, double* rr,

@@ -26,7 +26,7 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
                            const int32_t* __restrict__ contrib, const float* __restrict__ Kf,
                            const float* __restrict__ Mf, const double* __restrict__ Kd,
                            const double* __restrict__ Md, const float* __restrict__ gamma, float ref,
-                           int logarithmic, float* __restrict__ S, float* __restrict__ R,
+                           int logarithmic, const int32_t* __restrict__ cols, float4* __restrict__ SR,
                            double* __restrict__ S64, double* __restrict__ R64) {
     const int f = blockIdx.y;
     const size_t slots = (size_t)W * npad;
@@ -47,8 +47,7 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
                 dr = fma(Md[code], pg64, dr);
             }
         }
-        S[(size_t)f * slots + s] = vs;
-        R[(size_t)f * slots + s] = vr;
+        SR[(size_t)f * slots + s] = make_float4(vs, vr, __int_as_float(__ldg(&cols[s])), 0.f);
         if (S64) {
             S64[(size_t)f * slots + s] = ds;
             R64[(size_t)f * slots + s] = dr;
@@ -57,14 +56,17 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
 }
 
 // slot-major [W][npad] -> reference ELL [dataRows][32] (same slot order)
-__global__ void k_export_ell(int W, int npad, int n, int dataRows, const float* __restrict__ src,
+__global__ void k_export_ell(int W, int npad, int n, int dataRows, const float4* __restrict__ src, int component,
                              float* __restrict__ dst) {
     const int f = blockIdx.y;
     const size_t total = (size_t)dataRows * kEllWidth;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int row = (int)(i / kEllWidth), slot = (int)(i % kEllWidth);
         float v = 0.f;
-        if (row < n && slot < W) v = src[(size_t)f * W * npad + (size_t)slot * npad + row];
+        if (row < n && slot < W) {
+            const float4 e = src[(size_t)f * W * npad + (size_t)slot * npad + row];
+            v = component == 0 ? e.x : e.y;
+        }
         dst[(size_t)f * total + i] = v;
     }
 }
@@ -302,20 +304,20 @@ __global__ void k_update_gamma(int rowsJ, int Epad, int E, const float* __restri
 
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
                         const float* Kf, const float* Mf, const double* Kd, const double* Md,
-                        const float* gamma, float ref, int logarithmic, float* S, float* R,
+                        const float* gamma, float ref, int logarithmic, const int32_t* cols, float4* SR,
                         double* S64, double* R64, cudaStream_t s) {
     const size_t slots = (size_t)W * npad;
     int blocks = (int)std::min<size_t>((slots + 255) / 256, 4096);
     k_assemble<<<dim3(blocks, F), 256, 0, s>>>(W, npad, E, cptr, contrib, Kf, Mf, Kd, Md, gamma, ref,
-                                               logarithmic, S, R, S64, R64);
+                                               logarithmic, cols, SR, S64, R64);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
-int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float* slotMajor,
+int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float4* SR, int component,
                           float* refLayout, cudaStream_t s) {
     int blocks = (int)std::min<size_t>(((size_t)dataRows * kEllWidth + 255) / 256, 4096);
-    k_export_ell<<<dim3(blocks, F), 256, 0, s>>>(W, npad, n, dataRows, slotMajor, refLayout);
+    k_export_ell<<<dim3(blocks, F), 256, 0, s>>>(W, npad, n, dataRows, SR, component, refLayout);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

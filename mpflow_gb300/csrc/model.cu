@@ -2,6 +2,7 @@
 // orchestration of the forward solve (EIT::solve, src/models/eit.cpp:139-213)
 // and of one regularised Gauss-Newton step (Solver::solveAbsolute,
 // src/solver/solver.cpp:196-225 with Inverse, src/solver/inverse.cpp:60-238).
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -41,7 +42,8 @@ struct mpf_eit {
     mpf::DevBuf<double> dcShift;      // [KP] constant difference to the reference's solution
     // workspace, grown on demand
     int capF = 0, capF64 = 0, capFJ = 0;
-    mpf::DevBuf<float> S, R, X, Rv, Pv, Qv;
+    mpf::DevBuf<float4> SR;           // packed slot values {S, R, column, 0} per frame
+    mpf::DevBuf<float> X, Rv, Pv, Qv;
     mpf::DevBuf<double> S64, R64, X64;
     mpf::DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, rr, bb, Gm, sumP, sumX;
     mpf::DevBuf<int> conv, active, iters;
@@ -57,6 +59,10 @@ struct mpf_eit {
     int lastFrames = 0;
     // captured CG iteration chunks keyed by the problem bytes
     std::map<std::string, cudaGraphExec_t> graphs;
+    // CG kernel variants {spmm, update, direction}: autotuned per frame count,
+    // or fixed by the caller (-1 = autotune)
+    std::map<int, std::array<int, 3>> cgVariants;
+    std::array<int, 3> forcedVariants{-1, -1, -1};
 
     ~mpf_eit() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -307,8 +313,7 @@ static int ensure_workspace(mpf_eit* m, int F, bool refine, bool jacobian) {
     const size_t vec = G * m->npad * m->KP;
     if (F > m->capF) {
         const size_t slots = (size_t)F * m->W * m->npad;
-        MPF_TRY(m->S.alloc(slots));
-        MPF_TRY(m->R.alloc(slots));
+        MPF_TRY(m->SR.alloc(slots));
         // fields survive growth only if the old contents are copied; simpler to invalidate
         m->X.release();
         MPF_TRY(m->X.alloc(vec));
@@ -376,8 +381,7 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol) {
     P.nblk = m->nblk;
     P.cols = m->cols.ptr;
     P.diagSlot = m->diagSlot.ptr;
-    P.S = m->S.ptr;
-    P.R = m->R.ptr;
+    P.SR = m->SR.ptr;
     P.alpha = m->alpha.ptr;
     P.x = m->X.ptr;
     P.r = m->Rv.ptr;
@@ -401,7 +405,61 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol) {
     P.iters = m->iters.ptr;
     P.counter = m->counter.ptr;
     P.tol2 = tol * tol;
+    auto it = m->cgVariants.find(F);
+    for (int k = 0; k < 3; ++k) {
+        int v = it != m->cgVariants.end() ? it->second[k] : cg_default_variant(m->KP);
+        if (m->forcedVariants[k] >= 0) v = m->forcedVariants[k];
+        (k == 0 ? P.variantSpmm : k == 1 ? P.variantUpdate : P.variantDirection) = v;
+    }
     return P;
+}
+
+// Autotuner: times every valid variant of the three iteration kernels on the
+// model's own assembled systems (F frames) with CUDA events and keeps the
+// fastest of each.  It overwrites the iteration vectors, so it runs only
+// before a cold solve; the caller re-initialises afterwards.
+static int tune_cg(mpf_eit* m, int F, cudaStream_t s) {
+    if (m->cgVariants.count(F)) return MPF_OK;
+    CgProblem P = make_problem(m, F, 0.0);  // tolerance 0: no group retires
+    cudaEvent_t e0, e1;
+    MPF_CUDA(cudaEventCreate(&e0));
+    MPF_CUDA(cudaEventCreate(&e1));
+    std::array<int, 3> best{};
+    int st = MPF_OK;
+    for (int which = 0; which < 3 && st == MPF_OK; ++which) {
+        float bestMs = 1e30f;
+        best[which] = cg_default_variant(m->KP);
+        for (int v = 0; v < kCgVariants && st == MPF_OK; ++v) {
+            if (!cg_variant_valid(m->KP, which, v)) continue;
+            CgProblem Q = P;
+            (which == 0 ? Q.variantSpmm : which == 1 ? Q.variantUpdate : Q.variantDirection) = v;
+            // fresh state with valid p.q, then one untimed launch
+            st = cg_launch_init(Q, true, s);
+            if (st == MPF_OK) st = cg_launch_kernel(Q, 0, s);
+            if (st == MPF_OK) st = cg_launch_kernel(Q, which, s);
+            float msMin = 1e30f;
+            for (int rep = 0; rep < 2 && st == MPF_OK; ++rep) {
+                cudaEventRecord(e0, s);
+                for (int i = 0; i < 4 && st == MPF_OK; ++i) st = cg_launch_kernel(Q, which, s);
+                cudaEventRecord(e1, s);
+                cudaError_t e = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e != cudaSuccess && st == MPF_OK) st = fail(MPF_ECUDA, "autotune timing: %s", cudaGetErrorString(e));
+                msMin = std::min(msMin, ms);
+            }
+            if (st == MPF_OK && msMin < bestMs) {
+                bestMs = msMin;
+                best[which] = v;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != MPF_OK) return st;
+    m->cgVariants[F] = best;
+    m->fieldsValid = false;
+    return MPF_OK;
 }
 
 // Runs CG iterations until every group converged or max_iter; returns the
@@ -477,7 +535,7 @@ static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
 
 int eit_assemble(mpf_eit* m, int F, const float* gamma, bool fp64, cudaStream_t s) {
     return fem_launch_assemble(F, m->W, m->npad, m->E, m->cptr.ptr, m->contrib.ptr, m->Kf.ptr, m->Mf.ptr,
-                               m->Kd.ptr, m->Md64.ptr, gamma, m->ref, m->logarithmic, m->S.ptr, m->R.ptr,
+                               m->Kd.ptr, m->Md64.ptr, gamma, m->ref, m->logarithmic, m->cols.ptr, m->SR.ptr,
                                fp64 ? m->S64.ptr : nullptr, fp64 ? m->R64.ptr : nullptr, s);
 }
 
@@ -486,8 +544,8 @@ int eit_assemble_export(mpf_eit* m, int F, const float* gamma, float* sOut, floa
     MPF_CHECK(F >= 1 && gamma, MPF_EINVAL, "mpf_eit_assemble: bad arguments");
     MPF_TRY(ensure_workspace(m, F, false, false));
     MPF_TRY(eit_assemble(m, F, gamma, false, s));
-    if (sOut) MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->S.ptr, sOut, s));
-    if (rOut) MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->R.ptr, rOut, s));
+    if (sOut) MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->SR.ptr, 0, sOut, s));
+    if (rOut) MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->SR.ptr, 1, rOut, s));
     return MPF_OK;
 }
 
@@ -501,6 +559,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     MPF_TRY(ensure_workspace(m, F, refine, wantJ));
     const bool warm = o.warm_start && m->fieldsValid && m->lastFrames == F;
     MPF_TRY(eit_assemble(m, F, gamma, refine, s));
+    if (!warm) MPF_TRY(tune_cg(m, F, s));
     CgProblem P = make_problem(m, F, o.tol);
     int totalIters = 0, notConv = 0, refinements = 0;
     double maxRel = 0.0;
@@ -690,6 +749,8 @@ int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, doub
     MPF_CHECK(F >= 1 && gamma && reps >= 1 && ms && bytes, MPF_EINVAL, "mpf_eit_profile_cg: bad arguments");
     MPF_TRY(ensure_workspace(m, F, false, false));
     MPF_TRY(eit_assemble(m, F, gamma, false, s));
+    MPF_TRY(tune_cg(m, F, s));
+    m->fieldsValid = false;  // the iteration vectors are overwritten below
     CgProblem P = make_problem(m, F, 0.0);
     MPF_TRY(cg_launch_init(P, true, s));
     cudaEvent_t ev[4];
@@ -716,6 +777,27 @@ int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, doub
     bytes[0] = G * ((double)m->nnz * 12.0 + 2.0 * K * n * 4.0);   // S, R, column + p gather + q
     bytes[1] = G * (6.0 * K * n * 4.0 + 2.0 * n * 4.0);            // x, r rw; p, q read; diagonal
     bytes[2] = G * (3.0 * K * n * 4.0 + 2.0 * n * 4.0);            // r, p read; p write; diagonal
+    return MPF_OK;
+}
+
+// Fixes the CG kernel variants (-1 = autotune); returns the variants a solve
+// with F frames uses (the autotuned ones once a cold solve has run).
+int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get) {
+    if (set) {
+        for (int k = 0; k < 3; ++k)
+            MPF_CHECK(set[k] < 0 || cg_variant_valid(m->KP, k, set[k]), MPF_EINVAL,
+                      "CG kernel variant %d is not available for kernel %d with %d right-hand sides", set[k], k,
+                      m->KP);
+        for (int k = 0; k < 3; ++k) m->forcedVariants[k] = set[k] < 0 ? -1 : set[k];
+        for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+        m->graphs.clear();
+    }
+    if (get) {
+        CgProblem P = make_problem(m, F < 1 ? 1 : F, 0.0);
+        get[0] = P.variantSpmm;
+        get[1] = P.variantUpdate;
+        get[2] = P.variantDirection;
+    }
     return MPF_OK;
 }
 

@@ -24,8 +24,7 @@ struct CgProblem {
     int n, npad, W, KP, G, Ca, nblk;  // nblk = npad / kRowTile
     const int32_t* cols;
     const int32_t* diagSlot;
-    const float* S;      // [F][W][npad]
-    const float* R;
+    const float4* SR;    // [F][W][npad] packed slot {S, R, column (int bits), 0}
     const float* alpha;  // [Ca] per active harmonic
     // vectors [G][npad][KP]
     float *x, *r, *p, *q;
@@ -48,9 +47,16 @@ struct CgProblem {
     int* iters;          // [G]
     unsigned* counter;   // [G] last-block-done counters (kept at zero between launches)
     double tol2;
+    // kernel variants (floats per lane x row steps in flight) of the three
+    // iteration kernels, chosen by the autotuner
+    int variantSpmm, variantUpdate, variantDirection;
 };
 
 // cg_kernels.cu
+// variant v = vecIdx * 3 + rbIdx, floats per lane {4, 2, 1}[vecIdx], row steps {1, 2, 4}[rbIdx]
+constexpr int kCgVariants = 9;
+bool cg_variant_valid(int KP, int which, int v);
+int cg_default_variant(int KP);
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s);
 int cg_launch_kernel(const CgProblem& P, int which /*0 spmm, 1 update, 2 direction*/, cudaStream_t s);
@@ -65,9 +71,9 @@ int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s);
 // fem_kernels.cu
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
                         const float* Kf, const float* Mf, const double* Kd, const double* Md,
-                        const float* gamma, float ref, int logarithmic, float* S, float* R,
+                        const float* gamma, float ref, int logarithmic, const int32_t* cols, float4* SR,
                         double* S64, double* R64, cudaStream_t s);
-int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float* slotMajor,
+int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float4* SR, int component,
                           float* refLayout, cudaStream_t s);
 struct MeasPlan {
     int nnz;                 // nonzeros of the unique excitation columns

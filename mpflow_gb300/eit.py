@@ -275,6 +275,14 @@ class EIT:
         check(lib().mpf_eit_group_iterations(self._h, ptr(out), out.size, ctypes.byref(cnt)))
         return out[:cnt.value].copy()
 
+    def cg_variants(self, frames: int = 1, set=None) -> np.ndarray:
+        """CG kernel variants {spmm, update, direction} a solve with `frames`
+        frames uses; `set` fixes them (-1 = autotune), see mpf_eit_cg_variants."""
+        get = np.zeros(3, np.int32)
+        sv = None if set is None else np.ascontiguousarray(set, np.int32)
+        check(lib().mpf_eit_cg_variants(self._h, None if sv is None else ptr(sv), int(frames), ptr(get)))
+        return get
+
     def profile_cg(self, gamma, reps: int = 20):
         """Mean CUDA-event time (ms) and algorithmic bytes of one launch of the
         SpMM, update and direction kernels (mpf_eit_profile_cg)."""

@@ -241,3 +241,33 @@ def test_profile_cg_reports_bandwidth():
     ms, by = model.profile_cg(torch.ones((2, mesh.elements.shape[0]), device="cuda"), reps=3)
     assert (ms > 0).all() and (by > 0).all()
     assert mp.lib().mpf_kernel_launches() - n0 >= 10
+
+
+@pytest.mark.parametrize("ports,components", [(16, 2), (32, 3)])
+def test_every_cg_variant_matches_oracle(ports, components):
+    """Every launch shape the autotuner may pick gives the oracle's voltages
+    (2.5D model: one Neumann harmonic plus regular ones)."""
+    import oracle
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=20, ports=ports, components=components, height=2.0)
+    g = inclusion_sigma(mesh, seed=5)
+    Vo, _, _ = oracle.eit_forward(orc, g, tol=1e-13)
+    model = mp.EIT(mesh, src, 1.0, components=components, height=2.0)
+    gt = torch.tensor(g, dtype=torch.float32, device="cuda")
+    model.solve(gt, mp.SolveOptions(tol=1e-7))
+    tuned = model.cg_variants(1)
+    assert ((tuned >= 0) & (tuned < 9)).all()
+    tried = 0
+    for v in range(9):
+        try:
+            model.cg_variants(1, set=[v, v, v])
+        except mp.MpfError as e:
+            assert e.status == 1
+            continue
+        tried += 1
+        V = model.solve(gt, mp.SolveOptions(tol=1e-7))[0].cpu().numpy().astype(np.float64)
+        assert rel_err(V, Vo) < 1e-4, (v, rel_err(V, Vo))
+    assert tried >= 5
+    model.cg_variants(1, set=[-1, -1, -1])
+    assert (model.cg_variants(1) == tuned).all()

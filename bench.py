@@ -54,6 +54,9 @@ def parse_args():
     p.add_argument("--tol", type=float, default=1e-5, help="CG relative tolerance of the GN forward solves")
     p.add_argument("--cpu-threads", type=int, default=0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cg-shapes", type=str, default="",
+                   help="fix the CG launch shapes 'spmm,update,direction' (codes of mpf_eit_cg_variants) "
+                        "instead of autotuning")
     p.add_argument("--profile-only", action="store_true",
                    help="only time the CG kernels (all groups active) on --frames frames; for ncu captures")
     return p.parse_args()
@@ -284,11 +287,14 @@ def run_gb300(a):
                    device=local, exact_jacobian=True)
     F = a.frames
     nsteps = a.warmup + a.steps
+    if a.cg_shapes:
+        model.cg_variants(F, set=[int(x) for x in a.cg_shapes.split(",")])
     if a.profile_only:
         v = torch.tensor(synthetic_frames(cent, F, seed=7), device=dev)
         ms, by = model.profile_cg(v, reps=max(a.steps, 1))
         names = ["k_spmm_dot", "k_update", "k_direction"]
         print(json.dumps({"profile_only": True, "frames": F, "groups": F * model.info["active_components"],
+                          "cg_shapes": model.cg_variants(F).tolist(),
                           "ms": dict(zip(names, ms.tolist())),
                           "gbs": dict(zip(names, (by / ms / 1e6).tolist())),
                           "algorithmic_bytes": dict(zip(names, by.tolist()))}), flush=True)

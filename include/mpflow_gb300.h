@@ -252,17 +252,19 @@ int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int3
  * reference returns one summed count (src/models/eit.cpp:207-210). */
 int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, int32_t* count);
 
-/* CG kernel variants of the SpMM, update and direction kernels.  Variant
- * v = 3 * i + k runs {4, 2, 1}[i] floats per lane and keeps {1, 2, 4}[k] row
- * steps in flight per warp.  By default the first cold solve with a given
- * frame count times every variant on the model's own systems and keeps the
- * fastest (the reference's fixed launch shape is src/sparse/
- * sparse_matrix.cpp:222-240).
- *   set: host, 3 ints, each a variant or -1 (autotune), or NULL to leave as is
- *   get: host, 3 ints receiving the variants a solve with `frames` frames
- *        uses, or NULL
- * Fails with MPF_EINVAL for a variant that the right-hand-side width does
- * not allow.  No reference counterpart. */
+/* Launch shapes of the CG SpMM, update and direction kernels.  Shape
+ * code = 3 * i + k + 9 * t runs {4, 2, 1}[i] floats per lane, keeps
+ * {1, 2, 4}[k] row steps in flight per warp and walks 2^t (t = 0..3) tiles of
+ * 128 rows per block.  By default the first cold solve with a given frame
+ * count times every shape on the model's own systems and keeps the fastest
+ * of each kernel (the reference's launch shape is fixed: src/numeric/
+ * sparse_matrix.cpp:262-288).
+ *   set: host, 3 ints, each a shape code or -1 (autotune), or NULL to leave
+ *        as is
+ *   get: host, 3 ints receiving the codes a solve with `frames` frames uses,
+ *        or NULL
+ * Fails with MPF_EINVAL for a shape that the right-hand-side width does not
+ * allow.  No reference counterpart. */
 int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int32_t* get);
 
 /* ======================================================================== */
@@ -300,6 +302,69 @@ int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const
  * of Inverse::solve (src/solver/inverse.cpp:213-238). */
 int mpf_cholesky_solve_f64(int32_t batch, int32_t n, double* A, double shift, double* B,
                            int32_t nrhs, int32_t* info, mpf_stream_t stream);
+
+/* ======================================================================== */
+/* Learned Gauss-Newton warm start.  No reference counterpart: the reference */
+/* starts every reconstruction from the homogeneous distribution            */
+/* (src/solver/solver.cpp:196-225).                                          */
+/* ======================================================================== */
+
+typedef struct mpf_mlp* mpf_mlp_t;
+
+/* Multilayer perceptron in -> hidden1 -> hidden2 -> out with GELU on the
+ * hidden layers, BF16 weights and activations on the tcgen05 tensor cores
+ * with FP32 accumulation, FP32 master weights.  Widths are multiples of 128.
+ * Weights are LeCun-uniform from `seed`, biases zero.  Synchronises. */
+int mpf_mlp_create(int32_t in, int32_t hidden1, int32_t hidden2, int32_t out, uint64_t seed,
+                   int32_t device, mpf_mlp_t* net);
+int mpf_mlp_destroy(mpf_mlp_t net);
+
+/* Layout of the flat FP32 parameter array: offsets[7] = {W1, b1, W2, b2, W3,
+ * b3, total}; each W row-major (outputs x inputs). */
+int mpf_mlp_layout(mpf_mlp_t net, int64_t* offsets);
+
+/* y (device, batch x ldy) = net(x) for x (device, batch x in FP32); the
+ * first min(ldy, out) outputs of each row are written.  Synchronises. */
+int mpf_mlp_forward(mpf_mlp_t net, int32_t batch, const float* x, float* y, int32_t ldy,
+                    mpf_stream_t stream);
+
+/* Forward and backward pass of the loss
+ *   (1 / (batch * valid)) sum_b sum_{j < valid} (y[b][j] - target[b][j])^2
+ * (target: device, batch x ldt) into the network's gradient array.  *loss
+ * (host) receives the loss when non-NULL, which synchronises the stream. */
+int mpf_mlp_backward(mpf_mlp_t net, int32_t batch, const float* x, const float* target, int32_t ldt,
+                     int32_t valid, double* loss, mpf_stream_t stream);
+
+/* One Adam step from the current gradients; weight_decay is decoupled and
+ * applies to the weight matrices only. */
+int mpf_mlp_adam(mpf_mlp_t net, float lr, float beta1, float beta2, float eps, float weight_decay,
+                 mpf_stream_t stream);
+
+/* Device buffer of offsets[6] floats <-> network: which = 0 reads the
+ * parameters, 1 writes them (and resets the Adam state), 2 reads the
+ * gradients of the last mpf_mlp_backward. */
+int mpf_mlp_params(mpf_mlp_t net, float* buffer, int32_t which, mpf_stream_t stream);
+
+/* Network input of the learned warm start, x[f][i] = (v_meas[f][i] - V0[i])
+ * / rms(V0) for the meas_count x drive_count voltages of each frame, V0 the
+ * voltages of the homogeneous distribution (gamma = 0 logarithmic, 1 linear;
+ * solved once per model).  v_meas and x: device, frames x (meas_count *
+ * drive_count) FP32. */
+int mpf_eit_learned_input(mpf_eit_t model, int32_t frames, const float* v_meas, float* x,
+                          mpf_stream_t stream);
+
+/* Gauss-Newton from a learned start.  gamma (device, frames x n_elements,
+ * output) starts as the network's prediction for each frame's voltages; a
+ * frame keeps it only if its relative data residual there is below the
+ * homogeneous start's, otherwise it restarts from the homogeneous
+ * distribution (accepted[f] = 0).  Then mpf_gn_solve iterations to `target`.
+ * The network maps meas_count * drive_count inputs to >= n_elements outputs.
+ *   iterations, residual, accepted: host, frames entries each, or NULL.
+ * Synchronises. */
+int mpf_gn_solve_learned(mpf_eit_t model, mpf_mlp_t net, int32_t frames, float* gamma,
+                         const float* v_meas, double lambda, double target, int32_t max_gn_iters,
+                         const mpf_solve_opts* opts, int32_t* iterations, double* residual,
+                         int32_t* accepted, mpf_gn_stats* stats, mpf_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -98,6 +98,16 @@ SIGNATURES = {
     "mpf_gram_split_bf16": (_I, [_I, _I, _I, _P, _I, _P, _P]),
     "mpf_cholesky_solve_f64": (_I, [_I, _I, _P, _D, _P, _I, _P, _P]),
     "mpf_gram_split_bf16_noalloc": (_I, [_I, _I, _I, _P, _I, _P, _P]),
+    "mpf_mlp_create": (_I, [_I, _I, _I, _I, ctypes.c_uint64, _I, _P]),
+    "mpf_mlp_destroy": (_I, [_P]),
+    "mpf_mlp_layout": (_I, [_P, _P]),
+    "mpf_mlp_forward": (_I, [_P, _I, _P, _P, _I, _P]),
+    "mpf_mlp_backward": (_I, [_P, _I, _P, _P, _I, _I, _P, _P]),
+    "mpf_mlp_adam": (_I, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P]),
+    "mpf_mlp_params": (_I, [_P, _P, _I, _P]),
+    "mpf_eit_learned_input": (_I, [_P, _I, _P, _P, _P]),
+    "mpf_gn_solve_learned": (_I, [_P, _P, _I, _P, _P, _D, _D, _I, ctypes.POINTER(SolveOpts), _P, _P, _P,
+                                  ctypes.POINTER(GnStats), _P]),
 }
 
 _lib = None

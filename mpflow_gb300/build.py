@@ -37,7 +37,8 @@ def _stale(out, deps):
 def build(verbose: bool = False, force: bool = False) -> str:
     """Compile the CUDA library if any source or header changed; return its path."""
     os.makedirs(OBJDIR, exist_ok=True)
-    headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(HERE, "..", "include", "*.h"))
+    headers = (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+               glob.glob(os.path.join(HERE, "..", "include", "*.h")))
     jobs = []
     objs = []
     for src in sources():

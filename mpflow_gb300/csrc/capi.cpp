@@ -52,6 +52,18 @@ int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda,
 int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
 int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
+int mlp_create(int in, int h1, int h2, int out, unsigned long long seed, int device, mpf_mlp** res);
+void mlp_destroy(mpf_mlp* n);
+void mlp_layout(const mpf_mlp* n, int64_t* off);
+int mlp_forward(mpf_mlp* n, int batch, const float* x, float* y, int ldy, cudaStream_t s);
+int mlp_backward(mpf_mlp* n, int batch, const float* x, const float* target, int ldt, int tvalid, double* loss,
+                 cudaStream_t s);
+int mlp_adam(mpf_mlp* n, float lr, float beta1, float beta2, float eps, float weightDecay, cudaStream_t s);
+int mlp_params(mpf_mlp* n, float* buf, int which, cudaStream_t s);
+int learned_input(mpf_eit* m, int F, const float* vMeas, float* x, cudaStream_t s);
+int gn_solve_learned(mpf_eit* m, mpf_mlp* net, int F, float* gamma, const float* vMeas, double lambda,
+                     double target, int maxIters, const mpf_solve_opts* o, int32_t* itersOut, double* resOut,
+                     int32_t* accepted, mpf_gn_stats* stats, cudaStream_t s);
 
 }  // namespace mpf
 
@@ -276,6 +288,63 @@ int mpf_cholesky_solve_f64(int32_t batch, int32_t n, double* A, double shift, do
         MPF_TRY(mpf::dense_cholesky_f64(batch, n, A, info, s));
         MPF_TRY(mpf::dense_cholesky_solve_f64(batch, n, A, B, nrhs, s));
         return MPF_OK;
+    })
+}
+
+int mpf_mlp_create(int32_t in, int32_t hidden1, int32_t hidden2, int32_t out, uint64_t seed, int32_t device,
+                   mpf_mlp_t* net) {
+    MPF_GUARD({ return mpf::mlp_create(in, hidden1, hidden2, out, (unsigned long long)seed, device, net); })
+}
+
+int mpf_mlp_destroy(mpf_mlp_t net) {
+    MPF_GUARD({
+        mpf::mlp_destroy(net);
+        return MPF_OK;
+    })
+}
+
+int mpf_mlp_layout(mpf_mlp_t net, int64_t* offsets) {
+    MPF_GUARD({
+        MPF_CHECK(net && offsets, MPF_EINVAL, "mpf_mlp_layout: null argument");
+        mpf::mlp_layout(net, offsets);
+        return MPF_OK;
+    })
+}
+
+int mpf_mlp_forward(mpf_mlp_t net, int32_t batch, const float* x, float* y, int32_t ldy, mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::mlp_forward(net, batch, x, y, ldy, (cudaStream_t)stream); })
+}
+
+int mpf_mlp_backward(mpf_mlp_t net, int32_t batch, const float* x, const float* target, int32_t ldt, int32_t valid,
+                     double* loss, mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::mlp_backward(net, batch, x, target, ldt, valid, loss, (cudaStream_t)stream); })
+}
+
+int mpf_mlp_adam(mpf_mlp_t net, float lr, float beta1, float beta2, float eps, float weight_decay,
+                 mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::mlp_adam(net, lr, beta1, beta2, eps, weight_decay, (cudaStream_t)stream); })
+}
+
+int mpf_mlp_params(mpf_mlp_t net, float* buffer, int32_t which, mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::mlp_params(net, buffer, which, (cudaStream_t)stream); })
+}
+
+int mpf_eit_learned_input(mpf_eit_t model, int32_t frames, const float* v_meas, float* x, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_learned_input: model == nullptr");
+        return mpf::learned_input(model, frames, v_meas, x, (cudaStream_t)stream);
+    })
+}
+
+int mpf_gn_solve_learned(mpf_eit_t model, mpf_mlp_t net, int32_t frames, float* gamma, const float* v_meas,
+                         double lambda, double target, int32_t max_gn_iters, const mpf_solve_opts* opts,
+                         int32_t* iterations, double* residual, int32_t* accepted, mpf_gn_stats* stats,
+                         mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model && net, MPF_EINVAL, "mpf_gn_solve_learned: null model or network");
+        MPF_CHECK(lambda >= 0.0 && target >= 0.0, MPF_EINVAL, "mpf_gn_solve_learned: lambda and target must be >= 0");
+        return mpf::gn_solve_learned(model, net, frames, gamma, v_meas, lambda, target, max_gn_iters, opts,
+                                     iterations, residual, accepted, stats, (cudaStream_t)stream);
     })
 }
 

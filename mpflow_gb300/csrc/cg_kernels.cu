@@ -13,15 +13,16 @@
 //   k_direction  p = D^-1 r + b p
 // Memory access: a lane moves VEC consecutive floats, so KP/VEC lanes cover
 // one node's right-hand sides and one warp instruction serves 32*VEC/KP
-// rows; each warp keeps RB row steps in flight.  VEC and RB are template
-// parameters chosen per model by the autotuner in model.cu (CUDA-event
-// timings of every variant on the model's own systems).  An ELL slot is one
-// packed float4 {S, R, column, 0} read as a broadcast; the SpMM fuses
-// S + alpha R (the system matrix is never materialised) and unrolls up to
-// kWFast slots.  Inner products: each thread sums at most 16 products with
-// an error-free (TwoProduct/TwoSum) float pair, everything above that level
-// is FP64; the per-block partials are combined by the last block of the group
-// in a fixed order, so results are deterministic.
+// rows; each warp keeps RB row steps in flight, and a block walks
+// P.tiles[k] consecutive 128-row tiles.  VEC and RB (template parameters)
+// and the tiles per block (runtime) are chosen per model by the autotuner in
+// model.cu (CUDA-event timings of every variant on the model's own systems).
+// An ELL slot is one packed float4 {S, R, column, 0} read as a broadcast;
+// the SpMM fuses S + alpha R (the system matrix is never materialised) and
+// unrolls up to kWFast slots.  Inner products: each thread accumulates its
+// products in a compensated (TwoProduct/TwoSum) float pair, everything above
+// that level is FP64; the per-block partials are combined by the last block
+// of the group in a fixed order, so results are deterministic.
 #include "model.h"
 
 namespace mpf {
@@ -64,8 +65,9 @@ __device__ __forceinline__ void stv(float* p, const float (&v)[V]) {
     }
 }
 
-// Error-free accumulation of a*b into a float pair (Knuth TwoSum + FMA
-// TwoProduct); value() is exact to about 2^-48 relative per thread.
+// Compensated accumulation of a*b into a float pair: FMA TwoProduct gives
+// the product's rounding error and Knuth's TwoSum the sum's, both collected
+// in c, so value() carries about twice the float precision.
 struct DotAcc {
     float s = 0.f, c = 0.f;
     __device__ __forceinline__ void add(float a, float b) {
@@ -80,10 +82,10 @@ struct DotAcc {
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
-__device__ __forceinline__ float diag_inv(const float4* SR, const int32_t* diagSlot, int npad, int row,
+__device__ __forceinline__ float diag_inv(const float2* SR, const int32_t* diagSlot, int npad, int row,
                                           float alpha) {
     const int ds = __ldg(&diagSlot[row]);
-    const float4 e = __ldg(&SR[(size_t)ds * npad + row]);
+    const float2 e = __ldg(&SR[(size_t)ds * npad + row]);
     const float d = e.x + alpha * e.y;
     return d != 0.f ? 1.f / d : 0.f;
 }
@@ -93,7 +95,7 @@ __device__ __forceinline__ float diag_inv(const float4* SR, const int32_t* diagS
 // then sees all partials of the group).
 template <int KP, int VEC, int NDOT>
 __device__ __forceinline__ bool block_partials(const DotAcc (&acc)[NDOT][VEC], double* const (&part)[NDOT], int g,
-                                               int nblk, unsigned* counter) {
+                                               unsigned* counter) {
     using Sh = Shape<KP, VEC>;
     __shared__ double red[NDOT][kWarps * Sh::SUB][KP];
     __shared__ bool amLast;
@@ -109,58 +111,75 @@ __device__ __forceinline__ bool block_partials(const DotAcc (&acc)[NDOT][VEC], d
         for (int d = 0; d < NDOT; ++d) {
             double s = 0.0;
             for (int w = 0; w < kWarps * Sh::SUB; ++w) s += red[d][w][threadIdx.x];
-            part[d][((size_t)g * nblk + blockIdx.x) * KP + threadIdx.x] = s;
+            part[d][((size_t)g * gridDim.x + blockIdx.x) * KP + threadIdx.x] = s;
         }
     }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) amLast = atomicAdd(&counter[g], 1u) == (unsigned)(nblk - 1);
+    if (threadIdx.x == 0) amLast = atomicAdd(&counter[g], 1u) == gridDim.x - 1;
     __syncthreads();
     if (amLast) __threadfence();
     return amLast;
 }
 
-// Fixed-order sum of the block partials of group g, right-hand side j.
-__device__ __forceinline__ double sum_partials(const double* part, int g, int nblk, int KP, int j) {
+// Fixed-order sum of the block partials of group g, right-hand side j (one
+// partial per block of the launch's x dimension).
+__device__ __forceinline__ double sum_partials(const double* part, int g, int KP, int j) {
     double s = 0.0;
-    const double* p = part + (size_t)g * nblk * KP + j;
-    for (int b = 0; b < nblk; ++b) s += __ldcg(p + (size_t)b * KP);
+    const double* p = part + (size_t)g * gridDim.x * KP + j;
+    for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(p + (size_t)b * KP);
     return s;
 }
 
-// y[i] = (S + alpha R) x over the rows row[i] (kWFast slots unrolled, rest looped)
+// y[i] = (S + alpha R) x over the rows row[i].  The first kWFast slots are
+// unrolled in three independent batches -- all column loads, then all value
+// loads and gathers -- so a warp waits for one memory latency per batch
+// instead of one per slot; slots past kWFast (meshes with more than kWFast
+// entries in a row) are looped.  Padding slots point at their own row with
+// value 0.
 template <int KP, int VEC, int RB>
-__device__ __forceinline__ void spmm_rows(const float4* SR, int W, int npad, float alpha, const float* x, int j0,
-                                          const int (&row)[RB], float (&y)[RB][VEC]) {
+__device__ __forceinline__ void spmm_rows(const int32_t* cols, const float2* SR, int W, int npad, float alpha,
+                                          const float* x, int j0, const int (&row)[RB], float (&y)[RB][VEC]) {
 #pragma unroll
     for (int i = 0; i < RB; ++i)
 #pragma unroll
         for (int v = 0; v < VEC; ++v) y[i][v] = 0.f;
+    int col[kWFast][RB];
+#pragma unroll
+    for (int k = 0; k < kWFast; ++k)
+#pragma unroll
+        for (int i = 0; i < RB; ++i) col[k][i] = k < W ? __ldg(&cols[(size_t)k * npad + row[i]]) : row[i];
+    float a[kWFast][RB];
+#pragma unroll
+    for (int k = 0; k < kWFast; ++k)
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+            float2 e = make_float2(0.f, 0.f);
+            if (k < W) e = __ldg(&SR[(size_t)k * npad + row[i]]);
+            a[k][i] = e.x + alpha * e.y;
+        }
 #pragma unroll
     for (int k = 0; k < kWFast; ++k) {
         if (k < W) {
-            float4 e[RB];
-#pragma unroll
-            for (int i = 0; i < RB; ++i) e[i] = __ldg(&SR[(size_t)k * npad + row[i]]);
 #pragma unroll
             for (int i = 0; i < RB; ++i) {
                 float xv[VEC];
-                ldv<VEC>(x + (size_t)__float_as_int(e[i].z) * KP + j0, xv);
-                const float a = e[i].x + alpha * e[i].y;
+                ldv<VEC>(x + (size_t)col[k][i] * KP + j0, xv);
 #pragma unroll
-                for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(a, xv[v], y[i][v]);
+                for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(a[k][i], xv[v], y[i][v]);
             }
         }
     }
     for (int k = kWFast; k < W; ++k) {
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
-            const float4 e = __ldg(&SR[(size_t)k * npad + row[i]]);
+            const int c = __ldg(&cols[(size_t)k * npad + row[i]]);
+            const float2 e = __ldg(&SR[(size_t)k * npad + row[i]]);
             float xv[VEC];
-            ldv<VEC>(x + (size_t)__float_as_int(e.z) * KP + j0, xv);
-            const float a = e.x + alpha * e.y;
+            ldv<VEC>(x + (size_t)c * KP + j0, xv);
+            const float av = e.x + alpha * e.y;
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(a, xv[v], y[i][v]);
+            for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(av, xv[v], y[i][v]);
         }
     }
 }
@@ -185,7 +204,7 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
     const int f = g / P.Ca, ci = g % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
-    const float4* SR = P.SR + (size_t)f * P.W * P.npad;
+    const float2* SR = P.SR + (size_t)f * P.W * P.npad;
     const size_t vb = (size_t)g * P.npad * KP;
     const float* b = P.b + (P.bPerGroup ? vb : (size_t)ci * P.npad * KP);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -203,7 +222,7 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
         for (int i = 0; i < RB; ++i) row[i] = rowBase + (st + i) * Sh::SUB + sub;
         float y[RB][VEC];
         if (!zeroGuess) {
-            spmm_rows<KP, VEC, RB>(SR, P.W, P.npad, alpha, P.x + vb, j0, row, y);
+            spmm_rows<KP, VEC, RB>(P.cols, SR, P.W, P.npad, alpha, P.x + vb, j0, row, y);
         } else {
 #pragma unroll
             for (int i = 0; i < RB; ++i) {
@@ -231,13 +250,13 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
         }
     }
     double* const parts[3] = {P.partA, P.partB, P.partC};
-    if (block_partials<KP, VEC, 3>(acc, parts, g, P.nblk, P.counter)) {
+    if (block_partials<KP, VEC, 3>(acc, parts, g, P.counter)) {
         int notConv = 0;
         if (threadIdx.x < KP) {
             const int j = threadIdx.x;
-            double rz = sum_partials(P.partA, g, P.nblk, KP, j);
-            double bz = sum_partials(P.partB, g, P.nblk, KP, j);
-            P.sumP[(size_t)g * KP + j] = dc ? sum_partials(P.partC, g, P.nblk, KP, j) : 0.0;
+            double rz = sum_partials(P.partA, g, KP, j);
+            double bz = sum_partials(P.partB, g, KP, j);
+            P.sumP[(size_t)g * KP + j] = dc ? sum_partials(P.partC, g, KP, j) : 0.0;
             P.rz[(size_t)g * KP + j] = rz;
             P.bz[(size_t)g * KP + j] = bz;
             P.beta[(size_t)g * KP + j] = 0.0;
@@ -263,7 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
     const int f = g / P.Ca, ci = g % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
-    const float4* SR = P.SR + (size_t)f * P.W * P.npad;
+    const float2* SR = P.SR + (size_t)f * P.W * P.npad;
     const size_t vb = (size_t)g * P.npad * KP;
     const float* p = P.p + vb;
     float* q = P.q + vb;
@@ -275,13 +294,16 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
         for (int v = 0; v < VEC; ++v) sp[v] = (float)((double)P.dcScale * P.sumP[(size_t)g * KP + j0 + v]);
     }
     DotAcc acc[1][VEC];
-    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
-    for (int st = 0; st < Sh::STEPS; st += RB) {
+    const int tile0 = blockIdx.x * P.tiles[0];
+    const int nsteps = (min(P.nblk, tile0 + P.tiles[0]) - tile0) * Sh::STEPS;
+    for (int st = 0; st < nsteps; st += RB) {
+        const int rowBase = (tile0 + st / Sh::STEPS) * kRowTile + warp * kRowsPerWarp +
+                            (st % Sh::STEPS) * Sh::SUB + sub;
         int row[RB];
 #pragma unroll
-        for (int i = 0; i < RB; ++i) row[i] = rowBase + (st + i) * Sh::SUB + sub;
+        for (int i = 0; i < RB; ++i) row[i] = rowBase + i * Sh::SUB;
         float y[RB][VEC];
-        spmm_rows<KP, VEC, RB>(SR, P.W, P.npad, alpha, p, j0, row, y);
+        spmm_rows<KP, VEC, RB>(P.cols, SR, P.W, P.npad, alpha, p, j0, row, y);
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
             if (row[i] < P.n) {
@@ -296,8 +318,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
         }
     }
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, VEC, 1>(acc, parts, g, P.nblk, P.counter)) {
-        if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, P.nblk, KP, threadIdx.x);
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter)) {
+        if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x);
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
 }
@@ -311,7 +333,7 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
     if (!P.active[g]) return;
     const int f = g / P.Ca, ci = g % P.Ca;
     const float alpha = P.alpha[ci];
-    const float4* SR = P.SR + (size_t)f * P.W * P.npad;
+    const float2* SR = P.SR + (size_t)f * P.W * P.npad;
     const size_t vb = (size_t)g * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
@@ -323,13 +345,16 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
         a[v] = (!P.conv[s] && pq != 0.0) ? (float)(P.rz[s] / pq) : 0.f;
     }
     DotAcc acc[1][VEC];
-    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
-    for (int st = 0; st < Sh::STEPS; st += RB) {
+    const int tile0 = blockIdx.x * P.tiles[1];
+    const int nsteps = (min(P.nblk, tile0 + P.tiles[1]) - tile0) * Sh::STEPS;
+    for (int st = 0; st < nsteps; st += RB) {
+        const int rowBase = (tile0 + st / Sh::STEPS) * kRowTile + warp * kRowsPerWarp +
+                            (st % Sh::STEPS) * Sh::SUB + sub;
         float xv[RB][VEC], rv[RB][VEC], pv[RB][VEC], qv[RB][VEC], di[RB];
         size_t o[RB];
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
-            const int row = rowBase + (st + i) * Sh::SUB + sub;
+            const int row = rowBase + i * Sh::SUB;
             o[i] = vb + (size_t)row * KP + j0;
             ldv<VEC>(P.x + o[i], xv[i]);
             ldv<VEC>(P.r + o[i], rv[i]);
@@ -350,12 +375,12 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
         }
     }
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, VEC, 1>(acc, parts, g, P.nblk, P.counter)) {
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter)) {
         int notConv = 0;
         if (threadIdx.x < KP) {
             const size_t s = (size_t)g * KP + threadIdx.x;
             if (!P.conv[s]) {
-                const double rzn = sum_partials(P.partA, g, P.nblk, KP, threadIdx.x);
+                const double rzn = sum_partials(P.partA, g, KP, threadIdx.x);
                 const double rzo = P.rz[s];
                 P.beta[s] = rzo != 0.0 ? rzn / rzo : 0.0;
                 P.rz[s] = rzn;
@@ -383,7 +408,7 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
     const int f = g / P.Ca, ci = g % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
-    const float4* SR = P.SR + (size_t)f * P.W * P.npad;
+    const float2* SR = P.SR + (size_t)f * P.W * P.npad;
     const size_t vb = (size_t)g * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
@@ -396,13 +421,16 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
         be[v] = (float)P.beta[s];
     }
     DotAcc acc[1][VEC];
-    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
-    for (int st = 0; st < Sh::STEPS; st += RB) {
+    const int tile0 = blockIdx.x * P.tiles[2];
+    const int nsteps = (min(P.nblk, tile0 + P.tiles[2]) - tile0) * Sh::STEPS;
+    for (int st = 0; st < nsteps; st += RB) {
+        const int rowBase = (tile0 + st / Sh::STEPS) * kRowTile + warp * kRowsPerWarp +
+                            (st % Sh::STEPS) * Sh::SUB + sub;
         float rv[RB][VEC], pv[RB][VEC], di[RB];
         int row[RB];
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
-            row[i] = rowBase + (st + i) * Sh::SUB + sub;
+            row[i] = rowBase + i * Sh::SUB;
             const size_t o = vb + (size_t)row[i] * KP + j0;
             ldv<VEC>(P.r + o, rv[i]);
             ldv<VEC>(P.p + o, pv[i]);
@@ -420,8 +448,8 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
     }
     if (!dc) return;
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, VEC, 1>(acc, parts, g, P.nblk, P.counter)) {
-        if (threadIdx.x < KP) P.sumP[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, P.nblk, KP, threadIdx.x);
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter)) {
+        if (threadIdx.x < KP) P.sumP[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x);
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
 }
@@ -498,8 +526,8 @@ __global__ void __launch_bounds__(kThreads) k_residual64(CgProblem P, const doub
     if (amLast) {
         __threadfence();
         if (threadIdx.x < KP) {
-            rr[(size_t)g * KP + threadIdx.x] = sum_partials(partR, g, P.nblk, KP, threadIdx.x);
-            bb[(size_t)g * KP + threadIdx.x] = sum_partials(partB, g, P.nblk, KP, threadIdx.x);
+            rr[(size_t)g * KP + threadIdx.x] = sum_partials(partR, g, KP, threadIdx.x);
+            bb[(size_t)g * KP + threadIdx.x] = sum_partials(partB, g, KP, threadIdx.x);
         }
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
@@ -648,10 +676,11 @@ int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s) {
 // the launches are real (false while recording a CUDA graph, whose replays
 // are counted by the caller).
 static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count) {
-    const int v = which == 0 ? P.variantSpmm : which == 1 ? P.variantUpdate : P.variantDirection;
+    const int v = P.variant[which];
     CgKernel k = variant_kernel(P.KP, which, v);
     MPF_CHECK(k != nullptr, MPF_EINVAL, "CG kernel variant %d not available for %d right-hand sides", v, P.KP);
-    k<<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P);
+    const int t = P.tiles[which] >= 1 ? P.tiles[which] : 1;
+    k<<<dim3((P.nblk + t - 1) / t, P.G), kThreads, 0, s>>>(P);
     if (count) {
         MPF_LAUNCHED(1);
     } else {

@@ -19,102 +19,15 @@
 #include <mutex>
 
 #include "model.h"
+#include "tc_ptx.cuh"
 
 namespace mpf {
 namespace {
 
-// ---------------------------------------------------------------------------
-// PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint64_t global_timer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: gives up after ~2 s, raising the abort flag instead of hanging.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abortFlag) {
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = global_timer();
-    while (!mbar_try_wait(bar, parity)) {
-        if (*abortFlag) return false;
-        if (global_timer() - t0 > 2000000000ull) {
-            *abortFlag = 1;
-            return false;
-        }
-    }
-    return true;
-}
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
-            dst),
-        "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
-        : "memory");
-}
-// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
-// core-matrix groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((addr >> 4) & 0x3FFFu);      // start address
-    d |= (uint64_t)1 << 16;                      // leading byte offset (unused for SW128 K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;            // stride byte offset
-    d |= (uint64_t)1 << 46;                      // descriptor version (sm_100 family)
-    d |= (uint64_t)2 << 61;                      // 128-byte swizzle
-    return d;
-}
-// instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M=128, N=128
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-            dtmem),
-        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%"
-        "20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
+using namespace tc;
 
 // ---------------------------------------------------------------------------
-constexpr int kTile = 128;                       // M = N tile
-constexpr int kBK = 64;                          // K block (128 bytes of BF16)
 constexpr int kStages = 3;
-constexpr int kTileBytes = kTile * kBK * 2;      // 16 KB
 constexpr int kStageBytes = 4 * kTileBytes;      // A_hi, A_lo, B_hi, B_lo
 constexpr int kGramSmem = kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
 
@@ -166,13 +79,11 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmemBase)),
-                     "r"(128));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        tmem_alloc(smem_u32(&tmemBase), 128);
     }
-    tc_fence_before();
+    fence_before();
     __syncthreads();
-    tc_fence_after();
+    fence_after();
     const uint32_t tmem = tmemBase;
     volatile int* abortFlag = &localAbort;
 
@@ -198,7 +109,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
         for (int i = 0; i < nk; ++i) {
             const int s = i % kStages, round = i / kStages;
             if (!mbar_wait(fullBar + 8 * s, round & 1, abortFlag)) break;
-            tc_fence_after();
+            fence_after();
             const uint32_t st = smemBase + s * kStageBytes;
 #pragma unroll
             for (int kk = 0; kk < kBK / 16; ++kk) {
@@ -217,7 +128,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     // epilogue: every warp drains its 32 TMEM lanes
     const bool waited = nk > 0 && mbar_wait(doneBar, 0, abortFlag);
     const bool ok = __all_sync(0xffffffffu, waited && !*abortFlag);
-    tc_fence_after();
+    fence_after();
     const int row = warp * 32 + lane;
     float* out = ga.work + ((((size_t)b * ga.splits + split) * ga.tiles + blockIdx.x) * kTile + row) * kTile;
     if (ok) {
@@ -232,11 +143,11 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
         for (int c = 0; c < kTile; ++c) out[c] = 0.f;
         if (threadIdx.x == 0 && nk > 0) atomicExch(ga.abortFlag, 1);
     }
-    tc_fence_before();
+    fence_before();
     __syncthreads();
     if (warp == 1) {
-        tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128));
+        fence_after();
+        tmem_dealloc(tmem, 128);
     }
 }
 
@@ -429,20 +340,6 @@ int get_encoder(EncodeTiledFn* out) {
     return fn ? MPF_OK : status;
 }
 
-int make_map(CUtensorMap* map, const __nv_bfloat16* base, int totalRows, int ld) {
-    EncodeTiledFn enc;
-    MPF_TRY(get_encoder(&enc));
-    cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)totalRows};
-    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kTile};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    MPF_CHECK(r == CUDA_SUCCESS, MPF_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-    return MPF_OK;
-}
-
 int gram_splits(int tiles, int kblocks) {
     int s = 148 / tiles;
     s = std::max(1, std::min(s, kblocks / 8));
@@ -464,6 +361,20 @@ int* abort_flag_device() {
 
 }  // namespace
 
+int make_bf16_map(CUtensorMap* map, const __nv_bfloat16* base, int totalRows, int ld) {
+    EncodeTiledFn enc;
+    MPF_TRY(get_encoder(&enc));
+    cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)totalRows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kTile};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    MPF_CHECK(r == CUDA_SUCCESS, MPF_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return MPF_OK;
+}
+
 size_t dense_gram_work_floats(int batch, int rows, int cols) {
     const int nt = rows / kTile, tiles = nt * (nt + 1) / 2, kblocks = cols / kBK;
     return (size_t)batch * gram_splits(tiles, kblocks) * tiles * kTile * kTile;
@@ -478,8 +389,8 @@ static int gram_run(int batch, int rows, int cols, const __nv_bfloat16* hi, cons
     const int splits = gram_splits(tiles, kblocks);
     MPF_CHECK(workFloats >= (size_t)batch * splits * tiles * kTile * kTile, MPF_EINVAL, "gram: workspace too small");
     CUtensorMap mHi, mLo;
-    MPF_TRY(make_map(&mHi, hi, batch * rows, ld));
-    MPF_TRY(make_map(&mLo, lo, batch * rows, ld));
+    MPF_TRY(make_bf16_map(&mHi, hi, batch * rows, ld));
+    MPF_TRY(make_bf16_map(&mLo, lo, batch * rows, ld));
     int* flag = flagOverride ? flagOverride : abort_flag_device();
     MPF_CHECK(flag != nullptr, MPF_ENOMEM, "gram: abort flag allocation failed");
     static bool attr = false;

@@ -26,7 +26,7 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
                            const int32_t* __restrict__ contrib, const float* __restrict__ Kf,
                            const float* __restrict__ Mf, const double* __restrict__ Kd,
                            const double* __restrict__ Md, const float* __restrict__ gamma, float ref,
-                           int logarithmic, const int32_t* __restrict__ cols, float4* __restrict__ SR,
+                           int logarithmic, float2* __restrict__ SR,
                            double* __restrict__ S64, double* __restrict__ R64) {
     const int f = blockIdx.y;
     const size_t slots = (size_t)W * npad;
@@ -47,7 +47,7 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
                 dr = fma(Md[code], pg64, dr);
             }
         }
-        SR[(size_t)f * slots + s] = make_float4(vs, vr, __int_as_float(__ldg(&cols[s])), 0.f);
+        SR[(size_t)f * slots + s] = make_float2(vs, vr);
         if (S64) {
             S64[(size_t)f * slots + s] = ds;
             R64[(size_t)f * slots + s] = dr;
@@ -56,7 +56,7 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
 }
 
 // slot-major [W][npad] -> reference ELL [dataRows][32] (same slot order)
-__global__ void k_export_ell(int W, int npad, int n, int dataRows, const float4* __restrict__ src, int component,
+__global__ void k_export_ell(int W, int npad, int n, int dataRows, const float2* __restrict__ src, int component,
                              float* __restrict__ dst) {
     const int f = blockIdx.y;
     const size_t total = (size_t)dataRows * kEllWidth;
@@ -64,7 +64,7 @@ __global__ void k_export_ell(int W, int npad, int n, int dataRows, const float4*
         const int row = (int)(i / kEllWidth), slot = (int)(i % kEllWidth);
         float v = 0.f;
         if (row < n && slot < W) {
-            const float4 e = src[(size_t)f * W * npad + (size_t)slot * npad + row];
+            const float2 e = src[(size_t)f * W * npad + (size_t)slot * npad + row];
             v = component == 0 ? e.x : e.y;
         }
         dst[(size_t)f * total + i] = v;
@@ -300,21 +300,57 @@ __global__ void k_update_gamma(int rowsJ, int Epad, int E, const float* __restri
     gamma[(size_t)f * E + e] += (float)((double)s + (double)c);
 }
 
+// gamma[f][:] = value for the frames with frameMask[f] != 0 (all if null)
+__global__ void k_fill_frames(int E, const int* __restrict__ frameMask, float value, float* __restrict__ gamma) {
+    const int f = blockIdx.y;
+    if (frameMask && !frameMask[f]) return;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x)
+        gamma[(size_t)f * E + e] = value;
+}
+
+// Learned-start input x[f][i] = (v[f][i] - V0[i]) * invRms and, optionally,
+// the relative data residual of the homogeneous start |v - V0| / |v| per
+// frame (one block per frame, fixed-order reduction).
+__global__ void __launch_bounds__(256) k_learned_input(int L, const float* __restrict__ vMeas,
+                                                       const float* __restrict__ V0, float invRms,
+                                                       float* __restrict__ x, double* __restrict__ res0) {
+    __shared__ double red[2][256];
+    const int f = blockIdx.x;
+    double dd = 0.0, vv = 0.0;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        const float v = vMeas[(size_t)f * L + i], d = v - V0[i];
+        x[(size_t)f * L + i] = d * invRms;
+        dd += (double)d * d;
+        vv += (double)v * v;
+    }
+    red[0][threadIdx.x] = dd;
+    red[1][threadIdx.x] = vv;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + st];
+            red[1][threadIdx.x] += red[1][threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && res0) res0[f] = red[1][0] > 0.0 ? sqrt(red[0][0] / red[1][0]) : 0.0;
+}
+
 }  // namespace
 
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
                         const float* Kf, const float* Mf, const double* Kd, const double* Md,
-                        const float* gamma, float ref, int logarithmic, const int32_t* cols, float4* SR,
-                        double* S64, double* R64, cudaStream_t s) {
+                        const float* gamma, float ref, int logarithmic, float2* SR, double* S64, double* R64,
+                        cudaStream_t s) {
     const size_t slots = (size_t)W * npad;
     int blocks = (int)std::min<size_t>((slots + 255) / 256, 4096);
     k_assemble<<<dim3(blocks, F), 256, 0, s>>>(W, npad, E, cptr, contrib, Kf, Mf, Kd, Md, gamma, ref,
-                                               logarithmic, cols, SR, S64, R64);
+                                               logarithmic, SR, S64, R64);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
-int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float4* SR, int component,
+int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float2* SR, int component,
                           float* refLayout, cudaStream_t s) {
     int blocks = (int)std::min<size_t>(((size_t)dataRows * kEllWidth + 255) / 256, 4096);
     k_export_ell<<<dim3(blocks, F), 256, 0, s>>>(W, npad, n, dataRows, SR, component, refLayout);
@@ -401,6 +437,19 @@ int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, c
                             const int* frameActive, float* gamma, cudaStream_t s) {
     dim3 grid((E + 255) / 256, F);
     k_update_gamma<<<grid, 256, rowsJ * sizeof(float), s>>>(rowsJ, Epad, E, J, w, frameActive, gamma);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int fem_launch_fill_frames(int F, int E, const int* frameMask, float value, float* gamma, cudaStream_t s) {
+    k_fill_frames<<<dim3((E + 255) / 256, F), 256, 0, s>>>(E, frameMask, value, gamma);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int fem_launch_learned_input(int F, int L, const float* vMeas, const float* V0, float invRms, float* x,
+                             double* res0, cudaStream_t s) {
+    k_learned_input<<<F, 256, 0, s>>>(L, vMeas, V0, invRms, x, res0);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

@@ -42,7 +42,7 @@ struct mpf_eit {
     mpf::DevBuf<double> dcShift;      // [KP] constant difference to the reference's solution
     // workspace, grown on demand
     int capF = 0, capF64 = 0, capFJ = 0;
-    mpf::DevBuf<float4> SR;           // packed slot values {S, R, column, 0} per frame
+    mpf::DevBuf<float2> SR;           // slot values {S, R} per frame
     mpf::DevBuf<float> X, Rv, Pv, Qv;
     mpf::DevBuf<double> S64, R64, X64;
     mpf::DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, rr, bb, Gm, sumP, sumX;
@@ -63,6 +63,11 @@ struct mpf_eit {
     // or fixed by the caller (-1 = autotune)
     std::map<int, std::array<int, 3>> cgVariants;
     std::array<int, 3> forcedVariants{-1, -1, -1};
+    // learned warm start: homogeneous voltages and the network input
+    bool v0Ready = false;
+    float v0InvRms = 1.f;
+    mpf::DevBuf<float> V0, learnX;
+    mpf::DevBuf<double> res0;
 
     ~mpf_eit() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -370,6 +375,12 @@ static int ensure_workspace(mpf_eit* m, int F, bool refine, bool jacobian) {
     return MPF_OK;
 }
 
+// launch-shape code -> kernel variant and tiles per block
+static void set_shape(CgProblem& P, int which, int code) {
+    P.variant[which] = code % kCgVariants;
+    P.tiles[which] = 1 << (code / kCgVariants);
+}
+
 static CgProblem make_problem(mpf_eit* m, int F, double tol) {
     CgProblem P{};
     P.n = m->n;
@@ -407,9 +418,9 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol) {
     P.tol2 = tol * tol;
     auto it = m->cgVariants.find(F);
     for (int k = 0; k < 3; ++k) {
-        int v = it != m->cgVariants.end() ? it->second[k] : cg_default_variant(m->KP);
-        if (m->forcedVariants[k] >= 0) v = m->forcedVariants[k];
-        (k == 0 ? P.variantSpmm : k == 1 ? P.variantUpdate : P.variantDirection) = v;
+        int code = it != m->cgVariants.end() ? it->second[k] : cg_default_variant(m->KP);
+        if (m->forcedVariants[k] >= 0) code = m->forcedVariants[k];
+        set_shape(P, k, code);
     }
     return P;
 }
@@ -420,6 +431,7 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol) {
 // before a cold solve; the caller re-initialises afterwards.
 static int tune_cg(mpf_eit* m, int F, cudaStream_t s) {
     if (m->cgVariants.count(F)) return MPF_OK;
+    if (m->forcedVariants[0] >= 0 && m->forcedVariants[1] >= 0 && m->forcedVariants[2] >= 0) return MPF_OK;
     CgProblem P = make_problem(m, F, 0.0);  // tolerance 0: no group retires
     cudaEvent_t e0, e1;
     MPF_CUDA(cudaEventCreate(&e0));
@@ -429,10 +441,10 @@ static int tune_cg(mpf_eit* m, int F, cudaStream_t s) {
     for (int which = 0; which < 3 && st == MPF_OK; ++which) {
         float bestMs = 1e30f;
         best[which] = cg_default_variant(m->KP);
-        for (int v = 0; v < kCgVariants && st == MPF_OK; ++v) {
-            if (!cg_variant_valid(m->KP, which, v)) continue;
+        for (int v = 0; v < kCgVariants * kCgTileChoices && st == MPF_OK; ++v) {
+            if (!cg_variant_valid(m->KP, which, v % kCgVariants)) continue;
             CgProblem Q = P;
-            (which == 0 ? Q.variantSpmm : which == 1 ? Q.variantUpdate : Q.variantDirection) = v;
+            set_shape(Q, which, v);
             // fresh state with valid p.q, then one untimed launch
             st = cg_launch_init(Q, true, s);
             if (st == MPF_OK) st = cg_launch_kernel(Q, 0, s);
@@ -535,7 +547,7 @@ static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
 
 int eit_assemble(mpf_eit* m, int F, const float* gamma, bool fp64, cudaStream_t s) {
     return fem_launch_assemble(F, m->W, m->npad, m->E, m->cptr.ptr, m->contrib.ptr, m->Kf.ptr, m->Mf.ptr,
-                               m->Kd.ptr, m->Md64.ptr, gamma, m->ref, m->logarithmic, m->cols.ptr, m->SR.ptr,
+                               m->Kd.ptr, m->Md64.ptr, gamma, m->ref, m->logarithmic, m->SR.ptr,
                                fp64 ? m->S64.ptr : nullptr, fp64 ? m->R64.ptr : nullptr, s);
 }
 
@@ -695,9 +707,13 @@ int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, 
 }
 
 // Gauss-Newton iterations until every frame's relative data residual is at
-// most `target` (frames that reach it are frozen) or maxIters updates.
-int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, double target, int maxIters,
-             const mpf_solve_opts* oIn, int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s) {
+// most `target` (frames that reach it are frozen) or maxIters updates.  With
+// `fallback` (host, one threshold per frame), a frame whose residual at the
+// start is not below its threshold restarts from gamma0 (accepted[f] = 0)
+// before the first update.
+static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, double target, int maxIters,
+                   const mpf_solve_opts* oIn, const double* fallback, float gamma0, int32_t* accepted,
+                   int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s) {
     MPF_TRY(check_device(m));
     MPF_CHECK(F >= 1 && gamma && vMeas && maxIters >= 0, MPF_EINVAL, "mpf_gn_solve: bad arguments");
     auto t0 = std::chrono::steady_clock::now();
@@ -707,16 +723,35 @@ int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda,
     std::vector<int> mask(F, 1), iters(F, 0);
     std::vector<double> res(F, 0.0);
     int cgTotal = 0, gnIters = 0;
-    for (int it = 0;; ++it) {
+    bool warm = o.warm_start != 0, checkStart = fallback != nullptr;
+    if (accepted)
+        for (int f = 0; f < F; ++f) accepted[f] = 1;
+    for (int it = 0;;) {
         mpf_solve_stats fs{};
         mpf_solve_opts oi = o;
-        oi.warm_start = it > 0 ? 1 : o.warm_start;
+        oi.warm_start = warm ? 1 : 0;
         int st = eit_forward_ws(m, F, gamma, true, &oi, &fs, s);
         if (st != MPF_OK && st != MPF_ENOCONV) return st;
+        warm = true;
         cgTotal += fs.iterations;
         MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
         MPF_CUDA(cudaMemcpyAsync(res.data(), m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
         MPF_CUDA(cudaStreamSynchronize(s));
+        if (checkStart) {
+            checkStart = false;
+            std::vector<int> reject(F, 0);
+            int nrej = 0;
+            for (int f = 0; f < F; ++f) {
+                reject[f] = res[f] > target && !(res[f] < fallback[f]);
+                if (accepted) accepted[f] = !reject[f];
+                nrej += reject[f];
+            }
+            if (nrej) {
+                MPF_CUDA(cudaMemcpyAsync(m->frameMask.ptr, reject.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+                MPF_TRY(fem_launch_fill_frames(F, m->E, m->frameMask.ptr, gamma0, gamma, s));
+                continue;  // re-solve the restarted frames (the others start warm and converged)
+            }
+        }
         int live = 0;
         for (int f = 0; f < F; ++f) {
             if (mask[f] && res[f] <= target) mask[f] = 0;
@@ -728,6 +763,7 @@ int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda,
         MPF_TRY(gn_update(m, F, gamma, lambda, m->frameMask.ptr, s));
         MPF_TRY(gn_check(m, F, s));
         ++gnIters;
+        ++it;
     }
     int converged = 0;
     for (int f = 0; f < F; ++f) converged += res[f] <= target;
@@ -739,6 +775,74 @@ int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda,
         stats->frames_converged = converged;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
+    return MPF_OK;
+}
+
+int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, double target, int maxIters,
+             const mpf_solve_opts* oIn, int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s) {
+    return gn_loop(m, F, gamma, vMeas, lambda, target, maxIters, oIn, nullptr, 0.f, nullptr, itersOut, resOut, stats,
+                   s);
+}
+
+// ---------------------------------------------------------------------------
+// Learned warm start.  The network sees the measured voltages relative to
+// those of the homogeneous distribution, scaled by their RMS, and predicts
+// the parameter vector gamma directly.
+
+static float homogeneous_gamma(const mpf_eit* m) { return m->logarithmic ? 0.f : 1.f; }
+
+// V0 = voltages of the homogeneous distribution (solved once, FP64-refined).
+static int ensure_v0(mpf_eit* m, cudaStream_t s) {
+    if (m->v0Ready) return MPF_OK;
+    const int L = m->Mm * m->Md;
+    DevBuf<float> g0;
+    MPF_TRY(g0.alloc((size_t)m->E));
+    MPF_TRY(fem_launch_fill_frames(1, m->E, nullptr, homogeneous_gamma(m), g0.ptr, s));
+    mpf_solve_opts o{};
+    o.tol = 1e-6;
+    o.refine_tol = 1e-9;
+    MPF_TRY(eit_forward_ws(m, 1, g0.ptr, false, &o, nullptr, s));
+    MPF_TRY(m->V0.alloc((size_t)L));
+    MPF_CUDA(cudaMemcpyAsync(m->V0.ptr, m->V.ptr, sizeof(float) * L, cudaMemcpyDeviceToDevice, s));
+    std::vector<float> h(L);
+    MPF_CUDA(cudaMemcpyAsync(h.data(), m->V.ptr, sizeof(float) * L, cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    double ss = 0.0;
+    for (float v : h) ss += (double)v * v;
+    MPF_CHECK(ss > 0.0, MPF_EINVAL, "learned input: the homogeneous voltages are all zero");
+    m->v0InvRms = (float)(1.0 / std::sqrt(ss / L));
+    m->v0Ready = true;
+    return MPF_OK;
+}
+
+int learned_input(mpf_eit* m, int F, const float* vMeas, float* x, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && vMeas && x, MPF_EINVAL, "mpf_eit_learned_input: bad arguments");
+    MPF_TRY(ensure_v0(m, s));
+    return fem_launch_learned_input(F, m->Mm * m->Md, vMeas, m->V0.ptr, m->v0InvRms, x, nullptr, s);
+}
+
+int gn_solve_learned(mpf_eit* m, mpf_mlp* net, int F, float* gamma, const float* vMeas, double lambda,
+                     double target, int maxIters, const mpf_solve_opts* o, int32_t* itersOut, double* resOut,
+                     int32_t* accepted, mpf_gn_stats* stats, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma && vMeas && maxIters >= 0, MPF_EINVAL, "mpf_gn_solve_learned: bad arguments");
+    const int L = m->Mm * m->Md;
+    int in = 0, out = 0;
+    mlp_dims(net, &in, &out);
+    MPF_CHECK(in == L && out >= m->E, MPF_EINVAL,
+              "mpf_gn_solve_learned: the network maps %d -> %d values, the model needs %d -> %d", in, out, L, m->E);
+    auto t0 = std::chrono::steady_clock::now();
+    MPF_TRY(ensure_v0(m, s));
+    MPF_TRY(m->learnX.alloc((size_t)F * L));
+    MPF_TRY(m->res0.alloc((size_t)F));
+    MPF_TRY(fem_launch_learned_input(F, L, vMeas, m->V0.ptr, m->v0InvRms, m->learnX.ptr, m->res0.ptr, s));
+    std::vector<double> res0(F);
+    MPF_CUDA(cudaMemcpyAsync(res0.data(), m->res0.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
+    MPF_TRY(mlp_forward(net, F, m->learnX.ptr, gamma, m->E, s));  // synchronises
+    MPF_TRY(gn_loop(m, F, gamma, vMeas, lambda, target, maxIters, o, res0.data(), homogeneous_gamma(m), accepted,
+                    itersOut, resOut, stats, s));
+    if (stats) stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return MPF_OK;
 }
 
@@ -785,18 +889,17 @@ int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, doub
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get) {
     if (set) {
         for (int k = 0; k < 3; ++k)
-            MPF_CHECK(set[k] < 0 || cg_variant_valid(m->KP, k, set[k]), MPF_EINVAL,
-                      "CG kernel variant %d is not available for kernel %d with %d right-hand sides", set[k], k,
-                      m->KP);
+            MPF_CHECK(set[k] < 0 || (set[k] < kCgVariants * kCgTileChoices &&
+                                     cg_variant_valid(m->KP, k, set[k] % kCgVariants)),
+                      MPF_EINVAL, "CG launch shape %d is not available for kernel %d with %d right-hand sides",
+                      set[k], k, m->KP);
         for (int k = 0; k < 3; ++k) m->forcedVariants[k] = set[k] < 0 ? -1 : set[k];
         for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
         m->graphs.clear();
     }
     if (get) {
         CgProblem P = make_problem(m, F < 1 ? 1 : F, 0.0);
-        get[0] = P.variantSpmm;
-        get[1] = P.variantUpdate;
-        get[2] = P.variantDirection;
+        for (int k = 0; k < 3; ++k) get[k] = P.variant[k] + kCgVariants * (31 - __builtin_clz(P.tiles[k]));
     }
     return MPF_OK;
 }

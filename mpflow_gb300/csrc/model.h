@@ -2,7 +2,7 @@
 //
 // Data layout in HBM (one mesh, `frames` conductivity frames per call):
 //   cols      [W][npad]            int32  slot-major ELL columns, W = density
-//   S, R      [F][W][npad]         float  stiffness / mass slot values of each frame
+//   SR        [F][W][npad]         float2 {stiffness, mass} slot values of each frame
 //   S64, R64  [F][W][npad]         double same in FP64 (refinement residual only)
 //   X         [F][Ca][npad][KP]    float  fields: node-major, the KP right-hand
 //                                         sides of a node are contiguous, so one
@@ -24,7 +24,7 @@ struct CgProblem {
     int n, npad, W, KP, G, Ca, nblk;  // nblk = npad / kRowTile
     const int32_t* cols;
     const int32_t* diagSlot;
-    const float4* SR;    // [F][W][npad] packed slot {S, R, column (int bits), 0}
+    const float2* SR;    // [F][W][npad] slot values {S, R}; columns in `cols`
     const float* alpha;  // [Ca] per active harmonic
     // vectors [G][npad][KP]
     float *x, *r, *p, *q;
@@ -47,14 +47,18 @@ struct CgProblem {
     int* iters;          // [G]
     unsigned* counter;   // [G] last-block-done counters (kept at zero between launches)
     double tol2;
-    // kernel variants (floats per lane x row steps in flight) of the three
-    // iteration kernels, chosen by the autotuner
-    int variantSpmm, variantUpdate, variantDirection;
+    // launch shape of the three iteration kernels {spmm, update, direction},
+    // chosen by the autotuner: variant (floats per lane x row steps in
+    // flight) and 128-row tiles per block
+    int variant[3];
+    int tiles[3];
 };
 
 // cg_kernels.cu
-// variant v = vecIdx * 3 + rbIdx, floats per lane {4, 2, 1}[vecIdx], row steps {1, 2, 4}[rbIdx]
+// variant v = vecIdx * 3 + rbIdx, floats per lane {4, 2, 1}[vecIdx], row steps {1, 2, 4}[rbIdx];
+// a launch-shape code is v + kCgVariants * ti with 1 << ti tiles per block
 constexpr int kCgVariants = 9;
+constexpr int kCgTileChoices = 4;
 bool cg_variant_valid(int KP, int which, int v);
 int cg_default_variant(int KP);
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
@@ -71,9 +75,9 @@ int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s);
 // fem_kernels.cu
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
                         const float* Kf, const float* Mf, const double* Kd, const double* Md,
-                        const float* gamma, float ref, int logarithmic, const int32_t* cols, float4* SR,
-                        double* S64, double* R64, cudaStream_t s);
-int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float4* SR, int component,
+                        const float* gamma, float ref, int logarithmic, float2* SR, double* S64, double* R64,
+                        cudaStream_t s);
+int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float2* SR, int component,
                           float* refLayout, cudaStream_t s);
 struct MeasPlan {
     int nnz;                 // nonzeros of the unique excitation columns
@@ -110,6 +114,9 @@ int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int np
                              const float* betaC, const float* X, float* out, cudaStream_t s);
 int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, const float* V,
                         double* y, double* res, cudaStream_t s);
+int fem_launch_fill_frames(int F, int E, const int* frameMask, float value, float* gamma, cudaStream_t s);
+int fem_launch_learned_input(int F, int L, const float* vMeas, const float* V0, float invRms, float* x,
+                             double* res0, cudaStream_t s);
 int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, const double* w,
                             const int* frameActive, float* gamma, cudaStream_t s);
 
@@ -126,5 +133,9 @@ int dense_gram_split_bf16_noalloc(int batch, int rows, int cols, const float* A,
 int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s);
 int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s);
 int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s);
+
+// mlp_kernels.cu (used by the learned warm start)
+void mlp_dims(const mpf_mlp* n, int* in, int* out);
+int mlp_forward(mpf_mlp* n, int batch, const float* x, float* y, int ldy, cudaStream_t s);
 
 }  // namespace mpf

@@ -190,6 +190,12 @@ class EIT:
         g = gamma.reshape(-1, self.mesh.elements.shape[0]).contiguous()
         return g, g.shape[0]
 
+    def _vmeas(self, v_meas, F: int):
+        """Measured voltages in the logical (frames, Mm, Md) shape that solve()
+        returns -> the library's layout (column-major Mm x Md per frame)."""
+        Mm, Md = self.info["meas_count"], self.info["drive_count"]
+        return v_meas.reshape(F, Mm, Md).transpose(1, 2).contiguous()
+
     def assemble(self, gamma):
         """Stiffness and mass slot values in the reference ELL layout."""
         import torch
@@ -242,7 +248,7 @@ class EIT:
         g, F = self._frames(gamma)
         if g.data_ptr() != gamma.data_ptr():
             raise ValueError("gamma must be contiguous")
-        vm = v_meas.reshape(F, -1).contiguous()
+        vm = self._vmeas(v_meas, F)
         res = np.zeros(F)
         st = _ffi.SolveStats()
         o = (options or SolveOptions()).c()
@@ -259,7 +265,7 @@ class EIT:
         g, F = self._frames(gamma)
         if g.data_ptr() != gamma.data_ptr():
             raise ValueError("gamma must be contiguous")
-        vm = v_meas.reshape(F, -1).contiguous()
+        vm = self._vmeas(v_meas, F)
         iters = np.zeros(F, np.int32)
         res = np.zeros(F)
         st = _ffi.GnStats()
@@ -267,6 +273,35 @@ class EIT:
         check(lib().mpf_gn_solve(self._h, F, ptr(g), ptr(vm), float(lam), float(target), int(max_iters),
                                  ctypes.byref(o), ptr(iters), ptr(res), ctypes.byref(st), _stream()))
         return iters, res, st
+
+    def learned_input(self, v_meas):
+        """Network input of the learned warm start for (frames, Mm, Md)
+        voltages: (V - V0) / rms(V0) per frame (mpf_eit_learned_input)."""
+        import torch
+        F = v_meas.shape[0]
+        vm = self._vmeas(v_meas, F)
+        x = torch.empty((F, vm.shape[1] * vm.shape[2]), dtype=torch.float32, device=vm.device)
+        check(lib().mpf_eit_learned_input(self._h, F, ptr(vm), ptr(x), _stream()))
+        return x
+
+    def gn_solve_learned(self, net, v_meas, lam: float, target: float = 1e-3, max_iters: int = 10,
+                         options: SolveOptions | None = None):
+        """Gauss-Newton from the network's prediction (mpf_gn_solve_learned).
+        Returns (gamma, updates per frame, final residual per frame, accepted
+        per frame, GnStats)."""
+        import torch
+        F = v_meas.shape[0]
+        vm = self._vmeas(v_meas, F)
+        g = torch.empty((F, self.mesh.elements.shape[0]), dtype=torch.float32, device=vm.device)
+        iters = np.zeros(F, np.int32)
+        res = np.zeros(F)
+        acc = np.zeros(F, np.int32)
+        st = _ffi.GnStats()
+        o = (options or SolveOptions()).c()
+        check(lib().mpf_gn_solve_learned(self._h, net._h, F, ptr(g), ptr(vm), float(lam), float(target),
+                                         int(max_iters), ctypes.byref(o), ptr(iters), ptr(res), ptr(acc),
+                                         ctypes.byref(st), _stream()))
+        return g, iters, res, acc, st
 
     def group_iterations(self) -> np.ndarray:
         """CG iterations per (frame, active harmonic) group of the last inner solve."""

@@ -1,0 +1,189 @@
+"""Learned Gauss-Newton warm start (no counterpart in the reference, which
+starts every absolute reconstruction from the homogeneous distribution,
+src/solver/solver.cpp:196-225).
+
+A multilayer perceptron maps a frame's measured voltages, taken relative to
+the voltages of the homogeneous distribution, to the parameter vector gamma
+of every element.  Its training pairs are made by the forward solver itself
+(EIT.solve on seeded inclusion phantoms), its training and inference run in
+the library's own kernels (mpf_mlp_*: BF16 tcgen05 GEMMs with FP32
+accumulation, Adam on FP32 master weights), and the plain Gauss-Newton
+iteration is its judge: EIT.gn_solve_learned keeps a prediction only where it
+lowers the data residual below the homogeneous start's and then iterates to
+the target.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import time
+
+import numpy as np
+
+from ._ffi import check, lib, ptr
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class MLP:
+    """in -> hidden1 -> hidden2 -> out perceptron with GELU hidden layers
+    (mpf_mlp_create); widths are multiples of 128."""
+
+    def __init__(self, inputs: int, hidden1: int, hidden2: int, outputs: int, seed: int = 0, device: int = 0):
+        self.inputs, self.hidden1, self.hidden2, self.outputs = int(inputs), int(hidden1), int(hidden2), int(outputs)
+        self.device = int(device)
+        h = ctypes.c_void_p()
+        check(lib().mpf_mlp_create(self.inputs, self.hidden1, self.hidden2, self.outputs, int(seed), self.device,
+                                   ctypes.byref(h)))
+        self._h = h
+        off = np.zeros(7, np.int64)
+        check(lib().mpf_mlp_layout(h, ptr(off)))
+        self.offsets = off
+        self.param_count = int(off[6])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().mpf_mlp_destroy(h)
+            self._h = None
+
+    def forward(self, x):
+        """y = net(x) for a (batch, inputs) float32 CUDA tensor."""
+        import torch
+        x = x.contiguous()
+        y = torch.empty((x.shape[0], self.outputs), dtype=torch.float32, device=x.device)
+        check(lib().mpf_mlp_forward(self._h, x.shape[0], ptr(x), ptr(y), self.outputs, _stream()))
+        return y
+
+    def backward(self, x, target, valid: int | None = None, want_loss: bool = True):
+        """Gradients of the mean squared error over the first `valid` outputs;
+        returns the loss (host sync) or None."""
+        x = x.contiguous()
+        target = target.contiguous()
+        valid = int(valid if valid is not None else target.shape[1])
+        loss = ctypes.c_double(0.0)
+        check(lib().mpf_mlp_backward(self._h, x.shape[0], ptr(x), ptr(target), target.shape[1], valid,
+                                     ctypes.byref(loss) if want_loss else None, _stream()))
+        return loss.value if want_loss else None
+
+    def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
+             weight_decay: float = 0.0):
+        check(lib().mpf_mlp_adam(self._h, float(lr), float(beta1), float(beta2), float(eps), float(weight_decay),
+                                 _stream()))
+
+    def _params(self, which: int, buf=None):
+        import torch
+        if buf is None:
+            buf = torch.empty(self.param_count, dtype=torch.float32, device=f"cuda:{self.device}")
+        check(lib().mpf_mlp_params(self._h, ptr(buf), which, _stream()))
+        return buf
+
+    def parameters(self):
+        """Flat FP32 parameters W1 | b1 | W2 | b2 | W3 | b3 (see offsets)."""
+        return self._params(0)
+
+    def set_parameters(self, buf):
+        self._params(1, buf.contiguous())
+
+    def gradients(self):
+        return self._params(2)
+
+    def unpack(self, flat):
+        """Split a flat parameter (or gradient) vector into (W1, b1, W2, b2, W3, b3) numpy arrays."""
+        f = flat.detach().cpu().numpy() if hasattr(flat, "detach") else np.asarray(flat)
+        o = self.offsets
+        W1 = f[o[0]:o[0] + self.hidden1 * self.inputs].reshape(self.hidden1, self.inputs)
+        b1 = f[o[1]:o[1] + self.hidden1]
+        W2 = f[o[2]:o[2] + self.hidden2 * self.hidden1].reshape(self.hidden2, self.hidden1)
+        b2 = f[o[3]:o[3] + self.hidden2]
+        W3 = f[o[4]:o[4] + self.outputs * self.hidden2].reshape(self.outputs, self.hidden2)
+        b3 = f[o[5]:o[5] + self.outputs]
+        return W1, b1, W2, b2, W3, b3
+
+
+def round_up(v: int, m: int) -> int:
+    return (v + m - 1) // m * m
+
+
+def inclusion_frames(centroids: np.ndarray, count: int, rng: np.random.Generator, inclusions=(1, 3),
+                     radius=(0.05, 0.3), contrast=(0.1, 10.0), domain_radius: float = 1.0) -> np.ndarray:
+    """Log-conductivity frames in the library's dB parametrisation
+    (sigma = ref 10^(gamma/10)): a 0 dB background with 1-3 disks of radius
+    U(radius) and conductivity ratio log-uniform in `contrast`, centres
+    uniform in the disk that keeps the inclusion inside the domain."""
+    E = centroids.shape[0]
+    out = np.zeros((count, E), np.float32)
+    lo, hi = np.log(contrast[0]), np.log(contrast[1])
+    for f in range(count):
+        k = rng.integers(inclusions[0], inclusions[1] + 1)
+        for _ in range(k):
+            r = rng.uniform(*radius)
+            rc = (domain_radius - r) * math.sqrt(rng.uniform())
+            th = rng.uniform(0.0, 2.0 * math.pi)
+            c = np.array([rc * math.cos(th), rc * math.sin(th)])
+            ratio = math.exp(rng.uniform(lo, hi))
+            inside = ((centroids - c) ** 2).sum(axis=1) <= r * r
+            out[f, inside] = 10.0 * math.log10(ratio)
+    return out
+
+
+def generate_pairs(model, gammas: np.ndarray, batch: int = 64, options=None):
+    """Voltages of the forward model for every frame of `gammas` (count x E,
+    host).  Returns (V as (count, Mm, Md), gamma) CUDA tensors."""
+    import torch
+    from .eit import SolveOptions
+    opts = options or SolveOptions(tol=1e-5, max_iter=6000)
+    Vs = []
+    for i in range(0, gammas.shape[0], batch):
+        g = torch.tensor(gammas[i:i + batch], device=f"cuda:{model.device}")
+        Vs.append(model.solve(g, opts).contiguous())
+    return torch.cat(Vs), torch.tensor(gammas, device=f"cuda:{model.device}")
+
+
+def add_noise(V, snr_db: float, generator=None):
+    """V + Gaussian noise with std rms(V_frame) 10^(-snr/20) per frame."""
+    import torch
+    rms = V.reshape(V.shape[0], -1).pow(2).mean(dim=1).sqrt()
+    std = rms * 10.0 ** (-snr_db / 20.0)
+    noise = torch.randn(V.shape, device=V.device, generator=generator) * std.view(-1, *([1] * (V.dim() - 1)))
+    return V + noise
+
+
+def train_warm_start(model, net: MLP, V, gamma, epochs: int = 60, batch: int = 256, lr: float = 1e-3,
+                     weight_decay: float = 1e-4, snr_db: float | None = 60.0, seed: int = 0, log=None):
+    """Train `net` on (V, gamma) pairs with Adam and a cosine learning rate;
+    fresh measurement noise at `snr_db` every epoch (None: noise-free).
+    Returns the per-epoch mean losses and the wall time."""
+    import torch
+    N, E = gamma.shape
+    if batch % 128:
+        raise ValueError("batch must be a multiple of 128")
+    gen = torch.Generator(device=V.device)
+    gen.manual_seed(seed)
+    steps_per_epoch = max(1, N // batch)
+    total = epochs * steps_per_epoch
+    losses = []
+    t0 = time.perf_counter()
+    step = 0
+    for ep in range(epochs):
+        Vn = add_noise(V, snr_db, gen) if snr_db is not None else V
+        X = model.learned_input(Vn)
+        perm = torch.randperm(N, device=V.device, generator=gen)
+        acc = 0.0
+        for b in range(steps_per_epoch):
+            idx = perm[b * batch:(b + 1) * batch]
+            want = b == steps_per_epoch - 1
+            loss = net.backward(X[idx], gamma[idx], valid=E, want_loss=want)
+            if want:
+                acc = loss
+            cur = lr * 0.5 * (1.0 + math.cos(math.pi * step / total))
+            net.adam(cur, weight_decay=weight_decay)
+            step += 1
+        losses.append(acc)
+        if log:
+            log(f"epoch {ep}: loss {acc:.4g}")
+    torch.cuda.synchronize()
+    return losses, time.perf_counter() - t0

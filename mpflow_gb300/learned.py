@@ -28,6 +28,13 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+def _f32(t, name: str):
+    import torch
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32):
+        raise TypeError(f"{name} must be a float32 CUDA tensor")
+    return t.contiguous()
+
+
 class MLP:
     """in -> hidden1 -> hidden2 -> out perceptron with GELU hidden layers
     (mpf_mlp_create); widths are multiples of 128."""
@@ -53,7 +60,7 @@ class MLP:
     def forward(self, x):
         """y = net(x) for a (batch, inputs) float32 CUDA tensor."""
         import torch
-        x = x.contiguous()
+        x = _f32(x, "x")
         y = torch.empty((x.shape[0], self.outputs), dtype=torch.float32, device=x.device)
         check(lib().mpf_mlp_forward(self._h, x.shape[0], ptr(x), ptr(y), self.outputs, _stream()))
         return y
@@ -61,8 +68,8 @@ class MLP:
     def backward(self, x, target, valid: int | None = None, want_loss: bool = True):
         """Gradients of the mean squared error over the first `valid` outputs;
         returns the loss (host sync) or None."""
-        x = x.contiguous()
-        target = target.contiguous()
+        x = _f32(x, "x")
+        target = _f32(target, "target")
         valid = int(valid if valid is not None else target.shape[1])
         loss = ctypes.c_double(0.0)
         check(lib().mpf_mlp_backward(self._h, x.shape[0], ptr(x), ptr(target), target.shape[1], valid,
@@ -86,7 +93,7 @@ class MLP:
         return self._params(0)
 
     def set_parameters(self, buf):
-        self._params(1, buf.contiguous())
+        self._params(1, _f32(buf, "parameters"))
 
     def gradients(self):
         return self._params(2)

@@ -5,13 +5,20 @@ Workload (one "step"): reconstruct a batch of conductivity frames on the
 20k-node disk (80 rings: 19441 nodes, 38400 triangles), 32 electrodes with
 adjacent drive / adjacent measurement (1024 voltages per frame), 2.5D model
 with 8 axial harmonics (height 4, k_j = j*pi/2), logarithmic (dB)
-conductivity, by batched regularised Gauss-Newton until every frame's relative
-data residual ||V_meas - V(sigma)|| / ||V_meas|| is at most 1e-3.  Synthetic,
-seeded data: 1-3 circular inclusions (radius U(0.05, 0.3), contrast
-log-uniform in [0.1, 10]) on a 1 S/m background; V_meas from the forward
-model with FP64 refinement to 1e-9 (noise-free).  The metric is frames/s
-(frames that reach the target per second); the line also carries the CG SpMM
-bandwidth, the roofline of the dominant kernel and the CPU baseline.
+conductivity, until every frame's relative data residual
+||V_meas - V(sigma)|| / ||V_meas|| is at most 1e-3.  Synthetic, seeded data:
+1-3 circular inclusions (radius U(0.05, 0.3), contrast log-uniform in
+[0.1, 10]) on a 1 S/m background; V_meas from the forward model with FP64
+refinement to 1e-9 (noise-free).
+
+The headline value is the learned path: a network trained (before the timed
+region) on pairs that the forward solver generates predicts each frame's
+Gauss-Newton start, then batched GN iterates to the target (frames whose
+prediction does not lower the residual restart from the homogeneous
+distribution).  The same frames are also timed on the plain batched GN path
+and one frame at a time.  The metric is frames/s (frames that reach the
+target per second); the line also carries the CG SpMM bandwidth, the roofline
+of the dominant kernel and the CPU baseline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -57,6 +64,12 @@ def parse_args():
     p.add_argument("--cg-shapes", type=str, default="",
                    help="fix the CG launch shapes 'spmm,update,direction' (codes of mpf_eit_cg_variants) "
                         "instead of autotuning")
+    p.add_argument("--train-pairs", type=int, default=4096,
+                   help="training pairs of the learned warm start, generated by the forward solver")
+    p.add_argument("--epochs", type=int, default=80)
+    p.add_argument("--hidden", type=int, default=2048, help="hidden width of the warm-start network")
+    p.add_argument("--single-frames", type=int, default=4,
+                   help="frames per step timed one at a time on the plain GN path (0: skip)")
     p.add_argument("--profile-only", action="store_true",
                    help="only time the CG kernels (all groups active) on --frames frames; for ncu captures")
     return p.parse_args()
@@ -151,14 +164,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per SpMM launch per (frame, harmonic) group from the committed
-    ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", "cg_spmm_dot_R80.md")
+def profiled_traffic(kernel: str):
+    """DRAM bytes per launch per (frame, harmonic) group of a CG kernel from the
+    committed ncu summary (line '<kernel> dram_bytes_per_group_launch: X'),
+    or None."""
+    path = os.path.join(ROOT, "profiles", "cg_kernels_R80_F16.md")
     try:
         with open(path) as fh:
             for line in fh:
-                if line.startswith("dram_bytes_per_group_launch:"):
+                if line.startswith(f"{kernel} dram_bytes_per_group_launch:"):
                     return float(line.split(":", 1)[1])
     except OSError:
         pass
@@ -263,16 +277,39 @@ def run_reference(a):
 def workload_config(a, frames):
     return {"workload": (f"EIT 2.5D GN reconstruction: ring mesh {a.rings} rings (19441 nodes, 38400 "
                          f"triangles at 80), {a.electrodes} electrodes adjacent/adjacent, "
-                         f"{a.components} harmonics (height {a.height}), log-conductivity"),
+                         f"{a.components} harmonics (height {a.height}), log-conductivity, 1-3 inclusions "
+                         "r U(0.05,0.3) contrast log-U[0.1,10]"),
             "frames_per_step_per_gpu": frames, "target_rel_residual": a.target,
+            "target_data": "noise-free held-out frames (60 dB noise only on the training pairs)",
             "lambda_rel": a.lam_rel, "cg_tol": a.tol, "jacobian": "exact 2.5D derivative",
             "l2": "CG working set > L2 (129 MB) at >= 8 frames per step"}
+
+
+def timed_steps(nsteps, warmup, fn, barrier, stream, torch, lib):
+    """Run fn(step) for every step between barriers, CUDA events around each
+    call on `stream`; returns (per-step ms of the timed steps, their results,
+    kernel launches inside the timed steps)."""
+    times, results, launches = [], [], 0
+    for s in range(nsteps):
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = lib.mpf_kernel_launches()
+        e0.record(stream)
+        r = fn(s)
+        e1.record(stream)
+        barrier()
+        if s >= warmup:
+            times.append(e0.elapsed_time(e1))
+            results.append(r)
+            launches += lib.mpf_kernel_launches() - l0
+    return times, results, launches
 
 
 def run_gb300(a):
     import torch
     import torch.distributed as dist
     import mpflow_gb300 as mp
+    from mpflow_gb300.learned import generate_pairs, inclusion_frames, round_up, train_warm_start
 
     rank, world, local = dist_env()
     if world > 1:
@@ -299,57 +336,84 @@ def run_gb300(a):
                           "gbs": dict(zip(names, (by / ms / 1e6).tolist())),
                           "algorithmic_bytes": dict(zip(names, by.tolist()))}), flush=True)
         return
-    # synthetic truth and measurements per step (untimed)
+    lib = mp.lib()
+    # held-out frames and their noise-free measurements (untimed)
     truth = [synthetic_frames(cent, F, seed=1000 * (rank + 1) + s) for s in range(nsteps)]
-    vmeas = []
     ref_opts = mp.SolveOptions(tol=1e-5, refine_tol=1e-9, max_iter=6000)
-    for s in range(nsteps):
-        V = model.solve(torch.tensor(truth[s], device=dev), ref_opts)
-        vmeas.append(V.contiguous())
-    # regularisation from the Jacobian at the reference conductivity
+    vmeas = [model.solve(torch.tensor(truth[s], device=dev), ref_opts).contiguous() for s in range(nsteps)]
     _, J0 = model.solve(torch.zeros((1, E), device=dev), mp.SolveOptions(tol=a.tol), jacobian=True)
     lam = a.lam_rel * float(J0.norm() / np.sqrt(J0.shape[1]))
     del J0
     opts = mp.SolveOptions(tol=a.tol, max_iter=6000)
+
+    # learned warm start: pairs from the forward solver, training on the GPU (untimed, reported)
+    t0 = time.perf_counter()
+    gtrain = inclusion_frames(cent, a.train_pairs, np.random.default_rng(5 + 7919 * rank))
+    Vtr, gtr = generate_pairs(model, gtrain, batch=64, options=opts)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    L = Vtr.shape[1] * Vtr.shape[2]
+    net = mp.MLP(L, a.hidden, a.hidden, round_up(E, 128), seed=17 + rank)
+    losses, train_s = train_warm_start(model, net, Vtr, gtr, epochs=a.epochs, batch=256, lr=1e-3,
+                                       snr_db=60.0, seed=rank)
+    train_steps = a.epochs * max(1, a.train_pairs // 256)
+    del Vtr, gtr
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- device-resident timing: V_meas already in HBM
     stream = torch.cuda.current_stream()
-    frames_done, gn_updates, times_ms = 0, [], []
-    launches = 0
-    with ClockSampler(local) as clocks:
-        for s in range(nsteps):
-            g = torch.zeros((F, E), device=dev)
-            barrier()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            l0 = mp.lib().mpf_kernel_launches()
-            e0.record(stream)
-            iters, res, st = model.gn_solve(g, vmeas[s], lam, target=a.target, max_iters=a.max_gn, options=opts)
-            e1.record(stream)
-            barrier()
-            if s >= a.warmup:
-                launches += mp.lib().mpf_kernel_launches() - l0
-                times_ms.append(e0.elapsed_time(e1))
-                frames_done += int(st.frames_converged)
-                gn_updates.extend(iters.tolist())
-    step_ms = float(np.mean(times_ms))
-    total_ms = float(np.sum(times_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        n = torch.tensor([frames_done], device=dev, dtype=torch.float64)
-        dist.all_reduce(n)
-        frames_all = float(n.item())
-    else:
-        frames_all = float(frames_done)
-    value = frames_all / (total_ms / 1e3)
 
-    # ---- end to end through the public API: host V_meas in, host sigma out
+    def learned_step(s):
+        _, it, res, acc, st = model.gn_solve_learned(net, vmeas[s], lam, target=a.target, max_iters=a.max_gn,
+                                                     options=opts)
+        return it, acc, st
+
+    def plain_step(s):
+        g = torch.zeros((F, E), device=dev)
+        it, res, st = model.gn_solve(g, vmeas[s], lam, target=a.target, max_iters=a.max_gn, options=opts)
+        return it, None, st
+
+    def single_step(s):
+        its, conv = [], 0
+        for f in range(a.single_frames):
+            g = torch.zeros((1, E), device=dev)
+            it, res, st = model.gn_solve(g, vmeas[s][f:f + 1], lam, target=a.target, max_iters=a.max_gn,
+                                         options=opts)
+            its.append(int(it[0]))
+            conv += int(st.frames_converged)
+        return np.array(its), None, conv
+
+    def summarise(times, results, frames_per_step):
+        total_ms = float(np.sum(times))
+        done = float(sum(int(r[2].frames_converged) if hasattr(r[2], "frames_converged") else int(r[2])
+                         for r in results))
+        if world > 1:
+            t = torch.tensor([total_ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total_ms = float(t.item())
+            n = torch.tensor([done], device=dev, dtype=torch.float64)
+            dist.all_reduce(n)
+            done = float(n.item())
+        its = np.concatenate([r[0] for r in results])
+        return {"value": done / (total_ms / 1e3), "ms_per_step": float(np.mean(times)),
+                "gn_updates_mean": float(its.mean()),
+                "frames_converged_fraction": done / (frames_per_step * world * len(results))}
+
+    with ClockSampler(local) as clocks:
+        t_l, r_l, launches = timed_steps(nsteps, a.warmup, learned_step, barrier, stream, torch, lib)
+        t_p, r_p, _ = timed_steps(nsteps, a.warmup, plain_step, barrier, stream, torch, lib)
+        single = None
+        if a.single_frames > 0:
+            t_s, r_s, _ = timed_steps(nsteps, a.warmup, single_step, barrier, stream, torch, lib)
+            single = summarise(t_s, r_s, a.single_frames)
+    learned = summarise(t_l, r_l, F)
+    plain = summarise(t_p, r_p, F)
+    accepted = float(np.mean(np.concatenate([r[1] for r in r_l])))
+
+    # end to end through the public API: host V_meas in, host sigma out (learned path)
     host_v = [v.cpu().pin_memory() for v in vmeas]
     host_out = torch.empty((F, E), dtype=torch.float32).pin_memory()
     e2e_ms, e2e_frames = [], 0
@@ -357,8 +421,7 @@ def run_gb300(a):
         barrier()
         t0 = time.perf_counter()
         vm = host_v[s].to(dev, non_blocking=True)
-        g = torch.zeros((F, E), device=dev)
-        _, _, st = model.gn_solve(g, vm, lam, target=a.target, max_iters=a.max_gn, options=opts)
+        g, _, _, _, st = model.gn_solve_learned(net, vm, lam, target=a.target, max_iters=a.max_gn, options=opts)
         host_out.copy_(g, non_blocking=True)
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) * 1e3
@@ -367,33 +430,46 @@ def run_gb300(a):
             e2e_frames += int(st.frames_converged)
     e2e_value = e2e_frames * world / (sum(e2e_ms) / 1e3)
 
-    # ---- roofline of the CG kernels (CUDA events on the launching stream)
+    # roofline of the CG kernels (CUDA events on the launching stream)
     ms, by = model.profile_cg(torch.tensor(truth[0], device=dev), reps=10)
     gbs = by / ms / 1e6
     dom = int(np.argmax(ms))
     names = ["k_spmm_dot", "k_update", "k_direction"]
     peak, peak_kind = measured_peaks()
     groups = F * model.info["active_components"]
-    traffic_per_group = profiled_traffic()
+    traffic = profiled_traffic(names[dom])
     roofline = {"kernel": names[dom], "bound": "hbm", "achieved": float(gbs[dom]), "peak": peak,
                 "unit": "GB/s", "frac": float(gbs[dom] / peak), "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": (traffic_per_group * groups if (traffic_per_group and dom == 0) else None),
+                "traffic": traffic * groups if traffic else None,
                 "algorithmic_bytes": float(by[dom]), "launch_ms": float(ms[dom])}
 
     if rank != 0:
         return
     cpu = None
     if not a.no_cpu_baseline:
-        cpu = cpu_baseline(a, mesh, ports, pat, truth[0], float(np.mean(gn_updates)))
+        cpu = cpu_baseline(a, mesh, ports, pat, truth[0], plain["gn_updates_mean"])
+    mlp_flops = 6.0 * 256 * net.param_count * train_steps
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 inner products / refinement / Cholesky, split-BF16 J J^T)",
-        "data": "synthetic (seeded inclusion frames, noise-free; V_meas from the FP64-refined forward model)",
+        "metric": METRIC, "value": learned["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": learned["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 inner products / refinement / Cholesky, split-BF16 J J^T, "
+                                      "BF16 network)",
+        "data": "synthetic (seeded inclusion frames; V_meas noise-free from the FP64-refined forward model; "
+                "training pairs from the forward model with 60 dB noise)",
         "config": workload_config(a, F),
-        "method": "plain batched GN (homogeneous start)",
-        "gn_updates_mean": float(np.mean(gn_updates)),
-        "frames_converged_fraction": frames_all / (F * world * a.steps),
+        "method": "learned warm start + batched GN (plain GN fallback per frame)",
+        "gn_updates_mean": learned["gn_updates_mean"],
+        "frames_converged_fraction": learned["frames_converged_fraction"],
+        "learned": {"accepted_fraction": accepted,
+                    "gn_updates_saved_per_frame": plain["gn_updates_mean"] - learned["gn_updates_mean"],
+                    "train_pairs": a.train_pairs, "pair_generation_s": gen_s, "epochs": a.epochs,
+                    "train_s": train_s, "train_steps": train_steps, "loss_first": losses[0],
+                    "loss_last": losses[-1], "network": f"{L}-{a.hidden}-{a.hidden}-{round_up(E, 128)} GELU",
+                    "train_tflops": mlp_flops / train_s / 1e12},
+        "plain_gn_batched": plain,
+        "plain_gn_single_frame": single,
+        "learned_vs_plain_batched": learned["value"] / plain["value"],
+        "learned_vs_plain_single_frame": (learned["value"] / single["value"]) if single else None,
         "spmv_gbs": float(gbs[0]),
         "cg_kernel_ms": {k: float(v) for k, v in zip(names, ms)},
         "cg_kernel_gbs": {k: float(v) for k, v in zip(names, gbs)},

@@ -59,6 +59,8 @@ def parse_args():
                    help="Tikhonov lambda relative to the RMS row norm of J at the reference")
     p.add_argument("--max-gn", type=int, default=10)
     p.add_argument("--tol", type=float, default=1e-5, help="CG relative tolerance of the GN forward solves")
+    p.add_argument("--preconditioner", choices=["jacobi", "two-level"], default="two-level",
+                   help="CG preconditioner of every GPU solve (jacobi = the reference's)")
     p.add_argument("--cpu-threads", type=int, default=0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cg-shapes", type=str, default="",
@@ -339,12 +341,12 @@ def run_gb300(a):
     lib = mp.lib()
     # held-out frames and their noise-free measurements (untimed)
     truth = [synthetic_frames(cent, F, seed=1000 * (rank + 1) + s) for s in range(nsteps)]
-    ref_opts = mp.SolveOptions(tol=1e-5, refine_tol=1e-9, max_iter=6000)
+    ref_opts = mp.SolveOptions(tol=1e-5, refine_tol=1e-9, max_iter=6000, preconditioner=a.preconditioner)
     vmeas = [model.solve(torch.tensor(truth[s], device=dev), ref_opts).contiguous() for s in range(nsteps)]
-    _, J0 = model.solve(torch.zeros((1, E), device=dev), mp.SolveOptions(tol=a.tol), jacobian=True)
+    opts = mp.SolveOptions(tol=a.tol, max_iter=6000, preconditioner=a.preconditioner)
+    _, J0 = model.solve(torch.zeros((1, E), device=dev), opts, jacobian=True)
     lam = a.lam_rel * float(J0.norm() / np.sqrt(J0.shape[1]))
     del J0
-    opts = mp.SolveOptions(tol=a.tol, max_iter=6000)
 
     # learned warm start: pairs from the forward solver, training on the GPU (untimed, reported)
     t0 = time.perf_counter()
@@ -458,6 +460,7 @@ def run_gb300(a):
                 "training pairs from the forward model with 60 dB noise)",
         "config": workload_config(a, F),
         "method": "learned warm start + batched GN (plain GN fallback per frame)",
+        "cg_preconditioner": a.preconditioner,
         "gn_updates_mean": learned["gn_updates_mean"],
         "frames_converged_fraction": learned["frames_converged_fraction"],
         "learned": {"accepted_fraction": accepted,

@@ -166,6 +166,13 @@ typedef struct mpf_solve_opts {
     int32_t max_refine;    /* outer refinement steps (default 6) */
     int32_t warm_start;    /* 1: start from the fields left by the previous call */
     int32_t check_every;   /* iterations between host convergence checks (default 16) */
+    /* 0: Jacobi (the reference's preconditioner::diagonal,
+     *    src/numeric/preconditioner.cpp:59-76);
+     * 1: two-level -- Jacobi plus an exact coarse correction on aggregates of
+     *    64 consecutive (Morton-ordered) nodes, M^-1 = D^-1 + P (P^T A P)^-1 P^T.
+     *    Same solutions, fewer iterations; needs <= 64 distinct excitation
+     *    columns and <= 32768 nodes, otherwise Jacobi is used. */
+    int32_t preconditioner;
 } mpf_solve_opts;
 
 typedef struct mpf_solve_stats {

@@ -131,6 +131,32 @@ __device__ __forceinline__ double sum_partials(const double* part, int g, int KP
     return s;
 }
 
+// Restriction P^T v of one 128-row tile for the two-level preconditioner:
+// the rows of warps 0-3 form aggregate 2 * tile, those of warps 4-7
+// aggregate 2 * tile + 1 (kAgg = 64).  Every thread passes its sum over the
+// rows it handled; the block adds them in a fixed order and writes
+// out[agg][KP].  Called by all threads of the block.
+template <int KP, int VEC>
+__device__ __forceinline__ void restrict_tile(const float (&part)[VEC], int tile, int nc, float* __restrict__ out,
+                                              float* red) {
+    using Sh = Shape<KP, VEC>;
+    static_assert(kAgg * 2 == kRowTile && kRowsPerWarp * 4 == kAgg, "aggregate = 4 warps of rows");
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+#pragma unroll
+    for (int v = 0; v < VEC; ++v) red[(warp * Sh::SUB + sub) * KP + j0 + v] = part[v];
+    __syncthreads();
+    if (threadIdx.x < 2 * KP) {
+        const int half = threadIdx.x / KP, j = threadIdx.x % KP;
+        float s = 0.f;
+        for (int w = half * 4; w < half * 4 + 4; ++w)
+            for (int u = 0; u < Sh::SUB; ++u) s += red[(w * Sh::SUB + u) * KP + j];
+        const int agg = tile * 2 + half;
+        if (agg < nc) out[(size_t)agg * KP + j] = s;
+    }
+    __syncthreads();
+}
+
 // y[i] = (S + alpha R) x over the rows row[i].  The first kWFast slots are
 // unrolled in three independent batches -- all column loads, then all value
 // loads and gathers -- so a warp waits for one memory latency per batch
@@ -215,6 +241,7 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
         for (int v = 0; v < VEC; ++v) sx[v] = (float)((double)P.dcScale * P.sumX0[(size_t)g * KP + j0 + v]);
     }
     DotAcc acc[3][VEC];
+    float rsum[VEC] = {}, bsum[VEC] = {};
     const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
     for (int st = 0; st < Sh::STEPS; st += RB) {
         int row[RB];
@@ -244,13 +271,33 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
                 acc[0][v].add(rv[v], zv[v]);
                 acc[1][v].add(bv[v], di * bv[v]);
                 if (dc && real) acc[2][v].add(zv[v], 1.f);
+                rsum[v] += real ? rv[v] : 0.f;
+                bsum[v] += real ? bv[v] : 0.f;
             }
             stv<VEC>(P.r + vb + (size_t)row[i] * KP + j0, rv);
-            stv<VEC>(P.p + vb + (size_t)row[i] * KP + j0, zv);
+            if (!P.coarse) stv<VEC>(P.p + vb + (size_t)row[i] * KP + j0, zv);
         }
+    }
+    if (P.coarse) {
+        __shared__ float red[kWarps * 32 * VEC];
+        const size_t cb = (size_t)g * P.ncPad * KP;
+        restrict_tile<KP, VEC>(rsum, blockIdx.x, P.nc, P.rc + cb, red);
+        restrict_tile<KP, VEC>(bsum, blockIdx.x, P.nc, P.rcB + cb, red);
     }
     double* const parts[3] = {P.partA, P.partB, P.partC};
     if (block_partials<KP, VEC, 3>(acc, parts, g, P.counter)) {
+        if (P.coarse) {
+            // the coarse kernel completes r^T M^-1 r and b^T M^-1 b and sets the masks
+            if (threadIdx.x < KP) {
+                P.rzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x);
+                P.bzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partB, g, KP, threadIdx.x);
+            }
+            if (threadIdx.x == 0) {
+                P.iters[g] = 0;
+                P.counter[g] = 0;
+            }
+            return;
+        }
         int notConv = 0;
         if (threadIdx.x < KP) {
             const int j = threadIdx.x;
@@ -345,6 +392,8 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
         a[v] = (!P.conv[s] && pq != 0.0) ? (float)(P.rz[s] / pq) : 0.f;
     }
     DotAcc acc[1][VEC];
+    float rsum[VEC] = {};
+    __shared__ float red[kWarps * 32 * VEC];
     const int tile0 = blockIdx.x * P.tiles[1];
     const int nsteps = (min(P.nblk, tile0 + P.tiles[1]) - tile0) * Sh::STEPS;
     for (int st = 0; st < nsteps; st += RB) {
@@ -369,13 +418,24 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
                 xv[i][v] = fmaf(a[v], pv[i][v], xv[i][v]);
                 rv[i][v] = fmaf(-a[v], qv[i][v], rv[i][v]);
                 acc[0][v].add(rv[i][v], di[i] * rv[i][v]);
+                rsum[v] += rv[i][v];  // padding rows keep r = 0
             }
             stv<VEC>(P.x + o[i], xv[i]);
             stv<VEC>(P.r + o[i], rv[i]);
         }
+        if (P.coarse && (st % Sh::STEPS) + RB == Sh::STEPS) {
+            restrict_tile<KP, VEC>(rsum, tile0 + st / Sh::STEPS, P.nc, P.rc + (size_t)g * P.ncPad * KP, red);
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) rsum[v] = 0.f;
+        }
     }
     double* const parts[1] = {P.partA};
     if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter)) {
+        if (P.coarse) {
+            if (threadIdx.x < KP) P.rzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x);
+            if (threadIdx.x == 0) P.counter[g] = 0;
+            return;
+        }
         int notConv = 0;
         if (threadIdx.x < KP) {
             const size_t s = (size_t)g * KP + threadIdx.x;
@@ -417,8 +477,8 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
 #pragma unroll
     for (int v = 0; v < VEC; ++v) {
         const size_t s = (size_t)g * KP + j0 + v;
-        live[v] = !P.conv[s];
-        be[v] = (float)P.beta[s];
+        live[v] = P.first || !P.conv[s];
+        be[v] = P.first ? 0.f : (float)P.beta[s];
     }
     DotAcc acc[1][VEC];
     const int tile0 = blockIdx.x * P.tiles[2];
@@ -426,21 +486,29 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
     for (int st = 0; st < nsteps; st += RB) {
         const int rowBase = (tile0 + st / Sh::STEPS) * kRowTile + warp * kRowsPerWarp +
                             (st % Sh::STEPS) * Sh::SUB + sub;
-        float rv[RB][VEC], pv[RB][VEC], di[RB];
+        float rv[RB][VEC], pv[RB][VEC], di[RB], yv[VEC] = {};
         int row[RB];
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
             row[i] = rowBase + i * Sh::SUB;
             const size_t o = vb + (size_t)row[i] * KP + j0;
             ldv<VEC>(P.r + o, rv[i]);
-            ldv<VEC>(P.p + o, pv[i]);
+            if (P.first) {
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) pv[i][v] = 0.f;
+            } else {
+                ldv<VEC>(P.p + o, pv[i]);
+            }
             di[i] = diag_inv(SR, P.diagSlot, P.npad, row[i], alpha);
         }
+        // coarse correction: all rows of a warp step lie in one aggregate
+        if (P.coarse && rowBase < P.n) ldv<VEC>(P.yc + ((size_t)g * P.ncPad + rowBase / kAgg) * KP + j0, yv);
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
-                pv[i][v] = live[v] ? fmaf(be[v], pv[i][v], di[i] * rv[i][v]) : pv[i][v];
+                const float z = fmaf(di[i], rv[i][v], row[i] < P.n ? yv[v] : 0.f);
+                pv[i][v] = live[v] ? fmaf(be[v], pv[i][v], z) : pv[i][v];
                 if (dc && row[i] < P.n) acc[0][v].add(pv[i][v], 1.f);
             }
             stv<VEC>(P.p + vb + (size_t)row[i] * KP + j0, pv[i]);
@@ -668,8 +736,17 @@ bool cg_variant_valid(int KP, int which, int v) { return variant_kernel(KP, whic
 
 int cg_default_variant(int KP) { return KP <= 64 ? 1 : 0; }  // VEC 4, RB 2 (KP 128: RB 1)
 
+static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count);
+
+// Start of a solve: r0, and with the two-level preconditioner the coarse
+// solve and p0 = M^-1 r0 (the direction kernel with beta = 0).
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s) {
-    return dispatch_kp<InitL>(P.KP, P, zeroGuess, s);
+    MPF_TRY(dispatch_kp<InitL>(P.KP, P, zeroGuess, s));
+    if (!P.coarse) return MPF_OK;
+    MPF_TRY(cg_launch_coarse(P, true, s));
+    CgProblem Q = P;
+    Q.first = 1;
+    return launch_one(Q, 2, s, true);
 }
 
 // One CG iteration with the problem's chosen variants; `count` says whether
@@ -690,9 +767,13 @@ static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count)
 }
 
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s) {
-    for (int which = 0; which < 3; ++which) MPF_TRY(launch_one(P, which, s, false));
-    return MPF_OK;
+    MPF_TRY(launch_one(P, 0, s, false));
+    MPF_TRY(launch_one(P, 1, s, false));
+    if (P.coarse) MPF_TRY(cg_launch_coarse(P, false, s, false));
+    return launch_one(P, 2, s, false);
 }
+
+int cg_iteration_launches(const CgProblem& P) { return P.coarse ? 4 : 3; }
 
 int cg_launch_kernel(const CgProblem& P, int which, cudaStream_t s) { return launch_one(P, which, s, true); }
 

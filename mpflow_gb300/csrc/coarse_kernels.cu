@@ -1,0 +1,267 @@
+// Two-level preconditioner of the batched CG:
+//   M^-1 = D^-1 + P (P^T A P)^-1 P^T
+// with P the piecewise-constant prolongation from aggregates of kAgg = 64
+// consecutive rows.  The rows are in Morton order (model.cu), so an
+// aggregate is a compact patch of the mesh and the coarse space carries the
+// smooth error that Jacobi-preconditioned CG reduces slowest.  No reference
+// counterpart: the reference preconditions with the diagonal only
+// (src/numeric/preconditioner.cpp:59-76); the solutions are the same, the
+// iteration counts are not.
+//
+// Setup, once per assembled matrix (k_coarse_assemble / k_coarse_fixup, the
+// batched FP64 Cholesky of dense_kernels.cu, k_coarse_prep): the coarse
+// matrix of every (frame, harmonic) group in FP64, its Cholesky factor, and
+// an FP32 copy of the factor with inverted 32x32 diagonal blocks.
+// Per CG iteration, k_coarse (one CTA per group): (P^T A P) y = P^T r by
+// blocked forward / backward substitution in shared memory, y written for
+// the direction kernel, (P^T r).y added to r^T D^-1 r, then the CG scalars
+// and convergence masks of the group.
+#include <algorithm>
+
+#include "model.h"
+
+namespace mpf {
+namespace {
+
+constexpr int kCT = 256;  // threads of k_coarse
+
+// A_c[g][I][J] = sum over the slots of rows in aggregate I whose column lies
+// in aggregate J of (S + alpha R), FP64, fixed order.
+__global__ void k_coarse_assemble(CgProblem P, CoarsePlan cp, double* __restrict__ Ac) {
+    const int g = blockIdx.y;
+    const int f = g / P.Ca, ci = g % P.Ca;
+    const double alpha = (double)P.alpha[ci];
+    const float2* SR = P.SR + (size_t)f * P.W * P.npad;
+    double* A = Ac + (size_t)g * cp.ncPad * cp.ncPad;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cp.nnz; t += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = cp.pairPtr[t]; k < cp.pairPtr[t + 1]; ++k) {
+            const float2 e = __ldg(&SR[cp.slots[k]]);
+            s += (double)e.x + alpha * (double)e.y;
+        }
+        A[(size_t)cp.pairI[t] * cp.ncPad + cp.pairJ[t]] = s;
+    }
+}
+
+// Neumann groups: + c' |I| |J| (the coarse image of c' 1 1^T); padding
+// aggregates get an identity block.
+__global__ void k_coarse_fixup(CgProblem P, CoarsePlan cp, double* __restrict__ Ac) {
+    const int g = blockIdx.y;
+    const bool dc = P.dcFree[g % P.Ca] != 0;
+    double* A = Ac + (size_t)g * cp.ncPad * cp.ncPad;
+    const size_t total = (size_t)cp.ncPad * cp.ncPad;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int I = (int)(t / cp.ncPad), J = (int)(t % cp.ncPad);
+        if (I < cp.nc && J < cp.nc) {
+            if (dc) A[t] += (double)P.dcScale * (double)cp.aggSize[I] * (double)cp.aggSize[J];
+        } else if (I == J) {
+            A[t] = 1.0;
+        }
+    }
+}
+
+// FP64 Cholesky factor (column-major lower) -> FP32 row-major lower factor
+// and the inverses of its 32x32 diagonal blocks.  One warp per (block row,
+// group); lane c inverts column c by forward substitution.
+__global__ void __launch_bounds__(32) k_coarse_prep(int ncPad, const double* __restrict__ L64,
+                                                    float* __restrict__ Lc, float* __restrict__ LinvD) {
+    const int bi = blockIdx.x, g = blockIdx.y, lane = threadIdx.x;
+    const double* L = L64 + (size_t)g * ncPad * ncPad;
+    float* Lf = Lc + (size_t)g * ncPad * ncPad;
+    for (int r = 0; r < 32; ++r) {
+        const int row = bi * 32 + r;
+        for (int c = lane; c < ncPad; c += 32) Lf[(size_t)row * ncPad + c] = c <= row ? (float)L[row + (size_t)c * ncPad] : 0.f;
+    }
+    __shared__ double B[32][33];
+    for (int r = 0; r < 32; ++r) B[r][lane] = lane <= r ? L[(bi * 32 + r) + (size_t)(bi * 32 + lane) * ncPad] : 0.0;
+    __syncwarp();
+    double x[32];
+    for (int r = 0; r < 32; ++r) {
+        double s = r == lane ? 1.0 : 0.0;
+        for (int k = lane; k < r; ++k) s -= B[r][k] * x[k];
+        x[r] = r < lane ? 0.0 : s / B[r][r];
+    }
+    float* D = LinvD + ((size_t)g * (ncPad / 32) + bi) * 1024;
+    for (int r = 0; r < 32; ++r) D[r * 32 + lane] = (float)x[r];
+}
+
+// (L L^T) y = rhs in shared memory: y holds rhs on entry (row stride KP + 1),
+// the solution on exit.  Thread (r, c0) owns row r of the current 32-row
+// block and the right-hand sides c0, c0 + 8, ...
+template <int KP>
+__device__ void coarse_solve(const float* __restrict__ L, const float* __restrict__ Dv, int ncPad, float* y,
+                             float* tmp, float (*Ls)[33]) {
+    constexpr int YS = KP + 1, CPT = KP / 8;
+    const int r = threadIdx.x & 31, c0 = threadIdx.x >> 5;
+    const int nb = ncPad / 32;
+    // forward: L z = rhs
+    for (int bi = 0; bi < nb; ++bi) {
+        float acc[CPT];
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) acc[q] = 0.f;
+        for (int bj = 0; bj < bi; ++bj) {
+            for (int t = threadIdx.x; t < 1024; t += kCT)
+                Ls[t >> 5][t & 31] = __ldg(&L[(size_t)(bi * 32 + (t >> 5)) * ncPad + bj * 32 + (t & 31)]);
+            __syncthreads();
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k) {
+                const float l = Ls[r][k];
+                const float* yk = y + (bj * 32 + k) * YS + c0;
+#pragma unroll
+                for (int q = 0; q < CPT; ++q) acc[q] = fmaf(l, yk[8 * q], acc[q]);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) tmp[r * YS + c0 + 8 * q] = y[(bi * 32 + r) * YS + c0 + 8 * q] - acc[q];
+        for (int t = threadIdx.x; t < 1024; t += kCT) Ls[t >> 5][t & 31] = __ldg(&Dv[bi * 1024 + t]);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) {
+            float s = 0.f;
+            for (int k = 0; k <= r; ++k) s = fmaf(Ls[r][k], tmp[k * YS + c0 + 8 * q], s);
+            y[(bi * 32 + r) * YS + c0 + 8 * q] = s;
+        }
+        __syncthreads();
+    }
+    // backward: L^T x = z
+    for (int bi = nb - 1; bi >= 0; --bi) {
+        float acc[CPT];
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) acc[q] = 0.f;
+        for (int bj = bi + 1; bj < nb; ++bj) {
+            for (int t = threadIdx.x; t < 1024; t += kCT)
+                Ls[t >> 5][t & 31] = __ldg(&L[(size_t)(bj * 32 + (t >> 5)) * ncPad + bi * 32 + (t & 31)]);
+            __syncthreads();
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k) {
+                const float l = Ls[k][r];
+                const float* yk = y + (bj * 32 + k) * YS + c0;
+#pragma unroll
+                for (int q = 0; q < CPT; ++q) acc[q] = fmaf(l, yk[8 * q], acc[q]);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) tmp[r * YS + c0 + 8 * q] = y[(bi * 32 + r) * YS + c0 + 8 * q] - acc[q];
+        for (int t = threadIdx.x; t < 1024; t += kCT) Ls[t >> 5][t & 31] = __ldg(&Dv[bi * 1024 + t]);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) {
+            float s = 0.f;
+            for (int k = r; k < 32; ++k) s = fmaf(Ls[k][r], tmp[k * YS + c0 + 8 * q], s);
+            y[(bi * 32 + r) * YS + c0 + 8 * q] = s;
+        }
+        __syncthreads();
+    }
+}
+
+template <int KP>
+__global__ void __launch_bounds__(kCT) k_coarse(CgProblem P, int init) {
+    static_assert(KP % 8 == 0 && kCT % KP == 0, "right-hand sides per thread");
+    const int g = blockIdx.x;
+    if (!init && !P.active[g]) return;
+    constexpr int YS = KP + 1;
+    extern __shared__ float smc[];
+    float* y = smc;                         // [ncPad][YS]
+    float* tmp = y + (size_t)P.ncPad * YS;  // [32][YS]
+    float(*Ls)[33] = reinterpret_cast<float(*)[33]>(tmp + 32 * YS);
+    __shared__ double cdot[2][kCT];
+    const float* L = P.Lc + (size_t)g * P.ncPad * P.ncPad;
+    const float* Dv = P.LinvD + (size_t)g * (P.ncPad / 32) * 1024;
+    const size_t cb = (size_t)g * P.ncPad * KP;
+    constexpr int parts = kCT / KP;
+    const int j = threadIdx.x % KP, part = threadIdx.x / KP;
+    for (int sys = 0; sys < (init ? 2 : 1); ++sys) {
+        const float* src = (sys == 0 ? P.rc : P.rcB) + cb;
+        for (int t = threadIdx.x; t < P.ncPad * KP; t += kCT) y[(t / KP) * YS + t % KP] = src[t];
+        __syncthreads();
+        coarse_solve<KP>(L, Dv, P.ncPad, y, tmp, Ls);
+        double d = 0.0;
+        for (int I = part; I < P.nc; I += parts) d += (double)src[(size_t)I * KP + j] * (double)y[I * YS + j];
+        cdot[sys][threadIdx.x] = d;
+        if (sys == 0)
+            for (int t = threadIdx.x; t < P.ncPad * KP; t += kCT) P.yc[cb + t] = y[(t / KP) * YS + t % KP];
+        __syncthreads();
+    }
+    int notConv = 0;
+    if (threadIdx.x < KP) {
+        const size_t s = (size_t)g * KP + threadIdx.x;
+        double c0 = 0.0, c1 = 0.0;
+        for (int q = 0; q < parts; ++q) {
+            c0 += cdot[0][q * KP + threadIdx.x];
+            if (init) c1 += cdot[1][q * KP + threadIdx.x];
+        }
+        if (init) {
+            const double rz = P.rzFine[s] + c0, bz = P.bzFine[s] + c1;
+            P.rz[s] = rz;
+            P.bz[s] = bz;
+            P.beta[s] = 0.0;
+            const int c = rz <= P.tol2 * bz;
+            P.conv[s] = c;
+            notConv = !c;
+        } else if (!P.conv[s]) {
+            const double rzn = P.rzFine[s] + c0, rzo = P.rz[s];
+            P.beta[s] = rzo != 0.0 ? rzn / rzo : 0.0;
+            P.rz[s] = rzn;
+            const int c = rzn <= P.tol2 * P.bz[s];
+            P.conv[s] = c;
+            notConv = !c;
+        }
+    }
+    const int any = __syncthreads_or(notConv);
+    if (threadIdx.x == 0) {
+        P.active[g] = any;
+        if (!init) P.iters[g] += 1;
+    }
+}
+
+size_t coarse_smem(int ncPad, int KP) { return ((size_t)(ncPad + 32) * (KP + 1) + 32 * 33) * sizeof(float); }
+
+template <int KP>
+int launch_coarse_kp(const CgProblem& P, bool init, cudaStream_t s, bool count) {
+    const size_t smem = coarse_smem(P.ncPad, KP);
+    static size_t configured = 0;
+    if (smem > configured) {
+        MPF_CUDA(cudaFuncSetAttribute(k_coarse<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    k_coarse<KP><<<P.G, kCT, smem, s>>>(P, init ? 1 : 0);
+    if (count) {
+        MPF_LAUNCHED(1);
+    } else {
+        MPF_CUDA(cudaGetLastError());
+    }
+    return MPF_OK;
+}
+
+}  // namespace
+
+bool coarse_supported(int KP, int ncPad) {
+    return (KP == 16 || KP == 32 || KP == 64) && ncPad >= 32 && ncPad % 32 == 0 &&
+           coarse_smem(ncPad, KP) <= 200 * 1024;
+}
+
+int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count) {
+    switch (P.KP) {
+        case 16: return launch_coarse_kp<16>(P, init, s, count);
+        case 32: return launch_coarse_kp<32>(P, init, s, count);
+        case 64: return launch_coarse_kp<64>(P, init, s, count);
+        default: return fail(MPF_EINVAL, "two-level preconditioner: unsupported right-hand-side width %d", P.KP);
+    }
+}
+
+int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,
+                        float* Lc, float* LinvD) {
+    const size_t per = (size_t)cp.ncPad * cp.ncPad;
+    MPF_CUDA(cudaMemsetAsync(Ac64, 0, sizeof(double) * per * P.G, s));
+    k_coarse_assemble<<<dim3((cp.nnz + 255) / 256, P.G), 256, 0, s>>>(P, cp, Ac64);
+    k_coarse_fixup<<<dim3((int)std::min<size_t>((per + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64);
+    MPF_LAUNCHED(2);
+    MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s));
+    k_coarse_prep<<<dim3(cp.ncPad / 32, P.G), 32, 0, s>>>(cp.ncPad, Ac64, Lc, LinvD);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+}  // namespace mpf

@@ -56,15 +56,16 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
 }
 
 // slot-major [W][npad] -> reference ELL [dataRows][32] (same slot order)
+// (rowOf maps a reference node number to the internal row)
 __global__ void k_export_ell(int W, int npad, int n, int dataRows, const float2* __restrict__ src, int component,
-                             float* __restrict__ dst) {
+                             const int32_t* __restrict__ rowOf, float* __restrict__ dst) {
     const int f = blockIdx.y;
     const size_t total = (size_t)dataRows * kEllWidth;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int row = (int)(i / kEllWidth), slot = (int)(i % kEllWidth);
         float v = 0.f;
         if (row < n && slot < W) {
-            const float2 e = src[(size_t)f * W * npad + (size_t)slot * npad + row];
+            const float2 e = src[(size_t)f * W * npad + (size_t)slot * npad + rowOf[row]];
             v = component == 0 ? e.x : e.y;
         }
         dst[(size_t)f * total + i] = v;
@@ -228,7 +229,8 @@ __global__ void k_transpose(int rowsJ, int Epad, int E, const float* __restrict_
 __global__ void k_fields_export(int F, int Ca, int C, const int32_t* __restrict__ compOf, int npad, int KP,
                                 int dataRows, int cols, const int32_t* __restrict__ colU,
                                 const float* __restrict__ colScale, const float* __restrict__ betaC,
-                                const float* __restrict__ X, float* __restrict__ out, int n) {
+                                const float* __restrict__ X, const int32_t* __restrict__ rowOf,
+                                float* __restrict__ out, int n) {
     const size_t per = (size_t)dataRows * cols;
     const size_t total = (size_t)F * C * per;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
@@ -239,7 +241,7 @@ __global__ void k_fields_export(int F, int Ca, int C, const int32_t* __restrict_
         const int ci = compOf[c];
         float v = 0.f;
         if (ci >= 0 && node < n)
-            v = betaC[c] * colScale[col] * X[(((size_t)f * Ca + ci) * npad + node) * KP + colU[col]];
+            v = betaC[c] * colScale[col] * X[(((size_t)f * Ca + ci) * npad + rowOf[node]) * KP + colU[col]];
         out[i] = v;
     }
 }
@@ -351,9 +353,9 @@ int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, cons
 }
 
 int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float2* SR, int component,
-                          float* refLayout, cudaStream_t s) {
+                          const int32_t* rowOf, float* refLayout, cudaStream_t s) {
     int blocks = (int)std::min<size_t>(((size_t)dataRows * kEllWidth + 255) / 256, 4096);
-    k_export_ell<<<dim3(blocks, F), 256, 0, s>>>(W, npad, n, dataRows, SR, component, refLayout);
+    k_export_ell<<<dim3(blocks, F), 256, 0, s>>>(W, npad, n, dataRows, SR, component, rowOf, refLayout);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }
@@ -418,9 +420,10 @@ int fem_launch_transpose_jacobian(int F, int rowsJ, int Epad, int E, const float
 
 int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int npad, int KP, int dataRows,
                                int cols, int n, const int32_t* colU, const float* colScale,
-                               const float* betaC, const float* X, float* out, cudaStream_t s) {
+                               const float* betaC, const float* X, const int32_t* rowOf, float* out,
+                               cudaStream_t s) {
     k_fields_export<<<2048, 256, 0, s>>>(F, Ca, C, compOf, npad, KP, dataRows, cols, colU, colScale, betaC, X,
-                                         out, n);
+                                         rowOf, out, n);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

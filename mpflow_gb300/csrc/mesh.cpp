@@ -10,8 +10,12 @@
 //                       (src/fem/equation.cpp:76-176) plus this library's
 //                       slot-major layout and per-slot assembly lists
 //  * excitation_matrix -- Equation::initExcitationMatrix, src/fem/equation.cpp:183-215
+//  * morton_order    -- this library's internal node order (no reference
+//                       counterpart: the reference keeps the mesh order)
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <numeric>
 #include <unordered_map>
 
 #include "mpf_internal.h"
@@ -305,6 +309,34 @@ void excitation_matrix(int N, const double* nodes, const int32_t* edges, int por
             exc[b + (size_t)port * ld] += half / portLength;
         }
     }
+}
+
+static uint32_t spread_bits16(uint32_t v) {
+    v &= 0xFFFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+
+void morton_order(int N, const double* nodes, int32_t* perm) {
+    double x0 = 1e300, y0 = 1e300, x1 = -1e300, y1 = -1e300;
+    for (int i = 0; i < N; ++i) {
+        x0 = std::min(x0, nodes[2 * i]);
+        x1 = std::max(x1, nodes[2 * i]);
+        y0 = std::min(y0, nodes[2 * i + 1]);
+        y1 = std::max(y1, nodes[2 * i + 1]);
+    }
+    const double span = std::max(std::max(x1 - x0, y1 - y0), 1e-300);
+    std::vector<uint32_t> code(N);
+    for (int i = 0; i < N; ++i) {
+        const uint32_t qx = (uint32_t)std::lround((nodes[2 * i] - x0) / span * 65535.0);
+        const uint32_t qy = (uint32_t)std::lround((nodes[2 * i + 1] - y0) / span * 65535.0);
+        code[i] = spread_bits16(qx) | (spread_bits16(qy) << 1);
+    }
+    std::iota(perm, perm + N, 0);
+    std::stable_sort(perm, perm + N, [&](int32_t a, int32_t b) { return code[a] < code[b]; });
 }
 
 }  // namespace mpf

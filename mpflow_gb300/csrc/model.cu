@@ -2,6 +2,7 @@
 // orchestration of the forward solve (EIT::solve, src/models/eit.cpp:139-213)
 // and of one regularised Gauss-Newton step (Solver::solveAbsolute,
 // src/solver/solver.cpp:196-225 with Inverse, src/solver/inverse.cpp:60-238).
+#include <algorithm>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -26,6 +27,7 @@ struct mpf_eit {
     std::vector<double> betaAll;      // per component
     // device: static structure
     mpf::DevBuf<int32_t> cols, diagSlot, cptr, contrib, elements;
+    mpf::DevBuf<int32_t> rowOf;       // internal row of each node (Morton order, see eit_create)
     mpf::DevBuf<float> Kf, Mf;
     mpf::DevBuf<double> Kd, Md64;
     mpf::DevBuf<float> Bc;            // [Ca][npad][KP] right-hand sides per active harmonic
@@ -63,6 +65,14 @@ struct mpf_eit {
     // or fixed by the caller (-1 = autotune)
     std::map<int, std::array<int, 3>> cgVariants;
     std::array<int, 3> forcedVariants{-1, -1, -1};
+    // two-level preconditioner: aggregate plan (static) and per-frame-count workspace
+    int nc = 0, ncPad = 0, coarseOK = 0, capFC = 0;
+    mpf::DevBuf<int32_t> cPairI, cPairJ, cPairPtr, cSlots;
+    mpf::DevBuf<float> cAggSize;
+    int cNnz = 0;
+    mpf::DevBuf<double> Ac64, rzFine, bzFine;
+    mpf::DevBuf<float> Lc, LinvD, rcV, rcB, ycV;
+    mpf::DevBuf<int> infoC;
     // learned warm start: homogeneous voltages and the network input
     bool v0Ready = false;
     float v0InvRms = 1.f;
@@ -124,8 +134,26 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     m->height = d->height;
     m->portHeight = d->port_height;
 
+    // ---- internal node order: Morton (Z-order) of the coordinates, so that
+    // consecutive rows are spatially compact patches (SpMM gathers stay in
+    // L1, and the two-level preconditioner's aggregates of consecutive rows
+    // are compact).  Elements keep their order; every node-indexed export
+    // maps back through rowOf.
+    std::vector<int32_t> perm(m->n), rowOf(m->n);
+    morton_order(m->n, d->nodes, perm.data());
+    for (int i = 0; i < m->n; ++i) rowOf[perm[i]] = i;
+    std::vector<int32_t> elems((size_t)3 * m->E);
+    for (size_t k = 0; k < elems.size(); ++k) elems[k] = rowOf[d->elements[k]];
+    std::vector<int32_t> edgesP((size_t)2 * d->n_edges);
+    for (size_t k = 0; k < edgesP.size(); ++k) edgesP[k] = rowOf[d->edges[k]];
+    std::vector<double> nodesP((size_t)2 * m->n);
+    for (int i = 0; i < m->n; ++i) {
+        nodesP[2 * i] = d->nodes[2 * (size_t)perm[i]];
+        nodesP[2 * i + 1] = d->nodes[2 * (size_t)perm[i] + 1];
+    }
+
     // ---- FEM structure and elemental integrals
-    MPF_TRY(build_structure(m->n, m->E, d->elements, m->fs));
+    MPF_TRY(build_structure(m->n, m->E, elems.data(), m->fs));
     m->dataRows = m->fs.dataRows;
     m->npad = m->fs.npad;
     m->nblk = m->npad / kRowTile;
@@ -138,7 +166,7 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
 
     // ---- excitation matrix and unique right-hand sides
     std::vector<double> exc((size_t)m->n * m->L);
-    excitation_matrix(m->n, d->nodes, d->edges, m->L, d->port_edges, d->port_edges_cap, exc.data(), m->n);
+    excitation_matrix(m->n, nodesP.data(), edgesP.data(), m->L, d->port_edges, d->port_edges_cap, exc.data(), m->n);
     const int L = m->L, Md = m->Md, Mm = m->Mm;
     std::vector<std::vector<double>> canon;  // canonical pattern columns
     auto unique_of = [&](const std::vector<double>& col, int& u, float& scale) {
@@ -275,7 +303,6 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
         massCoef[ci] = m->exactJacobian ? m->alphaH[ci] : 0.f;
     }
     for (int c = 0; c < m->C; ++c) betaC[c] = m->compOf[c] >= 0 ? (float)m->betaAll[c] : 0.f;
-    std::vector<int32_t> elems(d->elements, d->elements + (size_t)3 * m->E);
 
     // ---- upload
     MPF_TRY(m->cols.upload(m->fs.cols));
@@ -283,6 +310,7 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     MPF_TRY(m->cptr.upload(m->fs.contribPtr));
     MPF_TRY(m->contrib.upload(m->fs.contrib));
     MPF_TRY(m->elements.upload(elems));
+    MPF_TRY(m->rowOf.upload(rowOf));
     MPF_TRY(m->Kf.upload(Kf));
     MPF_TRY(m->Mf.upload(Mf));
     MPF_TRY(m->Kd.upload(K));
@@ -308,6 +336,44 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     MPF_TRY(m->rowScale.upload(rowS));
     MPF_TRY(m->colU.upload(colU));
     MPF_TRY(m->colScale.upload(colS));
+
+    // ---- two-level preconditioner plan: aggregates of kAgg consecutive rows
+    // and, per nonzero aggregate pair (I, J), the matrix slots that sum into
+    // the coarse entry (padding slots excluded)
+    m->nc = (m->n + kAgg - 1) / kAgg;
+    m->ncPad = round_up(m->nc, 32);
+    m->coarseOK = coarse_supported(m->KP, m->ncPad) ? 1 : 0;
+    if (m->coarseOK) {
+        std::vector<std::vector<std::pair<int32_t, int32_t>>> byI(m->nc);
+        for (int r = 0; r < m->n; ++r)
+            for (int k = 0; k < m->W; ++k) {
+                const int32_t c = m->fs.cols[(size_t)k * P + r];
+                if (c == r && k != m->fs.diagSlot[r]) continue;
+                byI[r / kAgg].push_back({c / kAgg, (int32_t)((size_t)k * P + r)});
+            }
+        std::vector<int32_t> pI, pJ, pPtr{0}, slots;
+        for (int I = 0; I < m->nc; ++I) {
+            auto& v = byI[I];
+            std::sort(v.begin(), v.end());
+            for (size_t t = 0; t < v.size(); ++t) {
+                if (t == 0 || v[t].first != v[t - 1].first) {
+                    if (t > 0) pPtr.push_back((int32_t)slots.size());
+                    pI.push_back(I);
+                    pJ.push_back(v[t].first);
+                }
+                slots.push_back(v[t].second);
+            }
+            if (!v.empty()) pPtr.push_back((int32_t)slots.size());
+        }
+        std::vector<float> aggSize(m->nc);
+        for (int I = 0; I < m->nc; ++I) aggSize[I] = (float)std::min(kAgg, m->n - I * kAgg);
+        m->cNnz = (int)pI.size();
+        MPF_TRY(m->cPairI.upload(pI));
+        MPF_TRY(m->cPairJ.upload(pJ));
+        MPF_TRY(m->cPairPtr.upload(pPtr));
+        MPF_TRY(m->cSlots.upload(slots));
+        MPF_TRY(m->cAggSize.upload(aggSize));
+    }
     MPF_CUDA(cudaMallocHost(&m->pinnedActive, sizeof(int) * 4096));
     *out = m.release();
     return MPF_OK;
@@ -375,13 +441,34 @@ static int ensure_workspace(mpf_eit* m, int F, bool refine, bool jacobian) {
     return MPF_OK;
 }
 
+// Workspace of the two-level preconditioner for F frames (coarse vectors
+// start at zero: their padding aggregates are never written).
+static int ensure_coarse(mpf_eit* m, int F) {
+    if (F <= m->capFC) return MPF_OK;
+    const size_t G = (size_t)F * m->Ca, nc2 = (size_t)m->ncPad * m->ncPad, cv = G * m->ncPad * m->KP;
+    MPF_TRY(m->Ac64.alloc(G * nc2));
+    MPF_TRY(m->Lc.alloc(G * nc2));
+    MPF_TRY(m->LinvD.alloc(G * (m->ncPad / 32) * 1024));
+    MPF_TRY(m->rcV.alloc(cv));
+    MPF_TRY(m->rcB.alloc(cv));
+    MPF_TRY(m->ycV.alloc(cv));
+    MPF_CUDA(cudaMemset(m->rcV.ptr, 0, cv * sizeof(float)));
+    MPF_CUDA(cudaMemset(m->rcB.ptr, 0, cv * sizeof(float)));
+    MPF_CUDA(cudaMemset(m->ycV.ptr, 0, cv * sizeof(float)));
+    MPF_TRY(m->rzFine.alloc(G * m->KP));
+    MPF_TRY(m->bzFine.alloc(G * m->KP));
+    MPF_TRY(m->infoC.alloc(G));
+    m->capFC = F;
+    return MPF_OK;
+}
+
 // launch-shape code -> kernel variant and tiles per block
 static void set_shape(CgProblem& P, int which, int code) {
     P.variant[which] = code % kCgVariants;
     P.tiles[which] = 1 << (code / kCgVariants);
 }
 
-static CgProblem make_problem(mpf_eit* m, int F, double tol) {
+static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false) {
     CgProblem P{};
     P.n = m->n;
     P.npad = m->npad;
@@ -416,6 +503,18 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol) {
     P.iters = m->iters.ptr;
     P.counter = m->counter.ptr;
     P.tol2 = tol * tol;
+    if (coarse) {
+        P.coarse = 1;
+        P.nc = m->nc;
+        P.ncPad = m->ncPad;
+        P.rc = m->rcV.ptr;
+        P.rcB = m->rcB.ptr;
+        P.yc = m->ycV.ptr;
+        P.Lc = m->Lc.ptr;
+        P.LinvD = m->LinvD.ptr;
+        P.rzFine = m->rzFine.ptr;
+        P.bzFine = m->bzFine.ptr;
+    }
     auto it = m->cgVariants.find(F);
     for (int k = 0; k < 3; ++k) {
         int code = it != m->cgVariants.end() ? it->second[k] : cg_default_variant(m->KP);
@@ -505,7 +604,7 @@ static int run_cg(mpf_eit* m, const CgProblem& P, int maxIter, int checkEvery, c
     bool anyActive = true;
     while (done < maxIter) {
         MPF_CUDA(cudaGraphLaunch(exec, s));
-        add_launches(3LL * checkEvery);
+        add_launches((long long)cg_iteration_launches(P) * checkEvery);
         done += checkEvery;
         MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.active, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
         MPF_CUDA(cudaStreamSynchronize(s));
@@ -538,7 +637,9 @@ static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
     o.max_refine = 6;
     o.warm_start = 0;
     o.check_every = 16;
+    o.preconditioner = 0;
     if (in) o = *in;
+    if (o.preconditioner != 1) o.preconditioner = 0;
     if (o.tol <= 0.0) o.tol = 1e-6;
     if (o.max_iter <= 0) o.max_iter = 10 * n;
     if (o.max_refine <= 0) o.max_refine = 6;
@@ -556,8 +657,10 @@ int eit_assemble_export(mpf_eit* m, int F, const float* gamma, float* sOut, floa
     MPF_CHECK(F >= 1 && gamma, MPF_EINVAL, "mpf_eit_assemble: bad arguments");
     MPF_TRY(ensure_workspace(m, F, false, false));
     MPF_TRY(eit_assemble(m, F, gamma, false, s));
-    if (sOut) MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->SR.ptr, 0, sOut, s));
-    if (rOut) MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->SR.ptr, 1, rOut, s));
+    if (sOut)
+        MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->SR.ptr, 0, m->rowOf.ptr, sOut, s));
+    if (rOut)
+        MPF_TRY(fem_launch_export_ell(F, m->W, m->npad, m->n, m->dataRows, m->SR.ptr, 1, m->rowOf.ptr, rOut, s));
     return MPF_OK;
 }
 
@@ -572,7 +675,14 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     const bool warm = o.warm_start && m->fieldsValid && m->lastFrames == F;
     MPF_TRY(eit_assemble(m, F, gamma, refine, s));
     if (!warm) MPF_TRY(tune_cg(m, F, s));
-    CgProblem P = make_problem(m, F, o.tol);
+    const bool coarse = o.preconditioner == 1 && m->coarseOK;
+    if (coarse) MPF_TRY(ensure_coarse(m, F));
+    CgProblem P = make_problem(m, F, o.tol, coarse);
+    if (coarse) {
+        CoarsePlan cp{m->nc, m->ncPad, m->cNnz, m->cPairI.ptr, m->cPairJ.ptr, m->cPairPtr.ptr, m->cSlots.ptr,
+                      m->cAggSize.ptr};
+        MPF_TRY(coarse_launch_setup(P, cp, m->Ac64.ptr, m->infoC.ptr, s, m->Lc.ptr, m->LinvD.ptr));
+    }
     int totalIters = 0, notConv = 0, refinements = 0;
     double maxRel = 0.0;
     // fields are kept in the reference's convention; the iteration works on
@@ -624,6 +734,14 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
         if (maxRel > o.refine_tol) notConv = std::max(notConv, 1);
     }
     if (m->anyDcFree) MPF_TRY(cg_launch_dc_shift(P, m->dcShift.ptr, 1.f, s));
+    if (coarse) {
+        std::vector<int> info(P.G);
+        MPF_CUDA(cudaMemcpyAsync(info.data(), m->infoC.ptr, sizeof(int) * P.G, cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        for (int g = 0; g < P.G; ++g)
+            MPF_CHECK(info[g] == 0, MPF_EBREAKDOWN, "two-level preconditioner: coarse Cholesky failed at pivot %d "
+                      "(group %d)", info[g], g);
+    }
     m->fieldsValid = true;
     m->lastFrames = F;
     MeasPlan mp{(int)m->nzNode.count, m->nzNode.ptr, nullptr, m->nzVal.ptr, m->nzPtr.ptr};
@@ -665,7 +783,8 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
     MPF_CHECK(m->fieldsValid && F >= 1 && F <= m->lastFrames && out, MPF_EINVAL,
               "mpf_eit_fields: no forward solve with that many frames");
     MPF_TRY(fem_launch_fields_export(F, m->Ca, m->C, m->compOfD.ptr, m->npad, m->KP, m->dataRows, m->Md + m->Mm,
-                                     m->n, m->colU.ptr, m->colScale.ptr, m->betaC.ptr, m->X.ptr, out, s));
+                                     m->n, m->colU.ptr, m->colScale.ptr, m->betaC.ptr, m->X.ptr, m->rowOf.ptr, out,
+                                     s));
     return MPF_OK;
 }
 

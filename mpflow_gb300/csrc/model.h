@@ -52,7 +52,21 @@ struct CgProblem {
     // flight) and 128-row tiles per block
     int variant[3];
     int tiles[3];
+    // two-level preconditioner M^-1 = D^-1 + P (P^T A P)^-1 P^T over aggregates
+    // of kAgg consecutive rows (coarse == 0: Jacobi only)
+    int coarse;
+    int nc, ncPad;        // aggregates, padded to a multiple of 32
+    float* rc;            // [G][ncPad][KP] P^T r (restriction, written by k_update / k_init)
+    float* rcB;           // [G][ncPad][KP] P^T b (k_init, for b^T M^-1 b)
+    float* yc;            // [G][ncPad][KP] (P^T A P)^-1 P^T r
+    const float* Lc;      // [G][ncPad][ncPad] Cholesky factor of P^T A P, row-major lower, FP32
+    const float* LinvD;   // [G][ncPad/32][32][32] inverses of its diagonal blocks, row-major
+    double* rzFine;       // [G][KP] r^T D^-1 r of the last update / init
+    double* bzFine;       // [G][KP] b^T D^-1 b (init)
+    int first;            // k_direction: p = M^-1 r (start of an iteration)
 };
+
+constexpr int kAgg = 64;  // rows per coarse aggregate (divides kRowTile)
 
 // cg_kernels.cu
 // variant v = vecIdx * 3 + rbIdx, floats per lane {4, 2, 1}[vecIdx], row steps {1, 2, 4}[rbIdx];
@@ -62,7 +76,22 @@ constexpr int kCgTileChoices = 4;
 bool cg_variant_valid(int KP, int which, int v);
 int cg_default_variant(int KP);
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
+// coarse_kernels.cu
+struct CoarsePlan {
+    int nc, ncPad, nnz;              // aggregates, padded count, nonzero (I, J) pairs
+    const int32_t* pairI;            // [nnz]
+    const int32_t* pairJ;            // [nnz]
+    const int32_t* pairPtr;          // [nnz + 1] into slots
+    const int32_t* slots;            // slot indices k * npad + row
+    const float* aggSize;            // [nc] real rows per aggregate
+};
+int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,
+                        float* Lc, float* LinvD);
+// `count`: false while recording a CUDA graph (replays are counted by the caller)
+int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count = true);
+bool coarse_supported(int KP, int ncPad);
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s);
+int cg_iteration_launches(const CgProblem& P);
 int cg_launch_kernel(const CgProblem& P, int which /*0 spmm, 1 update, 2 direction*/, cudaStream_t s);
 int cg_launch_residual64(const CgProblem& P, const double* S64, const double* R64, const double* x64,
                          const double* b64, const double* sumX64, double* partR, double* partB, double* rr,
@@ -78,7 +107,7 @@ int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, cons
                         const float* gamma, float ref, int logarithmic, float2* SR, double* S64, double* R64,
                         cudaStream_t s);
 int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float2* SR, int component,
-                          float* refLayout, cudaStream_t s);
+                          const int32_t* rowOf, float* refLayout, cudaStream_t s);
 struct MeasPlan {
     int nnz;                 // nonzeros of the unique excitation columns
     const int32_t* nzNode;   // [nnz]
@@ -111,7 +140,8 @@ int fem_launch_transpose_jacobian(int F, int rowsJ, int Epad, int E, const float
                                   cudaStream_t s);
 int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int npad, int KP,
                              int dataRows, int cols, int n, const int32_t* colU, const float* colScale,
-                             const float* betaC, const float* X, float* out, cudaStream_t s);
+                             const float* betaC, const float* X, const int32_t* rowOf, float* out,
+                             cudaStream_t s);
 int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, const float* V,
                         double* y, double* res, cudaStream_t s);
 int fem_launch_fill_frames(int F, int E, const int* frameMask, float value, float* gamma, cudaStream_t s);

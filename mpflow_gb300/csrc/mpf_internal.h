@@ -115,6 +115,9 @@ struct FemStructure {
     std::vector<int32_t> contrib;           // e*9 + i*3 + j, element order within a slot
 };
 int build_structure(int N, int E, const int32_t* elements, FemStructure& fs);
+// perm[i] = node placed at row i: nodes sorted by the Morton (Z-order) code of
+// their coordinates quantised to 16 bits per axis, ties by node number.
+void morton_order(int N, const double* nodes, int32_t* perm);
 void excitation_matrix(int N, const double* nodes, const int32_t* edges, int ports,
                        const int32_t* portEdges, int cap, double* exc, int ld);
 

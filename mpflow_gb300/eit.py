@@ -125,14 +125,23 @@ class Sources:
 
 
 class SolveOptions:
+    """mpf_solve_opts; preconditioner "jacobi" (the reference's) or
+    "two-level" (Jacobi plus an aggregation coarse correction)."""
+
+    PRECONDITIONERS = {"jacobi": 0, "two-level": 1}
+
     def __init__(self, tol=1e-6, max_iter=0, refine_tol=0.0, max_refine=6, warm_start=False,
-                 check_every=16):
+                 check_every=16, preconditioner: str = "jacobi"):
         self.tol, self.max_iter, self.refine_tol = tol, max_iter, refine_tol
         self.max_refine, self.warm_start, self.check_every = max_refine, warm_start, check_every
+        if preconditioner not in self.PRECONDITIONERS:
+            raise ValueError(f"preconditioner must be one of {sorted(self.PRECONDITIONERS)}")
+        self.preconditioner = preconditioner
 
     def c(self) -> _ffi.SolveOpts:
         return _ffi.SolveOpts(float(self.tol), int(self.max_iter), float(self.refine_tol),
-                              int(self.max_refine), int(bool(self.warm_start)), int(self.check_every))
+                              int(self.max_refine), int(bool(self.warm_start)), int(self.check_every),
+                              self.PRECONDITIONERS[self.preconditioner])
 
 
 def _stream():

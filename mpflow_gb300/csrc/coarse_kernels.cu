@@ -12,10 +12,11 @@
 // batched FP64 Cholesky of dense_kernels.cu, k_coarse_prep): the coarse
 // matrix of every (frame, harmonic) group in FP64, its Cholesky factor, and
 // an FP32 copy of the factor with inverted 32x32 diagonal blocks.
-// Per CG iteration, k_coarse (one CTA per group): (P^T A P) y = P^T r by
-// blocked forward / backward substitution in shared memory, y written for
-// the direction kernel, (P^T r).y added to r^T D^-1 r, then the CG scalars
-// and convergence masks of the group.
+// The setup ends with the explicit inverse (P^T A P)^-1 in FP32
+// (k_coarse_inverse: blocked triangular solves on identity columns), so the
+// per-iteration kernel k_coarse is a dense product y = (P^T A P)^-1 P^T r
+// with no sequential dependence; it also adds (P^T r).y to r^T D^-1 r and
+// updates the CG scalars and convergence masks of every group.
 #include <algorithm>
 
 #include "model.h"
@@ -156,41 +157,98 @@ __device__ void coarse_solve(const float* __restrict__ L, const float* __restric
     }
 }
 
+// Setup: columns [32 * blockIdx.x, +32) of (P^T A P)^-1 by triangular solves
+// on identity columns; Binv is row-major and symmetric up to rounding.
+__global__ void __launch_bounds__(kCT) k_coarse_inverse(int ncPad, const float* __restrict__ Lc,
+                                                        const float* __restrict__ LinvD, float* __restrict__ Binv) {
+    constexpr int YS = 33;
+    extern __shared__ float smc[];
+    float* y = smc;
+    float* tmp = y + (size_t)ncPad * YS;
+    float(*Ls)[33] = reinterpret_cast<float(*)[33]>(tmp + 32 * YS);
+    const int g = blockIdx.y, col0 = blockIdx.x * 32;
+    for (int t = threadIdx.x; t < ncPad * 32; t += kCT) y[(t / 32) * YS + t % 32] = (t / 32 == col0 + t % 32) ? 1.f : 0.f;
+    __syncthreads();
+    coarse_solve<32>(Lc + (size_t)g * ncPad * ncPad, LinvD + (size_t)g * (ncPad / 32) * 1024, ncPad, y, tmp, Ls);
+    float* B = Binv + (size_t)g * ncPad * ncPad;
+    for (int t = threadIdx.x; t < ncPad * 32; t += kCT) B[(size_t)(t / 32) * ncPad + col0 + t % 32] = y[(t / 32) * YS + t % 32];
+}
+
+// Per iteration: y = Binv (P^T r) for rows [64 * blockIdx.x, +64) of every
+// group, written for the direction kernel, and (P^T r).y; the last block of
+// the group adds it to r^T D^-1 r and updates the CG scalars and masks.  In
+// the start-of-solve mode it also solves for P^T b to complete b^T M^-1 b.
+constexpr int kRowsPerCta = 64;
+
 template <int KP>
 __global__ void __launch_bounds__(kCT) k_coarse(CgProblem P, int init) {
-    static_assert(KP % 8 == 0 && kCT % KP == 0, "right-hand sides per thread");
-    const int g = blockIdx.x;
+    constexpr int CPT = KP / 4;  // right-hand sides per thread: 4 threads per row
+    const int g = blockIdx.y;
     if (!init && !P.active[g]) return;
-    constexpr int YS = KP + 1;
-    extern __shared__ float smc[];
-    float* y = smc;                         // [ncPad][YS]
-    float* tmp = y + (size_t)P.ncPad * YS;  // [32][YS]
-    float(*Ls)[33] = reinterpret_cast<float(*)[33]>(tmp + 32 * YS);
-    __shared__ double cdot[2][kCT];
-    const float* L = P.Lc + (size_t)g * P.ncPad * P.ncPad;
-    const float* Dv = P.LinvD + (size_t)g * (P.ncPad / 32) * 1024;
-    const size_t cb = (size_t)g * P.ncPad * KP;
-    constexpr int parts = kCT / KP;
-    const int j = threadIdx.x % KP, part = threadIdx.x / KP;
+    extern __shared__ float smc[];  // [ncPad][KP] restricted vector
+    __shared__ double red[2][kCT / 4][4];
+    __shared__ bool amLast;
+    const int ncPad = P.ncPad;
+    const size_t cb = (size_t)g * ncPad * KP;
+    const int lr = threadIdx.x >> 2, cq = threadIdx.x & 3;
+    const int row = blockIdx.x * kRowsPerCta + lr;
+    const float* B = P.Binv + ((size_t)g * ncPad + row) * ncPad;
+    double* part = P.partC + ((size_t)g * gridDim.x + blockIdx.x) * 2 * KP;
     for (int sys = 0; sys < (init ? 2 : 1); ++sys) {
         const float* src = (sys == 0 ? P.rc : P.rcB) + cb;
-        for (int t = threadIdx.x; t < P.ncPad * KP; t += kCT) y[(t / KP) * YS + t % KP] = src[t];
+        for (int t = threadIdx.x; t < ncPad * KP / 4; t += kCT)
+            reinterpret_cast<float4*>(smc)[t] = reinterpret_cast<const float4*>(src)[t];
         __syncthreads();
-        coarse_solve<KP>(L, Dv, P.ncPad, y, tmp, Ls);
-        double d = 0.0;
-        for (int I = part; I < P.nc; I += parts) d += (double)src[(size_t)I * KP + j] * (double)y[I * YS + j];
-        cdot[sys][threadIdx.x] = d;
-        if (sys == 0)
-            for (int t = threadIdx.x; t < P.ncPad * KP; t += kCT) P.yc[cb + t] = y[(t / KP) * YS + t % KP];
+        float acc[CPT];
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) acc[q] = 0.f;
+        for (int k = 0; k < ncPad; k += 4) {
+            const float4 b = __ldg(reinterpret_cast<const float4*>(B + k));
+            const float* v = smc + (size_t)k * KP + cq;
+#pragma unroll
+            for (int q = 0; q < CPT; ++q) {
+                float a = acc[q];
+                a = fmaf(b.x, v[4 * q], a);
+                a = fmaf(b.y, v[KP + 4 * q], a);
+                a = fmaf(b.z, v[2 * KP + 4 * q], a);
+                a = fmaf(b.w, v[3 * KP + 4 * q], a);
+                acc[q] = a;
+            }
+        }
+        // partial (P^T v).y of this CTA's rows, per right-hand side
+        double d[CPT];
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) {
+            d[q] = (double)smc[(size_t)row * KP + cq + 4 * q] * (double)acc[q];
+            if (sys == 0) P.yc[cb + (size_t)row * KP + cq + 4 * q] = acc[q];
+        }
         __syncthreads();
+        // reduce over the 64 rows, fixed order: column c = cq + 4 q
+        for (int q = 0; q < CPT; ++q) {
+            red[sys][lr][cq] = d[q];
+            __syncthreads();
+            if (threadIdx.x < 4) {
+                double t = 0.0;
+                for (int i = 0; i < kRowsPerCta; ++i) t += red[sys][i][threadIdx.x];
+                part[sys * KP + threadIdx.x + 4 * q] = t;
+            }
+            __syncthreads();
+        }
     }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) amLast = atomicAdd(&P.counter[g], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!amLast) return;
+    __threadfence();
     int notConv = 0;
     if (threadIdx.x < KP) {
         const size_t s = (size_t)g * KP + threadIdx.x;
         double c0 = 0.0, c1 = 0.0;
-        for (int q = 0; q < parts; ++q) {
-            c0 += cdot[0][q * KP + threadIdx.x];
-            if (init) c1 += cdot[1][q * KP + threadIdx.x];
+        for (unsigned b = 0; b < gridDim.x; ++b) {
+            const double* pb = P.partC + ((size_t)g * gridDim.x + b) * 2 * KP;
+            c0 += __ldcg(pb + threadIdx.x);
+            if (init) c1 += __ldcg(pb + KP + threadIdx.x);
         }
         if (init) {
             const double rz = P.rzFine[s] + c0, bz = P.bzFine[s] + c1;
@@ -213,20 +271,21 @@ __global__ void __launch_bounds__(kCT) k_coarse(CgProblem P, int init) {
     if (threadIdx.x == 0) {
         P.active[g] = any;
         if (!init) P.iters[g] += 1;
+        P.counter[g] = 0;
     }
 }
 
-size_t coarse_smem(int ncPad, int KP) { return ((size_t)(ncPad + 32) * (KP + 1) + 32 * 33) * sizeof(float); }
+size_t coarse_solve_smem(int ncPad) { return ((size_t)(ncPad + 32) * 33 + 32 * 33) * sizeof(float); }
 
 template <int KP>
 int launch_coarse_kp(const CgProblem& P, bool init, cudaStream_t s, bool count) {
-    const size_t smem = coarse_smem(P.ncPad, KP);
+    const size_t smem = (size_t)P.ncPad * KP * sizeof(float);
     static size_t configured = 0;
     if (smem > configured) {
         MPF_CUDA(cudaFuncSetAttribute(k_coarse<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
-    k_coarse<KP><<<P.G, kCT, smem, s>>>(P, init ? 1 : 0);
+    k_coarse<KP><<<dim3(P.ncPad / kRowsPerCta, P.G), kCT, smem, s>>>(P, init ? 1 : 0);
     if (count) {
         MPF_LAUNCHED(1);
     } else {
@@ -238,8 +297,8 @@ int launch_coarse_kp(const CgProblem& P, bool init, cudaStream_t s, bool count) 
 }  // namespace
 
 bool coarse_supported(int KP, int ncPad) {
-    return (KP == 16 || KP == 32 || KP == 64) && ncPad >= 32 && ncPad % 32 == 0 &&
-           coarse_smem(ncPad, KP) <= 200 * 1024;
+    return (KP == 16 || KP == 32 || KP == 64) && ncPad >= kRowsPerCta && ncPad % kRowsPerCta == 0 &&
+           (size_t)ncPad * KP * sizeof(float) <= 200 * 1024 && coarse_solve_smem(ncPad) <= 200 * 1024;
 }
 
 int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count) {
@@ -252,7 +311,7 @@ int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count) 
 }
 
 int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,
-                        float* Lc, float* LinvD) {
+                        float* Lc, float* LinvD, float* Binv) {
     const size_t per = (size_t)cp.ncPad * cp.ncPad;
     MPF_CUDA(cudaMemsetAsync(Ac64, 0, sizeof(double) * per * P.G, s));
     k_coarse_assemble<<<dim3((cp.nnz + 255) / 256, P.G), 256, 0, s>>>(P, cp, Ac64);
@@ -260,7 +319,14 @@ int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, 
     MPF_LAUNCHED(2);
     MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s));
     k_coarse_prep<<<dim3(cp.ncPad / 32, P.G), 32, 0, s>>>(cp.ncPad, Ac64, Lc, LinvD);
-    MPF_LAUNCHED(1);
+    const size_t smem = coarse_solve_smem(cp.ncPad);
+    static size_t configured = 0;
+    if (smem > configured) {
+        MPF_CUDA(cudaFuncSetAttribute(k_coarse_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    k_coarse_inverse<<<dim3(cp.ncPad / 32, P.G), kCT, smem, s>>>(cp.ncPad, Lc, LinvD, Binv);
+    MPF_LAUNCHED(2);
     return MPF_OK;
 }
 

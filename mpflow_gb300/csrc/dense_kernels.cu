@@ -39,6 +39,7 @@ struct GramArgs {
     int splits;      // K splits
     float* work;     // [batch][splits][tiles][128][128]
     int* abortFlag;  // device flag raised by a timed-out wait
+    const int* frameMask;  // [batch] entries to compute, or null for all
 };
 
 // One CTA = one (batch, upper tile, K split).  Warp 0 lane 0 issues TMA,
@@ -53,6 +54,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int b = blockIdx.z;
+    if (ga.frameMask && !ga.frameMask[b]) return;
     const int split = blockIdx.y;
     // tile index -> (tm, tn) with tm <= tn
     int t = blockIdx.x, tm = 0;
@@ -154,8 +156,10 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
 // Sum the K splits in order and write the full symmetric matrix, either FP32
 // (C) or FP64 with a diagonal shift (A64).
 __global__ void k_gram_reduce(int rows, int tiles, int nt, int splits, const float* __restrict__ work,
-                              float* __restrict__ C, double* __restrict__ A64, double shift) {
+                              float* __restrict__ C, double* __restrict__ A64, double shift,
+                              const int* __restrict__ frameMask) {
     const int b = blockIdx.z, tile = blockIdx.y;
+    if (frameMask && !frameMask[b]) return;
     int t = tile, tm = 0;
     while (t >= nt - tm) {
         t -= nt - tm;
@@ -195,7 +199,8 @@ __global__ void k_split_bf16(int batch, int rows, int cols, const float* __restr
 // FP64 Cholesky, 32x32 blocks, column-major (lower triangle holds L).
 constexpr int NB = 32;
 
-__global__ void k_potrf_diag(int n, double* A, int k, int* info) {
+__global__ void k_potrf_diag(int n, double* A, int k, int* info, const int* frameMask) {
+    if (frameMask && !frameMask[blockIdx.x]) return;
     __shared__ double a[NB][NB + 1];
     __shared__ int bad;
     double* M = A + (size_t)blockIdx.x * n * n;
@@ -233,7 +238,8 @@ __global__ void k_potrf_diag(int n, double* A, int k, int* info) {
 }
 
 // L_ik = A_ik L_kk^-T for the block rows below the diagonal block k
-__global__ void k_trsm(int n, double* A, int k) {
+__global__ void k_trsm(int n, double* A, int k, const int* frameMask) {
+    if (frameMask && !frameMask[blockIdx.y]) return;
     __shared__ double L[NB][NB + 1];
     __shared__ double X[NB][NB + 1];
     double* M = A + (size_t)blockIdx.y * n * n;
@@ -260,7 +266,8 @@ __global__ void k_trsm(int n, double* A, int k) {
 }
 
 // A_ij -= L_ik L_jk^T for k < j <= i
-__global__ void k_syrk(int n, double* A, int k) {
+__global__ void k_syrk(int n, double* A, int k, const int* frameMask) {
+    if (frameMask && !frameMask[blockIdx.y]) return;
     __shared__ double Li[NB][NB + 1];
     __shared__ double Lj[NB][NB + 1];
     double* M = A + (size_t)blockIdx.y * n * n;
@@ -288,7 +295,9 @@ __global__ void k_syrk(int n, double* A, int k) {
 
 // Forward then backward substitution with L (column-major lower), one block
 // per (batch, right-hand side).
-__global__ void k_chol_solve(int n, const double* __restrict__ Lall, double* __restrict__ Ball, int nrhs) {
+__global__ void k_chol_solve(int n, const double* __restrict__ Lall, double* __restrict__ Ball, int nrhs,
+                             const int* __restrict__ frameMask) {
+    if (frameMask && !frameMask[blockIdx.x / nrhs]) return;
     extern __shared__ double x[];
     const int b = blockIdx.x / nrhs, c = blockIdx.x % nrhs;
     const double* L = Lall + (size_t)b * n * n;
@@ -382,7 +391,7 @@ size_t dense_gram_work_floats(int batch, int rows, int cols) {
 
 static int gram_run(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo, int ld,
                     float* C, double* A64, double shift, float* work, size_t workFloats, cudaStream_t s,
-                    int* flagOverride = nullptr) {
+                    int* flagOverride = nullptr, const int* frameMask = nullptr) {
     MPF_CHECK(rows % kTile == 0 && cols % kBK == 0 && ld % 8 == 0 && ld >= cols, MPF_EINVAL,
               "gram: rows %% 128, cols %% 64 and ld %% 8 must be 0 (rows=%d cols=%d ld=%d)", rows, cols, ld);
     const int nt = rows / kTile, tiles = nt * (nt + 1) / 2, kblocks = cols / kBK;
@@ -398,10 +407,10 @@ static int gram_run(int batch, int rows, int cols, const __nv_bfloat16* hi, cons
         MPF_CUDA(cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmem));
         attr = true;
     }
-    GramArgs ga{rows, kblocks, tiles, nt, splits, work, flag};
+    GramArgs ga{rows, kblocks, tiles, nt, splits, work, flag, frameMask};
     k_gram_tc<<<dim3(tiles, splits, batch), 128, kGramSmem, s>>>(mHi, mLo, ga);
     MPF_LAUNCHED(1);
-    k_gram_reduce<<<dim3(16, tiles, batch), 256, 0, s>>>(rows, tiles, nt, splits, work, C, A64, shift);
+    k_gram_reduce<<<dim3(16, tiles, batch), 256, 0, s>>>(rows, tiles, nt, splits, work, C, A64, shift, frameMask);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }
@@ -412,8 +421,9 @@ int dense_gram_split_bf16(int batch, int rows, int cols, const __nv_bfloat16* hi
 }
 
 int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo, int ld,
-                         double shift, double* A64, float* work, size_t workFloats, cudaStream_t s) {
-    return gram_run(batch, rows, cols, hi, lo, ld, nullptr, A64, shift, work, workFloats, s);
+                         double shift, double* A64, float* work, size_t workFloats, cudaStream_t s,
+                         const int* frameMask) {
+    return gram_run(batch, rows, cols, hi, lo, ld, nullptr, A64, shift, work, workFloats, s, nullptr, frameMask);
 }
 
 int dense_gram_check_abort(bool* aborted) {
@@ -516,25 +526,26 @@ int dense_gram_split_bf16_noalloc(int batch, int rows, int cols, const float* A,
     return MPF_OK;
 }
 
-int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s) {
+int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s, const int* frameMask) {
     MPF_CHECK(n % NB == 0, MPF_EINVAL, "cholesky: n must be a multiple of %d (got %d)", NB, n);
     MPF_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * batch, s));
     const int nb = n / NB;
     for (int k = 0; k < nb; ++k) {
-        k_potrf_diag<<<batch, 256, 0, s>>>(n, A, k, info);
+        k_potrf_diag<<<batch, 256, 0, s>>>(n, A, k, info, frameMask);
         const int m = nb - k - 1;
         if (m > 0) {
-            k_trsm<<<dim3(m, batch), 64, 0, s>>>(n, A, k);
-            k_syrk<<<dim3(m * (m + 1) / 2, batch), 256, 0, s>>>(n, A, k);
+            k_trsm<<<dim3(m, batch), 64, 0, s>>>(n, A, k, frameMask);
+            k_syrk<<<dim3(m * (m + 1) / 2, batch), 256, 0, s>>>(n, A, k, frameMask);
         }
     }
     MPF_LAUNCHED(3 * nb - 2);
     return MPF_OK;
 }
 
-int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s) {
+int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s,
+                             const int* frameMask) {
     MPF_CHECK((size_t)n * sizeof(double) <= 48 * 1024, MPF_EINVAL, "cholesky solve: n too large (%d)", n);
-    k_chol_solve<<<batch * nrhs, 512, n * sizeof(double), s>>>(n, L, B, nrhs);
+    k_chol_solve<<<batch * nrhs, 512, n * sizeof(double), s>>>(n, L, B, nrhs, frameMask);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(512) k_jacobian(JacPlan jp, int npad, const fl
     float(*Ms)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33 + 32 * 9);
     float(*Ke)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33 + 2 * 32 * 9);
     const int f = blockIdx.y;
+    if (jp.frameMask && !jp.frameMask[f]) return;
     const int e0 = blockIdx.x * 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nthreads = blockDim.x;
     const int e = e0 + lane;
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(512) k_jacobian(JacPlan jp, int npad, const fl
             if (row >= jp.rowsJ) continue;
             const float v = valid ? deriv * jp.rowScale[row] * acc[a][m] : 0.f;
             const size_t o = base + (size_t)row * jp.Epad + e;
-            J[o] = v;
+            if (jp.writeF32) J[o] = v;
             if (Jhi) {
                 const __nv_bfloat16 h = __float2bfloat16_rn(v);
                 Jhi[o] = h;
@@ -278,9 +279,9 @@ __global__ void k_residual(int rowsJ, int Mm, int Md, int MP, const float* __res
 
 // gamma[e] += sum_r J[r][e] w[r]  (J^T w of the dual Gauss-Newton step,
 // src/solver/inverse.cpp:198-204 then src/solver/solver.cpp:222)
-__global__ void k_update_gamma(int rowsJ, int Epad, int E, const float* __restrict__ J,
-                               const double* __restrict__ w, const int* __restrict__ frameActive,
-                               float* __restrict__ gamma) {
+__global__ void k_update_gamma(int rowsJ, int Epad, int E, const __nv_bfloat16* __restrict__ Jhi,
+                               const __nv_bfloat16* __restrict__ Jlo, const double* __restrict__ w,
+                               const int* __restrict__ frameActive, float* __restrict__ gamma) {
     extern __shared__ float ws[];
     const int f = blockIdx.y;
     if (frameActive && !frameActive[f]) return;
@@ -288,11 +289,13 @@ __global__ void k_update_gamma(int rowsJ, int Epad, int E, const float* __restri
     __syncthreads();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    const float* Jf = J + (size_t)f * rowsJ * Epad;
+    const __nv_bfloat16* Hf = Jhi + (size_t)f * rowsJ * Epad;
+    const __nv_bfloat16* Lf = Jlo + (size_t)f * rowsJ * Epad;
     float s = 0.f, c = 0.f;
     for (int r = 0; r < rowsJ; ++r) {
         // compensated float sum of J[r][e] * w[r]
-        const float a = __ldg(&Jf[(size_t)r * Epad + e]), b = ws[r];
+        const float a = __bfloat162float(Hf[(size_t)r * Epad + e]) + __bfloat162float(Lf[(size_t)r * Epad + e]);
+        const float b = ws[r];
         const float p = __fmul_rn(a, b), pe = __fmaf_rn(a, b, -p);
         const float t = __fadd_rn(s, p), z = __fsub_rn(t, s);
         const float te = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
@@ -436,10 +439,10 @@ int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, co
     return MPF_OK;
 }
 
-int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, const double* w,
-                            const int* frameActive, float* gamma, cudaStream_t s) {
+int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const __nv_bfloat16* Jhi, const __nv_bfloat16* Jlo,
+                            const double* w, const int* frameActive, float* gamma, cudaStream_t s) {
     dim3 grid((E + 255) / 256, F);
-    k_update_gamma<<<grid, 256, rowsJ * sizeof(float), s>>>(rowsJ, Epad, E, J, w, frameActive, gamma);
+    k_update_gamma<<<grid, 256, rowsJ * sizeof(float), s>>>(rowsJ, Epad, E, Jhi, Jlo, w, frameActive, gamma);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

@@ -71,7 +71,7 @@ struct mpf_eit {
     mpf::DevBuf<float> cAggSize;
     int cNnz = 0;
     mpf::DevBuf<double> Ac64, rzFine, bzFine;
-    mpf::DevBuf<float> Lc, LinvD, rcV, rcB, ycV;
+    mpf::DevBuf<float> Lc, LinvD, Binv, rcV, rcB, ycV;
     mpf::DevBuf<int> infoC;
     // learned warm start: homogeneous voltages and the network input
     bool v0Ready = false;
@@ -341,7 +341,7 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     // and, per nonzero aggregate pair (I, J), the matrix slots that sum into
     // the coarse entry (padding slots excluded)
     m->nc = (m->n + kAgg - 1) / kAgg;
-    m->ncPad = round_up(m->nc, 32);
+    m->ncPad = round_up(m->nc, 64);
     m->coarseOK = coarse_supported(m->KP, m->ncPad) ? 1 : 0;
     if (m->coarseOK) {
         std::vector<std::vector<std::pair<int32_t, int32_t>>> byI(m->nc);
@@ -428,7 +428,6 @@ static int ensure_workspace(mpf_eit* m, int F, bool refine, bool jacobian) {
     }
     if (jacobian && F > m->capFJ) {
         const size_t jsz = (size_t)F * m->rowsJ * m->Epad;
-        MPF_TRY(m->J.alloc(jsz));
         MPF_TRY(m->Jhi.alloc(jsz));
         MPF_TRY(m->Jlo.alloc(jsz));
         MPF_TRY(m->gramWork.alloc(dense_gram_work_floats(F, m->rowsJ, m->Epad)));
@@ -449,6 +448,7 @@ static int ensure_coarse(mpf_eit* m, int F) {
     MPF_TRY(m->Ac64.alloc(G * nc2));
     MPF_TRY(m->Lc.alloc(G * nc2));
     MPF_TRY(m->LinvD.alloc(G * (m->ncPad / 32) * 1024));
+    MPF_TRY(m->Binv.alloc(G * nc2));
     MPF_TRY(m->rcV.alloc(cv));
     MPF_TRY(m->rcB.alloc(cv));
     MPF_TRY(m->ycV.alloc(cv));
@@ -510,8 +510,7 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false
         P.rc = m->rcV.ptr;
         P.rcB = m->rcB.ptr;
         P.yc = m->ycV.ptr;
-        P.Lc = m->Lc.ptr;
-        P.LinvD = m->LinvD.ptr;
+        P.Binv = m->Binv.ptr;
         P.rzFine = m->rzFine.ptr;
         P.bzFine = m->bzFine.ptr;
     }
@@ -664,6 +663,19 @@ int eit_assemble_export(mpf_eit* m, int F, const float* gamma, float* sOut, floa
     return MPF_OK;
 }
 
+// Jacobian of the last forward solve's fields into the workspace: the BF16
+// hi/lo split always, FP32 J only when `f32` (the C-ABI forward output);
+// frames with frameMask[f] == 0 are skipped.
+static int eit_jacobian(mpf_eit* m, int F, const float* gamma, const int* frameMask, bool f32, cudaStream_t s) {
+    MPF_TRY(ensure_workspace(m, F, false, true));
+    if (f32) MPF_TRY(m->J.alloc((size_t)m->capFJ * m->rowsJ * m->Epad));
+    JacPlan jp{m->rowsJ, m->Epad, m->E, m->KP, m->Ca, m->rowD.ptr, m->rowM.ptr, m->rowScale.ptr,
+               m->beta2.ptr, m->massCoef.ptr, m->elements.ptr, m->Kf.ptr, m->Mf.ptr, m->exactJacobian,
+               m->ref, (float)m->height, m->logarithmic, frameMask, f32 ? 1 : 0};
+    return fem_launch_jacobian(F, jp, m->MmPad, m->npad, m->X.ptr, gamma, f32 ? m->J.ptr : nullptr, m->Jhi.ptr,
+                               m->Jlo.ptr, s);
+}
+
 // Forward solve into the workspace (fields X, voltages V, optional J).
 int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_solve_opts* optsIn,
                    mpf_solve_stats* stats, cudaStream_t s) {
@@ -681,7 +693,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     if (coarse) {
         CoarsePlan cp{m->nc, m->ncPad, m->cNnz, m->cPairI.ptr, m->cPairJ.ptr, m->cPairPtr.ptr, m->cSlots.ptr,
                       m->cAggSize.ptr};
-        MPF_TRY(coarse_launch_setup(P, cp, m->Ac64.ptr, m->infoC.ptr, s, m->Lc.ptr, m->LinvD.ptr));
+        MPF_TRY(coarse_launch_setup(P, cp, m->Ac64.ptr, m->infoC.ptr, s, m->Lc.ptr, m->LinvD.ptr, m->Binv.ptr));
     }
     int totalIters = 0, notConv = 0, refinements = 0;
     double maxRel = 0.0;
@@ -748,12 +760,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     MPF_TRY(fem_launch_gram_meas(P.G, m->KP, m->npad, mp, m->X.ptr, m->Gm.ptr, s));
     MPF_TRY(fem_launch_voltages(F, m->Ca, m->KP, m->Mm, m->Md, m->Gm.ptr, m->beta.ptr, m->measU.ptr,
                                 m->measScale.ptr, m->driveU.ptr, m->driveScale.ptr, m->V.ptr, s));
-    if (wantJ) {
-        JacPlan jp{m->rowsJ, m->Epad, m->E, m->KP, m->Ca, m->rowD.ptr, m->rowM.ptr, m->rowScale.ptr,
-                   m->beta2.ptr, m->massCoef.ptr, m->elements.ptr, m->Kf.ptr, m->Mf.ptr, m->exactJacobian,
-                   m->ref, (float)m->height, m->logarithmic};
-        MPF_TRY(fem_launch_jacobian(F, jp, m->MmPad, m->npad, m->X.ptr, gamma, m->J.ptr, m->Jhi.ptr, m->Jlo.ptr, s));
-    }
+    if (wantJ) MPF_TRY(eit_jacobian(m, F, gamma, nullptr, true, s));
     MPF_CUDA(cudaStreamSynchronize(s));
     MPF_CUDA(cudaGetLastError());
     if (stats) {
@@ -793,14 +800,15 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
 static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* frameActive, cudaStream_t s) {
     const double mu = (double)m->ref * lambda * (double)m->ref * lambda;
     MPF_TRY(dense_gram_f64_shift(F, m->rowsJ, m->Epad, m->Jhi.ptr, m->Jlo.ptr, m->Epad, mu, m->A64.ptr,
-                                 m->gramWork.ptr, m->gramWork.count, s));
-    MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s));
-    MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s));
-    MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->J.ptr, m->y.ptr, frameActive, gamma, s));
+                                 m->gramWork.ptr, m->gramWork.count, s, frameActive));
+    MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, frameActive));
+    MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s, frameActive));
+    MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->Jhi.ptr, m->Jlo.ptr, m->y.ptr, frameActive, gamma,
+                                    s));
     return MPF_OK;
 }
 
-static int gn_check(mpf_eit* m, int F, cudaStream_t s) {
+static int gn_check(mpf_eit* m, int F, cudaStream_t s, const int* hostMask = nullptr) {
     std::vector<int> info(F);
     MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
     MPF_CUDA(cudaStreamSynchronize(s));
@@ -808,7 +816,8 @@ static int gn_check(mpf_eit* m, int F, cudaStream_t s) {
     MPF_TRY(dense_gram_check_abort(&aborted));
     MPF_CHECK(!aborted, MPF_ETIMEOUT, "gram kernel: a pipeline wait timed out");
     for (int f = 0; f < F; ++f)
-        MPF_CHECK(info[f] == 0, MPF_EBREAKDOWN, "Cholesky of (J J^T + mu I) failed at pivot %d (frame %d)", info[f], f);
+        MPF_CHECK(info[f] == 0 || (hostMask && !hostMask[f]), MPF_EBREAKDOWN,
+                  "Cholesky of (J J^T + mu I) failed at pivot %d (frame %d)", info[f], f);
     return MPF_OK;
 }
 
@@ -816,9 +825,11 @@ int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, 
             double* residual, mpf_solve_stats* stats, cudaStream_t s) {
     MPF_TRY(check_device(m));
     MPF_CHECK(F >= 1 && gamma && vMeas, MPF_EINVAL, "mpFlow::solver::Solver::solveAbsolute: bad arguments");
-    int st = eit_forward_ws(m, F, gamma, true, o, stats, s);
+    int st = eit_forward_ws(m, F, gamma, false, o, stats, s);
     if (st != MPF_OK && st != MPF_ENOCONV) return st;
+    MPF_TRY(ensure_workspace(m, F, false, true));
     MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
+    MPF_TRY(eit_jacobian(m, F, gamma, nullptr, false, s));
     MPF_TRY(gn_update(m, F, gamma, lambda, nullptr, s));
     if (residual) MPF_CUDA(cudaMemcpyAsync(residual, m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
     MPF_TRY(gn_check(m, F, s));
@@ -849,8 +860,9 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         mpf_solve_stats fs{};
         mpf_solve_opts oi = o;
         oi.warm_start = warm ? 1 : 0;
-        int st = eit_forward_ws(m, F, gamma, true, &oi, &fs, s);
+        int st = eit_forward_ws(m, F, gamma, false, &oi, &fs, s);
         if (st != MPF_OK && st != MPF_ENOCONV) return st;
+        MPF_TRY(ensure_workspace(m, F, false, true));
         warm = true;
         cgTotal += fs.iterations;
         MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
@@ -879,8 +891,9 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         if (live == 0 || it == maxIters) break;
         for (int f = 0; f < F; ++f) iters[f] += mask[f];
         MPF_CUDA(cudaMemcpyAsync(m->frameMask.ptr, mask.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+        MPF_TRY(eit_jacobian(m, F, gamma, m->frameMask.ptr, false, s));
         MPF_TRY(gn_update(m, F, gamma, lambda, m->frameMask.ptr, s));
-        MPF_TRY(gn_check(m, F, s));
+        MPF_TRY(gn_check(m, F, s, mask.data()));
         ++gnIters;
         ++it;
     }

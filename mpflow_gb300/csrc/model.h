@@ -59,8 +59,7 @@ struct CgProblem {
     float* rc;            // [G][ncPad][KP] P^T r (restriction, written by k_update / k_init)
     float* rcB;           // [G][ncPad][KP] P^T b (k_init, for b^T M^-1 b)
     float* yc;            // [G][ncPad][KP] (P^T A P)^-1 P^T r
-    const float* Lc;      // [G][ncPad][ncPad] Cholesky factor of P^T A P, row-major lower, FP32
-    const float* LinvD;   // [G][ncPad/32][32][32] inverses of its diagonal blocks, row-major
+    const float* Binv;    // [G][ncPad][ncPad] (P^T A P)^-1, row-major, FP32
     double* rzFine;       // [G][KP] r^T D^-1 r of the last update / init
     double* bzFine;       // [G][KP] b^T D^-1 b (init)
     int first;            // k_direction: p = M^-1 r (start of an iteration)
@@ -85,8 +84,9 @@ struct CoarsePlan {
     const int32_t* slots;            // slot indices k * npad + row
     const float* aggSize;            // [nc] real rows per aggregate
 };
+// Lc [G][ncPad][ncPad], LinvD [G][ncPad/32][1024]: FP32 factor scratch; Binv: the inverse (P.Binv)
 int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,
-                        float* Lc, float* LinvD);
+                        float* Lc, float* LinvD, float* Binv);
 // `count`: false while recording a CUDA graph (replays are counted by the caller)
 int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count = true);
 bool coarse_supported(int KP, int ncPad);
@@ -133,6 +133,8 @@ struct JacPlan {
     int exact;
     float ref, height;       // J *= -height (open sources)
     int logarithmic;
+    const int* frameMask;    // [F] frames to compute, or null for all
+    int writeF32;            // 0: only the BF16 hi/lo split (the Gauss-Newton path)
 };
 int fem_launch_jacobian(int F, const JacPlan& jp, int MP, int npad, const float* X, const float* gamma,
                         float* J, __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s);
@@ -147,8 +149,9 @@ int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, co
 int fem_launch_fill_frames(int F, int E, const int* frameMask, float value, float* gamma, cudaStream_t s);
 int fem_launch_learned_input(int F, int L, const float* vMeas, const float* V0, float invRms, float* x,
                              double* res0, cudaStream_t s);
-int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const float* J, const double* w,
-                            const int* frameActive, float* gamma, cudaStream_t s);
+// gamma += J^T w with J = hi + lo (the BF16 split the Gram is formed from)
+int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const __nv_bfloat16* Jhi, const __nv_bfloat16* Jlo,
+                            const double* w, const int* frameActive, float* gamma, cudaStream_t s);
 
 // dense_kernels.cu
 int dense_gram_split_bf16(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo,
@@ -157,12 +160,15 @@ size_t dense_gram_work_floats(int batch, int rows, int cols);
 int dense_split_bf16(int batch, int rows, int cols, const float* A, int lda, __nv_bfloat16* hi,
                      __nv_bfloat16* lo, cudaStream_t s);
 int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi, const __nv_bfloat16* lo,
-                         int ld, double shift, double* A64, float* work, size_t workFloats, cudaStream_t s);
+                         int ld, double shift, double* A64, float* work, size_t workFloats, cudaStream_t s,
+                         const int* frameMask = nullptr);
 int dense_gram_check_abort(bool* aborted);
 int dense_gram_split_bf16_noalloc(int batch, int rows, int cols, const float* A, int lda, float* C, cudaStream_t s);
 int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s);
-int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s);
-int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s);
+// frameMask: [batch] entries to process (null: all); skipped entries keep their contents
+int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s, const int* frameMask = nullptr);
+int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s,
+                             const int* frameMask = nullptr);
 
 // mlp_kernels.cu (used by the learned warm start)
 void mlp_dims(const mpf_mlp* n, int* in, int* out);

@@ -14,9 +14,10 @@
 // an FP32 copy of the factor with inverted 32x32 diagonal blocks.
 // The setup ends with the explicit inverse (P^T A P)^-1 in FP32
 // (k_coarse_inverse: blocked triangular solves on identity columns), so the
-// per-iteration kernel k_coarse is a dense product y = (P^T A P)^-1 P^T r
-// with no sequential dependence; it also adds (P^T r).y to r^T D^-1 r and
-// updates the CG scalars and convergence masks of every group.
+// per-iteration kernel k_coarse is a dense register-tiled product
+// y = (P^T A P)^-1 P^T r with no sequential dependence; it also adds
+// (P^T r).y to r^T D^-1 r and updates the CG scalars and convergence masks
+// of every group.
 #include <algorithm>
 
 #include "model.h"
@@ -174,63 +175,112 @@ __global__ void __launch_bounds__(kCT) k_coarse_inverse(int ncPad, const float* 
     for (int t = threadIdx.x; t < ncPad * 32; t += kCT) B[(size_t)(t / 32) * ncPad + col0 + t % 32] = y[(t / 32) * YS + t % 32];
 }
 
-// Per iteration: y = Binv (P^T r) for rows [64 * blockIdx.x, +64) of every
-// group, written for the direction kernel, and (P^T r).y; the last block of
-// the group adds it to r^T D^-1 r and updates the CG scalars and masks.  In
-// the start-of-solve mode it also solves for P^T b to complete b^T M^-1 b.
-constexpr int kRowsPerCta = 64;
+// Per iteration: y = Binv (P^T r), register-tiled.  A CTA owns 64 rows of
+// one group (grid = ncPad / 64 x groups) and 32 right-hand sides at a time;
+// its 128 threads each hold 4 rows x 4 columns.  Binv rows stream through
+// shared memory in 32-wide k chunks (double-buffered with cp.async), P^T r
+// sits in shared memory whole.  The CTA writes y for the direction kernel
+// and its partial (P^T r).y; the last CTA of the group adds the partials in
+// a fixed order to r^T D^-1 r and updates the CG scalars and convergence
+// masks.  In the start-of-solve mode it also solves for P^T b to complete
+// b^T M^-1 b.
+constexpr int kCoarseRows = 64;    // rows per CTA
+constexpr int kCoarseThreads = 128;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 template <int KP>
-__global__ void __launch_bounds__(kCT) k_coarse(CgProblem P, int init) {
-    constexpr int CPT = KP / 4;  // right-hand sides per thread: 4 threads per row
-    const int g = blockIdx.y;
+__global__ void __launch_bounds__(kCoarseThreads) k_coarse(CgProblem P, int init) {
+    constexpr int NCH = KP < 32 ? 1 : KP / 32;  // 32-column chunks
+    constexpr int BS = 36;                      // Binv chunk row stride (floats, 16-byte multiple)
+    const int g = blockIdx.y, r0 = blockIdx.x * kCoarseRows;
     if (!init && !P.active[g]) return;
-    extern __shared__ float smc[];  // [ncPad][KP] restricted vector
-    __shared__ double red[2][kCT / 4][4];
-    __shared__ bool amLast;
     const int ncPad = P.ncPad;
+    extern __shared__ __align__(16) float smc[];
+    float* Rs = smc;                              // [ncPad][KP]
+    float* Bs = smc + (size_t)ncPad * KP;         // [2][64][BS]
+    __shared__ double red[16][33];
+    __shared__ bool amLast;
+    const float* B = P.Binv + ((size_t)g * ncPad + r0) * ncPad;
     const size_t cb = (size_t)g * ncPad * KP;
-    const int lr = threadIdx.x >> 2, cq = threadIdx.x & 3;
-    const int row = blockIdx.x * kRowsPerCta + lr;
-    const float* B = P.Binv + ((size_t)g * ncPad + row) * ncPad;
+    const int rl = threadIdx.x & 15, cgp = threadIdx.x >> 4;  // rows rl + 16 i, columns 4 cgp + j
     double* part = P.partC + ((size_t)g * gridDim.x + blockIdx.x) * 2 * KP;
+    auto load_chunk = [&](int buf, int k0) {
+        // 64 rows x 32 floats = 512 16-byte pieces, 4 per thread
+        for (int t = threadIdx.x; t < 512; t += kCoarseThreads) {
+            const int row = t >> 3, piece = t & 7;
+            cp_async16(Bs + ((size_t)buf * 64 + row) * BS + piece * 4, B + (size_t)row * ncPad + k0 + piece * 4);
+        }
+        cp_async_commit();
+    };
     for (int sys = 0; sys < (init ? 2 : 1); ++sys) {
         const float* src = (sys == 0 ? P.rc : P.rcB) + cb;
-        for (int t = threadIdx.x; t < ncPad * KP / 4; t += kCT)
-            reinterpret_cast<float4*>(smc)[t] = reinterpret_cast<const float4*>(src)[t];
-        __syncthreads();
-        float acc[CPT];
+        for (int t = threadIdx.x; t < ncPad * KP / 4; t += kCoarseThreads) cp_async16(Rs + 4 * t, src + 4 * t);
+        cp_async_commit();
+        for (int ch = 0; ch < NCH; ++ch) {
+            const int col0 = ch * 32 + cgp * 4;
+            float acc[4][4];
 #pragma unroll
-        for (int q = 0; q < CPT; ++q) acc[q] = 0.f;
-        for (int k = 0; k < ncPad; k += 4) {
-            const float4 b = __ldg(reinterpret_cast<const float4*>(B + k));
-            const float* v = smc + (size_t)k * KP + cq;
+            for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int q = 0; q < CPT; ++q) {
-                float a = acc[q];
-                a = fmaf(b.x, v[4 * q], a);
-                a = fmaf(b.y, v[KP + 4 * q], a);
-                a = fmaf(b.z, v[2 * KP + 4 * q], a);
-                a = fmaf(b.w, v[3 * KP + 4 * q], a);
-                acc[q] = a;
+                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+            load_chunk(0, 0);
+            const int nk = ncPad / 32;
+            for (int kc = 0; kc < nk; ++kc) {
+                if (kc + 1 < nk) {
+                    load_chunk((kc + 1) & 1, (kc + 1) * 32);
+                    cp_async_wait1();
+                } else {
+                    cp_async_wait0();
+                }
+                __syncthreads();
+                const float* Bc = Bs + (size_t)(kc & 1) * 64 * BS;
+                if (col0 < KP) {
+#pragma unroll 8
+                    for (int kk = 0; kk < 32; ++kk) {
+                        const float4 rv = *reinterpret_cast<const float4*>(Rs + (size_t)(kc * 32 + kk) * KP + col0);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const float bv = Bc[(rl + 16 * i) * BS + kk];
+                            acc[i][0] = fmaf(bv, rv.x, acc[i][0]);
+                            acc[i][1] = fmaf(bv, rv.y, acc[i][1]);
+                            acc[i][2] = fmaf(bv, rv.z, acc[i][2]);
+                            acc[i][3] = fmaf(bv, rv.w, acc[i][3]);
+                        }
+                    }
+                }
+                __syncthreads();
             }
-        }
-        // partial (P^T v).y of this CTA's rows, per right-hand side
-        double d[CPT];
+            // y out and per-column partial dots over this CTA's rows
+            double d[4] = {0.0, 0.0, 0.0, 0.0};
+            if (col0 < KP) {
 #pragma unroll
-        for (int q = 0; q < CPT; ++q) {
-            d[q] = (double)smc[(size_t)row * KP + cq + 4 * q] * (double)acc[q];
-            if (sys == 0) P.yc[cb + (size_t)row * KP + cq + 4 * q] = acc[q];
-        }
-        __syncthreads();
-        // reduce over the 64 rows, fixed order: column c = cq + 4 q
-        for (int q = 0; q < CPT; ++q) {
-            red[sys][lr][cq] = d[q];
+                for (int i = 0; i < 4; ++i) {
+                    const int row = r0 + rl + 16 * i;
+                    const float4 rr = *reinterpret_cast<const float4*>(Rs + (size_t)row * KP + col0);
+                    d[0] += (double)rr.x * acc[i][0];
+                    d[1] += (double)rr.y * acc[i][1];
+                    d[2] += (double)rr.z * acc[i][2];
+                    d[3] += (double)rr.w * acc[i][3];
+                    if (sys == 0)
+                        *reinterpret_cast<float4*>(P.yc + cb + (size_t)row * KP + col0) =
+                            make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) red[rl][cgp * 4 + j] = d[j];
             __syncthreads();
-            if (threadIdx.x < 4) {
+            if (threadIdx.x < 32 && ch * 32 + (int)threadIdx.x < KP) {
                 double t = 0.0;
-                for (int i = 0; i < kRowsPerCta; ++i) t += red[sys][i][threadIdx.x];
-                part[sys * KP + threadIdx.x + 4 * q] = t;
+                for (int q = 0; q < 16; ++q) t += red[q][threadIdx.x];
+                part[sys * KP + ch * 32 + threadIdx.x] = t;
             }
             __syncthreads();
         }
@@ -275,17 +325,19 @@ __global__ void __launch_bounds__(kCT) k_coarse(CgProblem P, int init) {
     }
 }
 
+size_t coarse_apply_smem(int ncPad, int KP) { return ((size_t)ncPad * KP + 2 * 64 * 36) * sizeof(float); }
+
 size_t coarse_solve_smem(int ncPad) { return ((size_t)(ncPad + 32) * 33 + 32 * 33) * sizeof(float); }
 
 template <int KP>
 int launch_coarse_kp(const CgProblem& P, bool init, cudaStream_t s, bool count) {
-    const size_t smem = (size_t)P.ncPad * KP * sizeof(float);
+    const size_t smem = coarse_apply_smem(P.ncPad, KP);
     static size_t configured = 0;
     if (smem > configured) {
         MPF_CUDA(cudaFuncSetAttribute(k_coarse<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
-    k_coarse<KP><<<dim3(P.ncPad / kRowsPerCta, P.G), kCT, smem, s>>>(P, init ? 1 : 0);
+    k_coarse<KP><<<dim3(P.ncPad / kCoarseRows, P.G), kCoarseThreads, smem, s>>>(P, init ? 1 : 0);
     if (count) {
         MPF_LAUNCHED(1);
     } else {
@@ -297,8 +349,8 @@ int launch_coarse_kp(const CgProblem& P, bool init, cudaStream_t s, bool count) 
 }  // namespace
 
 bool coarse_supported(int KP, int ncPad) {
-    return (KP == 16 || KP == 32 || KP == 64) && ncPad >= kRowsPerCta && ncPad % kRowsPerCta == 0 &&
-           (size_t)ncPad * KP * sizeof(float) <= 200 * 1024 && coarse_solve_smem(ncPad) <= 200 * 1024;
+    return (KP == 16 || KP == 32 || KP == 64) && ncPad >= kCoarseRows && ncPad % kCoarseRows == 0 &&
+           ncPad <= 1024 && coarse_apply_smem(ncPad, KP) <= 200 * 1024 && coarse_solve_smem(ncPad) <= 200 * 1024;
 }
 
 int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count) {

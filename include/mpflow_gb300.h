@@ -164,7 +164,9 @@ typedef struct mpf_solve_opts {
     int32_t max_iter;      /* 0: 10 * n_nodes, the reference default */
     double refine_tol;     /* > 0: FP64-residual iterative refinement to this level */
     int32_t max_refine;    /* outer refinement steps (default 6) */
-    int32_t warm_start;    /* 1: start from the fields left by the previous call */
+    int32_t warm_start;    /* 1: start from the fields left by the previous call (same frame
+                            *    count); 2: start every frame from the fields of the
+                            *    homogeneous distribution (solved once per model) */
     int32_t check_every;   /* iterations between host convergence checks (default 16) */
     /* 0: Jacobi (the reference's preconditioner::diagonal,
      *    src/numeric/preconditioner.cpp:59-76);

@@ -76,7 +76,7 @@ struct mpf_eit {
     // learned warm start: homogeneous voltages and the network input
     bool v0Ready = false;
     float v0InvRms = 1.f;
-    mpf::DevBuf<float> V0, learnX;
+    mpf::DevBuf<float> V0, X0, learnX;
     mpf::DevBuf<double> res0;
 
     ~mpf_eit() {
@@ -676,6 +676,8 @@ static int eit_jacobian(mpf_eit* m, int F, const float* gamma, const int* frameM
                                m->Jlo.ptr, s);
 }
 
+static int ensure_v0(mpf_eit* m, cudaStream_t s);
+
 // Forward solve into the workspace (fields X, voltages V, optional J).
 int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_solve_opts* optsIn,
                    mpf_solve_stats* stats, cudaStream_t s) {
@@ -684,6 +686,16 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     fill_defaults(optsIn, o, m->n);
     const bool refine = o.refine_tol > 0.0;
     MPF_TRY(ensure_workspace(m, F, refine, wantJ));
+    if (o.warm_start == 2) {
+        // every frame starts from the homogeneous fields
+        MPF_TRY(ensure_v0(m, s));
+        MPF_TRY(ensure_workspace(m, F, refine, wantJ));
+        const size_t per = (size_t)m->Ca * m->npad * m->KP;
+        for (int f = 0; f < F; ++f)
+            MPF_CUDA(cudaMemcpyAsync(m->X.ptr + f * per, m->X0.ptr, per * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        m->fieldsValid = true;
+        m->lastFrames = F;
+    }
     const bool warm = o.warm_start && m->fieldsValid && m->lastFrames == F;
     MPF_TRY(eit_assemble(m, F, gamma, refine, s));
     if (!warm) MPF_TRY(tune_cg(m, F, s));
@@ -853,17 +865,17 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
     std::vector<int> mask(F, 1), iters(F, 0);
     std::vector<double> res(F, 0.0);
     int cgTotal = 0, gnIters = 0;
-    bool warm = o.warm_start != 0, checkStart = fallback != nullptr;
+    int warm = o.warm_start, checkStart = fallback != nullptr;
     if (accepted)
         for (int f = 0; f < F; ++f) accepted[f] = 1;
     for (int it = 0;;) {
         mpf_solve_stats fs{};
         mpf_solve_opts oi = o;
-        oi.warm_start = warm ? 1 : 0;
+        oi.warm_start = warm;
         int st = eit_forward_ws(m, F, gamma, false, &oi, &fs, s);
         if (st != MPF_OK && st != MPF_ENOCONV) return st;
         MPF_TRY(ensure_workspace(m, F, false, true));
-        warm = true;
+        warm = 1;
         cgTotal += fs.iterations;
         MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
         MPF_CUDA(cudaMemcpyAsync(res.data(), m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
@@ -934,6 +946,9 @@ static int ensure_v0(mpf_eit* m, cudaStream_t s) {
     o.tol = 1e-6;
     o.refine_tol = 1e-9;
     MPF_TRY(eit_forward_ws(m, 1, g0.ptr, false, &o, nullptr, s));
+    const size_t per = (size_t)m->Ca * m->npad * m->KP;
+    MPF_TRY(m->X0.alloc(per));
+    MPF_CUDA(cudaMemcpyAsync(m->X0.ptr, m->X.ptr, per * sizeof(float), cudaMemcpyDeviceToDevice, s));
     MPF_TRY(m->V0.alloc((size_t)L));
     MPF_CUDA(cudaMemcpyAsync(m->V0.ptr, m->V.ptr, sizeof(float) * L, cudaMemcpyDeviceToDevice, s));
     std::vector<float> h(L);

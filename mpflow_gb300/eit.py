@@ -129,18 +129,23 @@ class SolveOptions:
     "two-level" (Jacobi plus an aggregation coarse correction)."""
 
     PRECONDITIONERS = {"jacobi": 0, "two-level": 1}
+    # warm_start: False/0 cold, True/1/"previous" fields of the previous call,
+    # 2/"homogeneous" fields of the homogeneous distribution
+    WARM_STARTS = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, "previous": 1, "homogeneous": 2}
 
     def __init__(self, tol=1e-6, max_iter=0, refine_tol=0.0, max_refine=6, warm_start=False,
                  check_every=16, preconditioner: str = "jacobi"):
         self.tol, self.max_iter, self.refine_tol = tol, max_iter, refine_tol
         self.max_refine, self.warm_start, self.check_every = max_refine, warm_start, check_every
+        if warm_start not in self.WARM_STARTS:
+            raise ValueError(f"warm_start must be one of {list(self.WARM_STARTS)}")
         if preconditioner not in self.PRECONDITIONERS:
             raise ValueError(f"preconditioner must be one of {sorted(self.PRECONDITIONERS)}")
         self.preconditioner = preconditioner
 
     def c(self) -> _ffi.SolveOpts:
         return _ffi.SolveOpts(float(self.tol), int(self.max_iter), float(self.refine_tol),
-                              int(self.max_refine), int(bool(self.warm_start)), int(self.check_every),
+                              int(self.max_refine), self.WARM_STARTS[self.warm_start], int(self.check_every),
                               self.PRECONDITIONERS[self.preconditioner])
 
 

@@ -316,3 +316,22 @@ def test_two_level_warm_start_and_gn():
     # same reconstruction, fewer CG iterations
     assert rel_err(res["two-level"][0], res["jacobi"][0]) < 1e-2
     assert res["two-level"][1] < res["jacobi"][1]
+
+
+def test_homogeneous_field_warm_start():
+    """warm_start='homogeneous' reproduces the cold solve with fewer iterations."""
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=24, ports=16, components=3, height=2.0, logarithmic=True)
+    model = mp.EIT(mesh, src, 1.0, components=3, height=2.0, logarithmic=True)
+    g = torch.tensor(np.stack([10 * np.log10(inclusion_sigma(mesh, seed=s)) for s in range(3)]),
+                     dtype=torch.float32, device="cuda")
+    for pc in ("jacobi", "two-level"):
+        V1 = model.solve(g, mp.SolveOptions(tol=1e-7, preconditioner=pc)).cpu().numpy()
+        cold = model.last_stats.iterations
+        V2 = model.solve(g, mp.SolveOptions(tol=1e-7, preconditioner=pc, warm_start="homogeneous")).cpu().numpy()
+        assert rel_err(V2, V1) < 1e-5
+        assert model.last_stats.iterations < cold
+        # the homogeneous distribution itself needs no iterations from its own fields
+        model.solve(torch.zeros_like(g), mp.SolveOptions(tol=1e-6, preconditioner=pc, warm_start="homogeneous"))
+        assert model.last_stats.iterations <= 1

@@ -248,6 +248,27 @@ int mpf_gn_solve(mpf_eit_t model, int32_t frames, float* gamma, const float* v_m
                  double target, int32_t max_gn_iters, const mpf_solve_opts* opts, int32_t* iterations,
                  double* residual, mpf_gn_stats* stats, mpf_stream_t stream);
 
+/* Regulariser of the inverse step: solver::Inverse::RegularizationType
+ * (include/mpflow/solver/inverse.h:31-35). */
+enum mpf_regularization { MPF_REG_IDENTITY = 0, MPF_REG_NOSER = 1, MPF_REG_LAPLACIAN = 2 };
+
+/* One regularised inverse step, solver::Inverse::updateJacobian + solve
+ * (src/solver/inverse.cpp:60-238):
+ *   (J^T J + (ref * factor)^2 R) result = J^T (measurement - calculation)
+ * for `images` right-hand sides (parallelImages), R = I, diag(J^T J) (NOSER)
+ * or L^T L with the reference's edge-length Laplacian.  R = I is solved in
+ * its dual form for any mesh size; NOSER and Laplacian assemble the E x E
+ * system and need n_elements <= 6144 (MPF_ENOTSUP beyond).  Exact FP64
+ * Cholesky solve where the reference runs a dense CG.  Synchronises.
+ *   jacobian:    device, reference layout (column-major jacobian_rows x E),
+ *                e.g. the output of mpf_eit_forward
+ *   calculation, measurement: device, images x (meas_count * drive_count),
+ *                each image column-major meas_count x drive_count
+ *   result:      device, images x n_elements */
+int mpf_inverse_solve(mpf_eit_t model, int32_t regularization, double factor, int32_t images,
+                      const float* jacobian, const float* calculation, const float* measurement,
+                      float* result, mpf_stream_t stream);
+
 /* Kernel timing hook: runs `reps` CG iterations on the systems of `gamma`
  * and reports, for the SpMM, update and direction kernels, the mean CUDA-
  * event time of one launch (ms[3]) and its algorithmic bytes (bytes[3]).

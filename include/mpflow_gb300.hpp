@@ -1,0 +1,661 @@
+// mpflow_gb300.hpp -- C++ facade with mpFlow's class names and signatures.
+//
+// Header-only, on top of the C ABI in mpflow_gb300.h.  It keeps the names,
+// constructor and method signatures of the reference's public classes so that
+// code written against them compiles with few changes:
+//   numeric::Matrix<T>          include/mpflow/numeric/matrix.h
+//   numeric::IrregularMesh      include/mpflow/numeric/irregular_mesh.h
+//   numeric::ConjugateGradient  include/mpflow/numeric/conjugate_gradient.h (solver tag)
+//   FEM::Ports, FEM::Sources<T> include/mpflow/fem/ports.h, sources.h
+//   FEM::Equation, basis::Linear include/mpflow/fem/equation.h (template tags)
+//   models::EIT<...>            include/mpflow/models/eit.h
+//   solver::Inverse<...>        include/mpflow/solver/inverse.h
+//   solver::Solver<...>         include/mpflow/solver/solver.h
+// Differences a caller sees: Eigen arrays become numeric::Array2<T> (row-major
+// host arrays with (i, j) access); cublasHandle_t parameters are accepted and
+// ignored (no cuBLAS is used); failures throw the exception type the
+// reference throws (std::invalid_argument for bad arguments,
+// std::runtime_error otherwise) with the library's message.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <fstream>
+#include <iomanip>
+#include <limits>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mpflow_gb300.h"
+
+typedef struct cublasContext* cublasHandle_t;  // accepted for signature compatibility, never used
+
+namespace mpFlow {
+
+namespace detail {
+inline void check(int status, const char* where) {
+    if (status == MPF_OK) return;
+    const std::string msg = std::string(where) + ": " + mpf_last_error();
+    if (status == MPF_EINVAL) throw std::invalid_argument(msg);
+    throw std::runtime_error(msg);
+}
+inline void cuda(cudaError_t e, const char* where) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(where) + ": " + cudaGetErrorString(e));
+}
+}  // namespace detail
+
+namespace math {
+// include/mpflow/mathematics.h:42-44
+inline unsigned roundTo(unsigned value, unsigned step) { return value == 0 ? 0 : ((value + step - 1) / step) * step; }
+}  // namespace math
+
+namespace numeric {
+
+// Row-major host array standing in for the reference's Eigen arrays.
+template <class T>
+struct Array2 {
+    unsigned rowsCount = 0, colsCount = 0;
+    std::vector<T> data;
+    Array2() = default;
+    Array2(unsigned r, unsigned c, T v = T(0)) : rowsCount(r), colsCount(c), data((size_t)r * c, v) {}
+    unsigned rows() const { return rowsCount; }
+    unsigned cols() const { return colsCount; }
+    T& operator()(unsigned i, unsigned j) { return data[(size_t)i * colsCount + j]; }
+    const T& operator()(unsigned i, unsigned j) const { return data[(size_t)i * colsCount + j]; }
+};
+
+// Dense column-major matrix with padded leading dimension dataRows =
+// roundTo(rows, 16) unless rows % 16 == 0 or rows == 1 (src/numeric/matrix.cpp:
+// 35-97); owns a device buffer and a host copy.
+template <class type>
+class Matrix {
+public:
+    Matrix(unsigned const rows, unsigned const cols, cudaStream_t const stream = nullptr, type const value = type(0),
+           bool const allocHost = true)
+        : rows(rows), cols(cols), dataRows(mpf_data_rows(rows)), dataCols(mpf_data_rows(cols)) {
+        if (rows == 0) throw std::invalid_argument("mpFlow::numeric::Matrix::Matrix: rows == 0");
+        if (cols == 0) throw std::invalid_argument("mpFlow::numeric::Matrix::Matrix: cols == 0");
+        detail::cuda(cudaMalloc((void**)&deviceData, sizeof(type) * (size_t)dataRows * dataCols),
+                     "mpFlow::numeric::Matrix::Matrix: cudaMalloc");
+        if (allocHost) host_.assign((size_t)dataRows * dataCols, type(0));
+        fill(value, stream);
+    }
+    Matrix(Matrix const&) = delete;
+    Matrix& operator=(Matrix const&) = delete;
+    virtual ~Matrix() { cudaFree(deviceData); }
+
+    static std::shared_ptr<Matrix<type>> eye(unsigned const size, cudaStream_t const stream = nullptr) {
+        auto m = std::make_shared<Matrix<type>>(size, size, stream);
+        for (unsigned i = 0; i < size; ++i) (*m)(i, i) = type(1);
+        m->copyToDevice(stream);
+        return m;
+    }
+
+    void copyToDevice(cudaStream_t const stream = nullptr) {
+        requireHost("copyToDevice");
+        detail::cuda(cudaMemcpyAsync(deviceData, host_.data(), sizeof(type) * host_.size(), cudaMemcpyHostToDevice,
+                                     stream),
+                     "mpFlow::numeric::Matrix::copyToDevice");
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::numeric::Matrix::copyToDevice");
+    }
+    void copyToHost(cudaStream_t const stream = nullptr) const {
+        requireHost("copyToHost");
+        detail::cuda(cudaMemcpyAsync(host_.data(), deviceData, sizeof(type) * host_.size(), cudaMemcpyDeviceToHost,
+                                     stream),
+                     "mpFlow::numeric::Matrix::copyToHost");
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::numeric::Matrix::copyToHost");
+    }
+    void fill(type const value, cudaStream_t const stream = nullptr) {
+        std::vector<type> v((size_t)dataRows * dataCols, type(0));
+        for (unsigned j = 0; j < cols; ++j)
+            for (unsigned i = 0; i < rows; ++i) v[i + (size_t)j * dataRows] = value;
+        if (!host_.empty()) host_ = v;
+        detail::cuda(cudaMemcpyAsync(deviceData, v.data(), sizeof(type) * v.size(), cudaMemcpyHostToDevice, stream),
+                     "mpFlow::numeric::Matrix::fill");
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::numeric::Matrix::fill");
+    }
+    // device-side copy of another matrix of the same shape
+    void copy(std::shared_ptr<Matrix<type> const> const other, cudaStream_t const stream = nullptr) {
+        if (!other || other->dataRows != dataRows || other->dataCols != dataCols)
+            throw std::invalid_argument("mpFlow::numeric::Matrix::copy: shape mismatch");
+        detail::cuda(cudaMemcpyAsync(deviceData, other->deviceData, sizeof(type) * (size_t)dataRows * dataCols,
+                                     cudaMemcpyDeviceToDevice, stream),
+                     "mpFlow::numeric::Matrix::copy");
+    }
+
+    type& operator()(unsigned const i, unsigned const j) {
+        requireHost("operator()");
+        if (i >= rows || j >= cols) throw std::invalid_argument("mpFlow::numeric::Matrix::operator(): index out of range");
+        return host_[i + (size_t)j * dataRows];
+    }
+    type operator()(unsigned const i, unsigned const j) const {
+        requireHost("operator()");
+        if (i >= rows || j >= cols) throw std::invalid_argument("mpFlow::numeric::Matrix::operator(): index out of range");
+        return host_[i + (size_t)j * dataRows];
+    }
+
+    // text I/O (src/numeric/matrix.cpp:684-822): whitespace-separated rows
+    static std::shared_ptr<Matrix<type>> loadtxt(std::istream& istream, cudaStream_t const stream = nullptr) {
+        std::vector<std::vector<type>> values;
+        std::string line;
+        while (std::getline(istream, line)) {
+            std::istringstream ls(line);
+            std::vector<type> row;
+            type v;
+            while (ls >> v) row.push_back(v);
+            if (!row.empty()) values.push_back(row);
+        }
+        if (values.empty()) throw std::runtime_error("mpFlow::numeric::Matrix::loadtxt: no values");
+        auto m = std::make_shared<Matrix<type>>((unsigned)values.size(), (unsigned)values[0].size(), stream);
+        for (unsigned i = 0; i < m->rows; ++i) {
+            if (values[i].size() != m->cols) throw std::runtime_error("mpFlow::numeric::Matrix::loadtxt: ragged rows");
+            for (unsigned j = 0; j < m->cols; ++j) (*m)(i, j) = values[i][j];
+        }
+        m->copyToDevice(stream);
+        return m;
+    }
+    static std::shared_ptr<Matrix<type>> loadtxt(std::string const filename, cudaStream_t const stream = nullptr) {
+        std::ifstream f(filename);
+        if (!f) throw std::runtime_error("mpFlow::numeric::Matrix::loadtxt: cannot open file: " + filename);
+        return loadtxt(f, stream);
+    }
+    void savetxt(std::ostream& ostream) const {
+        ostream << std::setprecision(std::numeric_limits<type>::max_digits10);
+        for (unsigned i = 0; i < rows; ++i) {
+            for (unsigned j = 0; j < cols; ++j) ostream << (j ? " " : "") << (*this)(i, j);
+            ostream << "\n";
+        }
+    }
+    void savetxt(std::string const filename) const {
+        std::ofstream f(filename);
+        if (!f) throw std::runtime_error("mpFlow::numeric::Matrix::savetxt: cannot open file: " + filename);
+        savetxt(f);
+    }
+
+    unsigned const rows, cols, dataRows, dataCols;
+    type* deviceData = nullptr;
+    type* hostData() const { return host_.data(); }
+    // the EIT model whose solve produced this matrix (used by solver::Inverse)
+    mpf_eit_t owner = nullptr;
+
+private:
+    void requireHost(const char* what) const {
+        if (host_.empty())
+            throw std::logic_error(std::string("mpFlow::numeric::Matrix::") + what + ": host memory was not allocated");
+    }
+    mutable std::vector<type> host_;
+};
+
+// Krylov solver tags of models::EIT (the solve itself runs in the library)
+template <class T>
+class ConjugateGradient {};
+
+// Triangular mesh (src/numeric/irregular_mesh.cpp); edges, element edges and
+// boundary are derived by mpf_mesh_edges.
+class IrregularMesh {
+public:
+    IrregularMesh(Array2<double> const& nodes, Array2<int> const& elements) : nodes(nodes), elements(elements) {
+        if (nodes.cols() != 2) throw std::invalid_argument("mpFlow::numeric::IrregularMesh::IrregularMesh: nodes.cols != 2");
+        if (elements.cols() != 3)
+            throw std::invalid_argument("mpFlow::numeric::IrregularMesh::IrregularMesh: elements.cols != 3");
+        const unsigned e = elements.rows();
+        std::vector<int32_t> ed((size_t)6 * e), ee((size_t)3 * e), bd((size_t)3 * e);
+        int32_t ne = 0, nb = 0;
+        detail::check(mpf_mesh_edges((int32_t)nodes.rows(), (int32_t)e, nodes.data.data(), elements.data.data(),
+                                     ed.data(), ee.data(), bd.data(), &ne, &nb),
+                      "mpFlow::numeric::IrregularMesh::IrregularMesh");
+        edges = Array2<int>((unsigned)ne, 2);
+        std::copy(ed.begin(), ed.begin() + 2 * (size_t)ne, edges.data.begin());
+        elementEdges = Array2<int>(e, 3);
+        std::copy(ee.begin(), ee.end(), elementEdges.data.begin());
+        boundary.assign(bd.begin(), bd.begin() + nb);
+    }
+
+    // concentric-ring disk (stands in for the distmesh branch of fromConfig)
+    static std::shared_ptr<IrregularMesh> ring(unsigned const rings, double const radius = 1.0) {
+        int32_t n = 0, e = 0;
+        detail::check(mpf_ring_mesh_counts((int32_t)rings, &n, &e), "mpFlow::numeric::IrregularMesh::ring");
+        Array2<double> nd((unsigned)n, 2);
+        Array2<int> el((unsigned)e, 3);
+        detail::check(mpf_ring_mesh((int32_t)rings, radius, nd.data.data(), el.data.data()),
+                      "mpFlow::numeric::IrregularMesh::ring");
+        return std::make_shared<IrregularMesh>(nd, el);
+    }
+
+    Array2<double> elementNodes(unsigned const element) const {
+        Array2<double> out(3, 2);
+        for (unsigned i = 0; i < 3; ++i)
+            for (unsigned k = 0; k < 2; ++k) out(i, k) = nodes(elements(element, i), k);
+        return out;
+    }
+    Array2<double> edgeNodes(unsigned const edge) const {
+        Array2<double> out(2, 2);
+        for (unsigned i = 0; i < 2; ++i)
+            for (unsigned k = 0; k < 2; ++k) out(i, k) = nodes(edges(edge, i), k);
+        return out;
+    }
+
+    Array2<double> const nodes;
+    Array2<int> const elements;
+    Array2<int> elementEdges;
+    Array2<int> edges;
+    std::vector<int> boundary;
+};
+
+}  // namespace numeric
+
+namespace FEM {
+
+namespace basis {
+class Linear {};
+}  // namespace basis
+
+// equation template tag: data type, basis, logarithmic parametrisation
+template <class dataType_ = float, class basisFunctionType = basis::Linear, bool logarithmic_ = true>
+class Equation {
+public:
+    typedef dataType_ dataType;
+    static bool const logarithmic = logarithmic_;
+};
+
+class Ports {
+public:
+    explicit Ports(numeric::Array2<int> const& edges) : edges(edges), count(edges.rows()) {
+        if (edges.rows() == 0) throw std::invalid_argument("mpFlow::FEM::Ports::Ports: edges.rows() == 0");
+    }
+    virtual ~Ports() {}
+
+    static std::shared_ptr<Ports> circularBoundary(unsigned const count, double const width,
+                                                   std::shared_ptr<numeric::IrregularMesh const> const mesh,
+                                                   double const offset = 0.0, bool const clockwise = false) {
+        if (!mesh) throw std::invalid_argument("mpFlow::FEM::Ports::circularBoundary: mesh == nullptr");
+        const int32_t cap = 512;
+        std::vector<int32_t> out((size_t)count * cap, -1);
+        int32_t mx = 0;
+        detail::check(mpf_ports_circular((int32_t)mesh->nodes.rows(), mesh->nodes.data.data(),
+                                         (int32_t)mesh->elements.rows(), mesh->elements.data.data(),
+                                         mesh->edges.data.data(), (int32_t)mesh->boundary.size(),
+                                         mesh->boundary.data(), (int32_t)count, width, offset, clockwise ? 1 : 0,
+                                         out.data(), cap, &mx),
+                      "mpFlow::FEM::Ports::circularBoundary");
+        numeric::Array2<int> e(count, (unsigned)std::max(mx, 1), -1);
+        for (unsigned p = 0; p < count; ++p)
+            for (unsigned k = 0; k < e.cols(); ++k) e(p, k) = out[(size_t)p * cap + k];
+        return std::make_shared<Ports>(e);
+    }
+
+    numeric::Array2<int> const edges;
+    unsigned const count;
+};
+
+template <class dataType>
+class Sources {
+public:
+    enum Type { Open, Fixed };
+
+    Sources(Type const type, std::vector<dataType> const& values, std::shared_ptr<Ports const> const ports,
+            std::shared_ptr<numeric::Matrix<int> const> const drivePattern,
+            std::shared_ptr<numeric::Matrix<int> const> const measurementPattern, cudaStream_t const stream)
+        : type(type), values(values), ports(ports) {
+        if (!ports) throw std::invalid_argument("mpFlow::FEM::Sources::Sources: ports == nullptr");
+        if (!drivePattern) throw std::invalid_argument("mpFlow::FEM::Sources::Sources: drivePattern == nullptr");
+        if (!measurementPattern)
+            throw std::invalid_argument("mpFlow::FEM::Sources::Sources: measurementPattern == nullptr");
+        if (values.size() != drivePattern->cols)
+            throw std::invalid_argument("mpFlow::FEM::Sources::Sources: invalid size of values vector");
+        this->drivePattern = convert(drivePattern, stream);
+        this->measurementPattern = convert(measurementPattern, stream);
+        // pattern = [value_c * drive_c | meas] (src/fem/sources.cpp:50-75)
+        const unsigned L = drivePattern->rows, Md = drivePattern->cols, Mm = measurementPattern->cols;
+        pattern = std::make_shared<numeric::Matrix<dataType>>(L, Md + Mm, stream);
+        for (unsigned i = 0; i < L; ++i) {
+            for (unsigned j = 0; j < Md; ++j) (*pattern)(i, j) = values[j] * (dataType)(*drivePattern)(i, j);
+            for (unsigned j = 0; j < Mm; ++j) (*pattern)(i, Md + j) = (dataType)(*measurementPattern)(i, j);
+        }
+        pattern->copyToDevice(stream);
+    }
+    Sources(Type const type, dataType const value, std::shared_ptr<Ports const> const ports,
+            std::shared_ptr<numeric::Matrix<int> const> const drivePattern,
+            std::shared_ptr<numeric::Matrix<int> const> const measurementPattern, cudaStream_t const stream)
+        : Sources(type, std::vector<dataType>(drivePattern ? drivePattern->cols : 0, value), ports, drivePattern,
+                  measurementPattern, stream) {}
+    virtual ~Sources() {}
+
+    Type const type;
+    std::vector<dataType> const values;
+    std::shared_ptr<Ports const> const ports;
+    std::shared_ptr<numeric::Matrix<dataType>> drivePattern;
+    std::shared_ptr<numeric::Matrix<dataType>> measurementPattern;
+    std::shared_ptr<numeric::Matrix<dataType>> pattern;
+
+private:
+    static std::shared_ptr<numeric::Matrix<dataType>> convert(std::shared_ptr<numeric::Matrix<int> const> const m,
+                                                              cudaStream_t const stream) {
+        auto out = std::make_shared<numeric::Matrix<dataType>>(m->rows, m->cols, stream);
+        for (unsigned i = 0; i < m->rows; ++i)
+            for (unsigned j = 0; j < m->cols; ++j) (*out)(i, j) = (dataType)(*m)(i, j);
+        out->copyToDevice(stream);
+        return out;
+    }
+};
+
+}  // namespace FEM
+
+namespace models {
+
+// 2.5D EIT forward model (src/models/eit.cpp).  Besides the reference's
+// members it carries `options` (mpf_solve_opts: tolerance, refinement,
+// preconditioner) and `handle()` for direct C-ABI calls.
+template <template <class> class numericalSolverType = numeric::ConjugateGradient,
+          class equationType_ = FEM::Equation<float, FEM::basis::Linear, false>>
+class EIT {
+public:
+    typedef equationType_ equationType;
+    typedef typename equationType::dataType dataType;
+    static bool const logarithmic = equationType::logarithmic;
+
+    EIT(std::shared_ptr<numeric::IrregularMesh const> const mesh, std::shared_ptr<FEM::Sources<dataType> const> const sources,
+        dataType const referenceValue, cublasHandle_t const handle, cudaStream_t const stream,
+        unsigned const components = 1, double const height = 1.0, double const portHeight = 1.0)
+        : mesh(mesh), sources(sources), referenceValue(referenceValue), height(height), portHeight(portHeight) {
+        (void)handle;
+        if (!mesh) throw std::invalid_argument("mpFlow::models::EIT::EIT: mesh == nullptr");
+        if (!sources) throw std::invalid_argument("mpFlow::models::EIT::EIT: sources == nullptr");
+        const unsigned L = sources->ports->count, Md = sources->drivePattern->cols, Mm = sources->measurementPattern->cols;
+        std::vector<double> drive((size_t)L * Md), meas((size_t)L * Mm), vals(sources->values.begin(), sources->values.end());
+        for (unsigned j = 0; j < Md; ++j)
+            for (unsigned i = 0; i < L; ++i) drive[i + (size_t)j * L] = (*sources->drivePattern)(i, j);
+        for (unsigned j = 0; j < Mm; ++j)
+            for (unsigned i = 0; i < L; ++i) meas[i + (size_t)j * L] = (*sources->measurementPattern)(i, j);
+        int device = 0;
+        detail::cuda(cudaGetDevice(&device), "mpFlow::models::EIT::EIT");
+        mpf_eit_desc d{};
+        d.n_nodes = (int32_t)mesh->nodes.rows();
+        d.n_elements = (int32_t)mesh->elements.rows();
+        d.nodes = mesh->nodes.data.data();
+        d.elements = mesh->elements.data.data();
+        d.edges = mesh->edges.data.data();
+        d.n_edges = (int32_t)mesh->edges.rows();
+        d.ports = (int32_t)L;
+        d.port_edges = sources->ports->edges.data.data();
+        d.port_edges_cap = (int32_t)sources->ports->edges.cols();
+        d.drive_count = (int32_t)Md;
+        d.meas_count = (int32_t)Mm;
+        d.drive_pattern = drive.data();
+        d.meas_pattern = meas.data();
+        d.source_values = vals.data();
+        d.source_type = sources->type == FEM::Sources<dataType>::Open ? MPF_SOURCE_OPEN : MPF_SOURCE_FIXED;
+        d.reference_value = referenceValue;
+        d.logarithmic = logarithmic ? 1 : 0;
+        d.components = (int32_t)components;
+        d.height = height;
+        d.port_height = portHeight;
+        d.device = device;
+        d.jacobian_mode = 0;
+        detail::check(mpf_eit_create(&d, &model_), "mpFlow::models::EIT::EIT");
+        detail::check(mpf_eit_get_info(model_, &info_), "mpFlow::models::EIT::EIT");
+        result = std::make_shared<numeric::Matrix<dataType>>(Mm, Md, stream);
+        jacobian = std::make_shared<numeric::Matrix<dataType>>((unsigned)info_.jacobian_rows, mesh->elements.rows(), stream,
+                                                               dataType(0), false);
+        jacobian->owner = model_;
+        result->owner = model_;
+        for (unsigned c = 0; c < components; ++c)
+            fields.push_back(std::make_shared<numeric::Matrix<dataType>>(mesh->nodes.rows(), Md + Mm, stream,
+                                                                         dataType(0), false));
+        field = fields[0];
+        options.tol = 1e-6;
+        options.max_iter = 0;
+        options.refine_tol = 0.0;
+        options.max_refine = 6;
+        options.warm_start = 0;
+        options.check_every = 16;
+        options.preconditioner = 0;
+    }
+    EIT(EIT const&) = delete;
+    EIT& operator=(EIT const&) = delete;
+    virtual ~EIT() { mpf_eit_destroy(model_); }
+
+    // forward solve of one material distribution (E x 1); returns the
+    // Mm x Md electrode voltages and updates jacobian and fields
+    std::shared_ptr<numeric::Matrix<dataType> const> solve(
+        std::shared_ptr<numeric::Matrix<dataType> const> const materialDistribution, cublasHandle_t const handle,
+        cudaStream_t const stream, unsigned* const steps = nullptr) {
+        (void)handle;
+        if (!materialDistribution)
+            throw std::invalid_argument("mpFlow::models::EIT::solve: materialDistribution == nullptr");
+        if (materialDistribution->rows != mesh->elements.rows())
+            throw std::invalid_argument("mpFlow::models::EIT::solve: materialDistribution has wrong size");
+        const unsigned Mm = result->rows, Md = result->cols;
+        float* V = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&V, sizeof(float) * (size_t)Mm * Md, stream), "mpFlow::models::EIT::solve");
+        mpf_solve_stats st{};
+        const int status = mpf_eit_forward(model_, 1, materialDistribution->deviceData, V, jacobian->deviceData,
+                                           &options, &st, stream);
+        if (status == MPF_OK || status == MPF_ENOCONV) {
+            detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(float) * result->dataRows, V, sizeof(float) * Mm,
+                                           sizeof(float) * Mm, Md, cudaMemcpyDeviceToDevice, stream),
+                         "mpFlow::models::EIT::solve");
+            fieldsValid_ = true;
+        }
+        cudaFreeAsync(V, stream);
+        detail::check(status == MPF_ENOCONV ? MPF_OK : status, "mpFlow::models::EIT::solve");
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::models::EIT::solve");
+        if (steps) *steps = (unsigned)st.iterations;
+        lastStats = st;
+        return result;
+    }
+
+    // potentials of the last solve, one matrix per 2.5D component
+    void updateFields(cudaStream_t const stream) {
+        if (!fieldsValid_) throw std::logic_error("mpFlow::models::EIT::updateFields: no solve yet");
+        const size_t per = (size_t)fields[0]->dataRows * fields[0]->cols;  // export layout: dataRows x cols per component
+        float* buf = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&buf, sizeof(float) * per * fields.size(), stream), "updateFields");
+        const int st = mpf_eit_fields(model_, 1, buf, stream);
+        if (st == MPF_OK)
+            for (size_t c = 0; c < fields.size(); ++c)
+                cudaMemcpyAsync(fields[c]->deviceData, buf + c * per, sizeof(float) * per, cudaMemcpyDeviceToDevice, stream);
+        cudaFreeAsync(buf, stream);
+        detail::check(st, "mpFlow::models::EIT::updateFields");
+        detail::cuda(cudaStreamSynchronize(stream), "updateFields");
+    }
+
+    mpf_eit_t handle() const { return model_; }
+    mpf_eit_info const& info() const { return info_; }
+
+    std::shared_ptr<numeric::IrregularMesh const> const mesh;
+    std::shared_ptr<FEM::Sources<dataType> const> const sources;
+    dataType const referenceValue;
+    double const height;
+    double const portHeight;
+    std::vector<std::shared_ptr<numeric::Matrix<dataType>>> fields;
+    std::shared_ptr<numeric::Matrix<dataType>> field;
+    std::shared_ptr<numeric::Matrix<dataType>> result;
+    std::shared_ptr<numeric::Matrix<dataType>> jacobian;
+    mpf_solve_opts options{};
+    mpf_solve_stats lastStats{};
+
+private:
+    mpf_eit_t model_ = nullptr;
+    mpf_eit_info info_{};
+    bool fieldsValid_ = false;
+};
+
+}  // namespace models
+
+namespace solver {
+
+// Regularised inverse step (src/solver/inverse.cpp); the system is solved
+// exactly by mpf_inverse_solve (dual form for R = I).
+template <class dataType, template <class> class numericalSolverType = numeric::ConjugateGradient>
+class Inverse {
+public:
+    enum RegularizationType { identity, noser, laplacian };
+
+    Inverse(std::shared_ptr<numeric::IrregularMesh const> const mesh,
+            std::shared_ptr<numeric::Matrix<dataType> const> const jacobian, dataType const referenceValue,
+            unsigned const parallelImages, cublasHandle_t const handle, cudaStream_t const stream)
+        : referenceValue(referenceValue), mesh(mesh), parallelImages_(parallelImages) {
+        if (!mesh) throw std::invalid_argument("mpFlow::solver::Inverse::Inverse: mesh == nullptr");
+        if (parallelImages == 0) throw std::invalid_argument("mpFlow::solver::Inverse::Inverse: parallelImages == 0");
+        result = std::make_shared<numeric::Matrix<dataType>>(mesh->elements.rows(), parallelImages, stream);
+        updateJacobian(jacobian, handle, stream);
+    }
+
+    void updateJacobian(std::shared_ptr<numeric::Matrix<dataType> const> const jacobian, cublasHandle_t const,
+                        cudaStream_t const) {
+        if (!jacobian) throw std::invalid_argument("mpFlow::solver::Inverse::updateJacobian: jacobian == nullptr");
+        if (!jacobian->owner)
+            throw std::invalid_argument("mpFlow::solver::Inverse::updateJacobian: jacobian does not come from a model");
+        this->jacobian = jacobian;
+    }
+
+    std::shared_ptr<numeric::Matrix<dataType> const> solve(
+        std::vector<std::shared_ptr<numeric::Matrix<dataType>>> const& calculation,
+        std::vector<std::shared_ptr<numeric::Matrix<dataType>>> const& measurement, cublasHandle_t const,
+        cudaStream_t const stream, unsigned const maxIterations = 0, unsigned* const iterations = nullptr) {
+        (void)maxIterations;
+        if (calculation.size() != parallelImages_ || measurement.size() != parallelImages_)
+            throw std::invalid_argument("mpFlow::solver::Inverse::solve: wrong number of images");
+        const unsigned Mm = calculation[0]->rows, Md = calculation[0]->cols, P = parallelImages_;
+        const size_t per = (size_t)Mm * Md;
+        float *calc = nullptr, *meas = nullptr, *out = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&calc, sizeof(float) * per * P * 2, stream), "mpFlow::solver::Inverse::solve");
+        meas = calc + per * P;
+        const unsigned E = mesh->elements.rows();
+        detail::cuda(cudaMallocAsync((void**)&out, sizeof(float) * (size_t)E * P, stream), "mpFlow::solver::Inverse::solve");
+        for (unsigned p = 0; p < P; ++p) {
+            cudaMemcpy2DAsync(calc + p * per, sizeof(float) * Mm, calculation[p]->deviceData,
+                              sizeof(float) * calculation[p]->dataRows, sizeof(float) * Mm, Md, cudaMemcpyDeviceToDevice,
+                              stream);
+            cudaMemcpy2DAsync(meas + p * per, sizeof(float) * Mm, measurement[p]->deviceData,
+                              sizeof(float) * measurement[p]->dataRows, sizeof(float) * Mm, Md, cudaMemcpyDeviceToDevice,
+                              stream);
+        }
+        const int st = mpf_inverse_solve(jacobian->owner, (int32_t)regularizationType_, regularizationFactor_, (int32_t)P,
+                                         jacobian->deviceData, calc, meas, out, stream);
+        if (st == MPF_OK)
+            cudaMemcpy2DAsync(result->deviceData, sizeof(float) * result->dataRows, out, sizeof(float) * E,
+                              sizeof(float) * E, P, cudaMemcpyDeviceToDevice, stream);
+        cudaFreeAsync(calc, stream);
+        cudaFreeAsync(out, stream);
+        detail::check(st, "mpFlow::solver::Inverse::solve");
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::solver::Inverse::solve");
+        if (iterations) *iterations = 1;  // one exact solve
+        return result;
+    }
+
+    void setRegularizationFactor(dataType const factor, cublasHandle_t const, cudaStream_t const) {
+        regularizationFactor_ = factor;
+    }
+    void setRegularizationType(RegularizationType const type, cublasHandle_t const, cudaStream_t const) {
+        regularizationType_ = type;
+    }
+    void setRegularizationParameter(dataType const factor, RegularizationType const type, cublasHandle_t const,
+                                    cudaStream_t const) {
+        regularizationFactor_ = factor;
+        regularizationType_ = type;
+    }
+    dataType regularizationFactor() const { return regularizationFactor_; }
+    RegularizationType regularizationType() const { return regularizationType_; }
+
+    dataType const referenceValue;
+
+private:
+    std::shared_ptr<numeric::IrregularMesh const> const mesh;
+    std::shared_ptr<numeric::Matrix<dataType> const> jacobian;
+    std::shared_ptr<numeric::Matrix<dataType>> result;
+    unsigned const parallelImages_;
+    dataType regularizationFactor_ = dataType(0);
+    RegularizationType regularizationType_ = identity;
+};
+
+// Difference and absolute reconstruction (src/solver/solver.cpp).
+template <class forwardModelType = models::EIT<>,
+          template <class> class numericalInverseSolverType = numeric::ConjugateGradient>
+class Solver {
+public:
+    typedef typename forwardModelType::dataType dataType;
+
+    Solver(std::shared_ptr<forwardModelType> const forwardModel, unsigned const parallelImages,
+           cublasHandle_t const handle, cudaStream_t const stream)
+        : forwardModel(forwardModel) {
+        if (!forwardModel) throw std::invalid_argument("mpFlow::solver::Solver::Solver: forwardModel == nullptr");
+        if (parallelImages == 0) throw std::invalid_argument("mpFlow::solver::Solver::Solver: parallelImages == 0");
+        const unsigned Mm = forwardModel->result->rows, Md = forwardModel->result->cols;
+        for (unsigned p = 0; p < parallelImages; ++p) {
+            measurement.push_back(std::make_shared<numeric::Matrix<dataType>>(Mm, Md, stream));
+            calculation.push_back(std::make_shared<numeric::Matrix<dataType>>(Mm, Md, stream));
+        }
+        const unsigned E = forwardModel->mesh->elements.rows();
+        const dataType start = forwardModelType::logarithmic ? dataType(0) : dataType(1);
+        referenceDistribution = std::make_shared<numeric::Matrix<dataType>>(E, 1, stream, start);
+        materialDistribution = std::make_shared<numeric::Matrix<dataType>>(E, 1, stream, start);
+        inverseSolver = std::make_shared<Inverse<dataType, numericalInverseSolverType>>(
+            forwardModel->mesh, forwardModel->jacobian, forwardModel->referenceValue, parallelImages, handle, stream);
+    }
+
+    // forward solve at the reference distribution; measurement and
+    // calculation start from its voltages (src/solver/solver.cpp:142-166)
+    void preSolve(cublasHandle_t const handle, cudaStream_t const stream) {
+        auto const initial = forwardModel->solve(referenceDistribution, handle, stream);
+        inverseSolver->updateJacobian(forwardModel->jacobian, handle, stream);
+        for (auto& m : measurement) m->copy(initial, stream);
+        for (auto& c : calculation) c->copy(initial, stream);
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::solver::Solver::preSolve");
+    }
+
+    std::shared_ptr<numeric::Matrix<dataType> const> solveDifferential(cublasHandle_t const handle,
+                                                                        cudaStream_t const stream,
+                                                                        unsigned const maxIterations = 0,
+                                                                        unsigned* const iterations = nullptr) {
+        auto const result = inverseSolver->solve(calculation, measurement, handle, stream, maxIterations, iterations);
+        add_first_column(result, referenceDistribution, stream);
+        return materialDistribution;
+    }
+
+    std::shared_ptr<numeric::Matrix<dataType> const> solveAbsolute(cublasHandle_t const handle,
+                                                                    cudaStream_t const stream,
+                                                                    unsigned const maxIterations = 0,
+                                                                    unsigned* const iterations = nullptr) {
+        if (measurement.size() != 1)
+            throw std::runtime_error("mpFlow::solver::Solver::solveAbsolute: parallelImages != 1");
+        forwardModel->solve(materialDistribution, handle, stream);
+        inverseSolver->updateJacobian(forwardModel->jacobian, handle, stream);
+        calculation[0]->copy(forwardModel->result, stream);
+        auto const result = inverseSolver->solve(calculation, measurement, handle, stream, maxIterations, iterations);
+        add_first_column(result, materialDistribution, stream);
+        return materialDistribution;
+    }
+
+    std::shared_ptr<forwardModelType> const forwardModel;
+    std::shared_ptr<Inverse<dataType, numericalInverseSolverType>> inverseSolver;
+    std::vector<std::shared_ptr<numeric::Matrix<dataType>>> measurement;
+    std::vector<std::shared_ptr<numeric::Matrix<dataType>>> calculation;
+    std::shared_ptr<numeric::Matrix<dataType>> referenceDistribution;
+    std::shared_ptr<numeric::Matrix<dataType>> materialDistribution;
+
+private:
+    // materialDistribution = base + first column of delta (host round trip: E values)
+    void add_first_column(std::shared_ptr<numeric::Matrix<dataType> const> const delta,
+                          std::shared_ptr<numeric::Matrix<dataType> const> const base, cudaStream_t const stream) {
+        const unsigned E = base->rows;
+        std::vector<dataType> a(E), b(E);
+        cudaMemcpyAsync(a.data(), base->deviceData, sizeof(dataType) * E, cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(b.data(), delta->deviceData, sizeof(dataType) * E, cudaMemcpyDeviceToHost, stream);
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::solver::Solver");
+        for (unsigned i = 0; i < E; ++i) a[i] += b[i];
+        detail::cuda(cudaMemcpyAsync(materialDistribution->deviceData, a.data(), sizeof(dataType) * E,
+                                     cudaMemcpyHostToDevice, stream),
+                     "mpFlow::solver::Solver");
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::solver::Solver");
+    }
+};
+
+}  // namespace solver
+}  // namespace mpFlow

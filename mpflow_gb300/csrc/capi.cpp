@@ -52,6 +52,8 @@ int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda,
 int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
 int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
+int inverse_solve(mpf_eit* m, int reg, double factor, int images, const float* Jref, const float* calc,
+                  const float* meas, float* result, cudaStream_t s);
 int mlp_create(int in, int h1, int h2, int out, unsigned long long seed, int device, mpf_mlp** res);
 void mlp_destroy(mpf_mlp* n);
 void mlp_layout(const mpf_mlp* n, int64_t* off);
@@ -345,6 +347,15 @@ int mpf_gn_solve_learned(mpf_eit_t model, mpf_mlp_t net, int32_t frames, float* 
         MPF_CHECK(lambda >= 0.0 && target >= 0.0, MPF_EINVAL, "mpf_gn_solve_learned: lambda and target must be >= 0");
         return mpf::gn_solve_learned(model, net, frames, gamma, v_meas, lambda, target, max_gn_iters, opts,
                                      iterations, residual, accepted, stats, (cudaStream_t)stream);
+    })
+}
+
+int mpf_inverse_solve(mpf_eit_t model, int32_t regularization, double factor, int32_t images, const float* jacobian,
+                      const float* calculation, const float* measurement, float* result, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpFlow::solver::Inverse::solve: model == nullptr");
+        return mpf::inverse_solve(model, regularization, factor, images, jacobian, calculation, measurement, result,
+                                  (cudaStream_t)stream);
     })
 }
 

@@ -1,0 +1,93 @@
+// State of one device-resident EIT model (the object behind mpf_eit_t),
+// shared by the translation units that orchestrate it (model.cu, inverse.cu).
+#pragma once
+
+#include <array>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "model.h"
+
+struct mpf_eit {
+    // sizes
+    int n = 0, E = 0, dataRows = 0, npad = 0, nblk = 0, W = 0, levels = 0;
+    int L = 0, Md = 0, Mm = 0, MdPad = 0, MmPad = 0, rowsJ = 0, Epad = 0;
+    int K = 0, KP = 0, C = 0, Ca = 0;
+    int sourceType = 0, logarithmic = 0, device = 0;
+    float ref = 1.f;
+    double height = 1.0, portHeight = 1.0;
+    // host copies
+    mpf::FemStructure fs;
+    std::vector<int> compOf;          // component -> active index or -1
+    std::vector<float> alphaH, betaH; // per active component
+    std::vector<double> betaAll;      // per component
+    // device: static structure
+    mpf::DevBuf<int32_t> cols, diagSlot, cptr, contrib, elements;
+    mpf::DevBuf<int32_t> rowOf;       // internal row of each node (Morton order, see eit_create)
+    mpf::DevBuf<float> Kf, Mf;
+    mpf::DevBuf<double> Kd, Md64;
+    mpf::DevBuf<float> Bc;            // [Ca][npad][KP] right-hand sides per active harmonic
+    mpf::DevBuf<double> Bc64;
+    mpf::DevBuf<float> alpha, beta, beta2, betaC, massCoef;
+    int exactJacobian = 0;
+    mpf::DevBuf<int32_t> dcFree, compOfD;
+    mpf::DevBuf<int32_t> nzPtr, nzNode;
+    mpf::DevBuf<double> nzVal;
+    mpf::DevBuf<int32_t> driveU, measU, rowD, rowM, colU;
+    mpf::DevBuf<float> driveScale, measScale, rowScale, colScale;
+    int anyDcFree = 0;
+    float dcScale = 1.f;              // c' of the Neumann rank-one term
+    mpf::DevBuf<double> dcShift;      // [KP] constant difference to the reference's solution
+    // workspace, grown on demand
+    int capF = 0, capF64 = 0, capFJ = 0;
+    mpf::DevBuf<float2> SR;           // slot values {S, R} per frame
+    mpf::DevBuf<float> X, Rv, Pv, Qv;
+    mpf::DevBuf<double> S64, R64, X64;
+    mpf::DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, rr, bb, Gm, sumP, sumX;
+    mpf::DevBuf<int> conv, active, iters;
+    mpf::DevBuf<unsigned> counter;
+    mpf::DevBuf<float> V, J, gramWork;
+    mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
+    mpf::DevBuf<double> A64, y, res;
+    mpf::DevBuf<int> info, frameMask;
+    long long nnz = 0;                // used ELL slots (matrix nonzeros)
+    std::vector<int> activeHost, itersHost;
+    int* pinnedActive = nullptr;
+    bool fieldsValid = false;
+    int lastFrames = 0;
+    // captured CG iteration chunks keyed by the problem bytes
+    std::map<std::string, cudaGraphExec_t> graphs;
+    // CG kernel variants {spmm, update, direction}: autotuned per frame count,
+    // or fixed by the caller (-1 = autotune)
+    std::map<int, std::array<int, 3>> cgVariants;
+    std::array<int, 3> forcedVariants{-1, -1, -1};
+    // two-level preconditioner: aggregate plan (static) and per-frame-count workspace
+    int nc = 0, ncPad = 0, coarseOK = 0, capFC = 0;
+    mpf::DevBuf<int32_t> cPairI, cPairJ, cPairPtr, cSlots;
+    mpf::DevBuf<float> cAggSize;
+    int cNnz = 0;
+    mpf::DevBuf<double> Ac64, rzFine, bzFine;
+    mpf::DevBuf<float> Lc, LinvD, Binv, rcV, rcB, ycV;
+    mpf::DevBuf<int> infoC;
+    // host copy of the mesh (reference numbering) for the Laplacian regulariser
+    std::vector<double> hostNodes;
+    std::vector<int32_t> hostElements;
+    // regularised inverse (mpf_inverse_solve) workspace
+    mpf::DevBuf<float> invJ, invWork;
+    mpf::DevBuf<__nv_bfloat16> invHi, invLo;
+    mpf::DevBuf<double> invA, invY, invB;
+    mpf::DevBuf<int> invInfo;
+    mpf::DevBuf<int32_t> lapRow, lapCol;
+    mpf::DevBuf<double> lapVal;
+    // learned warm start: homogeneous voltages and the network input
+    bool v0Ready = false;
+    float v0InvRms = 1.f;
+    mpf::DevBuf<float> V0, X0, learnX;
+    mpf::DevBuf<double> res0;
+
+    ~mpf_eit() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        if (pinnedActive) cudaFreeHost(pinnedActive);
+    }
+};

@@ -12,78 +12,7 @@
 
 #include "model.h"
 
-struct mpf_eit {
-    // sizes
-    int n = 0, E = 0, dataRows = 0, npad = 0, nblk = 0, W = 0, levels = 0;
-    int L = 0, Md = 0, Mm = 0, MdPad = 0, MmPad = 0, rowsJ = 0, Epad = 0;
-    int K = 0, KP = 0, C = 0, Ca = 0;
-    int sourceType = 0, logarithmic = 0, device = 0;
-    float ref = 1.f;
-    double height = 1.0, portHeight = 1.0;
-    // host copies
-    mpf::FemStructure fs;
-    std::vector<int> compOf;          // component -> active index or -1
-    std::vector<float> alphaH, betaH; // per active component
-    std::vector<double> betaAll;      // per component
-    // device: static structure
-    mpf::DevBuf<int32_t> cols, diagSlot, cptr, contrib, elements;
-    mpf::DevBuf<int32_t> rowOf;       // internal row of each node (Morton order, see eit_create)
-    mpf::DevBuf<float> Kf, Mf;
-    mpf::DevBuf<double> Kd, Md64;
-    mpf::DevBuf<float> Bc;            // [Ca][npad][KP] right-hand sides per active harmonic
-    mpf::DevBuf<double> Bc64;
-    mpf::DevBuf<float> alpha, beta, beta2, betaC, massCoef;
-    int exactJacobian = 0;
-    mpf::DevBuf<int32_t> dcFree, compOfD;
-    mpf::DevBuf<int32_t> nzPtr, nzNode;
-    mpf::DevBuf<double> nzVal;
-    mpf::DevBuf<int32_t> driveU, measU, rowD, rowM, colU;
-    mpf::DevBuf<float> driveScale, measScale, rowScale, colScale;
-    int anyDcFree = 0;
-    float dcScale = 1.f;              // c' of the Neumann rank-one term
-    mpf::DevBuf<double> dcShift;      // [KP] constant difference to the reference's solution
-    // workspace, grown on demand
-    int capF = 0, capF64 = 0, capFJ = 0;
-    mpf::DevBuf<float2> SR;           // slot values {S, R} per frame
-    mpf::DevBuf<float> X, Rv, Pv, Qv;
-    mpf::DevBuf<double> S64, R64, X64;
-    mpf::DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, rr, bb, Gm, sumP, sumX;
-    mpf::DevBuf<int> conv, active, iters;
-    mpf::DevBuf<unsigned> counter;
-    mpf::DevBuf<float> V, J, gramWork;
-    mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
-    mpf::DevBuf<double> A64, y, res;
-    mpf::DevBuf<int> info, frameMask;
-    long long nnz = 0;                // used ELL slots (matrix nonzeros)
-    std::vector<int> activeHost, itersHost;
-    int* pinnedActive = nullptr;
-    bool fieldsValid = false;
-    int lastFrames = 0;
-    // captured CG iteration chunks keyed by the problem bytes
-    std::map<std::string, cudaGraphExec_t> graphs;
-    // CG kernel variants {spmm, update, direction}: autotuned per frame count,
-    // or fixed by the caller (-1 = autotune)
-    std::map<int, std::array<int, 3>> cgVariants;
-    std::array<int, 3> forcedVariants{-1, -1, -1};
-    // two-level preconditioner: aggregate plan (static) and per-frame-count workspace
-    int nc = 0, ncPad = 0, coarseOK = 0, capFC = 0;
-    mpf::DevBuf<int32_t> cPairI, cPairJ, cPairPtr, cSlots;
-    mpf::DevBuf<float> cAggSize;
-    int cNnz = 0;
-    mpf::DevBuf<double> Ac64, rzFine, bzFine;
-    mpf::DevBuf<float> Lc, LinvD, Binv, rcV, rcB, ycV;
-    mpf::DevBuf<int> infoC;
-    // learned warm start: homogeneous voltages and the network input
-    bool v0Ready = false;
-    float v0InvRms = 1.f;
-    mpf::DevBuf<float> V0, X0, learnX;
-    mpf::DevBuf<double> res0;
-
-    ~mpf_eit() {
-        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
-        if (pinnedActive) cudaFreeHost(pinnedActive);
-    }
-};
+#include "eit_state.h"
 
 namespace mpf {
 namespace {
@@ -133,6 +62,9 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     m->C = d->components;
     m->height = d->height;
     m->portHeight = d->port_height;
+
+    m->hostNodes.assign(d->nodes, d->nodes + (size_t)2 * m->n);
+    m->hostElements.assign(d->elements, d->elements + (size_t)3 * m->E);
 
     // ---- internal node order: Morton (Z-order) of the coordinates, so that
     // consecutive rows are spatially compact patches (SpMM gathers stay in

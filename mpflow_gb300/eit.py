@@ -317,6 +317,26 @@ class EIT:
                                          ctypes.byref(st), _stream()))
         return g, iters, res, acc, st
 
+    REGULARIZATIONS = {"identity": 0, "noser": 1, "laplacian": 2}
+
+    def inverse(self, jacobian, calculation, measurement, factor: float, regularization: str = "identity"):
+        """One regularised inverse step (solver::Inverse, mpf_inverse_solve):
+        (J^T J + (ref factor)^2 R) dsigma = J^T (measurement - calculation) for
+        every image.  jacobian: (rowsJ, E) as returned by solve(jacobian=True)
+        for one frame; calculation, measurement: (images, Mm, Md).  Returns
+        dsigma (images, E)."""
+        import torch
+        if regularization not in self.REGULARIZATIONS:
+            raise ValueError(f"regularization must be one of {sorted(self.REGULARIZATIONS)}")
+        J = jacobian.reshape(self.jacobian_rows, -1).t().contiguous()  # reference layout storage (E, rowsJ)
+        images = calculation.shape[0]
+        calc = self._vmeas(calculation, images)
+        meas = self._vmeas(measurement, images)
+        out = torch.empty((images, self.mesh.elements.shape[0]), dtype=torch.float32, device=calc.device)
+        check(lib().mpf_inverse_solve(self._h, self.REGULARIZATIONS[regularization], float(factor), images, ptr(J),
+                                      ptr(calc), ptr(meas), ptr(out), _stream()))
+        return out
+
     def group_iterations(self) -> np.ndarray:
         """CG iterations per (frame, active harmonic) group of the last inner solve."""
         out = np.zeros(65536, np.int32)

@@ -392,3 +392,43 @@ def inverse_dual(J: np.ndarray, y: np.ndarray, ref: float, lam: float) -> np.nda
     w = np.ascontiguousarray(y, dtype=np.float64).copy()
     lib().orc_cholesky_solve(rows, _p(G), _p(w))
     return Jf.T @ w
+
+
+def laplacian_gram(nodes: np.ndarray, elements: np.ndarray) -> np.ndarray:
+    """L^T L of the edge-length Laplacian of Inverse::calcRegularizationMatrix
+    (src/solver/inverse.cpp:98-113): L[edge][element] = sign * |edge| with the
+    sign flipping between the two elements that share an edge (dense E x E)."""
+    E = elements.shape[0]
+    LtL = np.zeros((E, E))
+    first = {}
+    for e in range(E):
+        for i in range(3):
+            a, b = int(elements[e, i]), int(elements[e, (i + 1) % 3])
+            key = (min(a, b), max(a, b))
+            l2 = float(((nodes[a] - nodes[b]) ** 2).sum())
+            LtL[e, e] += l2
+            if key in first:
+                o = first[key]
+                LtL[e, o] -= l2
+                LtL[o, e] -= l2
+            else:
+                first[key] = e
+    return LtL
+
+
+def inverse_regularised(J: np.ndarray, Y: np.ndarray, ref: float, factor: float, kind: str,
+                        nodes=None, elements=None) -> np.ndarray:
+    """(J^T J + (ref*factor)^2 R) X = J^T Y in FP64 for R = I, diag(J^T J)
+    (NOSER) or the Laplacian L^T L (src/solver/inverse.cpp:60-130,213-238),
+    solved directly.  J: rows x E, Y: rows x images; returns E x images."""
+    JtJ = J.T @ J
+    mu = (ref * factor) ** 2
+    if kind == "identity":
+        R = np.eye(J.shape[1])
+    elif kind == "noser":
+        R = np.diag(np.diag(JtJ))
+    elif kind == "laplacian":
+        R = laplacian_gram(nodes, elements)
+    else:
+        raise ValueError(kind)
+    return np.linalg.solve(JtJ + mu * R, J.T @ Y)

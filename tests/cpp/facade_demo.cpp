@@ -1,0 +1,99 @@
+// Reconstruction through the C++ facade with mpFlow's class names: a forward
+// solve, a differential reconstruction of a low-conductivity inclusion, and a
+// text round trip of the voltages.  Prints one JSON line; exit status 0 when
+// every check holds.  Usage: facade_demo <rings> <electrodes>
+#include <cstdio>
+#include <cstdlib>
+#include <sstream>
+
+#include "mpflow_gb300.hpp"
+
+using namespace mpFlow;
+typedef models::EIT<numeric::ConjugateGradient, FEM::Equation<float, FEM::basis::Linear, false>> Model;
+
+int main(int argc, char** argv) {
+    const unsigned rings = argc > 1 ? (unsigned)atoi(argv[1]) : 16;
+    const unsigned L = argc > 2 ? (unsigned)atoi(argv[2]) : 16;
+    cudaStream_t stream = nullptr;
+    cublasHandle_t handle = nullptr;
+    try {
+        auto mesh = numeric::IrregularMesh::ring(rings);
+        auto ports = FEM::Ports::circularBoundary(L, 0.1, mesh);
+        auto pattern = std::make_shared<numeric::Matrix<int>>(L, L, stream);
+        for (unsigned j = 0; j < L; ++j) {
+            (*pattern)(j, j) = 1;
+            (*pattern)((j + 1) % L, j) = -1;
+        }
+        pattern->copyToDevice(stream);
+        auto sources = std::make_shared<FEM::Sources<float>>(FEM::Sources<float>::Open, 1e-3f, ports, pattern, pattern,
+                                                            stream);
+        auto model = std::make_shared<Model>(mesh, sources, 1.0f, handle, stream, 1, 1.0, 1.0);
+        model->options.tol = 1e-7;
+        const unsigned E = mesh->elements.rows();
+
+        // forward solve at the reference conductivity
+        auto reference = std::make_shared<numeric::Matrix<float>>(E, 1, stream, 1.0f);
+        unsigned steps = 0;
+        auto V0 = model->solve(reference, handle, stream, &steps);
+        V0->copyToHost(stream);
+        double sumV = 0.0, sumAbs = 0.0;
+        for (unsigned i = 0; i < V0->rows; ++i)
+            for (unsigned j = 0; j < V0->cols; ++j) {
+                sumV += (*V0)(i, j);
+                sumAbs += std::fabs((*V0)(i, j));
+            }
+
+        // measurement: an inclusion of 0.5 S/m at (0.3, 0.2), radius 0.25
+        auto target = std::make_shared<numeric::Matrix<float>>(E, 1, stream, 1.0f);
+        std::vector<int> inside;
+        for (unsigned e = 0; e < E; ++e) {
+            auto xy = mesh->elementNodes(e);
+            const double cx = (xy(0, 0) + xy(1, 0) + xy(2, 0)) / 3.0, cy = (xy(0, 1) + xy(1, 1) + xy(2, 1)) / 3.0;
+            if ((cx - 0.3) * (cx - 0.3) + (cy - 0.2) * (cy - 0.2) < 0.0625) {
+                (*target)(e, 0) = 0.5f;
+                inside.push_back((int)e);
+            }
+        }
+        target->copyToDevice(stream);
+        solver::Solver<Model> solver(model, 1, handle, stream);
+        solver.preSolve(handle, stream);
+        auto Vt = model->solve(target, handle, stream);
+        solver.measurement[0]->copy(Vt, stream);
+        // regularisation factor relative to the Jacobian's RMS row norm
+        const size_t nj = (size_t)model->jacobian->dataRows * E;
+        std::vector<float> J(nj);
+        cudaMemcpy(J.data(), model->jacobian->deviceData, sizeof(float) * nj, cudaMemcpyDeviceToHost);
+        double jj = 0.0;
+        for (float v : J) jj += (double)v * v;
+        const float factor = (float)(0.05 * std::sqrt(jj / model->jacobian->rows));
+        solver.inverseSolver->setRegularizationParameter(factor, solver::Inverse<float>::identity, handle, stream);
+        auto sigma = solver.solveDifferential(handle, stream);
+        std::vector<float> s(E);
+        cudaMemcpy(s.data(), sigma->deviceData, sizeof(float) * E, cudaMemcpyDeviceToHost);
+        double in = 0.0, out = 0.0;
+        std::vector<char> mark(E, 0);
+        for (int e : inside) mark[e] = 1;
+        for (unsigned e = 0; e < E; ++e) (mark[e] ? in : out) += s[e] - 1.0;
+        in /= std::max<size_t>(inside.size(), 1);
+        out /= std::max<size_t>(E - inside.size(), 1);
+
+        // text round trip
+        std::stringstream txt;
+        V0->savetxt(txt);
+        auto back = numeric::Matrix<float>::loadtxt(txt, stream);
+        back->copyToHost(stream);
+        double rt = 0.0;
+        for (unsigned i = 0; i < V0->rows; ++i)
+            for (unsigned j = 0; j < V0->cols; ++j) rt = std::max(rt, (double)std::fabs((*back)(i, j) - (*V0)(i, j)));
+
+        const bool ok = steps > 0 && std::isfinite(sumAbs) && sumAbs > 0.0 && in < out && in < -0.01 &&
+                        rt <= 1e-6 * sumAbs;
+        printf("{\"steps\": %u, \"sum_v\": %.9e, \"sum_abs_v\": %.9e, \"mean_delta_inside\": %.6e, "
+               "\"mean_delta_outside\": %.6e, \"text_roundtrip_max_err\": %.3e, \"ok\": %s}\n",
+               steps, sumV, sumAbs, in, out, rt, ok ? "true" : "false");
+        return ok ? 0 : 1;
+    } catch (std::exception const& ex) {
+        printf("{\"error\": \"%s\", \"ok\": false}\n", ex.what());
+        return 2;
+    }
+}

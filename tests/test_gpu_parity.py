@@ -335,3 +335,38 @@ def test_homogeneous_field_warm_start():
         # the homogeneous distribution itself needs no iterations from its own fields
         model.solve(torch.zeros_like(g), mp.SolveOptions(tol=1e-6, preconditioner=pc, warm_start="homogeneous"))
         assert model.last_stats.iterations <= 1
+
+
+@pytest.mark.parametrize("kind", ["identity", "noser", "laplacian"])
+def test_inverse_regularisers_match_oracle(kind):
+    """mpf_inverse_solve (solver::Inverse) for two parallel images against the
+    FP64 oracle solve of the same regularised system."""
+    import oracle
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=16, ports=16)
+    E = mesh.elements.shape[0]
+    model = mp.EIT(mesh, src, 1.0)
+    opts = mp.SolveOptions(tol=1e-7, refine_tol=1e-10)
+    ref = torch.ones((1, E), device="cuda")
+    calc1, J = model.solve(ref, opts, jacobian=True)
+    gs = torch.tensor(np.stack([inclusion_sigma(mesh, seed=s) for s in (1, 2)]), dtype=torch.float32, device="cuda")
+    meas = model.solve(gs, opts)
+    calc = calc1.expand(2, -1, -1).contiguous()
+    Jn = J[0].cpu().numpy().astype(np.float64)
+    # factors that regularise each R to a comparable strength: (ref factor)^2 R
+    # adds about a tenth of J^T J's mean diagonal
+    djj = float((Jn ** 2).sum(axis=0).mean())
+    if kind == "identity":
+        factor = np.sqrt(0.1 * djj)
+    elif kind == "noser":
+        factor = np.sqrt(0.1)
+    else:
+        factor = np.sqrt(0.1 * djj / float(np.diag(oracle.laplacian_gram(mesh.nodes, mesh.elements)).mean()))
+    out = model.inverse(J[0], calc, meas, factor, kind).cpu().numpy()
+    # oracle on the same J and data (J rows in the library's d * MP + m order)
+    Y = np.stack([oracle.flatten_measurement(meas[i].cpu().numpy().astype(np.float64), orc)
+                  - oracle.flatten_measurement(calc[i].cpu().numpy().astype(np.float64), orc) for i in range(2)], 1)
+    X = oracle.inverse_regularised(Jn, Y, 1.0, factor, kind, mesh.nodes, mesh.elements)
+    for i in range(2):
+        assert rel_err(out[i], X[:, i]) < 2e-3, (kind, i, rel_err(out[i], X[:, i]))

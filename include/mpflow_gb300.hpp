@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <fstream>
+#include <functional>
 #include <iomanip>
 #include <limits>
 #include <memory>
@@ -48,6 +49,163 @@ inline void cuda(cudaError_t e, const char* where) {
     if (e != cudaSuccess) throw std::runtime_error(std::string(where) + ": " + cudaGetErrorString(e));
 }
 }  // namespace detail
+
+// Minimal JSON reader for the configuration files that the reference reads
+// with json-parser (the *fromConfig factories): objects, arrays, strings,
+// numbers, booleans, null.  A missing key reads as a null value, as in
+// json-parser.
+namespace json {
+class value {
+public:
+    enum Type { none, object, array, string, number, boolean };
+    Type type = none;
+    double num = 0.0;
+    bool flag = false;
+    std::string str;
+    std::vector<value> items;
+    std::vector<std::pair<std::string, value>> members;
+
+    const value& operator[](const std::string& key) const {
+        for (auto const& kv : members)
+            if (kv.first == key) return kv.second;
+        return null_value();
+    }
+    const value& operator[](const char* key) const { return (*this)[std::string(key)]; }
+    const value& operator[](size_t i) const { return i < items.size() ? items[i] : null_value(); }
+    const value& operator[](int i) const { return i >= 0 ? (*this)[(size_t)i] : null_value(); }
+    const value& operator[](unsigned i) const { return (*this)[(size_t)i]; }
+    size_t size() const { return type == array ? items.size() : members.size(); }
+    double asDouble(double def = 0.0) const { return type == number ? num : def; }
+    long asInt(long def = 0) const { return type == number ? (long)std::llround(num) : def; }
+    bool asBool(bool def = false) const { return type == boolean ? flag : def; }
+    std::string asString(std::string const& def = "") const { return type == string ? str : def; }
+
+    static const value& null_value() {
+        static const value v;
+        return v;
+    }
+};
+
+inline value parse(std::string const& text) {
+    size_t i = 0;
+    auto fail = [&](const char* what) -> void {
+        throw std::invalid_argument(std::string("mpFlow::json::parse: ") + what + " at offset " + std::to_string(i));
+    };
+    auto ws = [&]() {
+        while (i < text.size() && (text[i] == ' ' || text[i] == '\n' || text[i] == '\t' || text[i] == '\r')) ++i;
+    };
+    std::function<value()> parse_value;
+    auto parse_string = [&]() -> std::string {
+        if (text[i] != '"') fail("string expected");
+        ++i;
+        std::string out;
+        while (i < text.size() && text[i] != '"') {
+            char c = text[i++];
+            if (c == '\\' && i < text.size()) {
+                const char e = text[i++];
+                c = e == 'n' ? '\n' : e == 't' ? '\t' : e == 'r' ? '\r' : e == 'b' ? '\b' : e == 'f' ? '\f' : e;
+            }
+            out.push_back(c);
+        }
+        if (i >= text.size()) fail("unterminated string");
+        ++i;
+        return out;
+    };
+    parse_value = [&]() -> value {
+        ws();
+        if (i >= text.size()) fail("unexpected end");
+        value v;
+        const char c = text[i];
+        if (c == '{') {
+            v.type = value::object;
+            ++i;
+            ws();
+            if (text[i] == '}') {
+                ++i;
+                return v;
+            }
+            for (;;) {
+                ws();
+                std::string key = parse_string();
+                ws();
+                if (text[i] != ':') fail("':' expected");
+                ++i;
+                v.members.emplace_back(key, parse_value());
+                ws();
+                if (text[i] == ',') {
+                    ++i;
+                    continue;
+                }
+                if (text[i] == '}') {
+                    ++i;
+                    return v;
+                }
+                fail("',' or '}' expected");
+            }
+        }
+        if (c == '[') {
+            v.type = value::array;
+            ++i;
+            ws();
+            if (text[i] == ']') {
+                ++i;
+                return v;
+            }
+            for (;;) {
+                v.items.push_back(parse_value());
+                ws();
+                if (text[i] == ',') {
+                    ++i;
+                    continue;
+                }
+                if (text[i] == ']') {
+                    ++i;
+                    return v;
+                }
+                fail("',' or ']' expected");
+            }
+        }
+        if (c == '"') {
+            v.type = value::string;
+            v.str = parse_string();
+            return v;
+        }
+        if (text.compare(i, 4, "true") == 0) {
+            v.type = value::boolean;
+            v.flag = true;
+            i += 4;
+            return v;
+        }
+        if (text.compare(i, 5, "false") == 0) {
+            v.type = value::boolean;
+            i += 5;
+            return v;
+        }
+        if (text.compare(i, 4, "null") == 0) {
+            i += 4;
+            return v;
+        }
+        size_t used = 0;
+        v.type = value::number;
+        v.num = std::stod(text.substr(i, 64), &used);
+        if (used == 0) fail("value expected");
+        i += used;
+        return v;
+    };
+    value root = parse_value();
+    ws();
+    if (i != text.size()) fail("trailing characters");
+    return root;
+}
+
+inline value parse_file(std::string const& filename) {
+    std::ifstream f(filename);
+    if (!f) throw std::runtime_error("mpFlow::json::parse_file: cannot open " + filename);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return parse(ss.str());
+}
+}  // namespace json
 
 namespace math {
 // include/mpflow/mathematics.h:42-44
@@ -164,6 +322,20 @@ public:
         if (!f) throw std::runtime_error("mpFlow::numeric::Matrix::loadtxt: cannot open file: " + filename);
         return loadtxt(f, stream);
     }
+    // src/numeric/matrix.cpp:877-906: a JSON array of rows (or of values: one column)
+    static std::shared_ptr<Matrix<type>> fromJsonArray(json::value const& array, cudaStream_t const stream = nullptr) {
+        if (array.type != json::value::array || array.size() == 0) return nullptr;
+        const unsigned rows = (unsigned)array.size();
+        const unsigned cols = array[0].type == json::value::array ? (unsigned)array[0].size() : 1;
+        auto m = std::make_shared<Matrix<type>>(rows, cols, stream);
+        for (unsigned r = 0; r < rows; ++r)
+            for (unsigned c = 0; c < cols; ++c)
+                (*m)(r, c) = (type)(cols == 1 && array[r].type != json::value::array ? array[r].asDouble()
+                                                                                    : array[r][c].asDouble());
+        m->copyToDevice(stream);
+        return m;
+    }
+
     void savetxt(std::ostream& ostream) const {
         ostream << std::setprecision(std::numeric_limits<type>::max_digits10);
         for (unsigned i = 0; i < rows; ++i) {
@@ -225,6 +397,35 @@ public:
         detail::check(mpf_ring_mesh((int32_t)rings, radius, nd.data.data(), el.data.data()),
                       "mpFlow::numeric::IrregularMesh::ring");
         return std::make_shared<IrregularMesh>(nd, el);
+    }
+
+    // src/numeric/irregular_mesh.cpp:48-126: a mesh directory (string, or
+    // {"path": ...}) holding nodes.txt and elements.txt; edges are always
+    // derived here.  The reference's distmesh branch ({"radius",
+    // "outerEdgeLength", "innerEdgeLength"}) needs libdistmesh, which this
+    // library does not carry; {"rings": R, "radius": r} builds the ring mesh.
+    static std::shared_ptr<IrregularMesh> fromConfig(json::value const& config, json::value const& portConfig,
+                                                     cudaStream_t const stream, std::string const path = "./") {
+        (void)portConfig;
+        if (config.type == json::value::string || config["path"].type == json::value::string) {
+            const std::string dir = path + "/" + (config.type == json::value::string ? config.str : config["path"].str);
+            auto nodes = Matrix<double>::loadtxt(dir + "/nodes.txt", stream);
+            auto elements = Matrix<int>::loadtxt(dir + "/elements.txt", stream);
+            Array2<double> nd(nodes->rows, nodes->cols);
+            for (unsigned i = 0; i < nodes->rows; ++i)
+                for (unsigned j = 0; j < nodes->cols; ++j) nd(i, j) = (*nodes)(i, j);
+            Array2<int> el(elements->rows, elements->cols);
+            for (unsigned i = 0; i < elements->rows; ++i)
+                for (unsigned j = 0; j < elements->cols; ++j) el(i, j) = (*elements)(i, j);
+            return std::make_shared<IrregularMesh>(nd, el);
+        }
+        if (config["rings"].type == json::value::number)
+            return ring((unsigned)config["rings"].asInt(), config["radius"].asDouble(1.0));
+        if (config["outerEdgeLength"].type != json::value::none)
+            throw std::runtime_error(
+                "mpFlow::numeric::IrregularMesh::fromConfig: distmesh meshing is not available; give a mesh "
+                "directory or {\"rings\": R, \"radius\": r}");
+        return nullptr;
     }
 
     Array2<double> elementNodes(unsigned const element) const {
@@ -289,6 +490,25 @@ public:
         return std::make_shared<Ports>(e);
     }
 
+    // src/fem/ports.cpp:79-114: a file of port edges (string or {"edges":
+    // file}) or {"count", "width", "offset", "clockwise"} on a circular boundary
+    static std::shared_ptr<Ports> fromConfig(json::value const& config,
+                                             std::shared_ptr<numeric::IrregularMesh const> const mesh,
+                                             cudaStream_t const stream, std::string const path = "./",
+                                             std::string const meshPath = "./mesh") {
+        (void)meshPath;
+        if (config.type == json::value::string || config["edges"].type == json::value::string) {
+            auto m = numeric::Matrix<int>::loadtxt(
+                path + "/" + (config.type == json::value::string ? config.str : config["edges"].str), stream);
+            numeric::Array2<int> e(m->rows, m->cols);
+            for (unsigned i = 0; i < m->rows; ++i)
+                for (unsigned j = 0; j < m->cols; ++j) e(i, j) = (*m)(i, j);
+            return std::make_shared<Ports>(e);
+        }
+        return circularBoundary((unsigned)config["count"].asInt(), config["width"].asDouble(),
+                                mesh, config["offset"].asDouble(), config["clockwise"].asBool());
+    }
+
     numeric::Array2<int> const edges;
     unsigned const count;
 };
@@ -325,6 +545,25 @@ public:
         : Sources(type, std::vector<dataType>(drivePattern ? drivePattern->cols : 0, value), ports, drivePattern,
                   measurementPattern, stream) {}
     virtual ~Sources() {}
+
+    // src/fem/sources.cpp:92-131: "type" ("voltage" -> Fixed, else Open),
+    // "value" (number or per-pattern array, default 1), "drivePattern" and
+    // "measurementPattern" as JSON arrays of rows (default: identity)
+    static std::shared_ptr<Sources<dataType>> fromConfig(json::value const& config, std::shared_ptr<Ports const> const ports,
+                                                         cudaStream_t const stream) {
+        auto pattern = [&](json::value const& c) {
+            auto m = numeric::Matrix<int>::fromJsonArray(c, stream);
+            return m ? m : numeric::Matrix<int>::eye(ports->count, stream);
+        };
+        auto drive = pattern(config["drivePattern"]);
+        auto meas = pattern(config["measurementPattern"]);
+        std::vector<dataType> excitation(drive->cols);
+        for (unsigned i = 0; i < drive->cols; ++i)
+            excitation[i] = (dataType)(config["value"].type == json::value::array ? config["value"][i].asDouble()
+                                                                                  : config["value"].asDouble(1.0));
+        const Type t = config["type"].asString() == "voltage" ? Fixed : Open;
+        return std::make_shared<Sources<dataType>>(t, excitation, ports, drive, meas, stream);
+    }
 
     Type const type;
     std::vector<dataType> const values;
@@ -420,6 +659,29 @@ public:
     EIT& operator=(EIT const&) = delete;
     virtual ~EIT() { mpf_eit_destroy(model_); }
 
+    // src/models/eit.cpp:102-131
+    static std::shared_ptr<EIT<numericalSolverType, equationType>> fromConfig(
+        json::value const& config, cublasHandle_t const handle, cudaStream_t const stream, std::string const path = "./",
+        std::shared_ptr<numeric::IrregularMesh const> const externalMesh = nullptr) {
+        auto const mesh = externalMesh ? externalMesh
+                                       : std::shared_ptr<numeric::IrregularMesh const>(
+                                             numeric::IrregularMesh::fromConfig(config["mesh"], config["ports"], stream, path));
+        if (!mesh) throw std::invalid_argument("mpFlow::models::EIT::fromConfig: invalid mesh config");
+        const std::string meshPath = config["mesh"].type == json::value::string ? config["mesh"].str
+                                     : config["mesh"]["path"].type == json::value::string ? config["mesh"]["path"].str
+                                                                                           : std::string("mesh");
+        auto const ports = FEM::Ports::fromConfig(config["ports"], mesh, stream, path, meshPath);
+        auto const sources = FEM::Sources<dataType>::fromConfig(config["source"], ports, stream);
+        const dataType referenceValue = (dataType)(config["material"].type == json::value::object
+                                                       ? config["material"]["referenceValue"].asDouble(1.0)
+                                                       : config["material"].asDouble(1.0));
+        const unsigned components = (unsigned)std::max(1L, config["2.5D"]["components"].asInt(1));
+        const double height = config["2.5D"]["height"].asDouble(1.0);
+        const double portHeight = config["ports"]["height"].asDouble(1.0);
+        return std::make_shared<EIT<numericalSolverType, equationType>>(mesh, sources, referenceValue, handle, stream,
+                                                                        components, height, portHeight);
+    }
+
     // forward solve of one material distribution (E x 1); returns the
     // Mm x Md electrode voltages and updates jacobian and fields
     std::shared_ptr<numeric::Matrix<dataType> const> solve(
@@ -463,6 +725,23 @@ public:
         cudaFreeAsync(buf, stream);
         detail::check(st, "mpFlow::models::EIT::updateFields");
         detail::cuda(cudaStreamSynchronize(stream), "updateFields");
+    }
+
+    // jacobian *= mask (elementwise, same shape): Matrix::elementwiseMultiply
+    // as the reference's noSensitivity option uses it (src/solver/solver.cpp:116-122)
+    void maskJacobian(std::shared_ptr<numeric::Matrix<dataType> const> const mask, cudaStream_t const stream) {
+        if (!mask || mask->rows != jacobian->rows || mask->cols != jacobian->cols)
+            throw std::invalid_argument("mpFlow::models::EIT::maskJacobian: mask shape differs from the jacobian");
+        const size_t n = (size_t)jacobian->dataRows * jacobian->cols;
+        std::vector<dataType> J(n);
+        detail::cuda(cudaMemcpyAsync(J.data(), jacobian->deviceData, sizeof(dataType) * n, cudaMemcpyDeviceToHost, stream),
+                     "maskJacobian");
+        detail::cuda(cudaStreamSynchronize(stream), "maskJacobian");
+        for (unsigned j = 0; j < jacobian->cols; ++j)
+            for (unsigned i = 0; i < jacobian->rows; ++i) J[i + (size_t)j * jacobian->dataRows] *= (*mask)(i, j);
+        detail::cuda(cudaMemcpyAsync(jacobian->deviceData, J.data(), sizeof(dataType) * n, cudaMemcpyHostToDevice, stream),
+                     "maskJacobian");
+        detail::cuda(cudaStreamSynchronize(stream), "maskJacobian");
     }
 
     mpf_eit_t handle() const { return model_; }
@@ -598,6 +877,40 @@ public:
         materialDistribution = std::make_shared<numeric::Matrix<dataType>>(E, 1, stream, start);
         inverseSolver = std::make_shared<Inverse<dataType, numericalInverseSolverType>>(
             forwardModel->mesh, forwardModel->jacobian, forwardModel->referenceValue, parallelImages, handle, stream);
+    }
+
+    // src/solver/solver.cpp:64-135: {"model": ..., "solver": {"parallelImages",
+    // "regularizationFactor", "regularizationType"}}; the model's "material"
+    // may name a reference distribution file and "noSensitivity" a 0/1 mask
+    // of the Jacobian.  Ends with preSolve.
+    static std::shared_ptr<Solver<forwardModelType, numericalInverseSolverType>> fromConfig(
+        json::value const& config, cublasHandle_t const handle, cudaStream_t const stream, std::string const path = "./",
+        std::shared_ptr<numeric::IrregularMesh const> const externalMesh = nullptr) {
+        auto const& modelConfig = config["model"];
+        auto const& solverConfig = config["solver"];
+        auto const forwardModel = forwardModelType::fromConfig(modelConfig, handle, stream, path, externalMesh);
+        std::shared_ptr<numeric::Matrix<dataType>> reference;
+        if (modelConfig["material"].type == json::value::string)
+            reference = numeric::Matrix<dataType>::loadtxt(path + "/" + modelConfig["material"].str, stream);
+        else if (modelConfig["material"]["distribution"].type == json::value::string)
+            reference = numeric::Matrix<dataType>::loadtxt(path + "/" + modelConfig["material"]["distribution"].str, stream);
+        const unsigned parallelImages = (unsigned)std::max(1L, solverConfig["parallelImages"].asInt(1));
+        auto solver = std::make_shared<Solver<forwardModelType, numericalInverseSolverType>>(forwardModel, parallelImages,
+                                                                                            handle, stream);
+        if (reference) solver->referenceDistribution = reference;
+        solver->preSolve(handle, stream);
+        if (modelConfig["noSensitivity"].type == json::value::string) {
+            auto mask = numeric::Matrix<dataType>::loadtxt(path + "/" + modelConfig["noSensitivity"].str, stream);
+            forwardModel->maskJacobian(mask, stream);
+            solver->inverseSolver->updateJacobian(forwardModel->jacobian, handle, stream);
+        }
+        const std::string type = solverConfig["regularizationType"].asString();
+        typedef Inverse<dataType, numericalInverseSolverType> inverseType;
+        solver->inverseSolver->setRegularizationParameter(
+            (dataType)solverConfig["regularizationFactor"].asDouble(),
+            type == "noser" ? inverseType::noser : type == "laplacian" ? inverseType::laplacian : inverseType::identity,
+            handle, stream);
+        return solver;
     }
 
     // forward solve at the reference distribution; measurement and

@@ -5,13 +5,59 @@
 #include <cstdio>
 #include <cstdlib>
 #include <sstream>
+#include <string>
 
 #include "mpflow_gb300.hpp"
 
 using namespace mpFlow;
 typedef models::EIT<numeric::ConjugateGradient, FEM::Equation<float, FEM::basis::Linear, false>> Model;
 
+// json-selftest: parse a configuration without touching the GPU
+static int json_selftest() {
+    auto v = json::parse(R"({"model": {"mesh": {"rings": 12, "radius": 1.5}, "ports": {"count": 8, "width": 0.2,
+        "clockwise": true}, "source": {"type": "voltage", "value": [1, 2.5e-3], "drivePattern": [[1, 0], [-1, 1]]},
+        "2.5D": {"components": 3, "height": 2.0}, "material": {"referenceValue": 0.5}},
+        "solver": {"regularizationType": "noser", "parallelImages": 2, "note": "a \"quoted\" word"}})");
+    const bool ok = v["model"]["mesh"]["rings"].asInt() == 12 && v["model"]["mesh"]["radius"].asDouble() == 1.5 &&
+                    v["model"]["ports"]["clockwise"].asBool() && v["model"]["source"]["value"][1].asDouble() == 2.5e-3 &&
+                    v["model"]["source"]["drivePattern"][1][0].asInt() == -1 &&
+                    v["model"]["2.5D"]["components"].asInt() == 3 && v["solver"]["regularizationType"].asString() == "noser" &&
+                    v["solver"]["note"].asString() == "a \"quoted\" word" && v["solver"]["missing"].type == json::value::none &&
+                    v["model"]["material"]["referenceValue"].asDouble() == 0.5;
+    printf("{\"json_selftest\": %s}\n", ok ? "true" : "false");
+    return ok ? 0 : 1;
+}
+
+// config <dir>: Solver::fromConfig(<dir>/config.json), measurement from
+// <dir>/measurement.txt, differential reconstruction into <dir>/result.txt
+static int from_config(std::string const& dir) {
+    cudaStream_t stream = nullptr;
+    cublasHandle_t handle = nullptr;
+    auto config = json::parse_file(dir + "/config.json");
+    auto solver = solver::Solver<Model>::fromConfig(config, handle, stream, dir);
+    auto meas = numeric::Matrix<float>::loadtxt(dir + "/measurement.txt", stream);
+    solver->measurement[0]->copy(meas, stream);
+    auto sigma = solver->solveDifferential(handle, stream);
+    const unsigned E = solver->forwardModel->mesh->elements.rows();
+    numeric::Matrix<float> out(E, 1, stream);
+    std::vector<float> s(E);
+    cudaMemcpy(s.data(), sigma->deviceData, sizeof(float) * E, cudaMemcpyDeviceToHost);
+    for (unsigned e = 0; e < E; ++e) out(e, 0) = s[e];
+    out.savetxt(dir + "/result.txt");
+    printf("{\"elements\": %u, \"ok\": true}\n", E);
+    return 0;
+}
+
 int main(int argc, char** argv) {
+    if (argc > 1 && std::string(argv[1]) == "json-selftest") return json_selftest();
+    if (argc > 2 && std::string(argv[1]) == "config") {
+        try {
+            return from_config(argv[2]);
+        } catch (std::exception const& ex) {
+            printf("{\"error\": \"%s\", \"ok\": false}\n", ex.what());
+            return 2;
+        }
+    }
     const unsigned rings = argc > 1 ? (unsigned)atoi(argv[1]) : 16;
     const unsigned L = argc > 2 ? (unsigned)atoi(argv[2]) : 16;
     cudaStream_t stream = nullptr;

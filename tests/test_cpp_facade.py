@@ -29,6 +29,45 @@ def test_facade_compiles_and_links(tmp_path):
     assert os.path.exists(_build(tmp_path))
 
 
+def test_facade_json_reader(tmp_path):
+    r = subprocess.run([_build(tmp_path), "json-selftest"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and json.loads(r.stdout)["json_selftest"], (r.stdout, r.stderr)
+
+
+@pytest.mark.gpu
+def test_solver_from_config_matches_python(tmp_path):
+    """Solver::fromConfig on a mesh directory + JSON config (the reference's
+    on-disk format) reconstructs what the Python binding computes."""
+    import torch
+    import mpflow_gb300 as mp
+    from conftest import inclusion_sigma, make_setup
+    exe = _build(tmp_path)
+    mesh, src, _ = make_setup(rings=16, ports=16)
+    d = tmp_path / "case"
+    (d / "mesh").mkdir(parents=True)
+    np.savetxt(d / "mesh" / "nodes.txt", mesh.nodes, fmt="%.17g")
+    np.savetxt(d / "mesh" / "elements.txt", mesh.elements, fmt="%d")
+    pat = mp.adjacent_pattern(16).astype(int).tolist()
+    model = mp.EIT(mesh, src, 1.0)
+    E = mesh.elements.shape[0]
+    opts = mp.SolveOptions(tol=1e-6)
+    V0, J = model.solve(torch.ones((1, E), device="cuda"), opts, jacobian=True)
+    Vm = model.solve(torch.tensor(inclusion_sigma(mesh, seed=3), dtype=torch.float32, device="cuda")[None], opts)
+    np.savetxt(d / "measurement.txt", Vm[0].cpu().numpy(), fmt="%.9g")
+    factor = float(np.sqrt(0.1 * (J[0].cpu().numpy().astype(np.float64) ** 2).sum(axis=0).mean()))
+    cfg = {"model": {"mesh": "mesh", "ports": {"count": 16, "width": 0.1, "offset": 0.0},
+                     "source": {"type": "current", "value": 1e-3, "drivePattern": pat, "measurementPattern": pat},
+                     "material": 1.0},
+           "solver": {"parallelImages": 1, "regularizationFactor": factor, "regularizationType": "identity"}}
+    (d / "config.json").write_text(json.dumps(cfg))
+    r = subprocess.run([exe, "config", str(d)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    got = np.loadtxt(d / "result.txt")
+    Vmt = torch.tensor(np.loadtxt(d / "measurement.txt"), dtype=torch.float32, device="cuda")[None]
+    want = 1.0 + model.inverse(J[0], V0, Vmt, factor, "identity")[0].cpu().numpy()
+    assert np.abs(got - want).max() <= 1e-5 * max(np.abs(want - 1.0).max(), 1e-12) + 1e-6
+
+
 @pytest.mark.gpu
 def test_facade_reconstruction_matches_python(tmp_path):
     exe = _build(tmp_path)

@@ -37,7 +37,12 @@ enum mpf_status {
     MPF_ENOTSUP = 8      /* valid request this build does not implement */
 };
 
-/* Source types, include/mpflow/fem/sources.h:31-34 (Sources::Type). */
+/* Source types, include/mpflow/fem/sources.h:31-34 (Sources::Type).  OPEN:
+ * current sources, voltages measured.  FIXED: voltage sources, the port
+ * nodes carry Dirichlet rows (EIT::applyMixedBoundaryCondition,
+ * src/models/eit.cpp:251-270) and the port currents are measured; solved in
+ * the equivalent symmetric form (Dirichlet columns eliminated), without FP64
+ * refinement and with the reference Jacobian only. */
 enum mpf_source_type { MPF_SOURCE_OPEN = 0, MPF_SOURCE_FIXED = 1 };
 
 /* Message of the last failed call on this thread ("" if none). */

@@ -70,6 +70,14 @@ struct mpf_eit {
     mpf::DevBuf<double> Ac64, rzFine, bzFine;
     mpf::DevBuf<float> Lc, LinvD, Binv, rcV, rcB, ycV;
     mpf::DevBuf<int> infoC;
+    // voltage (Fixed) sources: Dirichlet rows on port nodes (fixed_kernels.cu)
+    int fixed = 0;
+    mpf::DevBuf<int32_t> fxZero, fxDiag;                               // slots to clear / Dirichlet diagonals
+    mpf::DevBuf<int32_t> fxLiftPtr, fxLiftRow, fxLiftSlot, fxLiftCol;  // interior rows with port-node columns
+    mpf::DevBuf<int32_t> fxCurPtr, fxCurRow, fxCurSlot, fxCurCol;      // port-node rows (all their slots)
+    int fxNZero = 0, fxNLift = 0, capFX = 0;
+    mpf::DevBuf<float> bFix, curX;                                     // per-group right-hand sides, port currents
+    mpf::DevBuf<float2> dVals;                                         // unmasked slot values of port-node rows
     // host copy of the mesh (reference numbering) for the Laplacian regulariser
     std::vector<double> hostNodes;
     std::vector<int32_t> hostElements;
@@ -91,3 +99,10 @@ struct mpf_eit {
         if (pinnedActive) cudaFreeHost(pinnedActive);
     }
 };
+
+namespace mpf {
+// fixed_kernels.cu: voltage (Fixed) sources
+int fixed_plan(mpf_eit* m, const std::vector<double>& excBin);
+int fixed_prepare(mpf_eit* m, int F, cudaStream_t s);
+int fixed_currents(mpf_eit* m, int F, cudaStream_t s);
+}  // namespace mpf

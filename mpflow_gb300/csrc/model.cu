@@ -42,8 +42,10 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     MPF_CHECK(d->components >= 1, MPF_EINVAL, "mpflow::models::EIT::EIT: components < 1");
     MPF_CHECK(d->height > 0.0, MPF_EINVAL, "mpFlow::models::EIT::EIT: height <= 0.0");
     MPF_CHECK(d->port_height > 0.0, MPF_EINVAL, "mpFlow::models::EIT::EIT: portHeight <= 0.0");
-    MPF_CHECK(d->source_type == MPF_SOURCE_OPEN, MPF_ENOTSUP,
-              "mpf_eit_create: voltage (fixed) sources are not implemented in this build");
+    MPF_CHECK(d->source_type == MPF_SOURCE_OPEN || d->source_type == MPF_SOURCE_FIXED, MPF_EINVAL,
+              "mpf_eit_create: unknown source type %d", d->source_type);
+    MPF_CHECK(!(d->source_type == MPF_SOURCE_FIXED && d->jacobian_mode == 1), MPF_ENOTSUP,
+              "mpf_eit_create: the exact 2.5D Jacobian is implemented for current (open) sources only");
     auto m = std::make_unique<mpf_eit>();
     m->device = d->device;
     MPF_TRY(check_device(m.get()));
@@ -99,6 +101,10 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     // ---- excitation matrix and unique right-hand sides
     std::vector<double> exc((size_t)m->n * m->L);
     excitation_matrix(m->n, nodesP.data(), edgesP.data(), m->L, d->port_edges, d->port_edges_cap, exc.data(), m->n);
+    m->fixed = d->source_type == MPF_SOURCE_FIXED ? 1 : 0;
+    // voltage sources: binarised excitation (src/models/eit_kernel.cu:40-41)
+    if (m->fixed)
+        for (auto& v : exc) v = std::fabs(v) >= 1e-9 ? 1.0 : 0.0;
     const int L = m->L, Md = m->Md, Mm = m->Mm;
     std::vector<std::vector<double>> canon;  // canonical pattern columns
     auto unique_of = [&](const std::vector<double>& col, int& u, float& scale) {
@@ -173,6 +179,17 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
         double alpha = std::pow(2.0 * c * M_PI / m->height, 2);
         double beta = c == 0 ? 1.0 / m->height
                              : 2.0 * std::sin(c * M_PI * m->portHeight / m->height) / (c * M_PI * m->portHeight);
+        if (m->fixed) {
+            // voltage sources: no beta weighting, the measured currents carry
+            // the height (src/models/eit.cpp:170-197); the Dirichlet rows make
+            // every harmonic nonsingular
+            m->betaAll[c] = 1.0;
+            m->compOf[c] = (int)m->alphaH.size();
+            m->alphaH.push_back((float)alpha);
+            m->betaH.push_back((float)m->height);
+            dcf.push_back(0);
+            continue;
+        }
         m->betaAll[c] = beta;
         // a harmonic whose excitation vanishes to rounding contributes nothing
         if (std::fabs(beta) <= 1e-12 * std::fabs(beta0)) continue;
@@ -230,8 +247,10 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     std::vector<float> massCoef(m->Ca, 0.f);
     m->exactJacobian = d->jacobian_mode == 1 ? 1 : 0;
     for (int ci = 0; ci < m->Ca; ++ci) {
-        // reference: -h sum_c beta_c^2 (Y K Y); exact: -sum_c beta_c (Y (K + alpha_c M) Y)
-        beta2[ci] = m->exactJacobian ? (float)(m->betaH[ci] / m->height) : m->betaH[ci] * m->betaH[ci];
+        // reference: -h sum_c beta_c^2 (Y K Y); exact: -sum_c beta_c (Y (K + alpha_c M) Y);
+        // voltage sources: +h sum_c (Y K Y) (the sign is applied in eit_jacobian)
+        beta2[ci] = m->fixed ? 1.f
+                    : m->exactJacobian ? (float)(m->betaH[ci] / m->height) : m->betaH[ci] * m->betaH[ci];
         massCoef[ci] = m->exactJacobian ? m->alphaH[ci] : 0.f;
     }
     for (int c = 0; c < m->C; ++c) betaC[c] = m->compOf[c] >= 0 ? (float)m->betaAll[c] : 0.f;
@@ -268,6 +287,7 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     MPF_TRY(m->rowScale.upload(rowS));
     MPF_TRY(m->colU.upload(colU));
     MPF_TRY(m->colScale.upload(colS));
+    if (m->fixed) MPF_TRY(fixed_plan(m.get(), exc));
 
     // ---- two-level preconditioner plan: aggregates of kAgg consecutive rows
     // and, per nonzero aggregate pair (I, J), the matrix slots that sum into
@@ -417,8 +437,8 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false
     P.r = m->Rv.ptr;
     P.p = m->Pv.ptr;
     P.q = m->Qv.ptr;
-    P.b = m->Bc.ptr;
-    P.bPerGroup = 0;
+    P.b = m->fixed ? m->bFix.ptr : m->Bc.ptr;  // voltage sources: per-group Dirichlet right-hand sides
+    P.bPerGroup = m->fixed ? 1 : 0;
     P.dcFree = m->dcFree.ptr;
     P.partA = m->partA.ptr;
     P.partB = m->partB.ptr;
@@ -603,7 +623,7 @@ static int eit_jacobian(mpf_eit* m, int F, const float* gamma, const int* frameM
     if (f32) MPF_TRY(m->J.alloc((size_t)m->capFJ * m->rowsJ * m->Epad));
     JacPlan jp{m->rowsJ, m->Epad, m->E, m->KP, m->Ca, m->rowD.ptr, m->rowM.ptr, m->rowScale.ptr,
                m->beta2.ptr, m->massCoef.ptr, m->elements.ptr, m->Kf.ptr, m->Mf.ptr, m->exactJacobian,
-               m->ref, (float)m->height, m->logarithmic, frameMask, f32 ? 1 : 0};
+               m->ref, m->fixed ? -(float)m->height : (float)m->height, m->logarithmic, frameMask, f32 ? 1 : 0};
     return fem_launch_jacobian(F, jp, m->MmPad, m->npad, m->X.ptr, gamma, f32 ? m->J.ptr : nullptr, m->Jhi.ptr,
                                m->Jlo.ptr, s);
 }
@@ -629,7 +649,10 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
         m->lastFrames = F;
     }
     const bool warm = o.warm_start && m->fieldsValid && m->lastFrames == F;
+    MPF_CHECK(!(m->fixed && refine), MPF_ENOTSUP,
+              "forward solve: FP64 refinement is implemented for current (open) sources only");
     MPF_TRY(eit_assemble(m, F, gamma, refine, s));
+    if (m->fixed) MPF_TRY(fixed_prepare(m, F, s));
     if (!warm) MPF_TRY(tune_cg(m, F, s));
     const bool coarse = o.preconditioner == 1 && m->coarseOK;
     if (coarse) MPF_TRY(ensure_coarse(m, F));
@@ -701,7 +724,8 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     m->fieldsValid = true;
     m->lastFrames = F;
     MeasPlan mp{(int)m->nzNode.count, m->nzNode.ptr, nullptr, m->nzVal.ptr, m->nzPtr.ptr};
-    MPF_TRY(fem_launch_gram_meas(P.G, m->KP, m->npad, mp, m->X.ptr, m->Gm.ptr, s));
+    if (m->fixed) MPF_TRY(fixed_currents(m, F, s));
+    MPF_TRY(fem_launch_gram_meas(P.G, m->KP, m->npad, mp, m->fixed ? m->curX.ptr : m->X.ptr, m->Gm.ptr, s));
     MPF_TRY(fem_launch_voltages(F, m->Ca, m->KP, m->Mm, m->Md, m->Gm.ptr, m->beta.ptr, m->measU.ptr,
                                 m->measScale.ptr, m->driveU.ptr, m->driveScale.ptr, m->V.ptr, s));
     if (wantJ) MPF_TRY(eit_jacobian(m, F, gamma, nullptr, true, s));

@@ -432,3 +432,49 @@ def inverse_regularised(J: np.ndarray, Y: np.ndarray, ref: float, factor: float,
     else:
         raise ValueError(kind)
     return np.linalg.solve(JtJ + mu * R, J.T @ Y)
+
+
+def dense_matrix(layout: Layout, values: np.ndarray, n: int) -> np.ndarray:
+    """Dense n x n matrix of reference-ELL slot values (rows x 32)."""
+    A = np.zeros((n, n))
+    ids = layout.colIds[:n]
+    v = values[:n]
+    rows, ks = np.nonzero(ids != INVALID)
+    np.add.at(A, (rows, ids[rows, ks].astype(np.int64)), v[rows, ks])
+    return A
+
+
+def eit_forward_fixed(s: Setup, gamma: np.ndarray, want_jacobian: bool = True):
+    """Restatement of EIT::solve for voltage (Fixed) sources
+    (src/models/eit.cpp:85-91,160-205,251-270, src/models/eit_kernel.cu:34-54):
+    the excitation matrix is binarised (|Exc| >= 1e-9 -> 1), every node that
+    belongs to a port gets a Dirichlet row (identity) carrying the port's
+    voltage, the harmonics are not weighted by beta, the measured quantity is
+    the current height * A x collected by the binarised attachment matrix,
+    and J = +height * sum_c J_c.  Solved exactly (dense), which is the limit
+    the reference's CG converges to."""
+    n = s.nodes.shape[0]
+    excb = (np.abs(s.exc) >= 1e-9).astype(np.float64)
+    dirichlet = excb.any(axis=1)
+    pattern = np.concatenate([s.drive * s.values[None, :], s.meas], axis=1)
+    att = s.meas.T @ excb.T
+    S = dense_matrix(s.layout, update_matrix(s.layout, s.layout.elemS, gamma, s.ref, s.logarithmic), n)
+    R = dense_matrix(s.layout, update_matrix(s.layout, s.layout.elemR, gamma, s.ref, s.logarithmic), n)
+    V = np.zeros((s.Mm, s.Md))
+    J = np.zeros((s.rowsJ, s.elements.shape[0]), order="F") if want_jacobian else None
+    fields = []
+    for c in range(s.components):
+        alpha, _ = s.alpha_beta(c)
+        A = S + alpha * R
+        Ab = A.copy()
+        Ab[dirichlet, :] = 0.0
+        Ab[dirichlet, dirichlet] = 1.0
+        x = np.linalg.solve(Ab, excb @ pattern)
+        fields.append(x)
+        if want_jacobian:
+            calc_jacobian(s.elements, s.K, x, s.Md, s.Mm, gamma, s.ref, s.logarithmic, s.rowsJ,
+                          J=J, additive=(c > 0))
+        V += att @ (s.height * (A @ x))[:, :s.Md]
+    if want_jacobian:
+        J *= s.height
+    return V, J, fields

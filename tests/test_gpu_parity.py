@@ -370,3 +370,26 @@ def test_inverse_regularisers_match_oracle(kind):
     X = oracle.inverse_regularised(Jn, Y, 1.0, factor, kind, mesh.nodes, mesh.elements)
     for i in range(2):
         assert rel_err(out[i], X[:, i]) < 2e-3, (kind, i, rel_err(out[i], X[:, i]))
+
+
+@pytest.mark.parametrize("components,height,pc", [(1, 1.0, "jacobi"), (3, 2.0, "jacobi"), (3, 2.0, "two-level")])
+def test_fixed_sources_match_oracle(components, height, pc):
+    """Voltage sources (Dirichlet rows on the port nodes, currents measured)
+    against the oracle's dense solve of the reference's system."""
+    import oracle
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=16, ports=16, components=components, height=height, current=1.0)
+    fixed = mp.Sources(mp.FIXED, 1.0, src.ports, src.drivePattern, src.measurementPattern)
+    g = inclusion_sigma(mesh, seed=6)
+    Vo, Jo, Fo = oracle.eit_forward_fixed(orc, g)
+    model = mp.EIT(mesh, fixed, 1.0, components=components, height=height)
+    V, J = model.solve(torch.tensor(g, dtype=torch.float32, device="cuda"),
+                       mp.SolveOptions(tol=1e-8, preconditioner=pc), jacobian=True)
+    assert rel_err(V[0].cpu().numpy(), Vo) < 1e-4, rel_err(V[0].cpu().numpy(), Vo)
+    assert rel_err(J[0].cpu().numpy(), Jo) < 1e-4, rel_err(J[0].cpu().numpy(), Jo)
+    n = mesh.nodes.shape[0]
+    Fg = model.fields(1)[0].cpu().numpy()
+    for c in range(components):
+        err = np.abs(Fg[c][:, :n].T - Fo[c]).max() / np.abs(Fo[c]).max()
+        assert err < 1e-5, (c, err)

@@ -119,3 +119,23 @@ def test_golden_fixture(name):
     assert np.abs(Jp - z["J_probe"]).max() / np.abs(z["J_probe"]).max() < 1e-9
     assert np.array_equal(orc.layout.colIds, z["colIds"])
     assert np.array_equal(orc.portEdges, z["portEdges"])
+
+
+def test_fixed_source_oracle_jacobian_is_derivative():
+    """Voltage sources, one harmonic: the reference's Jacobian formula equals the
+    finite-difference derivative of the measured currents, and the current
+    matrix is symmetric (reciprocity)."""
+    import oracle
+    from conftest import make_setup
+    mesh, src, orc = make_setup(rings=16, ports=16, current=1.0)
+    g = np.ones(mesh.elements.shape[0])
+    V, J, _ = oracle.eit_forward_fixed(orc, g)
+    assert np.abs(V - V.T).max() <= 1e-12 * np.abs(V).max()
+    e, h = 57, 1e-4
+    gp, gm = g.copy(), g.copy()
+    gp[e] += h
+    gm[e] -= h
+    Vp, _, _ = oracle.eit_forward_fixed(orc, gp, want_jacobian=False)
+    Vm, _, _ = oracle.eit_forward_fixed(orc, gm, want_jacobian=False)
+    fd = oracle.flatten_measurement((Vp - Vm) / (2 * h), orc)
+    assert np.abs(fd - J[:, e]).max() <= 1e-5 * np.abs(J[:, e]).max()

@@ -21,6 +21,14 @@ target per second); the line also carries the CG SpMM bandwidth, the roofline
 of the dominant kernel and the CPU baseline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`--workload uneven` times the batch of uneven meshes instead: 64 ring meshes
+with R ~ U{20..100} rings and 16 or 32 electrodes (seed 3), 4 harmonics
+(height 4), 16 frames per mesh of a moving circular inclusion (radius
+U(0.1, 0.3), contrast log-uniform in [0.1, 10]); one step = the forward
+solves of all meshes and frames in the same CG launches.  Its line reports
+mesh-frames/s, the CG bandwidth against the HBM roofline and the same solves
+issued one mesh at a time.
 """
 from __future__ import annotations
 
@@ -49,6 +57,10 @@ def parse_args():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--workload", choices=["gn", "uneven"], default="gn",
+                   help="gn: learned/plain GN reconstruction (default); uneven: batch of uneven meshes")
+    p.add_argument("--meshes", type=int, default=64, help="uneven workload: meshes per step")
+    p.add_argument("--mesh-frames", type=int, default=16, help="uneven workload: frames per mesh")
     p.add_argument("--frames", type=int, default=32, help="frames per step per GPU")
     p.add_argument("--rings", type=int, default=80)
     p.add_argument("--electrodes", type=int, default=32)
@@ -496,10 +508,165 @@ def run_gb300(a):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+UNEVEN_METRIC = "EIT forward solves of 64 uneven meshes x 16 frames in one batch: mesh-frames/s; CG GB/s"
+UNEVEN_UNIT = "mesh-frames/s"
+
+
+def uneven_setup(a):
+    """Seeded mesh sizes, electrode counts and moving-inclusion frames."""
+    import mpflow_gb300 as mp
+    rng = np.random.default_rng(3)
+    rings = rng.integers(20, 101, size=a.meshes)
+    elec = rng.choice([16, 32], size=a.meshes)
+    meshes, frames = [], []
+    for i in range(a.meshes):
+        mesh = mp.IrregularMesh.ring(int(rings[i]))
+        ports = mp.Ports.circularBoundary(int(elec[i]), 0.1, mesh)
+        pat = mp.adjacent_pattern(int(elec[i]))
+        src = mp.Sources(mp.OPEN, 1e-3, ports, pat, pat)
+        cent = mesh.nodes[mesh.elements].mean(axis=1)
+        r = rng.uniform(0.1, 0.3)
+        contrast = np.exp(rng.uniform(np.log(0.1), np.log(10.0)))
+        orbit = rng.uniform(0.0, 0.9 - r)
+        phase = rng.uniform(0.0, 2 * np.pi)
+        g = np.ones((a.mesh_frames, cent.shape[0]), np.float32)
+        for f in range(a.mesh_frames):
+            th = phase + 2 * np.pi * f / a.mesh_frames
+            c = orbit * np.array([np.cos(th), np.sin(th)])
+            g[f, np.linalg.norm(cent - c, axis=1) < r] = contrast
+        meshes.append((mesh, ports, pat, src))
+        frames.append(g)
+    return rings, elec, meshes, frames
+
+
+def uneven_config(a, rings, elec):
+    return {"workload": (f"{a.meshes} ring meshes, rings U{{20..100}} and 16/32 electrodes (seed 3), "
+                         f"adjacent/adjacent, 4 harmonics (height 4), {a.mesh_frames} frames per mesh: moving "
+                         "inclusion r U(0.1,0.3), contrast log-U[0.1,10], linear conductivity"),
+            "nodes_total": int(sum(1 + 3 * r * (r + 1) for r in rings)),
+            "meshes_16_electrodes": int((elec == 16).sum()), "meshes_32_electrodes": int((elec == 32).sum()),
+            "frames_per_mesh": a.mesh_frames, "cg_tol": a.tol, "preconditioner": "jacobi",
+            "l2": "CG working set (GBs) far above L2 (129 MB)"}
+
+
+def run_uneven(a):
+    import torch
+    import mpflow_gb300 as mp
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rings, elec, meshes, frames = uneven_setup(a)
+    models = [mp.EIT(m, src, 1.0, components=4, height=4.0, device=local) for m, _, _, src in meshes]
+    batch = mp.EITBatch(models)
+    gam = [torch.tensor(g, device=dev) for g in frames]
+    opts = mp.SolveOptions(tol=a.tol)
+    lib = mp.lib()
+    stream = torch.cuda.current_stream()
+    nsteps = a.warmup + a.steps
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    cg = []
+
+    def batch_step(s):
+        V = batch.solve(gam, opts)
+        cg.append(batch.cg_stats())
+        return V
+
+    def sequential_step(s):
+        return [m.solve(g, opts) for m, g in zip(models, gam)]
+
+    mf = a.meshes * a.mesh_frames
+    with ClockSampler(local) as clocks:
+        t_b, _, launches = timed_steps(nsteps, a.warmup, batch_step, barrier, stream, torch, lib)
+        t_s, _, _ = timed_steps(min(nsteps, a.warmup + 2), a.warmup, sequential_step, barrier, stream, torch, lib)
+    iters = batch.iterations(a.mesh_frames)
+    cg_ms = float(np.mean([c[0] for c in cg[a.warmup:]]))
+    cg_bytes = float(np.mean([c[1] for c in cg[a.warmup:]]))
+
+    def max_over_ranks(ms):
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return ms
+
+    total_b = max_over_ranks(float(np.sum(t_b)))
+    total_s = max_over_ranks(float(np.sum(t_s)))
+    value = mf * world * len(t_b) / (total_b / 1e3)
+    seq_value = mf * world * len(t_s) / (total_s / 1e3)
+
+    # end to end through the public API: pinned host frames in, host voltages out
+    host_g = [g.cpu().pin_memory() for g in gam]
+    e2e_ms = []
+    h2d = sum(g.numel() * 4 for g in gam)
+    d2h = 0
+    for s in range(nsteps):
+        barrier()
+        t0 = time.perf_counter()
+        gd = [h.to(dev, non_blocking=True) for h in host_g]
+        V = batch.solve(gd, opts)
+        Vh = [v.cpu() for v in V]
+        torch.cuda.synchronize()
+        if s >= a.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        d2h = sum(v.numel() * 4 for v in Vh)
+    e2e_value = mf * world * len(e2e_ms) / (max_over_ranks(float(np.sum(e2e_ms))) / 1e3)
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    gbs = cg_bytes / cg_ms / 1e6
+    cpu = None
+    if not a.no_cpu_baseline:
+        import oracle
+        if a.cpu_threads > 0:
+            oracle.set_threads(a.cpu_threads)
+        i = int(np.argsort(rings)[len(rings) // 2])  # the median mesh, one frame
+        mesh, ports, pat, _ = meshes[i]
+        so = oracle.Setup(mesh.nodes, mesh.elements, mesh.edges, mesh.boundary, ports.edges, pat, pat,
+                          np.full(int(elec[i]), 1e-3), ref=1.0, components=4, height=4.0)
+        t0 = time.perf_counter()
+        oracle.eit_forward(so, frames[i][0].astype(np.float64), tol=a.tol, want_jacobian=False)
+        dt = time.perf_counter() - t0
+        cpu = {"value": 1.0 / dt, "unit": UNEVEN_UNIT, "cores": oracle.num_threads(), "kind": "port",
+               "sample": f"1 frame of the median mesh ({int(rings[i])} rings, {int(elec[i])} electrodes), FP64 "
+                         f"Jacobi-PCG forward solve, {dt:.2f} s"}
+    line = {
+        "metric": UNEVEN_METRIC, "value": value, "unit": UNEVEN_UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": float(np.mean(t_b)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 inner products)",
+        "data": "synthetic (seeded meshes and moving-inclusion frames)",
+        "config": uneven_config(a, rings, elec),
+        "cg": {"ms": cg_ms, "algorithmic_bytes": cg_bytes, "gbs": gbs,
+               "iterations_max": int(iters.max()), "iterations_mean": float(iters.mean()),
+               "launch_shapes": batch.cg_variants(a.mesh_frames).tolist()},
+        "roofline": {"kernel": "batched CG (k_spmm_dot + k_update + k_direction)", "bound": "hbm",
+                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                     "peak_source": f"{peak_kind} hbm_gbs", "traffic": None},
+        "one_mesh_at_a_time": {"value": seq_value, "ms_per_step": float(np.mean(t_s))},
+        "batch_vs_one_mesh_at_a_time": value / seq_value,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNEVEN_UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "clocks": clocks.summary(),
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse_args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "uneven":
+        run_uneven(a)
     else:
         run_gb300(a)
 

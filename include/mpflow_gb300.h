@@ -303,6 +303,52 @@ int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, 
 int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int32_t* get);
 
 /* ======================================================================== */
+/* Batches of uneven meshes                                                  */
+/* ======================================================================== */
+
+/* Forward solves of several models -- meshes of different size and electrode
+ * count sharing one harmonic set (components, height) -- as independent
+ * systems in the same CG launches: one launch per kernel and right-hand-side
+ * width (16, 32, 64 or 128 unique excitations) covers every (mesh, frame,
+ * harmonic) group, each with its own scalars and convergence mask.  The
+ * reference solves one EIT model at a time (EIT::solve,
+ * src/models/eit.cpp:139-213); calling it once per mesh gives the same
+ * voltages.  The models must outlive the batch; they stay usable on their
+ * own.  Fails with MPF_ENOTSUP for voltage (fixed) sources and MPF_EINVAL for
+ * models on different devices or with different harmonic sets. */
+typedef struct mpf_batch* mpf_batch_t;
+int mpf_batch_create(const mpf_eit_t* models, int32_t count, mpf_batch_t* batch);
+int mpf_batch_destroy(mpf_batch_t batch);
+
+/* EIT::solve for `frames` frames of every model.  gamma[i]: device,
+ * frames x n_elements(i); voltages[i]: device, frames x Mm(i) x Md(i), each
+ * frame column-major (as mpf_eit_forward).  Both are host arrays of `count`
+ * device pointers.  Cold start, Jacobi preconditioner, FP32 (MPF_ENOTSUP for
+ * refine_tol > 0, warm_start != 0 or preconditioner != 0); launch shapes are
+ * autotuned per width class at the first call with a frame count.
+ * Synchronises `stream`.  stats->iterations: slowest group. */
+int mpf_batch_forward(mpf_batch_t batch, int32_t frames, const float* const* gamma, float* const* voltages,
+                      const mpf_solve_opts* opts, mpf_solve_stats* stats, mpf_stream_t stream);
+
+/* CG iterations of every group of the last mpf_batch_forward, ordered
+ * [model][frame][active harmonic]; writes min(count, cap) entries. */
+int mpf_batch_iterations(mpf_batch_t batch, int32_t* iterations, int32_t cap, int32_t* count);
+
+/* Device time of the last call's CG (initialisation and iterations, CUDA
+ * events on its stream) and the algorithmic bytes its iterations moved:
+ * per iteration and group nnz * 12 + 11 * K * n * 4 + 4 * n * 4 (SpMM, update
+ * and direction passes; K unique excitations, n nodes of the group's mesh).
+ * No reference counterpart (measurement support). */
+int mpf_batch_cg_stats(mpf_batch_t batch, double* cg_ms, double* cg_bytes);
+
+/* Launch shapes of the batch's CG kernels (codes as mpf_eit_cg_variants):
+ * set (3 codes or -1, or NULL) applies to every width class; get receives
+ * 3 codes per width class (ascending width, at most cap entries) used with
+ * `frames` frames; *classes receives the number of width classes. */
+int mpf_batch_cg_variants(mpf_batch_t batch, const int32_t* set, int32_t frames, int32_t* get, int32_t cap,
+                          int32_t* classes);
+
+/* ======================================================================== */
 /* Dense building blocks                                                     */
 /* ======================================================================== */
 

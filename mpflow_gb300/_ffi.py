@@ -96,6 +96,12 @@ SIGNATURES = {
     "mpf_eit_group_iterations": (_I, [_P, _P, _I, _P]),
     "mpf_eit_cg_variants": (_I, [_P, _P, _I, _P]),
     "mpf_inverse_solve": (_I, [_P, _I, _D, _I, _P, _P, _P, _P, _P]),
+    "mpf_batch_create": (_I, [_P, _I, _P]),
+    "mpf_batch_destroy": (_I, [_P]),
+    "mpf_batch_forward": (_I, [_P, _I, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P]),
+    "mpf_batch_iterations": (_I, [_P, _P, _I, _P]),
+    "mpf_batch_cg_stats": (_I, [_P, _P, _P]),
+    "mpf_batch_cg_variants": (_I, [_P, _P, _I, _P, _I, _P]),
     "mpf_gram_split_bf16": (_I, [_I, _I, _I, _P, _I, _P, _P]),
     "mpf_cholesky_solve_f64": (_I, [_I, _I, _P, _D, _P, _I, _P, _P]),
     "mpf_gram_split_bf16_noalloc": (_I, [_I, _I, _I, _P, _I, _P, _P]),

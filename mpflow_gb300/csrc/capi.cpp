@@ -52,6 +52,13 @@ int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda,
 int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
 int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
+int batch_create(mpf_eit* const* models, int count, mpf_batch** out);
+int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* V, const mpf_solve_opts* in,
+                  mpf_solve_stats* stats, cudaStream_t s);
+int batch_iterations(mpf_batch* b, int32_t* out, int cap, int32_t* count);
+int batch_cg_stats(mpf_batch* b, double* ms, double* bytes);
+int batch_cg_variants(mpf_batch* b, const int32_t* set, int F, int32_t* get, int cap, int32_t* classes);
+void batch_destroy(mpf_batch* b);
 int inverse_solve(mpf_eit* m, int reg, double factor, int images, const float* Jref, const float* calc,
                   const float* meas, float* result, cudaStream_t s);
 int mlp_create(int in, int h1, int h2, int out, unsigned long long seed, int device, mpf_mlp** res);
@@ -247,6 +254,50 @@ int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_cg_variants: model == nullptr");
         return mpf::cg_variants(model, set, frames, get);
+    })
+}
+
+int mpf_batch_create(const mpf_eit_t* models, int32_t count, mpf_batch_t* batch) {
+    MPF_GUARD({
+        MPF_CHECK(models && batch && count >= 1, MPF_EINVAL, "mpf_batch_create: bad arguments");
+        return mpf::batch_create(models, count, batch);
+    })
+}
+
+int mpf_batch_destroy(mpf_batch_t batch) {
+    MPF_GUARD({
+        mpf::batch_destroy(batch);
+        return MPF_OK;
+    })
+}
+
+int mpf_batch_forward(mpf_batch_t batch, int32_t frames, const float* const* gamma, float* const* voltages,
+                      const mpf_solve_opts* opts, mpf_solve_stats* stats, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(batch, MPF_EINVAL, "mpf_batch_forward: batch == nullptr");
+        return mpf::batch_forward(batch, frames, gamma, voltages, opts, stats, (cudaStream_t)stream);
+    })
+}
+
+int mpf_batch_iterations(mpf_batch_t batch, int32_t* iterations, int32_t cap, int32_t* count) {
+    MPF_GUARD({
+        MPF_CHECK(batch && (iterations || cap == 0), MPF_EINVAL, "mpf_batch_iterations: bad arguments");
+        return mpf::batch_iterations(batch, iterations, cap, count);
+    })
+}
+
+int mpf_batch_cg_stats(mpf_batch_t batch, double* cg_ms, double* cg_bytes) {
+    MPF_GUARD({
+        MPF_CHECK(batch, MPF_EINVAL, "mpf_batch_cg_stats: batch == nullptr");
+        return mpf::batch_cg_stats(batch, cg_ms, cg_bytes);
+    })
+}
+
+int mpf_batch_cg_variants(mpf_batch_t batch, const int32_t* set, int32_t frames, int32_t* get, int32_t cap,
+                          int32_t* classes) {
+    MPF_GUARD({
+        MPF_CHECK(batch && frames >= 1, MPF_EINVAL, "mpf_batch_cg_variants: bad arguments");
+        return mpf::batch_cg_variants(batch, set, frames, get, cap, classes);
     })
 }
 

@@ -90,12 +90,26 @@ __device__ __forceinline__ float diag_inv(const float2* SR, const int32_t* diagS
     return d != 0.f ? 1.f / d : 0.f;
 }
 
+// Rows of one mesh: a single mesh covers tiles [0, nblk) and rows < n; a
+// batch of stacked meshes reads its segment table (see CgProblem).
+struct Seg {
+    int tile0, nblk, end;
+    float dcScale;
+};
+__device__ __forceinline__ Seg segment(const CgProblem& P, int mesh) {
+    if (P.seg) {
+        const int4 d = __ldg(&P.seg[mesh]);
+        return {d.x, d.y, d.z, __int_as_float(d.w)};
+    }
+    return {0, P.nblk, P.n, P.dcScale};
+}
+
 // Block-level reduction of per-thread partials into part[g][blk][KP]; returns
 // true in every thread of the block that finishes the group last (that block
-// then sees all partials of the group).
+// then sees all partials of the group).  nb: blocks of the group.
 template <int KP, int VEC, int NDOT>
 __device__ __forceinline__ bool block_partials(const DotAcc (&acc)[NDOT][VEC], double* const (&part)[NDOT], int g,
-                                               unsigned* counter) {
+                                               unsigned* counter, int nb) {
     using Sh = Shape<KP, VEC>;
     __shared__ double red[NDOT][kWarps * Sh::SUB][KP];
     __shared__ bool amLast;
@@ -116,18 +130,18 @@ __device__ __forceinline__ bool block_partials(const DotAcc (&acc)[NDOT][VEC], d
     }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) amLast = atomicAdd(&counter[g], 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) amLast = atomicAdd(&counter[g], 1u) == (unsigned)(nb - 1);
     __syncthreads();
     if (amLast) __threadfence();
     return amLast;
 }
 
-// Fixed-order sum of the block partials of group g, right-hand side j (one
-// partial per block of the launch's x dimension).
-__device__ __forceinline__ double sum_partials(const double* part, int g, int KP, int j) {
+// Fixed-order sum of the block partials of group g, right-hand side j (the
+// group's nb blocks; partials are strided by the launch's x dimension).
+__device__ __forceinline__ double sum_partials(const double* part, int g, int KP, int j, int nb) {
     double s = 0.0;
     const double* p = part + (size_t)g * gridDim.x * KP + j;
-    for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(p + (size_t)b * KP);
+    for (int b = 0; b < nb; ++b) s += __ldcg(p + (size_t)b * KP);
     return s;
 }
 
@@ -227,22 +241,25 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
     using Sh = Shape<KP, VEC>;
     constexpr int RB = Sh::STEPS < 2 ? Sh::STEPS : 2;
     const int g = blockIdx.y;
-    const int f = g / P.Ca, ci = g % P.Ca;
+    const int slice = g / P.M;
+    const Seg sg = segment(P, g - slice * P.M);
+    if ((int)blockIdx.x >= sg.nblk) return;
+    const int f = slice / P.Ca, ci = slice % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
     const float2* SR = P.SR + (size_t)f * P.W * P.npad;
-    const size_t vb = (size_t)g * P.npad * KP;
+    const size_t vb = (size_t)slice * P.npad * KP;
     const float* b = P.b + (P.bPerGroup ? vb : (size_t)ci * P.npad * KP);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
     float sx[VEC] = {};
     if (dc && !zeroGuess && P.sumX0) {
 #pragma unroll
-        for (int v = 0; v < VEC; ++v) sx[v] = (float)((double)P.dcScale * P.sumX0[(size_t)g * KP + j0 + v]);
+        for (int v = 0; v < VEC; ++v) sx[v] = (float)((double)sg.dcScale * P.sumX0[(size_t)g * KP + j0 + v]);
     }
     DotAcc acc[3][VEC];
     float rsum[VEC] = {}, bsum[VEC] = {};
-    const int rowBase = blockIdx.x * kRowTile + warp * kRowsPerWarp;
+    const int rowBase = (sg.tile0 + blockIdx.x) * kRowTile + warp * kRowsPerWarp;
     for (int st = 0; st < Sh::STEPS; st += RB) {
         int row[RB];
 #pragma unroll
@@ -260,7 +277,7 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
         }
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
-            const bool real = row[i] < P.n;
+            const bool real = row[i] < sg.end;
             float bv[VEC], rv[VEC], zv[VEC];
             ldv<VEC>(b + (size_t)row[i] * KP + j0, bv);
             const float di = diag_inv(SR, P.diagSlot, P.npad, row[i], alpha);
@@ -285,12 +302,13 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
         restrict_tile<KP, VEC>(bsum, blockIdx.x, P.nc, P.rcB + cb, red);
     }
     double* const parts[3] = {P.partA, P.partB, P.partC};
-    if (block_partials<KP, VEC, 3>(acc, parts, g, P.counter)) {
+    const int nb = sg.nblk;
+    if (block_partials<KP, VEC, 3>(acc, parts, g, P.counter, nb)) {
         if (P.coarse) {
             // the coarse kernel completes r^T M^-1 r and b^T M^-1 b and sets the masks
             if (threadIdx.x < KP) {
-                P.rzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x);
-                P.bzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partB, g, KP, threadIdx.x);
+                P.rzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
+                P.bzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partB, g, KP, threadIdx.x, nb);
             }
             if (threadIdx.x == 0) {
                 P.iters[g] = 0;
@@ -301,9 +319,9 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
         int notConv = 0;
         if (threadIdx.x < KP) {
             const int j = threadIdx.x;
-            double rz = sum_partials(P.partA, g, KP, j);
-            double bz = sum_partials(P.partB, g, KP, j);
-            P.sumP[(size_t)g * KP + j] = dc ? sum_partials(P.partC, g, KP, j) : 0.0;
+            double rz = sum_partials(P.partA, g, KP, j, nb);
+            double bz = sum_partials(P.partB, g, KP, j, nb);
+            P.sumP[(size_t)g * KP + j] = dc ? sum_partials(P.partC, g, KP, j, nb) : 0.0;
             P.rz[(size_t)g * KP + j] = rz;
             P.bz[(size_t)g * KP + j] = bz;
             P.beta[(size_t)g * KP + j] = 0.0;
@@ -326,11 +344,15 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
     using Sh = Shape<KP, VEC>;
     const int g = blockIdx.y;
     if (!P.active[g]) return;
-    const int f = g / P.Ca, ci = g % P.Ca;
+    const int slice = g / P.M;
+    const Seg sg = segment(P, g - slice * P.M);
+    const int T = P.tiles[0], nb = (sg.nblk + T - 1) / T;
+    if ((int)blockIdx.x >= nb) return;
+    const int f = slice / P.Ca, ci = slice % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
     const float2* SR = P.SR + (size_t)f * P.W * P.npad;
-    const size_t vb = (size_t)g * P.npad * KP;
+    const size_t vb = (size_t)slice * P.npad * KP;
     const float* p = P.p + vb;
     float* q = P.q + vb;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -338,11 +360,11 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
     float sp[VEC] = {};
     if (dc) {
 #pragma unroll
-        for (int v = 0; v < VEC; ++v) sp[v] = (float)((double)P.dcScale * P.sumP[(size_t)g * KP + j0 + v]);
+        for (int v = 0; v < VEC; ++v) sp[v] = (float)((double)sg.dcScale * P.sumP[(size_t)g * KP + j0 + v]);
     }
     DotAcc acc[1][VEC];
-    const int tile0 = blockIdx.x * P.tiles[0];
-    const int nsteps = (min(P.nblk, tile0 + P.tiles[0]) - tile0) * Sh::STEPS;
+    const int tile0 = sg.tile0 + blockIdx.x * T;
+    const int nsteps = (min(sg.tile0 + sg.nblk, tile0 + T) - tile0) * Sh::STEPS;
     for (int st = 0; st < nsteps; st += RB) {
         const int rowBase = (tile0 + st / Sh::STEPS) * kRowTile + warp * kRowsPerWarp +
                             (st % Sh::STEPS) * Sh::SUB + sub;
@@ -353,7 +375,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
         spmm_rows<KP, VEC, RB>(P.cols, SR, P.W, P.npad, alpha, p, j0, row, y);
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
-            if (row[i] < P.n) {
+            if (row[i] < sg.end) {
 #pragma unroll
                 for (int v = 0; v < VEC; ++v) y[i][v] += sp[v];
             }
@@ -365,8 +387,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
         }
     }
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter)) {
-        if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x);
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter, nb)) {
+        if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
 }
@@ -378,10 +400,14 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
     using Sh = Shape<KP, VEC>;
     const int g = blockIdx.y;
     if (!P.active[g]) return;
-    const int f = g / P.Ca, ci = g % P.Ca;
+    const int slice = g / P.M;
+    const Seg sg = segment(P, g - slice * P.M);
+    const int T = P.tiles[1], nb = (sg.nblk + T - 1) / T;
+    if ((int)blockIdx.x >= nb) return;
+    const int f = slice / P.Ca, ci = slice % P.Ca;
     const float alpha = P.alpha[ci];
     const float2* SR = P.SR + (size_t)f * P.W * P.npad;
-    const size_t vb = (size_t)g * P.npad * KP;
+    const size_t vb = (size_t)slice * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
     float a[VEC];
@@ -394,8 +420,8 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
     DotAcc acc[1][VEC];
     float rsum[VEC] = {};
     __shared__ float red[kWarps * 32 * VEC];
-    const int tile0 = blockIdx.x * P.tiles[1];
-    const int nsteps = (min(P.nblk, tile0 + P.tiles[1]) - tile0) * Sh::STEPS;
+    const int tile0 = sg.tile0 + blockIdx.x * T;
+    const int nsteps = (min(sg.tile0 + sg.nblk, tile0 + T) - tile0) * Sh::STEPS;
     for (int st = 0; st < nsteps; st += RB) {
         const int rowBase = (tile0 + st / Sh::STEPS) * kRowTile + warp * kRowsPerWarp +
                             (st % Sh::STEPS) * Sh::SUB + sub;
@@ -424,15 +450,17 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
             stv<VEC>(P.r + o[i], rv[i]);
         }
         if (P.coarse && (st % Sh::STEPS) + RB == Sh::STEPS) {
-            restrict_tile<KP, VEC>(rsum, tile0 + st / Sh::STEPS, P.nc, P.rc + (size_t)g * P.ncPad * KP, red);
+            restrict_tile<KP, VEC>(rsum, tile0 - sg.tile0 + st / Sh::STEPS, P.nc, P.rc + (size_t)g * P.ncPad * KP,
+                                   red);
 #pragma unroll
             for (int v = 0; v < VEC; ++v) rsum[v] = 0.f;
         }
     }
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter)) {
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter, nb)) {
         if (P.coarse) {
-            if (threadIdx.x < KP) P.rzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x);
+            if (threadIdx.x < KP)
+                P.rzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
             if (threadIdx.x == 0) P.counter[g] = 0;
             return;
         }
@@ -440,7 +468,7 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
         if (threadIdx.x < KP) {
             const size_t s = (size_t)g * KP + threadIdx.x;
             if (!P.conv[s]) {
-                const double rzn = sum_partials(P.partA, g, KP, threadIdx.x);
+                const double rzn = sum_partials(P.partA, g, KP, threadIdx.x, nb);
                 const double rzo = P.rz[s];
                 P.beta[s] = rzo != 0.0 ? rzn / rzo : 0.0;
                 P.rz[s] = rzn;
@@ -465,11 +493,15 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
     using Sh = Shape<KP, VEC>;
     const int g = blockIdx.y;
     if (!P.active[g]) return;
-    const int f = g / P.Ca, ci = g % P.Ca;
+    const int slice = g / P.M;
+    const Seg sg = segment(P, g - slice * P.M);
+    const int T = P.tiles[2], nb = (sg.nblk + T - 1) / T;
+    if ((int)blockIdx.x >= nb) return;
+    const int f = slice / P.Ca, ci = slice % P.Ca;
     const bool dc = P.dcFree[ci] != 0;
     const float alpha = P.alpha[ci];
     const float2* SR = P.SR + (size_t)f * P.W * P.npad;
-    const size_t vb = (size_t)g * P.npad * KP;
+    const size_t vb = (size_t)slice * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
     float be[VEC];
@@ -481,8 +513,8 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
         be[v] = P.first ? 0.f : (float)P.beta[s];
     }
     DotAcc acc[1][VEC];
-    const int tile0 = blockIdx.x * P.tiles[2];
-    const int nsteps = (min(P.nblk, tile0 + P.tiles[2]) - tile0) * Sh::STEPS;
+    const int tile0 = sg.tile0 + blockIdx.x * T;
+    const int nsteps = (min(sg.tile0 + sg.nblk, tile0 + T) - tile0) * Sh::STEPS;
     for (int st = 0; st < nsteps; st += RB) {
         const int rowBase = (tile0 + st / Sh::STEPS) * kRowTile + warp * kRowsPerWarp +
                             (st % Sh::STEPS) * Sh::SUB + sub;
@@ -502,22 +534,24 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
             di[i] = diag_inv(SR, P.diagSlot, P.npad, row[i], alpha);
         }
         // coarse correction: all rows of a warp step lie in one aggregate
-        if (P.coarse && rowBase < P.n) ldv<VEC>(P.yc + ((size_t)g * P.ncPad + rowBase / kAgg) * KP + j0, yv);
+        if (P.coarse && rowBase < sg.end)
+            ldv<VEC>(P.yc + ((size_t)g * P.ncPad + (rowBase - sg.tile0 * kRowTile) / kAgg) * KP + j0, yv);
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
-                const float z = fmaf(di[i], rv[i][v], row[i] < P.n ? yv[v] : 0.f);
+                const float z = fmaf(di[i], rv[i][v], row[i] < sg.end ? yv[v] : 0.f);
                 pv[i][v] = live[v] ? fmaf(be[v], pv[i][v], z) : pv[i][v];
-                if (dc && row[i] < P.n) acc[0][v].add(pv[i][v], 1.f);
+                if (dc && row[i] < sg.end) acc[0][v].add(pv[i][v], 1.f);
             }
             stv<VEC>(P.p + vb + (size_t)row[i] * KP + j0, pv[i]);
         }
     }
     if (!dc) return;
     double* const parts[1] = {P.partA};
-    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter)) {
-        if (threadIdx.x < KP) P.sumP[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x);
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter, nb)) {
+        if (threadIdx.x < KP)
+            P.sumP[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
 }
@@ -594,8 +628,8 @@ __global__ void __launch_bounds__(kThreads) k_residual64(CgProblem P, const doub
     if (amLast) {
         __threadfence();
         if (threadIdx.x < KP) {
-            rr[(size_t)g * KP + threadIdx.x] = sum_partials(partR, g, KP, threadIdx.x);
-            bb[(size_t)g * KP + threadIdx.x] = sum_partials(partB, g, KP, threadIdx.x);
+            rr[(size_t)g * KP + threadIdx.x] = sum_partials(partR, g, KP, threadIdx.x, P.nblk);
+            bb[(size_t)g * KP + threadIdx.x] = sum_partials(partB, g, KP, threadIdx.x, P.nblk);
         }
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
@@ -614,11 +648,15 @@ __global__ void k_to_float(size_t count, const double* x64, float* x) {
 // x += sign * shift[j] on the real rows of every Neumann group: converts
 // between the solution of (A + c' 1 1^T) x = b and the reference's
 // (A + 1 1^T) x = b, which differ only by (sum(b) / n^2)(1 - 1/c') 1.
+// shift: [M][KP], one row per stacked mesh.
 __global__ void k_dc_shift(CgProblem P, const double* shift, float sign) {
     const int g = blockIdx.y;
-    if (!P.dcFree[g % P.Ca]) return;
-    const size_t vb = (size_t)g * P.npad * P.KP;
-    const size_t count = (size_t)P.n * P.KP;
+    const int slice = g / P.M, mesh = g - slice * P.M;
+    if (!P.dcFree[slice % P.Ca]) return;
+    const Seg sg = segment(P, mesh);
+    const size_t vb = ((size_t)slice * P.npad + (size_t)sg.tile0 * kRowTile) * P.KP;
+    const size_t count = (size_t)(sg.end - sg.tile0 * kRowTile) * P.KP;
+    shift += (size_t)mesh * P.KP;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
         P.x[vb + i] += sign * (float)shift[i % P.KP];
 }

@@ -26,7 +26,7 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
                            const int32_t* __restrict__ contrib, const float* __restrict__ Kf,
                            const float* __restrict__ Mf, const double* __restrict__ Kd,
                            const double* __restrict__ Md, const float* __restrict__ gamma, float ref,
-                           int logarithmic, float2* __restrict__ SR,
+                           int logarithmic, float2* __restrict__ SR, size_t ld, size_t frameStride,
                            double* __restrict__ S64, double* __restrict__ R64) {
     const int f = blockIdx.y;
     const size_t slots = (size_t)W * npad;
@@ -47,7 +47,7 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
                 dr = fma(Md[code], pg64, dr);
             }
         }
-        SR[(size_t)f * slots + s] = make_float2(vs, vr);
+        SR[(size_t)f * frameStride + (s / npad) * ld + s % npad] = make_float2(vs, vr);
         if (S64) {
             S64[(size_t)f * slots + s] = ds;
             R64[(size_t)f * slots + s] = dr;
@@ -346,11 +346,13 @@ __global__ void __launch_bounds__(256) k_learned_input(int L, const float* __res
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
                         const float* Kf, const float* Mf, const double* Kd, const double* Md,
                         const float* gamma, float ref, int logarithmic, float2* SR, double* S64, double* R64,
-                        cudaStream_t s) {
+                        cudaStream_t s, size_t ld, size_t frameStride) {
     const size_t slots = (size_t)W * npad;
+    if (ld == 0) ld = npad;
+    if (frameStride == 0) frameStride = slots;
     int blocks = (int)std::min<size_t>((slots + 255) / 256, 4096);
     k_assemble<<<dim3(blocks, F), 256, 0, s>>>(W, npad, E, cptr, contrib, Kf, Mf, Kd, Md, gamma, ref,
-                                               logarithmic, SR, S64, R64);
+                                               logarithmic, SR, ld, frameStride, S64, R64);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

@@ -368,8 +368,7 @@ static int ensure_workspace(mpf_eit* m, int F, bool refine, bool jacobian) {
         MPF_CHECK(G <= 4096, MPF_EINVAL, "too many (frame, harmonic) groups in one call: %zu (max 4096)", G);
         m->capF = F;
         m->fieldsValid = false;
-        for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
-        m->graphs.clear();
+        cg_graphs_clear(m->graphs);
     }
     if (refine && F > m->capF64) {
         const size_t slots = (size_t)F * m->W * m->npad;
@@ -414,12 +413,6 @@ static int ensure_coarse(mpf_eit* m, int F) {
     return MPF_OK;
 }
 
-// launch-shape code -> kernel variant and tiles per block
-static void set_shape(CgProblem& P, int which, int code) {
-    P.variant[which] = code % kCgVariants;
-    P.tiles[which] = 1 << (code / kCgVariants);
-}
-
 static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false) {
     CgProblem P{};
     P.n = m->n;
@@ -429,6 +422,8 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false
     P.G = F * m->Ca;
     P.Ca = m->Ca;
     P.nblk = m->nblk;
+    P.M = 1;
+    P.seg = nullptr;
     P.cols = m->cols.ptr;
     P.diagSlot = m->diagSlot.ptr;
     P.SR = m->SR.ptr;
@@ -470,55 +465,18 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false
     for (int k = 0; k < 3; ++k) {
         int code = it != m->cgVariants.end() ? it->second[k] : cg_default_variant(m->KP);
         if (m->forcedVariants[k] >= 0) code = m->forcedVariants[k];
-        set_shape(P, k, code);
+        cg_set_shape(P, k, code);
     }
     return P;
 }
 
-// Autotuner: times every valid variant of the three iteration kernels on the
-// model's own assembled systems (F frames) with CUDA events and keeps the
-// fastest of each.  It overwrites the iteration vectors, so it runs only
-// before a cold solve; the caller re-initialises afterwards.
+// Autotuner (cg_driver.cpp) on the model's own assembled systems (F frames);
+// it overwrites the iteration vectors, so it runs only before a cold solve.
 static int tune_cg(mpf_eit* m, int F, cudaStream_t s) {
     if (m->cgVariants.count(F)) return MPF_OK;
     if (m->forcedVariants[0] >= 0 && m->forcedVariants[1] >= 0 && m->forcedVariants[2] >= 0) return MPF_OK;
-    CgProblem P = make_problem(m, F, 0.0);  // tolerance 0: no group retires
-    cudaEvent_t e0, e1;
-    MPF_CUDA(cudaEventCreate(&e0));
-    MPF_CUDA(cudaEventCreate(&e1));
     std::array<int, 3> best{};
-    int st = MPF_OK;
-    for (int which = 0; which < 3 && st == MPF_OK; ++which) {
-        float bestMs = 1e30f;
-        best[which] = cg_default_variant(m->KP);
-        for (int v = 0; v < kCgVariants * kCgTileChoices && st == MPF_OK; ++v) {
-            if (!cg_variant_valid(m->KP, which, v % kCgVariants)) continue;
-            CgProblem Q = P;
-            set_shape(Q, which, v);
-            // fresh state with valid p.q, then one untimed launch
-            st = cg_launch_init(Q, true, s);
-            if (st == MPF_OK) st = cg_launch_kernel(Q, 0, s);
-            if (st == MPF_OK) st = cg_launch_kernel(Q, which, s);
-            float msMin = 1e30f;
-            for (int rep = 0; rep < 2 && st == MPF_OK; ++rep) {
-                cudaEventRecord(e0, s);
-                for (int i = 0; i < 4 && st == MPF_OK; ++i) st = cg_launch_kernel(Q, which, s);
-                cudaEventRecord(e1, s);
-                cudaError_t e = cudaEventSynchronize(e1);
-                float ms = 0.f;
-                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-                if (e != cudaSuccess && st == MPF_OK) st = fail(MPF_ECUDA, "autotune timing: %s", cudaGetErrorString(e));
-                msMin = std::min(msMin, ms);
-            }
-            if (st == MPF_OK && msMin < bestMs) {
-                bestMs = msMin;
-                best[which] = v;
-            }
-        }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (st != MPF_OK) return st;
+    MPF_TRY(cg_autotune(make_problem(m, F, 0.0), best, s));
     m->cgVariants[F] = best;
     m->fieldsValid = false;
     return MPF_OK;
@@ -528,57 +486,7 @@ static int tune_cg(mpf_eit* m, int F, cudaStream_t s) {
 // iteration count of the slowest group and the number of unconverged groups.
 static int run_cg(mpf_eit* m, const CgProblem& P, int maxIter, int checkEvery, cudaStream_t s, int* itersOut,
                   int* notConverged) {
-    const int G = P.G;
-    std::string key(reinterpret_cast<const char*>(&P), sizeof(P));
-    key += std::to_string(checkEvery);
-    cudaGraphExec_t exec = nullptr;
-    auto it = m->graphs.find(key);
-    if (it != m->graphs.end()) {
-        exec = it->second;
-    } else {
-        cudaStream_t cap;
-        MPF_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-        cudaGraph_t graph;
-        MPF_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        int st = MPF_OK;
-        for (int i = 0; i < checkEvery && st == MPF_OK; ++i) st = cg_launch_iteration(P, cap);
-        cudaError_t e = cudaStreamEndCapture(cap, &graph);
-        cudaStreamDestroy(cap);
-        if (st != MPF_OK) return st;
-        MPF_CHECK(e == cudaSuccess, MPF_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        MPF_CHECK(e == cudaSuccess, MPF_ECUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
-        m->graphs[key] = exec;
-    }
-    int done = 0;
-    bool anyActive = true;
-    while (done < maxIter) {
-        MPF_CUDA(cudaGraphLaunch(exec, s));
-        add_launches((long long)cg_iteration_launches(P) * checkEvery);
-        done += checkEvery;
-        MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.active, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
-        MPF_CUDA(cudaStreamSynchronize(s));
-        anyActive = false;
-        for (int g = 0; g < G; ++g) anyActive |= m->pinnedActive[g] != 0;
-        if (!anyActive) break;
-    }
-    MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.iters, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
-    MPF_CUDA(cudaStreamSynchronize(s));
-    int mx = 0;
-    m->itersHost.assign(m->pinnedActive, m->pinnedActive + G);
-    for (int g = 0; g < G; ++g) mx = std::max(mx, m->pinnedActive[g]);
-    *itersOut = mx;
-    if (anyActive) {
-        MPF_CUDA(cudaMemcpyAsync(m->pinnedActive, P.active, sizeof(int) * G, cudaMemcpyDeviceToHost, s));
-        MPF_CUDA(cudaStreamSynchronize(s));
-        int nc = 0;
-        for (int g = 0; g < G; ++g) nc += m->pinnedActive[g] != 0;
-        *notConverged = nc;
-    } else {
-        *notConverged = 0;
-    }
-    return MPF_OK;
+    return cg_run(m->graphs, m->pinnedActive, &P, 1, maxIter, checkEvery, s, m->itersHost, itersOut, notConverged);
 }
 
 static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
@@ -997,8 +905,7 @@ int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get) {
                       MPF_EINVAL, "CG launch shape %d is not available for kernel %d with %d right-hand sides",
                       set[k], k, m->KP);
         for (int k = 0; k < 3; ++k) m->forcedVariants[k] = set[k] < 0 ? -1 : set[k];
-        for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
-        m->graphs.clear();
+        cg_graphs_clear(m->graphs);
     }
     if (get) {
         CgProblem P = make_problem(m, F < 1 ? 1 : F, 0.0);

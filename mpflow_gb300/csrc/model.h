@@ -11,9 +11,21 @@
 //   Jhi, Jlo  [F][rowsJ][Epad]     bf16   split of J for the tensor-core Gram
 // A "group" g = f*Ca + ci is one (frame, active harmonic) pair; all KP
 // right-hand sides of a group share one matrix S + alpha_c R.
+//
+// A batch of uneven meshes (batch.cu) stacks the meshes' row ranges in one
+// set of arrays: each mesh owns 128-row tiles [tile0, tile0 + tiles) of
+// `cols`, `SR` and every vector slice, and group g = slice * M + mesh, with
+// slice = f * Ca + ci as above.  Columns are global rows, so an SpMM never
+// leaves its mesh's block of the block-diagonal matrix, and every group has
+// its own scalars, masks and block reductions.
 #pragma once
 
 #include <cuda_bf16.h>
+
+#include <array>
+#include <map>
+#include <string>
+#include <vector>
 
 #include "mpf_internal.h"
 
@@ -21,7 +33,14 @@ namespace mpf {
 
 // Per-launch view of a batched CG problem.
 struct CgProblem {
-    int n, npad, W, KP, G, Ca, nblk;  // nblk = npad / kRowTile
+    // n: real rows, npad: rows of a vector slice, nblk: 128-row tiles of the
+    // largest mesh (the grid's x extent); for one mesh nblk = npad / kRowTile
+    int n, npad, W, KP, G, Ca, nblk;
+    // stacked meshes: M meshes per slice, seg[mesh] = {first tile, tiles,
+    // end row (first row + real rows), c' of the Neumann term as float bits};
+    // seg == nullptr for a single mesh (M = 1, tiles [0, nblk), rows < n)
+    int M;
+    const int4* seg;
     const int32_t* cols;
     const int32_t* diagSlot;
     const float2* SR;    // [F][W][npad] slot values {S, R}; columns in `cols`
@@ -37,7 +56,7 @@ struct CgProblem {
     double* partC;
     double* sumP;        // [G][KP] sum(p) of Neumann groups (the 1 1^T term)
     const double* sumX0; // [G][KP] sum(x0) for a warm start, or null
-    float dcScale;       // c' of the rank-one term c' 1 1^T (see model.cu)
+    float dcScale;       // c' of the rank-one term c' 1 1^T (see model.cu); per mesh in seg
     double* rz;          // [G][KP]
     double* pq;
     double* bz;
@@ -93,6 +112,24 @@ bool coarse_supported(int KP, int ncPad);
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s);
 int cg_iteration_launches(const CgProblem& P);
 int cg_launch_kernel(const CgProblem& P, int which /*0 spmm, 1 update, 2 direction*/, cudaStream_t s);
+
+// cg_driver.cpp: host drivers shared by single models and batches of meshes.
+// Captured CUDA graphs of CG iteration chunks, keyed by the problems' bytes.
+using CgGraphCache = std::map<std::string, cudaGraphExec_t>;
+void cg_graphs_clear(CgGraphCache& cache);
+// launch-shape code -> kernel variant and tiles per block
+void cg_set_shape(CgProblem& P, int which, int code);
+// Autotuner: times every valid launch shape of the three iteration kernels on
+// P's own systems with CUDA events and returns the fastest shape code of each.
+// It overwrites P's iteration vectors (run it before a cold solve only).
+int cg_autotune(const CgProblem& P, std::array<int, 3>& best, cudaStream_t s);
+// Runs CG iterations of nP problems, recorded together as CUDA graphs of
+// checkEvery iterations, until every group of every problem converged or
+// maxIter; pinned: host buffer of at least sum(G) ints.  iters receives the
+// per-group iteration counts (problems in order), maxIters the slowest group's
+// count and notConverged the groups still active.
+int cg_run(CgGraphCache& cache, int* pinned, const CgProblem* Ps, int nP, int maxIter, int checkEvery,
+           cudaStream_t s, std::vector<int>& iters, int* maxIters, int* notConverged);
 int cg_launch_residual64(const CgProblem& P, const double* S64, const double* R64, const double* x64,
                          const double* b64, const double* sumX64, double* partR, double* partB, double* rr,
                          double* bb, cudaStream_t s);
@@ -105,7 +142,9 @@ int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s);
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
                         const float* Kf, const float* Mf, const double* Kd, const double* Md,
                         const float* gamma, float ref, int logarithmic, float2* SR, double* S64, double* R64,
-                        cudaStream_t s);
+                        cudaStream_t s, size_t ld = 0, size_t frameStride = 0);
+// (SR of a stacked mesh: pass SR at the mesh's first row, ld = the batch's
+// rows per slot, frameStride = its slots per frame; 0 = this mesh's own)
 int fem_launch_export_ell(int F, int W, int npad, int n, int dataRows, const float2* SR, int component,
                           const int32_t* rowOf, float* refLayout, cudaStream_t s);
 struct MeasPlan {

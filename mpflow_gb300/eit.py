@@ -362,6 +362,75 @@ class EIT:
         return ms, by
 
 
+class EITBatch:
+    """Forward solves of several EIT models (meshes of uneven size, 16 or 32
+    electrodes, one harmonic set) in the same CG launches (mpf_batch_*).
+
+    ``solve`` takes one (frames x elements_i) float32 CUDA tensor per model
+    and returns one (frames x Mm_i x Md_i) voltage tensor per model, equal to
+    ``models[i].solve`` (cold start, Jacobi preconditioner)."""
+
+    def __init__(self, models):
+        self.models = list(models)
+        handles = (ctypes.c_void_p * len(self.models))(*[m._h.value for m in self.models])
+        h = ctypes.c_void_p()
+        check(lib().mpf_batch_create(handles, len(self.models), ctypes.byref(h)))
+        self._h = h
+        self.last_stats = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().mpf_batch_destroy(h)
+            self._h = None
+
+    def solve(self, gammas, options: SolveOptions | None = None, raise_on_noconv: bool = True):
+        import torch
+        if len(gammas) != len(self.models):
+            raise ValueError(f"expected {len(self.models)} material tensors, got {len(gammas)}")
+        gs, Vs = [], []
+        F = None
+        for m, g in zip(self.models, gammas):
+            gg, Fi = m._frames(g)
+            if F is not None and Fi != F:
+                raise ValueError("every model needs the same number of frames")
+            F = Fi
+            gs.append(gg)
+            Vs.append(torch.empty((F, m.info["drive_count"], m.info["meas_count"]), dtype=torch.float32,
+                                  device=gg.device))
+        gp = (ctypes.c_void_p * len(gs))(*[g.data_ptr() for g in gs])
+        vp = (ctypes.c_void_p * len(Vs))(*[v.data_ptr() for v in Vs])
+        st = _ffi.SolveStats()
+        o = (options or SolveOptions()).c()
+        status = lib().mpf_batch_forward(self._h, F, gp, vp, ctypes.byref(o), ctypes.byref(st), _stream())
+        self.last_stats = st
+        if status != _ffi.MPF_OK and (raise_on_noconv or status != 4):
+            check(status)
+        return [v.transpose(1, 2) for v in Vs]
+
+    def iterations(self, frames: int) -> np.ndarray:
+        """CG iterations of the last solve, shape (models, frames, active harmonics)."""
+        out = np.zeros(len(self.models) * frames * 128, np.int32)
+        cnt = ctypes.c_int32(0)
+        check(lib().mpf_batch_iterations(self._h, ptr(out), out.size, ctypes.byref(cnt)))
+        return out[:cnt.value].reshape(len(self.models), frames, -1).copy()
+
+    def cg_stats(self):
+        """(device ms, algorithmic bytes) of the last solve's CG."""
+        ms, by = ctypes.c_double(0), ctypes.c_double(0)
+        check(lib().mpf_batch_cg_stats(self._h, ctypes.byref(ms), ctypes.byref(by)))
+        return ms.value, by.value
+
+    def cg_variants(self, frames: int = 1, set=None) -> np.ndarray:
+        """Launch-shape codes per width class (rows) and kernel (columns)."""
+        get = np.zeros(12, np.int32)
+        ncl = ctypes.c_int32(0)
+        sv = None if set is None else np.ascontiguousarray(set, np.int32)
+        check(lib().mpf_batch_cg_variants(self._h, None if sv is None else ptr(sv), int(frames), ptr(get), get.size,
+                                          ctypes.byref(ncl)))
+        return get[:3 * ncl.value].reshape(-1, 3).copy()
+
+
 def gram_split_bf16(A):
     """C = A A^T (rows x rows) for a batch of row-major float32 CUDA matrices."""
     import torch

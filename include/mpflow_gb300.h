@@ -288,9 +288,10 @@ int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int3
 int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, int32_t* count);
 
 /* Launch shapes of the CG SpMM, update and direction kernels.  Shape
- * code = 3 * i + k + 9 * t runs {4, 2, 1}[i] floats per lane, keeps
- * {1, 2, 4}[k] row steps in flight per warp and walks 2^t (t = 0..3) tiles of
- * 128 rows per block.  By default the first cold solve with a given frame
+ * code = 3 * i + k + 9 * t (+ 36 * u for the SpMM) runs {4, 2, 1}[i] floats
+ * per lane, keeps {1, 2, 4}[k] row steps in flight per warp and walks 2^t
+ * (t = 0..3) tiles of 128 rows per block; u = 1 stages each tile's ELL slots
+ * in shared memory one tile ahead (SpMM codes 0..71, others 0..35).  By default the first cold solve with a given frame
  * count times every shape on the model's own systems and keeps the fastest
  * of each kernel (the reference's launch shape is fixed: src/numeric/
  * sparse_matrix.cpp:262-288).

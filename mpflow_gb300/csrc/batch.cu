@@ -355,9 +355,8 @@ int batch_cg_stats(mpf_batch* b, double* ms, double* bytes) {
 int batch_cg_variants(mpf_batch* b, const int32_t* set, int F, int32_t* get, int cap, int32_t* classes) {
     if (set) {
         for (int k = 0; k < 3; ++k) {
-            MPF_CHECK(set[k] < kCgVariants * kCgTileChoices, MPF_EINVAL, "mpf_batch_cg_variants: bad shape %d", set[k]);
             for (auto& cp : b->classes)
-                MPF_CHECK(set[k] < 0 || cg_variant_valid(cp->KP, k, set[k] % kCgVariants), MPF_EINVAL,
+                MPF_CHECK(set[k] < 0 || cg_shape_valid(cp->KP, k, set[k]), MPF_EINVAL,
                           "mpf_batch_cg_variants: shape %d not available for %d right-hand sides", set[k], cp->KP);
             b->forced[k] = set[k];
         }

@@ -19,8 +19,9 @@ void cg_graphs_clear(CgGraphCache& cache) {
 }
 
 void cg_set_shape(CgProblem& P, int which, int code) {
-    P.variant[which] = code % kCgVariants;
-    P.tiles[which] = 1 << (code / kCgVariants);
+    const int group = kCgVariants * kCgTileChoices;
+    P.variant[which] = code % kCgVariants + kCgVariants * (code / group);
+    P.tiles[which] = 1 << ((code % group) / kCgVariants);
 }
 
 int cg_autotune(const CgProblem& P0, std::array<int, 3>& best, cudaStream_t s) {
@@ -33,8 +34,8 @@ int cg_autotune(const CgProblem& P0, std::array<int, 3>& best, cudaStream_t s) {
     for (int which = 0; which < 3 && st == MPF_OK; ++which) {
         float bestMs = 1e30f;
         best[which] = cg_default_variant(P.KP);
-        for (int v = 0; v < kCgVariants * kCgTileChoices && st == MPF_OK; ++v) {
-            if (!cg_variant_valid(P.KP, which, v % kCgVariants)) continue;
+        for (int v = 0; v < cg_shape_count(which) && st == MPF_OK; ++v) {
+            if (!cg_shape_valid(P.KP, which, v)) continue;
             CgProblem Q = P;
             cg_set_shape(Q, which, v);
             // fresh state with valid p.q, then one untimed launch

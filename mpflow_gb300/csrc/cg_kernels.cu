@@ -17,9 +17,11 @@
 // P.tiles[k] consecutive 128-row tiles.  VEC and RB (template parameters)
 // and the tiles per block (runtime) are chosen per model by the autotuner in
 // model.cu (CUDA-event timings of every variant on the model's own systems).
-// An ELL slot is one packed float4 {S, R, column, 0} read as a broadcast;
-// the SpMM fuses S + alpha R (the system matrix is never materialised) and
-// unrolls up to kWFast slots.  Inner products: each thread accumulates its
+// An ELL slot is a column index (int32 array) and a float2 {S, R}; the
+// SpMM fuses S + alpha R (the system matrix is never materialised) and
+// unrolls up to kWFast slots.  A second SpMM form stages each 128-row tile's
+// slots in shared memory with cp.async, one tile ahead of the rows it
+// multiplies (k_spmm_dot_staged); the autotuner picks between the two.  Inner products: each thread accumulates its
 // products in a compensated (TwoProduct/TwoSum) float pair, everything above
 // that level is FP64; the per-block partials are combined by the last block
 // of the group in a fixed order, so results are deterministic.
@@ -393,6 +395,140 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot(CgProblem P) {
     }
 }
 
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Dynamic shared memory of k_spmm_dot_staged: two buffers of a tile's W
+// column rows (128 int32) and W value rows (128 float2).
+inline size_t staged_smem_bytes(int W) { return (size_t)2 * W * kRowTile * (sizeof(int32_t) + sizeof(float2)); }
+
+// k_spmm_dot with the tile's slot arrays in shared memory: while the block
+// multiplies tile t it copies tile t + 1's columns and values (16-byte
+// cp.async chunks: 512 B per column row, 1 KB per value row, all aligned
+// because tiles start at multiples of 128 rows), so a row's only global
+// latency is the gather of p.
+template <int KP, int VEC, int RB>
+__global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
+    using Sh = Shape<KP, VEC>;
+    extern __shared__ __align__(16) unsigned char stageSmem[];
+    const int g = blockIdx.y;
+    if (!P.active[g]) return;
+    const int slice = g / P.M;
+    const Seg sg = segment(P, g - slice * P.M);
+    const int T = P.tiles[0], nb = (sg.nblk + T - 1) / T;
+    if ((int)blockIdx.x >= nb) return;
+    const int f = slice / P.Ca, ci = slice % P.Ca;
+    const bool dc = P.dcFree[ci] != 0;
+    const float alpha = P.alpha[ci];
+    const int W = P.W;
+    const float2* SR = P.SR + (size_t)f * W * P.npad;
+    const size_t vb = (size_t)slice * P.npad * KP;
+    const float* p = P.p + vb;
+    float* q = P.q + vb;
+    int32_t* cs = reinterpret_cast<int32_t*>(stageSmem);
+    float2* vs = reinterpret_cast<float2*>(stageSmem + (size_t)2 * W * kRowTile * sizeof(int32_t));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    float sp[VEC] = {};
+    if (dc) {
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) sp[v] = (float)((double)sg.dcScale * P.sumP[(size_t)g * KP + j0 + v]);
+    }
+    DotAcc acc[1][VEC];
+    const int tile0 = sg.tile0 + blockIdx.x * T;
+    const int tileEnd = min(sg.tile0 + sg.nblk, tile0 + T);
+    constexpr int kColChunks = kRowTile / 4, kValChunks = kRowTile / 2;  // 16-byte chunks per slot row
+    auto stage = [&](int tile, int buf) {
+        const size_t r0 = (size_t)tile * kRowTile;
+        for (int c = threadIdx.x; c < W * (kColChunks + kValChunks); c += kThreads) {
+            if (c < W * kColChunks) {
+                const int k = c / kColChunks, o = (c % kColChunks) * 4;
+                cp_async16(cs + (buf * W + k) * kRowTile + o, P.cols + (size_t)k * P.npad + r0 + o);
+            } else {
+                const int cv = c - W * kColChunks;
+                const int k = cv / kValChunks, o = (cv % kValChunks) * 2;
+                cp_async16(vs + (buf * W + k) * kRowTile + o, SR + (size_t)k * P.npad + r0 + o);
+            }
+        }
+        cp_async_commit();
+    };
+    stage(tile0, 0);
+    for (int t = tile0; t < tileEnd; ++t) {
+        const int buf = (t - tile0) & 1;
+        if (t + 1 < tileEnd) {
+            stage(t + 1, buf ^ 1);
+            cp_async_wait1();
+        } else {
+            cp_async_wait0();
+        }
+        __syncthreads();
+        const int32_t* ct = cs + buf * W * kRowTile;
+        const float2* vt = vs + buf * W * kRowTile;
+        for (int st = 0; st < Sh::STEPS; st += RB) {
+            int lr[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i) lr[i] = warp * kRowsPerWarp + (st + i) * Sh::SUB + sub;
+            float y[RB][VEC];
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) y[i][v] = 0.f;
+#pragma unroll
+            for (int k = 0; k < kWFast; ++k) {
+                if (k < W) {
+#pragma unroll
+                    for (int i = 0; i < RB; ++i) {
+                        const int c = ct[k * kRowTile + lr[i]];
+                        const float2 e = vt[k * kRowTile + lr[i]];
+                        const float av = e.x + alpha * e.y;
+                        float xv[VEC];
+                        ldv<VEC>(p + (size_t)c * KP + j0, xv);
+#pragma unroll
+                        for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(av, xv[v], y[i][v]);
+                    }
+                }
+            }
+            for (int k = kWFast; k < W; ++k) {
+#pragma unroll
+                for (int i = 0; i < RB; ++i) {
+                    const int c = ct[k * kRowTile + lr[i]];
+                    const float2 e = vt[k * kRowTile + lr[i]];
+                    const float av = e.x + alpha * e.y;
+                    float xv[VEC];
+                    ldv<VEC>(p + (size_t)c * KP + j0, xv);
+#pragma unroll
+                    for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(av, xv[v], y[i][v]);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < RB; ++i) {
+                const int row = t * kRowTile + lr[i];
+                if (row < sg.end) {
+#pragma unroll
+                    for (int v = 0; v < VEC; ++v) y[i][v] += sp[v];
+                }
+                stv<VEC>(q + (size_t)row * KP + j0, y[i]);
+                float pv[VEC];
+                ldv<VEC>(p + (size_t)row * KP + j0, pv);
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) acc[0][v].add(pv[v], y[i][v]);
+            }
+        }
+        __syncthreads();  // the next stage() overwrites this buffer
+    }
+    double* const parts[1] = {P.partA};
+    if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter, nb)) {
+        if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
+        if (threadIdx.x == 0) P.counter[g] = 0;
+    }
+}
+
 // x += a p, r -= a q, z = D^-1 r, rz' = r.z; the last block updates the
 // scalars, the convergence mask and the group's active flag.
 template <int KP, int VEC, int RB>
@@ -686,8 +822,9 @@ __global__ void __launch_bounds__(kThreads) k_colsum(int n, int npad, int KP, in
 
 // ---------------------------------------------------------------------------
 // Variant table: variant v = vecIdx * 3 + rbIdx with VEC in {4, 2, 1} and
-// RB in {1, 2, 4}; entries whose lane mapping or step count does not fit the
-// right-hand-side width are null.
+// RB in {1, 2, 4} (SpMM: v + 9 for the shared-memory-staged form); entries
+// whose lane mapping or step count does not fit the right-hand-side width
+// are null.
 using CgKernel = void (*)(CgProblem);
 
 template <int KP, int VEC, int RB>
@@ -696,10 +833,11 @@ constexpr bool valid_variant() {
 }
 
 template <int KP, int VEC, int RB>
-void fill_variant(CgKernel (&t)[3][kCgVariants], int v) {
+void fill_variant(CgKernel (&t)[3][2 * kCgVariants], int v) {
     if constexpr (KP / VEC <= 32) {
         if constexpr (valid_variant<KP, VEC, RB>()) {
             t[0][v] = k_spmm_dot<KP, VEC, RB>;
+            t[0][v + kCgVariants] = k_spmm_dot_staged<KP, VEC, RB>;
             t[1][v] = k_update<KP, VEC, RB>;
             t[2][v] = k_direction<KP, VEC, RB>;
         }
@@ -708,7 +846,7 @@ void fill_variant(CgKernel (&t)[3][kCgVariants], int v) {
 
 template <int KP>
 struct VariantTable {
-    CgKernel k[3][kCgVariants] = {};
+    CgKernel k[3][2 * kCgVariants] = {};
     VariantTable() {
         fill_variant<KP, 4, 1>(k, 0);
         fill_variant<KP, 4, 2>(k, 1);
@@ -727,7 +865,7 @@ CgKernel variant_kernel(int KP, int which, int v) {
     static const VariantTable<32> t32;
     static const VariantTable<64> t64;
     static const VariantTable<128> t128;
-    if (v < 0 || v >= kCgVariants || which < 0 || which > 2) return nullptr;
+    if (v < 0 || v >= 2 * kCgVariants || which < 0 || which > 2) return nullptr;
     switch (KP) {
         case 16: return t16.k[which][v];
         case 32: return t32.k[which][v];
@@ -772,6 +910,20 @@ struct Res64L {
 
 bool cg_variant_valid(int KP, int which, int v) { return variant_kernel(KP, which, v) != nullptr; }
 
+int cg_shape_count(int which) { return which == 0 ? 2 * kCgVariants * kCgTileChoices : kCgVariants * kCgTileChoices; }
+
+bool cg_shape_valid(int KP, int which, int code) {
+    if (code < 0 || code >= cg_shape_count(which)) return false;
+    const int group = kCgVariants * kCgTileChoices;
+    return cg_variant_valid(KP, which, code % kCgVariants + kCgVariants * (code / group));
+}
+
+int cg_shape_code(const CgProblem& P, int which) {
+    const int v = P.variant[which];
+    return v % kCgVariants + kCgVariants * (31 - __builtin_clz(P.tiles[which])) +
+           kCgVariants * kCgTileChoices * (v / kCgVariants);
+}
+
 int cg_default_variant(int KP) { return KP <= 64 ? 1 : 0; }  // VEC 4, RB 2 (KP 128: RB 1)
 
 static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count);
@@ -795,7 +947,14 @@ static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count)
     CgKernel k = variant_kernel(P.KP, which, v);
     MPF_CHECK(k != nullptr, MPF_EINVAL, "CG kernel variant %d not available for %d right-hand sides", v, P.KP);
     const int t = P.tiles[which] >= 1 ? P.tiles[which] : 1;
-    k<<<dim3((P.nblk + t - 1) / t, P.G), kThreads, 0, s>>>(P);
+    size_t smem = 0;
+    if (which == 0 && v >= kCgVariants) {
+        smem = staged_smem_bytes(P.W);
+        MPF_CHECK(smem <= 200 * 1024, MPF_EINVAL, "staged SpMM: %d ELL slots do not fit shared memory", P.W);
+        if (smem > 48 * 1024)
+            MPF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    k<<<dim3((P.nblk + t - 1) / t, P.G), kThreads, smem, s>>>(P);
     if (count) {
         MPF_LAUNCHED(1);
     } else {

@@ -900,8 +900,7 @@ int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, doub
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get) {
     if (set) {
         for (int k = 0; k < 3; ++k)
-            MPF_CHECK(set[k] < 0 || (set[k] < kCgVariants * kCgTileChoices &&
-                                     cg_variant_valid(m->KP, k, set[k] % kCgVariants)),
+            MPF_CHECK(set[k] < 0 || cg_shape_valid(m->KP, k, set[k]),
                       MPF_EINVAL, "CG launch shape %d is not available for kernel %d with %d right-hand sides",
                       set[k], k, m->KP);
         for (int k = 0; k < 3; ++k) m->forcedVariants[k] = set[k] < 0 ? -1 : set[k];
@@ -909,7 +908,7 @@ int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get) {
     }
     if (get) {
         CgProblem P = make_problem(m, F < 1 ? 1 : F, 0.0);
-        for (int k = 0; k < 3; ++k) get[k] = P.variant[k] + kCgVariants * (31 - __builtin_clz(P.tiles[k]));
+        for (int k = 0; k < 3; ++k) get[k] = cg_shape_code(P, k);
     }
     return MPF_OK;
 }

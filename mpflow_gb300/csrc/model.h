@@ -87,11 +87,15 @@ struct CgProblem {
 constexpr int kAgg = 64;  // rows per coarse aggregate (divides kRowTile)
 
 // cg_kernels.cu
-// variant v = vecIdx * 3 + rbIdx, floats per lane {4, 2, 1}[vecIdx], row steps {1, 2, 4}[rbIdx];
-// a launch-shape code is v + kCgVariants * ti with 1 << ti tiles per block
+// variant v = vecIdx * 3 + rbIdx, floats per lane {4, 2, 1}[vecIdx], row steps {1, 2, 4}[rbIdx]
+// (SpMM: v + 9 is the shared-memory-staged form); a launch-shape code is
+// v % 9 + kCgVariants * ti + 36 * (v / 9) with 1 << ti tiles per block
 constexpr int kCgVariants = 9;
 constexpr int kCgTileChoices = 4;
 bool cg_variant_valid(int KP, int which, int v);
+int cg_shape_count(int which);                      // 72 SpMM codes, 36 for the others
+bool cg_shape_valid(int KP, int which, int code);
+int cg_shape_code(const CgProblem& P, int which);
 int cg_default_variant(int KP);
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
 // coarse_kernels.cu

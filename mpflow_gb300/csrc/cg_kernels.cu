@@ -404,15 +404,15 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Dynamic shared memory of k_spmm_dot_staged: two buffers of a tile's W
-// column rows (128 int32) and W value rows (128 float2).
+// Dynamic shared memory of k_spmm_dot_staged: per warp, two buffers of its
+// 16 rows' W column entries (int32) and W value entries (float2).
 inline size_t staged_smem_bytes(int W) { return (size_t)2 * W * kRowTile * (sizeof(int32_t) + sizeof(float2)); }
 
-// k_spmm_dot with the tile's slot arrays in shared memory: while the block
-// multiplies tile t it copies tile t + 1's columns and values (16-byte
-// cp.async chunks: 512 B per column row, 1 KB per value row, all aligned
-// because tiles start at multiples of 128 rows), so a row's only global
-// latency is the gather of p.
+// k_spmm_dot with the slot arrays in shared memory: every warp copies the W
+// columns and values of its 16 rows of tile t + 1 (16-byte cp.async chunks:
+// 64 B of columns and 128 B of values per slot, aligned because tiles start
+// at multiples of 128 rows) while it multiplies tile t, so a row's only
+// global latency is the gather of p; warps synchronise only with themselves.
 template <int KP, int VEC, int RB>
 __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
     using Sh = Shape<KP, VEC>;
@@ -431,10 +431,12 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
     const size_t vb = (size_t)slice * P.npad * KP;
     const float* p = P.p + vb;
     float* q = P.q + vb;
-    int32_t* cs = reinterpret_cast<int32_t*>(stageSmem);
-    float2* vs = reinterpret_cast<float2*>(stageSmem + (size_t)2 * W * kRowTile * sizeof(int32_t));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    // this warp's buffers: [2][W][16] columns, then [2][W][16] values
+    int32_t* cs = reinterpret_cast<int32_t*>(stageSmem) + (size_t)warp * 2 * W * kRowsPerWarp;
+    float2* vs = reinterpret_cast<float2*>(stageSmem + (size_t)2 * W * kRowTile * sizeof(int32_t)) +
+                 (size_t)warp * 2 * W * kRowsPerWarp;
     float sp[VEC] = {};
     if (dc) {
 #pragma unroll
@@ -443,17 +445,17 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
     DotAcc acc[1][VEC];
     const int tile0 = sg.tile0 + blockIdx.x * T;
     const int tileEnd = min(sg.tile0 + sg.nblk, tile0 + T);
-    constexpr int kColChunks = kRowTile / 4, kValChunks = kRowTile / 2;  // 16-byte chunks per slot row
+    constexpr int kColChunks = kRowsPerWarp / 4, kValChunks = kRowsPerWarp / 2;  // 16-byte chunks per slot
     auto stage = [&](int tile, int buf) {
-        const size_t r0 = (size_t)tile * kRowTile;
-        for (int c = threadIdx.x; c < W * (kColChunks + kValChunks); c += kThreads) {
+        const size_t r0 = (size_t)tile * kRowTile + warp * kRowsPerWarp;
+        for (int c = lane; c < W * (kColChunks + kValChunks); c += 32) {
             if (c < W * kColChunks) {
                 const int k = c / kColChunks, o = (c % kColChunks) * 4;
-                cp_async16(cs + (buf * W + k) * kRowTile + o, P.cols + (size_t)k * P.npad + r0 + o);
+                cp_async16(cs + (buf * W + k) * kRowsPerWarp + o, P.cols + (size_t)k * P.npad + r0 + o);
             } else {
                 const int cv = c - W * kColChunks;
                 const int k = cv / kValChunks, o = (cv % kValChunks) * 2;
-                cp_async16(vs + (buf * W + k) * kRowTile + o, SR + (size_t)k * P.npad + r0 + o);
+                cp_async16(vs + (buf * W + k) * kRowsPerWarp + o, SR + (size_t)k * P.npad + r0 + o);
             }
         }
         cp_async_commit();
@@ -467,13 +469,13 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
         } else {
             cp_async_wait0();
         }
-        __syncthreads();
-        const int32_t* ct = cs + buf * W * kRowTile;
-        const float2* vt = vs + buf * W * kRowTile;
+        __syncwarp();
+        const int32_t* ct = cs + buf * W * kRowsPerWarp;
+        const float2* vt = vs + buf * W * kRowsPerWarp;
         for (int st = 0; st < Sh::STEPS; st += RB) {
             int lr[RB];
 #pragma unroll
-            for (int i = 0; i < RB; ++i) lr[i] = warp * kRowsPerWarp + (st + i) * Sh::SUB + sub;
+            for (int i = 0; i < RB; ++i) lr[i] = (st + i) * Sh::SUB + sub;
             float y[RB][VEC];
 #pragma unroll
             for (int i = 0; i < RB; ++i)
@@ -484,8 +486,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
                 if (k < W) {
 #pragma unroll
                     for (int i = 0; i < RB; ++i) {
-                        const int c = ct[k * kRowTile + lr[i]];
-                        const float2 e = vt[k * kRowTile + lr[i]];
+                        const int c = ct[k * kRowsPerWarp + lr[i]];
+                        const float2 e = vt[k * kRowsPerWarp + lr[i]];
                         const float av = e.x + alpha * e.y;
                         float xv[VEC];
                         ldv<VEC>(p + (size_t)c * KP + j0, xv);
@@ -497,8 +499,8 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
             for (int k = kWFast; k < W; ++k) {
 #pragma unroll
                 for (int i = 0; i < RB; ++i) {
-                    const int c = ct[k * kRowTile + lr[i]];
-                    const float2 e = vt[k * kRowTile + lr[i]];
+                    const int c = ct[k * kRowsPerWarp + lr[i]];
+                    const float2 e = vt[k * kRowsPerWarp + lr[i]];
                     const float av = e.x + alpha * e.y;
                     float xv[VEC];
                     ldv<VEC>(p + (size_t)c * KP + j0, xv);
@@ -508,7 +510,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
             }
 #pragma unroll
             for (int i = 0; i < RB; ++i) {
-                const int row = t * kRowTile + lr[i];
+                const int row = t * kRowTile + warp * kRowsPerWarp + lr[i];
                 if (row < sg.end) {
 #pragma unroll
                     for (int v = 0; v < VEC; ++v) y[i][v] += sp[v];
@@ -520,7 +522,7 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
                 for (int v = 0; v < VEC; ++v) acc[0][v].add(pv[v], y[i][v]);
             }
         }
-        __syncthreads();  // the next stage() overwrites this buffer
+        __syncwarp();  // the next stage() overwrites this buffer
     }
     double* const parts[1] = {P.partA};
     if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter, nb)) {

@@ -180,6 +180,14 @@ typedef struct mpf_solve_opts {
      *    Same solutions, fewer iterations; needs <= 64 distinct excitation
      *    columns and <= 32768 nodes, otherwise Jacobi is used. */
     int32_t preconditioner;
+    /* 0: conjugate gradient (numeric::ConjugateGradient,
+     *    src/numeric/conjugate_gradient.cpp:61-161);
+     * 1: BiCGSTAB (numeric::BiCGSTAB, src/numeric/bicgstab.cpp:83-193),
+     *    right-preconditioned with Jacobi, each right-hand side stopped at
+     *    |r| <= tol |b|; the Neumann harmonic is iterated with the same
+     *    c' 1 1^T term as the CG, so both return the same fields.  Needs the
+     *    Jacobi preconditioner (preconditioner = 1 is ignored). */
+    int32_t solver;
 } mpf_solve_opts;
 
 typedef struct mpf_solve_stats {
@@ -324,9 +332,10 @@ int mpf_batch_destroy(mpf_batch_t batch);
 /* EIT::solve for `frames` frames of every model.  gamma[i]: device,
  * frames x n_elements(i); voltages[i]: device, frames x Mm(i) x Md(i), each
  * frame column-major (as mpf_eit_forward).  Both are host arrays of `count`
- * device pointers.  Cold start, Jacobi preconditioner, FP32 (MPF_ENOTSUP for
- * refine_tol > 0, warm_start != 0 or preconditioner != 0); launch shapes are
- * autotuned per width class at the first call with a frame count.
+ * device pointers.  Cold start, Jacobi preconditioner, FP32, CG or BiCGSTAB
+ * (opts->solver; MPF_ENOTSUP for refine_tol > 0, warm_start != 0 or
+ * preconditioner != 0); CG launch shapes are autotuned per width class at
+ * the first call with a frame count.
  * Synchronises `stream`.  stats->iterations: slowest group. */
 int mpf_batch_forward(mpf_batch_t batch, int32_t frames, const float* const* gamma, float* const* voltages,
                       const mpf_solve_opts* opts, mpf_solve_stats* stats, mpf_stream_t stream);
@@ -335,11 +344,12 @@ int mpf_batch_forward(mpf_batch_t batch, int32_t frames, const float* const* gam
  * [model][frame][active harmonic]; writes min(count, cap) entries. */
 int mpf_batch_iterations(mpf_batch_t batch, int32_t* iterations, int32_t cap, int32_t* count);
 
-/* Device time of the last call's CG (initialisation and iterations, CUDA
- * events on its stream) and the algorithmic bytes its iterations moved:
- * per iteration and group nnz * 12 + 11 * K * n * 4 + 4 * n * 4 (SpMM, update
- * and direction passes; K unique excitations, n nodes of the group's mesh).
- * No reference counterpart (measurement support). */
+/* Device time of the last call's Krylov solve (initialisation and
+ * iterations, CUDA events on its stream) and the algorithmic bytes its
+ * iterations moved: per iteration and group nnz * 12 + 11 * K * n * 4 +
+ * 4 * n * 4 for CG (SpMM, update and direction passes; K unique excitations,
+ * n nodes of the group's mesh), 2 * nnz * 12 + 21 * K * n * 4 + 6 * n * 4 for
+ * BiCGSTAB.  No reference counterpart (measurement support). */
 int mpf_batch_cg_stats(mpf_batch_t batch, double* cg_ms, double* cg_bytes);
 
 /* Launch shapes of the batch's CG kernels (codes as mpf_eit_cg_variants):

@@ -6,6 +6,7 @@
 //   numeric::Matrix<T>          include/mpflow/numeric/matrix.h
 //   numeric::IrregularMesh      include/mpflow/numeric/irregular_mesh.h
 //   numeric::ConjugateGradient  include/mpflow/numeric/conjugate_gradient.h (solver tag)
+//   numeric::BiCGSTAB           include/mpflow/numeric/bicgstab.h (solver tag)
 //   FEM::Ports, FEM::Sources<T> include/mpflow/fem/ports.h, sources.h
 //   FEM::Equation, basis::Linear include/mpflow/fem/equation.h (template tags)
 //   models::EIT<...>            include/mpflow/models/eit.h
@@ -363,9 +364,23 @@ private:
     mutable std::vector<type> host_;
 };
 
-// Krylov solver tags of models::EIT (the solve itself runs in the library)
+// Krylov solver tags of models::EIT (the solve itself runs in the library):
+// numeric::ConjugateGradient (include/mpflow/numeric/conjugate_gradient.h) and
+// numeric::BiCGSTAB (include/mpflow/numeric/bicgstab.h)
 template <class T>
 class ConjugateGradient {};
+template <class T>
+class BiCGSTAB {};
+
+// mpf_solve_opts::solver of a solver tag
+template <template <class> class S>
+struct SolverCode {
+    static int32_t const value = 0;
+};
+template <>
+struct SolverCode<BiCGSTAB> {
+    static int32_t const value = 1;
+};
 
 // Triangular mesh (src/numeric/irregular_mesh.cpp); edges, element edges and
 // boundary are derived by mpf_mesh_edges.
@@ -654,6 +669,7 @@ public:
         options.warm_start = 0;
         options.check_every = 16;
         options.preconditioner = 0;
+        options.solver = numeric::SolverCode<numericalSolverType>::value;
     }
     EIT(EIT const&) = delete;
     EIT& operator=(EIT const&) = delete;

@@ -52,7 +52,7 @@ class EitInfo(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("refine_tol", ctypes.c_double),
                 ("max_refine", ctypes.c_int32), ("warm_start", ctypes.c_int32),
-                ("check_every", ctypes.c_int32), ("preconditioner", ctypes.c_int32)]
+                ("check_every", ctypes.c_int32), ("preconditioner", ctypes.c_int32), ("solver", ctypes.c_int32)]
 
 
 class SolveStats(ctypes.Structure):

@@ -40,6 +40,10 @@ struct BatchClass {
     DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, sumP, Gm;
     DevBuf<int> conv, active, iters;
     DevBuf<unsigned> counter;
+    // BiCGSTAB vectors and scalars (grown on first use)
+    int capFB = 0;
+    DevBuf<float> Rhat, Zv, Tv;
+    DevBuf<double> omegaW, rr2W;
 };
 
 }  // namespace mpf
@@ -185,7 +189,20 @@ static int batch_workspace(mpf_batch* b, int F) {
     return MPF_OK;
 }
 
-static CgProblem class_problem(mpf_batch* b, BatchClass& cl, int F, double tol, const std::array<int, 3>* shapes) {
+static int class_bicgstab(mpf_batch* b, BatchClass& cl, int F) {
+    if (F <= cl.capFB) return MPF_OK;
+    const size_t G = (size_t)F * b->Ca * cl.members.size(), vec = (size_t)F * b->Ca * cl.npad * cl.KP;
+    MPF_TRY(cl.Rhat.alloc(vec));
+    MPF_TRY(cl.Zv.alloc(vec));
+    MPF_TRY(cl.Tv.alloc(vec));
+    MPF_TRY(cl.omegaW.alloc(G * cl.KP));
+    MPF_TRY(cl.rr2W.alloc(G * cl.KP));
+    cl.capFB = F;
+    return MPF_OK;
+}
+
+static CgProblem class_problem(mpf_batch* b, BatchClass& cl, int F, double tol, const std::array<int, 3>* shapes,
+                               int solver = 0) {
     CgProblem P{};
     P.npad = cl.npad;
     P.n = cl.npad;
@@ -220,6 +237,14 @@ static CgProblem class_problem(mpf_batch* b, BatchClass& cl, int F, double tol, 
     P.iters = cl.iters.ptr;
     P.counter = cl.counter.ptr;
     P.tol2 = tol * tol;
+    if (solver == 1) {
+        P.solver = 1;
+        P.rhat = cl.Rhat.ptr;
+        P.zv = cl.Zv.ptr;
+        P.tv = cl.Tv.ptr;
+        P.omega = cl.omegaW.ptr;
+        P.rr2 = cl.rr2W.ptr;
+    }
     for (int k = 0; k < 3; ++k) {
         int code = shapes ? (*shapes)[k] : cg_default_variant(cl.KP);
         if (b->forced[k] >= 0) code = b->forced[k];
@@ -238,6 +263,7 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
     if (in) o = *in;
     MPF_CHECK(o.refine_tol <= 0.0 && o.warm_start == 0 && o.preconditioner == 0, MPF_ENOTSUP,
               "mpf_batch_forward: batches solve cold with the Jacobi preconditioner and no FP64 refinement");
+    const int solver = o.solver == 1 ? 1 : 0;
     if (o.tol <= 0.0) o.tol = 1e-6;
     if (o.max_iter <= 0) o.max_iter = 10 * b->maxN;
     if (o.check_every <= 0) o.check_every = 16;
@@ -256,7 +282,9 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
         }
     }
     const int nC = (int)b->classes.size();
-    if (!b->variants.count(F)) {
+    if (solver == 1)
+        for (auto& cp : b->classes) MPF_TRY(class_bicgstab(b, *cp, F));
+    if (!b->variants.count(F) && solver == 0) {
         std::vector<std::array<int, 3>> best(nC);
         for (int c = 0; c < nC; ++c) {
             if (b->forced[0] >= 0 && b->forced[1] >= 0 && b->forced[2] >= 0) {
@@ -268,7 +296,11 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
         b->variants[F] = best;
     }
     std::vector<CgProblem> Ps;
-    for (int c = 0; c < nC; ++c) Ps.push_back(class_problem(b, *b->classes[c], F, o.tol, &b->variants[F][c]));
+    for (int c = 0; c < nC; ++c) {
+        auto it = b->variants.find(F);
+        Ps.push_back(class_problem(b, *b->classes[c], F, o.tol, it != b->variants.end() ? &it->second[c] : nullptr,
+                                   solver));
+    }
     cudaEvent_t e0, e1;
     MPF_CUDA(cudaEventCreate(&e0));
     MPF_CUDA(cudaEventCreate(&e1));
@@ -289,8 +321,8 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
     cudaEventDestroy(e1);
     if (st != MPF_OK) return st;
     // per-group iterations in [mesh][frame][harmonic] order and the
-    // algorithmic bytes the iterations moved (per iteration and group: the
-    // SpMM's nnz*12 + 2*K*n*4, the update's 6*K*n*4 + 2*n*4 and the
+    // algorithmic bytes the iterations moved (CG, per iteration and group:
+    // the SpMM's nnz*12 + 2*K*n*4, the update's 6*K*n*4 + 2*n*4 and the
     // direction's 3*K*n*4 + 2*n*4, K = unique excitation columns)
     b->iters.assign((size_t)b->M * F * b->Ca, 0);
     double bytes = 0.0;
@@ -304,7 +336,9 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
                 const int it = iters[off + (size_t)sl * Mc + j];
                 b->iters[(size_t)cl.members[j] * F * b->Ca + sl] = it;
                 const double n = m->n, K = m->K;
-                bytes += it * ((double)m->nnz * 12.0 + 11.0 * K * n * 4.0 + 4.0 * n * 4.0);
+                // BiCGSTAB: two SpMVs, 21 vector passes, three diagonal reads
+                bytes += solver == 1 ? it * (2.0 * m->nnz * 12.0 + 21.0 * K * n * 4.0 + 6.0 * n * 4.0)
+                                     : it * ((double)m->nnz * 12.0 + 11.0 * K * n * 4.0 + 4.0 * n * 4.0);
             }
         off += (size_t)F * b->Ca * Mc;
     }

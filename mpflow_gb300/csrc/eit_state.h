@@ -47,6 +47,10 @@ struct mpf_eit {
     mpf::DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, rr, bb, Gm, sumP, sumX;
     mpf::DevBuf<int> conv, active, iters;
     mpf::DevBuf<unsigned> counter;
+    // BiCGSTAB vectors and scalars (grown on first use)
+    int capFB = 0;
+    mpf::DevBuf<float> Rhat, Zv, Tv;
+    mpf::DevBuf<double> omegaW, rr2W;
     mpf::DevBuf<float> V, J, gramWork;
     mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
     mpf::DevBuf<double> A64, y, res;

@@ -413,7 +413,20 @@ static int ensure_coarse(mpf_eit* m, int F) {
     return MPF_OK;
 }
 
-static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false) {
+// BiCGSTAB's three extra vectors and two scalar arrays for F frames.
+static int ensure_bicgstab(mpf_eit* m, int F) {
+    if (F <= m->capFB) return MPF_OK;
+    const size_t G = (size_t)F * m->Ca, vec = G * m->npad * m->KP;
+    MPF_TRY(m->Rhat.alloc(vec));
+    MPF_TRY(m->Zv.alloc(vec));
+    MPF_TRY(m->Tv.alloc(vec));
+    MPF_TRY(m->omegaW.alloc(G * m->KP));
+    MPF_TRY(m->rr2W.alloc(G * m->KP));
+    m->capFB = F;
+    return MPF_OK;
+}
+
+static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false, int solver = 0) {
     CgProblem P{};
     P.n = m->n;
     P.npad = m->npad;
@@ -461,6 +474,14 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false
         P.rzFine = m->rzFine.ptr;
         P.bzFine = m->bzFine.ptr;
     }
+    if (solver == 1) {
+        P.solver = 1;
+        P.rhat = m->Rhat.ptr;
+        P.zv = m->Zv.ptr;
+        P.tv = m->Tv.ptr;
+        P.omega = m->omegaW.ptr;
+        P.rr2 = m->rr2W.ptr;
+    }
     auto it = m->cgVariants.find(F);
     for (int k = 0; k < 3; ++k) {
         int code = it != m->cgVariants.end() ? it->second[k] : cg_default_variant(m->KP);
@@ -497,8 +518,11 @@ static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
     o.warm_start = 0;
     o.check_every = 16;
     o.preconditioner = 0;
+    o.solver = 0;
     if (in) o = *in;
     if (o.preconditioner != 1) o.preconditioner = 0;
+    if (o.solver != 1) o.solver = 0;
+    if (o.solver == 1) o.preconditioner = 0;  // BiCGSTAB: Jacobi only
     if (o.tol <= 0.0) o.tol = 1e-6;
     if (o.max_iter <= 0) o.max_iter = 10 * n;
     if (o.max_refine <= 0) o.max_refine = 6;
@@ -561,10 +585,12 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
               "forward solve: FP64 refinement is implemented for current (open) sources only");
     MPF_TRY(eit_assemble(m, F, gamma, refine, s));
     if (m->fixed) MPF_TRY(fixed_prepare(m, F, s));
-    if (!warm) MPF_TRY(tune_cg(m, F, s));
+    const bool bicg = o.solver == 1;
+    if (bicg) MPF_TRY(ensure_bicgstab(m, F));
+    if (!warm && !bicg) MPF_TRY(tune_cg(m, F, s));
     const bool coarse = o.preconditioner == 1 && m->coarseOK;
     if (coarse) MPF_TRY(ensure_coarse(m, F));
-    CgProblem P = make_problem(m, F, o.tol, coarse);
+    CgProblem P = make_problem(m, F, o.tol, coarse, o.solver);
     if (coarse) {
         CoarsePlan cp{m->nc, m->ncPad, m->cNnz, m->cPairI.ptr, m->cPairJ.ptr, m->cPairPtr.ptr, m->cSlots.ptr,
                       m->cAggSize.ptr};

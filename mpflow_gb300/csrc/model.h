@@ -82,6 +82,12 @@ struct CgProblem {
     double* rzFine;       // [G][KP] r^T D^-1 r of the last update / init
     double* bzFine;       // [G][KP] b^T D^-1 b (init)
     int first;            // k_direction: p = M^-1 r (start of an iteration)
+    // solver 1: BiCGSTAB (bicgstab_kernels.cu).  Reuses x, r; p holds
+    // y = K^-1 p, q holds nu = A y; rz = rho, pq = alpha, beta, bz = |b|^2.
+    int solver;
+    float *rhat, *zv, *tv;  // shadow residual, z = K^-1 s, t = A z (vector layout)
+    double* omega;          // [G][KP]
+    double* rr2;            // [G][KP] |r|^2 of the last update
 };
 
 constexpr int kAgg = 64;  // rows per coarse aggregate (divides kRowTile)
@@ -141,6 +147,10 @@ int cg_launch_colsum(const CgProblem& P, const float* x, const double* x64, doub
 int cg_launch_dc_shift(const CgProblem& P, const double* shift, float sign, cudaStream_t s);
 int cg_launch_accumulate64(const CgProblem& P, double* x64, cudaStream_t s);
 int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s);
+// bicgstab_kernels.cu (cg_launch_init / cg_launch_iteration dispatch here for solver 1)
+int bicgstab_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
+int bicgstab_launch_iteration(const CgProblem& P, cudaStream_t s);
+constexpr int kBicgstabLaunches = 5;
 
 // fem_kernels.cu
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,

@@ -126,15 +126,17 @@ class Sources:
 
 class SolveOptions:
     """mpf_solve_opts; preconditioner "jacobi" (the reference's) or
-    "two-level" (Jacobi plus an aggregation coarse correction)."""
+    "two-level" (Jacobi plus an aggregation coarse correction); solver "cg"
+    (numeric::ConjugateGradient) or "bicgstab" (numeric::BiCGSTAB, Jacobi)."""
 
     PRECONDITIONERS = {"jacobi": 0, "two-level": 1}
+    SOLVERS = {"cg": 0, "bicgstab": 1}
     # warm_start: False/0 cold, True/1/"previous" fields of the previous call,
     # 2/"homogeneous" fields of the homogeneous distribution
     WARM_STARTS = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, "previous": 1, "homogeneous": 2}
 
     def __init__(self, tol=1e-6, max_iter=0, refine_tol=0.0, max_refine=6, warm_start=False,
-                 check_every=16, preconditioner: str = "jacobi"):
+                 check_every=16, preconditioner: str = "jacobi", solver: str = "cg"):
         self.tol, self.max_iter, self.refine_tol = tol, max_iter, refine_tol
         self.max_refine, self.warm_start, self.check_every = max_refine, warm_start, check_every
         if warm_start not in self.WARM_STARTS:
@@ -142,11 +144,14 @@ class SolveOptions:
         if preconditioner not in self.PRECONDITIONERS:
             raise ValueError(f"preconditioner must be one of {sorted(self.PRECONDITIONERS)}")
         self.preconditioner = preconditioner
+        if solver not in self.SOLVERS:
+            raise ValueError(f"solver must be one of {sorted(self.SOLVERS)}")
+        self.solver = solver
 
     def c(self) -> _ffi.SolveOpts:
         return _ffi.SolveOpts(float(self.tol), int(self.max_iter), float(self.refine_tol),
                               int(self.max_refine), self.WARM_STARTS[self.warm_start], int(self.check_every),
-                              self.PRECONDITIONERS[self.preconditioner])
+                              self.PRECONDITIONERS[self.preconditioner], self.SOLVERS[self.solver])
 
 
 def _stream():

@@ -244,6 +244,57 @@ def pcg(layout: Layout, values: np.ndarray, b: np.ndarray, x0: np.ndarray | None
     return x, iters
 
 
+def bicgstab(layout: Layout, values: np.ndarray, b: np.ndarray, x0: np.ndarray | None = None,
+             tol: float = 1e-12, max_iter: int = 0):
+    """Right-preconditioned BiCGSTAB with the Jacobi preconditioner over
+    independent columns, restating BiCGSTAB::solve (src/numeric/bicgstab.cpp:
+    83-193): y = K^-1 p, nu = A y, alpha = rho / (rHat, nu), s = r - alpha nu,
+    z = K^-1 s, t = A z, omega = (z, K^-1 t) / (K^-1 t, K^-1 t),
+    x += alpha y + omega z, r = s - omega t.  The reference stops when column
+    0 reaches |r| / |b| < eps; here every column stops on its own at
+    |r| <= tol |b| and keeps its x and r from then on.  dcFree is ignored, as
+    in the reference.  Returns (x, iterations per column)."""
+    n = layout.n
+    ids = layout.colIds[:n].astype(np.int64)
+    vals = np.asarray(values, np.float64)[:n]
+    diag = np.where(ids == np.arange(n)[:, None], vals, 0.0).sum(axis=1)
+    dinv = np.where(diag != 0.0, 1.0 / np.where(diag != 0.0, diag, 1.0), 0.0)[:, None]
+    b = np.asarray(b, np.float64)
+    cols = b.shape[1]
+    x = np.zeros((n, cols)) if x0 is None else np.array(x0, np.float64)
+    r = b - ell_multiply(layout, values, x)
+    rhat = r.copy()
+    rho = np.ones(cols)
+    alpha = np.ones(cols)
+    omega = np.ones(cols)
+    nu = np.zeros((n, cols))
+    p = np.zeros((n, cols))
+    bb = (b * b).sum(axis=0)
+    live = (r * r).sum(axis=0) > tol * tol * bb
+    iters = np.zeros(cols, np.int64)
+    for _ in range(max_iter if max_iter > 0 else 10 * n):
+        if not live.any():
+            break
+        rho_old, rho = rho, np.where(live, (rhat * r).sum(axis=0), rho)
+        beta = (rho / rho_old) * (alpha / omega)
+        p = np.where(live, r + beta * (p - omega * nu), p)
+        y = dinv * p
+        nu = np.where(live, ell_multiply(layout, values, y), nu)
+        den = (rhat * nu).sum(axis=0)
+        alpha = np.where(live, rho / np.where(den != 0.0, den, 1.0), alpha)
+        s = r - alpha * nu
+        z = dinv * s
+        t = ell_multiply(layout, values, z)
+        kt = dinv * t
+        tt = (kt * kt).sum(axis=0)
+        omega = np.where(live, (z * kt).sum(axis=0) / np.where(tt > 0.0, tt, 1.0), omega)
+        x = np.where(live, x + alpha * y + omega * z, x)
+        r = np.where(live, s - omega * t, r)
+        iters += live
+        live = live & ((r * r).sum(axis=0) > tol * tol * bb)
+    return x, iters
+
+
 def calc_jacobian(elements, K, phi, drive_count, meas_count, gamma, ref, logarithmic,
                   rowsJ, J=None, additive=False):
     """J (rowsJ x E, column-major), src/fem/equation_kernel.cu:197-245."""
@@ -321,8 +372,9 @@ class Setup:
 
 
 def eit_forward(s: Setup, gamma: np.ndarray, tol: float = 1e-12, want_jacobian: bool = True,
-                max_iter: int = 0, exact: bool = False):
-    """Restatement of EIT::solve for current (Open) sources.
+                max_iter: int = 0, exact: bool = False, solver: str = "cg"):
+    """Restatement of EIT::solve for current (Open) sources (solver "cg" or
+    "bicgstab", the numericalSolverType template argument of models::EIT).
 
     Returns (V, J, fields): V is Mm x Md, J is rowsJ x E column-major (row =
     drive * roundMeas + meas), fields is a list of n x (Md+Mm) arrays per
@@ -341,7 +393,10 @@ def eit_forward(s: Setup, gamma: np.ndarray, tol: float = 1e-12, want_jacobian: 
         alpha, beta = s.alpha_beta(c)
         sysv = update_system_matrix(s.layout, S, R, alpha)
         excitation = (s.exc @ pattern) * beta
-        x, _ = pcg(s.layout, sysv, excitation, tol=tol, max_iter=max_iter, dc_free=(c == 0))
+        if solver == "bicgstab":
+            x, _ = bicgstab(s.layout, sysv, excitation, tol=tol, max_iter=max_iter)
+        else:
+            x, _ = pcg(s.layout, sysv, excitation, tol=tol, max_iter=max_iter, dc_free=(c == 0))
         fields.append(x)
         if want_jacobian and not exact:
             calc_jacobian(s.elements, s.K, x, s.Md, s.Mm, gamma, s.ref, s.logarithmic, s.rowsJ,

@@ -11,6 +11,7 @@
 
 using namespace mpFlow;
 typedef models::EIT<numeric::ConjugateGradient, FEM::Equation<float, FEM::basis::Linear, false>> Model;
+typedef models::EIT<numeric::BiCGSTAB, FEM::Equation<float, FEM::basis::Linear, false>> ModelBi;
 
 // json-selftest: parse a configuration without touching the GPU
 static int json_selftest() {
@@ -89,6 +90,20 @@ int main(int argc, char** argv) {
                 sumAbs += std::fabs((*V0)(i, j));
             }
 
+        // the same solve with the BiCGSTAB solver tag
+        auto modelBi = std::make_shared<ModelBi>(mesh, sources, 1.0f, handle, stream, 1, 1.0, 1.0);
+        modelBi->options.tol = 1e-7;
+        unsigned stepsBi = 0;
+        auto Vb = modelBi->solve(reference, handle, stream, &stepsBi);
+        Vb->copyToHost(stream);
+        double biErr = 0.0, vMax = 0.0;
+        for (unsigned i = 0; i < V0->rows; ++i)
+            for (unsigned j = 0; j < V0->cols; ++j) {
+                biErr = std::max(biErr, (double)std::fabs((*Vb)(i, j) - (*V0)(i, j)));
+                vMax = std::max(vMax, (double)std::fabs((*V0)(i, j)));
+            }
+        biErr /= std::max(vMax, 1e-300);
+
         // measurement: an inclusion of 0.5 S/m at (0.3, 0.2), radius 0.25
         auto target = std::make_shared<numeric::Matrix<float>>(E, 1, stream, 1.0f);
         std::vector<int> inside;
@@ -133,10 +148,11 @@ int main(int argc, char** argv) {
             for (unsigned j = 0; j < V0->cols; ++j) rt = std::max(rt, (double)std::fabs((*back)(i, j) - (*V0)(i, j)));
 
         const bool ok = steps > 0 && std::isfinite(sumAbs) && sumAbs > 0.0 && in < out && in < -0.01 &&
-                        rt <= 1e-6 * sumAbs;
+                        rt <= 1e-6 * sumAbs && stepsBi > 0 && biErr <= 1e-5;
         printf("{\"steps\": %u, \"sum_v\": %.9e, \"sum_abs_v\": %.9e, \"mean_delta_inside\": %.6e, "
-               "\"mean_delta_outside\": %.6e, \"text_roundtrip_max_err\": %.3e, \"ok\": %s}\n",
-               steps, sumV, sumAbs, in, out, rt, ok ? "true" : "false");
+               "\"mean_delta_outside\": %.6e, \"text_roundtrip_max_err\": %.3e, \"bicgstab_steps\": %u, "
+               "\"bicgstab_rel_err\": %.3e, \"ok\": %s}\n",
+               steps, sumV, sumAbs, in, out, rt, stepsBi, biErr, ok ? "true" : "false");
         return ok ? 0 : 1;
     } catch (std::exception const& ex) {
         printf("{\"error\": \"%s\", \"ok\": false}\n", ex.what());

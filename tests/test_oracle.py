@@ -139,3 +139,20 @@ def test_fixed_source_oracle_jacobian_is_derivative():
     Vm, _, _ = oracle.eit_forward_fixed(orc, gm, want_jacobian=False)
     fd = oracle.flatten_measurement((Vp - Vm) / (2 * h), orc)
     assert np.abs(fd - J[:, e]).max() <= 1e-5 * np.abs(J[:, e]).max()
+
+
+def test_bicgstab_oracle_matches_cg_oracle():
+    """The two Krylov solvers of models::EIT give the same voltages and
+    Jacobian; fields agree up to a constant on the Neumann harmonic (the
+    reference's BiCGSTAB ignores dcFree)."""
+    mesh, src, orc = make_setup(rings=16, ports=16, components=3, height=2.0)
+    g = inclusion_sigma(mesh, seed=1)
+    V1, J1, F1 = oracle.eit_forward(orc, g, tol=1e-13)
+    V2, J2, F2 = oracle.eit_forward(orc, g, tol=1e-13, solver="bicgstab")
+    assert np.abs(V1 - V2).max() <= 1e-11 * np.abs(V1).max()
+    assert np.abs(J1 - J2).max() <= 1e-11 * np.abs(J1).max()
+    for c in range(3):
+        d = F1[c] - F2[c]
+        assert np.abs(d - d.mean(axis=0)).max() <= 1e-11 * np.abs(F1[c]).max()
+        if c > 0:
+            assert np.abs(d).max() <= 1e-11 * np.abs(F1[c]).max()

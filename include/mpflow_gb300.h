@@ -225,6 +225,23 @@ int mpf_eit_forward(mpf_eit_t model, int32_t frames, const float* gamma, float* 
  * (drive_count + meas_count). */
 int mpf_eit_fields(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t stream);
 
+/* EIT::solve for complex material values: the reference's
+ * models::EIT<..., FEM::Equation<thrust::complex<float>, ...>> instantiations
+ * (src/models/eit.cpp:289-304).  p(gamma) = ref * gamma or
+ * ref * exp(ln(10) gamma / 10) with complex gamma
+ * (src/fem/equation_kernel.cu:35-43; a complex reference value is expressed
+ * through gamma), complex S and R, BiCGSTAB over complex vectors with the
+ * reference's inner product sum a conj(b) (src/numeric/matrix_kernel.cu:
+ * 404-413), Jacobi-preconditioned, each right-hand side stopped at
+ * |r| <= tol |b|, FP32 with FP64 inner products.
+ *   gamma:    device, frames x n_elements complex (re, im interleaved)
+ *   voltages: device, frames x (Mm x Md column-major) complex, interleaved
+ * Cold start only; MPF_ENOTSUP for refine_tol > 0, warm_start != 0, voltage
+ * (fixed) sources or more than 64 unique excitations.  The complex Jacobian
+ * is not computed.  Synchronises `stream`. */
+int mpf_eit_forward_complex(mpf_eit_t model, int32_t frames, const float* gamma, float* voltages,
+                            const mpf_solve_opts* opts, mpf_solve_stats* stats, mpf_stream_t stream);
+
 /* ======================================================================== */
 /* Regularised Gauss-Newton                                                  */
 /* ======================================================================== */

@@ -765,6 +765,10 @@ static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count)
 // solve and p0 = M^-1 r0 (the direction kernel with beta = 0).
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s) {
     if (P.solver == 1) return bicgstab_launch_init(P, zeroGuess, s);
+    if (P.solver == 2) {
+        MPF_CHECK(zeroGuess, MPF_ENOTSUP, "complex admittivity: warm starts are not implemented");
+        return zbicgstab_launch_init(P, s);
+    }
     MPF_TRY(dispatch_kp<InitL>(P.KP, P, zeroGuess, s));
     if (!P.coarse) return MPF_OK;
     MPF_TRY(cg_launch_coarse(P, true, s));
@@ -799,13 +803,14 @@ static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count)
 
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s) {
     if (P.solver == 1) return bicgstab_launch_iteration(P, s);
+    if (P.solver == 2) return zbicgstab_launch_iteration(P, s);
     MPF_TRY(launch_one(P, 0, s, false));
     MPF_TRY(launch_one(P, 1, s, false));
     if (P.coarse) MPF_TRY(cg_launch_coarse(P, false, s, false));
     return launch_one(P, 2, s, false);
 }
 
-int cg_iteration_launches(const CgProblem& P) { return P.solver == 1 ? kBicgstabLaunches : P.coarse ? 4 : 3; }
+int cg_iteration_launches(const CgProblem& P) { return P.solver >= 1 ? kBicgstabLaunches : P.coarse ? 4 : 3; }
 
 int cg_launch_kernel(const CgProblem& P, int which, cudaStream_t s) { return launch_one(P, which, s, true); }
 

@@ -51,6 +51,12 @@ struct mpf_eit {
     int capFB = 0;
     mpf::DevBuf<float> Rhat, Zv, Tv;
     mpf::DevBuf<double> omegaW, rr2W;
+    // complex admittivity (complex_kernels.cu): complex slot values, seven
+    // complex vectors, imaginary parts of the scalars, complex Gram
+    int capFZ = 0;
+    mpf::DevBuf<float4> SRz;
+    mpf::DevBuf<float> Xz, Rz, Yz, Nz, Hz, Zz, Tz, Vz;
+    mpf::DevBuf<double> zRhoI, zAlphaI, zBetaI, zOmega, zOmegaI, zSumI, zRr, Gmz;
     mpf::DevBuf<float> V, J, gramWork;
     mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
     mpf::DevBuf<double> A64, y, res;

@@ -426,6 +426,20 @@ static int ensure_bicgstab(mpf_eit* m, int F) {
     return MPF_OK;
 }
 
+// Complex-admittivity workspace for F frames.
+static int ensure_complex(mpf_eit* m, int F) {
+    if (F <= m->capFZ) return MPF_OK;
+    const size_t G = (size_t)F * m->Ca, vec2 = 2 * G * m->npad * m->KP, sc = G * m->KP;
+    MPF_TRY(m->SRz.alloc((size_t)F * m->W * m->npad));
+    for (auto* b : {&m->Xz, &m->Rz, &m->Yz, &m->Nz, &m->Hz, &m->Zz, &m->Tz}) MPF_TRY(b->alloc(vec2));
+    for (auto* b : {&m->zRhoI, &m->zAlphaI, &m->zBetaI, &m->zOmega, &m->zOmegaI, &m->zSumI, &m->zRr})
+        MPF_TRY(b->alloc(sc));
+    MPF_TRY(m->Gmz.alloc(2 * G * m->KP * m->KP));
+    MPF_TRY(m->Vz.alloc(2 * (size_t)F * m->Mm * m->Md));
+    m->capFZ = F;
+    return MPF_OK;
+}
+
 static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false, int solver = 0) {
     CgProblem P{};
     P.n = m->n;
@@ -673,6 +687,62 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     return notConv ? fail(MPF_ENOCONV, "forward solve: %d systems did not converge", notConv) : MPF_OK;
+}
+
+// Forward solve for complex material values (complex_kernels.cu): gamma
+// [F][E] complex, V [F][Mm][Md] complex (column-major per frame), both with
+// interleaved real and imaginary parts.
+int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, const mpf_solve_opts* optsIn,
+                        mpf_solve_stats* stats, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma && Vout, MPF_EINVAL, "mpf_eit_forward_complex: bad arguments");
+    MPF_CHECK(!m->fixed, MPF_ENOTSUP, "mpf_eit_forward_complex: voltage (fixed) sources are not implemented");
+    MPF_CHECK(m->KP <= 64, MPF_ENOTSUP, "mpf_eit_forward_complex: at most 64 unique excitations");
+    auto t0 = std::chrono::steady_clock::now();
+    mpf_solve_opts o;
+    fill_defaults(optsIn, o, m->n);
+    MPF_CHECK(o.refine_tol <= 0.0 && o.warm_start == 0, MPF_ENOTSUP,
+              "mpf_eit_forward_complex: cold FP32 solves only (no refinement, no warm start)");
+    MPF_TRY(ensure_workspace(m, F, false, false));
+    MPF_TRY(ensure_complex(m, F));
+    MPF_TRY(fem_launch_zassemble(F, m->W, m->npad, m->E, m->cptr.ptr, m->contrib.ptr, m->Kf.ptr, m->Mf.ptr, gamma,
+                                 m->ref, m->logarithmic, m->SRz.ptr, s));
+    CgProblem P = make_problem(m, F, o.tol);
+    P.solver = 2;
+    P.SR = nullptr;
+    P.SRz = m->SRz.ptr;
+    P.x = m->Xz.ptr;
+    P.r = m->Rz.ptr;
+    P.p = m->Yz.ptr;
+    P.q = m->Nz.ptr;
+    P.rhat = m->Hz.ptr;
+    P.zv = m->Zz.ptr;
+    P.tv = m->Tz.ptr;
+    P.omega = m->zOmega.ptr;
+    P.rr2 = m->zRr.ptr;
+    P.rzI = m->zRhoI.ptr;
+    P.pqI = m->zAlphaI.ptr;
+    P.betaI = m->zBetaI.ptr;
+    P.omegaI = m->zOmegaI.ptr;
+    P.sumPI = m->zSumI.ptr;
+    int iters = 0, notConv = 0;
+    MPF_TRY(cg_launch_init(P, true, s));
+    MPF_TRY(run_cg(m, P, o.max_iter, o.check_every, s, &iters, &notConv));
+    if (m->anyDcFree) MPF_TRY(cg_launch_zdc_shift(P, m->dcShift.ptr, 1.f, s));
+    MPF_TRY(fem_launch_zgram_meas(P.G, m->KP, m->npad, m->nzPtr.ptr, m->nzNode.ptr, m->nzVal.ptr, m->Xz.ptr,
+                                  m->Gmz.ptr, s));
+    MPF_TRY(fem_launch_zvoltages(F, m->Ca, m->KP, m->Mm, m->Md, m->Gmz.ptr, m->beta.ptr, m->measU.ptr,
+                                 m->measScale.ptr, m->driveU.ptr, m->driveScale.ptr, Vout, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    MPF_CUDA(cudaGetLastError());
+    if (stats) {
+        stats->iterations = iters;
+        stats->refinements = 0;
+        stats->not_converged = notConv;
+        stats->max_rel_residual = 0.0;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return notConv ? fail(MPF_ENOCONV, "complex forward solve: %d systems did not converge", notConv) : MPF_OK;
 }
 
 int eit_forward(mpf_eit* m, int F, const float* gamma, float* V, float* Jref, const mpf_solve_opts* o,

@@ -88,6 +88,13 @@ struct CgProblem {
     float *rhat, *zv, *tv;  // shadow residual, z = K^-1 s, t = A z (vector layout)
     double* omega;          // [G][KP]
     double* rr2;            // [G][KP] |r|^2 of the last update
+    // solver 2: complex BiCGSTAB (complex_kernels.cu).  Vectors hold KP
+    // complex values per node (re, im interleaved); SRz holds the complex
+    // slot values {S.re, S.im, R.re, R.im}; the *I arrays are the imaginary
+    // parts of rho, alpha, beta, omega and sum(.) (real parts in rz, pq,
+    // beta, omega, sumP)
+    const float4* SRz;
+    double *rzI, *pqI, *betaI, *omegaI, *sumPI;
 };
 
 constexpr int kAgg = 64;  // rows per coarse aggregate (divides kRowTile)
@@ -151,6 +158,17 @@ int cg_launch_to_float(const CgProblem& P, const double* x64, cudaStream_t s);
 int bicgstab_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
 int bicgstab_launch_iteration(const CgProblem& P, cudaStream_t s);
 constexpr int kBicgstabLaunches = 5;
+// complex_kernels.cu: complex admittivity (solver 2)
+int zbicgstab_launch_init(const CgProblem& P, cudaStream_t s);
+int zbicgstab_launch_iteration(const CgProblem& P, cudaStream_t s);
+int fem_launch_zassemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib, const float* Kf,
+                         const float* Mf, const float* gamma2, float ref, int logarithmic, float4* SRz, cudaStream_t s);
+int cg_launch_zdc_shift(const CgProblem& P, const double* shift, float sign, cudaStream_t s);
+int fem_launch_zgram_meas(int G, int KP, int npad, const int32_t* nzPtr, const int32_t* nzNode, const double* nzVal,
+                          const float* Xz, double* Gmz, cudaStream_t s);
+int fem_launch_zvoltages(int F, int Ca, int KP, int Mm, int Md, const double* Gmz, const float* beta,
+                         const int32_t* measU, const float* measScale, const int32_t* driveU, const float* driveScale,
+                         float* Vz, cudaStream_t s);
 
 // fem_kernels.cu
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,

@@ -251,6 +251,29 @@ class EIT:
             return Vm, J.transpose(1, 2)
         return Vm
 
+    def solve_complex(self, materialDistribution, options: SolveOptions | None = None,
+                      raise_on_noconv: bool = True):
+        """Forward solve for complex material values (complex64 CUDA tensor,
+        frames x elements); returns complex64 voltages (frames x Mm x Md),
+        mpf_eit_forward_complex."""
+        import torch
+        g = materialDistribution
+        if not (isinstance(g, torch.Tensor) and g.is_cuda and g.dtype == torch.complex64):
+            raise TypeError("materialDistribution must be a complex64 CUDA tensor")
+        g = g.reshape(-1, self.mesh.elements.shape[0]).contiguous()
+        F = g.shape[0]
+        Mm, Md = self.info["meas_count"], self.info["drive_count"]
+        V = torch.empty((F, Md, Mm), dtype=torch.complex64, device=g.device)
+        st = _ffi.SolveStats()
+        o = (options or SolveOptions(solver="bicgstab")).c()
+        status = lib().mpf_eit_forward_complex(self._h, F, ctypes.c_void_p(g.data_ptr()),
+                                               ctypes.c_void_p(V.data_ptr()), ctypes.byref(o), ctypes.byref(st),
+                                               _stream())
+        self.last_stats = st
+        if status != _ffi.MPF_OK and (raise_on_noconv or status != 4):
+            check(status)
+        return V.transpose(1, 2)
+
     def fields(self, frames: int):
         """Potentials of the last solve: (frames, components, Md+Mm, data_rows)."""
         import torch

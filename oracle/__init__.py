@@ -533,3 +533,32 @@ def eit_forward_fixed(s: Setup, gamma: np.ndarray, want_jacobian: bool = True):
     if want_jacobian:
         J *= s.height
     return V, J, fields
+
+
+def eit_forward_complex(s: Setup, gamma: np.ndarray) -> np.ndarray:
+    """Restatement of EIT::solve for complex material values (the
+    Equation<thrust::complex<T>> instantiations, src/models/eit.cpp:139-245
+    and :289-304; p(gamma) of src/fem/equation_kernel.cu:35-43 with complex
+    gamma), current sources.  The complex systems are solved directly in FP64
+    (the reference iterates to the same solution); the Neumann harmonic is
+    (A + 1 1^T) x = b as in the reference's CG.  Returns V (Mm x Md, complex)."""
+    g = np.asarray(gamma, np.complex128)
+    p = s.ref * (np.exp(math.log(10.0) * g / 10.0) if s.logarithmic else g)
+    S = (update_matrix(s.layout, s.layout.elemS, p.real, 1.0, False) +
+         1j * update_matrix(s.layout, s.layout.elemS, p.imag, 1.0, False))
+    R = (update_matrix(s.layout, s.layout.elemR, p.real, 1.0, False) +
+         1j * update_matrix(s.layout, s.layout.elemR, p.imag, 1.0, False))
+    n = s.nodes.shape[0]
+    pattern = np.concatenate([s.drive * s.values[None, :], s.meas], axis=1)
+    att = s.meas.T @ s.exc.T
+    V = np.zeros((s.Mm, s.Md), np.complex128)
+    for c in range(s.components):
+        alpha, beta = s.alpha_beta(c)
+        sys_re = update_system_matrix(s.layout, S.real.copy(), R.real.copy(), alpha)
+        sys_im = update_system_matrix(s.layout, S.imag.copy(), R.imag.copy(), alpha)
+        A = dense_matrix(s.layout, sys_re, n) + 1j * dense_matrix(s.layout, sys_im, n)
+        if c == 0:
+            A = A + 1.0
+        x = np.linalg.solve(A, (s.exc @ pattern) * beta)
+        V += att @ x[:, :s.Md]
+    return V

@@ -1,0 +1,69 @@
+"""Complex admittivity (mpf_eit_forward_complex) against the FP64 oracle's
+complex forward model and against the real path, through the C ABI."""
+import numpy as np
+import pytest
+
+from conftest import inclusion_sigma, make_setup
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _complex_frames(mesh, count, seed, logarithmic):
+    """Conductivity with an inclusion plus a permittivity-like imaginary part."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for f in range(count):
+        sig = inclusion_sigma(mesh, seed=seed + f)
+        eps = 0.1 + 0.2 * rng.random(mesh.elements.shape[0])
+        g = sig + 1j * eps * sig
+        out.append(10.0 * np.log10(g) if logarithmic else g)
+    return np.stack(out)
+
+
+@pytest.mark.parametrize("logarithmic", [False, True])
+def test_complex_forward_matches_oracle(logarithmic):
+    import oracle
+    import torch
+    import mpflow_gb300 as mp
+    mesh, src, orc = make_setup(rings=16, ports=16, components=3, height=2.0, logarithmic=logarithmic)
+    g = _complex_frames(mesh, 2, seed=3, logarithmic=logarithmic)
+    model = mp.EIT(mesh, src, 1.0, components=3, height=2.0, logarithmic=logarithmic)
+    V = model.solve_complex(torch.tensor(g, dtype=torch.complex64, device="cuda"),
+                            mp.SolveOptions(tol=1e-7, solver="bicgstab"))
+    assert model.last_stats.not_converged == 0 and model.last_stats.iterations > 0
+    for f in range(2):
+        Vo = oracle.eit_forward_complex(orc, g[f])
+        assert np.abs(Vo.imag).max() > 1e-3 * np.abs(Vo.real).max()  # a genuinely complex case
+        assert rel_err(V[f].cpu().numpy(), Vo) < 1e-4, f
+
+
+def test_complex_with_real_values_equals_real_solve():
+    import torch
+    import mpflow_gb300 as mp
+    mesh, src, _ = make_setup(rings=20, ports=32, width=0.1, components=4, height=4.0)
+    g = np.stack([inclusion_sigma(mesh, seed=s) for s in range(3)])
+    model = mp.EIT(mesh, src, 1.0, components=4, height=4.0)
+    Vr = model.solve(torch.tensor(g, dtype=torch.float32, device="cuda"), mp.SolveOptions(tol=1e-7))
+    Vz = model.solve_complex(torch.tensor(g, dtype=torch.complex64, device="cuda"),
+                             mp.SolveOptions(tol=1e-7, solver="bicgstab"))
+    Vr = Vr.cpu().numpy()
+    Vz = Vz.cpu().numpy()
+    assert rel_err(Vz.real, Vr) < 2e-5
+    assert np.abs(Vz.imag).max() <= 1e-6 * np.abs(Vr).max()
+
+
+def test_complex_rejects_unsupported_options():
+    import torch
+    import mpflow_gb300 as mp
+    mesh, src, _ = make_setup(rings=12, ports=16, width=0.2)
+    model = mp.EIT(mesh, src, 1.0)
+    g = torch.ones((1, mesh.elements.shape[0]), dtype=torch.complex64, device="cuda")
+    for opts in (mp.SolveOptions(refine_tol=1e-9), mp.SolveOptions(warm_start=True)):
+        with pytest.raises(mp.MpfError) as e:
+            model.solve_complex(g, opts)
+        assert e.value.status == 8

@@ -156,3 +156,13 @@ def test_bicgstab_oracle_matches_cg_oracle():
         assert np.abs(d - d.mean(axis=0)).max() <= 1e-11 * np.abs(F1[c]).max()
         if c > 0:
             assert np.abs(d).max() <= 1e-11 * np.abs(F1[c]).max()
+
+
+def test_complex_oracle_reduces_to_real():
+    """With zero imaginary part the complex forward model is the real one."""
+    mesh, src, orc = make_setup(rings=12, ports=8, width=0.3, components=3, height=2.0)
+    g = inclusion_sigma(mesh, seed=2)
+    V, _, _ = oracle.eit_forward(orc, g, tol=1e-14, want_jacobian=False)
+    Vz = oracle.eit_forward_complex(orc, g.astype(np.complex128))
+    assert np.abs(Vz.imag).max() <= 1e-12 * np.abs(V).max()
+    assert np.abs(Vz.real - V).max() <= 1e-9 * np.abs(V).max()

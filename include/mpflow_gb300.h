@@ -363,7 +363,7 @@ int mpf_batch_iterations(mpf_batch_t batch, int32_t* iterations, int32_t cap, in
 
 /* Device time of the last call's Krylov solve (initialisation and
  * iterations, CUDA events on its stream) and the algorithmic bytes its
- * iterations moved: per iteration and group nnz * 12 + 11 * K * n * 4 +
+ * iterations moved: per iteration and group nnz * 12 + 10 * K * n * 4 +
  * 4 * n * 4 for CG (SpMM, update and direction passes; K unique excitations,
  * n nodes of the group's mesh), 2 * nnz * 12 + 21 * K * n * 4 + 6 * n * 4 for
  * BiCGSTAB.  No reference counterpart (measurement support). */

@@ -38,8 +38,9 @@ struct BatchClass {
     DevBuf<float2> SR;          // [F][W][npad]
     DevBuf<float> X, Rv, Pv, Qv;
     DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, sumP, Gm;
-    DevBuf<int> conv, active, iters;
+    DevBuf<int> conv, active, iters, pend;
     DevBuf<unsigned> counter;
+    DevBuf<double> alphaX;
     // BiCGSTAB vectors and scalars (grown on first use)
     int capFB = 0;
     DevBuf<float> Rhat, Zv, Tv;
@@ -173,6 +174,9 @@ static int batch_workspace(mpf_batch* b, int F) {
         MPF_TRY(cl.betaW.alloc(sc));
         MPF_TRY(cl.sumP.alloc(sc));
         MPF_TRY(cl.conv.alloc(sc));
+        MPF_TRY(cl.alphaX.alloc(sc));
+        MPF_TRY(cl.pend.alloc(G));
+        MPF_CUDA(cudaMemset(cl.pend.ptr, 0, G * sizeof(int)));
         MPF_TRY(cl.active.alloc(G));
         MPF_TRY(cl.iters.alloc(G));
         MPF_TRY(cl.counter.alloc(G));
@@ -236,6 +240,8 @@ static CgProblem class_problem(mpf_batch* b, BatchClass& cl, int F, double tol, 
     P.active = cl.active.ptr;
     P.iters = cl.iters.ptr;
     P.counter = cl.counter.ptr;
+    P.alphaX = cl.alphaX.ptr;
+    P.pend = cl.pend.ptr;
     P.tol2 = tol * tol;
     if (solver == 1) {
         P.solver = 1;
@@ -322,8 +328,8 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
     if (st != MPF_OK) return st;
     // per-group iterations in [mesh][frame][harmonic] order and the
     // algorithmic bytes the iterations moved (CG, per iteration and group:
-    // the SpMM's nnz*12 + 2*K*n*4, the update's 6*K*n*4 + 2*n*4 and the
-    // direction's 3*K*n*4 + 2*n*4, K = unique excitation columns)
+    // the SpMM's nnz*12 + 2*K*n*4, the update's 3*K*n*4 + 2*n*4 and the
+    // direction's 5*K*n*4 + 2*n*4, K = unique excitation columns)
     b->iters.assign((size_t)b->M * F * b->Ca, 0);
     double bytes = 0.0;
     size_t off = 0;
@@ -338,7 +344,7 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
                 const double n = m->n, K = m->K;
                 // BiCGSTAB: two SpMVs, 21 vector passes, three diagonal reads
                 bytes += solver == 1 ? it * (2.0 * m->nnz * 12.0 + 21.0 * K * n * 4.0 + 6.0 * n * 4.0)
-                                     : it * ((double)m->nnz * 12.0 + 11.0 * K * n * 4.0 + 4.0 * n * 4.0);
+                                     : it * ((double)m->nnz * 12.0 + 10.0 * K * n * 4.0 + 4.0 * n * 4.0);
             }
         off += (size_t)F * b->Ca * Mc;
     }

@@ -120,6 +120,8 @@ int cg_run(CgGraphCache& cache, int* pinned, const CgProblem* Ps, int nP, int ma
     if (anyActive) {
         for (int g = 0; g < Gtot; ++g) nc += pinned[g] != 0;
     }
+    // the x update of groups that retired in their last k_update
+    for (int i = 0; i < nP; ++i) MPF_TRY(cg_launch_finalize(Ps[i], s));
     MPF_TRY(fetch(false));
     iters.assign(pinned, pinned + Gtot);
     *maxIters = Gtot ? *std::max_element(iters.begin(), iters.end()) : 0;

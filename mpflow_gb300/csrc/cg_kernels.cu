@@ -9,8 +9,11 @@
 //
 // One CG iteration is three launches, each a single pass over the vectors:
 //   k_spmm_dot   q = (S + alpha R) p,  pq = p.q
-//   k_update     x += a p, r -= a q, z = D^-1 r, rz' = r.z  (+ convergence)
-//   k_direction  p = D^-1 r + b p
+//   k_update     r -= a q, z = D^-1 r, rz' = r.z  (+ convergence)
+//   k_direction  x += a p_old, p = D^-1 r + b p_old
+// x is updated where the old p is read anyway (10 vector passes per
+// iteration instead of 11); cg_launch_finalize applies the last update of
+// groups that retired.
 // Memory access: a lane moves VEC consecutive floats, so KP/VEC lanes cover
 // one node's right-hand sides and one warp instruction serves 32*VEC/KP
 // rows; each warp keeps RB row steps in flight, and a block walks
@@ -137,6 +140,8 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
     double* const parts[3] = {P.partA, P.partB, P.partC};
     const int nb = sg.nblk;
     if (block_partials<KP, VEC, 3>(acc, parts, g, P.counter, nb)) {
+        if (threadIdx.x < KP) P.alphaX[(size_t)g * KP + threadIdx.x] = 0.0;
+        if (threadIdx.x == 0) P.pend[g] = 0;
         if (P.coarse) {
             // the coarse kernel completes r^T M^-1 r and b^T M^-1 b and sets the masks
             if (threadIdx.x < KP) {
@@ -394,15 +399,13 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
     for (int st = 0; st < nsteps; st += RB) {
         const int rowBase = (tile0 + st / Sh::STEPS) * kRowTile + warp * kRowsPerWarp +
                             (st % Sh::STEPS) * Sh::SUB + sub;
-        float xv[RB][VEC], rv[RB][VEC], pv[RB][VEC], qv[RB][VEC], di[RB];
+        float rv[RB][VEC], qv[RB][VEC], di[RB];
         size_t o[RB];
 #pragma unroll
         for (int i = 0; i < RB; ++i) {
             const int row = rowBase + i * Sh::SUB;
             o[i] = vb + (size_t)row * KP + j0;
-            ldv<VEC>(P.x + o[i], xv[i]);
             ldv<VEC>(P.r + o[i], rv[i]);
-            ldv<VEC>(P.p + o[i], pv[i]);
             ldv<VEC>(P.q + o[i], qv[i]);
             di[i] = diag_inv(SR, P.diagSlot, P.npad, row, alpha);
         }
@@ -410,12 +413,10 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
         for (int i = 0; i < RB; ++i) {
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
-                xv[i][v] = fmaf(a[v], pv[i][v], xv[i][v]);
                 rv[i][v] = fmaf(-a[v], qv[i][v], rv[i][v]);
                 acc[0][v].add(rv[i][v], di[i] * rv[i][v]);
                 rsum[v] += rv[i][v];  // padding rows keep r = 0
             }
-            stv<VEC>(P.x + o[i], xv[i]);
             stv<VEC>(P.r + o[i], rv[i]);
         }
         if (P.coarse && (st % Sh::STEPS) + RB == Sh::STEPS) {
@@ -427,6 +428,13 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
     }
     double* const parts[1] = {P.partA};
     if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter, nb)) {
+        // the step length of this iteration, for the deferred x update
+        if (threadIdx.x < KP) {
+            const size_t s = (size_t)g * KP + threadIdx.x;
+            const double pq = P.pq[s];
+            P.alphaX[s] = (!P.conv[s] && pq != 0.0) ? (double)(float)(P.rz[s] / pq) : 0.0;
+        }
+        if (threadIdx.x == 0) P.pend[g] = 1;
         if (P.coarse) {
             if (threadIdx.x < KP)
                 P.rzFine[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
@@ -455,8 +463,9 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
     }
 }
 
-// p = D^-1 r + beta p on the right-hand sides still iterating; Neumann
-// harmonics also reduce sum(p) for the next SpMM.
+// x += alphaX p_old (the step of the update just made), p = D^-1 r + beta p
+// on the right-hand sides still iterating; Neumann harmonics also reduce
+// sum(p) for the next SpMM.
 template <int KP, int VEC, int RB>
 __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
     using Sh = Shape<KP, VEC>;
@@ -473,14 +482,16 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
     const size_t vb = (size_t)slice * P.npad * KP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
-    float be[VEC];
+    float be[VEC], ax[VEC];
     bool live[VEC];
 #pragma unroll
     for (int v = 0; v < VEC; ++v) {
         const size_t s = (size_t)g * KP + j0 + v;
         live[v] = P.first || !P.conv[s];
         be[v] = P.first ? 0.f : (float)P.beta[s];
+        ax[v] = P.first ? 0.f : (float)P.alphaX[s];
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.pend[g] = 0;  // x is brought up to date below
     DotAcc acc[1][VEC];
     const int tile0 = sg.tile0 + blockIdx.x * T;
     const int nsteps = (min(sg.tile0 + sg.nblk, tile0 + T) - tile0) * Sh::STEPS;
@@ -499,6 +510,11 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
                 for (int v = 0; v < VEC; ++v) pv[i][v] = 0.f;
             } else {
                 ldv<VEC>(P.p + o, pv[i]);
+                float xv[VEC];
+                ldv<VEC>(P.x + o, xv);
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) xv[v] = fmaf(ax[v], pv[i][v], xv[v]);
+                stv<VEC>(P.x + o, xv);
             }
             di[i] = diag_inv(SR, P.diagSlot, P.npad, row[i], alpha);
         }
@@ -522,6 +538,35 @@ __global__ void __launch_bounds__(kThreads) k_direction(CgProblem P) {
         if (threadIdx.x < KP)
             P.sumP[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
         if (threadIdx.x == 0) P.counter[g] = 0;
+    }
+}
+
+// x += alphaX p on the groups whose last x update is pending (they retired
+// in k_update, so k_direction skipped them); pend is cleared by the caller.
+template <int KP>
+__global__ void __launch_bounds__(kThreads) k_finalize_x(CgProblem P) {
+    constexpr int VEC = KP >= 32 ? 4 : 2;
+    using Sh = Shape<KP, VEC>;
+    const int g = blockIdx.y;
+    if (!P.pend[g]) return;
+    const int slice = g / P.M;
+    const Seg sg = segment(P, g - slice * P.M);
+    if ((int)blockIdx.x >= sg.nblk) return;
+    const size_t vb = (size_t)slice * P.npad * KP;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    float ax[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; ++v) ax[v] = (float)P.alphaX[(size_t)g * KP + j0 + v];
+    const int rowBase = (sg.tile0 + blockIdx.x) * kRowTile + warp * kRowsPerWarp + sub;
+    for (int st = 0; st < Sh::STEPS; ++st) {
+        const size_t o = vb + (size_t)(rowBase + st * Sh::SUB) * KP + j0;
+        float xv[VEC], pv[VEC];
+        ldv<VEC>(P.x + o, xv);
+        ldv<VEC>(P.p + o, pv);
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) xv[v] = fmaf(ax[v], pv[v], xv[v]);
+        stv<VEC>(P.x + o, xv);
     }
 }
 
@@ -728,6 +773,15 @@ struct InitL {
     }
 };
 template <int KP>
+struct FinalizeL {
+    static int run(const CgProblem& P, cudaStream_t s) {
+        k_finalize_x<KP><<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P);
+        MPF_LAUNCHED(1);
+        MPF_CUDA(cudaMemsetAsync(P.pend, 0, sizeof(int) * P.G, s));
+        return MPF_OK;
+    }
+};
+template <int KP>
 struct Res64L {
     static int run(const CgProblem& P, const double* S64, const double* R64, const double* x64,
                    const double* b64, const double* sumX64, double* partR, double* partB, double* rr,
@@ -813,6 +867,11 @@ int cg_launch_iteration(const CgProblem& P, cudaStream_t s) {
 int cg_iteration_launches(const CgProblem& P) { return P.solver >= 1 ? kBicgstabLaunches : P.coarse ? 4 : 3; }
 
 int cg_launch_kernel(const CgProblem& P, int which, cudaStream_t s) { return launch_one(P, which, s, true); }
+
+int cg_launch_finalize(const CgProblem& P, cudaStream_t s) {
+    if (P.solver != 0) return MPF_OK;
+    return dispatch_kp<FinalizeL>(P.KP, P, s);
+}
 
 int cg_launch_residual64(const CgProblem& P, const double* S64, const double* R64, const double* x64,
                          const double* b64, const double* sumX64, double* partR, double* partB, double* rr,

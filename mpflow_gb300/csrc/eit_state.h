@@ -45,8 +45,9 @@ struct mpf_eit {
     mpf::DevBuf<float> X, Rv, Pv, Qv;
     mpf::DevBuf<double> S64, R64, X64;
     mpf::DevBuf<double> partA, partB, partC, rz, pq, bz, betaW, rr, bb, Gm, sumP, sumX;
-    mpf::DevBuf<int> conv, active, iters;
+    mpf::DevBuf<int> conv, active, iters, pend;
     mpf::DevBuf<unsigned> counter;
+    mpf::DevBuf<double> alphaX;
     // BiCGSTAB vectors and scalars (grown on first use)
     int capFB = 0;
     mpf::DevBuf<float> Rhat, Zv, Tv;

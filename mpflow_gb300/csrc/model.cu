@@ -357,6 +357,9 @@ static int ensure_workspace(mpf_eit* m, int F, bool refine, bool jacobian) {
         MPF_TRY(m->sumP.alloc(sc));
         MPF_TRY(m->sumX.alloc(sc));
         MPF_TRY(m->conv.alloc(sc));
+        MPF_TRY(m->alphaX.alloc(sc));
+        MPF_TRY(m->pend.alloc(G));
+        MPF_CUDA(cudaMemset(m->pend.ptr, 0, G * sizeof(int)));
         MPF_TRY(m->active.alloc(G));
         MPF_TRY(m->iters.alloc(G));
         MPF_TRY(m->counter.alloc(G));
@@ -476,6 +479,8 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false
     P.active = m->active.ptr;
     P.iters = m->iters.ptr;
     P.counter = m->counter.ptr;
+    P.alphaX = m->alphaX.ptr;
+    P.pend = m->pend.ptr;
     P.tol2 = tol * tol;
     if (coarse) {
         P.coarse = 1;
@@ -986,8 +991,8 @@ int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, doub
     const double G = (double)F * m->Ca, n = m->n, K = m->K;
     for (int k = 0; k < 3; ++k) ms[k] = acc[k] / reps;
     bytes[0] = G * ((double)m->nnz * 12.0 + 2.0 * K * n * 4.0);   // S, R, column + p gather + q
-    bytes[1] = G * (6.0 * K * n * 4.0 + 2.0 * n * 4.0);            // x, r rw; p, q read; diagonal
-    bytes[2] = G * (3.0 * K * n * 4.0 + 2.0 * n * 4.0);            // r, p read; p write; diagonal
+    bytes[1] = G * (3.0 * K * n * 4.0 + 2.0 * n * 4.0);            // r rw, q read; diagonal
+    bytes[2] = G * (5.0 * K * n * 4.0 + 2.0 * n * 4.0);            // r, p, x read; p, x write; diagonal
     return MPF_OK;
 }
 

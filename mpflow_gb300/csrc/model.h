@@ -82,6 +82,12 @@ struct CgProblem {
     double* rzFine;       // [G][KP] r^T D^-1 r of the last update / init
     double* bzFine;       // [G][KP] b^T D^-1 b (init)
     int first;            // k_direction: p = M^-1 r (start of an iteration)
+    // deferred x update: k_update records alphaX = rz / pq of every
+    // right-hand side and pend[g] = 1; k_direction applies x += alphaX p
+    // while it still holds the old p and clears pend[g]; groups that retired
+    // in k_update (k_direction skips them) get it from cg_launch_finalize
+    double* alphaX;       // [G][KP]
+    int* pend;            // [G]
     // solver 1: BiCGSTAB (bicgstab_kernels.cu).  Reuses x, r; p holds
     // y = K^-1 p, q holds nu = A y; rz = rho, pq = alpha, beta, bz = |b|^2.
     int solver;
@@ -129,6 +135,8 @@ bool coarse_supported(int KP, int ncPad);
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s);
 int cg_iteration_launches(const CgProblem& P);
 int cg_launch_kernel(const CgProblem& P, int which /*0 spmm, 1 update, 2 direction*/, cudaStream_t s);
+// x += alphaX p on the groups whose last x update is still pending (end of a CG solve)
+int cg_launch_finalize(const CgProblem& P, cudaStream_t s);
 
 // cg_driver.cpp: host drivers shared by single models and batches of meshes.
 // Captured CUDA graphs of CG iteration chunks, keyed by the problems' bytes.

@@ -53,6 +53,12 @@ const char* mpf_version(void);
  * (kernels inside replayed CUDA graphs included).  No reference counterpart
  * (measurement support). */
 long long mpf_kernel_launches(void);
+/* Failure-path self-test of the bounded device waits (no reference
+ * counterpart): a kernel waits on an mbarrier that nothing arrives on, with
+ * the wait routine of the tensor-core kernels limited to timeout_us
+ * (1..2000000); it gives up, raises its abort flag and returns, so the call
+ * returns MPF_ETIMEOUT and the context stays usable.  Synchronises. */
+int mpf_selftest_bounded_wait(int32_t timeout_us, mpf_stream_t stream);
 
 /* ======================================================================== */
 /* Host-side mesh and FEM setup (no GPU needed)                             */

@@ -75,6 +75,7 @@ SIGNATURES = {
     "mpf_last_error": (ctypes.c_char_p, []),
     "mpf_version": (ctypes.c_char_p, []),
     "mpf_kernel_launches": (ctypes.c_longlong, []),
+    "mpf_selftest_bounded_wait": (_I, [_I, _P]),
     "mpf_data_rows": (ctypes.c_uint32, [ctypes.c_uint32]),
     "mpf_ring_mesh_counts": (_I, [_I, _P, _P]),
     "mpf_ring_mesh": (_I, [_I, _D, _P, _P]),

@@ -54,6 +54,7 @@ int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda,
 int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
 int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
+int wait_selftest(int timeoutUs, cudaStream_t s);
 int batch_create(mpf_eit* const* models, int count, mpf_batch** out);
 int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* V, const mpf_solve_opts* in,
                   mpf_solve_stats* stats, cudaStream_t s);
@@ -97,6 +98,10 @@ const char* mpf_last_error(void) { return mpf::last_error(); }
 const char* mpf_version(void) { return "mpflow_gb300 0.1.0 (sm_103a)"; }
 
 long long mpf_kernel_launches(void) { return mpf::launches(); }
+
+int mpf_selftest_bounded_wait(int32_t timeout_us, mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::wait_selftest(timeout_us, (cudaStream_t)stream); })
+}
 
 uint32_t mpf_data_rows(uint32_t rows) { return mpf::data_rows(rows); }
 

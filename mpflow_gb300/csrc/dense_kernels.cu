@@ -355,6 +355,19 @@ int gram_splits(int tiles, int kblocks) {
     return std::max(1, std::min(s, kblocks));
 }
 
+// Failure-path self-test: one thread waits on an mbarrier that nothing
+// arrives on, through the same bounded wait as the tensor-core kernels; the
+// wait gives up after limitNs and reports through *flag.
+__global__ void k_wait_selftest(int* flag, unsigned long long limitNs) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int localAbort;
+    if (threadIdx.x != 0) return;
+    localAbort = 0;
+    mbar_init(smem_u32(&bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (!mbar_wait(smem_u32(&bar), 0, &localAbort, limitNs)) atomicExch(flag, 1);
+}
+
 int* abort_flag_device() {
     static int* flag = nullptr;
     static std::once_flag once;
@@ -382,6 +395,20 @@ int make_bf16_map(CUtensorMap* map, const __nv_bfloat16* base, int totalRows, in
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     MPF_CHECK(r == CUDA_SUCCESS, MPF_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return MPF_OK;
+}
+
+int wait_selftest(int timeoutUs, cudaStream_t s) {
+    MPF_CHECK(timeoutUs >= 1 && timeoutUs <= 2000000, MPF_EINVAL, "mpf_selftest_bounded_wait: timeout %d us",
+              timeoutUs);
+    DevBuf<int> flag;
+    MPF_TRY(flag.alloc(1));
+    MPF_CUDA(cudaMemsetAsync(flag.ptr, 0, sizeof(int), s));
+    k_wait_selftest<<<1, 32, 0, s>>>(flag.ptr, (unsigned long long)timeoutUs * 1000ull);
+    MPF_LAUNCHED(1);
+    int h = 0;
+    MPF_CUDA(cudaMemcpyAsync(&h, flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    return h ? fail(MPF_ETIMEOUT, "bounded wait ran out after %d us (self-test)", timeoutUs) : MPF_OK;
 }
 
 size_t dense_gram_work_floats(int batch, int rows, int cols) {

@@ -38,13 +38,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up after ~2 s, raising the abort flag instead of hanging.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abortFlag) {
+// Bounded wait: gives up after limitNs (default 2 s), raising the abort flag
+// instead of hanging.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abortFlag,
+                                          uint64_t limitNs = 2000000000ull) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_timer();
     while (!mbar_try_wait(bar, parity)) {
         if (*abortFlag) return false;
-        if (global_timer() - t0 > 2000000000ull) {
+        if (global_timer() - t0 > limitNs) {
             *abortFlag = 1;
             return false;
         }

@@ -54,3 +54,9 @@ def test_invalid_model_arguments_are_rejected():
     assert L.mpf_eit_create(None, ctypes.byref(h)) == 1
     assert L.mpf_eit_forward(None, 1, None, None, None, None, None, None) == 1
     assert b"model == nullptr" in L.mpf_last_error()
+
+
+def test_selftest_rejects_bad_timeout_without_gpu():
+    L = mpflow_gb300.lib()
+    assert L.mpf_selftest_bounded_wait(0, None) == 1
+    assert L.mpf_selftest_bounded_wait(3000000, None) == 1

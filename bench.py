@@ -546,7 +546,7 @@ def uneven_config(a, rings, elec):
                          "inclusion r U(0.1,0.3), contrast log-U[0.1,10], linear conductivity"),
             "nodes_total": int(sum(1 + 3 * r * (r + 1) for r in rings)),
             "meshes_16_electrodes": int((elec == 16).sum()), "meshes_32_electrodes": int((elec == 32).sum()),
-            "frames_per_mesh": a.mesh_frames, "cg_tol": a.tol, "preconditioner": "jacobi",
+            "frames_per_mesh": a.mesh_frames, "cg_tol": a.tol, "preconditioner": a.preconditioner,
             "l2": "CG working set (GBs) far above L2 (129 MB)"}
 
 
@@ -563,7 +563,7 @@ def run_uneven(a):
     models = [mp.EIT(m, src, 1.0, components=4, height=4.0, device=local) for m, _, _, src in meshes]
     batch = mp.EITBatch(models)
     gam = [torch.tensor(g, device=dev) for g in frames]
-    opts = mp.SolveOptions(tol=a.tol)
+    opts = mp.SolveOptions(tol=a.tol, preconditioner=a.preconditioner)
     lib = mp.lib()
     stream = torch.cuda.current_stream()
     nsteps = a.warmup + a.steps

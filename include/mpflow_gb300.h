@@ -355,10 +355,11 @@ int mpf_batch_destroy(mpf_batch_t batch);
 /* EIT::solve for `frames` frames of every model.  gamma[i]: device,
  * frames x n_elements(i); voltages[i]: device, frames x Mm(i) x Md(i), each
  * frame column-major (as mpf_eit_forward).  Both are host arrays of `count`
- * device pointers.  Cold start, Jacobi preconditioner, FP32, CG or BiCGSTAB
- * (opts->solver; MPF_ENOTSUP for refine_tol > 0, warm_start != 0 or
- * preconditioner != 0); CG launch shapes are autotuned per width class at
- * the first call with a frame count.
+ * device pointers.  Cold start, FP32, CG (Jacobi or, with
+ * opts->preconditioner = 1, the two-level preconditioner on every mesh's own
+ * coarse space) or BiCGSTAB (Jacobi); MPF_ENOTSUP for refine_tol > 0 or
+ * warm_start != 0.  CG launch shapes are autotuned per width class at the
+ * first call with a frame count.
  * Synchronises `stream`.  stats->iterations: slowest group. */
 int mpf_batch_forward(mpf_batch_t batch, int32_t frames, const float* const* gamma, float* const* voltages,
                       const mpf_solve_opts* opts, mpf_solve_stats* stats, mpf_stream_t stream);
@@ -371,7 +372,8 @@ int mpf_batch_iterations(mpf_batch_t batch, int32_t* iterations, int32_t cap, in
  * iterations, CUDA events on its stream) and the algorithmic bytes its
  * iterations moved: per iteration and group nnz * 12 + 10 * K * n * 4 +
  * 4 * n * 4 for CG (SpMM, update and direction passes; K unique excitations,
- * n nodes of the group's mesh), 2 * nnz * 12 + 21 * K * n * 4 + 6 * n * 4 for
+ * n nodes of the group's mesh; two-level: + ncPad^2 * 4 + 3 * ncPad * K * 4
+ * for the coarse product), 2 * nnz * 12 + 21 * K * n * 4 + 6 * n * 4 for
  * BiCGSTAB.  No reference counterpart (measurement support). */
 int mpf_batch_cg_stats(mpf_batch_t batch, double* cg_ms, double* cg_bytes);
 

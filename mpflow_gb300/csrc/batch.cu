@@ -13,6 +13,11 @@
 // its own rows, CG scalars, convergence mask and block reductions.  All width
 // classes are recorded in one CUDA graph per check interval.
 //
+// The two-level preconditioner (preconditioner = 1) works per mesh as well:
+// every group gets the coarse space of its own mesh (aggregates of 64
+// Morton-ordered rows), padded to the largest coarse size of its width class
+// with identity blocks, so the coarse setup and product run as one batch.
+//
 // The models stay usable on their own: the batch reads their static device
 // arrays (assembly lists, right-hand sides, measurement tables) and keeps its
 // own workspace, so every model must outlive the batch.
@@ -45,6 +50,13 @@ struct BatchClass {
     int capFB = 0;
     DevBuf<float> Rhat, Zv, Tv;
     DevBuf<double> omegaW, rr2W;
+    // two-level preconditioner: stacked coarse plan (static) and workspace
+    int coarseOK = 0, ncPad = 0, cNnz = 0, capFC = 0;
+    DevBuf<int32_t> cPairI, cPairJ, cPairPtr, cSlots, cMeshPairPtr, cMeshNc;
+    DevBuf<float> cAggSize;
+    DevBuf<double> Ac64, rzFine, bzFine;
+    DevBuf<float> Lc, LinvD, Binv, rcV, rcB, ycV;
+    DevBuf<int> infoC;
 };
 
 }  // namespace mpf
@@ -71,6 +83,77 @@ struct mpf_batch {
 };
 
 namespace mpf {
+
+// Stacked coarse plan of a width class: every member's (I, J) pairs with
+// its slot indices moved to the stacked layout, per-mesh pair ranges,
+// aggregate counts and sizes.  Built from the same rule as the model's own
+// plan (model.cu): aggregates of kAgg consecutive rows, padding slots out.
+static int class_coarse_plan(mpf_eit* const* models, BatchClass& cl) {
+    const int Mc = (int)cl.members.size();
+    cl.ncPad = 0;
+    for (int j = 0; j < Mc; ++j) cl.ncPad = std::max(cl.ncPad, models[cl.members[j]]->ncPad);
+    cl.coarseOK = coarse_supported(cl.KP, cl.ncPad) ? 1 : 0;
+    if (!cl.coarseOK) return MPF_OK;
+    std::vector<int32_t> pI, pJ, pPtr{0}, slots, meshPtr{0}, meshNc(Mc);
+    std::vector<float> aggSize((size_t)Mc * cl.ncPad, 0.f);
+    for (int j = 0; j < Mc; ++j) {
+        const mpf_eit* m = models[cl.members[j]];
+        const int row0 = cl.tile0[j] * kRowTile, n = m->n, P = m->npad;
+        meshNc[j] = m->nc;
+        for (int I = 0; I < m->nc; ++I) aggSize[(size_t)j * cl.ncPad + I] = (float)std::min(kAgg, n - I * kAgg);
+        std::vector<std::vector<std::pair<int32_t, int32_t>>> byI(m->nc);
+        for (int r = 0; r < n; ++r)
+            for (int k = 0; k < m->W; ++k) {
+                const int32_t c = m->fs.cols[(size_t)k * P + r];
+                if (c == r && k != m->fs.diagSlot[r]) continue;
+                byI[r / kAgg].push_back({c / kAgg, (int32_t)((size_t)k * cl.npad + row0 + r)});
+            }
+        for (int I = 0; I < m->nc; ++I) {
+            auto& v = byI[I];
+            std::sort(v.begin(), v.end());
+            for (size_t t = 0; t < v.size(); ++t) {
+                if (t == 0 || v[t].first != v[t - 1].first) {
+                    if (t > 0) pPtr.push_back((int32_t)slots.size());
+                    pI.push_back(I);
+                    pJ.push_back(v[t].first);
+                }
+                slots.push_back(v[t].second);
+            }
+            if (!v.empty()) pPtr.push_back((int32_t)slots.size());
+        }
+        meshPtr.push_back((int32_t)pI.size());
+    }
+    cl.cNnz = (int)pI.size();
+    MPF_TRY(cl.cPairI.upload(pI));
+    MPF_TRY(cl.cPairJ.upload(pJ));
+    MPF_TRY(cl.cPairPtr.upload(pPtr));
+    MPF_TRY(cl.cSlots.upload(slots));
+    MPF_TRY(cl.cMeshPairPtr.upload(meshPtr));
+    MPF_TRY(cl.cMeshNc.upload(meshNc));
+    MPF_TRY(cl.cAggSize.upload(aggSize));
+    return MPF_OK;
+}
+
+static int class_coarse_workspace(mpf_batch* b, BatchClass& cl, int F) {
+    if (F <= cl.capFC) return MPF_OK;
+    const size_t G = (size_t)F * b->Ca * cl.members.size(), nc2 = (size_t)cl.ncPad * cl.ncPad;
+    const size_t cv = G * cl.ncPad * cl.KP;
+    MPF_TRY(cl.Ac64.alloc(G * nc2));
+    MPF_TRY(cl.Lc.alloc(G * nc2));
+    MPF_TRY(cl.LinvD.alloc(G * (cl.ncPad / 32) * 1024));
+    MPF_TRY(cl.Binv.alloc(G * nc2));
+    MPF_TRY(cl.rcV.alloc(cv));
+    MPF_TRY(cl.rcB.alloc(cv));
+    MPF_TRY(cl.ycV.alloc(cv));
+    MPF_CUDA(cudaMemset(cl.rcV.ptr, 0, cv * sizeof(float)));
+    MPF_CUDA(cudaMemset(cl.rcB.ptr, 0, cv * sizeof(float)));
+    MPF_CUDA(cudaMemset(cl.ycV.ptr, 0, cv * sizeof(float)));
+    MPF_TRY(cl.rzFine.alloc(G * cl.KP));
+    MPF_TRY(cl.bzFine.alloc(G * cl.KP));
+    MPF_TRY(cl.infoC.alloc(G));
+    cl.capFC = F;
+    return MPF_OK;
+}
 
 int batch_create(mpf_eit* const* models, int count, mpf_batch** out) {
     MPF_CHECK(models && out && count >= 1, MPF_EINVAL, "mpf_batch_create: bad arguments");
@@ -142,6 +225,7 @@ int batch_create(mpf_eit* const* models, int count, mpf_batch** out) {
         MPF_TRY(cl->cols.upload(cols));
         MPF_TRY(cl->diagSlot.upload(diag));
         MPF_TRY(cl->seg.upload(seg));
+        MPF_TRY(class_coarse_plan(models, *cl));
         b->classes.push_back(std::move(cl));
     }
     *out = b.release();
@@ -206,7 +290,7 @@ static int class_bicgstab(mpf_batch* b, BatchClass& cl, int F) {
 }
 
 static CgProblem class_problem(mpf_batch* b, BatchClass& cl, int F, double tol, const std::array<int, 3>* shapes,
-                               int solver = 0) {
+                               int solver = 0, bool coarse = false) {
     CgProblem P{};
     P.npad = cl.npad;
     P.n = cl.npad;
@@ -243,6 +327,16 @@ static CgProblem class_problem(mpf_batch* b, BatchClass& cl, int F, double tol, 
     P.alphaX = cl.alphaX.ptr;
     P.pend = cl.pend.ptr;
     P.tol2 = tol * tol;
+    if (coarse) {
+        P.coarse = 1;
+        P.ncPad = cl.ncPad;
+        P.rc = cl.rcV.ptr;
+        P.rcB = cl.rcB.ptr;
+        P.yc = cl.ycV.ptr;
+        P.Binv = cl.Binv.ptr;
+        P.rzFine = cl.rzFine.ptr;
+        P.bzFine = cl.bzFine.ptr;
+    }
     if (solver == 1) {
         P.solver = 1;
         P.rhat = cl.Rhat.ptr;
@@ -267,9 +361,10 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
         MPF_CHECK(gamma[i] && V[i], MPF_EINVAL, "mpf_batch_forward: gamma[%d] or voltages[%d] == nullptr", i, i);
     mpf_solve_opts o{1e-6, 0, 0.0, 6, 0, 16, 0};
     if (in) o = *in;
-    MPF_CHECK(o.refine_tol <= 0.0 && o.warm_start == 0 && o.preconditioner == 0, MPF_ENOTSUP,
-              "mpf_batch_forward: batches solve cold with the Jacobi preconditioner and no FP64 refinement");
+    MPF_CHECK(o.refine_tol <= 0.0 && o.warm_start == 0, MPF_ENOTSUP,
+              "mpf_batch_forward: batches solve cold without FP64 refinement");
     const int solver = o.solver == 1 ? 1 : 0;
+    const bool coarse = o.preconditioner == 1 && solver == 0;
     if (o.tol <= 0.0) o.tol = 1e-6;
     if (o.max_iter <= 0) o.max_iter = 10 * b->maxN;
     if (o.check_every <= 0) o.check_every = 16;
@@ -303,9 +398,18 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
     }
     std::vector<CgProblem> Ps;
     for (int c = 0; c < nC; ++c) {
+        BatchClass& cl = *b->classes[c];
         auto it = b->variants.find(F);
-        Ps.push_back(class_problem(b, *b->classes[c], F, o.tol, it != b->variants.end() ? &it->second[c] : nullptr,
-                                   solver));
+        const bool cc = coarse && cl.coarseOK;
+        Ps.push_back(class_problem(b, cl, F, o.tol, it != b->variants.end() ? &it->second[c] : nullptr, solver, cc));
+        if (cc) {
+            MPF_TRY(class_coarse_workspace(b, cl, F));
+            Ps.back() = class_problem(b, cl, F, o.tol, it != b->variants.end() ? &it->second[c] : nullptr, solver, cc);
+            CoarsePlan cp{0, cl.ncPad, cl.cNnz, cl.cPairI.ptr, cl.cPairJ.ptr, cl.cPairPtr.ptr, cl.cSlots.ptr,
+                          cl.cAggSize.ptr, cl.cMeshPairPtr.ptr, cl.cMeshNc.ptr};
+            MPF_TRY(coarse_launch_setup(Ps.back(), cp, cl.Ac64.ptr, cl.infoC.ptr, s, cl.Lc.ptr, cl.LinvD.ptr,
+                                        cl.Binv.ptr));
+        }
     }
     cudaEvent_t e0, e1;
     MPF_CUDA(cudaEventCreate(&e0));
@@ -326,6 +430,14 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st != MPF_OK) return st;
+    for (int c = 0; c < nC; ++c) {
+        if (!Ps[c].coarse) continue;
+        std::vector<int> info(Ps[c].G);
+        MPF_CUDA(cudaMemcpy(info.data(), b->classes[c]->infoC.ptr, sizeof(int) * info.size(), cudaMemcpyDeviceToHost));
+        for (int g = 0; g < Ps[c].G; ++g)
+            MPF_CHECK(info[g] == 0, MPF_EBREAKDOWN, "two-level preconditioner: coarse Cholesky failed at pivot %d "
+                      "(group %d of width class %d)", info[g], g, Ps[c].KP);
+    }
     // per-group iterations in [mesh][frame][harmonic] order and the
     // algorithmic bytes the iterations moved (CG, per iteration and group:
     // the SpMM's nnz*12 + 2*K*n*4, the update's 3*K*n*4 + 2*n*4 and the
@@ -342,9 +454,12 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
                 const int it = iters[off + (size_t)sl * Mc + j];
                 b->iters[(size_t)cl.members[j] * F * b->Ca + sl] = it;
                 const double n = m->n, K = m->K;
-                // BiCGSTAB: two SpMVs, 21 vector passes, three diagonal reads
+                // BiCGSTAB: two SpMVs, 21 vector passes, three diagonal reads;
+                // two-level CG: plus the coarse inverse and coarse vectors
+                const double coarseBytes =
+                    Ps[c].coarse ? (double)cl.ncPad * cl.ncPad * 4.0 + 3.0 * cl.ncPad * K * 4.0 : 0.0;
                 bytes += solver == 1 ? it * (2.0 * m->nnz * 12.0 + 21.0 * K * n * 4.0 + 6.0 * n * 4.0)
-                                     : it * ((double)m->nnz * 12.0 + 10.0 * K * n * 4.0 + 4.0 * n * 4.0);
+                                     : it * ((double)m->nnz * 12.0 + 10.0 * K * n * 4.0 + 4.0 * n * 4.0 + coarseBytes);
             }
         off += (size_t)F * b->Ca * Mc;
     }

@@ -78,6 +78,9 @@ struct Seg {
     int tile0, nblk, end;
     float dcScale;
 };
+// aggregates of kAgg rows of a segment's mesh (the coarse space's size)
+__device__ __forceinline__ int seg_aggregates(const Seg& sg) { return (sg.end - sg.tile0 * kRowTile + kAgg - 1) / kAgg; }
+
 __device__ __forceinline__ Seg segment(const CgProblem& P, int mesh) {
     if (P.seg) {
         const int4 d = __ldg(&P.seg[mesh]);

@@ -134,8 +134,8 @@ __global__ void __launch_bounds__(kThreads) k_init(CgProblem P, int zeroGuess) {
     if (P.coarse) {
         __shared__ float red[kWarps * 32 * VEC];
         const size_t cb = (size_t)g * P.ncPad * KP;
-        restrict_tile<KP, VEC>(rsum, blockIdx.x, P.nc, P.rc + cb, red);
-        restrict_tile<KP, VEC>(bsum, blockIdx.x, P.nc, P.rcB + cb, red);
+        restrict_tile<KP, VEC>(rsum, blockIdx.x, seg_aggregates(sg), P.rc + cb, red);
+        restrict_tile<KP, VEC>(bsum, blockIdx.x, seg_aggregates(sg), P.rcB + cb, red);
     }
     double* const parts[3] = {P.partA, P.partB, P.partC};
     const int nb = sg.nblk;
@@ -420,8 +420,8 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
             stv<VEC>(P.r + o[i], rv[i]);
         }
         if (P.coarse && (st % Sh::STEPS) + RB == Sh::STEPS) {
-            restrict_tile<KP, VEC>(rsum, tile0 - sg.tile0 + st / Sh::STEPS, P.nc, P.rc + (size_t)g * P.ncPad * KP,
-                                   red);
+            restrict_tile<KP, VEC>(rsum, tile0 - sg.tile0 + st / Sh::STEPS, seg_aggregates(sg),
+                                   P.rc + (size_t)g * P.ncPad * KP, red);
 #pragma unroll
             for (int v = 0; v < VEC; ++v) rsum[v] = 0.f;
         }

@@ -31,11 +31,14 @@ constexpr int kCT = 256;  // threads of k_coarse
 // in aggregate J of (S + alpha R), FP64, fixed order.
 __global__ void k_coarse_assemble(CgProblem P, CoarsePlan cp, double* __restrict__ Ac) {
     const int g = blockIdx.y;
-    const int f = g / P.Ca, ci = g % P.Ca;
+    const int slice = g / P.M, mesh = g - slice * P.M;
+    const int f = slice / P.Ca, ci = slice % P.Ca;
     const double alpha = (double)P.alpha[ci];
     const float2* SR = P.SR + (size_t)f * P.W * P.npad;
     double* A = Ac + (size_t)g * cp.ncPad * cp.ncPad;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cp.nnz; t += gridDim.x * blockDim.x) {
+    const int t0 = cp.meshPairPtr ? cp.meshPairPtr[mesh] : 0;
+    const int t1 = cp.meshPairPtr ? cp.meshPairPtr[mesh + 1] : cp.nnz;
+    for (int t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
         double s = 0.0;
         for (int k = cp.pairPtr[t]; k < cp.pairPtr[t + 1]; ++k) {
             const float2 e = __ldg(&SR[cp.slots[k]]);
@@ -49,13 +52,17 @@ __global__ void k_coarse_assemble(CgProblem P, CoarsePlan cp, double* __restrict
 // aggregates get an identity block.
 __global__ void k_coarse_fixup(CgProblem P, CoarsePlan cp, double* __restrict__ Ac) {
     const int g = blockIdx.y;
-    const bool dc = P.dcFree[g % P.Ca] != 0;
+    const int slice = g / P.M, mesh = g - slice * P.M;
+    const bool dc = P.dcFree[slice % P.Ca] != 0;
+    const int nc = cp.meshNc ? cp.meshNc[mesh] : cp.nc;
+    const float* aggSize = cp.meshNc ? cp.aggSize + (size_t)mesh * cp.ncPad : cp.aggSize;
+    const double dcScale = P.seg ? (double)__int_as_float(P.seg[mesh].w) : (double)P.dcScale;
     double* A = Ac + (size_t)g * cp.ncPad * cp.ncPad;
     const size_t total = (size_t)cp.ncPad * cp.ncPad;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
         const int I = (int)(t / cp.ncPad), J = (int)(t % cp.ncPad);
-        if (I < cp.nc && J < cp.nc) {
-            if (dc) A[t] += (double)P.dcScale * (double)cp.aggSize[I] * (double)cp.aggSize[J];
+        if (I < nc && J < nc) {
+            if (dc) A[t] += dcScale * (double)aggSize[I] * (double)aggSize[J];
         } else if (I == J) {
             A[t] = 1.0;
         }
@@ -366,7 +373,7 @@ int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, 
                         float* Lc, float* LinvD, float* Binv) {
     const size_t per = (size_t)cp.ncPad * cp.ncPad;
     MPF_CUDA(cudaMemsetAsync(Ac64, 0, sizeof(double) * per * P.G, s));
-    k_coarse_assemble<<<dim3((cp.nnz + 255) / 256, P.G), 256, 0, s>>>(P, cp, Ac64);
+    k_coarse_assemble<<<dim3(std::min((cp.nnz + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64);
     k_coarse_fixup<<<dim3((int)std::min<size_t>((per + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64);
     MPF_LAUNCHED(2);
     MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s));

@@ -74,7 +74,7 @@ struct CgProblem {
     // two-level preconditioner M^-1 = D^-1 + P (P^T A P)^-1 P^T over aggregates
     // of kAgg consecutive rows (coarse == 0: Jacobi only)
     int coarse;
-    int nc, ncPad;        // aggregates, padded to a multiple of 32
+    int nc, ncPad;        // aggregates (per mesh: from its segment), padded to a multiple of 64
     float* rc;            // [G][ncPad][KP] P^T r (restriction, written by k_update / k_init)
     float* rcB;           // [G][ncPad][KP] P^T b (k_init, for b^T M^-1 b)
     float* yc;            // [G][ncPad][KP] (P^T A P)^-1 P^T r
@@ -124,7 +124,11 @@ struct CoarsePlan {
     const int32_t* pairJ;            // [nnz]
     const int32_t* pairPtr;          // [nnz + 1] into slots
     const int32_t* slots;            // slot indices k * npad + row
-    const float* aggSize;            // [nc] real rows per aggregate
+    const float* aggSize;            // [nc] real rows per aggregate ([M][ncPad] for stacked meshes)
+    // stacked meshes (P.seg != nullptr): the pairs of mesh j are
+    // [meshPairPtr[j], meshPairPtr[j + 1]), its aggregate count meshNc[j]
+    const int32_t* meshPairPtr;
+    const int32_t* meshNc;
 };
 // Lc [G][ncPad][ncPad], LinvD [G][ncPad/32][1024]: FP32 factor scratch; Binv: the inverse (P.Binv)
 int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,

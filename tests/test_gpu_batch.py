@@ -70,6 +70,34 @@ def test_batch_matches_single_models_and_oracle():
     assert ms > 0 and by > 0
 
 
+def test_batch_two_level_matches_single_models():
+    """Every mesh of the batch gets its own coarse space (padded to the
+    largest of its width class): same voltages, fewer iterations."""
+    import oracle
+    import torch
+    import mpflow_gb300 as mp
+    setups = _setups()
+    gammas = [torch.tensor(_frames(mesh, i), dtype=torch.float32, device="cuda") for i, (mesh, _, _) in
+              enumerate(setups)]
+    batch = mp.EITBatch([m for _, _, m in setups])
+    jac = mp.SolveOptions(tol=1e-7)
+    two = mp.SolveOptions(tol=1e-7, preconditioner="two-level")
+    Vj = batch.solve(gammas, jac)
+    it_j = batch.iterations(FRAMES)
+    Vt = batch.solve(gammas, two)
+    it_t = batch.iterations(FRAMES)
+    assert batch.last_stats.not_converged == 0
+    for i, (mesh, orc, model) in enumerate(setups):
+        Vs = model.solve(gammas[i], two)
+        assert rel_err(Vt[i].cpu().numpy(), Vs.cpu().numpy()) < 2e-5, i
+        assert rel_err(Vt[i].cpu().numpy(), Vj[i].cpu().numpy()) < 2e-5, i
+    mesh, orc, _ = setups[3]
+    Vo, _, _ = oracle.eit_forward(orc, _frames(mesh, 3)[0], tol=1e-13, want_jacobian=False)
+    assert rel_err(Vt[3][0].cpu().numpy(), Vo) < 1e-4
+    # the largest mesh needs fewer iterations with its coarse space
+    assert it_t[3].max() < it_j[3].max()
+
+
 @pytest.mark.parametrize("shapes", [[1, 13, 22], [28, 4, 8], [35, 31, 10]])
 def test_batch_forced_launch_shapes(shapes):
     import torch

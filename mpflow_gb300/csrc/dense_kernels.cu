@@ -183,6 +183,56 @@ __global__ void k_gram_reduce(int rows, int tiles, int nt, int splits, const flo
     }
 }
 
+// A64[b] = J J^T + shift I in FP64 from the FP32 J (rows x ld row-major per
+// frame) on the FP64 pipe: the accurate Gram for frames whose split-BF16
+// J J^T + mu I is not positive definite (mu below the ~1e-5 relative error of
+// the BF16 split and FP32 accumulation).  64 x 64 output tiles of the upper
+// triangle, mirrored; 256 threads with 4 x 4 outputs each; K in chunks of 32
+// staged in shared memory as FP64.
+__global__ void __launch_bounds__(256) k_gram_f64(int rows, int cols, const float* __restrict__ J, int ld,
+                                                  double shift, double* __restrict__ A64,
+                                                  const int* __restrict__ frameMask) {
+    const int b = blockIdx.z, ti = blockIdx.y, tj = blockIdx.x;
+    if (frameMask && !frameMask[b]) return;
+    if (tj < ti) return;
+    __shared__ double As[32][65], Bs[32][65];
+    const float* Jb = J + (size_t)b * rows * ld;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < cols; k0 += 32) {
+        for (int t = threadIdx.x; t < 64 * 32; t += 256) {
+            const int r = t / 32, k = t % 32;
+            As[k][r] = (double)Jb[(size_t)(ti * 64 + r) * ld + k0 + k];
+            Bs[k][r] = (double)Jb[(size_t)(tj * 64 + r) * ld + k0 + k];
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+            double a[4], c[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                a[i] = As[k][ty + 16 * i];
+                c[i] = Bs[k][tx + 16 * i];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], c[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    double* A = A64 + (size_t)b * rows * rows;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = ti * 64 + ty + 16 * i, c = tj * 64 + tx + 16 * j;
+            const double v = acc[i][j] + (r == c ? shift : 0.0);
+            A[(size_t)r * rows + c] = v;
+            A[(size_t)c * rows + r] = v;
+        }
+}
+
 __global__ void k_split_bf16(int batch, int rows, int cols, const float* __restrict__ A, int lda,
                              __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
     const size_t total = (size_t)batch * rows * lda;
@@ -451,6 +501,15 @@ int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi,
                          double shift, double* A64, float* work, size_t workFloats, cudaStream_t s,
                          const int* frameMask) {
     return gram_run(batch, rows, cols, hi, lo, ld, nullptr, A64, shift, work, workFloats, s, nullptr, frameMask);
+}
+
+int dense_gram_f64_exact(int batch, int rows, int cols, const float* J, int ld, double shift, double* A64,
+                         const int* frameMask, cudaStream_t s) {
+    MPF_CHECK(rows % 64 == 0 && cols % 32 == 0 && ld >= cols, MPF_EINVAL,
+              "FP64 Gram: rows %% 64 and cols %% 32 must be 0 (rows=%d cols=%d)", rows, cols);
+    k_gram_f64<<<dim3(rows / 64, rows / 64, batch), 256, 0, s>>>(rows, cols, J, ld, shift, A64, frameMask);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
 }
 
 int dense_gram_check_abort(bool* aborted) {

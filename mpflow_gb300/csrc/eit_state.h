@@ -61,7 +61,7 @@ struct mpf_eit {
     mpf::DevBuf<float> V, J, gramWork;
     mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
     mpf::DevBuf<double> A64, y, res;
-    mpf::DevBuf<int> info, frameMask;
+    mpf::DevBuf<int> info, frameMask, redoMask;
     long long nnz = 0;                // used ELL slots (matrix nonzeros)
     std::vector<int> activeHost, itersHost;
     int* pinnedActive = nullptr;
@@ -95,7 +95,7 @@ struct mpf_eit {
     // regularised inverse (mpf_inverse_solve) workspace
     mpf::DevBuf<float> invJ, invWork;
     mpf::DevBuf<__nv_bfloat16> invHi, invLo;
-    mpf::DevBuf<double> invA, invY, invB;
+    mpf::DevBuf<double> invA, invY, invB, invYs, invR, invU;
     mpf::DevBuf<int> invInfo;
     mpf::DevBuf<int32_t> lapRow, lapCol;
     mpf::DevBuf<double> lapVal;

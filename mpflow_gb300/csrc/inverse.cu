@@ -8,7 +8,10 @@
 //  * NOSER and Laplacian, which have no dual form, build J^T J on the
 //    tensor cores (split-BF16 Gram of J^T) and factor the E x E system in
 //    FP64 (small meshes: E <= 6144 after padding to 128).
-// Both end in an exact FP64 Cholesky solve.
+// Both end in an exact FP64 Cholesky solve.  The dual form refines its
+// solution against the FP64 normal equations applied matrix-free with the
+// FP32 J (the split-BF16 Gram carries ~1e-5 relative error, which 1/mu
+// amplifies); when that refinement stalls, the Gram is rebuilt in FP64.
 #include <cmath>
 #include <unordered_map>
 
@@ -44,6 +47,33 @@ __global__ void k_jt_times(int rowsJ, int E, int ld, const float* __restrict__ J
         for (int r = 0; r < rowsJ; ++r) s += (double)J[(size_t)r * ld + e] * w[(size_t)p * rowsJ + r];
     if (outF && e < E) outF[(size_t)p * E + e] = (float)s;
     if (outD) outD[(size_t)p * ld + e] = s;
+}
+
+// res[p][r] = y[p][r] - sum_e J[r][e] u[p][e] - mu w[p][r] in FP64; one block
+// per (row, image), fixed-order tree reduction
+__global__ void __launch_bounds__(256) k_normal_residual(int rowsJ, int ld, const float* __restrict__ J,
+                                                         const double* __restrict__ u, const double* __restrict__ y,
+                                                         const double* __restrict__ w, double mu,
+                                                         double* __restrict__ res) {
+    const int r = blockIdx.x, p = blockIdx.y;
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int e = threadIdx.x; e < ld; e += 256) s += (double)J[(size_t)r * ld + e] * u[(size_t)p * ld + e];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const size_t i = (size_t)p * rowsJ + r;
+        res[i] = y[i] - red[0] - mu * w[i];
+    }
+}
+
+__global__ void k_axpy64(size_t n, const double* __restrict__ d, double* __restrict__ w) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        w[i] += d[i];
 }
 
 // regulariser on the FP64 system of padded order n (padding: identity)
@@ -116,6 +146,70 @@ int laplacian_coo(mpf_eit* m) {
 
 }  // namespace
 
+static bool pivot_failed(mpf_eit* m, cudaStream_t s);
+
+// w = (J J^T + mu I)^-1 y for the images in invY (overwritten by w): the
+// Cholesky solve with the factor in invA, then iterative refinement with the
+// residual y - J (J^T w) - mu w in FP64 from the FP32 J in invJ.  A step
+// that shrinks the residual by less than half switches to the FP64 Gram
+// (once).  Stops at a relative residual of 1e-13 or after 8 steps.
+static int refine_dual(mpf_eit* m, int rowsJ, int E, int ld, int images, double mu, bool exact, cudaStream_t s) {
+    const size_t ny = (size_t)images * rowsJ;
+    MPF_TRY(m->invYs.alloc(ny));
+    MPF_TRY(m->invR.alloc(ny));
+    MPF_TRY(m->invU.alloc((size_t)images * ld));
+    MPF_CUDA(cudaMemcpyAsync(m->invYs.ptr, m->invY.ptr, sizeof(double) * ny, cudaMemcpyDeviceToDevice, s));
+    MPF_TRY(dense_cholesky_solve_f64(1, rowsJ, m->invA.ptr, m->invY.ptr, images, s));
+    std::vector<double> yh(ny), rh(ny);
+    MPF_CUDA(cudaMemcpyAsync(yh.data(), m->invYs.ptr, sizeof(double) * ny, cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> ynorm(images, 0.0);
+    for (int p = 0; p < images; ++p)
+        for (int r = 0; r < rowsJ; ++r) ynorm[p] += yh[(size_t)p * rowsJ + r] * yh[(size_t)p * rowsJ + r];
+    double prev = 1e300;
+    for (int step = 0; step < 8; ++step) {
+        k_jt_times<<<dim3((ld + 255) / 256, images), 256, 0, s>>>(rowsJ, E, ld, m->invJ.ptr, m->invY.ptr, nullptr,
+                                                                  m->invU.ptr);
+        k_normal_residual<<<dim3(rowsJ, images), 256, 0, s>>>(rowsJ, ld, m->invJ.ptr, m->invU.ptr, m->invYs.ptr,
+                                                               m->invY.ptr, mu, m->invR.ptr);
+        MPF_LAUNCHED(2);
+        MPF_CUDA(cudaMemcpyAsync(rh.data(), m->invR.ptr, sizeof(double) * ny, cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        double rel = 0.0;
+        for (int p = 0; p < images; ++p) {
+            double rr = 0.0;
+            for (int r = 0; r < rowsJ; ++r) rr += rh[(size_t)p * rowsJ + r] * rh[(size_t)p * rowsJ + r];
+            if (ynorm[p] > 0.0) rel = std::max(rel, std::sqrt(rr / ynorm[p]));
+        }
+        if (rel <= 1e-13) break;
+        if (rel > 0.5 * prev) {
+            if (exact) break;
+            // the split-BF16 factor is too coarse for this mu: FP64 Gram, solve again
+            MPF_TRY(dense_gram_f64_exact(1, rowsJ, ld, m->invJ.ptr, ld, mu, m->invA.ptr, nullptr, s));
+            MPF_TRY(dense_cholesky_f64(1, rowsJ, m->invA.ptr, m->invInfo.ptr, s));
+            MPF_CUDA(cudaMemcpyAsync(m->invY.ptr, m->invYs.ptr, sizeof(double) * ny, cudaMemcpyDeviceToDevice, s));
+            MPF_TRY(dense_cholesky_solve_f64(1, rowsJ, m->invA.ptr, m->invY.ptr, images, s));
+            exact = true;
+            prev = 1e300;
+            continue;
+        }
+        prev = rel;
+        MPF_TRY(dense_cholesky_solve_f64(1, rowsJ, m->invA.ptr, m->invR.ptr, images, s));
+        k_axpy64<<<(int)std::min<size_t>((ny + 255) / 256, 1024), 256, 0, s>>>(ny, m->invR.ptr, m->invY.ptr);
+        MPF_LAUNCHED(1);
+    }
+    return MPF_OK;
+}
+
+// true when the last Cholesky of the inverse workspace met a non-positive
+// pivot (synchronises the stream)
+static bool pivot_failed(mpf_eit* m, cudaStream_t s) {
+    int info = 0;
+    if (cudaMemcpyAsync(&info, m->invInfo.ptr, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return false;
+    return info != 0;
+}
+
 int inverse_solve(mpf_eit* m, int reg, double factor, int images, const float* Jref, const float* calc,
                   const float* meas, float* result, cudaStream_t s) {
     MPF_CUDA(cudaSetDevice(m->device));
@@ -146,7 +240,14 @@ int inverse_solve(mpf_eit* m, int reg, double factor, int images, const float* J
         MPF_TRY(dense_gram_f64_shift(1, rowsJ, ld, m->invHi.ptr, m->invLo.ptr, ld, mu, m->invA.ptr, m->invWork.ptr,
                                      m->invWork.count, s));
         MPF_TRY(dense_cholesky_f64(1, rowsJ, m->invA.ptr, m->invInfo.ptr, s));
-        MPF_TRY(dense_cholesky_solve_f64(1, rowsJ, m->invA.ptr, m->invY.ptr, images, s));
+        bool exact = false;
+        if (pivot_failed(m, s)) {
+            // mu below the split-BF16 Gram's error: the FP64 Gram of the FP32 J
+            MPF_TRY(dense_gram_f64_exact(1, rowsJ, ld, m->invJ.ptr, ld, mu, m->invA.ptr, nullptr, s));
+            MPF_TRY(dense_cholesky_f64(1, rowsJ, m->invA.ptr, m->invInfo.ptr, s));
+            exact = true;
+        }
+        MPF_TRY(refine_dual(m, rowsJ, E, ld, images, mu, exact, s));
         k_jt_times<<<dim3((ld + 255) / 256, images), 256, 0, s>>>(rowsJ, E, ld, m->invJ.ptr, m->invY.ptr, result,
                                                                     nullptr);
         MPF_LAUNCHED(1);
@@ -169,20 +270,29 @@ int inverse_solve(mpf_eit* m, int reg, double factor, int images, const float* J
         MPF_CUDA(cudaMemsetAsync(Jt, 0, sizeof(float) * (size_t)n * rowsJ, s));
         MPF_CUDA(cudaMemcpyAsync(Jt, Jref, sizeof(float) * (size_t)E * rowsJ, cudaMemcpyDeviceToDevice, s));
         MPF_TRY(dense_split_bf16(1, n, rowsJ, Jt, rowsJ, m->invHi.ptr, m->invLo.ptr, s));
+        auto regularise = [&]() -> int {
+            k_regularise<<<(n + 255) / 256, 256, 0, s>>>(n, E, reg, mu, m->invA.ptr);
+            MPF_LAUNCHED(1);
+            if (reg == MPF_REG_LAPLACIAN) {
+                MPF_TRY(laplacian_coo(m));
+                const int nnz = (int)m->lapVal.count;
+                k_add_coo<<<(nnz + 255) / 256, 256, 0, s>>>(nnz, n, mu, m->lapRow.ptr, m->lapCol.ptr, m->lapVal.ptr,
+                                                             m->invA.ptr);
+                MPF_LAUNCHED(1);
+            }
+            return MPF_OK;
+        };
         MPF_TRY(dense_gram_f64_shift(1, n, rowsJ, m->invHi.ptr, m->invLo.ptr, rowsJ, 0.0, m->invA.ptr, m->invWork.ptr,
                                      m->invWork.count, s));
-        k_regularise<<<(n + 255) / 256, 256, 0, s>>>(n, E, reg, mu, m->invA.ptr);
-        MPF_LAUNCHED(1);
-        if (reg == MPF_REG_LAPLACIAN) {
-            MPF_TRY(laplacian_coo(m));
-            const int nnz = (int)m->lapVal.count;
-            k_add_coo<<<(nnz + 255) / 256, 256, 0, s>>>(nnz, n, mu, m->lapRow.ptr, m->lapCol.ptr, m->lapVal.ptr,
-                                                         m->invA.ptr);
-            MPF_LAUNCHED(1);
-        }
+        MPF_TRY(regularise());
         k_jt_times<<<dim3((n + 255) / 256, images), 256, 0, s>>>(rowsJ, E, n, Jrow, m->invY.ptr, nullptr, m->invB.ptr);
         MPF_LAUNCHED(1);
         MPF_TRY(dense_cholesky_f64(1, n, m->invA.ptr, m->invInfo.ptr, s));
+        if (pivot_failed(m, s)) {
+            MPF_TRY(dense_gram_f64_exact(1, n, rowsJ, Jt, rowsJ, 0.0, m->invA.ptr, nullptr, s));
+            MPF_TRY(regularise());
+            MPF_TRY(dense_cholesky_f64(1, n, m->invA.ptr, m->invInfo.ptr, s));
+        }
         MPF_TRY(dense_cholesky_solve_f64(1, n, m->invA.ptr, m->invB.ptr, images, s));
         k_to_float_rows<<<dim3((E + 255) / 256, images), 256, 0, s>>>(images, E, n, m->invB.ptr, result);
         MPF_LAUNCHED(1);

@@ -778,7 +778,21 @@ static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* 
     const double mu = (double)m->ref * lambda * (double)m->ref * lambda;
     MPF_TRY(dense_gram_f64_shift(F, m->rowsJ, m->Epad, m->Jhi.ptr, m->Jlo.ptr, m->Epad, mu, m->A64.ptr,
                                  m->gramWork.ptr, m->gramWork.count, s, frameActive));
+    MPF_CUDA(cudaMemsetAsync(m->info.ptr, 0, sizeof(int) * F, s));
     MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, frameActive));
+    // frames whose split-BF16 J J^T + mu I is not positive definite (mu below
+    // the Gram's ~1e-5 relative error): FP32 J and the FP64 Gram, factor again
+    std::vector<int> info(F), redo(F, 0);
+    MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    bool any = false;
+    for (int f = 0; f < F; ++f) any |= (redo[f] = info[f] != 0) != 0;
+    if (any) {
+        MPF_TRY(m->redoMask.upload(redo));
+        MPF_TRY(eit_jacobian(m, F, gamma, m->redoMask.ptr, true, s));
+        MPF_TRY(dense_gram_f64_exact(F, m->rowsJ, m->Epad, m->J.ptr, m->Epad, mu, m->A64.ptr, m->redoMask.ptr, s));
+        MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, m->redoMask.ptr));
+    }
     MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s, frameActive));
     MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->Jhi.ptr, m->Jlo.ptr, m->y.ptr, frameActive, gamma,
                                     s));

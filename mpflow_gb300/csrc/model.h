@@ -246,6 +246,9 @@ int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi,
                          int ld, double shift, double* A64, float* work, size_t workFloats, cudaStream_t s,
                          const int* frameMask = nullptr);
 int dense_gram_check_abort(bool* aborted);
+// A64 = J J^T + shift I in FP64 from FP32 J (rows % 64 == 0, cols % 32 == 0)
+int dense_gram_f64_exact(int batch, int rows, int cols, const float* J, int ld, double shift, double* A64,
+                         const int* frameMask, cudaStream_t s);
 int dense_gram_split_bf16_noalloc(int batch, int rows, int cols, const float* A, int lda, float* C, cudaStream_t s);
 int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s);
 // frameMask: [batch] entries to process (null: all); skipped entries keep their contents

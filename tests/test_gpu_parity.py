@@ -134,7 +134,7 @@ def test_gn_step_matches_oracle_dual():
     d_ref = oracle.inverse_dual(J0, y, 1.0, lam)
     model = mp.EIT(mesh, src, 1.0)
     gt = torch.ones((1, mesh.elements.shape[0]), dtype=torch.float32, device="cuda")
-    vm = torch.tensor(Vmeas.T.reshape(1, -1), dtype=torch.float32, device="cuda")  # column-major Mm x Md
+    vm = torch.tensor(Vmeas[None], dtype=torch.float32, device="cuda")  # (frames, Mm, Md) as solve() returns
     res = model.gn_step(gt, vm, lam, mp.SolveOptions(tol=1e-7, refine_tol=1e-10))
     d = gt[0].cpu().numpy() - 1.0
     assert abs(res[0] - np.linalg.norm(y) / np.linalg.norm(oracle.flatten_measurement(Vmeas, orc))) < 1e-5

@@ -242,10 +242,14 @@ int mpf_eit_fields(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t 
  * |r| <= tol |b|, FP32 with FP64 inner products.
  *   gamma:    device, frames x n_elements complex (re, im interleaved)
  *   voltages: device, frames x (Mm x Md column-major) complex, interleaved
+ *   jacobian: device, frames x (jacobian_rows x n_elements column-major)
+ *             complex, interleaved, or NULL: calcJacobian's bilinear form
+ *             with complex fields and complex p'(gamma)
+ *             (src/fem/equation_kernel.cu:197-245)
  * Cold start only; MPF_ENOTSUP for refine_tol > 0, warm_start != 0, voltage
- * (fixed) sources or more than 64 unique excitations.  The complex Jacobian
- * is not computed.  Synchronises `stream`. */
-int mpf_eit_forward_complex(mpf_eit_t model, int32_t frames, const float* gamma, float* voltages,
+ * (fixed) sources or more than 64 unique excitations.  Synchronises
+ * `stream`. */
+int mpf_eit_forward_complex(mpf_eit_t model, int32_t frames, const float* gamma, float* voltages, float* jacobian,
                             const mpf_solve_opts* opts, mpf_solve_stats* stats, mpf_stream_t stream);
 
 /* ======================================================================== */

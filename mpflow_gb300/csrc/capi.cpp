@@ -43,7 +43,7 @@ int eit_assemble_export(mpf_eit* m, int F, const float* gamma, float* sOut, floa
 int eit_forward(mpf_eit* m, int F, const float* gamma, float* V, float* Jref, const mpf_solve_opts* o,
                 mpf_solve_stats* stats, cudaStream_t s);
 int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s);
-int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, const mpf_solve_opts* optsIn,
+int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, float* Jref, const mpf_solve_opts* optsIn,
                         mpf_solve_stats* stats, cudaStream_t s);
 int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, const mpf_solve_opts* o,
             double* residual, mpf_solve_stats* stats, cudaStream_t s);
@@ -215,11 +215,11 @@ int mpf_eit_forward(mpf_eit_t model, int32_t frames, const float* gamma, float* 
     })
 }
 
-int mpf_eit_forward_complex(mpf_eit_t model, int32_t frames, const float* gamma, float* voltages,
+int mpf_eit_forward_complex(mpf_eit_t model, int32_t frames, const float* gamma, float* voltages, float* jacobian,
                             const mpf_solve_opts* opts, mpf_solve_stats* stats, mpf_stream_t stream) {
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_forward_complex: model == nullptr");
-        return mpf::eit_forward_complex(model, frames, gamma, voltages, opts, stats, (cudaStream_t)stream);
+        return mpf::eit_forward_complex(model, frames, gamma, voltages, jacobian, opts, stats, (cudaStream_t)stream);
     })
 }
 

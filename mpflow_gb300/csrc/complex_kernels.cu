@@ -12,6 +12,8 @@
 //              real c' 1 1^T term as the real solvers do (k_zbi_*)
 //   voltages   V = sum_c beta_c Att Phi_c with complex Phi (k_zgram_meas,
 //              k_zvoltages)
+//   Jacobian   calcJacobianKernel's bilinear form with complex fields and
+//              complex p'(gamma) (k_zjacobian), then the reference layout
 // Vectors are node-major with KP complex values per node (re, im
 // interleaved); a lane moves CV = 2 complex values (16 bytes).
 #include "cg_common.cuh"
@@ -490,6 +492,120 @@ __global__ void k_zvoltages(int F, int Ca, int KP, int Mm, int Md, const double*
     }
 }
 
+// Complex Jacobian, the formula of the real k_jacobian (fem_kernels.cu) with
+// complex fields Y_c and complex p'(gamma):
+//   J[d*MP + m][e] += -h p'(gamma_e) sd sm sum_ij Y_c[n_i][ud] Ke[i+3j] Y_c[n_j][um]
+// for harmonic ci (beta_c^2 folded into the fields as in the real kernel).
+// A block owns 32 elements (one per lane) and stages the complex fields of
+// their 3 nodes; warp w handles drive rows w, w + 8, ...; the harmonics
+// accumulate into J [F][rowsJ][Epad] (complex) in global memory.
+template <int KP, int MP>
+__global__ void __launch_bounds__(256) k_zjacobian(JacPlan jp, int npad, const float* __restrict__ X,
+                                                   const float2* __restrict__ gamma, float2* __restrict__ J,
+                                                   int ci) {
+    extern __shared__ float2 zjsm[];  // Ys [3][KP][33], then Ts [3][KP][33]
+    float2(*Ys)[KP][33] = reinterpret_cast<float2(*)[KP][33]>(zjsm);
+    float2(*Ts)[KP][33] = reinterpret_cast<float2(*)[KP][33]>(zjsm + 3 * KP * 33);
+    __shared__ float Ke[32][9];
+    const int f = blockIdx.y;
+    const int e0 = blockIdx.x * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int e = e0 + lane;
+    const float mc = jp.massCoef[ci];
+    for (int i = threadIdx.x; i < 32 * 9; i += blockDim.x) {
+        const int el = i / 9, k = i % 9;
+        const bool in = e0 + el < jp.E;
+        Ke[el][k] = in ? jp.Kf[(size_t)(e0 + el) * 9 + k] + (jp.exact ? mc * jp.Mf[(size_t)(e0 + el) * 9 + k] : 0.f)
+                       : 0.f;
+    }
+    const float2* Xg = reinterpret_cast<const float2*>(X) + ((size_t)f * jp.Ca + ci) * npad * KP;
+    for (int i = threadIdx.x; i < 32 * 3 * KP; i += blockDim.x) {
+        const int u = i % KP, l = (i / KP) % 3, el = i / (3 * KP);
+        float2 v = make_float2(0.f, 0.f);
+        if (e0 + el < jp.E) v = Xg[(size_t)jp.elements[(size_t)(e0 + el) * 3 + l] * KP + u];
+        Ys[l][u][el] = v;
+    }
+    __syncthreads();
+    const float b2 = jp.beta2[ci];
+    for (int i = threadIdx.x; i < 32 * 3 * KP; i += blockDim.x) {
+        const int el = i % 32, u = (i / 32) % KP, jj = i / (32 * KP);
+        float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int ii = 0; ii < 3; ++ii) {
+            const float k = b2 * Ke[el][ii * 3 + jj];
+            t.x = fmaf(k, Ys[ii][u][el].x, t.x);
+            t.y = fmaf(k, Ys[ii][u][el].y, t.y);
+        }
+        Ts[jj][u][el] = t;
+    }
+    __syncthreads();
+    const bool valid = e < jp.E;
+    float2 deriv = make_float2(0.f, 0.f);
+    if (valid) {
+        const float2 g = gamma[(size_t)f * jp.E + e];
+        if (jp.logarithmic) {
+            const float a = 0.2302585093f * g.x, b = 0.2302585093f * g.y;
+            float sn, cs;
+            sincosf(b, &sn, &cs);
+            const float mag = -jp.height * 0.2302585093f * jp.ref * expf(a);
+            deriv = make_float2(mag * cs, mag * sn);
+        } else {
+            deriv = make_float2(-jp.height * jp.ref, 0.f);
+        }
+    }
+    const int drives = jp.rowsJ / MP;
+    const size_t base = (size_t)f * jp.rowsJ * jp.Epad;
+    for (int d = warp; d < drives; d += blockDim.x / 32) {
+        const int ud = jp.rowD[d * MP];
+        float2 acc[MP];
+#pragma unroll
+        for (int m = 0; m < MP; ++m) acc[m] = make_float2(0.f, 0.f);
+        if (ud >= 0) {
+#pragma unroll
+            for (int jj = 0; jj < 3; ++jj) {
+                const float2 td = Ts[jj][ud][lane];
+#pragma unroll
+                for (int m = 0; m < MP; ++m) {
+                    const int um = jp.rowM[m];
+                    const float2 ym = um >= 0 ? Ys[jj][um][lane] : make_float2(0.f, 0.f);
+                    acc[m] = cfma(td, ym, acc[m]);
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < MP; ++m) {
+            const int row = d * MP + m;
+            const size_t o = base + (size_t)row * jp.Epad + e;
+            const float2 v = valid ? cmul(deriv, make_float2(jp.rowScale[row] * acc[m].x, jp.rowScale[row] * acc[m].y))
+                                   : make_float2(0.f, 0.f);
+            if (ci == 0) {
+                J[o] = v;
+            } else {
+                const float2 old = J[o];
+                J[o] = make_float2(old.x + v.x, old.y + v.y);
+            }
+        }
+    }
+}
+
+// [F][rowsJ][Epad] -> the reference layout [F][E][rowsJ] (column-major rowsJ x E)
+__global__ void k_ztranspose(int rowsJ, int Epad, int E, const float2* __restrict__ J, float2* __restrict__ Jref) {
+    __shared__ float2 tile[32][33];
+    const int f = blockIdx.z, e0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const float2* Jf = J + (size_t)f * rowsJ * Epad;
+    float2* Rf = Jref + (size_t)f * E * rowsJ;
+    for (int k = ty; k < 32; k += 8) {
+        const int r = r0 + k, e = e0 + tx;
+        tile[k][tx] = (r < rowsJ && e < E) ? Jf[(size_t)r * Epad + e] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        const int e = e0 + k, r = r0 + tx;
+        if (e < E && r < rowsJ) Rf[(size_t)e * rowsJ + r] = tile[tx][k];
+    }
+}
+
 template <int KP>
 int zinit_kp(const CgProblem& P, cudaStream_t s) {
     k_zbi_init<KP><<<dim3(P.nblk, P.G), kThreads, 0, s>>>(P);
@@ -509,7 +625,40 @@ int ziter_kp(const CgProblem& P, cudaStream_t s) {
     return MPF_OK;
 }
 
+template <int KP, int MP>
+int zjac_kp(int F, const JacPlan& jp, int npad, const float* X, const float* gamma2, float* Jz, cudaStream_t s) {
+    const dim3 grid(jp.Epad / 32, F);
+    const size_t smem = sizeof(float2) * 2 * 3 * KP * 33;
+    if (smem > 48 * 1024)
+        MPF_CUDA(cudaFuncSetAttribute(k_zjacobian<KP, MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    for (int ci = 0; ci < jp.Ca; ++ci)
+        k_zjacobian<KP, MP><<<grid, 256, smem, s>>>(jp, npad, X, reinterpret_cast<const float2*>(gamma2),
+                                                    reinterpret_cast<float2*>(Jz), ci);
+    MPF_LAUNCHED(jp.Ca);
+    return MPF_OK;
+}
+
 }  // namespace
+
+int fem_launch_zjacobian(int F, const JacPlan& jp, int MP, int npad, const float* Xz, const float* gamma2, float* Jz,
+                         cudaStream_t s) {
+#define MPF_ZJAC(KPv, MPv) \
+    if (jp.KP == KPv && MP == MPv) return zjac_kp<KPv, MPv>(F, jp, npad, Xz, gamma2, Jz, s);
+    MPF_ZJAC(16, 16)
+    MPF_ZJAC(32, 16)
+    MPF_ZJAC(32, 32)
+    MPF_ZJAC(64, 32)
+#undef MPF_ZJAC
+    return fail(MPF_ENOTSUP, "complex Jacobian: %d unique excitations with %d measurement rows", jp.KP, MP);
+}
+
+int fem_launch_ztranspose_jacobian(int F, int rowsJ, int Epad, int E, const float* Jz, float* Jref, cudaStream_t s) {
+    dim3 grid((E + 31) / 32, (rowsJ + 31) / 32, F);
+    k_ztranspose<<<grid, dim3(32, 8), 0, s>>>(rowsJ, Epad, E, reinterpret_cast<const float2*>(Jz),
+                                              reinterpret_cast<float2*>(Jref));
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
 
 int zbicgstab_launch_init(const CgProblem& P, cudaStream_t s) {
     switch (P.KP) {

@@ -58,6 +58,7 @@ struct mpf_eit {
     mpf::DevBuf<float4> SRz;
     mpf::DevBuf<float> Xz, Rz, Yz, Nz, Hz, Zz, Tz, Vz;
     mpf::DevBuf<double> zRhoI, zAlphaI, zBetaI, zOmega, zOmegaI, zSumI, zRr, Gmz;
+    mpf::DevBuf<float> Jz;  // complex Jacobian [F][rowsJ][Epad] (re, im), on request
     mpf::DevBuf<float> V, J, gramWork;
     mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
     mpf::DevBuf<double> A64, y, res;

@@ -697,7 +697,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
 // Forward solve for complex material values (complex_kernels.cu): gamma
 // [F][E] complex, V [F][Mm][Md] complex (column-major per frame), both with
 // interleaved real and imaginary parts.
-int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, const mpf_solve_opts* optsIn,
+int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, float* Jref, const mpf_solve_opts* optsIn,
                         mpf_solve_stats* stats, cudaStream_t s) {
     MPF_TRY(check_device(m));
     MPF_CHECK(F >= 1 && gamma && Vout, MPF_EINVAL, "mpf_eit_forward_complex: bad arguments");
@@ -738,6 +738,14 @@ int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, cons
                                   m->Gmz.ptr, s));
     MPF_TRY(fem_launch_zvoltages(F, m->Ca, m->KP, m->Mm, m->Md, m->Gmz.ptr, m->beta.ptr, m->measU.ptr,
                                  m->measScale.ptr, m->driveU.ptr, m->driveScale.ptr, Vout, s));
+    if (Jref) {
+        MPF_TRY(m->Jz.alloc(2 * (size_t)F * m->rowsJ * m->Epad));
+        JacPlan jp{m->rowsJ, m->Epad, m->E, m->KP, m->Ca, m->rowD.ptr, m->rowM.ptr, m->rowScale.ptr,
+                   m->beta2.ptr, m->massCoef.ptr, m->elements.ptr, m->Kf.ptr, m->Mf.ptr, m->exactJacobian,
+                   m->ref, (float)m->height, m->logarithmic, nullptr, 1};
+        MPF_TRY(fem_launch_zjacobian(F, jp, m->MmPad, m->npad, m->Xz.ptr, gamma, m->Jz.ptr, s));
+        MPF_TRY(fem_launch_ztranspose_jacobian(F, m->rowsJ, m->Epad, m->E, m->Jz.ptr, Jref, s));
+    }
     MPF_CUDA(cudaStreamSynchronize(s));
     MPF_CUDA(cudaGetLastError());
     if (stats) {

@@ -221,6 +221,10 @@ struct JacPlan {
 };
 int fem_launch_jacobian(int F, const JacPlan& jp, int MP, int npad, const float* X, const float* gamma,
                         float* J, __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s);
+// complex_kernels.cu: Jacobian of the complex-admittivity model
+int fem_launch_zjacobian(int F, const JacPlan& jp, int MP, int npad, const float* Xz, const float* gamma2, float* Jz,
+                         cudaStream_t s);
+int fem_launch_ztranspose_jacobian(int F, int rowsJ, int Epad, int E, const float* Jz, float* Jref, cudaStream_t s);
 int fem_launch_transpose_jacobian(int F, int rowsJ, int Epad, int E, const float* J, float* Jref,
                                   cudaStream_t s);
 int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int npad, int KP,

@@ -251,10 +251,11 @@ class EIT:
             return Vm, J.transpose(1, 2)
         return Vm
 
-    def solve_complex(self, materialDistribution, options: SolveOptions | None = None,
+    def solve_complex(self, materialDistribution, options: SolveOptions | None = None, jacobian: bool = False,
                       raise_on_noconv: bool = True):
         """Forward solve for complex material values (complex64 CUDA tensor,
-        frames x elements); returns complex64 voltages (frames x Mm x Md),
+        frames x elements); returns complex64 voltages (frames x Mm x Md) and,
+        if asked, the complex Jacobian (frames x rowsJ x E),
         mpf_eit_forward_complex."""
         import torch
         g = materialDistribution
@@ -264,14 +265,21 @@ class EIT:
         F = g.shape[0]
         Mm, Md = self.info["meas_count"], self.info["drive_count"]
         V = torch.empty((F, Md, Mm), dtype=torch.complex64, device=g.device)
+        J = None
+        if jacobian:
+            J = torch.empty((F, self.mesh.elements.shape[0], self.jacobian_rows), dtype=torch.complex64,
+                            device=g.device)
         st = _ffi.SolveStats()
         o = (options or SolveOptions(solver="bicgstab")).c()
         status = lib().mpf_eit_forward_complex(self._h, F, ctypes.c_void_p(g.data_ptr()),
-                                               ctypes.c_void_p(V.data_ptr()), ctypes.byref(o), ctypes.byref(st),
-                                               _stream())
+                                               ctypes.c_void_p(V.data_ptr()),
+                                               ctypes.c_void_p(J.data_ptr() if J is not None else 0),
+                                               ctypes.byref(o), ctypes.byref(st), _stream())
         self.last_stats = st
         if status != _ffi.MPF_OK and (raise_on_noconv or status != 4):
             check(status)
+        if jacobian:
+            return V.transpose(1, 2), J.transpose(1, 2)
         return V.transpose(1, 2)
 
     def fields(self, frames: int):

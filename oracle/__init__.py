@@ -535,13 +535,33 @@ def eit_forward_fixed(s: Setup, gamma: np.ndarray, want_jacobian: bool = True):
     return V, J, fields
 
 
-def eit_forward_complex(s: Setup, gamma: np.ndarray) -> np.ndarray:
+def calc_jacobian_complex(s: Setup, phi: np.ndarray, gamma: np.ndarray) -> np.ndarray:
+    """calcJacobianKernel (src/fem/equation_kernel.cu:197-245) for complex
+    fields phi (n x (Md+Mm)) and complex gamma: rowsJ x E, row
+    d * roundMeas + m, J[row, e] = p'(gamma_e) sum_ij phi[n_i, d] K_e[i + 3 j]
+    phi[n_j, Md + m] (bilinear, no conjugation)."""
+    E = s.elements.shape[0]
+    g = np.asarray(gamma, np.complex128)
+    deriv = s.ref * (math.log(10.0) / 10.0) * np.exp(math.log(10.0) * g / 10.0) if s.logarithmic else \
+        np.full(E, s.ref, np.complex128)
+    Kr = np.asarray(s.K, np.float64).reshape(E, 3, 3)        # flat i + 3 j -> Kr[e, j, i]
+    nodes = phi[s.elements]                                  # E x 3 x (Md+Mm)
+    el = np.einsum("eid,eji,ejm->edm", nodes[:, :, :s.Md], Kr, nodes[:, :, s.Md:s.Md + s.Mm])
+    roundMeas = _round16(s.Mm)
+    J = np.zeros((s.rowsJ, E), np.complex128)
+    for d in range(s.Md):
+        J[d * roundMeas:d * roundMeas + s.Mm, :] = (el[:, d, :] * deriv[:, None]).T
+    return J
+
+
+def eit_forward_complex(s: Setup, gamma: np.ndarray, want_jacobian: bool = False):
     """Restatement of EIT::solve for complex material values (the
     Equation<thrust::complex<T>> instantiations, src/models/eit.cpp:139-245
     and :289-304; p(gamma) of src/fem/equation_kernel.cu:35-43 with complex
     gamma), current sources.  The complex systems are solved directly in FP64
     (the reference iterates to the same solution); the Neumann harmonic is
-    (A + 1 1^T) x = b as in the reference's CG.  Returns V (Mm x Md, complex)."""
+    (A + 1 1^T) x = b as in the reference's CG.  Returns V (Mm x Md, complex)
+    and, with want_jacobian, (V, J) with J = -h sum_c J_c (rowsJ x E)."""
     g = np.asarray(gamma, np.complex128)
     p = s.ref * (np.exp(math.log(10.0) * g / 10.0) if s.logarithmic else g)
     S = (update_matrix(s.layout, s.layout.elemS, p.real, 1.0, False) +
@@ -552,6 +572,7 @@ def eit_forward_complex(s: Setup, gamma: np.ndarray) -> np.ndarray:
     pattern = np.concatenate([s.drive * s.values[None, :], s.meas], axis=1)
     att = s.meas.T @ s.exc.T
     V = np.zeros((s.Mm, s.Md), np.complex128)
+    J = np.zeros((s.rowsJ, s.elements.shape[0]), np.complex128) if want_jacobian else None
     for c in range(s.components):
         alpha, beta = s.alpha_beta(c)
         sys_re = update_system_matrix(s.layout, S.real.copy(), R.real.copy(), alpha)
@@ -561,4 +582,8 @@ def eit_forward_complex(s: Setup, gamma: np.ndarray) -> np.ndarray:
             A = A + 1.0
         x = np.linalg.solve(A, (s.exc @ pattern) * beta)
         V += att @ x[:, :s.Md]
+        if want_jacobian:
+            J += calc_jacobian_complex(s, x, g)
+    if want_jacobian:
+        return V, -s.height * J
     return V

@@ -33,13 +33,15 @@ def test_complex_forward_matches_oracle(logarithmic):
     mesh, src, orc = make_setup(rings=16, ports=16, components=3, height=2.0, logarithmic=logarithmic)
     g = _complex_frames(mesh, 2, seed=3, logarithmic=logarithmic)
     model = mp.EIT(mesh, src, 1.0, components=3, height=2.0, logarithmic=logarithmic)
-    V = model.solve_complex(torch.tensor(g, dtype=torch.complex64, device="cuda"),
-                            mp.SolveOptions(tol=1e-7, solver="bicgstab"))
+    V, J = model.solve_complex(torch.tensor(g, dtype=torch.complex64, device="cuda"),
+                               mp.SolveOptions(tol=1e-7, solver="bicgstab"), jacobian=True)
     assert model.last_stats.not_converged == 0 and model.last_stats.iterations > 0
     for f in range(2):
-        Vo = oracle.eit_forward_complex(orc, g[f])
+        Vo, Jo = oracle.eit_forward_complex(orc, g[f], want_jacobian=True)
         assert np.abs(Vo.imag).max() > 1e-3 * np.abs(Vo.real).max()  # a genuinely complex case
         assert rel_err(V[f].cpu().numpy(), Vo) < 1e-4, f
+        assert J[f].shape == Jo.shape
+        assert rel_err(J[f].cpu().numpy(), Jo) < 1e-4, f
 
 
 def test_complex_with_real_values_equals_real_solve():
@@ -48,13 +50,16 @@ def test_complex_with_real_values_equals_real_solve():
     mesh, src, _ = make_setup(rings=20, ports=32, width=0.1, components=4, height=4.0)
     g = np.stack([inclusion_sigma(mesh, seed=s) for s in range(3)])
     model = mp.EIT(mesh, src, 1.0, components=4, height=4.0)
-    Vr = model.solve(torch.tensor(g, dtype=torch.float32, device="cuda"), mp.SolveOptions(tol=1e-7))
-    Vz = model.solve_complex(torch.tensor(g, dtype=torch.complex64, device="cuda"),
-                             mp.SolveOptions(tol=1e-7, solver="bicgstab"))
-    Vr = Vr.cpu().numpy()
-    Vz = Vz.cpu().numpy()
+    Vr, Jr = model.solve(torch.tensor(g, dtype=torch.float32, device="cuda"), mp.SolveOptions(tol=1e-7),
+                         jacobian=True)
+    Vz, Jz = model.solve_complex(torch.tensor(g, dtype=torch.complex64, device="cuda"),
+                                 mp.SolveOptions(tol=1e-7, solver="bicgstab"), jacobian=True)
+    Vr, Jr = Vr.cpu().numpy(), Jr.cpu().numpy()
+    Vz, Jz = Vz.cpu().numpy(), Jz.cpu().numpy()
     assert rel_err(Vz.real, Vr) < 2e-5
     assert np.abs(Vz.imag).max() <= 1e-6 * np.abs(Vr).max()
+    assert rel_err(Jz.real, Jr) < 5e-5
+    assert np.abs(Jz.imag).max() <= 1e-6 * np.abs(Jr).max()
 
 
 def test_complex_rejects_unsupported_options():

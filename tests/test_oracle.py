@@ -166,3 +166,12 @@ def test_complex_oracle_reduces_to_real():
     Vz = oracle.eit_forward_complex(orc, g.astype(np.complex128))
     assert np.abs(Vz.imag).max() <= 1e-12 * np.abs(V).max()
     assert np.abs(Vz.real - V).max() <= 1e-9 * np.abs(V).max()
+
+
+def test_complex_oracle_jacobian_reduces_to_real():
+    mesh, src, orc = make_setup(rings=12, ports=8, width=0.3, components=2, height=2.0)
+    g = inclusion_sigma(mesh, seed=4)
+    _, J, _ = oracle.eit_forward(orc, g, tol=1e-14)
+    _, Jz = oracle.eit_forward_complex(orc, g.astype(np.complex128), want_jacobian=True)
+    assert np.abs(Jz.imag).max() <= 1e-12 * np.abs(J).max()
+    assert np.abs(Jz.real - J).max() <= 1e-8 * np.abs(J).max()

@@ -339,6 +339,40 @@ int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, 
 int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int32_t* get);
 
 /* ======================================================================== */
+/* Sparse matrices and Krylov solvers on a caller's matrix                   */
+/* ======================================================================== */
+
+/* numeric::SparseMatrix (include/mpflow/numeric/sparse_matrix.h:30-80) built
+ * from the reference ELL layout: values and column_ids are DEVICE arrays of
+ * data_rows(rows) x 32 (row-major, 0xFFFFFFFF padding), as
+ * SparseMatrix::deviceValues / deviceColumnIds; density = used slots per row
+ * (at most 32, MPF_EFULL otherwise).  The library keeps its own copy. */
+typedef struct mpf_sparse* mpf_sparse_t;
+int mpf_sparse_create(int32_t rows, const float* values, const uint32_t* column_ids, uint32_t density,
+                      mpf_sparse_t* matrix);
+int mpf_sparse_destroy(mpf_sparse_t matrix);
+
+/* SparseMatrix::multiply (src/numeric/sparse_matrix.cpp:262-288): y = A x for
+ * `cols` column-major columns (device, leading dimensions ldx, ldy >= rows). */
+int mpf_sparse_multiply(mpf_sparse_t matrix, const float* x, int32_t ldx, int32_t cols, float* y, int32_t ldy,
+                        mpf_stream_t stream);
+
+/* ConjugateGradient::solve / BiCGSTAB::solve (src/numeric/conjugate_gradient.cpp:
+ * 61-161, src/numeric/bicgstab.cpp:83-193) on every column of b at once,
+ * each column an independent system with its own scalars and convergence
+ * mask; x (device, column-major, ldx) is the initial guess and receives the
+ * solution.  solver: 0 CG, 1 BiCGSTAB; always Jacobi-preconditioned (the
+ * reference's KInv = preconditioner::diagonal).  dc_free solves
+ * (A + 1 1^T) x = b as the reference's iteration (its initial residual adds
+ * +sum(x) instead, src/numeric/conjugate_gradient.cpp:86-89; the same for a
+ * zero start).  max_iter <= 0: 10 * rows; tol <= 0: float epsilon, the
+ * reference's level.  *iterations: slowest column.  MPF_ENOCONV when a
+ * column hits max_iter (the reference returns silently).  Synchronises. */
+int mpf_sparse_solve(mpf_sparse_t matrix, int32_t solver, const float* b, int32_t ldb, float* x, int32_t ldx,
+                     int32_t cols, int32_t max_iter, double tol, int32_t dc_free, int32_t* iterations,
+                     mpf_stream_t stream);
+
+/* ======================================================================== */
 /* Batches of uneven meshes                                                  */
 /* ======================================================================== */
 

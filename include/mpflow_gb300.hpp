@@ -5,8 +5,9 @@
 // code written against them compiles with few changes:
 //   numeric::Matrix<T>          include/mpflow/numeric/matrix.h
 //   numeric::IrregularMesh      include/mpflow/numeric/irregular_mesh.h
-//   numeric::ConjugateGradient  include/mpflow/numeric/conjugate_gradient.h (solver tag)
-//   numeric::BiCGSTAB           include/mpflow/numeric/bicgstab.h (solver tag)
+//   numeric::SparseMatrix<T>    include/mpflow/numeric/sparse_matrix.h
+//   numeric::ConjugateGradient  include/mpflow/numeric/conjugate_gradient.h
+//   numeric::BiCGSTAB           include/mpflow/numeric/bicgstab.h
 //   FEM::Ports, FEM::Sources<T> include/mpflow/fem/ports.h, sources.h
 //   FEM::Equation, basis::Linear include/mpflow/fem/equation.h (template tags)
 //   models::EIT<...>            include/mpflow/models/eit.h
@@ -364,13 +365,223 @@ private:
     mutable std::vector<type> host_;
 };
 
-// Krylov solver tags of models::EIT (the solve itself runs in the library):
-// numeric::ConjugateGradient (include/mpflow/numeric/conjugate_gradient.h) and
-// numeric::BiCGSTAB (include/mpflow/numeric/bicgstab.h)
-template <class T>
-class ConjugateGradient {};
-template <class T>
-class BiCGSTAB {};
+// Sparse matrix in the reference ELL layout (include/mpflow/numeric/
+// sparse_matrix.h): dataRows x 32 values and column ids, row-major,
+// 0xFFFFFFFF padding, host and device copies.  multiply() and the solvers
+// below run in the library on its own copy (mpf_sparse_*), refreshed when
+// the device arrays changed through copyToDevice().
+template <class type_>
+class SparseMatrix {
+public:
+    typedef type_ type;
+    static unsigned const blockSize = 32;
+    static unsigned const invalidIndex = 0xFFFFFFFFu;
+
+    SparseMatrix(unsigned const rows, unsigned const cols, cudaStream_t const stream = nullptr)
+        : rows(rows), cols(cols) {
+        init(stream);
+    }
+    // src/numeric/sparse_matrix.cpp:29-42, 202-226: the nonzeros of every row
+    // in column order (the matrix's host copy is read)
+    SparseMatrix(std::shared_ptr<Matrix<type> const> const matrix, cudaStream_t const stream = nullptr)
+        : rows(matrix ? matrix->rows : 0), cols(matrix ? matrix->cols : 0) {
+        if (!matrix) throw std::invalid_argument("mpFlow::numeric::numeric::SparseMatrix::SparseMatrix: matrix == nullptr");
+        init(stream);
+        for (unsigned i = 0; i < rows; ++i)
+            for (unsigned j = 0; j < cols; ++j)
+                if ((*matrix)(i, j) != type(0)) setValue(i, j, (*matrix)(i, j));
+        copyToDevice(stream);
+    }
+    SparseMatrix(SparseMatrix const&) = delete;
+    SparseMatrix& operator=(SparseMatrix const&) = delete;
+    virtual ~SparseMatrix() {
+        if (handle_) mpf_sparse_destroy(handle_);
+        cudaFree(deviceValues);
+        cudaFree(deviceColumnIds);
+    }
+
+    void copyToDevice(cudaStream_t const stream = nullptr) {
+        detail::cuda(cudaMemcpyAsync(deviceValues, hostValues_.data(), sizeof(type) * hostValues_.size(),
+                                     cudaMemcpyHostToDevice, stream),
+                     "mpFlow::numeric::SparseMatrix::copyToDevice");
+        detail::cuda(cudaMemcpyAsync(deviceColumnIds, hostColumnIds_.data(), sizeof(unsigned) * hostColumnIds_.size(),
+                                     cudaMemcpyHostToDevice, stream),
+                     "mpFlow::numeric::SparseMatrix::copyToDevice");
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::numeric::SparseMatrix::copyToDevice");
+        dirty_ = true;
+    }
+    void copyToHost(cudaStream_t const stream = nullptr) {
+        detail::cuda(cudaMemcpyAsync(hostValues_.data(), deviceValues, sizeof(type) * hostValues_.size(),
+                                     cudaMemcpyDeviceToHost, stream),
+                     "mpFlow::numeric::SparseMatrix::copyToHost");
+        detail::cuda(cudaMemcpyAsync(hostColumnIds_.data(), deviceColumnIds, sizeof(unsigned) * hostColumnIds_.size(),
+                                     cudaMemcpyDeviceToHost, stream),
+                     "mpFlow::numeric::SparseMatrix::copyToHost");
+        detail::cuda(cudaStreamSynchronize(stream), "mpFlow::numeric::SparseMatrix::copyToHost");
+    }
+
+    // src/numeric/sparse_matrix.cpp:358-423 (host arrays)
+    unsigned getColumnId(unsigned const row, unsigned const col) const {
+        return hostColumnIds_[(size_t)row * blockSize + col];
+    }
+    type getValue(unsigned const row, unsigned const col) const {
+        for (unsigned i = 0; i < blockSize; ++i)
+            if (hostColumnIds_[(size_t)row * blockSize + i] == col) return hostValues_[(size_t)row * blockSize + i];
+        return type(0);
+    }
+    void setValue(unsigned const row, unsigned const col, type const& value) {
+        if (row >= rows || col >= cols)
+            throw std::logic_error("mpFlow::numeric::SparseMatrix::setValue(): index out of range");
+        unsigned slot = invalidIndex;
+        for (unsigned i = 0; i < blockSize; ++i) {
+            unsigned& id = hostColumnIds_[(size_t)row * blockSize + i];
+            if (id == col) {
+                slot = i;
+                break;
+            }
+            if (id == invalidIndex) {
+                slot = i;
+                id = col;
+                density = std::max(density, i + 1);
+                break;
+            }
+        }
+        if (slot == invalidIndex) throw std::logic_error("mpFlow::numeric::SparseMatrix::operator(): sparse format full");
+        hostValues_[(size_t)row * blockSize + slot] = value;
+    }
+
+    // src/numeric/sparse_matrix.cpp:262-288: result = this * matrix (device data)
+    void multiply(std::shared_ptr<Matrix<type> const> const matrix, cudaStream_t const stream,
+                  std::shared_ptr<Matrix<type>> result) const {
+        if (!matrix) throw std::invalid_argument("mpFlow::numeric::SparseMatrix::multiply: matrix == nullptr");
+        if (!result) throw std::invalid_argument("mpFlow::numeric::SparseMatrix::multiply: result == nullptr");
+        if (matrix->rows != cols || result->rows != rows || result->cols != matrix->cols)
+            throw std::invalid_argument("mpFlow::numeric::SparseMatrix::multiply: shape does not match");
+        detail::check(mpf_sparse_multiply(handle(), matrix->deviceData, (int32_t)matrix->dataRows,
+                                          (int32_t)matrix->cols, result->deviceData, (int32_t)result->dataRows,
+                                          stream),
+                      "mpFlow::numeric::SparseMatrix::multiply");
+    }
+
+    // src/numeric/sparse_matrix.cpp:228-244 (host copy)
+    std::shared_ptr<Matrix<type>> toMatrix(cudaStream_t const stream = nullptr) const {
+        auto m = std::make_shared<Matrix<type>>(rows, cols, stream);
+        for (unsigned i = 0; i < rows; ++i)
+            for (unsigned k = 0; k < blockSize; ++k) {
+                const unsigned c = hostColumnIds_[(size_t)i * blockSize + k];
+                if (c != invalidIndex) (*m)(i, c) = hostValues_[(size_t)i * blockSize + k];
+            }
+        m->copyToDevice(stream);
+        return m;
+    }
+
+    // the library's copy of the device arrays
+    mpf_sparse_t handle() const {
+        if (dirty_ || !handle_) {
+            if (handle_) mpf_sparse_destroy(handle_);
+            handle_ = nullptr;
+            detail::check(mpf_sparse_create((int32_t)rows, deviceValues, deviceColumnIds, density, &handle_),
+                          "mpFlow::numeric::SparseMatrix");
+            dirty_ = false;
+        }
+        return handle_;
+    }
+
+    unsigned const rows;
+    unsigned const cols;
+    unsigned dataRows = 0;
+    unsigned dataCols = 0;
+    unsigned density = 0;
+    type* deviceValues = nullptr;
+    unsigned* deviceColumnIds = nullptr;
+
+private:
+    void init(cudaStream_t const stream) {
+        if (rows == 0) throw std::invalid_argument("mpFlow::numeric::numeric::SparseMatrix::init: rows == 0");
+        if (cols == 0) throw std::invalid_argument("mpFlow::numeric::numeric::SparseMatrix::init: columns == 0");
+        dataRows = mpf_data_rows(rows);
+        dataCols = mpf_data_rows(cols);
+        hostValues_.assign((size_t)dataRows * blockSize, type(0));
+        hostColumnIds_.assign((size_t)dataRows * blockSize, invalidIndex);
+        detail::cuda(cudaMalloc((void**)&deviceValues, sizeof(type) * hostValues_.size()),
+                     "mpFlow::numeric::SparseMatrix::init: create device data memory");
+        detail::cuda(cudaMalloc((void**)&deviceColumnIds, sizeof(unsigned) * hostColumnIds_.size()),
+                     "mpFlow::numeric::SparseMatrix::init: create device data memory");
+        copyToDevice(stream);
+    }
+    std::vector<type> hostValues_;
+    std::vector<unsigned> hostColumnIds_;
+    mutable mpf_sparse_t handle_ = nullptr;
+    mutable bool dirty_ = true;
+};
+
+namespace krylov {
+// numeric::ConjugateGradient / numeric::BiCGSTAB solve through mpf_sparse_solve
+template <class dataType>
+unsigned solve(int32_t solver, std::shared_ptr<SparseMatrix<dataType>> const A,
+                      std::shared_ptr<Matrix<dataType> const> const b, cudaStream_t const stream,
+                      std::shared_ptr<Matrix<dataType>> const x, unsigned const maxIterations, bool const dcFree,
+                      char const* where) {
+    if (!A) throw std::invalid_argument(std::string(where) + ": A == nullptr");
+    if (!b) throw std::invalid_argument(std::string(where) + ": b == nullptr");
+    if (!x) throw std::invalid_argument(std::string(where) + ": x == nullptr");
+    int32_t iterations = 0;
+    const int status = mpf_sparse_solve(A->handle(), solver, b->deviceData, (int32_t)b->dataRows, x->deviceData,
+                                        (int32_t)x->dataRows, (int32_t)b->cols, (int32_t)maxIterations, 0.0,
+                                        dcFree ? 1 : 0, &iterations, stream);
+    if (status != MPF_OK && status != MPF_ENOCONV) mpFlow::detail::check(status, where);
+    return (unsigned)iterations;
+}
+}  // namespace krylov
+
+// numeric::ConjugateGradient (include/mpflow/numeric/conjugate_gradient.h):
+// all columns of b at once, Jacobi-preconditioned (KInv is accepted and
+// the diagonal preconditioner used in its place), the reference's
+// stopping level and iteration cap; returns the iterations of the slowest
+// column.  Also the solver tag of models::EIT.
+template <class dataType>
+class ConjugateGradient {
+public:
+    ConjugateGradient(unsigned const rows, unsigned const cols, cudaStream_t const stream = nullptr)
+        : rows(rows), cols(cols) {
+        (void)stream;
+        if (rows < 1) throw std::invalid_argument("mpFlow::numeric::ConjugateGradient::ConjugateGradient: rows <= 1");
+        if (cols < 1) throw std::invalid_argument("mpFlow::numeric::ConjugateGradient::ConjugateGradient: cols <= 1");
+    }
+    template <template <class> class matrixType, template <class> class preconditionerType = matrixType>
+    unsigned solve(std::shared_ptr<matrixType<dataType>> const A, std::shared_ptr<Matrix<dataType> const> const b,
+                   cublasHandle_t const handle, cudaStream_t const stream, std::shared_ptr<Matrix<dataType>> const x,
+                   std::shared_ptr<preconditionerType<dataType>> const KInv = nullptr, unsigned const maxIterations = 0,
+                   bool const dcFree = false) {
+        (void)handle;
+        (void)KInv;
+        return krylov::solve(0, A, b, stream, x, maxIterations, dcFree, "mpFlow::numeric::ConjugateGradient::solve");
+    }
+    unsigned const rows;
+    unsigned const cols;
+};
+
+// numeric::BiCGSTAB (include/mpflow/numeric/bicgstab.h), as above
+template <class dataType>
+class BiCGSTAB {
+public:
+    BiCGSTAB(unsigned const rows, unsigned const cols, cudaStream_t const stream = nullptr) : rows(rows), cols(cols) {
+        (void)stream;
+        if (rows < 1) throw std::invalid_argument("mpFlow::numeric::BiCGSTAB::BiCGSTAB: rows <= 1");
+        if (cols < 1) throw std::invalid_argument("mpFlow::numeric::BiCGSTAB::BiCGSTAB: cols <= 1");
+    }
+    template <template <class> class matrixType, template <class> class preconditionerType = matrixType>
+    unsigned solve(std::shared_ptr<matrixType<dataType>> const A, std::shared_ptr<Matrix<dataType> const> const b,
+                   cublasHandle_t const handle, cudaStream_t const stream, std::shared_ptr<Matrix<dataType>> const x,
+                   std::shared_ptr<preconditionerType<dataType>> const KInv = nullptr, unsigned const maxIterations = 0,
+                   bool const dcFree = false) {
+        (void)handle;
+        (void)KInv;
+        return krylov::solve(1, A, b, stream, x, maxIterations, dcFree, "mpFlow::numeric::BiCGSTAB::solve");
+    }
+    unsigned const rows;
+    unsigned const cols;
+};
 
 // mpf_solve_opts::solver of a solver tag
 template <template <class> class S>

@@ -5,12 +5,12 @@ The numerics live in the CUDA library ``_lib/libmpflow_gb300.so`` (C ABI in
 package does not touch the GPU; the first call that needs the library loads
 it and raises if it is missing (there is no CPU fallback).
 """
-from .eit import (EIT, FIXED, EITBatch, OPEN, IrregularMesh, Ports, SolveOptions, Sources, adjacent_pattern,
-                  cholesky_solve_f64, data_rows, gram_split_bf16)
+from .eit import (EIT, FIXED, EITBatch, OPEN, IrregularMesh, Ports, SolveOptions, Sources, SparseMatrix,
+                  adjacent_pattern, cholesky_solve_f64, data_rows, gram_split_bf16)
 from ._ffi import MpfError, lib
 from .learned import MLP, generate_pairs, inclusion_frames, train_warm_start
 
-__all__ = ["EIT", "EITBatch", "IrregularMesh", "Ports", "Sources", "SolveOptions", "adjacent_pattern", "data_rows",
-           "gram_split_bf16", "cholesky_solve_f64", "MpfError", "lib", "OPEN", "FIXED", "MLP",
-           "generate_pairs", "inclusion_frames", "train_warm_start"]
+__all__ = ["EIT", "EITBatch", "SparseMatrix", "IrregularMesh", "Ports", "Sources", "SolveOptions",
+           "adjacent_pattern", "data_rows", "gram_split_bf16", "cholesky_solve_f64", "MpfError", "lib", "OPEN",
+           "FIXED", "MLP", "generate_pairs", "inclusion_frames", "train_warm_start"]
 __version__ = "0.1.0"

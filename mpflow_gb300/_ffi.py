@@ -98,6 +98,10 @@ SIGNATURES = {
     "mpf_eit_group_iterations": (_I, [_P, _P, _I, _P]),
     "mpf_eit_cg_variants": (_I, [_P, _P, _I, _P]),
     "mpf_inverse_solve": (_I, [_P, _I, _D, _I, _P, _P, _P, _P, _P]),
+    "mpf_sparse_create": (_I, [_I, _P, _P, ctypes.c_uint32, _P]),
+    "mpf_sparse_destroy": (_I, [_P]),
+    "mpf_sparse_multiply": (_I, [_P, _P, _I, _I, _P, _I, _P]),
+    "mpf_sparse_solve": (_I, [_P, _I, _P, _I, _P, _I, _I, _I, _D, _I, _P, _P]),
     "mpf_batch_create": (_I, [_P, _I, _P]),
     "mpf_batch_destroy": (_I, [_P]),
     "mpf_batch_forward": (_I, [_P, _I, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P]),

@@ -56,6 +56,11 @@ int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
 int wait_selftest(int timeoutUs, cudaStream_t s);
 int batch_create(mpf_eit* const* models, int count, mpf_batch** out);
+int sparse_create(int rows, const float* values, const uint32_t* columnIds, uint32_t density, mpf_sparse** out);
+void sparse_destroy(mpf_sparse* A);
+int sparse_multiply(mpf_sparse* A, const float* x, int ldx, int cols, float* y, int ldy, cudaStream_t s);
+int sparse_solve(mpf_sparse* A, int solver, const float* b, int ldb, float* x, int ldx, int cols, int maxIter,
+                 double tol, int dcFree, int32_t* iterations, cudaStream_t s);
 int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* V, const mpf_solve_opts* in,
                   mpf_solve_stats* stats, cudaStream_t s);
 int batch_iterations(mpf_batch* b, int32_t* out, int cap, int32_t* count);
@@ -269,6 +274,36 @@ int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_cg_variants: model == nullptr");
         return mpf::cg_variants(model, set, frames, get);
+    })
+}
+
+int mpf_sparse_create(int32_t rows, const float* values, const uint32_t* column_ids, uint32_t density,
+                      mpf_sparse_t* matrix) {
+    MPF_GUARD({ return mpf::sparse_create(rows, values, column_ids, density, matrix); })
+}
+
+int mpf_sparse_destroy(mpf_sparse_t matrix) {
+    MPF_GUARD({
+        mpf::sparse_destroy(matrix);
+        return MPF_OK;
+    })
+}
+
+int mpf_sparse_multiply(mpf_sparse_t matrix, const float* x, int32_t ldx, int32_t cols, float* y, int32_t ldy,
+                        mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(matrix, MPF_EINVAL, "mpFlow::numeric::SparseMatrix::multiply: matrix == nullptr");
+        return mpf::sparse_multiply(matrix, x, ldx, cols, y, ldy, (cudaStream_t)stream);
+    })
+}
+
+int mpf_sparse_solve(mpf_sparse_t matrix, int32_t solver, const float* b, int32_t ldb, float* x, int32_t ldx,
+                     int32_t cols, int32_t max_iter, double tol, int32_t dc_free, int32_t* iterations,
+                     mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(matrix, MPF_EINVAL, "mpFlow::numeric::ConjugateGradient::solve: A == nullptr");
+        return mpf::sparse_solve(matrix, solver, b, ldb, x, ldx, cols, max_iter, tol, dc_free, iterations,
+                                 (cudaStream_t)stream);
     })
 }
 

@@ -398,6 +398,72 @@ class EIT:
         return ms, by
 
 
+class SparseMatrix:
+    """numeric::SparseMatrix on the GPU (mpf_sparse_*): built from the
+    reference ELL layout (data_rows x 32 values and uint32 column ids,
+    0xFFFFFFFF padding) or from a dense matrix; multiply() and solve() with
+    CG or BiCGSTAB on column-major right-hand sides."""
+
+    INVALID = 0xFFFFFFFF
+
+    def __init__(self, values, column_ids, rows: int, density: int):
+        import torch
+        dr = data_rows(rows)
+        v = torch.as_tensor(np.ascontiguousarray(values, np.float32).reshape(dr, 32)).cuda()
+        c = torch.as_tensor(np.ascontiguousarray(column_ids, np.uint32).view(np.int32).reshape(dr, 32)).cuda()
+        self.rows, self.density = int(rows), int(density)
+        h = ctypes.c_void_p()
+        check(lib().mpf_sparse_create(self.rows, ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(c.data_ptr()),
+                                      self.density, ctypes.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def from_dense(A: np.ndarray) -> "SparseMatrix":
+        """SparseMatrix(Matrix) of the reference: the nonzeros of each row in
+        column order (src/numeric/sparse_matrix.cpp:137-160 via setValue)."""
+        A = np.asarray(A, np.float64)
+        n = A.shape[0]
+        dr = data_rows(n)
+        vals = np.zeros((dr, 32), np.float32)
+        ids = np.full((dr, 32), SparseMatrix.INVALID, np.uint32)
+        density = 0
+        for i in range(n):
+            nz = np.nonzero(A[i])[0]
+            if len(nz) > 32:
+                raise ValueError("mpFlow::numeric::SparseMatrix::setValue: sparse format full")
+            vals[i, :len(nz)] = A[i, nz]
+            ids[i, :len(nz)] = nz
+            density = max(density, len(nz))
+        return SparseMatrix(vals, ids, n, density)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().mpf_sparse_destroy(h)
+            self._h = None
+
+    def multiply(self, x):
+        """y = A x for a (rows x cols) float32 CUDA tensor."""
+        import torch
+        xc = x.reshape(self.rows, -1).t().contiguous()  # column-major storage
+        y = torch.empty_like(xc)
+        check(lib().mpf_sparse_multiply(self._h, ctypes.c_void_p(xc.data_ptr()), self.rows, xc.shape[0],
+                                        ctypes.c_void_p(y.data_ptr()), self.rows, _stream()))
+        return y.t()
+
+    def solve(self, b, x0=None, solver: str = "cg", dc_free: bool = False, max_iter: int = 0, tol: float = 0.0):
+        """x with A x = b for every column of a (rows x cols) float32 CUDA
+        tensor; returns (x, iterations of the slowest column)."""
+        import torch
+        bc = b.reshape(self.rows, -1).t().contiguous()
+        xc = torch.zeros_like(bc) if x0 is None else x0.reshape(self.rows, -1).t().contiguous().clone()
+        it = ctypes.c_int32(0)
+        check(lib().mpf_sparse_solve(self._h, SolveOptions.SOLVERS[solver], ctypes.c_void_p(bc.data_ptr()), self.rows,
+                                     ctypes.c_void_p(xc.data_ptr()), self.rows, bc.shape[0], int(max_iter), float(tol),
+                                     int(bool(dc_free)), ctypes.byref(it), _stream()))
+        return xc.t(), it.value
+
+
 class EITBatch:
     """Forward solves of several EIT models (meshes of uneven size, 16 or 32
     electrodes, one harmonic set) in the same CG launches (mpf_batch_*).

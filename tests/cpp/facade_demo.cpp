@@ -104,6 +104,39 @@ int main(int argc, char** argv) {
             }
         biErr /= std::max(vMax, 1e-300);
 
+        // standalone sparse matrix and solvers: a diagonally dominant 1-D
+        // Laplacian from a dense matrix, x = A^-1 b by CG and BiCGSTAB
+        const unsigned ns = 200, nrhs = 3;
+        auto dense = std::make_shared<numeric::Matrix<float>>(ns, ns, stream);
+        for (unsigned i = 0; i < ns; ++i) {
+            (*dense)(i, i) = 3.f;
+            if (i > 0) (*dense)(i, i - 1) = -1.f;
+            if (i + 1 < ns) (*dense)(i, i + 1) = -1.f;
+        }
+        dense->copyToDevice(stream);
+        auto As = std::make_shared<numeric::SparseMatrix<float>>(dense, stream);
+        auto bs = std::make_shared<numeric::Matrix<float>>(ns, nrhs, stream);
+        for (unsigned j = 0; j < nrhs; ++j)
+            for (unsigned i = 0; i < ns; ++i) (*bs)(i, j) = (float)std::sin(0.1 * (i + 1) * (j + 1));
+        bs->copyToDevice(stream);
+        double sparseErr = 0.0;
+        unsigned cgSteps = 0, biSteps = 0;
+        for (int which = 0; which < 2; ++which) {
+            auto xs = std::make_shared<numeric::Matrix<float>>(ns, nrhs, stream);
+            if (which == 0) {
+                numeric::ConjugateGradient<float> cg(ns, nrhs, stream);
+                cgSteps = cg.solve<numeric::SparseMatrix>(As, bs, handle, stream, xs);
+            } else {
+                numeric::BiCGSTAB<float> bi(ns, nrhs, stream);
+                biSteps = bi.solve<numeric::SparseMatrix>(As, bs, handle, stream, xs);
+            }
+            auto ys = std::make_shared<numeric::Matrix<float>>(ns, nrhs, stream);
+            As->multiply(xs, stream, ys);
+            ys->copyToHost(stream);
+            for (unsigned j = 0; j < nrhs; ++j)
+                for (unsigned i = 0; i < ns; ++i) sparseErr = std::max(sparseErr, (double)std::fabs((*ys)(i, j) - (*bs)(i, j)));
+        }
+
         // measurement: an inclusion of 0.5 S/m at (0.3, 0.2), radius 0.25
         auto target = std::make_shared<numeric::Matrix<float>>(E, 1, stream, 1.0f);
         std::vector<int> inside;
@@ -148,11 +181,13 @@ int main(int argc, char** argv) {
             for (unsigned j = 0; j < V0->cols; ++j) rt = std::max(rt, (double)std::fabs((*back)(i, j) - (*V0)(i, j)));
 
         const bool ok = steps > 0 && std::isfinite(sumAbs) && sumAbs > 0.0 && in < out && in < -0.01 &&
-                        rt <= 1e-6 * sumAbs && stepsBi > 0 && biErr <= 1e-5;
+                        rt <= 1e-6 * sumAbs && stepsBi > 0 && biErr <= 1e-5 && cgSteps > 0 && biSteps > 0 &&
+                        sparseErr <= 1e-5;
         printf("{\"steps\": %u, \"sum_v\": %.9e, \"sum_abs_v\": %.9e, \"mean_delta_inside\": %.6e, "
                "\"mean_delta_outside\": %.6e, \"text_roundtrip_max_err\": %.3e, \"bicgstab_steps\": %u, "
-               "\"bicgstab_rel_err\": %.3e, \"ok\": %s}\n",
-               steps, sumV, sumAbs, in, out, rt, stepsBi, biErr, ok ? "true" : "false");
+               "\"bicgstab_rel_err\": %.3e, \"sparse_cg_steps\": %u, \"sparse_bicgstab_steps\": %u, "
+               "\"sparse_residual\": %.3e, \"ok\": %s}\n",
+               steps, sumV, sumAbs, in, out, rt, stepsBi, biErr, cgSteps, biSteps, sparseErr, ok ? "true" : "false");
         return ok ? 0 : 1;
     } catch (std::exception const& ex) {
         printf("{\"error\": \"%s\", \"ok\": false}\n", ex.what());

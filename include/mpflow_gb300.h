@@ -339,6 +339,33 @@ int mpf_eit_group_iterations(mpf_eit_t model, int32_t* iterations, int32_t cap, 
 int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int32_t* get);
 
 /* ======================================================================== */
+/* Dense matrix operations (numeric::Matrix)                                 */
+/* ======================================================================== */
+
+/* Device operations of the reference's column-major dense Matrix
+ * (src/numeric/matrix.cpp, kernels src/numeric/matrix_kernel.cu:35-631) on
+ * rows x cols FP32 matrices with leading dimension ld (>= rows, the
+ * reference's dataRows).  op: 0 setEye (C = I), 1 diag (C = diagonal of A),
+ * 2 add scalar (C = A + scalar), 3 add (C = A + B), 4 scalarMultiply
+ * (C = scalar A), 5 elementwiseMultiply (C = A .* B), 6 elementwiseDivision
+ * (C = A ./ B, 0 where B = 0).  C may alias A. */
+int mpf_matrix_elementwise(int32_t op, int32_t rows, int32_t cols, const float* A, const float* B, float* C,
+                           int32_t ld, float scalar, mpf_stream_t stream);
+
+/* Column reductions into row 0 of each column of result (leading dimension
+ * ldr), as Matrix::sum / vectorDotProduct / min / max leave them
+ * (matrix.cpp:455-660): op 0 sum, 1 dot of A and B, 2 min, 3 max; FP64
+ * accumulation in a fixed order. */
+int mpf_matrix_column_reduce(int32_t op, int32_t rows, int32_t cols, const float* A, const float* B, int32_t ld,
+                             float* result, int32_t ldr, mpf_stream_t stream);
+
+/* Matrix::multiply's cuBLAS GEMM (matrix.cpp:298-332): C (m x n) =
+ * op(A) op(B) with op(X) = X (trans 0) or X^T (trans 1), column-major,
+ * FP32 on a tiled kernel of this library. */
+int mpf_matrix_multiply(int32_t trans_a, int32_t trans_b, int32_t m, int32_t n, int32_t k, const float* A,
+                        int32_t lda, const float* B, int32_t ldb, float* C, int32_t ldc, mpf_stream_t stream);
+
+/* ======================================================================== */
 /* Sparse matrices and Krylov solvers on a caller's matrix                   */
 /* ======================================================================== */
 

@@ -37,6 +37,10 @@
 #include "mpflow_gb300.h"
 
 typedef struct cublasContext* cublasHandle_t;  // accepted for signature compatibility, never used
+#ifndef CUBLAS_API_H_
+// the transposition flags of Matrix::multiply (values as cublas_api.h)
+typedef enum { CUBLAS_OP_N = 0, CUBLAS_OP_T = 1, CUBLAS_OP_C = 2 } cublasOperation_t;
+#endif
 
 namespace mpFlow {
 
@@ -288,6 +292,83 @@ public:
                      "mpFlow::numeric::Matrix::copy");
     }
 
+    // device arithmetic (src/numeric/matrix.cpp, FP32 matrices): through
+    // mpf_matrix_elementwise / mpf_matrix_column_reduce / mpf_matrix_multiply
+    void setEye(cudaStream_t const stream = nullptr) {
+        if (rows != cols) throw std::invalid_argument("mpFlow::numeric::Matrix::setEye: matrix not square");
+        elementwise(0, nullptr, nullptr, type(0), stream, "setEye");
+    }
+    void diag(std::shared_ptr<Matrix<type> const> const matrix, cudaStream_t const stream = nullptr) {
+        sameShape(matrix, "diag");
+        elementwise(1, matrix->deviceData, nullptr, type(0), stream, "diag");
+    }
+    void add(type const value, cudaStream_t const stream = nullptr) {
+        elementwise(2, deviceData, nullptr, value, stream, "add");
+    }
+    void add(std::shared_ptr<Matrix<type> const> const value, cudaStream_t const stream = nullptr) {
+        sameShape(value, "add");
+        elementwise(3, deviceData, value->deviceData, type(0), stream, "add");
+    }
+    void scalarMultiply(type const scalar, cudaStream_t const stream = nullptr) {
+        elementwise(4, deviceData, nullptr, scalar, stream, "scalarMultiply");
+    }
+    void elementwiseMultiply(std::shared_ptr<Matrix<type> const> const A, std::shared_ptr<Matrix<type> const> const B,
+                             cudaStream_t const stream = nullptr) {
+        sameShape(A, "elementwiseMultiply");
+        sameShape(B, "elementwiseMultiply");
+        elementwise(5, A->deviceData, B->deviceData, type(0), stream, "elementwiseMultiply");
+    }
+    void elementwiseDivision(std::shared_ptr<Matrix<type> const> const A, std::shared_ptr<Matrix<type> const> const B,
+                             cudaStream_t const stream = nullptr) {
+        sameShape(A, "elementwiseDivision");
+        sameShape(B, "elementwiseDivision");
+        elementwise(6, A->deviceData, B->deviceData, type(0), stream, "elementwiseDivision");
+    }
+    // column reductions into row 0 (src/numeric/matrix.cpp:455-660)
+    void vectorDotProduct(std::shared_ptr<Matrix<type> const> const A, std::shared_ptr<Matrix<type> const> const B,
+                          cudaStream_t const stream = nullptr) {
+        sameShape(A, "vectorDotProduct");
+        sameShape(B, "vectorDotProduct");
+        reduce(1, A, B->deviceData, stream, "vectorDotProduct");
+    }
+    void sum(std::shared_ptr<Matrix<type> const> const value, cudaStream_t const stream = nullptr) {
+        sameShape(value, "sum");
+        reduce(0, value, nullptr, stream, "sum");
+    }
+    void min(std::shared_ptr<Matrix<type> const> const value, cudaStream_t const stream = nullptr) {
+        sameShape(value, "min");
+        reduce(2, value, nullptr, stream, "min");
+    }
+    void max(std::shared_ptr<Matrix<type> const> const value, cudaStream_t const stream = nullptr) {
+        sameShape(value, "max");
+        reduce(3, value, nullptr, stream, "max");
+    }
+    // this = op(A) op(B) (src/numeric/matrix.cpp:298-332)
+    void multiply(std::shared_ptr<Matrix<type> const> const A, std::shared_ptr<Matrix<type> const> const B,
+                  cublasHandle_t const handle, cudaStream_t const stream = nullptr,
+                  cublasOperation_t const transA = CUBLAS_OP_N, cublasOperation_t const transB = CUBLAS_OP_N) {
+        (void)handle;
+        if (!A) throw std::invalid_argument("mpFlow::numeric::Matrix::multiply: A == nullptr");
+        if (!B) throw std::invalid_argument("mpFlow::numeric::Matrix::multiply: B == nullptr");
+        const bool ta = transA != CUBLAS_OP_N, tb = transB != CUBLAS_OP_N;
+        const unsigned m = ta ? A->cols : A->rows, k = ta ? A->rows : A->cols;
+        const unsigned kb = tb ? B->cols : B->rows, n = tb ? B->rows : B->cols;
+        if (k != kb || m != rows || n != cols)
+            throw std::invalid_argument("mpFlow::numeric::Matrix::multiply: shape does not match");
+        detail::check(mpf_matrix_multiply(ta ? 1 : 0, tb ? 1 : 0, (int32_t)m, (int32_t)n, (int32_t)k, A->deviceData,
+                                          (int32_t)A->dataRows, B->deviceData, (int32_t)B->dataRows, deviceData,
+                                          (int32_t)dataRows, stream),
+                      "mpFlow::numeric::Matrix::multiply");
+    }
+    // this = A B with a sparse A (src/numeric/matrix.cpp:335-349)
+    template <template <class> class SparseType>
+    void multiply(std::shared_ptr<SparseType<type> const> const A, std::shared_ptr<Matrix<type> const> const B,
+                  cublasHandle_t const handle, cudaStream_t const stream = nullptr) {
+        (void)handle;
+        if (!A) throw std::invalid_argument("mpFlow::numeric::Matrix::multiply: A == nullptr");
+        A->multiply(B, stream, std::shared_ptr<Matrix<type>>(this, [](Matrix<type>*) {}));
+    }
+
     type& operator()(unsigned const i, unsigned const j) {
         requireHost("operator()");
         if (i >= rows || j >= cols) throw std::invalid_argument("mpFlow::numeric::Matrix::operator(): index out of range");
@@ -361,6 +442,22 @@ private:
     void requireHost(const char* what) const {
         if (host_.empty())
             throw std::logic_error(std::string("mpFlow::numeric::Matrix::") + what + ": host memory was not allocated");
+    }
+    void sameShape(std::shared_ptr<Matrix<type> const> const& other, const char* what) const {
+        if (!other) throw std::invalid_argument(std::string("mpFlow::numeric::Matrix::") + what + ": matrix == nullptr");
+        if (other->rows != rows || other->cols != cols || other->dataRows != dataRows)
+            throw std::invalid_argument(std::string("mpFlow::numeric::Matrix::") + what + ": shape does not match");
+    }
+    void elementwise(int op, const type* A, const type* B, type scalar, cudaStream_t stream, const char* what) {
+        detail::check(mpf_matrix_elementwise(op, (int32_t)rows, (int32_t)cols, A, B, deviceData, (int32_t)dataRows,
+                                             (float)scalar, stream),
+                      (std::string("mpFlow::numeric::Matrix::") + what).c_str());
+    }
+    void reduce(int op, std::shared_ptr<Matrix<type> const> const& A, const type* B, cudaStream_t stream,
+                const char* what) {
+        detail::check(mpf_matrix_column_reduce(op, (int32_t)rows, (int32_t)cols, A->deviceData, B, (int32_t)dataRows,
+                                               deviceData, (int32_t)dataRows, stream),
+                      (std::string("mpFlow::numeric::Matrix::") + what).c_str());
     }
     mutable std::vector<type> host_;
 };

@@ -98,6 +98,9 @@ SIGNATURES = {
     "mpf_eit_group_iterations": (_I, [_P, _P, _I, _P]),
     "mpf_eit_cg_variants": (_I, [_P, _P, _I, _P]),
     "mpf_inverse_solve": (_I, [_P, _I, _D, _I, _P, _P, _P, _P, _P]),
+    "mpf_matrix_elementwise": (_I, [_I, _I, _I, _P, _P, _P, _I, ctypes.c_float, _P]),
+    "mpf_matrix_column_reduce": (_I, [_I, _I, _I, _P, _P, _I, _P, _I, _P]),
+    "mpf_matrix_multiply": (_I, [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P]),
     "mpf_sparse_create": (_I, [_I, _P, _P, ctypes.c_uint32, _P]),
     "mpf_sparse_destroy": (_I, [_P]),
     "mpf_sparse_multiply": (_I, [_P, _P, _I, _I, _P, _I, _P]),

@@ -56,6 +56,12 @@ int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
 int wait_selftest(int timeoutUs, cudaStream_t s);
 int batch_create(mpf_eit* const* models, int count, mpf_batch** out);
+int matrix_elementwise(int op, int rows, int cols, const float* A, const float* B, float* C, int ld, float scalar,
+                       cudaStream_t s);
+int matrix_column_reduce(int op, int rows, int cols, const float* A, const float* B, int ld, float* result, int ldr,
+                         cudaStream_t s);
+int matrix_multiply(int transA, int transB, int m, int n, int k, const float* A, int lda, const float* B, int ldb,
+                    float* C, int ldc, cudaStream_t s);
 int sparse_create(int rows, const float* values, const uint32_t* columnIds, uint32_t density, mpf_sparse** out);
 void sparse_destroy(mpf_sparse* A);
 int sparse_multiply(mpf_sparse* A, const float* x, int ldx, int cols, float* y, int ldy, cudaStream_t s);
@@ -274,6 +280,23 @@ int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_cg_variants: model == nullptr");
         return mpf::cg_variants(model, set, frames, get);
+    })
+}
+
+int mpf_matrix_elementwise(int32_t op, int32_t rows, int32_t cols, const float* A, const float* B, float* C,
+                           int32_t ld, float scalar, mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::matrix_elementwise(op, rows, cols, A, B, C, ld, scalar, (cudaStream_t)stream); })
+}
+
+int mpf_matrix_column_reduce(int32_t op, int32_t rows, int32_t cols, const float* A, const float* B, int32_t ld,
+                             float* result, int32_t ldr, mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::matrix_column_reduce(op, rows, cols, A, B, ld, result, ldr, (cudaStream_t)stream); })
+}
+
+int mpf_matrix_multiply(int32_t trans_a, int32_t trans_b, int32_t m, int32_t n, int32_t k, const float* A,
+                        int32_t lda, const float* B, int32_t ldb, float* C, int32_t ldc, mpf_stream_t stream) {
+    MPF_GUARD({
+        return mpf::matrix_multiply(trans_a, trans_b, m, n, k, A, lda, B, ldb, C, ldc, (cudaStream_t)stream);
     })
 }
 

@@ -301,6 +301,27 @@ def workload_config(a, frames):
             "l2": "CG working set > L2 (129 MB) at >= 8 frames per step"}
 
 
+def aggregate_over_ranks(total_ms, done, world, device):
+    """Whole-job figures of a replicas-only run: the slowest rank's time and
+    the frames all ranks finished (no collective on the data path; these two
+    reductions only report)."""
+    if world <= 1:
+        return float(total_ms), float(done)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(total_ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(done)], device=device, dtype=torch.float64)
+    dist.all_reduce(n)
+    return float(t.item()), float(n.item())
+
+
+def rank_frame_seed(rank, step):
+    """Seed of the held-out frames of one rank and step: every rank
+    reconstructs its own frames."""
+    return 1000 * (rank + 1) + step
+
+
 def timed_steps(nsteps, warmup, fn, barrier, stream, torch, lib):
     """Run fn(step) for every step between barriers, CUDA events around each
     call on `stream`; returns (per-step ms of the timed steps, their results,
@@ -354,7 +375,7 @@ def run_gb300(a):
         return
     lib = mp.lib()
     # held-out frames and their noise-free measurements (untimed)
-    truth = [synthetic_frames(cent, F, seed=1000 * (rank + 1) + s) for s in range(nsteps)]
+    truth = [synthetic_frames(cent, F, seed=rank_frame_seed(rank, s)) for s in range(nsteps)]
     ref_opts = mp.SolveOptions(tol=1e-5, refine_tol=1e-9, max_iter=6000, preconditioner=a.preconditioner)
     vmeas = [model.solve(torch.tensor(truth[s], device=dev), ref_opts).contiguous() for s in range(nsteps)]
     opts = mp.SolveOptions(tol=a.tol, max_iter=6000, preconditioner=a.preconditioner)
@@ -407,16 +428,9 @@ def run_gb300(a):
         return np.array(its), None, conv
 
     def summarise(times, results, frames_per_step):
-        total_ms = float(np.sum(times))
         done = float(sum(int(r[2].frames_converged) if hasattr(r[2], "frames_converged") else int(r[2])
                          for r in results))
-        if world > 1:
-            t = torch.tensor([total_ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total_ms = float(t.item())
-            n = torch.tensor([done], device=dev, dtype=torch.float64)
-            dist.all_reduce(n)
-            done = float(n.item())
+        total_ms, done = aggregate_over_ranks(float(np.sum(times)), done, world, dev)
         its = np.concatenate([r[0] for r in results])
         return {"value": done / (total_ms / 1e3), "ms_per_step": float(np.mean(times)),
                 "gn_updates_mean": float(its.mean()),
@@ -448,7 +462,8 @@ def run_gb300(a):
         if s >= a.warmup:
             e2e_ms.append(dt)
             e2e_frames += int(st.frames_converged)
-    e2e_value = e2e_frames * world / (sum(e2e_ms) / 1e3)
+    e2e_total, e2e_done = aggregate_over_ranks(sum(e2e_ms), e2e_frames, world, dev)
+    e2e_value = e2e_done / (e2e_total / 1e3)
 
     # roofline of the CG kernels (CUDA events on the launching stream)
     ms, by = model.profile_cg(torch.tensor(truth[0], device=dev), reps=10)
@@ -592,11 +607,7 @@ def run_uneven(a):
     cg_bytes = float(np.mean([c[1] for c in cg[a.warmup:]]))
 
     def max_over_ranks(ms):
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return ms
+        return aggregate_over_ranks(ms, 0.0, world, dev)[0]
 
     total_b = max_over_ranks(float(np.sum(t_b)))
     total_s = max_over_ranks(float(np.sum(t_s)))

@@ -612,6 +612,37 @@ private:
     mutable bool dirty_ = true;
 };
 
+// numeric::preconditioner::diagonal (src/numeric/preconditioner.cpp:23-76,
+// kernels src/numeric/preconditioner_kernel.cu:31-83): result = D^-1 as a
+// 1-slot sparse matrix (slot 0 column = row, value 1 / a_ii; the dense form
+// divides by a_ii as the reference does, the sparse form leaves 0 where the
+// row has no diagonal entry).  Computed on the host copies; the solvers of
+// this library apply the same Jacobi preconditioner internally.
+namespace preconditioner {
+template <class type>
+void diagonal(std::shared_ptr<Matrix<type> const> const matrix, cudaStream_t const stream,
+              std::shared_ptr<SparseMatrix<type>> const result) {
+    if (!matrix) throw std::invalid_argument("mpFlow::numeric::preconditioner::diagonal: matrix == nullptr");
+    if (!result) throw std::invalid_argument("mpFlow::numeric::preconditioner::diagonal: result == nullptr");
+    const_cast<Matrix<type>&>(*matrix).copyToHost(stream);
+    for (unsigned i = 0; i < matrix->rows && i < result->rows; ++i) result->setValue(i, i, type(1) / (*matrix)(i, i));
+    result->density = 1;
+    result->copyToDevice(stream);
+}
+template <class type>
+void diagonal(std::shared_ptr<SparseMatrix<type> const> const matrix, cudaStream_t const stream,
+              std::shared_ptr<SparseMatrix<type>> const result) {
+    if (!matrix) throw std::invalid_argument("mpFlow::numeric::preconditioner::diagonal: matrix == nullptr");
+    if (!result) throw std::invalid_argument("mpFlow::numeric::preconditioner::diagonal: result == nullptr");
+    for (unsigned i = 0; i < matrix->rows && i < result->rows; ++i) {
+        const type d = matrix->getValue(i, i);
+        result->setValue(i, i, d != type(0) ? type(1) / d : type(0));
+    }
+    result->density = 1;
+    result->copyToDevice(stream);
+}
+}  // namespace preconditioner
+
 namespace krylov {
 // numeric::ConjugateGradient / numeric::BiCGSTAB solve through mpf_sparse_solve
 template <class dataType>

@@ -115,6 +115,9 @@ int main(int argc, char** argv) {
         }
         dense->copyToDevice(stream);
         auto As = std::make_shared<numeric::SparseMatrix<float>>(dense, stream);
+        auto KInv = std::make_shared<numeric::SparseMatrix<float>>(ns, ns, stream);
+        numeric::preconditioner::diagonal<float>(std::shared_ptr<numeric::SparseMatrix<float> const>(As), stream, KInv);
+        const bool precondOk = KInv->density == 1 && std::fabs(KInv->getValue(5, 5) - 1.f / 3.f) < 1e-7f;
         auto bs = std::make_shared<numeric::Matrix<float>>(ns, nrhs, stream);
         for (unsigned j = 0; j < nrhs; ++j)
             for (unsigned i = 0; i < ns; ++i) (*bs)(i, j) = (float)std::sin(0.1 * (i + 1) * (j + 1));
@@ -125,7 +128,7 @@ int main(int argc, char** argv) {
             auto xs = std::make_shared<numeric::Matrix<float>>(ns, nrhs, stream);
             if (which == 0) {
                 numeric::ConjugateGradient<float> cg(ns, nrhs, stream);
-                cgSteps = cg.solve<numeric::SparseMatrix>(As, bs, handle, stream, xs);
+                cgSteps = cg.solve<numeric::SparseMatrix>(As, bs, handle, stream, xs, KInv);
             } else {
                 numeric::BiCGSTAB<float> bi(ns, nrhs, stream);
                 biSteps = bi.solve<numeric::SparseMatrix>(As, bs, handle, stream, xs);
@@ -182,7 +185,7 @@ int main(int argc, char** argv) {
 
         const bool ok = steps > 0 && std::isfinite(sumAbs) && sumAbs > 0.0 && in < out && in < -0.01 &&
                         rt <= 1e-6 * sumAbs && stepsBi > 0 && biErr <= 1e-5 && cgSteps > 0 && biSteps > 0 &&
-                        sparseErr <= 1e-5;
+                        sparseErr <= 1e-5 && precondOk;
         printf("{\"steps\": %u, \"sum_v\": %.9e, \"sum_abs_v\": %.9e, \"mean_delta_inside\": %.6e, "
                "\"mean_delta_outside\": %.6e, \"text_roundtrip_max_err\": %.3e, \"bicgstab_steps\": %u, "
                "\"bicgstab_rel_err\": %.3e, \"sparse_cg_steps\": %u, \"sparse_bicgstab_steps\": %u, "

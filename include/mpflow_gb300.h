@@ -480,8 +480,9 @@ int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const
 /* Batched FP64 Cholesky solve of (A + shift I) X = B, A n x n symmetric
  * (row-major == column-major), B n x nrhs column-major, per batch entry.
  * A is overwritten by its factor.  info[batch] (device ints) receives 0 or
- * the 1-based index of the first non-positive pivot.  Replaces the dense CG
- * of Inverse::solve (src/solver/inverse.cpp:213-238). */
+ * the 1-based index of the first non-positive pivot.  n must be a multiple
+ * of 32 and at most 4864.  Replaces the dense CG of Inverse::solve
+ * (src/solver/inverse.cpp:213-238). */
 int mpf_cholesky_solve_f64(int32_t batch, int32_t n, double* A, double shift, double* B,
                            int32_t nrhs, int32_t* info, mpf_stream_t stream);
 

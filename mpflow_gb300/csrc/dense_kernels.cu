@@ -343,31 +343,79 @@ __global__ void k_syrk(int n, double* A, int k, const int* frameMask) {
     }
 }
 
-// Forward then backward substitution with L (column-major lower), one block
-// per (batch, right-hand side).
-__global__ void k_chol_solve(int n, const double* __restrict__ Lall, double* __restrict__ Ball, int nrhs,
-                             const int* __restrict__ frameMask) {
+// L L^T x = b with L column-major lower, one block of 256 threads per
+// (batch, right-hand side), in 32-row block steps.  Every read of L runs
+// down a column (consecutive threads, consecutive rows): the forward pass
+// is right-looking (after solving block k, the rows below it take
+// x[r] -= L[r][k-block] x[k-block]), the backward pass left-looking (block
+// k's columns take warp-reduced dots with the solved rows below).  The
+// 32 x 32 diagonal block is staged in shared memory and solved by one warp
+// with shuffles.
+__global__ void __launch_bounds__(256) k_chol_solve(int n, const double* __restrict__ Lall, double* __restrict__ Ball,
+                                                    int nrhs, const int* __restrict__ frameMask) {
     if (frameMask && !frameMask[blockIdx.x / nrhs]) return;
     extern __shared__ double x[];
+    __shared__ double D[NB][NB + 1];
     const int b = blockIdx.x / nrhs, c = blockIdx.x % nrhs;
     const double* L = Lall + (size_t)b * n * n;
     double* B = Ball + ((size_t)b * nrhs + c) * n;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = B[i];
+    const int nb = n / NB;
+    // forward: L z = b
+    for (int bk = 0; bk < nb; ++bk) {
+        const int k0 = bk * NB;
+        for (int i = threadIdx.x; i < NB * NB; i += blockDim.x) {
+            const int r = i % NB, cc = i / NB;
+            D[r][cc] = L[(size_t)(k0 + r) + (size_t)(k0 + cc) * n];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double xr = x[k0 + lane];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                if (lane == j) xr /= D[j][j];
+                const double xj = __shfl_sync(0xffffffffu, xr, j);
+                if (lane > j) xr -= D[lane][j] * xj;
+            }
+            x[k0 + lane] = xr;
+        }
+        __syncthreads();
+        for (int r = k0 + NB + threadIdx.x; r < n; r += blockDim.x) {
+            double s = 0.0;
+#pragma unroll 8
+            for (int j = 0; j < NB; ++j) s = fma(L[(size_t)r + (size_t)(k0 + j) * n], x[k0 + j], s);
+            x[r] -= s;
+        }
+    }
+    // backward: L^T x = z
+    for (int bk = nb - 1; bk >= 0; --bk) {
+        const int k0 = bk * NB, below = k0 + NB;
+        __syncthreads();
+        for (int cc = warp; cc < NB; cc += nwarps) {
+            const int col = k0 + cc;
+            double s = 0.0;
+            for (int r = below + lane; r < n; r += 32) s = fma(L[(size_t)r + (size_t)col * n], x[r], s);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) x[col] -= s;
+        }
+        for (int i = threadIdx.x; i < NB * NB; i += blockDim.x) {
+            const int r = i % NB, cc = i / NB;
+            D[r][cc] = L[(size_t)(k0 + r) + (size_t)(k0 + cc) * n];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double xc = x[k0 + lane];
+#pragma unroll
+            for (int j = NB - 1; j >= 0; --j) {
+                if (lane == j) xc /= D[j][j];
+                const double xj = __shfl_sync(0xffffffffu, xc, j);
+                if (lane < j) xc -= D[j][lane] * xj;
+            }
+            x[k0 + lane] = xc;
+        }
+    }
     __syncthreads();
-    for (int j = 0; j < n; ++j) {
-        const double xj = x[j] / L[(size_t)j + (size_t)j * n];
-        __syncthreads();
-        if (threadIdx.x == 0) x[j] = xj;
-        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) x[i] -= L[(size_t)i + (size_t)j * n] * xj;
-        __syncthreads();
-    }
-    for (int j = n - 1; j >= 0; --j) {
-        const double xj = x[j] / L[(size_t)j + (size_t)j * n];
-        __syncthreads();
-        if (threadIdx.x == 0) x[j] = xj;
-        for (int i = threadIdx.x; i < j; i += blockDim.x) x[i] -= L[(size_t)j + (size_t)i * n] * xj;
-        __syncthreads();
-    }
     for (int i = threadIdx.x; i < n; i += blockDim.x) B[i] = x[i];
 }
 
@@ -630,8 +678,9 @@ int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s, c
 
 int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s,
                              const int* frameMask) {
-    MPF_CHECK((size_t)n * sizeof(double) <= 48 * 1024, MPF_EINVAL, "cholesky solve: n too large (%d)", n);
-    k_chol_solve<<<batch * nrhs, 512, n * sizeof(double), s>>>(n, L, B, nrhs, frameMask);
+    MPF_CHECK((size_t)n * sizeof(double) <= 38 * 1024 && n % NB == 0, MPF_EINVAL,
+              "cholesky solve: n must be a multiple of %d and at most 4864 (%d)", NB, n);
+    k_chol_solve<<<batch * nrhs, 256, n * sizeof(double), s>>>(n, L, B, nrhs, frameMask);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

@@ -102,22 +102,23 @@ def test_gram_split_bf16_accuracy():
     assert err < 3e-5, err
 
 
-def test_cholesky_f64():
+@pytest.mark.parametrize("n,nrhs", [(32, 1), (256, 1), (1024, 1), (160, 3)])
+def test_cholesky_f64(n, nrhs):
     import mpflow_gb300 as mp
     torch = _torch()
-    rng = np.random.default_rng(5)
-    n = 256
+    rng = np.random.default_rng(5 + n)
     X = rng.standard_normal((3, n, n))
     A = np.einsum("bij,bkj->bik", X, X) / n
-    b = rng.standard_normal((3, 1, n))
+    b = rng.standard_normal((3, nrhs, n))
     At = torch.tensor(A, device="cuda")
     Bt = torch.tensor(b, device="cuda")
     info = mp.cholesky_solve_f64(At, Bt, shift=0.5)
     assert int(info.abs().sum()) == 0
     x = Bt.cpu().numpy()
     for k in range(3):
-        ref = np.linalg.solve(A[k] + 0.5 * np.eye(n), b[k, 0])
-        assert rel_err(x[k, 0], ref) < 1e-10
+        for c in range(nrhs):
+            ref = np.linalg.solve(A[k] + 0.5 * np.eye(n), b[k, c])
+            assert rel_err(x[k, c], ref) < 1e-10
 
 
 def test_gn_step_matches_oracle_dual():

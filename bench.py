@@ -84,6 +84,9 @@ def parse_args():
                    help="training pairs of the learned warm start, generated by the forward solver")
     p.add_argument("--epochs", type=int, default=80)
     p.add_argument("--hidden", type=int, default=2048, help="hidden width of the warm-start network")
+    p.add_argument("--learned-prior", choices=["on", "off"], default="on",
+                   help="on: the network learns the correction to the linear one-step GN prior "
+                        "(mpf_eit_learned_prior); off: it predicts gamma alone")
     p.add_argument("--single-frames", type=int, default=4,
                    help="frames per step timed one at a time on the plain GN path (0: skip)")
     p.add_argument("--profile-only", action="store_true",
@@ -346,7 +349,7 @@ def run_gb300(a):
     import torch
     import torch.distributed as dist
     import mpflow_gb300 as mp
-    from mpflow_gb300.learned import generate_pairs, inclusion_frames, round_up, train_warm_start
+    from mpflow_gb300.learned import generate_pairs, inclusion_frames, round_up, train_warm_start, zero_network
 
     rank, world, local = dist_env()
     if world > 1:
@@ -394,9 +397,16 @@ def run_gb300(a):
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     L = Vtr.shape[1] * Vtr.shape[2]
+    use_prior = a.learned_prior == "on"
+    prior_s = None
+    if use_prior:
+        t0 = time.perf_counter()
+        model.learned_prior(lam)
+        prior_s = time.perf_counter() - t0
     net = mp.MLP(L, a.hidden, a.hidden, round_up(E, 128), seed=17 + rank)
     losses, train_s = train_warm_start(model, net, Vtr, gtr, epochs=a.epochs, batch=256, lr=1e-3,
-                                       snr_db=60.0, seed=rank)
+                                       snr_db=60.0, seed=rank, prior=use_prior)
+    net0 = zero_network(L, round_up(E, 128)) if use_prior else None
     train_steps = a.epochs * max(1, a.train_pairs // 256)
     del Vtr, gtr
 
@@ -409,6 +419,11 @@ def run_gb300(a):
 
     def learned_step(s):
         _, it, res, acc, st = model.gn_solve_learned(net, vmeas[s], lam, target=a.target, max_iters=a.max_gn,
+                                                     options=gn_opts)
+        return it, acc, st
+
+    def prior_step(s):
+        _, it, res, acc, st = model.gn_solve_learned(net0, vmeas[s], lam, target=a.target, max_iters=a.max_gn,
                                                      options=gn_opts)
         return it, acc, st
 
@@ -433,12 +448,16 @@ def run_gb300(a):
         total_ms, done = aggregate_over_ranks(float(np.sum(times)), done, world, dev)
         its = np.concatenate([r[0] for r in results])
         return {"value": done / (total_ms / 1e3), "ms_per_step": float(np.mean(times)),
-                "gn_updates_mean": float(its.mean()),
+                "gn_updates_mean": float(its.mean()), "no_update_fraction": float(np.mean(its == 0)),
                 "frames_converged_fraction": done / (frames_per_step * world * len(results))}
 
     with ClockSampler(local) as clocks:
         t_l, r_l, launches = timed_steps(nsteps, a.warmup, learned_step, barrier, stream, torch, lib)
         t_p, r_p, _ = timed_steps(nsteps, a.warmup, plain_step, barrier, stream, torch, lib)
+        prior_only = None
+        if use_prior:
+            t_q, r_q, _ = timed_steps(nsteps, a.warmup, prior_step, barrier, stream, torch, lib)
+            prior_only = summarise(t_q, r_q, F)
         single = None
         if a.single_frames > 0:
             t_s, r_s, _ = timed_steps(nsteps, a.warmup, single_step, barrier, stream, torch, lib)
@@ -492,7 +511,9 @@ def run_gb300(a):
         "data": "synthetic (seeded inclusion frames; V_meas noise-free from the FP64-refined forward model; "
                 "training pairs from the forward model with 60 dB noise)",
         "config": workload_config(a, F),
-        "method": "learned warm start + batched GN (plain GN fallback per frame)",
+        "method": ("learned warm start = linear one-step GN prior from the homogeneous point + trained network "
+                   "correction" if use_prior else "learned warm start (network alone)")
+                  + "; batched GN from it (plain GN restart per frame when the start does not lower the residual)",
         "cg_preconditioner": a.preconditioner,
         "gn_first_solve_start": a.gn_warm_start,
         "gn_updates_mean": learned["gn_updates_mean"],
@@ -502,7 +523,12 @@ def run_gb300(a):
                     "train_pairs": a.train_pairs, "pair_generation_s": gen_s, "epochs": a.epochs,
                     "train_s": train_s, "train_steps": train_steps, "loss_first": losses[0],
                     "loss_last": losses[-1], "network": f"{L}-{a.hidden}-{a.hidden}-{round_up(E, 128)} GELU",
-                    "train_tflops": mlp_flops / train_s / 1e12},
+                    "train_tflops": mlp_flops / train_s / 1e12,
+                    "prior": ({"lambda": lam, "setup_s": prior_s,
+                               "what": "J0^T (J0 J0^T + mu I)^-1 at the homogeneous point, FP64 Gram/Cholesky, "
+                                       "applied as an FP32 GEMM"} if use_prior else None),
+                    "no_update_fraction": learned["no_update_fraction"]},
+        "prior_only_gn_batched": prior_only,
         "plain_gn_batched": plain,
         "plain_gn_single_frame": single,
         "learned_vs_plain_batched": learned["value"] / plain["value"],

@@ -536,8 +536,27 @@ int mpf_mlp_params(mpf_mlp_t net, float* buffer, int32_t which, mpf_stream_t str
 int mpf_eit_learned_input(mpf_eit_t model, int32_t frames, const float* v_meas, float* x,
                           mpf_stream_t stream);
 
+/* Linear prior of the learned start: the first Gauss-Newton update from the
+ * homogeneous distribution gamma_h, which is linear in the network input x,
+ *   prior(x) = gamma_h + J0^T (J0 J0^T + mu I)^-1 x / rms-scale,
+ * mu = (referenceValue lambda)^2 as in mpf_gn_step, J0 the FP32 Jacobian at
+ * gamma_h with the Gram and its Cholesky factor in FP64 (the fixed part of
+ * Solver::solveAbsolute's first iteration, src/solver/solver.cpp:196-225,
+ * taken once per model).  Held by the model as an n_elements x (meas_count
+ * * drive_count) FP32 matrix; lambda = 0 removes it.  While a prior is set,
+ * mpf_gn_solve_learned starts from prior(x) + net(x), so the network learns
+ * the correction to the linear step.  Synchronises. */
+int mpf_eit_learned_prior(mpf_eit_t model, double lambda, mpf_stream_t stream);
+
+/* out (device, frames x ldo, ldo >= n_elements) = prior(x) (mode 0),
+ * out += prior(x) (mode 1) or out -= prior(x) (mode -1); x device, frames x
+ * (meas_count * drive_count).  MPF_EINVAL when no prior is set. */
+int mpf_eit_learned_prior_apply(mpf_eit_t model, int32_t frames, const float* x, float* out, int32_t ldo,
+                                int32_t mode, mpf_stream_t stream);
+
 /* Gauss-Newton from a learned start.  gamma (device, frames x n_elements,
- * output) starts as the network's prediction for each frame's voltages; a
+ * output) starts as the network's prediction for each frame's voltages (plus
+ * the linear prior when one is set, mpf_eit_learned_prior); a
  * frame keeps it only if its relative data residual there is below the
  * homogeneous start's, otherwise it restarts from the homogeneous
  * distribution (accepted[f] = 0).  Then mpf_gn_solve iterations to `target`.

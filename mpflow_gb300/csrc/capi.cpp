@@ -84,6 +84,8 @@ int mlp_backward(mpf_mlp* n, int batch, const float* x, const float* target, int
 int mlp_adam(mpf_mlp* n, float lr, float beta1, float beta2, float eps, float weightDecay, cudaStream_t s);
 int mlp_params(mpf_mlp* n, float* buf, int which, cudaStream_t s);
 int learned_input(mpf_eit* m, int F, const float* vMeas, float* x, cudaStream_t s);
+int learned_prior(mpf_eit* m, double lambda, cudaStream_t s);
+int learned_prior_apply(mpf_eit* m, int F, const float* x, float* out, int ldo, int mode, cudaStream_t s);
 int gn_solve_learned(mpf_eit* m, mpf_mlp* net, int F, float* gamma, const float* vMeas, double lambda,
                      double target, int maxIters, const mpf_solve_opts* o, int32_t* itersOut, double* resOut,
                      int32_t* accepted, mpf_gn_stats* stats, cudaStream_t s);
@@ -459,6 +461,21 @@ int mpf_eit_learned_input(mpf_eit_t model, int32_t frames, const float* v_meas, 
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_learned_input: model == nullptr");
         return mpf::learned_input(model, frames, v_meas, x, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_learned_prior(mpf_eit_t model, double lambda, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_learned_prior: model == nullptr");
+        return mpf::learned_prior(model, lambda, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_learned_prior_apply(mpf_eit_t model, int32_t frames, const float* x, float* out, int32_t ldo,
+                                int32_t mode, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_learned_prior_apply: model == nullptr");
+        return mpf::learned_prior_apply(model, frames, x, out, ldo, mode, (cudaStream_t)stream);
     })
 }
 

@@ -105,6 +105,11 @@ struct mpf_eit {
     float v0InvRms = 1.f;
     mpf::DevBuf<float> V0, X0, learnX;
     mpf::DevBuf<double> res0;
+    // linear prior of the learned start (mpf_eit_learned_prior): W = J0^T
+    // (J0 J0^T + mu I)^-1 / invRms, column-major E x L with ld Epad
+    bool priorReady = false;
+    double priorLambda = 0.0;
+    mpf::DevBuf<float> priorW;
 
     ~mpf_eit() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);

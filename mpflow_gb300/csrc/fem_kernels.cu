@@ -2,6 +2,8 @@
 // layout exports and the Gauss-Newton residual / parameter update.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "model.h"
 
 namespace mpf {
@@ -341,6 +343,21 @@ __global__ void __launch_bounds__(256) k_learned_input(int L, const float* __res
     if (threadIdx.x == 0 && res0) res0[f] = red[1][0] > 0.0 ? sqrt(red[0][0] / red[1][0]) : 0.0;
 }
 
+// Unit right-hand sides of the learned start's linear prior: column i of B
+// (rowsJ x Mm*Md) is e_{row(i)}, row(i) = m + d * MP the Jacobian row of
+// measurement i = m + d * Mm.
+__global__ void k_prior_rhs(int rowsJ, int Mm, int MP, int L, double* __restrict__ B) {
+    const int i = blockIdx.y;
+    const int row = i % Mm + (i / Mm) * MP;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rowsJ; r += gridDim.x * blockDim.x)
+        B[(size_t)i * rowsJ + r] = r == row ? 1.0 : 0.0;
+}
+
+__global__ void k_prior_convert(size_t count, const double* __restrict__ B, double scale, float* __restrict__ Q) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < count; k += (size_t)gridDim.x * blockDim.x)
+        Q[k] = (float)(B[k] * scale);
+}
+
 }  // namespace
 
 int fem_launch_assemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib,
@@ -451,6 +468,21 @@ int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const __nv_bfloat
 
 int fem_launch_fill_frames(int F, int E, const int* frameMask, float value, float* gamma, cudaStream_t s) {
     k_fill_frames<<<dim3((E + 255) / 256, F), 256, 0, s>>>(E, frameMask, value, gamma);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int fem_launch_prior_rhs(int rowsJ, int Mm, int Md, double* B, cudaStream_t s) {
+    const int MP = rowsJ / (int)data_rows((uint32_t)Md);
+    MPF_CHECK(MP >= Mm && Mm * Md <= 65535, MPF_EINVAL, "learned prior: %d x %d measurements", Mm, Md);
+    k_prior_rhs<<<dim3((rowsJ + 255) / 256, Mm * Md), 256, 0, s>>>(rowsJ, Mm, MP, Mm * Md, B);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int fem_launch_prior_convert(int rowsJ, int L, const double* B, double scale, float* Q, cudaStream_t s) {
+    const size_t count = (size_t)rowsJ * L;
+    k_prior_convert<<<(int)std::min<size_t>((count + 255) / 256, 4096), 256, 0, s>>>(count, B, scale, Q);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

@@ -63,11 +63,12 @@ __global__ void __launch_bounds__(256) k_mat_column_reduce(int op, int rows, con
     if (threadIdx.x == 0) result[(size_t)c * ldr] = (float)red[0];
 }
 
-// C (m x n) = op(A) op(B), op(X) = X or X^T; 64 x 64 tiles, 256 threads with
-// 4 x 4 outputs each, k in chunks of 16 through shared memory
-__global__ void __launch_bounds__(256) k_mat_gemm(int transA, int transB, int m, int n, int k,
+// C (m x n) = alpha op(A) op(B) + beta C (C not read when beta == 0),
+// op(X) = X or X^T; 64 x 64 tiles, 256 threads with 4 x 4 outputs each, k in
+// chunks of 16 through shared memory
+__global__ void __launch_bounds__(256) k_mat_gemm(int transA, int transB, int m, int n, int k, float alpha,
                                                   const float* __restrict__ A, int lda, const float* __restrict__ B,
-                                                  int ldb, float* __restrict__ C, int ldc) {
+                                                  int ldb, float beta, float* __restrict__ C, int ldc) {
     __shared__ float As[16][65], Bs[16][65];
     const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -103,7 +104,10 @@ __global__ void __launch_bounds__(256) k_mat_gemm(int transA, int transB, int m,
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int i = i0 + ty + 16 * p, j = j0 + tx + 16 * q;
-            if (i < m && j < n) C[(size_t)j * ldc + i] = acc[p][q];
+            if (i < m && j < n) {
+                float* c = C + (size_t)j * ldc + i;
+                *c = beta == 0.f ? alpha * acc[p][q] : fmaf(alpha, acc[p][q], beta * *c);
+            }
         }
 }
 
@@ -131,15 +135,22 @@ int matrix_column_reduce(int op, int rows, int cols, const float* A, const float
     return MPF_OK;
 }
 
-int matrix_multiply(int transA, int transB, int m, int n, int k, const float* A, int lda, const float* B, int ldb,
-                    float* C, int ldc, cudaStream_t s) {
+int matrix_multiply_scaled(int transA, int transB, int m, int n, int k, float alpha, const float* A, int lda,
+                           const float* B, int ldb, float beta, float* C, int ldc, cudaStream_t s) {
     MPF_CHECK(m >= 1 && n >= 1 && k >= 1 && A && B && C && ldc >= m, MPF_EINVAL,
               "mpFlow::numeric::Matrix::multiply: bad arguments");
     MPF_CHECK(lda >= (transA ? k : m) && ldb >= (transB ? n : k), MPF_EINVAL,
               "mpFlow::numeric::Matrix::multiply: leading dimension too small");
-    k_mat_gemm<<<dim3((m + 63) / 64, (n + 63) / 64), 256, 0, s>>>(transA, transB, m, n, k, A, lda, B, ldb, C, ldc);
+    MPF_CHECK((n + 63) / 64 <= 65535, MPF_EINVAL, "mpFlow::numeric::Matrix::multiply: %d columns exceed the grid", n);
+    k_mat_gemm<<<dim3((m + 63) / 64, (n + 63) / 64), 256, 0, s>>>(transA, transB, m, n, k, alpha, A, lda, B, ldb,
+                                                                  beta, C, ldc);
     MPF_LAUNCHED(1);
     return MPF_OK;
+}
+
+int matrix_multiply(int transA, int transB, int m, int n, int k, const float* A, int lda, const float* B, int ldb,
+                    float* C, int ldc, cudaStream_t s) {
+    return matrix_multiply_scaled(transA, transB, m, n, k, 1.f, A, lda, B, ldb, 0.f, C, ldc, s);
 }
 
 }  // namespace mpf

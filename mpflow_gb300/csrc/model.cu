@@ -879,7 +879,17 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
             if (nrej) {
                 MPF_CUDA(cudaMemcpyAsync(m->frameMask.ptr, reject.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
                 MPF_TRY(fem_launch_fill_frames(F, m->E, m->frameMask.ptr, gamma0, gamma, s));
-                continue;  // re-solve the restarted frames (the others start warm and converged)
+                // a restarted frame begins from the homogeneous fields, which
+                // already solve its system: the re-solve below converges at
+                // once for every frame
+                if (m->v0Ready) {
+                    const size_t per = (size_t)m->Ca * m->npad * m->KP;
+                    for (int f = 0; f < F; ++f)
+                        if (reject[f])
+                            MPF_CUDA(cudaMemcpyAsync(m->X.ptr + f * per, m->X0.ptr, per * sizeof(float),
+                                                     cudaMemcpyDeviceToDevice, s));
+                }
+                continue;
             }
         }
         int live = 0;
@@ -956,6 +966,70 @@ int learned_input(mpf_eit* m, int F, const float* vMeas, float* x, cudaStream_t 
     return fem_launch_learned_input(F, m->Mm * m->Md, vMeas, m->V0.ptr, m->v0InvRms, x, nullptr, s);
 }
 
+// Linear prior of the learned start: the first Gauss-Newton update from the
+// homogeneous distribution gamma_h as a fixed linear map of the network input
+// x = (v - V0) invRms,
+//   prior(x) = gamma_h + J0^T (J0 J0^T + mu I)^-1 x / invRms,  mu = (ref lambda)^2,
+// J0 the FP32 Jacobian at gamma_h, the Gram J0 J0^T in FP64 and its inverse
+// from the FP64 Cholesky factor.  Stored as W = J0^T (J0 J0^T + mu I)^-1 /
+// invRms restricted to the measurement rows (E x L, column-major).
+int learned_prior(mpf_eit* m, double lambda, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(lambda >= 0.0 && std::isfinite(lambda), MPF_EINVAL, "mpf_eit_learned_prior: lambda must be >= 0");
+    m->priorReady = false;
+    if (lambda == 0.0) {
+        m->priorW.release();
+        return MPF_OK;
+    }
+    MPF_TRY(ensure_v0(m, s));
+    const int L = m->Mm * m->Md, R = m->rowsJ;
+    DevBuf<float> g0, Q;
+    DevBuf<double> A0, B;
+    DevBuf<int> info;
+    MPF_TRY(g0.alloc((size_t)m->E));
+    MPF_TRY(fem_launch_fill_frames(1, m->E, nullptr, homogeneous_gamma(m), g0.ptr, s));
+    mpf_solve_opts o{};
+    o.tol = 1e-6;
+    o.refine_tol = 1e-9;
+    MPF_TRY(eit_forward_ws(m, 1, g0.ptr, false, &o, nullptr, s));
+    MPF_TRY(eit_jacobian(m, 1, g0.ptr, nullptr, true, s));
+    const double mu = (double)m->ref * lambda * (double)m->ref * lambda;
+    MPF_TRY(A0.alloc((size_t)R * R));
+    MPF_TRY(info.alloc(1));
+    MPF_TRY(dense_gram_f64_exact(1, R, m->Epad, m->J.ptr, m->Epad, mu, A0.ptr, nullptr, s));
+    MPF_TRY(dense_cholesky_f64(1, R, A0.ptr, info.ptr, s));
+    int hinfo = 0;
+    MPF_CUDA(cudaMemcpyAsync(&hinfo, info.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    MPF_CHECK(hinfo == 0, MPF_EBREAKDOWN, "learned prior: Cholesky of J0 J0^T + mu I failed at pivot %d", hinfo);
+    MPF_TRY(B.alloc((size_t)R * L));
+    MPF_TRY(Q.alloc((size_t)R * L));
+    MPF_TRY(fem_launch_prior_rhs(R, m->Mm, m->Md, B.ptr, s));
+    MPF_TRY(dense_cholesky_solve_f64(1, R, A0.ptr, B.ptr, L, s));
+    MPF_TRY(fem_launch_prior_convert(R, L, B.ptr, 1.0 / (double)m->v0InvRms, Q.ptr, s));
+    MPF_TRY(m->priorW.alloc((size_t)m->Epad * L));
+    MPF_TRY(matrix_multiply_scaled(0, 0, m->E, L, R, 1.f, m->J.ptr, m->Epad, Q.ptr, R, 0.f, m->priorW.ptr, m->Epad,
+                                   s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    m->priorLambda = lambda;
+    m->priorReady = true;
+    return MPF_OK;
+}
+
+// out (frames x ldo) = prior(x) (mode 0), += prior(x) (mode 1) or -= prior(x) (mode -1)
+int learned_prior_apply(mpf_eit* m, int F, const float* x, float* out, int ldo, int mode, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(m->priorReady, MPF_EINVAL, "mpf_eit_learned_prior_apply: no prior (call mpf_eit_learned_prior first)");
+    MPF_CHECK(F >= 1 && x && out && ldo >= m->E && mode >= -1 && mode <= 1, MPF_EINVAL,
+              "mpf_eit_learned_prior_apply: bad arguments");
+    const int L = m->Mm * m->Md;
+    const float alpha = mode < 0 ? -1.f : 1.f, beta = mode == 0 ? 0.f : 1.f;
+    MPF_TRY(matrix_multiply_scaled(0, 0, m->E, F, L, alpha, m->priorW.ptr, m->Epad, x, L, beta, out, ldo, s));
+    const float gh = homogeneous_gamma(m);
+    if (gh != 0.f) MPF_TRY(matrix_elementwise(2, m->E, F, out, nullptr, out, ldo, alpha * gh, s));
+    return MPF_OK;
+}
+
 int gn_solve_learned(mpf_eit* m, mpf_mlp* net, int F, float* gamma, const float* vMeas, double lambda,
                      double target, int maxIters, const mpf_solve_opts* o, int32_t* itersOut, double* resOut,
                      int32_t* accepted, mpf_gn_stats* stats, cudaStream_t s) {
@@ -974,6 +1048,7 @@ int gn_solve_learned(mpf_eit* m, mpf_mlp* net, int F, float* gamma, const float*
     std::vector<double> res0(F);
     MPF_CUDA(cudaMemcpyAsync(res0.data(), m->res0.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
     MPF_TRY(mlp_forward(net, F, m->learnX.ptr, gamma, m->E, s));  // synchronises
+    if (m->priorReady) MPF_TRY(learned_prior_apply(m, F, m->learnX.ptr, gamma, m->E, 1, s));
     MPF_TRY(gn_loop(m, F, gamma, vMeas, lambda, target, maxIters, o, res0.data(), homogeneous_gamma(m), accepted,
                     itersOut, resOut, stats, s));
     if (stats) stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

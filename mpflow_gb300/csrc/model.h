@@ -234,6 +234,11 @@ int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int np
 int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, const float* V,
                         double* y, double* res, cudaStream_t s);
 int fem_launch_fill_frames(int F, int E, const int* frameMask, float value, float* gamma, cudaStream_t s);
+// linear prior of the learned start: unit right-hand sides B[i] = e_{row(i)}
+// (rowsJ x Mm*Md, FP64) for the Jacobian rows of the measurements, and
+// Q = scale * B in FP32
+int fem_launch_prior_rhs(int rowsJ, int Mm, int Md, double* B, cudaStream_t s);
+int fem_launch_prior_convert(int rowsJ, int L, const double* B, double scale, float* Q, cudaStream_t s);
 int fem_launch_learned_input(int F, int L, const float* vMeas, const float* V0, float invRms, float* x,
                              double* res0, cudaStream_t s);
 // gamma += J^T w with J = hi + lo (the BF16 split the Gram is formed from)
@@ -259,6 +264,12 @@ int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s);
 int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s, const int* frameMask = nullptr);
 int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s,
                              const int* frameMask = nullptr);
+
+// matrix_ops.cu: C = alpha op(A) op(B) + beta C, column-major FP32
+int matrix_multiply_scaled(int transA, int transB, int m, int n, int k, float alpha, const float* A, int lda,
+                           const float* B, int ldb, float beta, float* C, int ldc, cudaStream_t s);
+int matrix_elementwise(int op, int rows, int cols, const float* A, const float* B, float* C, int ld, float scalar,
+                       cudaStream_t s);
 
 // mlp_kernels.cu (used by the learned warm start)
 void mlp_dims(const mpf_mlp* n, int* in, int* out);

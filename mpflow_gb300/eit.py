@@ -190,6 +190,7 @@ class EIT:
         check(lib().mpf_eit_get_info(h, ctypes.byref(info)))
         self.info = {name: getattr(info, name) for name, _ in _ffi.EitInfo._fields_}
         self.last_stats = None
+        self.prior_lambda = None
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -333,6 +334,31 @@ class EIT:
         x = torch.empty((F, vm.shape[1] * vm.shape[2]), dtype=torch.float32, device=vm.device)
         check(lib().mpf_eit_learned_input(self._h, F, ptr(vm), ptr(x), _stream()))
         return x
+
+    def learned_prior(self, lam: float):
+        """Sets the linear prior of the learned start (mpf_eit_learned_prior):
+        the first Gauss-Newton update from the homogeneous distribution with
+        regularisation lam, as a fixed linear map of the network input.
+        lam = 0 removes it."""
+        check(lib().mpf_eit_learned_prior(self._h, float(lam), _stream()))
+        self.prior_lambda = float(lam) if lam else None
+
+    def learned_prior_apply(self, x, out=None, mode: int = 0):
+        """prior(x) for network inputs x (frames x L): into a new
+        (frames x n_elements) tensor, or into `out` (mode 0 =, 1 +=, -1 -=)."""
+        import torch
+        if not (isinstance(x, torch.Tensor) and x.is_cuda and x.dtype == torch.float32 and x.dim() == 2):
+            raise TypeError("x must be a (frames x inputs) float32 CUDA tensor")
+        x = x.contiguous()
+        E = self.mesh.elements.shape[0]
+        if out is None:
+            out = torch.empty((x.shape[0], E), dtype=torch.float32, device=x.device)
+            mode = 0
+        if out.dtype != torch.float32 or not out.is_contiguous() or out.shape[0] != x.shape[0] or out.shape[1] < E:
+            raise ValueError("out must be a contiguous float32 (frames x >= n_elements) tensor")
+        check(lib().mpf_eit_learned_prior_apply(self._h, x.shape[0], ptr(x), ptr(out), out.shape[1], int(mode),
+                                                _stream()))
+        return out
 
     def gn_solve_learned(self, net, v_meas, lam: float, target: float = 1e-3, max_iters: int = 10,
                          options: SolveOptions | None = None):

@@ -111,6 +111,18 @@ class MLP:
         return W1, b1, W2, b2, W3, b3
 
 
+def zero_network(inputs: int, outputs: int, device: int = 0) -> MLP:
+    """A network whose output is exactly zero (last layer zero): with a
+    linear prior set, mpf_gn_solve_learned then starts from the prior
+    alone."""
+    import torch
+    net = MLP(inputs, 128, 128, outputs, seed=0, device=device)
+    flat = net.parameters()
+    flat[int(net.offsets[4]):].zero_()
+    net.set_parameters(flat)
+    return net
+
+
 def round_up(v: int, m: int) -> int:
     return (v + m - 1) // m * m
 
@@ -160,10 +172,14 @@ def add_noise(V, snr_db: float, generator=None):
 
 
 def train_warm_start(model, net: MLP, V, gamma, epochs: int = 60, batch: int = 256, lr: float = 1e-3,
-                     weight_decay: float = 1e-4, snr_db: float | None = 60.0, seed: int = 0, log=None):
+                     weight_decay: float = 1e-4, snr_db: float | None = 60.0, seed: int = 0, log=None,
+                     prior: bool = False):
     """Train `net` on (V, gamma) pairs with Adam and a cosine learning rate;
     fresh measurement noise at `snr_db` every epoch (None: noise-free).
-    Returns the per-epoch mean losses and the wall time."""
+    With `prior` the model's linear prior is set (EIT.learned_prior) and the
+    network learns gamma - prior(x), the correction to the linear
+    Gauss-Newton step, as mpf_gn_solve_learned then starts from
+    prior(x) + net(x).  Returns the per-epoch mean losses and the wall time."""
     import torch
     N, E = gamma.shape
     if batch % 128:
@@ -172,18 +188,24 @@ def train_warm_start(model, net: MLP, V, gamma, epochs: int = 60, batch: int = 2
     gen.manual_seed(seed)
     steps_per_epoch = max(1, N // batch)
     total = epochs * steps_per_epoch
+    if prior and getattr(model, "prior_lambda", None) is None:
+        raise ValueError("prior=True needs the model's linear prior (EIT.learned_prior)")
     losses = []
     t0 = time.perf_counter()
     step = 0
+    T = torch.empty_like(gamma) if prior else gamma
     for ep in range(epochs):
         Vn = add_noise(V, snr_db, gen) if snr_db is not None else V
         X = model.learned_input(Vn)
+        if prior:
+            T.copy_(gamma)
+            model.learned_prior_apply(X, T, mode=-1)
         perm = torch.randperm(N, device=V.device, generator=gen)
         acc = 0.0
         for b in range(steps_per_epoch):
             idx = perm[b * batch:(b + 1) * batch]
             want = b == steps_per_epoch - 1
-            loss = net.backward(X[idx], gamma[idx], valid=E, want_loss=want)
+            loss = net.backward(X[idx], T[idx], valid=E, want_loss=want)
             if want:
                 acc = loss
             cur = lr * 0.5 * (1.0 + math.cos(math.pi * step / total))

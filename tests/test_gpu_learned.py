@@ -105,3 +105,71 @@ def test_learned_warm_start_saves_gauss_newton_updates():
     assert st_plain.frames_converged == 32 and st_learn.frames_converged == 32
     assert acc.sum() >= 16
     assert it_learn.mean() < it_plain.mean(), (it_learn.mean(), it_plain.mean())
+
+
+def _prior_setup(frames=8):
+    import mpflow_gb300 as mp
+    from mpflow_gb300.learned import inclusion_frames
+    import torch
+    mesh, src, _ = make_setup(rings=20, ports=16, logarithmic=True)
+    E = mesh.elements.shape[0]
+    model = mp.EIT(mesh, src, 1.0, logarithmic=True)
+    cent = mesh.nodes[mesh.elements].mean(axis=1)
+    gte = inclusion_frames(cent, frames, np.random.default_rng(17))
+    Vte = model.solve(torch.tensor(gte, device="cuda"), mp.SolveOptions(tol=1e-6, refine_tol=1e-10)).contiguous()
+    _, J0 = model.solve(torch.zeros((1, E), device="cuda"), mp.SolveOptions(tol=1e-6), jacobian=True)
+    lam = 2e-2 * float(J0.norm() / np.sqrt(J0.shape[1]))
+    return mp, torch, model, mesh, cent, E, Vte, lam
+
+
+def test_learned_prior_is_the_first_gauss_newton_update():
+    """prior(x) equals one Gauss-Newton step from the homogeneous start
+    (mpf_gn_step: split-BF16 Gram there, FP64 Gram in the prior), and the
+    accumulate modes add and subtract it."""
+    mp, torch, model, mesh, cent, E, Vte, lam = _prior_setup()
+    F = Vte.shape[0]
+    model.learned_prior(lam)
+    x = model.learned_input(Vte)
+    gp = model.learned_prior_apply(x)
+    g1 = torch.zeros((F, E), device="cuda")
+    model.gn_step(g1, Vte, lam, mp.SolveOptions(tol=1e-7, refine_tol=1e-10))
+    for f in range(F):
+        assert _rel(gp[f].cpu().numpy(), g1[f].cpu().numpy()) < 2e-3, f
+    acc = torch.ones((F, E), device="cuda")
+    model.learned_prior_apply(x, acc, mode=1)
+    assert _rel((acc - 1.0).cpu().numpy(), gp.cpu().numpy()) < 1e-6
+    model.learned_prior_apply(x, acc, mode=-1)
+    assert _rel(acc.cpu().numpy(), np.ones((F, E))) < 1e-6
+    model.learned_prior(0.0)
+    with pytest.raises(mp.MpfError):
+        model.learned_prior_apply(x)
+
+
+def test_learned_prior_and_network_save_gauss_newton_updates():
+    """With the linear prior, the learned start (prior + trained correction)
+    needs fewer Gauss-Newton updates than the homogeneous start, and the
+    prior alone (zero network) is reported beside it."""
+    from mpflow_gb300.learned import generate_pairs, inclusion_frames, round_up, train_warm_start, zero_network
+    mp, torch, model, mesh, cent, E, Vte, lam = _prior_setup(frames=32)
+    opts = mp.SolveOptions(tol=1e-6, max_iter=4000)
+    model.learned_prior(lam)
+    Vtr, gtr = generate_pairs(model, inclusion_frames(cent, 2048, np.random.default_rng(11)), batch=128,
+                              options=opts)
+    L = Vtr.shape[1] * Vtr.shape[2]
+    net = mp.MLP(L, 512, 512, round_up(E, 128), seed=5)
+    losses, _ = train_warm_start(model, net, Vtr, gtr, epochs=40, batch=256, lr=1e-3, snr_db=60.0, prior=True)
+    assert losses[-1] < losses[0], losses
+    target = 1e-3
+    g0 = torch.zeros((32, E), device="cuda")
+    it_plain, _, st_plain = model.gn_solve(g0, Vte, lam, target=target, max_iters=15, options=opts)
+    _, it_prior, _, acc_p, st_prior = model.gn_solve_learned(zero_network(L, round_up(E, 128)), Vte, lam,
+                                                             target=target, max_iters=15, options=opts)
+    _, it_learn, _, acc, st_learn = model.gn_solve_learned(net, Vte, lam, target=target, max_iters=15,
+                                                           options=opts)
+    print(f"GN updates: plain {it_plain.mean():.3f}, prior only {it_prior.mean():.3f} "
+          f"(direct {np.mean(it_prior == 0):.2f}), prior + network {it_learn.mean():.3f} "
+          f"(direct {np.mean(it_learn == 0):.2f}, accepted {acc.sum()}/32); loss {losses[0]:.3g} -> {losses[-1]:.3g}")
+    assert st_plain.frames_converged == 32 and st_prior.frames_converged == 32 and st_learn.frames_converged == 32
+    assert acc_p.sum() >= 24 and acc.sum() >= 24
+    assert it_prior.mean() < it_plain.mean()
+    assert it_learn.mean() < it_plain.mean()

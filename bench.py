@@ -87,6 +87,9 @@ def parse_args():
     p.add_argument("--learned-prior", choices=["on", "off"], default="on",
                    help="on: the network learns the correction to the linear one-step GN prior "
                         "(mpf_eit_learned_prior); off: it predicts gamma alone")
+    p.add_argument("--labels", choices=["gn", "truth"], default="gn",
+                   help="training targets with the prior: gn = where batched GN from the prior converges "
+                        "(learned.gn_labels), truth = the generating conductivity")
     p.add_argument("--single-frames", type=int, default=4,
                    help="frames per step timed one at a time on the plain GN path (0: skip)")
     p.add_argument("--profile-only", action="store_true",
@@ -103,18 +106,12 @@ def dist_env():
 
 
 def synthetic_frames(centroids: np.ndarray, count: int, seed: int) -> np.ndarray:
-    """Log-conductivity frames in dB (v = 10 log10(sigma / 1 S/m))."""
-    rng = np.random.default_rng(seed)
-    v = np.zeros((count, centroids.shape[0]), np.float32)
-    for f in range(count):
-        for _ in range(int(rng.integers(1, 4))):
-            r = rng.uniform(0.05, 0.3)
-            rc = rng.uniform(0.0, 0.95 - r)
-            th = rng.uniform(0.0, 2 * np.pi)
-            c = np.array([rc * np.cos(th), rc * np.sin(th)])
-            contrast = np.exp(rng.uniform(np.log(0.1), np.log(10.0)))
-            v[f, np.linalg.norm(centroids - c, axis=1) < r] = 10.0 * np.log10(contrast)
-    return v
+    """Held-out log-conductivity frames in dB (v = 10 log10(sigma / 1 S/m)):
+    the training pairs' family (1-3 disks, radius U(0.05, 0.3), contrast
+    log-uniform in [0.1, 10], centres uniform over the disk that keeps them
+    inside) from seeds the training never uses."""
+    from mpflow_gb300.learned import inclusion_frames
+    return inclusion_frames(centroids, count, np.random.default_rng(10_000_019 + seed))
 
 
 class ClockSampler:
@@ -349,7 +346,8 @@ def run_gb300(a):
     import torch
     import torch.distributed as dist
     import mpflow_gb300 as mp
-    from mpflow_gb300.learned import generate_pairs, inclusion_frames, round_up, train_warm_start, zero_network
+    from mpflow_gb300.learned import (generate_pairs, gn_labels, inclusion_frames, round_up, train_warm_start,
+                                      zero_network)
 
     rank, world, local = dist_env()
     if world > 1:
@@ -403,6 +401,12 @@ def run_gb300(a):
         t0 = time.perf_counter()
         model.learned_prior(lam)
         prior_s = time.perf_counter() - t0
+    label_s, label_conv = None, None
+    if use_prior and a.labels == "gn":
+        t0 = time.perf_counter()
+        gtr, label_conv = gn_labels(model, Vtr, lam, target=a.target, max_iters=4, options=gn_opts)
+        torch.cuda.synchronize()
+        label_s = time.perf_counter() - t0
     net = mp.MLP(L, a.hidden, a.hidden, round_up(E, 128), seed=17 + rank)
     losses, train_s = train_warm_start(model, net, Vtr, gtr, epochs=a.epochs, batch=256, lr=1e-3,
                                        snr_db=60.0, seed=rank, prior=use_prior)
@@ -524,6 +528,9 @@ def run_gb300(a):
                     "train_s": train_s, "train_steps": train_steps, "loss_first": losses[0],
                     "loss_last": losses[-1], "network": f"{L}-{a.hidden}-{a.hidden}-{round_up(E, 128)} GELU",
                     "train_tflops": mlp_flops / train_s / 1e12,
+                    "labels": (("GN from the prior to the target (<= 4 updates; the prior where it does not "
+                                "converge)") if label_s is not None else "generating conductivity"),
+                    "label_s": label_s, "label_converged_fraction": label_conv,
                     "prior": ({"lambda": lam, "setup_s": prior_s,
                                "what": "J0^T (J0 J0^T + mu I)^-1 at the homogeneous point, FP64 Gram/Cholesky, "
                                        "applied as an FP32 GEMM"} if use_prior else None),

@@ -281,7 +281,11 @@ typedef struct mpf_gn_stats {
  * `target`, for at most max_gn_iters updates; frames that reach the target
  * are frozen.  The reference leaves this outer loop to its caller
  * (src/solver/solver.cpp:196-225 is one step).  Forward solves after the
- * first start from the previous fields.
+ * first start from the previous fields.  A frame whose J J^T + mu I is not
+ * positive definite also in FP64, or whose update leaves the forward model's
+ * range (a non-finite value, |gamma| > 100 dB logarithmic, gamma <= 0
+ * linear), keeps its last gamma and is frozen unconverged; the other frames
+ * go on (mpf_gn_step reports a breakdown as MPF_EBREAKDOWN instead).
  *   iterations: host, frames ints (updates per frame) or NULL
  *   residual:   host, frames doubles (final residual per frame) or NULL */
 int mpf_gn_solve(mpf_eit_t model, int32_t frames, float* gamma, const float* v_meas, double lambda,

@@ -105,6 +105,9 @@ struct mpf_eit {
     float v0InvRms = 1.f;
     mpf::DevBuf<float> V0, X0, learnX;
     mpf::DevBuf<double> res0;
+    // Gauss-Newton loop: parameters before the update, frames it sent out of range
+    mpf::DevBuf<float> gammaPrev;
+    mpf::DevBuf<int> badFrame;
     // linear prior of the learned start (mpf_eit_learned_prior): W = J0^T
     // (J0 J0^T + mu I)^-1 / invRms, column-major E x L with ld Epad
     bool priorReady = false;

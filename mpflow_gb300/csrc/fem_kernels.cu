@@ -343,6 +343,27 @@ __global__ void __launch_bounds__(256) k_learned_input(int L, const float* __res
     if (threadIdx.x == 0 && res0) res0[f] = red[1][0] > 0.0 ? sqrt(red[0][0] / red[1][0]) : 0.0;
 }
 
+// bad[f] = 1 when an active frame's parameters left the range the forward
+// model can take: a non-finite value, |gamma| > 100 (dB, log-conductivity)
+// or gamma <= 0 (linear conductivity).  One block per frame.
+__global__ void k_gamma_check(int E, const float* __restrict__ gamma, const int* __restrict__ frameActive,
+                              int logarithmic, int* __restrict__ bad) {
+    const int f = blockIdx.x;
+    __shared__ int flag;
+    if (threadIdx.x == 0) flag = 0;
+    __syncthreads();
+    if (!frameActive || frameActive[f]) {
+        int b = 0;
+        for (int e = threadIdx.x; e < E; e += blockDim.x) {
+            const float g = gamma[(size_t)f * E + e];
+            b |= !isfinite(g) || (logarithmic ? fabsf(g) > 100.f : g <= 0.f);
+        }
+        if (b) flag = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) bad[f] = flag;
+}
+
 // Unit right-hand sides of the learned start's linear prior: column i of B
 // (rowsJ x Mm*Md) is e_{row(i)}, row(i) = m + d * MP the Jacobian row of
 // measurement i = m + d * Mm.
@@ -468,6 +489,13 @@ int fem_launch_update_gamma(int F, int rowsJ, int Epad, int E, const __nv_bfloat
 
 int fem_launch_fill_frames(int F, int E, const int* frameMask, float value, float* gamma, cudaStream_t s) {
     k_fill_frames<<<dim3((E + 255) / 256, F), 256, 0, s>>>(E, frameMask, value, gamma);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int fem_launch_gamma_check(int F, int E, const float* gamma, const int* frameActive, bool logarithmic, int* bad,
+                           cudaStream_t s) {
+    k_gamma_check<<<F, 256, 0, s>>>(E, gamma, frameActive, logarithmic ? 1 : 0, bad);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

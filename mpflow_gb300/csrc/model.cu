@@ -781,8 +781,12 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
 }
 
 // J J^T + mu I (split-BF16 tensor cores) -> FP64 Cholesky -> w -> gamma += J^T w
-// for the frames in frameActive (all if null); y holds the residual on entry.
-static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* frameActive, cudaStream_t s) {
+// for the frames in frameActive (all if null; hostActive: the same on the
+// host, or null); y holds the residual on entry.  With `broken`, a frame whose
+// factorisation fails also with the FP64 Gram is left unchanged and flagged
+// there; without it the failure is left in m->info for gn_check.
+static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* frameActive, cudaStream_t s,
+                     const int* hostActive = nullptr, std::vector<int>* broken = nullptr) {
     const double mu = (double)m->ref * lambda * (double)m->ref * lambda;
     MPF_TRY(dense_gram_f64_shift(F, m->rowsJ, m->Epad, m->Jhi.ptr, m->Jlo.ptr, m->Epad, mu, m->A64.ptr,
                                  m->gramWork.ptr, m->gramWork.count, s, frameActive));
@@ -800,6 +804,19 @@ static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* 
         MPF_TRY(eit_jacobian(m, F, gamma, m->redoMask.ptr, true, s));
         MPF_TRY(dense_gram_f64_exact(F, m->rowsJ, m->Epad, m->J.ptr, m->Epad, mu, m->A64.ptr, m->redoMask.ptr, s));
         MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, m->redoMask.ptr));
+        if (broken) {
+            MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
+            MPF_CUDA(cudaStreamSynchronize(s));
+            broken->assign(F, 0);
+            bool anyBroken = false;
+            for (int f = 0; f < F; ++f) anyBroken |= ((*broken)[f] = redo[f] && info[f] != 0) != 0;
+            if (anyBroken) {
+                std::vector<int> ok(F);
+                for (int f = 0; f < F; ++f) ok[f] = (!hostActive || hostActive[f]) && !(*broken)[f];
+                MPF_TRY(m->redoMask.upload(ok));
+                frameActive = m->redoMask.ptr;
+            }
+        }
     }
     MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s, frameActive));
     MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->Jhi.ptr, m->Jlo.ptr, m->y.ptr, frameActive, gamma,
@@ -901,7 +918,28 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         for (int f = 0; f < F; ++f) iters[f] += mask[f];
         MPF_CUDA(cudaMemcpyAsync(m->frameMask.ptr, mask.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
         MPF_TRY(eit_jacobian(m, F, gamma, m->frameMask.ptr, false, s));
-        MPF_TRY(gn_update(m, F, gamma, lambda, m->frameMask.ptr, s));
+        // a frame whose J J^T + mu I cannot be factored (also with the FP64
+        // Gram) keeps its gamma and leaves the iteration unconverged
+        std::vector<int> broken;
+        MPF_TRY(m->gammaPrev.alloc((size_t)F * m->E));
+        MPF_TRY(m->badFrame.alloc((size_t)F));
+        MPF_CUDA(cudaMemcpyAsync(m->gammaPrev.ptr, gamma, sizeof(float) * F * m->E, cudaMemcpyDeviceToDevice, s));
+        MPF_TRY(gn_update(m, F, gamma, lambda, m->frameMask.ptr, s, mask.data(), &broken));
+        for (int f = 0; f < F && !broken.empty(); ++f)
+            if (broken[f]) mask[f] = 0;
+        // an update that sends a frame's parameters out of the forward
+        // model's range (a diverging step) is undone and the frame frozen
+        // unconverged, so that it cannot break the batch's next solve
+        std::vector<int> bad(F);
+        MPF_TRY(fem_launch_gamma_check(F, m->E, gamma, m->frameMask.ptr, m->logarithmic, m->badFrame.ptr, s));
+        MPF_CUDA(cudaMemcpyAsync(bad.data(), m->badFrame.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        for (int f = 0; f < F; ++f)
+            if (bad[f]) {
+                mask[f] = 0;
+                MPF_CUDA(cudaMemcpyAsync(gamma + (size_t)f * m->E, m->gammaPrev.ptr + (size_t)f * m->E,
+                                         sizeof(float) * m->E, cudaMemcpyDeviceToDevice, s));
+            }
         MPF_TRY(gn_check(m, F, s, mask.data()));
         ++gnIters;
         ++it;

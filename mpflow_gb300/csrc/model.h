@@ -234,6 +234,9 @@ int fem_launch_fields_export(int F, int Ca, int C, const int32_t* compOf, int np
 int fem_launch_residual(int F, int rowsJ, int Mm, int Md, const float* vMeas, const float* V,
                         double* y, double* res, cudaStream_t s);
 int fem_launch_fill_frames(int F, int E, const int* frameMask, float value, float* gamma, cudaStream_t s);
+// bad[f] = active frame f has a non-finite or out-of-range parameter
+int fem_launch_gamma_check(int F, int E, const float* gamma, const int* frameActive, bool logarithmic, int* bad,
+                           cudaStream_t s);
 // linear prior of the learned start: unit right-hand sides B[i] = e_{row(i)}
 // (rowsJ x Mm*Md, FP64) for the Jacobian rows of the measurements, and
 // Q = scale * B in FP32

@@ -162,6 +162,33 @@ def generate_pairs(model, gammas: np.ndarray, batch: int = 64, options=None):
     return torch.cat(Vs), torch.tensor(gammas, device=f"cuda:{model.device}")
 
 
+def gn_labels(model, V, lam: float, target: float = 1e-3, max_iters: int = 4, batch: int = 64, options=None):
+    """Training targets of the learned start over the model's linear prior
+    (EIT.learned_prior): for every frame of V (count, Mm, Md), where batched
+    Gauss-Newton from the prior converges (relative data residual <=
+    target).  A frame that does not get there within max_iters updates keeps
+    the prior itself (zero correction).  Returns (labels (count x E) CUDA
+    tensor, fraction of frames that converged)."""
+    import torch
+    if getattr(model, "prior_lambda", None) is None:
+        raise ValueError("gn_labels needs the model's linear prior (EIT.learned_prior)")
+    E = model.mesh.elements.shape[0]
+    L = V.shape[1] * V.shape[2]
+    net0 = zero_network(L, round_up(E, 128), device=model.device)
+    out = torch.empty((V.shape[0], E), dtype=torch.float32, device=V.device)
+    converged = 0
+    for i in range(0, V.shape[0], batch):
+        Vb = V[i:i + batch].contiguous()
+        g, _, res, _, _ = model.gn_solve_learned(net0, Vb, lam, target=target, max_iters=max_iters, options=options)
+        bad = np.flatnonzero(~(res <= target))
+        if bad.size:
+            idx = torch.tensor(bad, device=V.device)
+            g[idx] = model.learned_prior_apply(model.learned_input(Vb[idx].contiguous()))
+        converged += Vb.shape[0] - bad.size
+        out[i:i + Vb.shape[0]] = g
+    return out, converged / V.shape[0]
+
+
 def add_noise(V, snr_db: float, generator=None):
     """V + Gaussian noise with std rms(V_frame) 10^(-snr/20) per frame."""
     import torch

@@ -146,18 +146,22 @@ def test_learned_prior_is_the_first_gauss_newton_update():
 
 
 def test_learned_prior_and_network_save_gauss_newton_updates():
-    """With the linear prior, the learned start (prior + trained correction)
-    needs fewer Gauss-Newton updates than the homogeneous start, and the
-    prior alone (zero network) is reported beside it."""
-    from mpflow_gb300.learned import generate_pairs, inclusion_frames, round_up, train_warm_start, zero_network
+    """With the linear prior, the learned start (prior + a correction trained
+    on where Gauss-Newton from the prior converges) needs fewer updates than
+    the homogeneous start, and the prior alone (zero network) is reported
+    beside it."""
+    from mpflow_gb300.learned import (generate_pairs, gn_labels, inclusion_frames, round_up, train_warm_start,
+                                      zero_network)
     mp, torch, model, mesh, cent, E, Vte, lam = _prior_setup(frames=32)
     opts = mp.SolveOptions(tol=1e-6, max_iter=4000)
     model.learned_prior(lam)
     Vtr, gtr = generate_pairs(model, inclusion_frames(cent, 2048, np.random.default_rng(11)), batch=128,
                               options=opts)
     L = Vtr.shape[1] * Vtr.shape[2]
+    labels, conv = gn_labels(model, Vtr, lam, target=1e-3, options=opts)
+    assert conv > 0.9, conv
     net = mp.MLP(L, 512, 512, round_up(E, 128), seed=5)
-    losses, _ = train_warm_start(model, net, Vtr, gtr, epochs=40, batch=256, lr=1e-3, snr_db=60.0, prior=True)
+    losses, _ = train_warm_start(model, net, Vtr, labels, epochs=40, batch=256, lr=1e-3, snr_db=60.0, prior=True)
     assert losses[-1] < losses[0], losses
     target = 1e-3
     g0 = torch.zeros((32, E), device="cuda")

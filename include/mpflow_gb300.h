@@ -485,7 +485,7 @@ int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const
  * (row-major == column-major), B n x nrhs column-major, per batch entry.
  * A is overwritten by its factor.  info[batch] (device ints) receives 0 or
  * the 1-based index of the first non-positive pivot.  n must be a multiple
- * of 32 and at most 4864.  Replaces the dense CG of Inverse::solve
+ * of 32 and at most 24576.  Replaces the dense CG of Inverse::solve
  * (src/solver/inverse.cpp:213-238). */
 int mpf_cholesky_solve_f64(int32_t batch, int32_t n, double* A, double shift, double* B,
                            int32_t nrhs, int32_t* info, mpf_stream_t stream);
@@ -539,6 +539,21 @@ int mpf_mlp_params(mpf_mlp_t net, float* buffer, int32_t which, mpf_stream_t str
  * drive_count) FP32. */
 int mpf_eit_learned_input(mpf_eit_t model, int32_t frames, const float* v_meas, float* x,
                           mpf_stream_t stream);
+
+/* Complex regularised inverse step, solver::Inverse<thrust::complex<float>>
+ * (src/solver/inverse.cpp:60-238, instantiated at :243):
+ *   (J^T J + (ref * factor)^2 R) result = J^T (measurement - calculation)
+ * with the plain (unconjugated) transpose of the reference's CUBLAS_OP_T
+ * products, R as in mpf_inverse_solve (identity in dual form for any mesh,
+ * NOSER and Laplacian on the E x E system for n_elements <= 6144).  The Gram
+ * is formed in FP64 from the FP32 J and factored as a complex symmetric
+ * L L^T in FP64 without pivoting where the reference runs a dense CG;
+ * MPF_EBREAKDOWN on a zero pivot.  Complex arrays hold interleaved (re, im)
+ * floats (thrust::complex<float>); shapes as in mpf_inverse_solve, e.g. the
+ * jacobian output of mpf_eit_forward_complex.  Synchronises. */
+int mpf_inverse_solve_complex(mpf_eit_t model, int32_t regularization, double factor, int32_t images,
+                              const float* jacobian, const float* calculation, const float* measurement,
+                              float* result, mpf_stream_t stream);
 
 /* Linear prior of the learned start: the first Gauss-Newton update from the
  * homogeneous distribution gamma_h, which is linear in the network input x,

@@ -85,6 +85,8 @@ int mlp_adam(mpf_mlp* n, float lr, float beta1, float beta2, float eps, float we
 int mlp_params(mpf_mlp* n, float* buf, int which, cudaStream_t s);
 int learned_input(mpf_eit* m, int F, const float* vMeas, float* x, cudaStream_t s);
 int learned_prior(mpf_eit* m, double lambda, cudaStream_t s);
+int inverse_solve_complex(mpf_eit* m, int reg, double factor, int images, const float* Jref, const float* calc,
+                          const float* meas, float* result, cudaStream_t s);
 int learned_prior_apply(mpf_eit* m, int F, const float* x, float* out, int ldo, int mode, cudaStream_t s);
 int gn_solve_learned(mpf_eit* m, mpf_mlp* net, int F, float* gamma, const float* vMeas, double lambda,
                      double target, int maxIters, const mpf_solve_opts* o, int32_t* itersOut, double* resOut,
@@ -461,6 +463,16 @@ int mpf_eit_learned_input(mpf_eit_t model, int32_t frames, const float* v_meas, 
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_learned_input: model == nullptr");
         return mpf::learned_input(model, frames, v_meas, x, (cudaStream_t)stream);
+    })
+}
+
+int mpf_inverse_solve_complex(mpf_eit_t model, int32_t regularization, double factor, int32_t images,
+                              const float* jacobian, const float* calculation, const float* measurement,
+                              float* result, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_inverse_solve_complex: model == nullptr");
+        return mpf::inverse_solve_complex(model, regularization, factor, images, jacobian, calculation, measurement,
+                                          result, (cudaStream_t)stream);
     })
 }
 

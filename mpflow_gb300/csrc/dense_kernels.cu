@@ -678,9 +678,12 @@ int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s, c
 
 int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s,
                              const int* frameMask) {
-    MPF_CHECK((size_t)n * sizeof(double) <= 38 * 1024 && n % NB == 0, MPF_EINVAL,
-              "cholesky solve: n must be a multiple of %d and at most 4864 (%d)", NB, n);
-    k_chol_solve<<<batch * nrhs, 256, n * sizeof(double), s>>>(n, L, B, nrhs, frameMask);
+    const size_t bytes = (size_t)n * sizeof(double);
+    MPF_CHECK(bytes <= 192 * 1024 && n % NB == 0, MPF_EINVAL,
+              "cholesky solve: n must be a multiple of %d and at most 24576 (%d)", NB, n);
+    if (bytes > 38 * 1024)
+        MPF_CUDA(cudaFuncSetAttribute(k_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    k_chol_solve<<<batch * nrhs, 256, bytes, s>>>(n, L, B, nrhs, frameMask);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

@@ -101,6 +101,8 @@ __global__ void k_to_float_rows(int images, int E, int ld, const double* __restr
     if (e < E) out[(size_t)p * E + e] = (float)x[(size_t)p * ld + e];
 }
 
+}  // namespace
+
 // L^T L of the reference's edge-length Laplacian (src/solver/inverse.cpp:
 // 98-113): L[edge][element] = +-length, + at the first element that visits
 // the edge and - at the second, so (L^T L)[a][a] is the sum of the squared
@@ -143,8 +145,6 @@ int laplacian_coo(mpf_eit* m) {
     MPF_TRY(m->lapVal.upload(vals));
     return MPF_OK;
 }
-
-}  // namespace
 
 static bool pivot_failed(mpf_eit* m, cudaStream_t s);
 

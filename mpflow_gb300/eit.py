@@ -399,6 +399,30 @@ class EIT:
                                       ptr(calc), ptr(meas), ptr(out), _stream()))
         return out
 
+    def inverse_complex(self, jacobian, calculation, measurement, factor: float, regularization: str = "identity"):
+        """Complex regularised inverse step (solver::Inverse on
+        thrust::complex<float>, mpf_inverse_solve_complex):
+        (J^T J + (ref factor)^2 R) dsigma = J^T (measurement - calculation)
+        with the plain transpose.  jacobian: complex64 (rowsJ, E) as returned
+        by solve_complex(jacobian=True) for one frame; calculation,
+        measurement: complex64 (images, Mm, Md).  Returns complex64 dsigma
+        (images, E)."""
+        import torch
+        if regularization not in self.REGULARIZATIONS:
+            raise ValueError(f"regularization must be one of {sorted(self.REGULARIZATIONS)}")
+        for name, t in (("jacobian", jacobian), ("calculation", calculation), ("measurement", measurement)):
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.complex64):
+                raise TypeError(f"{name} must be a complex64 CUDA tensor")
+        J = jacobian.reshape(self.jacobian_rows, -1).t().contiguous()  # reference layout storage (E, rowsJ)
+        images = calculation.shape[0]
+        calc = self._vmeas(calculation, images)
+        meas = self._vmeas(measurement, images)
+        out = torch.empty((images, self.mesh.elements.shape[0]), dtype=torch.complex64, device=calc.device)
+        vp = lambda t: ctypes.c_void_p(t.data_ptr())
+        check(lib().mpf_inverse_solve_complex(self._h, self.REGULARIZATIONS[regularization], float(factor), images,
+                                              vp(J), vp(calc), vp(meas), vp(out), _stream()))
+        return out
+
     def group_iterations(self) -> np.ndarray:
         """CG iterations per (frame, active harmonic) group of the last inner solve."""
         out = np.zeros(65536, np.int32)

@@ -475,7 +475,9 @@ def inverse_regularised(J: np.ndarray, Y: np.ndarray, ref: float, factor: float,
                         nodes=None, elements=None) -> np.ndarray:
     """(J^T J + (ref*factor)^2 R) X = J^T Y in FP64 for R = I, diag(J^T J)
     (NOSER) or the Laplacian L^T L (src/solver/inverse.cpp:60-130,213-238),
-    solved directly.  J: rows x E, Y: rows x images; returns E x images."""
+    solved directly.  J: rows x E, Y: rows x images; returns E x images.
+    Complex J and Y (the thrust::complex instantiations) use the plain
+    transpose, as the reference's CUBLAS_OP_T products."""
     JtJ = J.T @ J
     mu = (ref * factor) ** 2
     if kind == "identity":

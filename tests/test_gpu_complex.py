@@ -72,3 +72,43 @@ def test_complex_rejects_unsupported_options():
         with pytest.raises(mp.MpfError) as e:
             model.solve_complex(g, opts)
         assert e.value.status == 8
+
+
+@pytest.mark.parametrize("kind", ["identity", "noser", "laplacian"])
+def test_complex_inverse_matches_oracle(kind):
+    """mpf_inverse_solve_complex (solver::Inverse on thrust::complex<float>)
+    for two images against the FP64 complex solve of the same regularised
+    system with the plain transpose (numpy J.T, as the reference's
+    CUBLAS_OP_T)."""
+    import oracle
+    import torch
+    import mpflow_gb300 as mp
+    mesh, src, orc = make_setup(rings=16, ports=16, components=3, height=2.0)
+    E = mesh.elements.shape[0]
+    model = mp.EIT(mesh, src, 1.0, components=3, height=2.0)
+    opts = mp.SolveOptions(tol=1e-7, solver="bicgstab")
+    ref = torch.full((1, E), 1.0 + 0.15j, dtype=torch.complex64, device="cuda")
+    calc1, J = model.solve_complex(ref, opts, jacobian=True)
+    g = _complex_frames(mesh, 2, seed=7, logarithmic=False)
+    meas = model.solve_complex(torch.tensor(g, dtype=torch.complex64, device="cuda"), opts)
+    calc = calc1.expand(2, -1, -1).contiguous()
+    Jn = J[0].cpu().numpy().astype(np.complex128)
+    assert np.abs(Jn.imag).max() > 1e-3 * np.abs(Jn.real).max()
+    djj = float((np.abs(Jn) ** 2).sum(axis=0).mean())
+    if kind == "identity":
+        factor = np.sqrt(0.1 * djj)
+    elif kind == "noser":
+        factor = np.sqrt(0.1)
+    else:
+        factor = np.sqrt(0.1 * djj / float(np.diag(oracle.laplacian_gram(mesh.nodes, mesh.elements)).mean()))
+    out = model.inverse_complex(J[0], calc, meas, factor, kind).cpu().numpy()
+
+    def flat(V):
+        V = V.cpu().numpy().astype(np.complex128)
+        return oracle.flatten_measurement(V.real, orc) + 1j * oracle.flatten_measurement(V.imag, orc)
+
+    Y = np.stack([flat(meas[i]) - flat(calc[i]) for i in range(2)], 1)
+    X = oracle.inverse_regularised(Jn, Y, 1.0, factor, kind, mesh.nodes, mesh.elements)
+    assert np.abs(X.imag).max() > 1e-3 * np.abs(X.real).max()
+    for i in range(2):
+        assert rel_err(out[i], X[:, i]) < 1e-5, (kind, i, rel_err(out[i], X[:, i]))

@@ -102,13 +102,19 @@ def test_gram_split_bf16_accuracy():
     assert err < 3e-5, err
 
 
-@pytest.mark.parametrize("n,nrhs", [(32, 1), (256, 1), (1024, 1), (160, 3)])
+@pytest.mark.parametrize("n,nrhs", [(32, 1), (256, 1), (1024, 1), (160, 3), (5120, 2)])
 def test_cholesky_f64(n, nrhs):
+    """Batched FP64 Cholesky factor + solve; n = 5120 takes the solve's
+    shared-memory opt-in (x above 38 KB)."""
     import mpflow_gb300 as mp
     torch = _torch()
     rng = np.random.default_rng(5 + n)
-    X = rng.standard_normal((3, n, n))
-    A = np.einsum("bij,bkj->bik", X, X) / n
+    if n <= 1024:
+        X = rng.standard_normal((3, n, n))
+        A = np.einsum("bij,bkj->bik", X, X) / n
+    else:  # symmetric, diagonally dominant
+        B = rng.standard_normal((3, n, n)) / n
+        A = B + B.transpose(0, 2, 1) + np.eye(n)[None] * (1.0 + rng.random((3, 1, n)))
     b = rng.standard_normal((3, nrhs, n))
     At = torch.tensor(A, device="cuda")
     Bt = torch.tensor(b, device="cuda")

@@ -32,6 +32,8 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "mpflow_gb300.h"
@@ -53,6 +55,22 @@ inline void check(int status, const char* where) {
 }
 inline void cuda(cudaError_t e, const char* where) {
     if (e != cudaSuccess) throw std::runtime_error(std::string(where) + ": " + cudaGetErrorString(e));
+}
+// complex data types (thrust::complex<float>, std::complex<float>: anything
+// with real() and imag(), stored as an interleaved float pair)
+template <class T, class = void>
+struct is_complex : std::false_type {};
+template <class T>
+struct is_complex<T, std::void_t<decltype(std::declval<T const&>().imag())>> : std::true_type {};
+template <class T>
+double real_part(T const& v) {
+    if constexpr (is_complex<T>::value) return (double)v.real();
+    else return (double)v;
+}
+template <class T>
+double imag_part(T const& v) {
+    if constexpr (is_complex<T>::value) return (double)v.imag();
+    else return 0.0;
 }
 }  // namespace detail
 
@@ -960,11 +978,21 @@ public:
         if (!mesh) throw std::invalid_argument("mpFlow::models::EIT::EIT: mesh == nullptr");
         if (!sources) throw std::invalid_argument("mpFlow::models::EIT::EIT: sources == nullptr");
         const unsigned L = sources->ports->count, Md = sources->drivePattern->cols, Mm = sources->measurementPattern->cols;
-        std::vector<double> drive((size_t)L * Md), meas((size_t)L * Mm), vals(sources->values.begin(), sources->values.end());
+        std::vector<double> drive((size_t)L * Md), meas((size_t)L * Mm), vals;
+        for (auto const& v : sources->values) vals.push_back(detail::real_part(v));
         for (unsigned j = 0; j < Md; ++j)
-            for (unsigned i = 0; i < L; ++i) drive[i + (size_t)j * L] = (*sources->drivePattern)(i, j);
+            for (unsigned i = 0; i < L; ++i) drive[i + (size_t)j * L] = detail::real_part((*sources->drivePattern)(i, j));
         for (unsigned j = 0; j < Mm; ++j)
-            for (unsigned i = 0; i < L; ++i) meas[i + (size_t)j * L] = (*sources->measurementPattern)(i, j);
+            for (unsigned i = 0; i < L; ++i) meas[i + (size_t)j * L] = detail::real_part((*sources->measurementPattern)(i, j));
+        // complex models (thrust::complex instantiations, src/models/eit.cpp:289-304):
+        // currents and the reference value are real; a complex admittivity
+        // is expressed through the material distribution
+        if (detail::imag_part(referenceValue) != 0.0)
+            throw std::invalid_argument("mpFlow::models::EIT::EIT: complex referenceValue (express it through the "
+                                        "material distribution)");
+        for (auto const& v : sources->values)
+            if (detail::imag_part(v) != 0.0)
+                throw std::invalid_argument("mpFlow::models::EIT::EIT: complex source values are not supported");
         int device = 0;
         detail::cuda(cudaGetDevice(&device), "mpFlow::models::EIT::EIT");
         mpf_eit_desc d{};
@@ -983,7 +1011,7 @@ public:
         d.meas_pattern = meas.data();
         d.source_values = vals.data();
         d.source_type = sources->type == FEM::Sources<dataType>::Open ? MPF_SOURCE_OPEN : MPF_SOURCE_FIXED;
-        d.reference_value = referenceValue;
+        d.reference_value = detail::real_part(referenceValue);
         d.logarithmic = logarithmic ? 1 : 0;
         d.components = (int32_t)components;
         d.height = height;
@@ -1048,16 +1076,29 @@ public:
         if (materialDistribution->rows != mesh->elements.rows())
             throw std::invalid_argument("mpFlow::models::EIT::solve: materialDistribution has wrong size");
         const unsigned Mm = result->rows, Md = result->cols;
-        float* V = nullptr;
-        detail::cuda(cudaMallocAsync((void**)&V, sizeof(float) * (size_t)Mm * Md, stream), "mpFlow::models::EIT::solve");
+        dataType* V = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&V, sizeof(dataType) * (size_t)Mm * Md, stream), "mpFlow::models::EIT::solve");
         mpf_solve_stats st{};
-        const int status = mpf_eit_forward(model_, 1, materialDistribution->deviceData, V, jacobian->deviceData,
-                                           &options, &st, stream);
+        int status;
+        if constexpr (detail::is_complex<dataType>::value) {
+            static_assert(sizeof(dataType) == 2 * sizeof(float), "complex models take interleaved float pairs");
+            // complex admittivity: complex BiCGSTAB whatever the solver tag
+            // (the reference's CG on complex data is the same Krylov family)
+            mpf_solve_opts o = options;
+            o.solver = 1;
+            status = mpf_eit_forward_complex(model_, 1, reinterpret_cast<const float*>(materialDistribution->deviceData),
+                                             reinterpret_cast<float*>(V), reinterpret_cast<float*>(jacobian->deviceData),
+                                             &o, &st, stream);
+        } else {
+            status = mpf_eit_forward(model_, 1, materialDistribution->deviceData, V, jacobian->deviceData, &options,
+                                     &st, stream);
+        }
         if (status == MPF_OK || status == MPF_ENOCONV) {
-            detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(float) * result->dataRows, V, sizeof(float) * Mm,
-                                           sizeof(float) * Mm, Md, cudaMemcpyDeviceToDevice, stream),
+            detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, V,
+                                           sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md, cudaMemcpyDeviceToDevice,
+                                           stream),
                          "mpFlow::models::EIT::solve");
-            fieldsValid_ = true;
+            fieldsValid_ = !detail::is_complex<dataType>::value;
         }
         cudaFreeAsync(V, stream);
         detail::check(status == MPF_ENOCONV ? MPF_OK : status, "mpFlow::models::EIT::solve");
@@ -1069,6 +1110,8 @@ public:
 
     // potentials of the last solve, one matrix per 2.5D component
     void updateFields(cudaStream_t const stream) {
+        if (detail::is_complex<dataType>::value)
+            throw std::logic_error("mpFlow::models::EIT::updateFields: not available for complex models");
         if (!fieldsValid_) throw std::logic_error("mpFlow::models::EIT::updateFields: no solve yet");
         const size_t per = (size_t)fields[0]->dataRows * fields[0]->cols;  // export layout: dataRows x cols per component
         float* buf = nullptr;
@@ -1157,25 +1200,31 @@ public:
         if (calculation.size() != parallelImages_ || measurement.size() != parallelImages_)
             throw std::invalid_argument("mpFlow::solver::Inverse::solve: wrong number of images");
         const unsigned Mm = calculation[0]->rows, Md = calculation[0]->cols, P = parallelImages_;
-        const size_t per = (size_t)Mm * Md;
-        float *calc = nullptr, *meas = nullptr, *out = nullptr;
-        detail::cuda(cudaMallocAsync((void**)&calc, sizeof(float) * per * P * 2, stream), "mpFlow::solver::Inverse::solve");
+        const size_t per = (size_t)Mm * Md, w = sizeof(dataType);
+        dataType *calc = nullptr, *meas = nullptr, *out = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&calc, w * per * P * 2, stream), "mpFlow::solver::Inverse::solve");
         meas = calc + per * P;
         const unsigned E = mesh->elements.rows();
-        detail::cuda(cudaMallocAsync((void**)&out, sizeof(float) * (size_t)E * P, stream), "mpFlow::solver::Inverse::solve");
+        detail::cuda(cudaMallocAsync((void**)&out, w * (size_t)E * P, stream), "mpFlow::solver::Inverse::solve");
         for (unsigned p = 0; p < P; ++p) {
-            cudaMemcpy2DAsync(calc + p * per, sizeof(float) * Mm, calculation[p]->deviceData,
-                              sizeof(float) * calculation[p]->dataRows, sizeof(float) * Mm, Md, cudaMemcpyDeviceToDevice,
-                              stream);
-            cudaMemcpy2DAsync(meas + p * per, sizeof(float) * Mm, measurement[p]->deviceData,
-                              sizeof(float) * measurement[p]->dataRows, sizeof(float) * Mm, Md, cudaMemcpyDeviceToDevice,
-                              stream);
+            cudaMemcpy2DAsync(calc + p * per, w * Mm, calculation[p]->deviceData, w * calculation[p]->dataRows, w * Mm,
+                              Md, cudaMemcpyDeviceToDevice, stream);
+            cudaMemcpy2DAsync(meas + p * per, w * Mm, measurement[p]->deviceData, w * measurement[p]->dataRows, w * Mm,
+                              Md, cudaMemcpyDeviceToDevice, stream);
         }
-        const int st = mpf_inverse_solve(jacobian->owner, (int32_t)regularizationType_, regularizationFactor_, (int32_t)P,
-                                         jacobian->deviceData, calc, meas, out, stream);
+        const double factor = detail::real_part(regularizationFactor_);
+        int st;
+        if constexpr (detail::is_complex<dataType>::value)
+            st = mpf_inverse_solve_complex(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P,
+                                           reinterpret_cast<const float*>(jacobian->deviceData),
+                                           reinterpret_cast<const float*>(calc), reinterpret_cast<const float*>(meas),
+                                           reinterpret_cast<float*>(out), stream);
+        else
+            st = mpf_inverse_solve(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P,
+                                   jacobian->deviceData, calc, meas, out, stream);
         if (st == MPF_OK)
-            cudaMemcpy2DAsync(result->deviceData, sizeof(float) * result->dataRows, out, sizeof(float) * E,
-                              sizeof(float) * E, P, cudaMemcpyDeviceToDevice, stream);
+            cudaMemcpy2DAsync(result->deviceData, w * result->dataRows, out, w * E, w * E, P, cudaMemcpyDeviceToDevice,
+                              stream);
         cudaFreeAsync(calc, stream);
         cudaFreeAsync(out, stream);
         detail::check(st, "mpFlow::solver::Inverse::solve");

@@ -2,6 +2,9 @@
 // solve, a differential reconstruction of a low-conductivity inclusion, and a
 // text round trip of the voltages.  Prints one JSON line; exit status 0 when
 // every check holds.  Usage: facade_demo <rings> <electrodes>
+//        facade_demo complex <rings> <electrodes> <result file>: the complex
+//        (thrust::complex-style) model and differential reconstruction
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <sstream>
@@ -12,6 +15,69 @@
 using namespace mpFlow;
 typedef models::EIT<numeric::ConjugateGradient, FEM::Equation<float, FEM::basis::Linear, false>> Model;
 typedef models::EIT<numeric::BiCGSTAB, FEM::Equation<float, FEM::basis::Linear, false>> ModelBi;
+typedef std::complex<float> cfloat;
+typedef models::EIT<numeric::ConjugateGradient, FEM::Equation<cfloat, FEM::basis::Linear, false>> ModelZ;
+
+// complex admittivity: forward solve at 1 + 0.15i, an inclusion of
+// 0.5 + 0.3i at (0.3, 0.2) radius 0.25, solveDifferential with the identity
+// regulariser; writes the reconstruction (re im per element) to `file`
+static int complex_case(unsigned rings, unsigned L, std::string const& file) {
+    cudaStream_t stream = nullptr;
+    cublasHandle_t handle = nullptr;
+    auto mesh = numeric::IrregularMesh::ring(rings);
+    auto ports = FEM::Ports::circularBoundary(L, 0.1, mesh);
+    auto pattern = std::make_shared<numeric::Matrix<int>>(L, L, stream);
+    for (unsigned j = 0; j < L; ++j) {
+        (*pattern)(j, j) = 1;
+        (*pattern)((j + 1) % L, j) = -1;
+    }
+    pattern->copyToDevice(stream);
+    auto sources = std::make_shared<FEM::Sources<cfloat>>(FEM::Sources<cfloat>::Open, cfloat(1e-3f), ports, pattern,
+                                                          pattern, stream);
+    auto model = std::make_shared<ModelZ>(mesh, sources, cfloat(1.f), handle, stream, 1, 1.0, 1.0);
+    model->options.tol = 1e-7;
+    const unsigned E = mesh->elements.rows();
+    auto target = std::make_shared<numeric::Matrix<cfloat>>(E, 1, stream, cfloat(1.f, 0.15f));
+    for (unsigned e = 0; e < E; ++e) {
+        auto xy = mesh->elementNodes(e);
+        const double cx = (xy(0, 0) + xy(1, 0) + xy(2, 0)) / 3.0, cy = (xy(0, 1) + xy(1, 1) + xy(2, 1)) / 3.0;
+        if ((cx - 0.3) * (cx - 0.3) + (cy - 0.2) * (cy - 0.2) < 0.0625) (*target)(e, 0) = cfloat(0.5f, 0.3f);
+    }
+    target->copyToDevice(stream);
+    solver::Solver<ModelZ> solver(model, 1, handle, stream);
+    solver.referenceDistribution->fill(cfloat(1.f, 0.15f), stream);
+    solver.preSolve(handle, stream);
+    auto V0 = solver.calculation[0];
+    V0->copyToHost(stream);
+    double sumRe = 0.0, sumIm = 0.0;
+    for (unsigned i = 0; i < V0->rows; ++i)
+        for (unsigned j = 0; j < V0->cols; ++j) {
+            sumRe += (*V0)(i, j).real();
+            sumIm += (*V0)(i, j).imag();
+        }
+    auto Vt = model->solve(target, handle, stream);
+    solver.measurement[0]->copy(Vt, stream);
+    solver.inverseSolver->updateJacobian(model->jacobian, handle, stream);
+    // the Jacobian of the reference distribution (preSolve's), for the factor
+    model->solve(solver.referenceDistribution, handle, stream);
+    const size_t nj = (size_t)model->jacobian->dataRows * E;
+    std::vector<cfloat> J(nj);
+    cudaMemcpy(J.data(), model->jacobian->deviceData, sizeof(cfloat) * nj, cudaMemcpyDeviceToHost);
+    double jj = 0.0;
+    for (auto v : J) jj += std::norm(v);
+    const float factor = (float)(0.05 * std::sqrt(jj / model->jacobian->rows));
+    solver.inverseSolver->setRegularizationParameter(cfloat(factor), solver::Inverse<cfloat>::identity, handle, stream);
+    auto sigma = solver.solveDifferential(handle, stream);
+    std::vector<cfloat> s(E);
+    cudaMemcpy(s.data(), sigma->deviceData, sizeof(cfloat) * E, cudaMemcpyDeviceToHost);
+    FILE* f = fopen(file.c_str(), "w");
+    if (!f) return 3;
+    for (auto v : s) fprintf(f, "%.9g %.9g\n", v.real(), v.imag());
+    fclose(f);
+    printf("{\"complex\": true, \"sum_v_re\": %.9e, \"sum_v_im\": %.9e, \"factor\": %.9e, \"ok\": true}\n", sumRe,
+           sumIm, factor);
+    return 0;
+}
 
 // json-selftest: parse a configuration without touching the GPU
 static int json_selftest() {
@@ -51,6 +117,14 @@ static int from_config(std::string const& dir) {
 
 int main(int argc, char** argv) {
     if (argc > 1 && std::string(argv[1]) == "json-selftest") return json_selftest();
+    if (argc > 4 && std::string(argv[1]) == "complex") {
+        try {
+            return complex_case((unsigned)atoi(argv[2]), (unsigned)atoi(argv[3]), argv[4]);
+        } catch (std::exception const& ex) {
+            printf("{\"error\": \"%s\", \"ok\": false}\n", ex.what());
+            return 2;
+        }
+    }
     if (argc > 2 && std::string(argv[1]) == "config") {
         try {
             return from_config(argv[2]);

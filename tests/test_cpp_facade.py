@@ -84,3 +84,40 @@ def test_facade_reconstruction_matches_python(tmp_path):
     V = V[0].cpu().numpy().astype(np.float64)
     assert abs(V.sum() - out["sum_v"]) <= 1e-6 * np.abs(V).sum()
     assert abs(np.abs(V).sum() - out["sum_abs_v"]) <= 1e-6 * np.abs(V).sum()
+
+
+@pytest.mark.gpu
+def test_facade_complex_reconstruction_matches_python(tmp_path):
+    """models::EIT / solver::Solver instantiated on a complex data type (the
+    reference's thrust::complex<float> instantiations): forward solve and
+    differential reconstruction through the facade agree with the Python
+    binding of mpf_eit_forward_complex + mpf_inverse_solve_complex."""
+    exe = _build(tmp_path)
+    res_file = tmp_path / "complex_result.txt"
+    r = subprocess.run([exe, "complex", "16", "16", str(res_file)], capture_output=True, text=True, timeout=300)
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert r.returncode == 0 and out["ok"], (r.stdout, r.stderr)
+    got = np.loadtxt(res_file)
+    got = got[:, 0] + 1j * got[:, 1]
+    import torch
+    import mpflow_gb300 as mp
+    from conftest import make_setup
+    mesh, src, _ = make_setup(rings=16, ports=16)
+    model = mp.EIT(mesh, src, 1.0)
+    E = mesh.elements.shape[0]
+    opts = mp.SolveOptions(tol=1e-7, solver="bicgstab")
+    ref = torch.full((1, E), 1.0 + 0.15j, dtype=torch.complex64, device="cuda")
+    V0, J = model.solve_complex(ref, opts, jacobian=True)
+    c = mesh.nodes[mesh.elements].mean(axis=1)
+    inside = (c[:, 0] - 0.3) ** 2 + (c[:, 1] - 0.2) ** 2 < 0.0625
+    g = ref.clone()
+    g[0, torch.tensor(inside, device="cuda")] = 0.5 + 0.3j
+    Vt = model.solve_complex(g, opts)
+    V0n = V0[0].cpu().numpy()
+    scale = np.abs(V0n).sum()
+    assert abs(V0n.real.sum() - out["sum_v_re"]) <= 1e-5 * scale
+    assert abs(V0n.imag.sum() - out["sum_v_im"]) <= 1e-5 * scale
+    want = (1.0 + 0.15j) + model.inverse_complex(J[0], V0, Vt, out["factor"], "identity")[0].cpu().numpy()
+    delta = np.abs(want - (1.0 + 0.15j)).max()
+    assert delta > 1e-3
+    assert np.abs(got - want).max() <= 1e-4 * delta

@@ -175,3 +175,27 @@ def test_complex_oracle_jacobian_reduces_to_real():
     _, Jz = oracle.eit_forward_complex(orc, g.astype(np.complex128), want_jacobian=True)
     assert np.abs(Jz.imag).max() <= 1e-12 * np.abs(J).max()
     assert np.abs(Jz.real - J).max() <= 1e-8 * np.abs(J).max()
+
+
+def test_complex_inverse_dual_equals_primal():
+    """The complex inverse's dual form: with the reference's plain
+    transpose (CUBLAS_OP_T on complex data), J^T (J J^T + mu I)^-1 y equals
+    (J^T J + mu I)^-1 J^T y for the complex symmetric systems, on the
+    oracle's complex Jacobian."""
+    mesh, _, orc = make_setup(rings=12, ports=8, width=0.3, components=2, height=2.0)
+    E = mesh.elements.shape[0]
+    g0 = np.full(E, 1.0 + 0.2j)
+    V0, J = oracle.eit_forward_complex(orc, g0, want_jacobian=True)
+    g = g0.copy()
+    g[: E // 5] = 0.5 + 0.4j
+    Vt = oracle.eit_forward_complex(orc, g, want_jacobian=False)
+
+    def flat(V):
+        return oracle.flatten_measurement(V.real, orc) + 1j * oracle.flatten_measurement(V.imag, orc)
+
+    y = flat(Vt) - flat(V0)
+    mu = 0.1 * float((np.abs(J) ** 2).sum(axis=0).mean())
+    primal = oracle.inverse_regularised(J, y[:, None], 1.0, np.sqrt(mu), "identity")[:, 0]
+    dual = J.T @ np.linalg.solve(J @ J.T + mu * np.eye(J.shape[0]), y)
+    assert np.abs(primal.imag).max() > 1e-3 * np.abs(primal).max()
+    assert np.abs(primal - dual).max() <= 1e-9 * np.abs(primal).max()

@@ -199,3 +199,19 @@ def test_complex_inverse_dual_equals_primal():
     dual = J.T @ np.linalg.solve(J @ J.T + mu * np.eye(J.shape[0]), y)
     assert np.abs(primal.imag).max() > 1e-3 * np.abs(primal).max()
     assert np.abs(primal - dual).max() <= 1e-9 * np.abs(primal).max()
+
+
+def test_mesh_refinement_convergence_homogeneous_disk():
+    """Electrode voltages of the homogeneous disk converge under mesh
+    refinement.  Six electrodes of width pi/6 start and end on boundary nodes
+    at every even ring count, so only the discretisation changes between
+    meshes; the differences of successive refinements must shrink at least
+    like h (P1 elements: about h^2)."""
+    Vs = []
+    for rings in (6, 12, 24, 48):
+        mesh, _, orc = make_setup(rings=rings, ports=6, width=np.pi / 6)
+        V, _, _ = oracle.eit_forward(orc, np.ones(mesh.elements.shape[0]), tol=1e-13, want_jacobian=False)
+        Vs.append(np.asarray(V, np.float64))
+    d = [np.abs(Vs[k + 1] - Vs[k]).max() for k in range(3)]
+    assert all(d[k + 1] < 0.5 * d[k] for k in range(2)), d
+    assert np.abs(Vs[-1] - Vs[-2]).max() < 1e-2 * np.abs(Vs[-1]).max(), d

@@ -180,6 +180,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def measured_bf16_tflops():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
 def profiled_traffic(kernel: str):
     """DRAM bytes per launch per (frame, harmonic) group of a CG kernel from the
     committed ncu summary (line '<kernel> dram_bytes_per_group_launch: X'),
@@ -501,6 +510,20 @@ def run_gb300(a):
                 "traffic": traffic * groups if traffic else None,
                 "algorithmic_bytes": float(by[dom]), "launch_ms": float(ms[dom])}
 
+    # J J^T of the GN step on the tensor cores at this workload's size (all
+    # frames of a step in one launch), CUDA events
+    rows_j = model.jacobian_rows
+    jjt_ms = mp.profile_gram(F, rows_j, round_up(E, 64), reps=5)
+    bf16_peak, bf16_kind = measured_bf16_tflops()
+    jjt_tflops = 2.0 * rows_j * rows_j * E * F / (jjt_ms * 1e-3) / 1e12  # GEMM-equivalent flops
+    nt = rows_j // 128  # 128 x 128 output tiles; only those on and above the diagonal are computed
+    executed = jjt_tflops * 3.0 * (nt * (nt + 1) / 2) / (nt * nt)
+    jjt = {"frames": F, "rows": rows_j, "elements": E, "ms": jjt_ms, "tflops_gemm_equivalent": jjt_tflops,
+           "frac_of_bf16_peak_over_3": jjt_tflops / (bf16_peak / 3.0),
+           "tflops_executed": executed, "frac_executed_of_bf16_peak": executed / bf16_peak,
+           "peak_source": f"{bf16_kind} bf16_tflops (burst); 3 products hi.hi + hi.lo + lo.hi",
+           "note": "upper-triangle tiles only, so the GEMM-equivalent rate can exceed peak / 3"}
+
     if rank != 0:
         return
     cpu = None
@@ -544,6 +567,7 @@ def run_gb300(a):
         "cg_kernel_ms": {k: float(v) for k, v in zip(names, ms)},
         "cg_kernel_gbs": {k: float(v) for k, v in zip(names, gbs)},
         "roofline": roofline,
+        "jjt_tensor_core": jjt,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(vmeas[0].numel() * 4), "d2h_bytes_per_step": int(F * E * 4)},

@@ -481,6 +481,14 @@ int mpf_gram_split_bf16(int32_t batch, int32_t rows, int32_t cols, const float* 
 int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda,
                                 float* C, mpf_stream_t stream);
 
+/* Measurement hook: device time of the GN step's J J^T (split-BF16 tcgen05
+ * Gram of batch row-major rows x cols operands plus its split-K reduction
+ * into FP64 with a diagonal shift) on synthetic operands the call allocates,
+ * averaged over `reps` launches timed with CUDA events on `stream`.
+ * rows % 128 == 0, cols % 64 == 0.  Synchronises. */
+int mpf_profile_gram(int32_t batch, int32_t rows, int32_t cols, int32_t reps, double* ms_per_launch,
+                     mpf_stream_t stream);
+
 /* Batched FP64 Cholesky solve of (A + shift I) X = B, A n x n symmetric
  * (row-major == column-major), B n x nrhs column-major, per batch entry.
  * A is overwritten by its factor.  info[batch] (device ints) receives 0 or

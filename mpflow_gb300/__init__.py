@@ -6,11 +6,12 @@ package does not touch the GPU; the first call that needs the library loads
 it and raises if it is missing (there is no CPU fallback).
 """
 from .eit import (EIT, FIXED, EITBatch, OPEN, IrregularMesh, Ports, SolveOptions, Sources, SparseMatrix,
-                  adjacent_pattern, cholesky_solve_f64, data_rows, gram_split_bf16)
+                  adjacent_pattern, cholesky_solve_f64, data_rows, gram_split_bf16, profile_gram)
 from ._ffi import MpfError, lib
-from .learned import MLP, generate_pairs, inclusion_frames, train_warm_start
+from .learned import MLP, generate_pairs, gn_labels, inclusion_frames, train_warm_start, zero_network
 
 __all__ = ["EIT", "EITBatch", "SparseMatrix", "IrregularMesh", "Ports", "Sources", "SolveOptions",
-           "adjacent_pattern", "data_rows", "gram_split_bf16", "cholesky_solve_f64", "MpfError", "lib", "OPEN",
-           "FIXED", "MLP", "generate_pairs", "inclusion_frames", "train_warm_start"]
+           "adjacent_pattern", "data_rows", "gram_split_bf16", "profile_gram", "cholesky_solve_f64", "MpfError", "lib",
+           "OPEN", "FIXED", "MLP", "generate_pairs", "gn_labels", "inclusion_frames", "train_warm_start",
+           "zero_network"]
 __version__ = "0.1.0"

@@ -400,6 +400,11 @@ int mpf_gram_split_bf16(int32_t batch, int32_t rows, int32_t cols, const float* 
     })
 }
 
+int mpf_profile_gram(int32_t batch, int32_t rows, int32_t cols, int32_t reps, double* ms_per_launch,
+                     mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::dense_profile_gram(batch, rows, cols, reps, ms_per_launch, (cudaStream_t)stream); })
+}
+
 int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda, float* C,
                                 mpf_stream_t stream) {
     MPF_GUARD({

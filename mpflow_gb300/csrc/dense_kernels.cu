@@ -551,6 +551,55 @@ int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi,
     return gram_run(batch, rows, cols, hi, lo, ld, nullptr, A64, shift, work, workFloats, s, nullptr, frameMask);
 }
 
+// Measurement hook for the J J^T of the GN step: batch x (rows x cols) BF16
+// hi/lo operands filled with hashed values in [-1, 1), one warm-up, then
+// `reps` launches of the whole Gram (tcgen05 kernel + split-K reduction into
+// FP64 with a shift) timed with CUDA events on `s`.
+__global__ void k_fill_bf16_hash(size_t n, uint32_t seed, __nv_bfloat16* __restrict__ a) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        uint32_t h = (uint32_t)i * 2654435761u ^ seed;
+        h ^= h >> 16;
+        h *= 0x7feb352du;
+        h ^= h >> 15;
+        a[i] = __float2bfloat16((float)(h & 0xffffu) * (1.f / 32768.f) - 1.f);
+    }
+}
+
+int dense_profile_gram(int batch, int rows, int cols, int reps, double* msPerLaunch, cudaStream_t s) {
+    MPF_CHECK(batch >= 1 && reps >= 1 && msPerLaunch, MPF_EINVAL, "mpf_profile_gram: bad arguments");
+    MPF_CHECK(rows % kTile == 0 && cols % kBK == 0, MPF_EINVAL,
+              "mpf_profile_gram: rows %% %d and cols %% %d must be 0 (rows=%d cols=%d)", kTile, kBK, rows, cols);
+    const size_t n = (size_t)batch * rows * cols;
+    DevBuf<__nv_bfloat16> hi, lo;
+    DevBuf<float> work;
+    DevBuf<double> A;
+    MPF_TRY(hi.alloc(n));
+    MPF_TRY(lo.alloc(n));
+    MPF_TRY(work.alloc(dense_gram_work_floats(batch, rows, cols)));
+    MPF_TRY(A.alloc((size_t)batch * rows * rows));
+    k_fill_bf16_hash<<<2048, 256, 0, s>>>(n, 0x1234u, hi.ptr);
+    k_fill_bf16_hash<<<2048, 256, 0, s>>>(n, 0x9876u, lo.ptr);
+    MPF_LAUNCHED(2);
+    MPF_TRY(gram_run(batch, rows, cols, hi.ptr, lo.ptr, cols, nullptr, A.ptr, 1.0, work.ptr, work.count, s));
+    cudaEvent_t e0, e1;
+    MPF_CUDA(cudaEventCreate(&e0));
+    MPF_CUDA(cudaEventCreate(&e1));
+    MPF_CUDA(cudaEventRecord(e0, s));
+    for (int r = 0; r < reps; ++r)
+        MPF_TRY(gram_run(batch, rows, cols, hi.ptr, lo.ptr, cols, nullptr, A.ptr, 1.0, work.ptr, work.count, s));
+    MPF_CUDA(cudaEventRecord(e1, s));
+    MPF_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    MPF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    bool aborted = false;
+    MPF_TRY(dense_gram_check_abort(&aborted));
+    MPF_CHECK(!aborted, MPF_ETIMEOUT, "mpf_profile_gram: a pipeline wait timed out");
+    *msPerLaunch = (double)ms / reps;
+    return MPF_OK;
+}
+
 int dense_gram_f64_exact(int batch, int rows, int cols, const float* J, int ld, double shift, double* A64,
                          const int* frameMask, cudaStream_t s) {
     MPF_CHECK(rows % 64 == 0 && cols % 32 == 0 && ld >= cols, MPF_EINVAL,

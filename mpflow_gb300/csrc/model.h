@@ -258,6 +258,7 @@ int dense_gram_f64_shift(int batch, int rows, int cols, const __nv_bfloat16* hi,
                          int ld, double shift, double* A64, float* work, size_t workFloats, cudaStream_t s,
                          const int* frameMask = nullptr);
 int dense_gram_check_abort(bool* aborted);
+int dense_profile_gram(int batch, int rows, int cols, int reps, double* msPerLaunch, cudaStream_t s);
 // A64 = J J^T + shift I in FP64 from FP32 J (rows % 64 == 0, cols % 32 == 0)
 int dense_gram_f64_exact(int batch, int rows, int cols, const float* J, int ld, double shift, double* A64,
                          const int* frameMask, cudaStream_t s);

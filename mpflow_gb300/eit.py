@@ -595,6 +595,14 @@ def gram_split_bf16(A):
     return C
 
 
+def profile_gram(batch: int, rows: int, cols: int, reps: int = 5) -> float:
+    """Device milliseconds of one J J^T of the GN step (mpf_profile_gram)
+    for batch x (rows x cols) operands."""
+    ms = ctypes.c_double(0.0)
+    check(lib().mpf_profile_gram(int(batch), int(rows), int(cols), int(reps), ctypes.byref(ms), _stream()))
+    return ms.value
+
+
 def cholesky_solve_f64(A, Bm, shift: float = 0.0):
     """Solve (A + shift I) X = B for batches of float64 CUDA matrices (A overwritten)."""
     import torch

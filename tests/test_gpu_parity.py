@@ -403,3 +403,12 @@ def test_fixed_sources_match_oracle(components, height, pc):
     for c in range(components):
         err = np.abs(Fg[c][:, :n].T - Fo[c]).max() / np.abs(Fo[c]).max()
         assert err < 1e-5, (c, err)
+
+
+def test_profile_gram_hook():
+    """mpf_profile_gram (the bench's J J^T timing) runs and rejects bad shapes."""
+    import mpflow_gb300 as mp
+    ms = mp.profile_gram(2, 256, 512, reps=2)
+    assert 0.0 < ms < 1e3
+    with pytest.raises(mp.MpfError):
+        mp.profile_gram(1, 100, 512)

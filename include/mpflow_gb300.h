@@ -34,7 +34,7 @@ enum mpf_status {
     MPF_EBREAKDOWN = 5,  /* non-positive pivot / curvature (Cholesky info > 0) */
     MPF_ETIMEOUT = 6,    /* a bounded device-side wait ran out */
     MPF_EFULL = 7,       /* ELL row has more than 32 entries (std::logic_error) */
-    MPF_ENOTSUP = 8      /* valid request this build does not implement */
+    MPF_ENOTSUP = 8      /* valid request this library does not implement */
 };
 
 /* Source types, include/mpflow/fem/sources.h:31-34 (Sources::Type).  OPEN:

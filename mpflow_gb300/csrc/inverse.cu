@@ -255,7 +255,7 @@ int inverse_solve(mpf_eit* m, int reg, double factor, int images, const float* J
         // primal: (J^T J + mu R) dsigma = J^T y on the E x E system
         MPF_CHECK(n <= 6144, MPF_ENOTSUP,
                   "mpf_inverse_solve: NOSER and Laplacian regularisation solve the E x E system; %d elements exceed "
-                  "this build's limit of 6144",
+                  "this library's limit of 6144",
                   E);
         // J as row-major [rowsJ][n] (for J^T y) and J^T as row-major [n][rowsJ] (for the Gram)
         MPF_TRY(m->invJ.alloc((size_t)2 * rowsJ * n));

@@ -397,7 +397,7 @@ int inverse_solve_complex(mpf_eit* m, int reg, double factor, int images, const 
         const int n = round_up(E, 32);
         MPF_CHECK(n <= 6144, MPF_ENOTSUP,
                   "mpf_inverse_solve_complex: NOSER and Laplacian regularisation solve the E x E system; %d elements "
-                  "exceed this build's limit of 6144",
+                  "exceed this library's limit of 6144",
                   E);
         MPF_TRY(Jrow.alloc((size_t)rowsJ * n));
         MPF_TRY(Jt.alloc((size_t)n * rowsJ));

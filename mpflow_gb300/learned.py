@@ -8,7 +8,7 @@ of every element.  Its training pairs are made by the forward solver itself
 (EIT.solve on seeded inclusion phantoms), its training and inference run in
 the library's own kernels (mpf_mlp_*: BF16 tcgen05 GEMMs with FP32
 accumulation, Adam on FP32 master weights), and the plain Gauss-Newton
-iteration is its judge: EIT.gn_solve_learned keeps a prediction only where it
+iteration decides: EIT.gn_solve_learned keeps a prediction only where it
 lowers the data residual below the homogeneous start's and then iterates to
 the target.
 """

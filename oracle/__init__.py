@@ -1,7 +1,8 @@
 """FP64 CPU oracle for mpFlow's EIT hot path (TEST INFRASTRUCTURE ONLY).
 
-This package is the checker: only ``tests/``, ``__graft_entry__.smoke()`` and
-the CPU-baseline leg of ``bench.py`` may import it.  The product library in
+It is the reference results the tests compare against: only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may
+import it.  The product library in
 ``mpflow_gb300`` never imports or links anything here.
 
 The numerical work lives in ``eit_oracle.c`` (an FP64 restatement of the

@@ -19,6 +19,7 @@
 // (P^T r).y to r^T D^-1 r and updates the CG scalars and convergence masks
 // of every group.
 #include <algorithm>
+#include <atomic>
 
 #include "model.h"
 
@@ -339,10 +340,14 @@ size_t coarse_solve_smem(int ncPad) { return ((size_t)(ncPad + 32) * 33 + 32 * 3
 template <int KP>
 int launch_coarse_kp(const CgProblem& P, bool init, cudaStream_t s, bool count) {
     const size_t smem = coarse_apply_smem(P.ncPad, KP);
-    static size_t configured = 0;
-    if (smem > configured) {
+    // the attribute is per device: remember the size set on each
+    static std::atomic<size_t> configured[64];
+    int dev = 0;
+    MPF_CUDA(cudaGetDevice(&dev));
+    MPF_CHECK(dev >= 0 && dev < 64, MPF_EINVAL, "coarse correction: device ordinal %d out of range", dev);
+    if (smem > configured[dev].load()) {
         MPF_CUDA(cudaFuncSetAttribute(k_coarse<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
+        configured[dev].store(smem);
     }
     k_coarse<KP><<<dim3(P.ncPad / kCoarseRows, P.G), kCoarseThreads, smem, s>>>(P, init ? 1 : 0);
     if (count) {
@@ -379,10 +384,13 @@ int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, 
     MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s));
     k_coarse_prep<<<dim3(cp.ncPad / 32, P.G), 32, 0, s>>>(cp.ncPad, Ac64, Lc, LinvD);
     const size_t smem = coarse_solve_smem(cp.ncPad);
-    static size_t configured = 0;
-    if (smem > configured) {
+    static std::atomic<size_t> configured[64];
+    int dev = 0;
+    MPF_CUDA(cudaGetDevice(&dev));
+    MPF_CHECK(dev >= 0 && dev < 64, MPF_EINVAL, "coarse setup: device ordinal %d out of range", dev);
+    if (smem > configured[dev].load()) {
         MPF_CUDA(cudaFuncSetAttribute(k_coarse_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
+        configured[dev].store(smem);
     }
     k_coarse_inverse<<<dim3(cp.ncPad / 32, P.G), kCT, smem, s>>>(cp.ncPad, Lc, LinvD, Binv);
     MPF_LAUNCHED(2);

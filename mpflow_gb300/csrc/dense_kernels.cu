@@ -466,17 +466,24 @@ __global__ void k_wait_selftest(int* flag, unsigned long long limitNs) {
     if (!mbar_wait(smem_u32(&bar), 0, &localAbort, limitNs)) atomicExch(flag, 1);
 }
 
+// one pipeline abort flag per device (a kernel must not touch another
+// device's memory), allocated on first use on the current device
 int* abort_flag_device() {
-    static int* flag = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) {
-            flag = nullptr;
-            return;
+    static std::mutex mu;
+    static int* flags[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!flags[dev]) {
+        int* f = nullptr;
+        if (cudaMalloc(&f, sizeof(int)) != cudaSuccess) return nullptr;
+        if (cudaMemset(f, 0, sizeof(int)) != cudaSuccess) {
+            cudaFree(f);
+            return nullptr;
         }
-        cudaMemset(flag, 0, sizeof(int));
-    });
-    return flag;
+        flags[dev] = f;
+    }
+    return flags[dev];
 }
 
 }  // namespace
@@ -527,11 +534,8 @@ static int gram_run(int batch, int rows, int cols, const __nv_bfloat16* hi, cons
     MPF_TRY(make_bf16_map(&mLo, lo, batch * rows, ld));
     int* flag = flagOverride ? flagOverride : abort_flag_device();
     MPF_CHECK(flag != nullptr, MPF_ENOMEM, "gram: abort flag allocation failed");
-    static bool attr = false;
-    if (!attr) {
-        MPF_CUDA(cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmem));
-        attr = true;
-    }
+    // per device and cheap: set on every call
+    MPF_CUDA(cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmem));
     GramArgs ga{rows, kblocks, tiles, nt, splits, work, flag, frameMask};
     k_gram_tc<<<dim3(tiles, splits, batch), 128, kGramSmem, s>>>(mHi, mLo, ga);
     MPF_LAUNCHED(1);

@@ -341,11 +341,8 @@ static int gemm(mpf_mlp* n, const __nv_bfloat16* A, int M, int lda, const __nv_b
     MPF_TRY(make_bf16_map(&mB, Bm, N, ldb));
     const int kblocks = K / kBK, tiles = (M / kTile) * (N / kTile);
     const int splits = allowSplit ? gemm_splits(tiles, kblocks) : 1;
-    static bool attr = false;
-    if (!attr) {
-        MPF_CUDA(cudaFuncSetAttribute(k_gemm_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
-        attr = true;
-    }
+    // per device and cheap: set on every call
+    MPF_CUDA(cudaFuncSetAttribute(k_gemm_nt, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
     GemmArgs ga{kblocks, splits, splits > 1 ? n->part.ptr : out, splits > 1 ? N : ldOut, (size_t)M * N,
                 n->flag.ptr};
     MPF_CHECK(splits == 1 || (size_t)splits * M * N <= n->part.count, MPF_EINVAL, "mlp gemm: split buffer too small");

@@ -60,3 +60,17 @@ def test_selftest_rejects_bad_timeout_without_gpu():
     L = mpflow_gb300.lib()
     assert L.mpf_selftest_bounded_wait(0, None) == 1
     assert L.mpf_selftest_bounded_wait(3000000, None) == 1
+
+
+def test_new_entry_points_reject_bad_arguments_without_gpu():
+    """Argument checks of the complex inverse, the learned prior and the
+    Gram measurement hook run before any device work."""
+    L = mpflow_gb300.lib()
+    assert L.mpf_inverse_solve_complex(None, 0, 1.0, 1, None, None, None, None, None) == 1
+    assert b"model == nullptr" in L.mpf_last_error()
+    assert L.mpf_eit_learned_prior(None, 1.0, None) == 1
+    assert L.mpf_eit_learned_prior_apply(None, 1, None, None, 0, 0, None) == 1
+    ms = ctypes.c_double(0.0)
+    assert L.mpf_profile_gram(1, 100, 64, 1, ctypes.byref(ms), None) == 1
+    assert b"rows" in L.mpf_last_error()
+    assert L.mpf_profile_gram(0, 128, 64, 1, ctypes.byref(ms), None) == 1

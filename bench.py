@@ -11,14 +11,16 @@ conductivity, until every frame's relative data residual
 [0.1, 10]) on a 1 S/m background; V_meas from the forward model with FP64
 refinement to 1e-9 (noise-free).
 
-The headline value is the learned path: a network trained (before the timed
-region) on pairs that the forward solver generates predicts each frame's
-Gauss-Newton start, then batched GN iterates to the target (frames whose
-prediction does not lower the residual restart from the homogeneous
-distribution).  The same frames are also timed on the plain batched GN path
-and one frame at a time.  The metric is frames/s (frames that reach the
-target per second); the line also carries the CG SpMM bandwidth, the roofline
-of the dominant kernel and the CPU baseline.
+The headline value is the learned path.  Each frame's Gauss-Newton start is
+the linear one-step GN prior from the homogeneous point plus a network's
+correction.  The network is trained before the timed region on pairs the
+forward solver generates, with targets where batched GN from the prior
+converges.  Batched GN then iterates to the target; a frame whose start does
+not lower the residual restarts from the homogeneous distribution.  The same
+frames are also timed on the prior alone, on the plain batched GN path and
+one frame at a time.  The metric is frames/s (frames that reach the target
+per second).  The line also carries the CG SpMM bandwidth, the roofline of
+the dominant kernel, the tensor-core J J^T rate and the CPU baseline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 

@@ -1,7 +1,9 @@
 // EIT model: host-side setup of the device-resident structure and the
-// orchestration of the forward solve (EIT::solve, src/models/eit.cpp:139-213)
-// and of one regularised Gauss-Newton step (Solver::solveAbsolute,
-// src/solver/solver.cpp:196-225 with Inverse, src/solver/inverse.cpp:60-238).
+// orchestration of the forward solve (EIT::solve, src/models/eit.cpp:139-213),
+// of the regularised Gauss-Newton step and loop (Solver::solveAbsolute,
+// src/solver/solver.cpp:196-225 with Inverse, src/solver/inverse.cpp:60-238;
+// per-frame masks, undo and freeze of diverging frames), and of the learned
+// warm start (the linear one-step GN prior and the network's correction).
 #include <algorithm>
 #include <array>
 #include <chrono>

@@ -512,6 +512,14 @@ def run_gb300(a):
                 "traffic": traffic * groups if traffic else None,
                 "algorithmic_bytes": float(by[dom]), "launch_ms": float(ms[dom])}
 
+    # assembly and Jacobian kernels (HBM-bound), CUDA events on the launching stream
+    fem_ms, fem_by = model.profile_fem(torch.tensor(truth[0], device=dev), reps=5)
+    fem = {}
+    for i, name in enumerate(["k_assemble", "k_jacobian"]):
+        gbs_i = float(fem_by[i] / fem_ms[i] / 1e6)
+        fem[name] = {"ms": float(fem_ms[i]), "algorithmic_bytes": float(fem_by[i]), "gbs": gbs_i,
+                     "frac_of_hbm": gbs_i / peak, "frames": F}
+
     # J J^T of the GN step on the tensor cores at this workload's size (all
     # frames of a step in one launch), CUDA events
     rows_j = model.jacobian_rows
@@ -570,6 +578,7 @@ def run_gb300(a):
         "cg_kernel_gbs": {k: float(v) for k, v in zip(names, gbs)},
         "roofline": roofline,
         "jjt_tensor_core": jjt,
+        "fem_kernels": fem,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(vmeas[0].numel() * 4), "d2h_bytes_per_step": int(F * E * 4)},

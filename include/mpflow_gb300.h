@@ -313,6 +313,14 @@ int mpf_inverse_solve(mpf_eit_t model, int32_t regularization, double factor, in
                       const float* jacobian, const float* calculation, const float* measurement,
                       float* result, mpf_stream_t stream);
 
+/* Kernel timing hook for the FEM kernels: after a forward solve of `gamma`,
+ * times `reps` launches each of the assembly (S, R slot values of all
+ * frames) and of the Jacobian (split-BF16 J of all frames) with CUDA events
+ * on `stream`; ms[2] mean time of one launch, bytes[2] its algorithmic bytes.
+ * No reference counterpart (measurement support).  Synchronises. */
+int mpf_eit_profile_fem(mpf_eit_t model, int32_t frames, const float* gamma, int32_t reps, double* ms,
+                        double* bytes, mpf_stream_t stream);
+
 /* Kernel timing hook: runs `reps` CG iterations on the systems of `gamma`
  * and reports, for the SpMM, update and direction kernels, the mean CUDA-
  * event time of one launch (ms[3]) and its algorithmic bytes (bytes[3]).

@@ -124,6 +124,7 @@ SIGNATURES = {
     "mpf_eit_learned_input": (_I, [_P, _I, _P, _P, _P]),
     "mpf_eit_learned_prior": (_I, [_P, _D, _P]),
     "mpf_profile_gram": (_I, [_I, _I, _I, _I, _P, _P]),
+    "mpf_eit_profile_fem": (_I, [_P, _I, _P, _I, _P, _P, _P]),
     "mpf_inverse_solve_complex": (_I, [_P, _I, _D, _I, _P, _P, _P, _P, _P]),
     "mpf_eit_learned_prior_apply": (_I, [_P, _I, _P, _P, _I, _I, _P]),
     "mpf_gn_solve_learned": (_I, [_P, _P, _I, _P, _P, _D, _D, _I, ctypes.POINTER(SolveOpts), _P, _P, _P,

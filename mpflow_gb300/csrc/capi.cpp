@@ -52,6 +52,7 @@ void eit_destroy(mpf_eit* m);
 int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, double target, int maxIters,
              const mpf_solve_opts* o, int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s);
 int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
+int profile_fem(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
 int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
 int wait_selftest(int timeoutUs, cudaStream_t s);
@@ -262,6 +263,14 @@ int mpf_gn_solve(mpf_eit_t model, int32_t frames, float* gamma, const float* v_m
         MPF_CHECK(lambda >= 0.0 && target >= 0.0, MPF_EINVAL, "mpf_gn_solve: lambda and target must be >= 0");
         return mpf::gn_solve(model, frames, gamma, v_meas, lambda, target, max_gn_iters, opts, iterations, residual,
                              stats, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_profile_fem(mpf_eit_t model, int32_t frames, const float* gamma, int32_t reps, double* ms,
+                        double* bytes, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_profile_fem: model == nullptr");
+        return mpf::profile_fem(model, frames, gamma, reps, ms, bytes, (cudaStream_t)stream);
     })
 }
 

@@ -1133,6 +1133,46 @@ int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, doub
     return MPF_OK;
 }
 
+// Times the assembly and Jacobian kernels with CUDA events on `s`, on the
+// fields of a forward solve of gamma.  Algorithmic bytes per launch:
+//   assembly: E (12 connectivity + 36 K + 36 M) read once, and per frame
+//             4 E (gamma) + 8 nnz (S, R slot values written);
+//   Jacobian: per frame Ca K n 4 (fields of the active harmonics) + 52 E
+//             (connectivity, elemental matrices, gamma) + 4 rowsJ E (the
+//             split-BF16 J written).
+int profile_fem(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma && reps >= 1 && ms && bytes, MPF_EINVAL, "mpf_eit_profile_fem: bad arguments");
+    mpf_solve_opts o{};
+    o.tol = 1e-5;
+    const int st = eit_forward_ws(m, F, gamma, false, &o, nullptr, s);
+    if (st != MPF_OK && st != MPF_ENOCONV) return st;
+    MPF_TRY(ensure_workspace(m, F, false, true));
+    cudaEvent_t ev[3];
+    for (auto& e : ev) MPF_CUDA(cudaEventCreate(&e));
+    double acc[2] = {0.0, 0.0};
+    for (int r = 0; r < reps; ++r) {
+        MPF_CUDA(cudaEventRecord(ev[0], s));
+        MPF_TRY(eit_assemble(m, F, gamma, false, s));
+        MPF_CUDA(cudaEventRecord(ev[1], s));
+        MPF_TRY(eit_jacobian(m, F, gamma, nullptr, false, s));
+        MPF_CUDA(cudaEventRecord(ev[2], s));
+        MPF_CUDA(cudaEventSynchronize(ev[2]));
+        for (int k = 0; k < 2; ++k) {
+            float t = 0.f;
+            MPF_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+            acc[k] += t;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    const double E = m->E, n = m->n, K = m->K, Ca = m->Ca, rows = m->rowsJ;
+    ms[0] = acc[0] / reps;
+    ms[1] = acc[1] / reps;
+    bytes[0] = E * 84.0 + F * (E * 4.0 + 8.0 * (double)m->nnz);
+    bytes[1] = F * (Ca * K * n * 4.0 + 52.0 * E + 4.0 * rows * E);
+    return MPF_OK;
+}
+
 // Fixes the CG kernel variants (-1 = autotune); returns the variants a solve
 // with F frames uses (the autotuned ones once a cold solve has run).
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get) {

@@ -438,6 +438,15 @@ class EIT:
         check(lib().mpf_eit_cg_variants(self._h, None if sv is None else ptr(sv), int(frames), ptr(get)))
         return get
 
+    def profile_fem(self, gamma, reps: int = 10):
+        """Mean CUDA-event time (ms) and algorithmic bytes of one launch of
+        the assembly and the Jacobian kernels (mpf_eit_profile_fem)."""
+        g, F = self._frames(gamma)
+        ms = np.zeros(2)
+        by = np.zeros(2)
+        check(lib().mpf_eit_profile_fem(self._h, F, ptr(g), int(reps), ptr(ms), ptr(by), _stream()))
+        return ms, by
+
     def profile_cg(self, gamma, reps: int = 20):
         """Mean CUDA-event time (ms) and algorithmic bytes of one launch of the
         SpMM, update and direction kernels (mpf_eit_profile_cg)."""

@@ -412,3 +412,15 @@ def test_profile_gram_hook():
     assert 0.0 < ms < 1e3
     with pytest.raises(mp.MpfError):
         mp.profile_gram(1, 100, 512)
+
+
+def test_profile_fem_hook():
+    """mpf_eit_profile_fem (the bench's assembly / Jacobian timing)."""
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, _ = make_setup(rings=16, ports=16, components=2, height=2.0)
+    model = mp.EIT(mesh, src, 1.0, components=2, height=2.0)
+    g = torch.ones((2, mesh.elements.shape[0]), device="cuda")
+    ms, by = model.profile_fem(g, reps=2)
+    assert (ms > 0).all() and (by > 0).all()
+    assert by[1] > by[0]  # the Jacobian writes rowsJ x E per frame

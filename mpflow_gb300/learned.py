@@ -162,19 +162,23 @@ def generate_pairs(model, gammas: np.ndarray, batch: int = 64, options=None):
     return torch.cat(Vs), torch.tensor(gammas, device=f"cuda:{model.device}")
 
 
-def gn_labels(model, V, lam: float, target: float = 1e-3, max_iters: int = 4, batch: int = 64, options=None):
+def gn_labels(model, V, lam: float, target: float = 1e-3, max_iters: int = 4, batch: int = 64, options=None,
+              net0=None):
     """Training targets of the learned start over the model's linear prior
     (EIT.learned_prior): for every frame of V (count, Mm, Md), where batched
     Gauss-Newton from the prior converges (relative data residual <=
     target).  A frame that does not get there within max_iters updates keeps
     the prior itself (zero correction).  Returns (labels (count x E) CUDA
-    tensor, fraction of frames that converged)."""
+    tensor, fraction of frames that converged).  `net0`: the network whose
+    output is added to the prior during the GN runs, a zero network
+    (`zero_network`) by default."""
     import torch
     if getattr(model, "prior_lambda", None) is None:
         raise ValueError("gn_labels needs the model's linear prior (EIT.learned_prior)")
     E = model.mesh.elements.shape[0]
     L = V.shape[1] * V.shape[2]
-    net0 = zero_network(L, round_up(E, 128), device=model.device)
+    if net0 is None:
+        net0 = zero_network(L, round_up(E, 128), device=model.device)
     out = torch.empty((V.shape[0], E), dtype=torch.float32, device=V.device)
     converged = 0
     for i in range(0, V.shape[0], batch):

@@ -366,12 +366,12 @@ int mpf_matrix_elementwise(int32_t op, int32_t rows, int32_t cols, const float* 
 
 /* Column reductions into row 0 of each column of result (leading dimension
  * ldr), as Matrix::sum / vectorDotProduct / min / max leave them
- * (matrix.cpp:455-660): op 0 sum, 1 dot of A and B, 2 min, 3 max; FP64
+ * (src/numeric/matrix.cpp:455-660): op 0 sum, 1 dot of A and B, 2 min, 3 max; FP64
  * accumulation in a fixed order. */
 int mpf_matrix_column_reduce(int32_t op, int32_t rows, int32_t cols, const float* A, const float* B, int32_t ld,
                              float* result, int32_t ldr, mpf_stream_t stream);
 
-/* Matrix::multiply's cuBLAS GEMM (matrix.cpp:298-332): C (m x n) =
+/* Matrix::multiply's cuBLAS GEMM (src/numeric/matrix.cpp:298-332): C (m x n) =
  * op(A) op(B) with op(X) = X (trans 0) or X^T (trans 1), column-major,
  * FP32 on a tiled kernel of this library. */
 int mpf_matrix_multiply(int32_t trans_a, int32_t trans_b, int32_t m, int32_t n, int32_t k, const float* A,
@@ -493,7 +493,8 @@ int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const
  * Gram of batch row-major rows x cols operands plus its split-K reduction
  * into FP64 with a diagonal shift) on synthetic operands the call allocates,
  * averaged over `reps` launches timed with CUDA events on `stream`.
- * rows % 128 == 0, cols % 64 == 0.  Synchronises. */
+ * rows % 128 == 0, cols % 64 == 0.  No reference counterpart (measurement
+ * support).  Synchronises. */
 int mpf_profile_gram(int32_t batch, int32_t rows, int32_t cols, int32_t reps, double* ms_per_launch,
                      mpf_stream_t stream);
 

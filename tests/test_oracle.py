@@ -215,3 +215,47 @@ def test_mesh_refinement_convergence_homogeneous_disk():
     d = [np.abs(Vs[k + 1] - Vs[k]).max() for k in range(3)]
     assert all(d[k + 1] < 0.5 * d[k] for k in range(2)), d
     assert np.abs(Vs[-1] - Vs[-2]).max() < 1e-2 * np.abs(Vs[-1]).max(), d
+
+
+def test_complex_symmetric_cholesky_restatement():
+    """The complex inverse factors J J^T + mu I as L L^T with complex L and
+    no conjugation (zinverse.cu).  Restated here in FP64 numpy with the
+    same column order, Smith's division and the principal square root from
+    |z|, on a complex Gram of the oracle's complex Jacobian: L L^T
+    reproduces the matrix and the solve matches numpy's."""
+    mesh, _, orc = make_setup(rings=12, ports=8, width=0.3, components=2, height=2.0)
+    E = mesh.elements.shape[0]
+    _, J = oracle.eit_forward_complex(orc, np.full(E, 1.0 + 0.3j), want_jacobian=True)
+    n = J.shape[0]
+    mu = 0.05 * float((np.abs(J) ** 2).sum(axis=1).mean())
+    A = J @ J.T + mu * np.eye(n)
+
+    def zsqrt(z):
+        r = abs(z)
+        if z.real >= 0:
+            t = np.sqrt(0.5 * (r + z.real))
+            return complex(t, z.imag / (2 * t))
+        t = np.sqrt(0.5 * (r - z.real))
+        return complex(abs(z.imag) / (2 * t), np.copysign(t, z.imag))
+
+    def zdiv(a, b):
+        if abs(b.real) >= abs(b.imag):
+            r = b.imag / b.real
+            d = b.real + b.imag * r
+            return complex((a.real + a.imag * r) / d, (a.imag - a.real * r) / d)
+        r = b.real / b.imag
+        d = b.imag + b.real * r
+        return complex((a.real * r + a.imag) / d, (a.imag * r - a.real) / d)
+
+    L = A.copy()
+    for j in range(n):
+        L[j, j] = zsqrt(L[j, j])
+        for i in range(j + 1, n):
+            L[i, j] = zdiv(L[i, j], L[j, j])
+        L[j + 1:, j + 1:] -= np.tril(np.outer(L[j + 1:, j], L[j + 1:, j]))
+    L = np.tril(L)
+    assert np.abs(L @ L.T - A).max() <= 1e-12 * np.abs(A).max()
+    b = np.random.default_rng(2).standard_normal(n) + 1j * np.random.default_rng(3).standard_normal(n)
+    z = np.linalg.solve(L, b)            # forward: L z = b
+    x = np.linalg.solve(L.T, z)          # backward: L^T x = z (plain transpose)
+    assert np.abs(x - np.linalg.solve(A, b)).max() <= 1e-9 * np.abs(x).max()

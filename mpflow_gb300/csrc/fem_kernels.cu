@@ -113,15 +113,12 @@ __global__ void k_voltages(int F, int Ca, int KP, int Mm, int Md, const double* 
 // for all harmonics at once:
 //   J[d*MP + m][e] = -h p'(gamma_e) sd sm sum_c beta_c^2
 //                    sum_ij Y_c[n_i][ud] K_e[i+3j] Y_c[n_j][um]
-// A block owns 32 consecutive elements (one per lane) and the drive rows of
-// its blockIdx.z slice; warp w of slice z owns drive rows [g*DPT, (g+1)*DPT),
-// g = z * warps + w, and all MP measurement rows.  Fields of the 3 element
-// nodes are staged through shared memory per harmonic (by every slice: the
-// slices are separate blocks so that one block's field gathers overlap
-// another's arithmetic); the output rows of a warp are 32 consecutive
-// elements, i.e. coalesced 128-byte stores.
+// A block owns 32 consecutive elements (one per lane); warp w owns drive rows
+// [w*DPT, (w+1)*DPT) and all MP measurement rows.  Fields of the 3 element
+// nodes are staged through shared memory per harmonic; the output rows of a
+// warp are 32 consecutive elements, i.e. coalesced 128-byte stores.
 template <int KP, int MP, int DPT>
-__global__ void __launch_bounds__(256, 2) k_jacobian(JacPlan jp, int npad, const float* __restrict__ X,
+__global__ void __launch_bounds__(512) k_jacobian(JacPlan jp, int npad, const float* __restrict__ X,
                                                   const float* __restrict__ gamma, float* __restrict__ J,
                                                   __nv_bfloat16* __restrict__ Jhi,
                                                   __nv_bfloat16* __restrict__ Jlo) {
@@ -147,7 +144,7 @@ __global__ void __launch_bounds__(256, 2) k_jacobian(JacPlan jp, int npad, const
     for (int a = 0; a < DPT; ++a)
 #pragma unroll
         for (int m = 0; m < MP; ++m) acc[a][m] = 0.f;
-    const int dBase = (blockIdx.z * (blockDim.x >> 5) + warp) * DPT;
+    const int dBase = warp * DPT;
     const int drives = jp.rowsJ / MP;
     for (int ci = 0; ci < jp.Ca; ++ci) {
         const float* Xg = X + ((size_t)f * jp.Ca + ci) * npad * KP;
@@ -428,14 +425,11 @@ static int launch_jac(int F, const JacPlan& jp, int npad, const float* X, const 
                       __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s) {
     const int warps = (jp.rowsJ / MP + DPT - 1) / DPT;
     MPF_CHECK(warps >= 1 && warps <= 16, MPF_ENOTSUP, "jacobian: %d drive rows not supported", jp.rowsJ / MP);
-    // drive-row slices of at most 8 warps per element tile (separate blocks,
-    // two resident per SM); warps past the last drive row write nothing
-    const int slices = (warps + 7) / 8, wpb = (warps + slices - 1) / slices;
-    dim3 grid(jp.Epad / 32, F, slices);
+    dim3 grid(jp.Epad / 32, F);
     const size_t smem = sizeof(float) * (6 * KP * 33 + 3 * 32 * 9);
     if (smem > 48 * 1024)
         MPF_CUDA(cudaFuncSetAttribute(k_jacobian<KP, MP, DPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_jacobian<KP, MP, DPT><<<grid, wpb * 32, smem, s>>>(jp, npad, X, gamma, J, Jhi, Jlo);
+    k_jacobian<KP, MP, DPT><<<grid, warps * 32, smem, s>>>(jp, npad, X, gamma, J, Jhi, Jlo);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

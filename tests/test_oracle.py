@@ -105,14 +105,15 @@ def test_cholesky_reports_breakdown():
     assert oracle.lib().orc_cholesky(2, oracle._p(A)) == 2
 
 
-@pytest.mark.parametrize("name", ["config1_small"])
+@pytest.mark.parametrize("name", ["config1_small", "config2_r40"])
 def test_golden_fixture(name):
     """The oracle reproduces the committed fixture (regression pin)."""
     path = os.path.join(GOLDEN, f"{name}.npz")
     if not os.path.exists(path):
         pytest.skip("fixture not generated")
     z = np.load(path)
-    mesh, _, orc = make_setup(rings=int(z["rings"]), ports=int(z["ports"]))
+    extra = {"components": int(z["components"]), "height": float(z["height"])} if "components" in z.files else {}
+    mesh, _, orc = make_setup(rings=int(z["rings"]), ports=int(z["ports"]), **extra)
     V, J, _ = oracle.eit_forward(orc, z["sigma"], tol=1e-13)
     assert np.abs(V - z["V"]).max() / np.abs(z["V"]).max() < 1e-10
     Jp = J @ z["probes"]
@@ -259,3 +260,14 @@ def test_complex_symmetric_cholesky_restatement():
     z = np.linalg.solve(L, b)            # forward: L z = b
     x = np.linalg.solve(L.T, z)          # backward: L^T x = z (plain transpose)
     assert np.abs(x - np.linalg.solve(A, b)).max() <= 1e-9 * np.abs(x).max()
+
+
+def test_golden_fixture_complex():
+    """The complex oracle reproduces its committed fixture (regression pin)."""
+    z = np.load(os.path.join(GOLDEN, "complex_small.npz"))
+    _, _, orc = make_setup(rings=int(z["rings"]), ports=int(z["ports"]), components=int(z["components"]),
+                           height=float(z["height"]))
+    V, J = oracle.eit_forward_complex(orc, z["gamma"], want_jacobian=True)
+    assert np.abs(V - z["V"]).max() / np.abs(z["V"]).max() < 1e-10
+    Jp = J @ z["probes"]
+    assert np.abs(Jp - z["J_probe"]).max() / np.abs(z["J_probe"]).max() < 1e-9

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <fstream>
 #include <functional>
@@ -71,6 +72,31 @@ template <class T>
 double imag_part(T const& v) {
     if constexpr (is_complex<T>::value) return (double)v.imag();
     else return 0.0;
+}
+// The library computes in FP32: a real data type maps to float, a complex
+// one to an interleaved float pair.  Data types of that size (float,
+// thrust::complex<float>, std::complex<float>) are passed through; wider
+// ones (double, complex<double>) are converted on the way in and out.
+template <class T>
+using lib_type = typename std::conditional<is_complex<T>::value, std::complex<float>, float>::type;
+template <class T>
+constexpr bool lib_native() { return sizeof(T) == sizeof(lib_type<T>); }
+template <class To, class From>
+To convert_value(From const& v) {
+    if constexpr (is_complex<From>::value) return To(v.real(), v.imag());
+    else return To(v);
+}
+// n values of type From on the device -> n values of type To on the device,
+// through the host
+template <class To, class From>
+void convert_device(To* dst, From const* src, size_t n, cudaStream_t s, const char* where) {
+    std::vector<From> h(n);
+    cuda(cudaMemcpyAsync(h.data(), src, sizeof(From) * n, cudaMemcpyDeviceToHost, s), where);
+    cuda(cudaStreamSynchronize(s), where);
+    std::vector<To> t(n);
+    for (size_t i = 0; i < n; ++i) t[i] = convert_value<To>(h[i]);
+    cuda(cudaMemcpyAsync(dst, t.data(), sizeof(To) * n, cudaMemcpyHostToDevice, s), where);
+    cuda(cudaStreamSynchronize(s), where);
 }
 }  // namespace detail
 
@@ -1075,32 +1101,53 @@ public:
             throw std::invalid_argument("mpFlow::models::EIT::solve: materialDistribution == nullptr");
         if (materialDistribution->rows != mesh->elements.rows())
             throw std::invalid_argument("mpFlow::models::EIT::solve: materialDistribution has wrong size");
+        typedef detail::lib_type<dataType> L;
+        constexpr bool native = detail::lib_native<dataType>();
+        const char* where = "mpFlow::models::EIT::solve";
         const unsigned Mm = result->rows, Md = result->cols;
-        dataType* V = nullptr;
-        detail::cuda(cudaMallocAsync((void**)&V, sizeof(dataType) * (size_t)Mm * Md, stream), "mpFlow::models::EIT::solve");
+        const size_t E = mesh->elements.rows(), nJ = (size_t)jacobian->dataRows * E;
+        L *V = nullptr, *g = nullptr, *Jl = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&V, sizeof(L) * (size_t)Mm * Md, stream), where);
+        if (!native) {
+            detail::cuda(cudaMallocAsync((void**)&g, sizeof(L) * E, stream), where);
+            detail::cuda(cudaMallocAsync((void**)&Jl, sizeof(L) * nJ, stream), where);
+            detail::convert_device(g, materialDistribution->deviceData, E, stream, where);
+        }
+        const float* gp = reinterpret_cast<const float*>(native ? (const void*)materialDistribution->deviceData : g);
+        float* Jp = reinterpret_cast<float*>(native ? (void*)jacobian->deviceData : Jl);
         mpf_solve_stats st{};
         int status;
         if constexpr (detail::is_complex<dataType>::value) {
-            static_assert(sizeof(dataType) == 2 * sizeof(float), "complex models take interleaved float pairs");
             // complex admittivity: complex BiCGSTAB whatever the solver tag
             // (the reference's CG on complex data is the same Krylov family)
             mpf_solve_opts o = options;
             o.solver = 1;
-            status = mpf_eit_forward_complex(model_, 1, reinterpret_cast<const float*>(materialDistribution->deviceData),
-                                             reinterpret_cast<float*>(V), reinterpret_cast<float*>(jacobian->deviceData),
-                                             &o, &st, stream);
+            status = mpf_eit_forward_complex(model_, 1, gp, reinterpret_cast<float*>(V), Jp, &o, &st, stream);
         } else {
-            status = mpf_eit_forward(model_, 1, materialDistribution->deviceData, V, jacobian->deviceData, &options,
-                                     &st, stream);
+            status = mpf_eit_forward(model_, 1, gp, reinterpret_cast<float*>(V), Jp, &options, &st, stream);
         }
         if (status == MPF_OK || status == MPF_ENOCONV) {
-            detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, V,
-                                           sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md, cudaMemcpyDeviceToDevice,
-                                           stream),
-                         "mpFlow::models::EIT::solve");
-            fieldsValid_ = !detail::is_complex<dataType>::value;
+            if (native) {
+                detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, V,
+                                               sizeof(L) * Mm, sizeof(L) * Mm, Md, cudaMemcpyDeviceToDevice, stream),
+                             where);
+            } else {
+                std::vector<L> hv((size_t)Mm * Md);
+                detail::cuda(cudaMemcpyAsync(hv.data(), V, sizeof(L) * hv.size(), cudaMemcpyDeviceToHost, stream), where);
+                detail::cuda(cudaStreamSynchronize(stream), where);
+                std::vector<dataType> hd(hv.size());
+                for (size_t i = 0; i < hv.size(); ++i) hd[i] = detail::convert_value<dataType>(hv[i]);
+                detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, hd.data(),
+                                               sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md,
+                                               cudaMemcpyHostToDevice, stream),
+                             where);
+                detail::convert_device(jacobian->deviceData, Jl, nJ, stream, where);
+            }
+            fieldsValid_ = !detail::is_complex<dataType>::value && native;
         }
         cudaFreeAsync(V, stream);
+        if (g) cudaFreeAsync(g, stream);
+        if (Jl) cudaFreeAsync(Jl, stream);
         detail::check(status == MPF_ENOCONV ? MPF_OK : status, "mpFlow::models::EIT::solve");
         detail::cuda(cudaStreamSynchronize(stream), "mpFlow::models::EIT::solve");
         if (steps) *steps = (unsigned)st.iterations;
@@ -1213,20 +1260,39 @@ public:
                               Md, cudaMemcpyDeviceToDevice, stream);
         }
         const double factor = detail::real_part(regularizationFactor_);
+        typedef detail::lib_type<dataType> L;
+        constexpr bool native = detail::lib_native<dataType>();
+        const char* where = "mpFlow::solver::Inverse::solve";
+        const size_t nJ = (size_t)jacobian->dataRows * E;
+        L *calcL = nullptr, *JL = nullptr, *outL = nullptr;
+        if (!native) {
+            detail::cuda(cudaMallocAsync((void**)&calcL, sizeof(L) * per * P * 2, stream), where);
+            detail::cuda(cudaMallocAsync((void**)&JL, sizeof(L) * nJ, stream), where);
+            detail::cuda(cudaMallocAsync((void**)&outL, sizeof(L) * (size_t)E * P, stream), where);
+            detail::convert_device(calcL, calc, per * P * 2, stream, where);  // calc and meas are contiguous
+            detail::convert_device(JL, jacobian->deviceData, nJ, stream, where);
+        }
+        const float* Jp = reinterpret_cast<const float*>(native ? (const void*)jacobian->deviceData : JL);
+        const float* cp = reinterpret_cast<const float*>(native ? (const void*)calc : calcL);
+        const float* mp_ = reinterpret_cast<const float*>(native ? (const void*)meas : calcL + per * P);
+        float* op = reinterpret_cast<float*>(native ? (void*)out : outL);
         int st;
         if constexpr (detail::is_complex<dataType>::value)
-            st = mpf_inverse_solve_complex(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P,
-                                           reinterpret_cast<const float*>(jacobian->deviceData),
-                                           reinterpret_cast<const float*>(calc), reinterpret_cast<const float*>(meas),
-                                           reinterpret_cast<float*>(out), stream);
+            st = mpf_inverse_solve_complex(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P, Jp, cp,
+                                           mp_, op, stream);
         else
-            st = mpf_inverse_solve(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P,
-                                   jacobian->deviceData, calc, meas, out, stream);
-        if (st == MPF_OK)
+            st = mpf_inverse_solve(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P, Jp, cp, mp_, op,
+                                   stream);
+        if (st == MPF_OK) {
+            if (!native) detail::convert_device(out, outL, (size_t)E * P, stream, where);
             cudaMemcpy2DAsync(result->deviceData, w * result->dataRows, out, w * E, w * E, P, cudaMemcpyDeviceToDevice,
                               stream);
+        }
         cudaFreeAsync(calc, stream);
         cudaFreeAsync(out, stream);
+        if (calcL) cudaFreeAsync(calcL, stream);
+        if (JL) cudaFreeAsync(JL, stream);
+        if (outL) cudaFreeAsync(outL, stream);
         detail::check(st, "mpFlow::solver::Inverse::solve");
         detail::cuda(cudaStreamSynchronize(stream), "mpFlow::solver::Inverse::solve");
         if (iterations) *iterations = 1;  // one exact solve

@@ -124,10 +124,10 @@ def test_facade_complex_reconstruction_matches_python(tmp_path):
 
 
 def test_facade_instantiates_on_thrust_complex(tmp_path):
-    """The reference's complex instantiations compile against the facade with
-    thrust::complex<float> itself: solver::Solver, solver::Inverse and
-    models::EIT explicitly instantiated (every member), complex detection
-    checked at compile time."""
+    """The reference's instantiations compile against the facade with its own
+    data types: thrust::complex<float>, double and thrust::complex<double>
+    (solver::Solver, solver::Inverse and models::EIT explicitly instantiated,
+    every member); complex detection checked at compile time."""
     cccl = os.path.join(CUDA, "include", "cccl")
     if not os.path.exists(os.path.join(cccl, "thrust", "complex.h")):
         pytest.skip("thrust headers not found")
@@ -143,6 +143,13 @@ def test_facade_instantiates_on_thrust_complex(tmp_path):
         "template class solver::Inverse<tc, numeric::ConjugateGradient>;\n"
         "template class solver::Solver<M1>;\n"
         "template class solver::Solver<M2, numeric::BiCGSTAB>;\n"
+        "typedef models::EIT<numeric::ConjugateGradient, FEM::Equation<double, FEM::basis::Linear, false>> M3;\n"
+        "typedef thrust::complex<double> td;\n"
+        "typedef models::EIT<numeric::BiCGSTAB, FEM::Equation<td, FEM::basis::Linear, true>> M4;\n"
+        "template class solver::Solver<M3>;\n"
+        "template class solver::Solver<M4, numeric::BiCGSTAB>;\n"
+        "template class solver::Inverse<double, numeric::ConjugateGradient>;\n"
+        "static_assert(!detail::lib_native<double>() && !detail::lib_native<td>(), \"converted through FP32\");\n"
         "static_assert(detail::is_complex<tc>::value, \"thrust::complex is complex\");\n"
         "static_assert(!detail::is_complex<float>::value, \"float is real\");\n"
         "static_assert(sizeof(tc) == 2 * sizeof(float), \"interleaved pair\");\n")
@@ -150,3 +157,27 @@ def test_facade_instantiates_on_thrust_complex(tmp_path):
            os.path.join(CUDA, "include"), "-I", cccl, str(src)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_facade_precision_conversion(tmp_path):
+    """Wider data types (double, complex<double>) go through the library's
+    FP32 interface by value conversion (detail::convert_value), checked
+    here without a GPU."""
+    cccl = os.path.join(CUDA, "include", "cccl")
+    if not os.path.exists(os.path.join(cccl, "thrust", "complex.h")):
+        pytest.skip("thrust headers not found")
+    src = tmp_path / "convert.cpp"
+    src.write_text(
+        "#include <thrust/complex.h>\n#include <cstdio>\n#include \"mpflow_gb300.hpp\"\nusing namespace mpFlow;\n"
+        "int main() {\n"
+        "  bool ok = detail::convert_value<double>(1.5f) == 1.5 && detail::convert_value<float>(2.0) == 2.0f;\n"
+        "  auto z = detail::convert_value<std::complex<float>>(thrust::complex<double>(1.25, -2.5));\n"
+        "  auto w = detail::convert_value<thrust::complex<double>>(std::complex<float>(0.5f, 3.f));\n"
+        "  ok = ok && z.real() == 1.25f && z.imag() == -2.5f && w.real() == 0.5 && w.imag() == 3.0;\n"
+        "  std::printf(ok ? \"ok\\n\" : \"fail\\n\");\n  return ok ? 0 : 1;\n}\n")
+    exe = str(tmp_path / "convert")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I",
+                        os.path.join(CUDA, "include"), "-I", cccl, str(src), "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", (r.stdout, r.stderr)

@@ -62,9 +62,11 @@ class IrregularMesh:
         return IrregularMesh(nodes, elements)
 
     def elementNodes(self, element: int) -> np.ndarray:
+        """Coordinates of the element's three nodes (IrregularMesh::elementNodes), 3 x 2."""
         return self.nodes[self.elements[element]]
 
     def edgeNodes(self, edge: int) -> np.ndarray:
+        """Coordinates of the edge's two nodes (IrregularMesh::edgeNodes), 2 x 2."""
         return self.nodes[self.edges[edge]]
 
 
@@ -80,6 +82,10 @@ class Ports:
     @staticmethod
     def circularBoundary(count: int, width: float, mesh: IrregularMesh, offset: float = 0.0,
                          clockwise: bool = False, cap: int = 512) -> "Ports":
+        """`count` electrodes of `width` radians evenly spaced on the
+        boundary from `offset` (FEM::Ports::circularBoundary,
+        src/fem/ports.cpp:32-77, mpf_ports_circular); at most `cap` edges per
+        port."""
         out = np.full((count, cap), -1, np.int32)
         mx = ctypes.c_int32(0)
         check(lib().mpf_ports_circular(mesh.nodes.shape[0], ptr(mesh.nodes), mesh.elements.shape[0],
@@ -149,6 +155,7 @@ class SolveOptions:
         self.solver = solver
 
     def c(self) -> _ffi.SolveOpts:
+        """The options as the C ABI's mpf_solve_opts."""
         return _ffi.SolveOpts(float(self.tol), int(self.max_iter), float(self.refine_tol),
                               int(self.max_refine), self.WARM_STARTS[self.warm_start], int(self.check_every),
                               self.PRECONDITIONERS[self.preconditioner], self.SOLVERS[self.solver])
@@ -201,6 +208,7 @@ class EIT:
     # -- shapes
     @property
     def jacobian_rows(self) -> int:
+        """Rows of the Jacobian: drive count x measurement count, each padded to 16."""
         return self.info["jacobian_rows"]
 
     def _frames(self, gamma):
@@ -546,6 +554,10 @@ class EITBatch:
             self._h = None
 
     def solve(self, gammas, options: SolveOptions | None = None, raise_on_noconv: bool = True):
+        """Forward solves of every model's frames in the same launches
+        (mpf_batch_forward): gammas is one (frames x elements) float32 CUDA
+        tensor per model, all with the same frame count.  Returns each
+        model's voltages (frames x Mm x Md)."""
         import torch
         if len(gammas) != len(self.models):
             raise ValueError(f"expected {len(self.models)} material tensors, got {len(gammas)}")

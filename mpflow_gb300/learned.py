@@ -78,6 +78,8 @@ class MLP:
 
     def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
              weight_decay: float = 0.0):
+        """One Adam step from the last backward's gradients (mpf_mlp_adam);
+        decoupled weight decay on the weight matrices."""
         check(lib().mpf_mlp_adam(self._h, float(lr), float(beta1), float(beta2), float(eps), float(weight_decay),
                                  _stream()))
 
@@ -93,9 +95,11 @@ class MLP:
         return self._params(0)
 
     def set_parameters(self, buf):
+        """Load a flat FP32 parameter vector (resets the Adam state)."""
         self._params(1, _f32(buf, "parameters"))
 
     def gradients(self):
+        """Flat FP32 gradients of the last backward, laid out as parameters()."""
         return self._params(2)
 
     def unpack(self, flat):
@@ -124,6 +128,7 @@ def zero_network(inputs: int, outputs: int, device: int = 0) -> MLP:
 
 
 def round_up(v: int, m: int) -> int:
+    """v rounded up to a multiple of m."""
     return (v + m - 1) // m * m
 
 

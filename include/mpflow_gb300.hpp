@@ -1101,53 +1101,38 @@ public:
             throw std::invalid_argument("mpFlow::models::EIT::solve: materialDistribution == nullptr");
         if (materialDistribution->rows != mesh->elements.rows())
             throw std::invalid_argument("mpFlow::models::EIT::solve: materialDistribution has wrong size");
-        typedef detail::lib_type<dataType> L;
-        constexpr bool native = detail::lib_native<dataType>();
-        const char* where = "mpFlow::models::EIT::solve";
-        const unsigned Mm = result->rows, Md = result->cols;
-        const size_t E = mesh->elements.rows(), nJ = (size_t)jacobian->dataRows * E;
-        L *V = nullptr, *g = nullptr, *Jl = nullptr;
-        detail::cuda(cudaMallocAsync((void**)&V, sizeof(L) * (size_t)Mm * Md, stream), where);
-        if (!native) {
-            detail::cuda(cudaMallocAsync((void**)&g, sizeof(L) * E, stream), where);
-            detail::cuda(cudaMallocAsync((void**)&Jl, sizeof(L) * nJ, stream), where);
-            detail::convert_device(g, materialDistribution->deviceData, E, stream, where);
-        }
-        const float* gp = reinterpret_cast<const float*>(native ? (const void*)materialDistribution->deviceData : g);
-        float* Jp = reinterpret_cast<float*>(native ? (void*)jacobian->deviceData : Jl);
         mpf_solve_stats st{};
         int status;
-        if constexpr (detail::is_complex<dataType>::value) {
-            // complex admittivity: complex BiCGSTAB whatever the solver tag
-            // (the reference's CG on complex data is the same Krylov family)
-            mpf_solve_opts o = options;
-            o.solver = 1;
-            status = mpf_eit_forward_complex(model_, 1, gp, reinterpret_cast<float*>(V), Jp, &o, &st, stream);
-        } else {
-            status = mpf_eit_forward(model_, 1, gp, reinterpret_cast<float*>(V), Jp, &options, &st, stream);
-        }
-        if (status == MPF_OK || status == MPF_ENOCONV) {
-            if (native) {
-                detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, V,
-                                               sizeof(L) * Mm, sizeof(L) * Mm, Md, cudaMemcpyDeviceToDevice, stream),
-                             where);
+        if constexpr (detail::lib_native<dataType>()) {
+            // float, thrust::complex<float>, std::complex<float>: the library's own precision
+            const unsigned Mm = result->rows, Md = result->cols;
+            dataType* V = nullptr;
+            detail::cuda(cudaMallocAsync((void**)&V, sizeof(dataType) * (size_t)Mm * Md, stream),
+                         "mpFlow::models::EIT::solve");
+            if constexpr (detail::is_complex<dataType>::value) {
+                // complex admittivity: complex BiCGSTAB whatever the solver tag
+                // (the reference's CG on complex data is the same Krylov family)
+                mpf_solve_opts o = options;
+                o.solver = 1;
+                status = mpf_eit_forward_complex(model_, 1,
+                                                 reinterpret_cast<const float*>(materialDistribution->deviceData),
+                                                 reinterpret_cast<float*>(V),
+                                                 reinterpret_cast<float*>(jacobian->deviceData), &o, &st, stream);
             } else {
-                std::vector<L> hv((size_t)Mm * Md);
-                detail::cuda(cudaMemcpyAsync(hv.data(), V, sizeof(L) * hv.size(), cudaMemcpyDeviceToHost, stream), where);
-                detail::cuda(cudaStreamSynchronize(stream), where);
-                std::vector<dataType> hd(hv.size());
-                for (size_t i = 0; i < hv.size(); ++i) hd[i] = detail::convert_value<dataType>(hv[i]);
-                detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, hd.data(),
-                                               sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md,
-                                               cudaMemcpyHostToDevice, stream),
-                             where);
-                detail::convert_device(jacobian->deviceData, Jl, nJ, stream, where);
+                status = mpf_eit_forward(model_, 1, materialDistribution->deviceData, V, jacobian->deviceData,
+                                         &options, &st, stream);
             }
-            fieldsValid_ = !detail::is_complex<dataType>::value && native;
+            if (status == MPF_OK || status == MPF_ENOCONV) {
+                detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, V,
+                                               sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md,
+                                               cudaMemcpyDeviceToDevice, stream),
+                             "mpFlow::models::EIT::solve");
+                fieldsValid_ = !detail::is_complex<dataType>::value;
+            }
+            cudaFreeAsync(V, stream);
+        } else {
+            status = solve_converted(materialDistribution, stream, &st);
         }
-        cudaFreeAsync(V, stream);
-        if (g) cudaFreeAsync(g, stream);
-        if (Jl) cudaFreeAsync(Jl, stream);
         detail::check(status == MPF_ENOCONV ? MPF_OK : status, "mpFlow::models::EIT::solve");
         detail::cuda(cudaStreamSynchronize(stream), "mpFlow::models::EIT::solve");
         if (steps) *steps = (unsigned)st.iterations;
@@ -1205,6 +1190,46 @@ public:
     mpf_solve_stats lastStats{};
 
 private:
+    // double, complex<double>: through the library's FP32 interface, values
+    // converted on the way in (material) and out (voltages, Jacobian)
+    int solve_converted(std::shared_ptr<numeric::Matrix<dataType> const> const& materialDistribution,
+                        cudaStream_t const stream, mpf_solve_stats* st) {
+        typedef detail::lib_type<dataType> L;
+        const char* where = "mpFlow::models::EIT::solve";
+        const unsigned Mm = result->rows, Md = result->cols;
+        const size_t E = mesh->elements.rows(), nJ = (size_t)jacobian->dataRows * E;
+        L *V = nullptr, *g = nullptr, *Jl = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&V, sizeof(L) * (size_t)Mm * Md, stream), where);
+        detail::cuda(cudaMallocAsync((void**)&g, sizeof(L) * E, stream), where);
+        detail::cuda(cudaMallocAsync((void**)&Jl, sizeof(L) * nJ, stream), where);
+        detail::convert_device(g, materialDistribution->deviceData, E, stream, where);
+        int status;
+        if constexpr (detail::is_complex<dataType>::value) {
+            mpf_solve_opts o = options;
+            o.solver = 1;
+            status = mpf_eit_forward_complex(model_, 1, reinterpret_cast<const float*>(g), reinterpret_cast<float*>(V),
+                                             reinterpret_cast<float*>(Jl), &o, st, stream);
+        } else {
+            status = mpf_eit_forward(model_, 1, g, V, Jl, &options, st, stream);
+        }
+        if (status == MPF_OK || status == MPF_ENOCONV) {
+            std::vector<L> hv((size_t)Mm * Md);
+            detail::cuda(cudaMemcpyAsync(hv.data(), V, sizeof(L) * hv.size(), cudaMemcpyDeviceToHost, stream), where);
+            detail::cuda(cudaStreamSynchronize(stream), where);
+            std::vector<dataType> hd(hv.size());
+            for (size_t i = 0; i < hv.size(); ++i) hd[i] = detail::convert_value<dataType>(hv[i]);
+            detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, hd.data(),
+                                           sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md, cudaMemcpyHostToDevice,
+                                           stream),
+                         where);
+            detail::convert_device(jacobian->deviceData, Jl, nJ, stream, where);
+        }
+        cudaFreeAsync(V, stream);
+        cudaFreeAsync(g, stream);
+        cudaFreeAsync(Jl, stream);
+        return status;
+    }
+
     mpf_eit_t model_ = nullptr;
     mpf_eit_info info_{};
     bool fieldsValid_ = false;
@@ -1260,39 +1285,26 @@ public:
                               Md, cudaMemcpyDeviceToDevice, stream);
         }
         const double factor = detail::real_part(regularizationFactor_);
-        typedef detail::lib_type<dataType> L;
-        constexpr bool native = detail::lib_native<dataType>();
-        const char* where = "mpFlow::solver::Inverse::solve";
-        const size_t nJ = (size_t)jacobian->dataRows * E;
-        L *calcL = nullptr, *JL = nullptr, *outL = nullptr;
-        if (!native) {
-            detail::cuda(cudaMallocAsync((void**)&calcL, sizeof(L) * per * P * 2, stream), where);
-            detail::cuda(cudaMallocAsync((void**)&JL, sizeof(L) * nJ, stream), where);
-            detail::cuda(cudaMallocAsync((void**)&outL, sizeof(L) * (size_t)E * P, stream), where);
-            detail::convert_device(calcL, calc, per * P * 2, stream, where);  // calc and meas are contiguous
-            detail::convert_device(JL, jacobian->deviceData, nJ, stream, where);
-        }
-        const float* Jp = reinterpret_cast<const float*>(native ? (const void*)jacobian->deviceData : JL);
-        const float* cp = reinterpret_cast<const float*>(native ? (const void*)calc : calcL);
-        const float* mp_ = reinterpret_cast<const float*>(native ? (const void*)meas : calcL + per * P);
-        float* op = reinterpret_cast<float*>(native ? (void*)out : outL);
         int st;
-        if constexpr (detail::is_complex<dataType>::value)
-            st = mpf_inverse_solve_complex(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P, Jp, cp,
-                                           mp_, op, stream);
-        else
-            st = mpf_inverse_solve(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P, Jp, cp, mp_, op,
-                                   stream);
-        if (st == MPF_OK) {
-            if (!native) detail::convert_device(out, outL, (size_t)E * P, stream, where);
+        if constexpr (detail::lib_native<dataType>()) {
+            // float, thrust::complex<float>, std::complex<float>: the library's own precision
+            if constexpr (detail::is_complex<dataType>::value)
+                st = mpf_inverse_solve_complex(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P,
+                                               reinterpret_cast<const float*>(jacobian->deviceData),
+                                               reinterpret_cast<const float*>(calc),
+                                               reinterpret_cast<const float*>(meas), reinterpret_cast<float*>(out),
+                                               stream);
+            else
+                st = mpf_inverse_solve(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)P,
+                                       jacobian->deviceData, calc, meas, out, stream);
+        } else {
+            st = solve_converted(factor, calc, per * P, E, out, stream);
+        }
+        if (st == MPF_OK)
             cudaMemcpy2DAsync(result->deviceData, w * result->dataRows, out, w * E, w * E, P, cudaMemcpyDeviceToDevice,
                               stream);
-        }
         cudaFreeAsync(calc, stream);
         cudaFreeAsync(out, stream);
-        if (calcL) cudaFreeAsync(calcL, stream);
-        if (JL) cudaFreeAsync(JL, stream);
-        if (outL) cudaFreeAsync(outL, stream);
         detail::check(st, "mpFlow::solver::Inverse::solve");
         detail::cuda(cudaStreamSynchronize(stream), "mpFlow::solver::Inverse::solve");
         if (iterations) *iterations = 1;  // one exact solve
@@ -1316,6 +1328,37 @@ public:
     dataType const referenceValue;
 
 private:
+    // double, complex<double>: through the library's FP32 interface; calc
+    // holds the calculation images followed by the measurement images
+    // (`images` values each), out receives E x P results
+    int solve_converted(double factor, dataType const* calc, size_t images, unsigned E, dataType* out,
+                        cudaStream_t const stream) {
+        typedef detail::lib_type<dataType> L;
+        const char* where = "mpFlow::solver::Inverse::solve";
+        const size_t nJ = (size_t)jacobian->dataRows * E, nOut = (size_t)E * parallelImages_;
+        L *calcL = nullptr, *JL = nullptr, *outL = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&calcL, sizeof(L) * images * 2, stream), where);
+        detail::cuda(cudaMallocAsync((void**)&JL, sizeof(L) * nJ, stream), where);
+        detail::cuda(cudaMallocAsync((void**)&outL, sizeof(L) * nOut, stream), where);
+        detail::convert_device(calcL, calc, images * 2, stream, where);
+        detail::convert_device(JL, jacobian->deviceData, nJ, stream, where);
+        int st;
+        if constexpr (detail::is_complex<dataType>::value)
+            st = mpf_inverse_solve_complex(jacobian->owner, (int32_t)regularizationType_, factor,
+                                           (int32_t)parallelImages_, reinterpret_cast<const float*>(JL),
+                                           reinterpret_cast<const float*>(calcL),
+                                           reinterpret_cast<const float*>(calcL + images),
+                                           reinterpret_cast<float*>(outL), stream);
+        else
+            st = mpf_inverse_solve(jacobian->owner, (int32_t)regularizationType_, factor, (int32_t)parallelImages_,
+                                   JL, calcL, calcL + images, outL, stream);
+        if (st == MPF_OK) detail::convert_device(out, outL, nOut, stream, where);
+        cudaFreeAsync(calcL, stream);
+        cudaFreeAsync(JL, stream);
+        cudaFreeAsync(outL, stream);
+        return st;
+    }
+
     std::shared_ptr<numeric::IrregularMesh const> const mesh;
     std::shared_ptr<numeric::Matrix<dataType> const> jacobian;
     std::shared_ptr<numeric::Matrix<dataType>> result;

@@ -36,6 +36,9 @@ struct BatchClass {
     std::vector<int> members;   // batch mesh index of each stacked mesh
     std::vector<int> tile0;     // its first 128-row tile
     DevBuf<int32_t> cols, diagSlot;
+    DevBuf<int32_t> haloRows, haloCnt;  // halo plan of the tile-staged SpMM (HaloPlan)
+    DevBuf<uint16_t> haloLcol;
+    int Hpad = 0;
     DevBuf<int4> seg;
     DevBuf<float> Bc;           // [Ca][npad][KP]
     DevBuf<double> dcShift;     // [members][KP]
@@ -224,6 +227,14 @@ int batch_create(mpf_eit* const* models, int count, mpf_batch** out) {
         }
         MPF_TRY(cl->cols.upload(cols));
         MPF_TRY(cl->diagSlot.upload(diag));
+        {
+            HaloPlan hp;
+            halo_plan(cols, cl->W, cl->npad, hp);
+            cl->Hpad = hp.Hpad;
+            MPF_TRY(cl->haloRows.upload(hp.halo));
+            MPF_TRY(cl->haloCnt.upload(hp.hcnt));
+            MPF_TRY(cl->haloLcol.upload(hp.lcol));
+        }
         MPF_TRY(cl->seg.upload(seg));
         MPF_TRY(class_coarse_plan(models, *cl));
         b->classes.push_back(std::move(cl));
@@ -270,7 +281,7 @@ static int batch_workspace(mpf_batch* b, int F) {
     }
     if (b->pinned) cudaFreeHost(b->pinned);
     b->pinned = nullptr;
-    MPF_CUDA(cudaMallocHost(&b->pinned, sizeof(int) * Gtot));
+    MPF_CUDA(cudaMallocHost(&b->pinned, sizeof(int) * (Gtot + 1)));
     b->pinnedCount = Gtot;
     cg_graphs_clear(b->graphs);
     b->capF = F;
@@ -303,6 +314,11 @@ static CgProblem class_problem(mpf_batch* b, BatchClass& cl, int F, double tol, 
     P.seg = cl.seg.ptr;
     P.cols = cl.cols.ptr;
     P.diagSlot = cl.diagSlot.ptr;
+    P.halo = cl.haloRows.ptr;
+    P.hcnt = cl.haloCnt.ptr;
+    P.lcol = cl.haloLcol.ptr;
+    P.Hpad = cl.Hpad;
+    P.abortFlag = abort_flag_device();
     P.SR = cl.SR.ptr;
     P.alpha = b->alpha.ptr;
     P.x = cl.X.ptr;
@@ -511,7 +527,7 @@ int batch_cg_variants(mpf_batch* b, const int32_t* set, int F, int32_t* get, int
     if (set) {
         for (int k = 0; k < 3; ++k) {
             for (auto& cp : b->classes)
-                MPF_CHECK(set[k] < 0 || cg_shape_valid(cp->KP, k, set[k]), MPF_EINVAL,
+                MPF_CHECK(set[k] < 0 || cg_shape_fits(cp->KP, cp->W, cp->Hpad, true, k, set[k]), MPF_EINVAL,
                           "mpf_batch_cg_variants: shape %d not available for %d right-hand sides", set[k], cp->KP);
             b->forced[k] = set[k];
         }

@@ -61,6 +61,14 @@ struct DotAcc {
         s = t;
         c = __fadd_rn(c, __fadd_rn(te, pe));
     }
+    // adds a float (e.g. a short FP32 partial sum) with Knuth's TwoSum
+    __device__ __forceinline__ void addf(float x) {
+        float t = __fadd_rn(s, x);
+        float z = __fsub_rn(t, s);
+        float te = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
+        s = t;
+        c = __fadd_rn(c, te);
+    }
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
@@ -119,6 +127,38 @@ __device__ __forceinline__ bool block_partials(const DotAcc (&acc)[NDOT][VEC], d
     __syncthreads();
     if (amLast) __threadfence();
     return amLast;
+}
+
+// block_partials with the reduction array in caller-provided shared memory
+// (red: NDOT * kWarps * SUB * KP doubles; amLast: one flag), for kernels
+// whose dynamic shared memory is free again when they reduce.
+template <int KP, int VEC, int NDOT>
+__device__ __forceinline__ bool block_partials_in(const DotAcc (&acc)[NDOT][VEC], double* const (&part)[NDOT],
+                                                  int g, unsigned* counter, int nb, double* red, int* amLast) {
+    using Sh = Shape<KP, VEC>;
+    constexpr int R = kWarps * Sh::SUB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+#pragma unroll
+    for (int d = 0; d < NDOT; ++d)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) red[((size_t)d * R + warp * Sh::SUB + sub) * KP + j0 + v] = acc[d][v].value();
+    __syncthreads();
+    if (threadIdx.x < KP) {
+#pragma unroll
+        for (int d = 0; d < NDOT; ++d) {
+            double s = 0.0;
+            for (int w = 0; w < R; ++w) s += red[((size_t)d * R + w) * KP + threadIdx.x];
+            part[d][((size_t)g * gridDim.x + blockIdx.x) * KP + threadIdx.x] = s;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) *amLast = atomicAdd(&counter[g], 1u) == (unsigned)(nb - 1);
+    __syncthreads();
+    const bool last = *amLast != 0;
+    if (last) __threadfence();
+    return last;
 }
 
 // Fixed-order sum of the block partials of group g, right-hand side j (the

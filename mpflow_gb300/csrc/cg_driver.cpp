@@ -13,6 +13,42 @@
 
 namespace mpf {
 
+void halo_plan(const std::vector<int32_t>& cols, int W, int npad, HaloPlan& out) {
+    const int tiles = npad / kRowTile;
+    std::vector<std::vector<int32_t>> lists(tiles);
+    int hmax = 0;
+    for (int t = 0; t < tiles; ++t) {
+        const int r0 = t * kRowTile;
+        auto& h = lists[t];
+        for (int k = 0; k < W; ++k)
+            for (int r = r0; r < r0 + kRowTile; ++r) {
+                const int32_t c = cols[(size_t)k * npad + r];
+                if (c < r0 || c >= r0 + kRowTile) h.push_back(c);
+            }
+        std::sort(h.begin(), h.end());
+        h.erase(std::unique(h.begin(), h.end()), h.end());
+        hmax = std::max(hmax, (int)h.size());
+    }
+    out.Hpad = std::max(8, round_up(hmax, 8));
+    out.halo.assign((size_t)tiles * out.Hpad, -1);  // -1: no halo row in this place
+    out.hcnt.assign(tiles, 0);
+    out.lcol.assign((size_t)tiles * W * kRowTile, 0);
+    for (int t = 0; t < tiles; ++t) {
+        const int r0 = t * kRowTile;
+        const auto& h = lists[t];
+        out.hcnt[t] = (int32_t)h.size();
+        std::copy(h.begin(), h.end(), out.halo.begin() + (size_t)t * out.Hpad);
+        for (int k = 0; k < W; ++k)
+            for (int r = 0; r < kRowTile; ++r) {
+                const int32_t c = cols[(size_t)k * npad + r0 + r];
+                const int local = (c >= r0 && c < r0 + kRowTile)
+                                      ? c - r0
+                                      : kRowTile + (int)(std::lower_bound(h.begin(), h.end(), c) - h.begin());
+                out.lcol[((size_t)t * W + k) * kRowTile + r] = (uint16_t)local;
+            }
+    }
+}
+
 void cg_graphs_clear(CgGraphCache& cache) {
     for (auto& kv : cache) cudaGraphExecDestroy(kv.second);
     cache.clear();
@@ -21,7 +57,9 @@ void cg_graphs_clear(CgGraphCache& cache) {
 void cg_set_shape(CgProblem& P, int which, int code) {
     const int group = kCgVariants * kCgTileChoices;
     P.variant[which] = code % kCgVariants + kCgVariants * (code / group);
-    P.tiles[which] = 1 << ((code % group) / kCgVariants);
+    // the tile-staged SpMM walks longer tile ranges: 4, 8, 16 or 32 tiles
+    const int shift = (which == 0 && cg_spmm_form(code) >= 2) ? 2 : 0;
+    P.tiles[which] = 1 << ((code % group) / kCgVariants + shift);
 }
 
 int cg_autotune(const CgProblem& P0, std::array<int, 3>& best, cudaStream_t s) {
@@ -35,7 +73,7 @@ int cg_autotune(const CgProblem& P0, std::array<int, 3>& best, cudaStream_t s) {
         float bestMs = 1e30f;
         best[which] = cg_default_variant(P.KP);
         for (int v = 0; v < cg_shape_count(which) && st == MPF_OK; ++v) {
-            if (!cg_shape_valid(P.KP, which, v)) continue;
+            if (!cg_shape_fits(P.KP, P.W, P.Hpad, P.halo != nullptr, which, v)) continue;
             CgProblem Q = P;
             cg_set_shape(Q, which, v);
             // fresh state with valid p.q, then one untimed launch
@@ -79,6 +117,7 @@ int cg_run(CgGraphCache& cache, int* pinned, const CgProblem* Ps, int nP, int ma
     if (it != cache.end()) {
         exec = it->second;
     } else {
+        for (int i = 0; i < nP; ++i) MPF_TRY(cg_prepare_launch(Ps[i]));
         cudaStream_t cap;
         MPF_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         cudaGraph_t graph;
@@ -95,6 +134,11 @@ int cg_run(CgGraphCache& cache, int* pinned, const CgProblem* Ps, int nP, int ma
         MPF_CHECK(e == cudaSuccess, MPF_ECUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
         cache[key] = exec;
     }
+    // the bulk-copy SpMM raises the device's abort flag when a wait gives up:
+    // it is read with the active flags (pinned[Gtot]) and ends the solve
+    int* abortFlag = nullptr;
+    for (int i = 0; i < nP; ++i)
+        if (Ps[i].abortFlag) abortFlag = Ps[i].abortFlag;
     auto fetch = [&](bool activeFlags) -> int {
         int off = 0;
         for (int i = 0; i < nP; ++i) {
@@ -102,7 +146,15 @@ int cg_run(CgGraphCache& cache, int* pinned, const CgProblem* Ps, int nP, int ma
                                      cudaMemcpyDeviceToHost, s));
             off += Ps[i].G;
         }
+        pinned[Gtot] = 0;
+        if (abortFlag) MPF_CUDA(cudaMemcpyAsync(pinned + Gtot, abortFlag, sizeof(int), cudaMemcpyDeviceToHost, s));
         MPF_CUDA(cudaStreamSynchronize(s));
+        if (pinned[Gtot]) {
+            // the result is undefined: clear the flag and the reduction counters
+            MPF_CUDA(cudaMemset(abortFlag, 0, sizeof(int)));
+            for (int i = 0; i < nP; ++i) MPF_CUDA(cudaMemset(Ps[i].counter, 0, sizeof(unsigned) * Ps[i].G));
+            return fail(MPF_ETIMEOUT, "CG: a bulk-copy wait of the tile-staged SpMM timed out");
+        }
         return MPF_OK;
     };
     int done = 0;

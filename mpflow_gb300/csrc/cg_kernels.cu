@@ -30,6 +30,7 @@
 // per-block partials are combined by the last block of the group in a fixed
 // order, so results are deterministic (helpers in cg_common.cuh).
 #include "cg_common.cuh"
+#include "tc_ptx.cuh"
 
 namespace mpf {
 namespace {
@@ -362,6 +363,240 @@ __global__ void __launch_bounds__(kThreads) k_spmm_dot_staged(CgProblem P) {
     }
     double* const parts[1] = {P.partA};
     if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter, nb)) {
+        if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
+        if (threadIdx.x == 0) P.counter[g] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tile-staged SpMM (k_spmm_halo).  The gathers of p are what limits the
+// direct forms: each row reads W neighbour rows of KP floats through L1/L2,
+// and the number of such loads a warp can keep in flight is bounded by its
+// registers.  Here a block copies, per 128-row tile, everything the tile's
+// products read into shared memory with bulk asynchronous copies (TMA,
+// cp.async.bulk, completion counted on an mbarrier): the tile's own 128 rows
+// of p (one contiguous copy), the W slot values {S, R} (one copy per slot)
+// and the slots' tile-local columns; its halo rows (the distinct columns
+// outside the tile) are gathered in 16-byte cp.async chunks by all threads,
+// whose completion the same mbarrier counts (one bulk copy per 128-byte halo
+// row was measured slower: the copy engine serialises small requests).  The
+// arithmetic then reads only shared memory.  NS stages are in flight per
+// block, so copies of tile t + NS - 1 overlap the products of tile t; on the
+// ring meshes a tile's halo is about half its own rows, so p crosses from L2
+// about 1.5 times per SpMM instead of once per slot.
+constexpr int kHaloMaxSmem = 227 * 1024;
+constexpr int kHaloMaxRows = 128;  // halo rows a tile may have (Hpad limit of the form)
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+// A wait that ignores the abort flag, for draining copies already issued
+// after another wait gave up (bounded by limitNs).
+__device__ __forceinline__ bool mbar_wait_drain(uint32_t bar, uint32_t parity, uint64_t limitNs) {
+    const uint64_t t0 = tc::global_timer();
+    while (!tc::mbar_try_wait(bar, parity))
+        if (tc::global_timer() - t0 > limitNs) return false;
+    return true;
+}
+
+struct HaloLayout {
+    uint32_t own, halo, sr, lc, stage;  // byte sizes of the parts of one stage
+};
+__host__ __device__ inline HaloLayout halo_layout(int KP, int W, int Hpad) {
+    HaloLayout l;
+    l.own = (uint32_t)kRowTile * KP * 4;
+    l.halo = (uint32_t)Hpad * KP * 4;
+    l.sr = (uint32_t)W * kRowTile * 8;
+    l.lc = (uint32_t)((W * kRowTile * 2 + 15) / 16 * 16);
+    l.stage = l.own + l.halo + l.sr + l.lc;
+    return l;
+}
+inline size_t halo_smem_bytes(int KP, int W, int Hpad, int NS) {
+    return (size_t)NS * halo_layout(KP, W, Hpad).stage + 16 * 8 /*mbarriers*/;
+}
+
+template <int KP, int VEC, int RB, int NS>
+__global__ void __launch_bounds__(kThreads, 3) k_spmm_halo(CgProblem P) {
+    using Sh = Shape<KP, VEC>;
+    constexpr int kChunks = KP / 4;                                    // 16-byte chunks per row of p
+    constexpr int kPer = (kHaloMaxRows * kChunks + kThreads - 1) / kThreads;  // halo chunks per thread
+    extern __shared__ __align__(128) unsigned char hsm[];
+    __shared__ int localAbort, amLast;
+    const int g = blockIdx.y;
+    if (!P.active[g]) return;
+    const int slice = g / P.M;
+    const Seg sg = segment(P, g - slice * P.M);
+    const int T = P.tiles[0], nb = (sg.nblk + T - 1) / T;
+    if ((int)blockIdx.x >= nb) return;
+    const int f = slice / P.Ca, ci = slice % P.Ca;
+    const bool dc = P.dcFree[ci] != 0;
+    const float alpha = P.alpha[ci];
+    const int W = P.W;
+    const float2* SR = P.SR + (size_t)f * W * P.npad;
+    const size_t vb = (size_t)slice * P.npad * KP;
+    const float* p = P.p + vb;
+    float* q = P.q + vb;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = lane / Sh::LPR, j0 = (lane % Sh::LPR) * VEC;
+    const HaloLayout L = halo_layout(KP, W, P.Hpad);
+    const uint32_t smem0 = tc::smem_u32(hsm);
+    const uint32_t bar0 = smem0 + NS * L.stage;  // NS mbarriers, 8 bytes each
+    if (threadIdx.x == 0) {
+        localAbort = 0;
+        for (int s = 0; s < NS; ++s) tc::mbar_init(bar0 + 8 * s, 1 + kThreads);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    float sp[VEC] = {};
+    if (dc) {
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) sp[v] = (float)((double)sg.dcScale * P.sumP[(size_t)g * KP + j0 + v]);
+    }
+    const int tile0 = sg.tile0 + blockIdx.x * T;
+    const int tileEnd = min(sg.tile0 + sg.nblk, tile0 + T);
+    // halo row of each of this thread's chunks (-1: none), loaded one tile
+    // ahead of the copies that use them so their latency is hidden
+    int hrow[kPer];
+    auto prefetch = [&](int t) {
+        const int32_t* hl = P.halo + (size_t)t * P.Hpad;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int i = (threadIdx.x + j * kThreads) / kChunks;
+            hrow[j] = i < P.Hpad ? __ldg(&hl[i]) : -1;
+        }
+    };
+    // all threads: thread 0 arms stage s's barrier with the bulk byte count and
+    // lanes 0..W+1 of warp 0 issue the bulk copies (own rows, local columns,
+    // slot values); every thread copies its 16-byte chunks of the halo rows
+    // with cp.async and has the barrier count their completion (one arrival
+    // per thread, so the barrier's count is 1 + kThreads)
+    auto issue = [&](int t, int s) {
+        const uint32_t st = smem0 + s * L.stage, bar = bar0 + 8 * s;
+        if (warp == 0) {
+            if (lane == 0) tc::mbar_expect_tx(bar, L.own + L.sr + (uint32_t)W * kRowTile * 2);
+            __syncwarp();
+            if (lane == 0) bulk_g2s(st, p + (size_t)t * kRowTile * KP, L.own, bar);
+            if (lane == 1)
+                bulk_g2s(st + L.own + L.halo + L.sr, P.lcol + (size_t)t * W * kRowTile, W * kRowTile * 2, bar);
+            if (lane >= 2 && lane < 2 + W)
+                bulk_g2s(st + L.own + L.halo + (lane - 2) * kRowTile * 8,
+                         SR + (size_t)(lane - 2) * P.npad + (size_t)t * kRowTile, kRowTile * 8, bar);
+        }
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int c = threadIdx.x + j * kThreads, i = c / kChunks, part = c % kChunks;
+            if (hrow[j] >= 0)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(st + L.own + (uint32_t)(i * KP + part * 4) * 4),
+                             "l"(p + (size_t)hrow[j] * KP + part * 4)
+                             : "memory");
+        }
+        asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+    };
+    int issued = 0;
+    for (int j = 0; j < NS - 1 && tile0 + j < tileEnd; ++j) {
+        prefetch(tile0 + j);
+        issue(tile0 + j, j);
+        ++issued;
+    }
+    if (tile0 + NS - 1 < tileEnd) prefetch(tile0 + NS - 1);
+    DotAcc acc[1][VEC];
+    bool failed = false;
+    int consumed = 0;
+    for (int t = tile0; t < tileEnd; ++t, ++consumed) {
+        // every warp is done with the stage the next copies overwrite (the
+        // tile before this one), and all agree whether a wait gave up
+        if (__syncthreads_or(failed)) break;
+        if (t + NS - 1 < tileEnd) {
+            issue(t + NS - 1, (consumed + NS - 1) % NS);
+            ++issued;
+            if (t + NS < tileEnd) prefetch(t + NS);
+        }
+        const int s = consumed % NS;
+        failed = !tc::mbar_wait(bar0 + 8 * s, (consumed / NS) & 1, &localAbort);
+        if (failed) continue;
+        const unsigned char* base = hsm + (size_t)s * L.stage;
+        const float* rowsS = reinterpret_cast<const float*>(base);  // own rows, then halo rows
+        const float2* vt = reinterpret_cast<const float2*>(base + L.own + L.halo);
+        const uint16_t* ct = reinterpret_cast<const uint16_t*>(base + L.own + L.halo + L.sr);
+        float tp[VEC] = {};  // this tile's p.q terms (FP32), folded into acc once per tile
+        for (int st = 0; st < Sh::STEPS; st += RB) {
+            int lr[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i) lr[i] = warp * kRowsPerWarp + (st + i) * Sh::SUB + sub;
+            float y[RB][VEC];
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) y[i][v] = 0.f;
+            // the first kWFast slots: all columns and values first, then the gathers
+            int c[kWFast][RB];
+            float av[kWFast][RB];
+#pragma unroll
+            for (int k = 0; k < kWFast; ++k)
+#pragma unroll
+                for (int i = 0; i < RB; ++i) {
+                    c[k][i] = k < W ? (int)ct[k * kRowTile + lr[i]] : lr[i];
+                    const float2 e = k < W ? vt[k * kRowTile + lr[i]] : make_float2(0.f, 0.f);
+                    av[k][i] = e.x + alpha * e.y;
+                }
+#pragma unroll
+            for (int k = 0; k < kWFast; ++k) {
+                if (k < W) {
+#pragma unroll
+                    for (int i = 0; i < RB; ++i) {
+                        float xv[VEC];
+                        ldv<VEC>(rowsS + (size_t)c[k][i] * KP + j0, xv);
+#pragma unroll
+                        for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(av[k][i], xv[v], y[i][v]);
+                    }
+                }
+            }
+            for (int k = kWFast; k < W; ++k) {
+#pragma unroll
+                for (int i = 0; i < RB; ++i) {
+                    const int cc = ct[k * kRowTile + lr[i]];
+                    const float2 e = vt[k * kRowTile + lr[i]];
+                    const float a = e.x + alpha * e.y;
+                    float xv[VEC];
+                    ldv<VEC>(rowsS + (size_t)cc * KP + j0, xv);
+#pragma unroll
+                    for (int v = 0; v < VEC; ++v) y[i][v] = fmaf(a, xv[v], y[i][v]);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < RB; ++i) {
+                const int row = t * kRowTile + lr[i];
+                if (row < sg.end) {
+#pragma unroll
+                    for (int v = 0; v < VEC; ++v) y[i][v] += sp[v];
+                }
+                stv<VEC>(q + (size_t)row * KP + j0, y[i]);
+                float pv[VEC];
+                ldv<VEC>(rowsS + (size_t)lr[i] * KP + j0, pv);
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) tp[v] = fmaf(pv[v], y[i][v], tp[v]);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) acc[0][v].addf(tp[v]);
+    }
+    if (__syncthreads_or(failed)) {
+        // a wait gave up: let the copies this block issued land (bounded)
+        // before the block exits, then report; the result is undefined
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (threadIdx.x == 0) {
+            for (int j = consumed > 0 ? consumed - 1 : 0; j < issued; ++j)
+                if (!mbar_wait_drain(bar0 + 8 * (j % NS), (j / NS) & 1, 1000000000ull)) break;
+            if (P.abortFlag) atomicExch(P.abortFlag, 1);
+        }
+        __syncthreads();
+        return;
+    }
+    // the stages are free again: reduce through their shared memory
+    double* const parts[1] = {P.partA};
+    if (block_partials_in<KP, VEC, 1>(acc, parts, g, P.counter, nb, reinterpret_cast<double*>(hsm), &amLast)) {
         if (threadIdx.x < KP) P.pq[(size_t)g * KP + threadIdx.x] = sum_partials(P.partA, g, KP, threadIdx.x, nb);
         if (threadIdx.x == 0) P.counter[g] = 0;
     }
@@ -711,20 +946,26 @@ constexpr bool valid_variant() {
 }
 
 template <int KP, int VEC, int RB>
-void fill_variant(CgKernel (&t)[3][2 * kCgVariants], int v) {
+void fill_variant(CgKernel (&t)[3][kSpmmForms * kCgVariants], int v) {
     if constexpr (KP / VEC <= 32) {
         if constexpr (valid_variant<KP, VEC, RB>()) {
             t[0][v] = k_spmm_dot<KP, VEC, RB>;
             t[0][v + kCgVariants] = k_spmm_dot_staged<KP, VEC, RB>;
             t[1][v] = k_update<KP, VEC, RB>;
             t[2][v] = k_direction<KP, VEC, RB>;
+            // tile-staged form: 2 or 3 stages, right-hand-side widths up to 64
+            // (a 128-wide tile needs 64 KB of own rows per stage)
+            if constexpr (KP <= 64 && VEC >= 2 && RB <= 2) {
+                t[0][v + 2 * kCgVariants] = k_spmm_halo<KP, VEC, RB, 2>;
+                t[0][v + 3 * kCgVariants] = k_spmm_halo<KP, VEC, RB, 3>;
+            }
         }
     }
 }
 
 template <int KP>
 struct VariantTable {
-    CgKernel k[3][2 * kCgVariants] = {};
+    CgKernel k[3][kSpmmForms * kCgVariants] = {};
     VariantTable() {
         fill_variant<KP, 4, 1>(k, 0);
         fill_variant<KP, 4, 2>(k, 1);
@@ -743,7 +984,7 @@ CgKernel variant_kernel(int KP, int which, int v) {
     static const VariantTable<32> t32;
     static const VariantTable<64> t64;
     static const VariantTable<128> t128;
-    if (v < 0 || v >= 2 * kCgVariants || which < 0 || which > 2) return nullptr;
+    if (v < 0 || v >= kSpmmForms * kCgVariants || which < 0 || which > 2) return nullptr;
     switch (KP) {
         case 16: return t16.k[which][v];
         case 32: return t32.k[which][v];
@@ -797,7 +1038,18 @@ struct Res64L {
 
 bool cg_variant_valid(int KP, int which, int v) { return variant_kernel(KP, which, v) != nullptr; }
 
-int cg_shape_count(int which) { return which == 0 ? 2 * kCgVariants * kCgTileChoices : kCgVariants * kCgTileChoices; }
+int cg_shape_count(int which) {
+    return which == 0 ? kSpmmForms * kCgVariants * kCgTileChoices : kCgVariants * kCgTileChoices;
+}
+
+int cg_spmm_form(int code) { return code / (kCgVariants * kCgTileChoices); }
+
+bool cg_shape_fits(int KP, int W, int Hpad, bool haveHalo, int which, int code) {
+    if (!cg_shape_valid(KP, which, code)) return false;
+    if (which != 0 || cg_spmm_form(code) < 2) return true;
+    const int NS = cg_spmm_form(code);
+    return haveHalo && Hpad > 0 && Hpad <= kHaloMaxRows && halo_smem_bytes(KP, W, Hpad, NS) <= (size_t)kHaloMaxSmem;
+}
 
 bool cg_shape_valid(int KP, int which, int code) {
     if (code < 0 || code >= cg_shape_count(which)) return false;
@@ -807,7 +1059,8 @@ bool cg_shape_valid(int KP, int which, int code) {
 
 int cg_shape_code(const CgProblem& P, int which) {
     const int v = P.variant[which];
-    return v % kCgVariants + kCgVariants * (31 - __builtin_clz(P.tiles[which])) +
+    const int shift = (which == 0 && v >= 2 * kCgVariants) ? 2 : 0;  // see cg_set_shape
+    return v % kCgVariants + kCgVariants * (31 - __builtin_clz(P.tiles[which]) - shift) +
            kCgVariants * kCgTileChoices * (v / kCgVariants);
 }
 
@@ -840,7 +1093,22 @@ static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count)
     MPF_CHECK(k != nullptr, MPF_EINVAL, "CG kernel variant %d not available for %d right-hand sides", v, P.KP);
     const int t = P.tiles[which] >= 1 ? P.tiles[which] : 1;
     size_t smem = 0;
-    if (which == 0 && v >= kCgVariants) {
+    if (which == 0 && v >= 2 * kCgVariants) {
+        const int NS = v / kCgVariants;
+        MPF_CHECK(P.halo && P.hcnt && P.lcol && P.Hpad > 0, MPF_EINVAL, "tile-staged SpMM: the problem has no halo plan");
+        MPF_CHECK(P.Hpad <= kHaloMaxRows, MPF_EINVAL, "tile-staged SpMM: %d halo rows per tile exceed %d", P.Hpad,
+                  kHaloMaxRows);
+        smem = halo_smem_bytes(P.KP, P.W, P.Hpad, NS);
+        MPF_CHECK(smem <= (size_t)kHaloMaxSmem, MPF_EINVAL,
+                  "tile-staged SpMM: %zu bytes of shared memory per block (%d halo rows, %d slots) exceed %d", smem,
+                  P.Hpad, P.W, kHaloMaxSmem);
+        // the attribute is set outside stream capture (cg_prepare_launch runs
+        // before a graph of iterations is recorded)
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        MPF_CUDA(cudaStreamIsCapturing(s, &cs));
+        if (cs == cudaStreamCaptureStatusNone)
+            MPF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    } else if (which == 0 && v >= kCgVariants) {
         smem = staged_smem_bytes(P.W);
         MPF_CHECK(smem <= 200 * 1024, MPF_EINVAL, "staged SpMM: %d ELL slots do not fit shared memory", P.W);
         if (smem > 48 * 1024)
@@ -852,6 +1120,23 @@ static int launch_one(const CgProblem& P, int which, cudaStream_t s, bool count)
     } else {
         MPF_CUDA(cudaGetLastError());
     }
+    return MPF_OK;
+}
+
+int cg_prepare_launch(const CgProblem& P) {
+    if (P.solver != 0) return MPF_OK;
+    const int v = P.variant[0];
+    CgKernel k = variant_kernel(P.KP, 0, v);
+    MPF_CHECK(k != nullptr, MPF_EINVAL, "CG kernel variant %d not available for %d right-hand sides", v, P.KP);
+    size_t smem = 0;
+    if (v >= 2 * kCgVariants) {
+        MPF_CHECK(P.halo && P.Hpad > 0, MPF_EINVAL, "tile-staged SpMM: the problem has no halo plan");
+        smem = halo_smem_bytes(P.KP, P.W, P.Hpad, v / kCgVariants);
+        MPF_CHECK(smem <= (size_t)kHaloMaxSmem, MPF_EINVAL, "tile-staged SpMM: %zu bytes of shared memory", smem);
+    } else if (v >= kCgVariants) {
+        smem = staged_smem_bytes(P.W);
+    }
+    if (smem > 48 * 1024) MPF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return MPF_OK;
 }
 

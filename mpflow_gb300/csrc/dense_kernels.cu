@@ -466,6 +466,8 @@ __global__ void k_wait_selftest(int* flag, unsigned long long limitNs) {
     if (!mbar_wait(smem_u32(&bar), 0, &localAbort, limitNs)) atomicExch(flag, 1);
 }
 
+}  // namespace
+
 // one pipeline abort flag per device (a kernel must not touch another
 // device's memory), allocated on first use on the current device
 int* abort_flag_device() {
@@ -485,8 +487,6 @@ int* abort_flag_device() {
     }
     return flags[dev];
 }
-
-}  // namespace
 
 int make_bf16_map(CUtensorMap* map, const __nv_bfloat16* base, int totalRows, int ld) {
     EncodeTiledFn enc;

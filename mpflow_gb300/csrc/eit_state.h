@@ -24,6 +24,9 @@ struct mpf_eit {
     std::vector<double> betaAll;      // per component
     // device: static structure
     mpf::DevBuf<int32_t> cols, diagSlot, cptr, contrib, elements;
+    mpf::DevBuf<int32_t> haloRows, haloCnt;  // halo plan of the tile-staged SpMM (mpf::HaloPlan)
+    mpf::DevBuf<uint16_t> haloLcol;
+    int Hpad = 0;
     mpf::DevBuf<int32_t> rowOf;       // internal row of each node (Morton order, see eit_create)
     mpf::DevBuf<float> Kf, Mf;
     mpf::DevBuf<double> Kd, Md64;

@@ -260,6 +260,14 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     // ---- upload
     MPF_TRY(m->cols.upload(m->fs.cols));
     MPF_TRY(m->diagSlot.upload(m->fs.diagSlot));
+    {
+        HaloPlan hp;
+        halo_plan(m->fs.cols, m->W, m->npad, hp);
+        m->Hpad = hp.Hpad;
+        MPF_TRY(m->haloRows.upload(hp.halo));
+        MPF_TRY(m->haloCnt.upload(hp.hcnt));
+        MPF_TRY(m->haloLcol.upload(hp.lcol));
+    }
     MPF_TRY(m->cptr.upload(m->fs.contribPtr));
     MPF_TRY(m->contrib.upload(m->fs.contrib));
     MPF_TRY(m->elements.upload(elems));
@@ -328,7 +336,7 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
         MPF_TRY(m->cSlots.upload(slots));
         MPF_TRY(m->cAggSize.upload(aggSize));
     }
-    MPF_CUDA(cudaMallocHost(&m->pinnedActive, sizeof(int) * 4096));
+    MPF_CUDA(cudaMallocHost(&m->pinnedActive, sizeof(int) * (4096 + 1)));
     *out = m.release();
     return MPF_OK;
 }
@@ -458,6 +466,11 @@ static CgProblem make_problem(mpf_eit* m, int F, double tol, bool coarse = false
     P.seg = nullptr;
     P.cols = m->cols.ptr;
     P.diagSlot = m->diagSlot.ptr;
+    P.halo = m->haloRows.ptr;
+    P.hcnt = m->haloCnt.ptr;
+    P.lcol = m->haloLcol.ptr;
+    P.Hpad = m->Hpad;
+    P.abortFlag = abort_flag_device();
     P.SR = m->SR.ptr;
     P.alpha = m->alpha.ptr;
     P.x = m->X.ptr;
@@ -1178,7 +1191,7 @@ int profile_fem(mpf_eit* m, int F, const float* gamma, int reps, double* ms, dou
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get) {
     if (set) {
         for (int k = 0; k < 3; ++k)
-            MPF_CHECK(set[k] < 0 || cg_shape_valid(m->KP, k, set[k]),
+            MPF_CHECK(set[k] < 0 || cg_shape_fits(m->KP, m->W, m->Hpad, true, k, set[k]),
                       MPF_EINVAL, "CG launch shape %d is not available for kernel %d with %d right-hand sides",
                       set[k], k, m->KP);
         for (int k = 0; k < 3; ++k) m->forcedVariants[k] = set[k] < 0 ? -1 : set[k];

@@ -82,6 +82,13 @@ struct CgProblem {
     double* rzFine;       // [G][KP] r^T D^-1 r of the last update / init
     double* bzFine;       // [G][KP] b^T D^-1 b (init)
     int first;            // k_direction: p = M^-1 r (start of an iteration)
+    // halo plan of the tile-staged SpMM (k_spmm_halo; see HaloPlan): null
+    // when the problem has none, and then that SpMM form is not offered
+    const int32_t* halo;   // [tiles][Hpad] distinct columns outside each 128-row tile
+    const int32_t* hcnt;   // [tiles] halo rows of each tile
+    const uint16_t* lcol;  // [tiles][W][128] tile-local column of every slot
+    int Hpad;              // halo rows reserved per tile (multiple of 8)
+    int* abortFlag;        // device flag raised by a timed-out wait of a bulk-copy pipeline
     // deferred x update: k_update records alphaX = rz / pq of every
     // right-hand side and pend[g] = 1; k_direction applies x += alphaX p
     // while it still holds the old p and clears pend[g]; groups that retired
@@ -105,15 +112,38 @@ struct CgProblem {
 
 constexpr int kAgg = 64;  // rows per coarse aggregate (divides kRowTile)
 
+// Halo plan of the tile-staged SpMM, built once per matrix structure from the
+// slot-major ELL columns: for every 128-row tile t, the distinct columns
+// outside the tile in ascending order (halo[t * Hpad + i], i < hcnt[t]; -1
+// in the unused places up to Hpad), and
+// every slot's column as an index into the tile's staged rows (lcol[(t * W +
+// k) * 128 + r]: c - 128 t inside the tile, 128 + i for halo row i).  A
+// tile's own rows and its halo rows are what k_spmm_halo copies into shared
+// memory; on the ring meshes the halo holds 48-87 rows per tile.
+struct HaloPlan {
+    int Hpad = 0;
+    std::vector<int32_t> halo, hcnt;
+    std::vector<uint16_t> lcol;
+};
+void halo_plan(const std::vector<int32_t>& cols, int W, int npad, HaloPlan& out);
+// the pipeline abort flag of the current device (dense_kernels.cu)
+int* abort_flag_device();
+
 // cg_kernels.cu
 // variant v = vecIdx * 3 + rbIdx, floats per lane {4, 2, 1}[vecIdx], row steps {1, 2, 4}[rbIdx]
-// (SpMM: v + 9 is the shared-memory-staged form); a launch-shape code is
-// v % 9 + kCgVariants * ti + 36 * (v / 9) with 1 << ti tiles per block
+// (SpMM: v + 9 * form with form 0 = slots read from global memory, 1 = slots
+// staged per warp with cp.async, 2 / 3 = tile-staged with 2 / 3 bulk-copy
+// stages, k_spmm_halo); a launch-shape code is v % 9 + kCgVariants * ti +
+// 36 * (v / 9) with 1 << ti tiles per block (4 << ti for the tile-staged SpMM)
 constexpr int kCgVariants = 9;
 constexpr int kCgTileChoices = 4;
+constexpr int kSpmmForms = 4;
 bool cg_variant_valid(int KP, int which, int v);
-int cg_shape_count(int which);                      // 72 SpMM codes, 36 for the others
+int cg_shape_count(int which);                      // 144 SpMM codes, 36 for the others
 bool cg_shape_valid(int KP, int which, int code);
+int cg_spmm_form(int code);
+// cg_shape_valid and, for the tile-staged SpMM, a halo plan whose stages fit shared memory
+bool cg_shape_fits(int KP, int W, int Hpad, bool haveHalo, int which, int code);
 int cg_shape_code(const CgProblem& P, int which);
 int cg_default_variant(int KP);
 int cg_launch_init(const CgProblem& P, bool zeroGuess, cudaStream_t s);
@@ -137,6 +167,9 @@ int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, 
 int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count = true);
 bool coarse_supported(int KP, int ncPad);
 int cg_launch_iteration(const CgProblem& P, cudaStream_t s);
+// kernel attributes of P's launch shapes (large dynamic shared memory), set
+// before an iteration graph is recorded
+int cg_prepare_launch(const CgProblem& P);
 int cg_iteration_launches(const CgProblem& P);
 int cg_launch_kernel(const CgProblem& P, int which /*0 spmm, 1 update, 2 direction*/, cudaStream_t s);
 // x += alphaX p on the groups whose last x update is still pending (end of a CG solve)
@@ -154,7 +187,7 @@ void cg_set_shape(CgProblem& P, int which, int code);
 int cg_autotune(const CgProblem& P, std::array<int, 3>& best, cudaStream_t s);
 // Runs CG iterations of nP problems, recorded together as CUDA graphs of
 // checkEvery iterations, until every group of every problem converged or
-// maxIter; pinned: host buffer of at least sum(G) ints.  iters receives the
+// maxIter; pinned: host buffer of at least sum(G) + 1 ints.  iters receives the
 // per-group iteration counts (problems in order), maxIters the slowest group's
 // count and notConverged the groups still active.
 int cg_run(CgGraphCache& cache, int* pinned, const CgProblem* Ps, int nP, int maxIter, int checkEvery,

@@ -98,7 +98,10 @@ def test_batch_two_level_matches_single_models():
     assert it_t[3].max() < it_j[3].max()
 
 
-@pytest.mark.parametrize("shapes", [[1, 13, 22], [28, 4, 8], [35, 31, 10]])
+# SpMM codes 72..143 are the tile-staged form (bulk copies of each tile's own
+# and halo rows, 2 or 3 stages) over the stacked meshes' tiles
+@pytest.mark.parametrize("shapes", [[1, 13, 22], [28, 4, 8], [35, 31, 10], [100, 13, 22], [108, 4, 8],
+                                    [130, 31, 10]])
 def test_batch_forced_launch_shapes(shapes):
     import torch
     import mpflow_gb300 as mp

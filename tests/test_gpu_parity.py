@@ -264,11 +264,13 @@ def test_every_cg_variant_matches_oracle(ports, components):
     gt = torch.tensor(g, dtype=torch.float32, device="cuda")
     model.solve(gt, mp.SolveOptions(tol=1e-7))
     tuned = model.cg_variants(1)
-    assert (tuned >= 0).all() and tuned[0] < 72 and (tuned[1:] < 36).all()
+    assert (tuned >= 0).all() and tuned[0] < 144 and (tuned[1:] < 36).all()
     tried = 0
     # 9 lane/row-step variants x 1, 2, 4, 8 tiles per block; SpMM codes 36..71
-    # are the shared-memory-staged form of codes 0..35
-    for v in range(72):
+    # are the form with per-warp cp.async staging of the slots, 72..107 and
+    # 108..143 the tile-staged form (own and halo rows copied in bulk) with 2
+    # and 3 stages
+    for v in range(144):
         shapes = [v, v, v] if v < 36 else [v, int(tuned[1]), int(tuned[2])]
         try:
             model.cg_variants(1, set=shapes)
@@ -278,7 +280,7 @@ def test_every_cg_variant_matches_oracle(ports, components):
         tried += 1
         V = model.solve(gt, mp.SolveOptions(tol=1e-7))[0].cpu().numpy().astype(np.float64)
         assert rel_err(V, Vo) < 1e-4, (v, rel_err(V, Vo))
-    assert tried >= 40
+    assert tried >= 70
     model.cg_variants(1, set=[-1, -1, -1])
     assert (model.cg_variants(1) == tuned).all()
 

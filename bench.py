@@ -191,19 +191,14 @@ def measured_bf16_tflops():
         return 1900.0, "fallback"
 
 
-def profiled_traffic(kernel: str):
-    """DRAM bytes per launch per (frame, harmonic) group of a CG kernel from the
-    committed ncu summary (line '<kernel> dram_bytes_per_group_launch: X'),
-    or None."""
-    path = os.path.join(ROOT, "profiles", "cg_kernels_R80_F16.md")
-    try:
-        with open(path) as fh:
-            for line in fh:
-                if line.startswith(f"{kernel} dram_bytes_per_group_launch:"):
-                    return float(line.split(":", 1)[1])
-    except OSError:
-        pass
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch and
+# per (frame, harmonic) group of the three CG iteration kernels on the
+# 80-ring, 32-electrode workload (32 right-hand sides per group), from one ncu
+# capture of `python bench.py --profile-only --frames 16 --steps 3
+# --cg-shapes 90,28,19` (112 groups; summary and full command in
+# profiles/cg_kernels_R80_F16.md).  Traffic grows with the group count, so a
+# launch of G groups moves G times these bytes.
+CG_DRAM_BYTES_PER_GROUP = {"k_spmm_halo": 4.96e6, "k_update": 7.12e6, "k_direction": 12.00e6}
 
 
 # ---------------------------------------------------------------------------
@@ -216,86 +211,90 @@ def build_problem(a):
     return mesh, ports, pat, src
 
 
-def cpu_baseline(a, mesh, ports, pat, frames_v, gn_iters_mean):
-    """One Gauss-Newton iteration of one frame with the FP64 oracle (the
-    reference's routines restated in C) on all host cores; frames/s =
-    1 / (seconds per GN iteration * (mean GN updates + 1 forward check))."""
+def reference_gn_frame(a, s, v_true):
+    """One frame reconstructed by the oracle's Gauss-Newton loop (FP64): the
+    forward model at the iterate, the data residual against the target, and
+    the dual regularised update, from the homogeneous start.  Returns
+    (seconds, updates, converged)."""
+    import oracle
+    Vm, _, _ = oracle.eit_forward(s, v_true, tol=1e-9, want_jacobian=False, exact=True)
+    vm = oracle.flatten_measurement(Vm, s)
+    t0 = time.perf_counter()
+    v = np.zeros_like(v_true)
+    n_up, lam, ok = 0, None, False
+    for it in range(a.max_gn + 1):
+        V, J, _ = oracle.eit_forward(s, v, tol=a.tol, exact=True)
+        y = vm - oracle.flatten_measurement(V, s)
+        ok = bool(np.linalg.norm(y) / np.linalg.norm(vm) <= a.target)
+        if ok or it == a.max_gn:
+            break
+        if lam is None:
+            lam = a.lam_rel * np.linalg.norm(J) / np.sqrt(J.shape[0])
+        v = v + oracle.inverse_dual(J, y, 1.0, lam)
+        n_up += 1
+    return time.perf_counter() - t0, n_up, ok
+
+
+def cpu_baseline(a, frame):
+    """The oracle's Gauss-Newton loop on one frame of the timed workload, on
+    all host cores: frames/s = 1 / seconds."""
     import oracle
     if a.cpu_threads > 0:
         oracle.set_threads(a.cpu_threads)
-    s = oracle.Setup(mesh.nodes, mesh.elements, mesh.edges, mesh.boundary, ports.edges, pat, pat,
-                     np.full(a.electrodes, 1e-3), ref=1.0, logarithmic=True, components=a.components,
-                     height=a.height)
-    v = frames_v[0].astype(np.float64)
-    t0 = time.perf_counter()
-    Vm, _, _ = oracle.eit_forward(s, v, tol=a.tol, want_jacobian=False, exact=True)
-    t1 = time.perf_counter()
-    v0 = np.zeros_like(v)
-    V0, J0, _ = oracle.eit_forward(s, v0, tol=a.tol, exact=True)
-    t2 = time.perf_counter()
-    y = oracle.flatten_measurement(Vm, s) - oracle.flatten_measurement(V0, s)
-    lam = a.lam_rel * np.linalg.norm(J0) / np.sqrt(J0.shape[0])
-    oracle.inverse_dual(J0, y, 1.0, lam)
-    t3 = time.perf_counter()
-    forward_s = t1 - t0
-    gn_iter_s = t3 - t1
-    per_frame = gn_iter_s * gn_iters_mean + forward_s
-    return {
-        "value": 1.0 / per_frame,
-        "unit": UNIT,
-        "cores": oracle.num_threads(),
-        "kind": "port",
-        "sample": (f"1 frame: FP64 forward ({forward_s:.2f} s) + 1 GN iteration = forward+Jacobian+dual "
-                   f"Cholesky step ({gn_iter_s:.2f} s), scaled to {gn_iters_mean:.2f} GN updates + 1 forward "
-                   "check per frame (GPU-measured mean)"),
-    }
+    s, _ = oracle_problem(a)
+    dt, n_up, ok = reference_gn_frame(a, s, frame.astype(np.float64))
+    return {"value": 1.0 / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": (f"1 frame (the first of the first timed step), FP64 Gauss-Newton from the homogeneous start "
+                       f"to the target: {n_up} updates, {dt:.2f} s, converged {ok}")}
+
+
+def oracle_problem(a):
+    """The workload's mesh, ports and model built by the oracle alone (the
+    FP64 restatement of the reference), so that the reference arm loads none
+    of this library's compiled code."""
+    import oracle
+    nodes, elements = oracle.ring_mesh(a.rings)
+    edges, _, boundary = oracle.mesh_edges(nodes, elements)
+    ports = oracle.circular_ports(nodes, elements, edges, boundary, a.electrodes, 0.1)
+    pat = oracle.adjacent_pattern(a.electrodes)
+    s = oracle.Setup(nodes, elements, edges, boundary, ports, pat, pat, np.full(a.electrodes, 1e-3), ref=1.0,
+                     logarithmic=True, components=a.components, height=a.height)
+    return s, nodes[elements].mean(axis=1)
 
 
 def run_reference(a):
-    """--impl reference: the reference's numerics (FP64 oracle port, all host
-    threads) on the same workload, one bounded frame per step."""
+    """--impl reference: the reference's numerics (the FP64 oracle, all host
+    threads) on the same workload.  Each step reconstructs a bounded sample of
+    the GPU arm's step: its first frame (the same seed), by the reference's
+    Gauss-Newton loop (src/solver/solver.cpp:196-225 around
+    src/models/eit.cpp:139-213 and the dual form of src/solver/inverse.cpp:
+    60-238) from the homogeneous start to the same target."""
     rank, world, _ = dist_env()
     if world > 1 and rank != 0:
         return
-    mesh, ports, pat, src = build_problem(a)
-    cent = mesh.nodes[mesh.elements].mean(axis=1)
     import oracle
     if a.cpu_threads > 0:
         oracle.set_threads(a.cpu_threads)
-    s = oracle.Setup(mesh.nodes, mesh.elements, mesh.edges, mesh.boundary, ports.edges, pat, pat,
-                     np.full(a.electrodes, 1e-3), ref=1.0, logarithmic=True, components=a.components,
-                     height=a.height)
-    times, iters = [], []
+    s, cent = oracle_problem(a)
+    times, iters, conv = [], [], 0
     for step in range(a.warmup + a.steps):
-        v_true = synthetic_frames(cent, 1, seed=10_000 + step)[0].astype(np.float64)
-        Vm, _, _ = oracle.eit_forward(s, v_true, tol=1e-9, want_jacobian=False, exact=True)
-        vm = oracle.flatten_measurement(Vm, s)
-        t0 = time.perf_counter()
-        v = np.zeros_like(v_true)
-        n_up = 0
-        lam = None
-        for it in range(a.max_gn + 1):
-            V, J, _ = oracle.eit_forward(s, v, tol=a.tol, exact=True)
-            y = vm - oracle.flatten_measurement(V, s)
-            if np.linalg.norm(y) / np.linalg.norm(vm) <= a.target or it == a.max_gn:
-                break
-            if lam is None:
-                lam = a.lam_rel * np.linalg.norm(J) / np.sqrt(J.shape[0])
-            v = v + oracle.inverse_dual(J, y, 1.0, lam)
-            n_up += 1
-        dt = time.perf_counter() - t0
+        v_true = synthetic_frames(cent, a.frames, seed=rank_frame_seed(0, step))[0].astype(np.float64)
+        dt, n_up, ok = reference_gn_frame(a, s, v_true)
         if step >= a.warmup:
             times.append(dt)
             iters.append(n_up)
-    value = len(times) / sum(times)
+            conv += int(ok)
+    value = conv / sum(times)
+    sample = (f"1 frame per step (the first frame of the GPU arm's step, same seed), FP64 Gauss-Newton from the "
+              f"homogeneous start to the target, {np.mean(iters):.2f} updates mean, {conv}/{len(times)} converged")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded inclusion frames, noise-free)",
-        "config": workload_config(a, frames=1),
+        "config": workload_config(a, a.frames),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-                         "sample": f"1 frame per step, full GN to target ({np.mean(iters):.2f} updates mean)"},
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -378,7 +377,7 @@ def run_gb300(a):
     if a.profile_only:
         v = torch.tensor(synthetic_frames(cent, F, seed=7), device=dev)
         ms, by = model.profile_cg(v, reps=max(a.steps, 1))
-        names = ["k_spmm_dot", "k_update", "k_direction"]
+        names = ["k_spmm_halo" if model.cg_variants(F)[0] >= 72 else "k_spmm_dot", "k_update", "k_direction"]
         print(json.dumps({"profile_only": True, "frames": F, "groups": F * model.info["active_components"],
                           "cg_shapes": model.cg_variants(F).tolist(),
                           "ms": dict(zip(names, ms.tolist())),
@@ -466,9 +465,19 @@ def run_gb300(a):
                 "gn_updates_mean": float(its.mean()), "no_update_fraction": float(np.mean(its == 0)),
                 "frames_converged_fraction": done / (frames_per_step * world * len(results))}
 
+    def with_phases(fn):
+        # the phase timer restarts at the first timed step and runs through the rest
+        def run(s):
+            if s == a.warmup:
+                model.phase_times(True)
+            return fn(s)
+        return run
+
     with ClockSampler(local) as clocks:
-        t_l, r_l, launches = timed_steps(nsteps, a.warmup, learned_step, barrier, stream, torch, lib)
-        t_p, r_p, _ = timed_steps(nsteps, a.warmup, plain_step, barrier, stream, torch, lib)
+        t_l, r_l, launches = timed_steps(nsteps, a.warmup, with_phases(learned_step), barrier, stream, torch, lib)
+        phases_l, _ = model.phase_times(False)
+        t_p, r_p, _ = timed_steps(nsteps, a.warmup, with_phases(plain_step), barrier, stream, torch, lib)
+        phases_p, _ = model.phase_times(False)
         prior_only = None
         if use_prior:
             t_q, r_q, _ = timed_steps(nsteps, a.warmup, prior_step, barrier, stream, torch, lib)
@@ -499,18 +508,35 @@ def run_gb300(a):
     e2e_total, e2e_done = aggregate_over_ranks(sum(e2e_ms), e2e_frames, world, dev)
     e2e_value = e2e_done / (e2e_total / 1e3)
 
-    # roofline of the CG kernels (CUDA events on the launching stream)
+    # device time per phase of one timed step (the library's CUDA-event phase
+    # timer, mpf_eit_phase_times); the phases of a step add up to its time
+    def breakdown(phases, times):
+        per = {k: v / len(times) for k, v in phases.items()}
+        total = sum(per.values())
+        return {"ms_per_step": per, "sum_ms": total, "step_ms": float(np.mean(times)),
+                "share": {k: v / total for k, v in per.items()} if total > 0 else None}
+
+    phase_learned = breakdown(phases_l, t_l)
+    phase_plain = breakdown(phases_p, t_p)
+
+    # roofline of the CG iteration (the largest phase of the step): its three
+    # kernels timed with CUDA events on the launching stream, every group active
     ms, by = model.profile_cg(torch.tensor(truth[0], device=dev), reps=10)
     gbs = by / ms / 1e6
-    dom = int(np.argmax(ms))
-    names = ["k_spmm_dot", "k_update", "k_direction"]
+    names = ["k_spmm_halo" if model.cg_variants(F)[0] >= 72 else "k_spmm_dot", "k_update", "k_direction"]
     peak, peak_kind = measured_peaks()
     groups = F * model.info["active_components"]
-    traffic = profiled_traffic(names[dom])
-    roofline = {"kernel": names[dom], "bound": "hbm", "achieved": float(gbs[dom]), "peak": peak,
-                "unit": "GB/s", "frac": float(gbs[dom] / peak), "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": traffic * groups if traffic else None,
-                "algorithmic_bytes": float(by[dom]), "launch_ms": float(ms[dom])}
+    traffic = [CG_DRAM_BYTES_PER_GROUP.get(n) for n in names]
+    roofline = {"kernel": "CG iteration: " + " + ".join(names), "bound": "hbm",
+                "achieved": float(by.sum() / ms.sum() / 1e6), "peak": peak, "unit": "GB/s",
+                "frac": float(by.sum() / ms.sum() / 1e6 / peak), "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": float(sum(traffic) * groups) if all(t is not None for t in traffic) else None,
+                "algorithmic_bytes": float(by.sum()), "launch_ms": float(ms.sum()),
+                "why": "the Krylov iterations are the largest phase of the timed step (phase_breakdown)"}
+    cg_kernels = {n: {"ms": float(ms[i]), "algorithmic_bytes": float(by[i]), "gbs": float(gbs[i]),
+                      "frac_of_hbm": float(gbs[i] / peak),
+                      "dram_bytes": (traffic[i] * groups if traffic[i] is not None else None)}
+                  for i, n in enumerate(names)}
 
     # assembly and Jacobian kernels (HBM-bound), CUDA events on the launching stream
     fem_ms, fem_by = model.profile_fem(torch.tensor(truth[0], device=dev), reps=5)
@@ -538,7 +564,7 @@ def run_gb300(a):
         return
     cpu = None
     if not a.no_cpu_baseline:
-        cpu = cpu_baseline(a, mesh, ports, pat, truth[0], plain["gn_updates_mean"])
+        cpu = cpu_baseline(a, truth[a.warmup][0])
     mlp_flops = 6.0 * 256 * net.param_count * train_steps
     line = {
         "metric": METRIC, "value": learned["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -574,8 +600,9 @@ def run_gb300(a):
         "learned_vs_plain_batched": learned["value"] / plain["value"],
         "learned_vs_plain_single_frame": (learned["value"] / single["value"]) if single else None,
         "spmv_gbs": float(gbs[0]),
-        "cg_kernel_ms": {k: float(v) for k, v in zip(names, ms)},
-        "cg_kernel_gbs": {k: float(v) for k, v in zip(names, gbs)},
+        "spmv": {"kernel": names[0], "gbs": float(gbs[0]), "frac_of_hbm": float(gbs[0] / peak), "target_frac": 0.70},
+        "cg_kernels": cg_kernels,
+        "phase_breakdown": {"learned": phase_learned, "plain_gn_batched": phase_plain},
         "roofline": roofline,
         "jjt_tensor_core": jjt,
         "fem_kernels": fem,

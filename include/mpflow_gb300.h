@@ -328,6 +328,30 @@ int mpf_eit_profile_fem(mpf_eit_t model, int32_t frames, const float* gamma, int
 int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int32_t reps, double* ms,
                        double* bytes, mpf_stream_t stream);
 
+/* Device-time breakdown of the model's forward and Gauss-Newton calls by
+ * phase.  While enabled, the library records a CUDA event on the call's
+ * stream at every change of phase and attributes the time between
+ * consecutive events to the phase that ran there, so the phases of a call add
+ * up to its device time from the first mark to the last (gaps in which the
+ * device waits for the host count toward the phase that follows them).
+ * enable = 1 starts (and clears) the accumulation, 0 stops it, -1 leaves it
+ * as it is; ms[min(cap, MPF_PHASES)] receives the milliseconds accumulated per
+ * phase (indices MPF_PHASE_*) and *calls the top-level calls timed.
+ * No reference counterpart (measurement support). */
+#define MPF_PHASES 11
+#define MPF_PHASE_ASSEMBLY 0    /* S, R slot values (and FP64 copies, Dirichlet rows) */
+#define MPF_PHASE_CG_SETUP 1    /* launch-shape autotuning, coarse-space factor and inverse */
+#define MPF_PHASE_CG 2          /* Krylov iterations, FP64 refinement, warm-start copies */
+#define MPF_PHASE_VOLTAGES 3    /* electrode voltages and data residuals */
+#define MPF_PHASE_JACOBIAN 4
+#define MPF_PHASE_GRAM 5        /* J J^T + mu I (tensor-core split-BF16, FP64 fallback) */
+#define MPF_PHASE_CHOLESKY 6    /* FP64 factor and triangular solves */
+#define MPF_PHASE_UPDATE 7      /* gamma += J^T w, range check, undo of diverged frames */
+#define MPF_PHASE_NETWORK 8     /* learned start: network forward pass */
+#define MPF_PHASE_PRIOR 9       /* learned start: network input and linear prior */
+#define MPF_PHASE_HOST 10       /* host decisions between device work (masks, convergence checks) */
+int mpf_eit_phase_times(mpf_eit_t model, int32_t enable, double* ms, int32_t cap, int64_t* calls);
+
 /* CG iterations of every (frame, harmonic) group in the last inner solve of
  * the last forward call, group g = frame * active_components + harmonic.
  * Writes min(count, cap) entries; *count receives the group count.  The

@@ -95,6 +95,7 @@ SIGNATURES = {
     "mpf_gn_solve": (_I, [_P, _I, _P, _P, _D, _D, _I, ctypes.POINTER(SolveOpts), _P, _P,
                           ctypes.POINTER(GnStats), _P]),
     "mpf_eit_profile_cg": (_I, [_P, _I, _P, _I, _P, _P, _P]),
+    "mpf_eit_phase_times": (_I, [_P, _I, _P, _I, _P]),
     "mpf_eit_group_iterations": (_I, [_P, _P, _I, _P]),
     "mpf_eit_cg_variants": (_I, [_P, _P, _I, _P]),
     "mpf_inverse_solve": (_I, [_P, _I, _D, _I, _P, _P, _P, _P, _P]),

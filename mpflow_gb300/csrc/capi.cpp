@@ -52,6 +52,7 @@ void eit_destroy(mpf_eit* m);
 int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, double target, int maxIters,
              const mpf_solve_opts* o, int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s);
 int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
+int phase_times(mpf_eit* m, int enable, double* ms, int cap, int64_t* calls);
 int profile_fem(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
 int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
 int cg_variants(mpf_eit* m, const int32_t* set, int F, int32_t* get);
@@ -279,6 +280,13 @@ int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int3
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_profile_cg: model == nullptr");
         return mpf::profile_cg(model, frames, gamma, reps, ms, bytes, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_phase_times(mpf_eit_t model, int32_t enable, double* ms, int32_t cap, int64_t* calls) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_phase_times: model == nullptr");
+        return mpf::phase_times(model, enable, ms, cap, calls);
     })
 }
 

@@ -117,13 +117,28 @@ struct mpf_eit {
     double priorLambda = 0.0;
     mpf::DevBuf<float> priorW;
 
+    // device-time breakdown by phase (mpf_eit_phase_times): while enabled,
+    // phase_mark records an event on the stream at every change of phase;
+    // phase_flush adds the time between consecutive marks to their phase
+    bool phaseOn = false;
+    std::vector<cudaEvent_t> phaseEvents;
+    std::vector<int> phaseIds;
+    int phaseUsed = 0;
+    double phaseMs[MPF_PHASES] = {};
+    long long phaseCalls = 0;
+
     ~mpf_eit() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
         if (pinnedActive) cudaFreeHost(pinnedActive);
+        for (auto e : phaseEvents) cudaEventDestroy(e);
     }
 };
 
 namespace mpf {
+// phase timer (model.cu): the phase the stream's work enters after this point
+int phase_mark(mpf_eit* m, int phase, cudaStream_t s);
+// attribute the marked intervals to their phases (synchronises)
+int phase_flush(mpf_eit* m, cudaStream_t s);
 // fixed_kernels.cu: voltage (Fixed) sources
 int fixed_plan(mpf_eit* m, const std::vector<double>& excBin);
 int fixed_prepare(mpf_eit* m, int F, cudaStream_t s);

@@ -33,6 +33,46 @@ double lead(const double* col, int L) {
 
 }  // namespace
 
+int phase_mark(mpf_eit* m, int phase, cudaStream_t s) {
+    if (!m->phaseOn) return MPF_OK;
+    if (m->phaseUsed == (int)m->phaseEvents.size()) {
+        cudaEvent_t e;
+        MPF_CUDA(cudaEventCreate(&e));
+        m->phaseEvents.push_back(e);
+        m->phaseIds.push_back(0);
+    }
+    MPF_CUDA(cudaEventRecord(m->phaseEvents[m->phaseUsed], s));
+    m->phaseIds[m->phaseUsed++] = phase;
+    return MPF_OK;
+}
+
+int phase_flush(mpf_eit* m, cudaStream_t s) {
+    if (!m->phaseOn || m->phaseUsed == 0) return MPF_OK;
+    MPF_TRY(phase_mark(m, MPF_PHASE_HOST, s));
+    MPF_CUDA(cudaEventSynchronize(m->phaseEvents[m->phaseUsed - 1]));
+    for (int i = 0; i + 1 < m->phaseUsed; ++i) {
+        float t = 0.f;
+        MPF_CUDA(cudaEventElapsedTime(&t, m->phaseEvents[i], m->phaseEvents[i + 1]));
+        m->phaseMs[m->phaseIds[i]] += t;
+    }
+    m->phaseUsed = 0;
+    ++m->phaseCalls;
+    return MPF_OK;
+}
+
+int phase_times(mpf_eit* m, int enable, double* ms, int cap, int64_t* calls) {
+    if (ms)
+        for (int i = 0; i < cap && i < MPF_PHASES; ++i) ms[i] = m->phaseMs[i];
+    if (calls) *calls = m->phaseCalls;
+    if (enable >= 0) {
+        m->phaseOn = enable != 0;
+        m->phaseUsed = 0;
+        m->phaseCalls = 0;
+        for (double& v : m->phaseMs) v = 0.0;
+    }
+    return MPF_OK;
+}
+
 int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     MPF_CHECK(d && out, MPF_EINVAL, "mpf_eit_create: null argument");
     MPF_CHECK(d->n_nodes > 0 && d->n_elements > 0 && d->nodes && d->elements && d->edges && d->port_edges,
@@ -604,6 +644,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     fill_defaults(optsIn, o, m->n);
     const bool refine = o.refine_tol > 0.0;
     MPF_TRY(ensure_workspace(m, F, refine, wantJ));
+    MPF_TRY(phase_mark(m, MPF_PHASE_CG, s));
     if (o.warm_start == 2) {
         // every frame starts from the homogeneous fields
         MPF_TRY(ensure_v0(m, s));
@@ -617,8 +658,10 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     const bool warm = o.warm_start && m->fieldsValid && m->lastFrames == F;
     MPF_CHECK(!(m->fixed && refine), MPF_ENOTSUP,
               "forward solve: FP64 refinement is implemented for current (open) sources only");
+    MPF_TRY(phase_mark(m, MPF_PHASE_ASSEMBLY, s));
     MPF_TRY(eit_assemble(m, F, gamma, refine, s));
     if (m->fixed) MPF_TRY(fixed_prepare(m, F, s));
+    MPF_TRY(phase_mark(m, MPF_PHASE_CG_SETUP, s));
     const bool bicg = o.solver == 1;
     if (bicg) MPF_TRY(ensure_bicgstab(m, F));
     if (!warm && !bicg) MPF_TRY(tune_cg(m, F, s));
@@ -630,6 +673,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
                       m->cAggSize.ptr};
         MPF_TRY(coarse_launch_setup(P, cp, m->Ac64.ptr, m->infoC.ptr, s, m->Lc.ptr, m->LinvD.ptr, m->Binv.ptr));
     }
+    MPF_TRY(phase_mark(m, MPF_PHASE_CG, s));
     int totalIters = 0, notConv = 0, refinements = 0;
     double maxRel = 0.0;
     // fields are kept in the reference's convention; the iteration works on
@@ -691,12 +735,17 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     }
     m->fieldsValid = true;
     m->lastFrames = F;
+    MPF_TRY(phase_mark(m, MPF_PHASE_VOLTAGES, s));
     MeasPlan mp{(int)m->nzNode.count, m->nzNode.ptr, nullptr, m->nzVal.ptr, m->nzPtr.ptr};
     if (m->fixed) MPF_TRY(fixed_currents(m, F, s));
     MPF_TRY(fem_launch_gram_meas(P.G, m->KP, m->npad, mp, m->fixed ? m->curX.ptr : m->X.ptr, m->Gm.ptr, s));
     MPF_TRY(fem_launch_voltages(F, m->Ca, m->KP, m->Mm, m->Md, m->Gm.ptr, m->beta.ptr, m->measU.ptr,
                                 m->measScale.ptr, m->driveU.ptr, m->driveScale.ptr, m->V.ptr, s));
-    if (wantJ) MPF_TRY(eit_jacobian(m, F, gamma, nullptr, true, s));
+    if (wantJ) {
+        MPF_TRY(phase_mark(m, MPF_PHASE_JACOBIAN, s));
+        MPF_TRY(eit_jacobian(m, F, gamma, nullptr, true, s));
+    }
+    MPF_TRY(phase_mark(m, MPF_PHASE_HOST, s));
     MPF_CUDA(cudaStreamSynchronize(s));
     MPF_CUDA(cudaGetLastError());
     if (stats) {
@@ -782,6 +831,7 @@ int eit_forward(mpf_eit* m, int F, const float* gamma, float* V, float* Jref, co
     if (V) MPF_CUDA(cudaMemcpyAsync(V, m->V.ptr, sizeof(float) * (size_t)F * m->Mm * m->Md, cudaMemcpyDeviceToDevice, s));
     if (Jref) MPF_TRY(fem_launch_transpose_jacobian(F, m->rowsJ, m->Epad, m->E, m->J.ptr, Jref, s));
     MPF_CUDA(cudaStreamSynchronize(s));
+    MPF_TRY(phase_flush(m, s));
     return st;
 }
 
@@ -803,8 +853,10 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
 static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* frameActive, cudaStream_t s,
                      const int* hostActive = nullptr, std::vector<int>* broken = nullptr) {
     const double mu = (double)m->ref * lambda * (double)m->ref * lambda;
+    MPF_TRY(phase_mark(m, MPF_PHASE_GRAM, s));
     MPF_TRY(dense_gram_f64_shift(F, m->rowsJ, m->Epad, m->Jhi.ptr, m->Jlo.ptr, m->Epad, mu, m->A64.ptr,
                                  m->gramWork.ptr, m->gramWork.count, s, frameActive));
+    MPF_TRY(phase_mark(m, MPF_PHASE_CHOLESKY, s));
     MPF_CUDA(cudaMemsetAsync(m->info.ptr, 0, sizeof(int) * F, s));
     MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, frameActive));
     // frames whose split-BF16 J J^T + mu I is not positive definite (mu below
@@ -816,8 +868,11 @@ static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* 
     for (int f = 0; f < F; ++f) any |= (redo[f] = info[f] != 0) != 0;
     if (any) {
         MPF_TRY(m->redoMask.upload(redo));
+        MPF_TRY(phase_mark(m, MPF_PHASE_JACOBIAN, s));
         MPF_TRY(eit_jacobian(m, F, gamma, m->redoMask.ptr, true, s));
+        MPF_TRY(phase_mark(m, MPF_PHASE_GRAM, s));
         MPF_TRY(dense_gram_f64_exact(F, m->rowsJ, m->Epad, m->J.ptr, m->Epad, mu, m->A64.ptr, m->redoMask.ptr, s));
+        MPF_TRY(phase_mark(m, MPF_PHASE_CHOLESKY, s));
         MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, m->redoMask.ptr));
         if (broken) {
             MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
@@ -833,7 +888,9 @@ static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* 
             }
         }
     }
+    MPF_TRY(phase_mark(m, MPF_PHASE_CHOLESKY, s));
     MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s, frameActive));
+    MPF_TRY(phase_mark(m, MPF_PHASE_UPDATE, s));
     MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->Jhi.ptr, m->Jlo.ptr, m->y.ptr, frameActive, gamma,
                                     s));
     return MPF_OK;
@@ -859,11 +916,15 @@ int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, 
     int st = eit_forward_ws(m, F, gamma, false, o, stats, s);
     if (st != MPF_OK && st != MPF_ENOCONV) return st;
     MPF_TRY(ensure_workspace(m, F, false, true));
+    MPF_TRY(phase_mark(m, MPF_PHASE_VOLTAGES, s));
     MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
+    MPF_TRY(phase_mark(m, MPF_PHASE_JACOBIAN, s));
     MPF_TRY(eit_jacobian(m, F, gamma, nullptr, false, s));
     MPF_TRY(gn_update(m, F, gamma, lambda, nullptr, s));
+    MPF_TRY(phase_mark(m, MPF_PHASE_HOST, s));
     if (residual) MPF_CUDA(cudaMemcpyAsync(residual, m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
     MPF_TRY(gn_check(m, F, s));
+    MPF_TRY(phase_flush(m, s));
     return st;
 }
 
@@ -896,8 +957,10 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         MPF_TRY(ensure_workspace(m, F, false, true));
         warm = 1;
         cgTotal += fs.iterations;
+        MPF_TRY(phase_mark(m, MPF_PHASE_VOLTAGES, s));
         MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
         MPF_CUDA(cudaMemcpyAsync(res.data(), m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
+        MPF_TRY(phase_mark(m, MPF_PHASE_HOST, s));
         MPF_CUDA(cudaStreamSynchronize(s));
         if (checkStart) {
             checkStart = false;
@@ -909,6 +972,7 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
                 nrej += reject[f];
             }
             if (nrej) {
+                MPF_TRY(phase_mark(m, MPF_PHASE_PRIOR, s));
                 MPF_CUDA(cudaMemcpyAsync(m->frameMask.ptr, reject.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
                 MPF_TRY(fem_launch_fill_frames(F, m->E, m->frameMask.ptr, gamma0, gamma, s));
                 // a restarted frame begins from the homogeneous fields, which
@@ -931,6 +995,7 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         }
         if (live == 0 || it == maxIters) break;
         for (int f = 0; f < F; ++f) iters[f] += mask[f];
+        MPF_TRY(phase_mark(m, MPF_PHASE_JACOBIAN, s));
         MPF_CUDA(cudaMemcpyAsync(m->frameMask.ptr, mask.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
         MPF_TRY(eit_jacobian(m, F, gamma, m->frameMask.ptr, false, s));
         // a frame whose J J^T + mu I cannot be factored (also with the FP64
@@ -948,6 +1013,7 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         std::vector<int> bad(F);
         MPF_TRY(fem_launch_gamma_check(F, m->E, gamma, m->frameMask.ptr, m->logarithmic, m->badFrame.ptr, s));
         MPF_CUDA(cudaMemcpyAsync(bad.data(), m->badFrame.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
+        MPF_TRY(phase_mark(m, MPF_PHASE_HOST, s));
         MPF_CUDA(cudaStreamSynchronize(s));
         for (int f = 0; f < F; ++f)
             if (bad[f]) {
@@ -959,6 +1025,7 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         ++gnIters;
         ++it;
     }
+    MPF_TRY(phase_flush(m, s));
     int converged = 0;
     for (int f = 0; f < F; ++f) converged += res[f] <= target;
     if (itersOut) std::copy(iters.begin(), iters.end(), itersOut);
@@ -1097,10 +1164,13 @@ int gn_solve_learned(mpf_eit* m, mpf_mlp* net, int F, float* gamma, const float*
     MPF_TRY(ensure_v0(m, s));
     MPF_TRY(m->learnX.alloc((size_t)F * L));
     MPF_TRY(m->res0.alloc((size_t)F));
+    MPF_TRY(phase_mark(m, MPF_PHASE_PRIOR, s));
     MPF_TRY(fem_launch_learned_input(F, L, vMeas, m->V0.ptr, m->v0InvRms, m->learnX.ptr, m->res0.ptr, s));
     std::vector<double> res0(F);
     MPF_CUDA(cudaMemcpyAsync(res0.data(), m->res0.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
+    MPF_TRY(phase_mark(m, MPF_PHASE_NETWORK, s));
     MPF_TRY(mlp_forward(net, F, m->learnX.ptr, gamma, m->E, s));  // synchronises
+    MPF_TRY(phase_mark(m, MPF_PHASE_PRIOR, s));
     if (m->priorReady) MPF_TRY(learned_prior_apply(m, F, m->learnX.ptr, gamma, m->E, 1, s));
     MPF_TRY(gn_loop(m, F, gamma, vMeas, lambda, target, maxIters, o, res0.data(), homogeneous_gamma(m), accepted,
                     itersOut, resOut, stats, s));

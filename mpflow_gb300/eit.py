@@ -455,6 +455,20 @@ class EIT:
         check(lib().mpf_eit_profile_fem(self._h, F, ptr(g), int(reps), ptr(ms), ptr(by), _stream()))
         return ms, by
 
+    PHASES = ("assembly", "cg_setup", "cg", "voltages", "jacobian", "gram", "cholesky", "update", "network",
+              "prior", "host")
+
+    def phase_times(self, enable=None):
+        """Device milliseconds accumulated per phase of the forward and
+        Gauss-Newton calls since the timer was last (re)started, and the
+        number of top-level calls timed (mpf_eit_phase_times).  enable=True
+        restarts the accumulation, False stops it, None leaves it running."""
+        ms = np.zeros(len(self.PHASES))
+        calls = ctypes.c_int64(0)
+        flag = -1 if enable is None else int(bool(enable))
+        check(lib().mpf_eit_phase_times(self._h, flag, ptr(ms), len(self.PHASES), ctypes.byref(calls)))
+        return dict(zip(self.PHASES, ms.tolist())), int(calls.value)
+
     def profile_cg(self, gamma, reps: int = 20):
         """Mean CUDA-event time (ms) and algorithmic bytes of one launch of the
         SpMM, update and direction kernels (mpf_eit_profile_cg)."""

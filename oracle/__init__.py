@@ -65,6 +65,8 @@ def _declare(L):
     L.orc_data_rows.restype = _U
     L.orc_num_threads.restype = _I
     L.orc_set_threads.argtypes = [_I]
+    L.orc_ring_mesh.argtypes = [_I, _D, _P, _P]
+    L.orc_ring_mesh.restype = _I
     L.orc_mesh_edges.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P]
     L.orc_mesh_edges.restype = _I
     L.orc_circular_ports.argtypes = [_I, _P, _I, _P, _P, _I, _P, _I, _D, _D, _I, _P, _I, _P]
@@ -125,6 +127,28 @@ def mesh_edges(nodes: np.ndarray, elements: np.ndarray):
     if ne < 0:
         raise ValueError("orc_mesh_edges: invalid mesh")
     return edges[:ne].copy(), elementEdges, boundary[:nb.value].copy()
+
+
+def ring_mesh(rings: int, radius: float = 1.0):
+    """Concentric-ring disk (nodes N x 2, elements E x 3) with N = 1 + 3R(R+1)
+    and E = 6R^2, the benchmark's mesh; the same numbering as the library's
+    generator, written independently (orc_ring_mesh)."""
+    R = int(rings)
+    nodes = np.zeros((1 + 3 * R * (R + 1), 2))
+    elements = np.zeros((6 * R * R, 3), np.int32)
+    e = lib().orc_ring_mesh(R, float(radius), _p(nodes), _p(elements))
+    if e != elements.shape[0]:
+        raise ValueError(f"orc_ring_mesh failed ({e})")
+    return nodes, elements
+
+
+def adjacent_pattern(count: int) -> np.ndarray:
+    """Adjacent pattern (+1 on port j, -1 on port j+1), ports x count."""
+    p = np.zeros((count, count))
+    j = np.arange(count)
+    p[j, j] = 1.0
+    p[(j + 1) % count, j] = -1.0
+    return p
 
 
 def circular_ports(nodes, elements, edges, boundary, count, width, offset=0.0, clockwise=False,

@@ -88,6 +88,50 @@ void orc_set_threads(int n) {
  *     the orientation circularBoundary relies on (src/fem/ports.cpp:51-63);
  *   - boundary lists boundary edge indices in increasing order.
  * Returns the number of edges, or -1 on bad input. */
+/* Concentric-ring disk, the workload mesh of the benchmark (no reference
+ * counterpart: the reference meshes with libdistmesh, which is absent).
+ * Node 0 is the centre; ring i (1..R) carries 6i nodes at radius
+ * radius*i/R, angles 2 pi k / (6i), numbered 1 + 3i(i-1) + k.  Triangles: the
+ * six around the centre, then for every ring i >= 2 and sector s the strip
+ * between rings i-1 and i (outer edge j, then the inner edge after it),
+ * each oriented counter-clockwise.  Returns the element count. */
+static int orc_ring_node(int ring, int k) { return ring == 0 ? 0 : 1 + 3 * ring * (ring - 1) + k % (6 * ring); }
+
+static void orc_ring_tri(const double* nodes, int* elements, int* e, int a, int b, int c) {
+    const double ax = nodes[2 * a], ay = nodes[2 * a + 1];
+    const double orient = (nodes[2 * b] - ax) * (nodes[2 * c + 1] - ay) - (nodes[2 * c] - ax) * (nodes[2 * b + 1] - ay);
+    int* t = elements + 3 * (*e);
+    t[0] = a;
+    t[1] = orient < 0.0 ? c : b;
+    t[2] = orient < 0.0 ? b : c;
+    ++(*e);
+}
+
+int orc_ring_mesh(int R, double radius, double* nodes, int* elements) {
+    if (R < 1 || !(radius > 0.0)) return -1;
+    nodes[0] = nodes[1] = 0.0;
+    for (int i = 1; i <= R; ++i) {
+        const double r = radius * (double)i / (double)R;
+        for (int k = 0; k < 6 * i; ++k) {
+            const double th = (2.0 * M_PI * (double)k) / (6.0 * (double)i);
+            const int id = orc_ring_node(i, k);
+            nodes[2 * id] = r * cos(th);
+            nodes[2 * id + 1] = r * sin(th);
+        }
+    }
+    int e = 0;
+    for (int k = 0; k < 6; ++k) orc_ring_tri(nodes, elements, &e, 0, orc_ring_node(1, k), orc_ring_node(1, k + 1));
+    for (int i = 2; i <= R; ++i)
+        for (int sct = 0; sct < 6; ++sct)
+            for (int j = 0; j < i; ++j) {
+                const int in0 = orc_ring_node(i - 1, sct * (i - 1) + j);
+                const int o0 = orc_ring_node(i, sct * i + j), o1 = orc_ring_node(i, sct * i + j + 1);
+                orc_ring_tri(nodes, elements, &e, in0, o0, o1);
+                if (j < i - 1) orc_ring_tri(nodes, elements, &e, in0, o1, orc_ring_node(i - 1, sct * (i - 1) + j + 1));
+            }
+    return e;
+}
+
 int orc_mesh_edges(int N, int E, const double* nodes, const int* elements,
                    int* edges /* cap 3E x 2 */, int* elementEdges /* E x 3 */,
                    int* boundary /* cap 3E */, int* nBoundary) {

@@ -461,7 +461,11 @@ def run_gb300(a):
                          for r in results))
         total_ms, done = aggregate_over_ranks(float(np.sum(times)), done, world, dev)
         its = np.concatenate([r[0] for r in results])
+        sts = [r[2] for r in results if hasattr(r[2], "solves_fp32")]
+        solves = ({"fp32_refined": sum(t.solves_fp32 for t in sts) / len(sts),
+                   "fp64": sum(t.solves_fp64 for t in sts) / len(sts)} if sts else None)
         return {"value": done / (total_ms / 1e3), "ms_per_step": float(np.mean(times)),
+                "gn_solves_per_step": solves,
                 "gn_updates_mean": float(its.mean()), "no_update_fraction": float(np.mean(its == 0)),
                 "frames_converged_fraction": done / (frames_per_step * world * len(results))}
 

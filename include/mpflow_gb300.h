@@ -194,6 +194,15 @@ typedef struct mpf_solve_opts {
      *    c' 1 1^T term as the CG, so both return the same fields.  Needs the
      *    Jacobi preconditioner (preconditioner = 1 is ignored). */
     int32_t solver;
+    /* Factor of J J^T + mu I in the Gauss-Newton update (mpf_gn_step,
+     * mpf_gn_solve, mpf_gn_solve_learned):
+     * 0: Cholesky in FP32 arithmetic (a cluster of CTAs per frame) with FP64
+     *    iterative refinement against the FP64 matrix; a frame whose FP32
+     *    factor breaks down or whose refinement stalls falls back to option 1
+     *    (default);
+     * 1: FP64 Cholesky only (the solve of src/solver/inverse.cpp:213-238 is a
+     *    dense CG on J^T J; both give the regularised update). */
+    int32_t gn_factor;
 } mpf_solve_opts;
 
 typedef struct mpf_solve_stats {
@@ -274,6 +283,8 @@ typedef struct mpf_gn_stats {
     int32_t cg_iterations;    /* CG iterations summed over the forward solves (slowest group) */
     int32_t frames_converged; /* frames whose residual reached the target */
     double seconds;           /* host wall time of the call (synchronised) */
+    int32_t solves_fp32;      /* frame updates solved by the FP32 factor with FP64 refinement */
+    int32_t solves_fp64;      /* frame updates solved by the FP64 factor (gn_factor 1, or the fallback) */
 } mpf_gn_stats;
 
 /* Batched Gauss-Newton reconstruction: repeats mpf_gn_step on every frame

@@ -52,7 +52,8 @@ class EitInfo(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("refine_tol", ctypes.c_double),
                 ("max_refine", ctypes.c_int32), ("warm_start", ctypes.c_int32),
-                ("check_every", ctypes.c_int32), ("preconditioner", ctypes.c_int32), ("solver", ctypes.c_int32)]
+                ("check_every", ctypes.c_int32), ("preconditioner", ctypes.c_int32), ("solver", ctypes.c_int32),
+                ("gn_factor", ctypes.c_int32)]
 
 
 class SolveStats(ctypes.Structure):
@@ -63,7 +64,8 @@ class SolveStats(ctypes.Structure):
 
 class GnStats(ctypes.Structure):
     _fields_ = [("gn_iterations", ctypes.c_int32), ("cg_iterations", ctypes.c_int32),
-                ("frames_converged", ctypes.c_int32), ("seconds", ctypes.c_double)]
+                ("frames_converged", ctypes.c_int32), ("seconds", ctypes.c_double),
+                ("solves_fp32", ctypes.c_int32), ("solves_fp64", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p

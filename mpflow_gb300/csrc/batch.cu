@@ -57,7 +57,7 @@ struct BatchClass {
     int coarseOK = 0, ncPad = 0, cNnz = 0, capFC = 0;
     DevBuf<int32_t> cPairI, cPairJ, cPairPtr, cSlots, cMeshPairPtr, cMeshNc;
     DevBuf<float> cAggSize;
-    DevBuf<double> Ac64, rzFine, bzFine;
+    DevBuf<double> Ac64, Lc64, rzFine, bzFine;
     DevBuf<float> Lc, LinvD, Binv, rcV, rcB, ycV;
     DevBuf<int> infoC;
 };
@@ -142,6 +142,7 @@ static int class_coarse_workspace(mpf_batch* b, BatchClass& cl, int F) {
     const size_t G = (size_t)F * b->Ca * cl.members.size(), nc2 = (size_t)cl.ncPad * cl.ncPad;
     const size_t cv = G * cl.ncPad * cl.KP;
     MPF_TRY(cl.Ac64.alloc(G * nc2));
+    MPF_TRY(cl.Lc64.alloc(G * nc2));
     MPF_TRY(cl.Lc.alloc(G * nc2));
     MPF_TRY(cl.LinvD.alloc(G * (cl.ncPad / 32) * 1024));
     MPF_TRY(cl.Binv.alloc(G * nc2));
@@ -153,7 +154,7 @@ static int class_coarse_workspace(mpf_batch* b, BatchClass& cl, int F) {
     MPF_CUDA(cudaMemset(cl.ycV.ptr, 0, cv * sizeof(float)));
     MPF_TRY(cl.rzFine.alloc(G * cl.KP));
     MPF_TRY(cl.bzFine.alloc(G * cl.KP));
-    MPF_TRY(cl.infoC.alloc(G));
+    MPF_TRY(cl.infoC.alloc(2 * G));
     cl.capFC = F;
     return MPF_OK;
 }
@@ -424,7 +425,7 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
             CoarsePlan cp{0, cl.ncPad, cl.cNnz, cl.cPairI.ptr, cl.cPairJ.ptr, cl.cPairPtr.ptr, cl.cSlots.ptr,
                           cl.cAggSize.ptr, cl.cMeshPairPtr.ptr, cl.cMeshNc.ptr};
             MPF_TRY(coarse_launch_setup(Ps.back(), cp, cl.Ac64.ptr, cl.infoC.ptr, s, cl.Lc.ptr, cl.LinvD.ptr,
-                                        cl.Binv.ptr));
+                                        cl.Binv.ptr, cl.Lc64.ptr));
         }
     }
     cudaEvent_t e0, e1;

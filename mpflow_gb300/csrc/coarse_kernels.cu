@@ -21,6 +21,8 @@
 #include <algorithm>
 #include <atomic>
 
+#include <vector>
+
 #include "model.h"
 
 namespace mpf {
@@ -375,14 +377,46 @@ int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count) 
 }
 
 int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,
-                        float* Lc, float* LinvD, float* Binv) {
+                        float* Lc, float* LinvD, float* Binv, double* L64) {
     const size_t per = (size_t)cp.ncPad * cp.ncPad;
     MPF_CUDA(cudaMemsetAsync(Ac64, 0, sizeof(double) * per * P.G, s));
     k_coarse_assemble<<<dim3(std::min((cp.nnz + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64);
     k_coarse_fixup<<<dim3((int)std::min<size_t>((per + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64);
     MPF_LAUNCHED(2);
-    MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s));
-    k_coarse_prep<<<dim3(cp.ncPad / 32, P.G), 32, 0, s>>>(cp.ncPad, Ac64, Lc, LinvD);
+    // The coarse operator is applied in FP32 (Binv), so its factor is taken
+    // in FP32 arithmetic, one CTA per group, into L64; a group whose FP32
+    // factor breaks down (a badly conditioned coarse matrix) is factored in
+    // FP64 in place and its factor copied over.  A group whose coarse matrix
+    // is not positive definite in FP64 either (a parameter far outside the
+    // model's range) is left without the coarse correction: its Binv is zero,
+    // so it iterates with Jacobi alone.
+    const double* Lsrc = Ac64;
+    std::vector<int> jacobiOnly;
+    if (L64) {
+        MPF_TRY(dense_potrf32(P.G, cp.ncPad, Ac64, L64, info, s));
+        std::vector<int> h(P.G), redo(P.G, 0);
+        MPF_CUDA(cudaMemcpyAsync(h.data(), info, sizeof(int) * P.G, cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        bool any = false;
+        for (int g = 0; g < P.G; ++g) any |= (redo[g] = h[g] != 0) != 0;
+        if (any) {
+            int* mask = info + P.G;  // info has 2 * G entries: pivots, then this mask
+            MPF_CUDA(cudaMemcpyAsync(mask, redo.data(), sizeof(int) * P.G, cudaMemcpyHostToDevice, s));
+            MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s, mask));
+            for (int g = 0; g < P.G; ++g)
+                if (redo[g])
+                    MPF_CUDA(cudaMemcpyAsync(L64 + per * g, Ac64 + per * g, sizeof(double) * per,
+                                             cudaMemcpyDeviceToDevice, s));
+            MPF_CUDA(cudaMemcpyAsync(h.data(), info, sizeof(int) * P.G, cudaMemcpyDeviceToHost, s));
+            MPF_CUDA(cudaStreamSynchronize(s));
+            for (int g = 0; g < P.G; ++g)
+                if (redo[g] && h[g] != 0) jacobiOnly.push_back(g);
+        }
+        Lsrc = L64;
+    } else {
+        MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s));
+    }
+    k_coarse_prep<<<dim3(cp.ncPad / 32, P.G), 32, 0, s>>>(cp.ncPad, Lsrc, Lc, LinvD);
     const size_t smem = coarse_solve_smem(cp.ncPad);
     static std::atomic<size_t> configured[64];
     int dev = 0;
@@ -394,6 +428,10 @@ int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, 
     }
     k_coarse_inverse<<<dim3(cp.ncPad / 32, P.G), kCT, smem, s>>>(cp.ncPad, Lc, LinvD, Binv);
     MPF_LAUNCHED(2);
+    for (int g : jacobiOnly) {
+        MPF_CUDA(cudaMemsetAsync(Binv + per * g, 0, sizeof(float) * per, s));
+        MPF_CUDA(cudaMemsetAsync(info + g, 0, sizeof(int), s));
+    }
     return MPF_OK;
 }
 

@@ -287,6 +287,248 @@ __global__ void k_potrf_diag(int n, double* A, int k, int* info, const int* fram
     }
 }
 
+// ---------------------------------------------------------------------------
+// Batched Cholesky in FP32 arithmetic (k_potrf32): one thread-block cluster
+// of CL CTAs per matrix (CL = 1 for batches that fill the GPU on their own).
+// Right-looking in 32-column steps on FP64 column-major storage:
+//   (a) warp 0 of every CTA factors the diagonal block (lane r owns row r)
+//       and inverts it -- the same values in every CTA;
+//   (b) every CTA solves all rows of the panel below against that inverse
+//       into its own shared memory (row stride 36 floats so rows can be read
+//       as float4);
+//   (c) the trailing lower triangle is updated in 32 x 32 tiles spread over
+//       the cluster's warps: lane r owns row r of a tile, loads its targets
+//       8 columns at a time, then accumulates the dot products of length 32
+//       from float4 broadcasts of the panel;
+//   a cluster barrier (release / acquire) ends the step, so the next step's
+//   reads of the diagonal block and panel see every rank's updates;
+//   (d) the step's block column (diagonal block from rank 0, each 32-row
+//       panel block from one rank) is stored from shared memory after that
+//       barrier, when no rank reads its input values any more.
+// The factor is returned in the FP64 storage (values of FP32 precision); the
+// strict upper triangle is not touched.  info[b] = the first pivot (1-based)
+// that is not positive (it is replaced by 1 so that the factorisation
+// finishes without NaN), as in the FP64 routine.  A CTA needs n * 36 * 4
+// bytes of shared memory (n <= 1536).
+constexpr int kPotrfThreads = 256;
+constexpr int kPanelStride = 36;
+
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_size() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kPotrfThreads, 1) k_potrf32(int n, const double* __restrict__ Ain, double* __restrict__ Lall,
+                                                           int* __restrict__ info, const int* __restrict__ frameMask) {
+    const unsigned CL = cluster_size(), rank = cluster_rank();
+    const int b = blockIdx.x / CL;
+    if (frameMask && !frameMask[b]) return;  // the whole cluster leaves together
+    extern __shared__ __align__(16) float panel[];  // [n][kPanelStride]
+    __shared__ float D[NB][NB + 1];                // diagonal block
+    __shared__ float Di[NB][NB + 1];               // its inverse
+    __shared__ int bad;
+    double* L = Lall + (size_t)b * n * n;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    auto step_sync = [&]() {
+        if (CL > 1)
+            cluster_sync_all();
+        else
+            __syncthreads();
+    };
+    if (Ain != Lall) {
+        const double* A = Ain + (size_t)b * n * n;
+        for (size_t t = rank * kPotrfThreads + threadIdx.x; t < (size_t)n * n; t += (size_t)CL * kPotrfThreads) {
+            const int r = (int)(t % n), c = (int)(t / n);
+            if (r >= c) L[t] = A[t];
+        }
+    }
+    if (threadIdx.x == 0) bad = 0;
+    step_sync();
+    const int nb = n / NB;
+    for (int k = 0; k < nb; ++k) {
+        const int o = k * NB;
+        // (a) diagonal block: factor and invert (warp 0 of every CTA)
+        if (warp == 0) {
+            for (int c = 0; c < NB; ++c) D[lane][c] = lane >= c ? (float)L[(size_t)(o + lane) + (size_t)(o + c) * n] : 0.f;
+            __syncwarp();
+            for (int j = 0; j < NB; ++j) {
+                if (lane == 0) {
+                    const float d = D[j][j];
+                    if (!(d > 0.f) || !isfinite(d)) {
+                        if (!bad && rank == 0) info[b] = o + j + 1;
+                        bad = 1;
+                        D[j][j] = 1.f;
+                    } else {
+                        D[j][j] = sqrtf(d);
+                    }
+                }
+                __syncwarp();
+                if (lane > j) D[lane][j] /= D[j][j];
+                __syncwarp();
+                if (lane > j)
+                    for (int l = j + 1; l <= lane; ++l) D[lane][l] = fmaf(-D[lane][j], D[l][j], D[lane][l]);
+                __syncwarp();
+            }
+            // column `lane` of D^-1 by forward substitution
+            float x[NB];
+#pragma unroll
+            for (int r = 0; r < NB; ++r) {
+                float v = r == lane ? 1.f : 0.f;
+#pragma unroll
+                for (int q = 0; q < r; ++q) v = fmaf(-D[r][q], x[q], v);
+                x[r] = r < lane ? 0.f : v / D[r][r];
+            }
+#pragma unroll
+            for (int r = 0; r < NB; ++r) Di[r][lane] = x[r];
+        }
+        __syncthreads();
+        // (b) panel rows: L_ik = A_ik D^-T (every CTA, all rows, into shared memory)
+        for (int i = o + NB + threadIdx.x; i < n; i += kPotrfThreads) {
+            float a[NB];
+#pragma unroll
+            for (int t = 0; t < NB; ++t) a[t] = (float)L[(size_t)i + (size_t)(o + t) * n];
+            float* pr = panel + (size_t)i * kPanelStride;
+#pragma unroll 1
+            for (int j = 0; j < NB; ++j) {
+                float v = 0.f;
+#pragma unroll
+                for (int t = 0; t <= j; ++t) v = fmaf(a[t], Di[j][t], v);
+                pr[j] = v;
+            }
+        }
+        __syncthreads();
+        // (c) trailing update A_ij -= L_ik L_jk^T on the lower tiles (bi >= bj > k)
+        const int m = nb - k - 1;
+        const int tiles = m * (m + 1) / 2;
+        const int wpc = kPotrfThreads / 32;
+#pragma unroll 1
+        for (int tI = rank * wpc + warp; tI < tiles; tI += CL * wpc) {
+            int bi = 0, rem = tI;
+            while (rem > bi) {
+                rem -= bi + 1;
+                ++bi;
+            }
+            const int bj = rem;  // 0 <= bj <= bi < m
+            const int i = o + NB + bi * NB + lane, j0 = o + NB + bj * NB;
+            const int cEnd = bi != bj ? NB : lane + 1;  // diagonal tiles: the lower part only
+            float4 pr[NB / 4];
+            const float4* rowI = reinterpret_cast<const float4*>(panel + (size_t)i * kPanelStride);
+#pragma unroll
+            for (int t = 0; t < NB / 4; ++t) pr[t] = rowI[t];
+            // 8 target columns at a time: their loads are issued together
+#pragma unroll 1
+            for (int c0 = 0; c0 < NB; c0 += 8) {
+                double* rowT = L + (size_t)i + (size_t)(j0 + c0) * n;
+                float tgt[8];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) tgt[c] = c0 + c < cEnd ? (float)rowT[(size_t)c * n] : 0.f;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const float4* rowJ = reinterpret_cast<const float4*>(panel + (size_t)(j0 + c0 + c) * kPanelStride);
+                    float v = 0.f;
+#pragma unroll
+                    for (int t = 0; t < NB / 4; ++t) {
+                        const float4 q = rowJ[t];
+                        v = fmaf(pr[t].x, q.x, v);
+                        v = fmaf(pr[t].y, q.y, v);
+                        v = fmaf(pr[t].z, q.z, v);
+                        v = fmaf(pr[t].w, q.w, v);
+                    }
+                    tgt[c] -= v;
+                }
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    if (c0 + c < cEnd) rowT[(size_t)c * n] = (double)tgt[c];
+            }
+        }
+        step_sync();
+        // (d) store block column k
+        if (rank == 0 && warp == 0)
+            for (int c = 0; c < NB; ++c)
+                if (lane >= c) L[(size_t)(o + lane) + (size_t)(o + c) * n] = (double)D[lane][c];
+        for (int i = o + NB + threadIdx.x; i < n; i += kPotrfThreads)
+            if ((unsigned)((i / NB) % CL) == rank) {
+                const float* pr = panel + (size_t)i * kPanelStride;
+                for (int j = 0; j < NB; ++j) L[(size_t)i + (size_t)(o + j) * n] = (double)pr[j];
+            }
+        __syncthreads();  // the next step overwrites D, Di and the panel
+    }
+}
+
+// A(j, i) = A(i, j) for i > j: the upper triangle becomes the mirror of the
+// lower one, the part the Cholesky routines read (the tensor-core Gram's
+// diagonal tiles are symmetric only to FP32 rounding).  32 x 32 tiles through
+// shared memory; grid (n/32, n/32, batch), tiles above the diagonal exit.
+__global__ void k_mirror_lower(int n, double* __restrict__ A, const int* __restrict__ frameMask) {
+    const int bi = blockIdx.x, bj = blockIdx.y, b = blockIdx.z;
+    if (bj > bi || (frameMask && !frameMask[b])) return;
+    __shared__ double t[32][33];
+    double* M = A + (size_t)b * n * n;
+    const int r = threadIdx.x & 31, c0 = threadIdx.x >> 5;  // 256 threads: 8 columns per pass
+    for (int c = c0; c < 32; c += 8) t[r][c] = M[(size_t)(bi * 32 + r) + (size_t)(bj * 32 + c) * n];
+    __syncthreads();
+    // element (bi*32 + c, bj*32 + r) of the tile goes to (bj*32 + r, bi*32 + c)
+    for (int c = c0; c < 32; c += 8)
+        if (bi != bj || c > r) M[(size_t)(bj * 32 + r) + (size_t)(bi * 32 + c) * n] = t[c][r];
+}
+
+// r = y - A x for every active frame (A full symmetric, FP64, column-major),
+// and per-block partial sums of |r|^2 and |y|^2 (rr/yy[b][blockIdx.x]).
+// Grid (n / 128, batch), 128 threads, one row each.
+__global__ void __launch_bounds__(128) k_sym_residual(int n, const double* __restrict__ A, const double* __restrict__ x,
+                                                      const double* __restrict__ y, double* __restrict__ r,
+                                                      double* __restrict__ rr, double* __restrict__ yy,
+                                                      const int* __restrict__ frameMask) {
+    const int b = blockIdx.y;
+    if (frameMask && !frameMask[b]) return;
+    const int i = blockIdx.x * 128 + threadIdx.x;
+    const double* M = A + (size_t)b * n * n;
+    const double* xb = x + (size_t)b * n;
+    __shared__ double xs[128];
+    double acc = 0.0;
+    for (int j0 = 0; j0 < n; j0 += 128) {
+        __syncthreads();
+        xs[threadIdx.x] = xb[j0 + threadIdx.x];
+        __syncthreads();
+#pragma unroll 8
+        for (int j = 0; j < 128; ++j) acc = fma(M[(size_t)i + (size_t)(j0 + j) * n], xs[j], acc);
+    }
+    const double yi = y[(size_t)b * n + i];
+    const double ri = yi - acc;
+    r[(size_t)b * n + i] = ri;
+    __shared__ double red[2][128];
+    red[0][threadIdx.x] = ri * ri;
+    red[1][threadIdx.x] = yi * yi;
+    __syncthreads();
+    for (int w = 64; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + w];
+            red[1][threadIdx.x] += red[1][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        rr[(size_t)b * gridDim.x + blockIdx.x] = red[0][0];
+        yy[(size_t)b * gridDim.x + blockIdx.x] = red[1][0];
+    }
+}
+
+// x += d on the active frames
+__global__ void k_add_masked(int n, int batch, double* __restrict__ x, const double* __restrict__ d,
+                             const int* __restrict__ frameMask) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)n * batch; t += (size_t)gridDim.x * blockDim.x)
+        if (!frameMask || frameMask[t / n]) x[t] += d[t];
+}
+
 // L_ik = A_ik L_kk^-T for the block rows below the diagonal block k
 __global__ void k_trsm(int n, double* A, int k, const int* frameMask) {
     if (frameMask && !frameMask[blockIdx.y]) return;
@@ -737,6 +979,60 @@ int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int n
     if (bytes > 38 * 1024)
         MPF_CUDA(cudaFuncSetAttribute(k_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     k_chol_solve<<<batch * nrhs, 256, bytes, s>>>(n, L, B, nrhs, frameMask);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int dense_potrf32(int batch, int n, const double* A, double* L, int* info, cudaStream_t s, const int* frameMask) {
+    MPF_CHECK(n % NB == 0 && n >= NB && n <= 1536, MPF_EINVAL,
+              "FP32 Cholesky: n must be a multiple of %d in [32, 1536] (got %d)", NB, n);
+    // the panel plus about 8 KB of static shared memory: opt in whenever the
+    // sum may pass the 48 KB default
+    const size_t smem = (size_t)n * kPanelStride * sizeof(float);
+    MPF_CUDA(cudaFuncSetAttribute(k_potrf32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MPF_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * batch, s));
+    // large matrices in small batches: a cluster of up to 4 CTAs per matrix
+    // so that the batch spreads over the SMs
+    int dev = 0, sms = 0;
+    MPF_CUDA(cudaGetDevice(&dev));
+    MPF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int CL = 1;
+    if (n >= 512)
+        while (CL < 4 && (long)batch * CL * 2 <= sms) CL *= 2;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(batch * CL));
+    cfg.blockDim = dim3(kPotrfThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    MPF_CUDA(cudaLaunchKernelEx(&cfg, k_potrf32, n, A, L, info, frameMask));
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int dense_mirror_lower(int batch, int n, double* A, cudaStream_t s, const int* frameMask) {
+    MPF_CHECK(n % 32 == 0, MPF_EINVAL, "mirror: n must be a multiple of 32 (got %d)", n);
+    k_mirror_lower<<<dim3(n / 32, n / 32, batch), 256, 0, s>>>(n, A, frameMask);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int dense_sym_residual(int batch, int n, const double* A, const double* x, const double* y, double* r, double* rr,
+                       double* yy, cudaStream_t s, const int* frameMask) {
+    MPF_CHECK(n % 128 == 0, MPF_EINVAL, "FP64 residual: n must be a multiple of 128 (got %d)", n);
+    k_sym_residual<<<dim3(n / 128, batch), 128, 0, s>>>(n, A, x, y, r, rr, yy, frameMask);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int dense_add_masked(int batch, int n, double* x, const double* d, cudaStream_t s, const int* frameMask) {
+    k_add_masked<<<std::min(1024, (n * batch + 255) / 256), 256, 0, s>>>(n, batch, x, d, frameMask);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

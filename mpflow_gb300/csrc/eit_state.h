@@ -65,7 +65,10 @@ struct mpf_eit {
     mpf::DevBuf<float> V, J, gramWork;
     mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
     mpf::DevBuf<double> A64, y, res;
-    mpf::DevBuf<int> info, frameMask, redoMask;
+    mpf::DevBuf<int> info, frameMask, redoMask, fbMask, solveMask, upMask;
+    // FP32 factor of the Gauss-Newton system with FP64 refinement (gn_update)
+    mpf::DevBuf<double> cholL, cholX, cholR, cholY, cholRR, cholYY;
+    mpf::DevBuf<int> info32, cholMask;
     long long nnz = 0;                // used ELL slots (matrix nonzeros)
     std::vector<int> activeHost, itersHost;
     int* pinnedActive = nullptr;
@@ -82,7 +85,7 @@ struct mpf_eit {
     mpf::DevBuf<int32_t> cPairI, cPairJ, cPairPtr, cSlots;
     mpf::DevBuf<float> cAggSize;
     int cNnz = 0;
-    mpf::DevBuf<double> Ac64, rzFine, bzFine;
+    mpf::DevBuf<double> Ac64, Lc64, rzFine, bzFine;
     mpf::DevBuf<float> Lc, LinvD, Binv, rcV, rcB, ycV;
     mpf::DevBuf<int> infoC;
     // voltage (Fixed) sources: Dirichlet rows on port nodes (fixed_kernels.cu)

@@ -450,6 +450,7 @@ static int ensure_coarse(mpf_eit* m, int F) {
     if (F <= m->capFC) return MPF_OK;
     const size_t G = (size_t)F * m->Ca, nc2 = (size_t)m->ncPad * m->ncPad, cv = G * m->ncPad * m->KP;
     MPF_TRY(m->Ac64.alloc(G * nc2));
+    MPF_TRY(m->Lc64.alloc(G * nc2));
     MPF_TRY(m->Lc.alloc(G * nc2));
     MPF_TRY(m->LinvD.alloc(G * (m->ncPad / 32) * 1024));
     MPF_TRY(m->Binv.alloc(G * nc2));
@@ -461,7 +462,7 @@ static int ensure_coarse(mpf_eit* m, int F) {
     MPF_CUDA(cudaMemset(m->ycV.ptr, 0, cv * sizeof(float)));
     MPF_TRY(m->rzFine.alloc(G * m->KP));
     MPF_TRY(m->bzFine.alloc(G * m->KP));
-    MPF_TRY(m->infoC.alloc(G));
+    MPF_TRY(m->infoC.alloc(2 * G));
     m->capFC = F;
     return MPF_OK;
 }
@@ -593,10 +594,12 @@ static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
     o.check_every = 16;
     o.preconditioner = 0;
     o.solver = 0;
+    o.gn_factor = 0;
     if (in) o = *in;
     if (o.preconditioner != 1) o.preconditioner = 0;
     if (o.solver != 1) o.solver = 0;
     if (o.solver == 1) o.preconditioner = 0;  // BiCGSTAB: Jacobi only
+    if (o.gn_factor != 1) o.gn_factor = 0;
     if (o.tol <= 0.0) o.tol = 1e-6;
     if (o.max_iter <= 0) o.max_iter = 10 * n;
     if (o.max_refine <= 0) o.max_refine = 6;
@@ -671,7 +674,8 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     if (coarse) {
         CoarsePlan cp{m->nc, m->ncPad, m->cNnz, m->cPairI.ptr, m->cPairJ.ptr, m->cPairPtr.ptr, m->cSlots.ptr,
                       m->cAggSize.ptr};
-        MPF_TRY(coarse_launch_setup(P, cp, m->Ac64.ptr, m->infoC.ptr, s, m->Lc.ptr, m->LinvD.ptr, m->Binv.ptr));
+        MPF_TRY(coarse_launch_setup(P, cp, m->Ac64.ptr, m->infoC.ptr, s, m->Lc.ptr, m->LinvD.ptr, m->Binv.ptr,
+                                    m->Lc64.ptr));
     }
     MPF_TRY(phase_mark(m, MPF_PHASE_CG, s));
     int totalIters = 0, notConv = 0, refinements = 0;
@@ -845,54 +849,174 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
     return MPF_OK;
 }
 
-// J J^T + mu I (split-BF16 tensor cores) -> FP64 Cholesky -> w -> gamma += J^T w
+// FP32 factor of A64 and FP64 iterative refinement of w = A64^-1 y for the
+// frames in `act` (host, 1 = solve): on return y holds the solution of every
+// frame that converged; fb[f] = 1 marks the frames that need the FP64 factor
+// instead (FP32 breakdown, stalled or unconverged refinement).  A64's lower
+// triangle is left intact (its upper triangle becomes the mirror image).
+static int gn_solve_fp32(mpf_eit* m, int F, const std::vector<int>& act, std::vector<int>& fb, cudaStream_t s) {
+    const int n = m->rowsJ, nbk = n / 128;
+    MPF_TRY(m->cholL.alloc((size_t)F * n * n));
+    MPF_TRY(m->cholX.alloc((size_t)F * n));
+    MPF_TRY(m->cholR.alloc((size_t)F * n));
+    MPF_TRY(m->cholY.alloc((size_t)F * n));
+    MPF_TRY(m->cholRR.alloc((size_t)F * nbk));
+    MPF_TRY(m->cholYY.alloc((size_t)F * nbk));
+    MPF_TRY(m->info32.alloc((size_t)F));
+    MPF_TRY(m->cholMask.alloc((size_t)F));
+    MPF_CUDA(cudaMemcpyAsync(m->cholMask.ptr, act.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+    // the residual below reads all of A64: make it the symmetric matrix whose
+    // lower triangle the factors use
+    MPF_TRY(dense_mirror_lower(F, n, m->A64.ptr, s, m->cholMask.ptr));
+    MPF_TRY(dense_potrf32(F, n, m->A64.ptr, m->cholL.ptr, m->info32.ptr, s, m->cholMask.ptr));
+    MPF_CUDA(cudaMemcpyAsync(m->cholY.ptr, m->y.ptr, sizeof(double) * F * n, cudaMemcpyDeviceToDevice, s));
+    MPF_CUDA(cudaMemcpyAsync(m->cholR.ptr, m->y.ptr, sizeof(double) * F * n, cudaMemcpyDeviceToDevice, s));
+    MPF_CUDA(cudaMemsetAsync(m->cholX.ptr, 0, sizeof(double) * F * n, s));
+    std::vector<int> info(F), live(act);
+    MPF_CUDA(cudaMemcpyAsync(info.data(), m->info32.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    fb.assign(F, 0);
+    bool any = false;
+    for (int f = 0; f < F; ++f) {
+        if (live[f] && info[f] != 0) {
+            fb[f] = 1;
+            live[f] = 0;
+        }
+        any |= live[f] != 0;
+    }
+    if (!any) return MPF_OK;
+    MPF_CUDA(cudaMemcpyAsync(m->cholMask.ptr, live.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+    // refinement: x += L^-T L^-1 r, r = y - A x, until |r| <= 1e-14 |y| or
+    // the residual stops shrinking (FP64 rounding) below 1e-10 |y|
+    constexpr int kMaxRefine = 10;
+    constexpr double kTol = 1e-14, kFloor = 1e-10;
+    std::vector<double> rr((size_t)F * nbk), yy((size_t)F * nbk), prev(F, 1e300);
+    std::vector<int> done(F, 0);
+    for (int it = 0; it < kMaxRefine; ++it) {
+        MPF_TRY(dense_cholesky_solve_f64(F, n, m->cholL.ptr, m->cholR.ptr, 1, s, m->cholMask.ptr));
+        MPF_TRY(dense_add_masked(F, n, m->cholX.ptr, m->cholR.ptr, s, m->cholMask.ptr));
+        MPF_TRY(dense_sym_residual(F, n, m->A64.ptr, m->cholX.ptr, m->cholY.ptr, m->cholR.ptr, m->cholRR.ptr,
+                                   m->cholYY.ptr, s, m->cholMask.ptr));
+        MPF_CUDA(cudaMemcpyAsync(rr.data(), m->cholRR.ptr, sizeof(double) * rr.size(), cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaMemcpyAsync(yy.data(), m->cholYY.ptr, sizeof(double) * yy.size(), cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        bool pending = false;
+        for (int f = 0; f < F; ++f) {
+            if (!live[f] || done[f]) continue;
+            double r2 = 0.0, y2 = 0.0;
+            for (int k = 0; k < nbk; ++k) {
+                r2 += rr[(size_t)f * nbk + k];
+                y2 += yy[(size_t)f * nbk + k];
+            }
+            const double rel = y2 > 0.0 ? std::sqrt(r2 / y2) : 0.0;
+            if (!(rel <= kTol)) {
+                if (!(rel < 0.5 * prev[f])) {
+                    // no longer gaining: at the FP64 floor (done), or stalled or
+                    // non-finite above it (the FP64 factor takes over)
+                    if (!(rel <= kFloor)) fb[f] = 1;
+                    done[f] = 1;
+                } else {
+                    pending = true;
+                }
+            } else {
+                done[f] = 1;
+            }
+            prev[f] = rel;
+        }
+        if (!pending) break;
+    }
+    for (int f = 0; f < F; ++f) {
+        if (live[f] && !done[f]) fb[f] = 1;  // refinement ran out of steps
+        if (fb[f]) live[f] = 0;
+    }
+    // y = x for the frames solved here
+    for (int f = 0; f < F; ++f)
+        if (live[f])
+            MPF_CUDA(cudaMemcpyAsync(m->y.ptr + (size_t)f * n, m->cholX.ptr + (size_t)f * n, sizeof(double) * n,
+                                     cudaMemcpyDeviceToDevice, s));
+    return MPF_OK;
+}
+
+// J J^T + mu I (split-BF16 tensor cores) -> factor -> w -> gamma += J^T w
 // for the frames in frameActive (all if null; hostActive: the same on the
-// host, or null); y holds the residual on entry.  With `broken`, a frame whose
+// host, or null); y holds the residual on entry.  gnFactor 0: FP32 factor
+// with FP64 refinement, the FP64 factor for the frames where that fails;
+// 1: the FP64 factor for every frame.  With `broken`, a frame whose
 // factorisation fails also with the FP64 Gram is left unchanged and flagged
-// there; without it the failure is left in m->info for gn_check.
+// there; without it the failure is left in m->info for gn_check.  counts
+// (optional): frames solved {FP32 + refinement, FP64}.  Every device mask
+// has its own buffer and is copied in stream order.
 static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* frameActive, cudaStream_t s,
-                     const int* hostActive = nullptr, std::vector<int>* broken = nullptr) {
+                     const int* hostActive = nullptr, std::vector<int>* broken = nullptr, int gnFactor = 0,
+                     int* counts = nullptr) {
     const double mu = (double)m->ref * lambda * (double)m->ref * lambda;
     MPF_TRY(phase_mark(m, MPF_PHASE_GRAM, s));
     MPF_TRY(dense_gram_f64_shift(F, m->rowsJ, m->Epad, m->Jhi.ptr, m->Jlo.ptr, m->Epad, mu, m->A64.ptr,
                                  m->gramWork.ptr, m->gramWork.count, s, frameActive));
     MPF_TRY(phase_mark(m, MPF_PHASE_CHOLESKY, s));
+    std::vector<int> act(F);
+    for (int f = 0; f < F; ++f) act[f] = hostActive ? (hostActive[f] != 0) : 1;
+    // frames for the FP64 factor: all (gnFactor 1, or n outside the FP32
+    // kernel's range) or the FP32 path's fallbacks
+    std::vector<int> fb = act;
+    const bool fp32 = gnFactor == 0 && m->rowsJ % 128 == 0 && m->rowsJ <= 1536;
+    if (fp32) MPF_TRY(gn_solve_fp32(m, F, act, fb, s));
+    int nfb = 0;
+    for (int f = 0; f < F; ++f) nfb += fb[f];
+    if (counts) {
+        for (int f = 0; f < F; ++f) counts[0] += act[f] && !fb[f];
+        counts[1] += nfb;
+    }
     MPF_CUDA(cudaMemsetAsync(m->info.ptr, 0, sizeof(int) * F, s));
-    MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, frameActive));
-    // frames whose split-BF16 J J^T + mu I is not positive definite (mu below
-    // the Gram's ~1e-5 relative error): FP32 J and the FP64 Gram, factor again
-    std::vector<int> info(F), redo(F, 0);
-    MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
-    MPF_CUDA(cudaStreamSynchronize(s));
-    bool any = false;
-    for (int f = 0; f < F; ++f) any |= (redo[f] = info[f] != 0) != 0;
-    if (any) {
-        MPF_TRY(m->redoMask.upload(redo));
-        MPF_TRY(phase_mark(m, MPF_PHASE_JACOBIAN, s));
-        MPF_TRY(eit_jacobian(m, F, gamma, m->redoMask.ptr, true, s));
-        MPF_TRY(phase_mark(m, MPF_PHASE_GRAM, s));
-        MPF_TRY(dense_gram_f64_exact(F, m->rowsJ, m->Epad, m->J.ptr, m->Epad, mu, m->A64.ptr, m->redoMask.ptr, s));
-        MPF_TRY(phase_mark(m, MPF_PHASE_CHOLESKY, s));
-        MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, m->redoMask.ptr));
-        if (broken) {
-            MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
-            MPF_CUDA(cudaStreamSynchronize(s));
-            broken->assign(F, 0);
-            bool anyBroken = false;
-            for (int f = 0; f < F; ++f) anyBroken |= ((*broken)[f] = redo[f] && info[f] != 0) != 0;
-            if (anyBroken) {
-                std::vector<int> ok(F);
-                for (int f = 0; f < F; ++f) ok[f] = (!hostActive || hostActive[f]) && !(*broken)[f];
-                MPF_TRY(m->redoMask.upload(ok));
-                frameActive = m->redoMask.ptr;
+    if (nfb) {
+        const int* fbMask = frameActive;
+        if (fp32) {
+            MPF_TRY(m->fbMask.alloc((size_t)F));
+            MPF_CUDA(cudaMemcpyAsync(m->fbMask.ptr, fb.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+            fbMask = m->fbMask.ptr;
+        }
+        MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, fbMask));
+        // frames whose split-BF16 J J^T + mu I is not positive definite (mu below
+        // the Gram's ~1e-5 relative error): FP32 J and the FP64 Gram, factor again
+        std::vector<int> info(F), redo(F, 0);
+        MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
+        MPF_CUDA(cudaStreamSynchronize(s));
+        bool any = false;
+        for (int f = 0; f < F; ++f) any |= (redo[f] = fb[f] && info[f] != 0) != 0;
+        if (any) {
+            MPF_TRY(m->redoMask.alloc((size_t)F));
+            MPF_CUDA(cudaMemcpyAsync(m->redoMask.ptr, redo.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+            MPF_TRY(phase_mark(m, MPF_PHASE_JACOBIAN, s));
+            MPF_TRY(eit_jacobian(m, F, gamma, m->redoMask.ptr, true, s));
+            MPF_TRY(phase_mark(m, MPF_PHASE_GRAM, s));
+            MPF_TRY(dense_gram_f64_exact(F, m->rowsJ, m->Epad, m->J.ptr, m->Epad, mu, m->A64.ptr, m->redoMask.ptr, s));
+            MPF_TRY(phase_mark(m, MPF_PHASE_CHOLESKY, s));
+            MPF_TRY(dense_cholesky_f64(F, m->rowsJ, m->A64.ptr, m->info.ptr, s, m->redoMask.ptr));
+            if (broken) {
+                MPF_CUDA(cudaMemcpyAsync(info.data(), m->info.ptr, sizeof(int) * F, cudaMemcpyDeviceToHost, s));
+                MPF_CUDA(cudaStreamSynchronize(s));
+                broken->assign(F, 0);
+                for (int f = 0; f < F; ++f) (*broken)[f] = redo[f] && info[f] != 0;
             }
         }
+        // triangular solves of the frames factored in FP64 (except broken ones)
+        std::vector<int> solve64(F);
+        for (int f = 0; f < F; ++f) solve64[f] = fb[f] && !(broken && !broken->empty() && (*broken)[f]);
+        MPF_TRY(m->solveMask.alloc((size_t)F));
+        MPF_CUDA(cudaMemcpyAsync(m->solveMask.ptr, solve64.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+        MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s, m->solveMask.ptr));
     }
-    MPF_TRY(phase_mark(m, MPF_PHASE_CHOLESKY, s));
-    MPF_TRY(dense_cholesky_solve_f64(F, m->rowsJ, m->A64.ptr, m->y.ptr, 1, s, frameActive));
+    // the update, on the active frames that were not left broken
+    const int* upMask = frameActive;
+    if (broken && !broken->empty()) {
+        std::vector<int> ok(F);
+        for (int f = 0; f < F; ++f) ok[f] = act[f] && !(*broken)[f];
+        MPF_TRY(m->upMask.alloc((size_t)F));
+        MPF_CUDA(cudaMemcpyAsync(m->upMask.ptr, ok.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+        upMask = m->upMask.ptr;
+    }
     MPF_TRY(phase_mark(m, MPF_PHASE_UPDATE, s));
-    MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->Jhi.ptr, m->Jlo.ptr, m->y.ptr, frameActive, gamma,
-                                    s));
+    MPF_TRY(fem_launch_update_gamma(F, m->rowsJ, m->Epad, m->E, m->Jhi.ptr, m->Jlo.ptr, m->y.ptr, upMask, gamma, s));
     return MPF_OK;
 }
 
@@ -920,7 +1044,9 @@ int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, 
     MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
     MPF_TRY(phase_mark(m, MPF_PHASE_JACOBIAN, s));
     MPF_TRY(eit_jacobian(m, F, gamma, nullptr, false, s));
-    MPF_TRY(gn_update(m, F, gamma, lambda, nullptr, s));
+    mpf_solve_opts od;
+    fill_defaults(o, od, m->n);
+    MPF_TRY(gn_update(m, F, gamma, lambda, nullptr, s, nullptr, nullptr, od.gn_factor));
     MPF_TRY(phase_mark(m, MPF_PHASE_HOST, s));
     if (residual) MPF_CUDA(cudaMemcpyAsync(residual, m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
     MPF_TRY(gn_check(m, F, s));
@@ -945,6 +1071,7 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
     std::vector<int> mask(F, 1), iters(F, 0);
     std::vector<double> res(F, 0.0);
     int cgTotal = 0, gnIters = 0;
+    int solves[2] = {0, 0};  // frame updates solved {FP32 factor + refinement, FP64 factor}
     int warm = o.warm_start, checkStart = fallback != nullptr;
     if (accepted)
         for (int f = 0; f < F; ++f) accepted[f] = 1;
@@ -1004,7 +1131,7 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         MPF_TRY(m->gammaPrev.alloc((size_t)F * m->E));
         MPF_TRY(m->badFrame.alloc((size_t)F));
         MPF_CUDA(cudaMemcpyAsync(m->gammaPrev.ptr, gamma, sizeof(float) * F * m->E, cudaMemcpyDeviceToDevice, s));
-        MPF_TRY(gn_update(m, F, gamma, lambda, m->frameMask.ptr, s, mask.data(), &broken));
+        MPF_TRY(gn_update(m, F, gamma, lambda, m->frameMask.ptr, s, mask.data(), &broken, o.gn_factor, solves));
         for (int f = 0; f < F && !broken.empty(); ++f)
             if (broken[f]) mask[f] = 0;
         // an update that sends a frame's parameters out of the forward
@@ -1034,6 +1161,8 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
         stats->gn_iterations = gnIters;
         stats->cg_iterations = cgTotal;
         stats->frames_converged = converged;
+        stats->solves_fp32 = solves[0];
+        stats->solves_fp64 = solves[1];
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     return MPF_OK;
@@ -1172,6 +1301,12 @@ int gn_solve_learned(mpf_eit* m, mpf_mlp* net, int F, float* gamma, const float*
     MPF_TRY(mlp_forward(net, F, m->learnX.ptr, gamma, m->E, s));  // synchronises
     MPF_TRY(phase_mark(m, MPF_PHASE_PRIOR, s));
     if (m->priorReady) MPF_TRY(learned_prior_apply(m, F, m->learnX.ptr, gamma, m->E, 1, s));
+    // a prediction outside the forward model's range (non-finite, |gamma| >
+    // 100 dB logarithmic, gamma <= 0 linear) is replaced by the homogeneous
+    // start, which the acceptance check below then rejects
+    MPF_TRY(m->badFrame.alloc((size_t)F));
+    MPF_TRY(fem_launch_gamma_check(F, m->E, gamma, nullptr, m->logarithmic, m->badFrame.ptr, s));
+    MPF_TRY(fem_launch_fill_frames(F, m->E, m->badFrame.ptr, homogeneous_gamma(m), gamma, s));
     MPF_TRY(gn_loop(m, F, gamma, vMeas, lambda, target, maxIters, o, res0.data(), homogeneous_gamma(m), accepted,
                     itersOut, resOut, stats, s));
     if (stats) stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -160,9 +160,11 @@ struct CoarsePlan {
     const int32_t* meshPairPtr;
     const int32_t* meshNc;
 };
-// Lc [G][ncPad][ncPad], LinvD [G][ncPad/32][1024]: FP32 factor scratch; Binv: the inverse (P.Binv)
+// Lc [G][ncPad][ncPad], LinvD [G][ncPad/32][1024]: FP32 factor scratch; Binv: the inverse (P.Binv);
+// L64 [G][ncPad][ncPad]: the factor taken in FP32 arithmetic (FP64 factor in
+// place of Ac64 where it breaks down; null: FP64 only); info: 2 * G ints
 int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,
-                        float* Lc, float* LinvD, float* Binv);
+                        float* Lc, float* LinvD, float* Binv, double* L64);
 // `count`: false while recording a CUDA graph (replays are counted by the caller)
 int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count = true);
 bool coarse_supported(int KP, int ncPad);
@@ -301,6 +303,20 @@ int dense_add_shift(int batch, int n, double* A, double shift, cudaStream_t s);
 int dense_cholesky_f64(int batch, int n, double* A, int* info, cudaStream_t s, const int* frameMask = nullptr);
 int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int nrhs, cudaStream_t s,
                              const int* frameMask = nullptr);
+// Cholesky in FP32 arithmetic of FP64 column-major matrices (n % 32 == 0,
+// n <= 1536), a cluster of up to 4 CTAs per matrix; L may equal A (in
+// place); the factor is stored in FP64; info[b] = first non-positive pivot
+// (1-based) or 0
+int dense_potrf32(int batch, int n, const double* A, double* L, int* info, cudaStream_t s,
+                  const int* frameMask = nullptr);
+// upper triangle := mirror of the lower one (the part the factors read)
+int dense_mirror_lower(int batch, int n, double* A, cudaStream_t s, const int* frameMask = nullptr);
+// r = y - A x (FP64, A full symmetric) with per-block partial |r|^2, |y|^2
+// (n / 128 per frame, in rr / yy)
+int dense_sym_residual(int batch, int n, const double* A, const double* x, const double* y, double* r, double* rr,
+                       double* yy, cudaStream_t s, const int* frameMask = nullptr);
+// x += d on the masked frames ([batch][n])
+int dense_add_masked(int batch, int n, double* x, const double* d, cudaStream_t s, const int* frameMask = nullptr);
 
 // matrix_ops.cu: C = alpha op(A) op(B) + beta C, column-major FP32
 int matrix_multiply_scaled(int transA, int transB, int m, int n, int k, float alpha, const float* A, int lda,

@@ -141,8 +141,12 @@ class SolveOptions:
     # 2/"homogeneous" fields of the homogeneous distribution
     WARM_STARTS = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, "previous": 1, "homogeneous": 2}
 
+    # gn_factor: factor of J J^T + mu I in the Gauss-Newton update
+    GN_FACTORS = {"fp32-refined": 0, "fp64": 1}
+
     def __init__(self, tol=1e-6, max_iter=0, refine_tol=0.0, max_refine=6, warm_start=False,
-                 check_every=16, preconditioner: str = "jacobi", solver: str = "cg"):
+                 check_every=16, preconditioner: str = "jacobi", solver: str = "cg",
+                 gn_factor: str = "fp32-refined"):
         self.tol, self.max_iter, self.refine_tol = tol, max_iter, refine_tol
         self.max_refine, self.warm_start, self.check_every = max_refine, warm_start, check_every
         if warm_start not in self.WARM_STARTS:
@@ -153,12 +157,16 @@ class SolveOptions:
         if solver not in self.SOLVERS:
             raise ValueError(f"solver must be one of {sorted(self.SOLVERS)}")
         self.solver = solver
+        if gn_factor not in self.GN_FACTORS:
+            raise ValueError(f"gn_factor must be one of {sorted(self.GN_FACTORS)}")
+        self.gn_factor = gn_factor
 
     def c(self) -> _ffi.SolveOpts:
         """The options as the C ABI's mpf_solve_opts."""
         return _ffi.SolveOpts(float(self.tol), int(self.max_iter), float(self.refine_tol),
                               int(self.max_refine), self.WARM_STARTS[self.warm_start], int(self.check_every),
-                              self.PRECONDITIONERS[self.preconditioner], self.SOLVERS[self.solver])
+                              self.PRECONDITIONERS[self.preconditioner], self.SOLVERS[self.solver],
+                              self.GN_FACTORS[self.gn_factor])
 
 
 def _stream():

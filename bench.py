@@ -77,6 +77,8 @@ def parse_args():
                    help="CG preconditioner of every GPU solve (jacobi = the reference's)")
     p.add_argument("--gn-warm-start", choices=["homogeneous", "cold"], default="homogeneous",
                    help="initial fields of each GN solve's first forward solve (and of the training-pair solves)")
+    p.add_argument("--gn-factor", choices=["fp32-refined", "fp64"], default="fp64",
+                   help="factor of J J^T + mu I in every Gauss-Newton update (mpf_solve_opts.gn_factor)")
     p.add_argument("--cpu-threads", type=int, default=0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cg-shapes", type=str, default="",
@@ -394,7 +396,8 @@ def run_gb300(a):
     # GN paths: the first forward solve of every frame starts from the fields of
     # the homogeneous distribution (solved once per model)
     gn_opts = mp.SolveOptions(tol=a.tol, max_iter=6000, preconditioner=a.preconditioner,
-                              warm_start="homogeneous" if a.gn_warm_start == "homogeneous" else 0)
+                              warm_start="homogeneous" if a.gn_warm_start == "homogeneous" else 0,
+                              gn_factor=a.gn_factor)
     lam = a.lam_rel * float(J0.norm() / np.sqrt(J0.shape[1]))
     del J0
 
@@ -582,6 +585,7 @@ def run_gb300(a):
                    "correction" if use_prior else "learned warm start (network alone)")
                   + "; batched GN from it (plain GN restart per frame when the start does not lower the residual)",
         "cg_preconditioner": a.preconditioner,
+        "gn_factor": a.gn_factor,
         "gn_first_solve_start": a.gn_warm_start,
         "gn_updates_mean": learned["gn_updates_mean"],
         "frames_converged_fraction": learned["frames_converged_fraction"],

@@ -195,13 +195,16 @@ typedef struct mpf_solve_opts {
      *    Jacobi preconditioner (preconditioner = 1 is ignored). */
     int32_t solver;
     /* Factor of J J^T + mu I in the Gauss-Newton update (mpf_gn_step,
-     * mpf_gn_solve, mpf_gn_solve_learned):
-     * 0: Cholesky in FP32 arithmetic (a cluster of CTAs per frame) with FP64
-     *    iterative refinement against the FP64 matrix; a frame whose FP32
-     *    factor breaks down or whose refinement stalls falls back to option 1
-     *    (default);
-     * 1: FP64 Cholesky only (the solve of src/solver/inverse.cpp:213-238 is a
-     *    dense CG on J^T J; both give the regularised update). */
+     * mpf_gn_solve, mpf_gn_solve_learned); the solve of
+     * src/solver/inverse.cpp:213-238 is a dense CG on J^T J, both give the
+     * regularised update:
+     * 0: FP64 Cholesky (default);
+     * 1: Cholesky in FP32 arithmetic (a cluster of up to 4 CTAs per frame,
+     *    3.9 ms for 32 frames of 1024 against 12.3 ms in FP64) with FP64
+     *    iterative refinement to 1e-10 against the FP64 matrix; a frame whose
+     *    FP32 factor breaks down or whose refinement stalls falls back to
+     *    option 0.  The refinement's triangular solves (2.2 ms per step for 32
+     *    frames) make it slower than option 0 on the 1024-row system. */
     int32_t gn_factor;
 } mpf_solve_opts;
 

@@ -593,7 +593,7 @@ __global__ void k_syrk(int n, double* A, int k, const int* frameMask) {
 // k's columns take warp-reduced dots with the solved rows below).  The
 // 32 x 32 diagonal block is staged in shared memory and solved by one warp
 // with shuffles.
-__global__ void __launch_bounds__(256) k_chol_solve(int n, const double* __restrict__ Lall, double* __restrict__ Ball,
+__global__ void __launch_bounds__(1024) k_chol_solve(int n, const double* __restrict__ Lall, double* __restrict__ Ball,
                                                     int nrhs, const int* __restrict__ frameMask) {
     if (frameMask && !frameMask[blockIdx.x / nrhs]) return;
     extern __shared__ double x[];
@@ -978,7 +978,10 @@ int dense_cholesky_solve_f64(int batch, int n, const double* L, double* B, int n
               "cholesky solve: n must be a multiple of %d and at most 24576 (%d)", NB, n);
     if (bytes > 38 * 1024)
         MPF_CUDA(cudaFuncSetAttribute(k_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    k_chol_solve<<<batch * nrhs, 256, bytes, s>>>(n, L, B, nrhs, frameMask);
+    // one thread per row (up to 1024): the row updates below each diagonal
+    // block are latency-bound loads of L, so more threads keep more in flight
+    const int threads = std::min(1024, std::max(256, n));
+    k_chol_solve<<<batch * nrhs, threads, bytes, s>>>(n, L, B, nrhs, frameMask);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

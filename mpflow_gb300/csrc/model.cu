@@ -599,7 +599,7 @@ static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
     if (o.preconditioner != 1) o.preconditioner = 0;
     if (o.solver != 1) o.solver = 0;
     if (o.solver == 1) o.preconditioner = 0;  // BiCGSTAB: Jacobi only
-    if (o.gn_factor != 1) o.gn_factor = 0;
+    if (o.gn_factor != 1) o.gn_factor = 0;  // 0: FP64 factor, 1: FP32 factor + FP64 refinement
     if (o.tol <= 0.0) o.tol = 1e-6;
     if (o.max_iter <= 0) o.max_iter = 10 * n;
     if (o.max_refine <= 0) o.max_refine = 6;
@@ -886,10 +886,12 @@ static int gn_solve_fp32(mpf_eit* m, int F, const std::vector<int>& act, std::ve
     }
     if (!any) return MPF_OK;
     MPF_CUDA(cudaMemcpyAsync(m->cholMask.ptr, live.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
-    // refinement: x += L^-T L^-1 r, r = y - A x, until |r| <= 1e-14 |y| or
-    // the residual stops shrinking (FP64 rounding) below 1e-10 |y|
-    constexpr int kMaxRefine = 10;
-    constexpr double kTol = 1e-14, kFloor = 1e-10;
+    // refinement: x += L^-T L^-1 r, r = y - A x, until |r| <= 1e-10 |y| (the
+    // split-BF16 Gram itself is accurate to ~1e-5) or the residual stops
+    // shrinking; the first check comes after two steps (each step gains
+    // about cond(A) * 6e-8, 1e-2 at the bench's conditioning)
+    constexpr int kMaxRefine = 8;
+    constexpr double kTol = 1e-10, kFloor = 1e-10;
     std::vector<double> rr((size_t)F * nbk), yy((size_t)F * nbk), prev(F, 1e300);
     std::vector<int> done(F, 0);
     for (int it = 0; it < kMaxRefine; ++it) {
@@ -897,6 +899,7 @@ static int gn_solve_fp32(mpf_eit* m, int F, const std::vector<int>& act, std::ve
         MPF_TRY(dense_add_masked(F, n, m->cholX.ptr, m->cholR.ptr, s, m->cholMask.ptr));
         MPF_TRY(dense_sym_residual(F, n, m->A64.ptr, m->cholX.ptr, m->cholY.ptr, m->cholR.ptr, m->cholRR.ptr,
                                    m->cholYY.ptr, s, m->cholMask.ptr));
+        if (it == 0) continue;
         MPF_CUDA(cudaMemcpyAsync(rr.data(), m->cholRR.ptr, sizeof(double) * rr.size(), cudaMemcpyDeviceToHost, s));
         MPF_CUDA(cudaMemcpyAsync(yy.data(), m->cholYY.ptr, sizeof(double) * yy.size(), cudaMemcpyDeviceToHost, s));
         MPF_CUDA(cudaStreamSynchronize(s));
@@ -939,9 +942,9 @@ static int gn_solve_fp32(mpf_eit* m, int F, const std::vector<int>& act, std::ve
 
 // J J^T + mu I (split-BF16 tensor cores) -> factor -> w -> gamma += J^T w
 // for the frames in frameActive (all if null; hostActive: the same on the
-// host, or null); y holds the residual on entry.  gnFactor 0: FP32 factor
-// with FP64 refinement, the FP64 factor for the frames where that fails;
-// 1: the FP64 factor for every frame.  With `broken`, a frame whose
+// host, or null); y holds the residual on entry.  gnFactor 0: the FP64
+// factor for every frame; 1: FP32 factor with FP64 refinement, the FP64
+// factor for the frames where that fails.  With `broken`, a frame whose
 // factorisation fails also with the FP64 Gram is left unchanged and flagged
 // there; without it the failure is left in m->info for gn_check.  counts
 // (optional): frames solved {FP32 + refinement, FP64}.  Every device mask
@@ -956,10 +959,10 @@ static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* 
     MPF_TRY(phase_mark(m, MPF_PHASE_CHOLESKY, s));
     std::vector<int> act(F);
     for (int f = 0; f < F; ++f) act[f] = hostActive ? (hostActive[f] != 0) : 1;
-    // frames for the FP64 factor: all (gnFactor 1, or n outside the FP32
+    // frames for the FP64 factor: all (gnFactor 0, or n outside the FP32
     // kernel's range) or the FP32 path's fallbacks
     std::vector<int> fb = act;
-    const bool fp32 = gnFactor == 0 && m->rowsJ % 128 == 0 && m->rowsJ <= 1536;
+    const bool fp32 = gnFactor == 1 && m->rowsJ % 128 == 0 && m->rowsJ <= 1536;
     if (fp32) MPF_TRY(gn_solve_fp32(m, F, act, fb, s));
     int nfb = 0;
     for (int f = 0; f < F; ++f) nfb += fb[f];

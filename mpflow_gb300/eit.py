@@ -142,11 +142,11 @@ class SolveOptions:
     WARM_STARTS = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, "previous": 1, "homogeneous": 2}
 
     # gn_factor: factor of J J^T + mu I in the Gauss-Newton update
-    GN_FACTORS = {"fp32-refined": 0, "fp64": 1}
+    GN_FACTORS = {"fp64": 0, "fp32-refined": 1}
 
     def __init__(self, tol=1e-6, max_iter=0, refine_tol=0.0, max_refine=6, warm_start=False,
                  check_every=16, preconditioner: str = "jacobi", solver: str = "cg",
-                 gn_factor: str = "fp32-refined"):
+                 gn_factor: str = "fp64"):
         self.tol, self.max_iter, self.refine_tol = tol, max_iter, refine_tol
         self.max_refine, self.warm_start, self.check_every = max_refine, warm_start, check_every
         if warm_start not in self.WARM_STARTS:

@@ -84,9 +84,14 @@ def parse_args():
     p.add_argument("--cg-shapes", type=str, default="",
                    help="fix the CG launch shapes 'spmm,update,direction' (codes of mpf_eit_cg_variants) "
                         "instead of autotuning")
-    p.add_argument("--train-pairs", type=int, default=4096,
+    p.add_argument("--train-pairs", type=int, default=16384,
                    help="training pairs of the learned warm start, generated by the forward solver")
     p.add_argument("--epochs", type=int, default=80)
+    p.add_argument("--train-tol", type=float, default=1e-4,
+                   help="CG tolerance of the training-pair and label solves (their inputs carry 60 dB noise)")
+    p.add_argument("--save-network", type=str, default="", help="write the trained network to this checkpoint")
+    p.add_argument("--load-network", type=str, default="",
+                   help="start from this checkpoint (MLP.save) instead of training a network")
     p.add_argument("--hidden", type=int, default=2048, help="hidden width of the warm-start network")
     p.add_argument("--learned-prior", choices=["on", "off"], default="on",
                    help="on: the network learns the correction to the linear one-step GN prior "
@@ -402,9 +407,14 @@ def run_gb300(a):
     del J0
 
     # learned warm start: pairs from the forward solver, training on the GPU (untimed, reported)
+    train_opts = mp.SolveOptions(tol=a.train_tol, max_iter=6000, preconditioner=a.preconditioner,
+                                 warm_start="homogeneous" if a.gn_warm_start == "homogeneous" else 0,
+                                 gn_factor=a.gn_factor)
+    if a.load_network:
+        a.train_pairs = 0
     t0 = time.perf_counter()
-    gtrain = inclusion_frames(cent, a.train_pairs, np.random.default_rng(5 + 7919 * rank))
-    Vtr, gtr = generate_pairs(model, gtrain, batch=64, options=gn_opts)
+    gtrain = inclusion_frames(cent, max(a.train_pairs, 64), np.random.default_rng(5 + 7919 * rank))
+    Vtr, gtr = generate_pairs(model, gtrain, batch=128, options=train_opts)
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     L = Vtr.shape[1] * Vtr.shape[2]
@@ -415,16 +425,22 @@ def run_gb300(a):
         model.learned_prior(lam)
         prior_s = time.perf_counter() - t0
     label_s, label_conv = None, None
-    if use_prior and a.labels == "gn":
+    if use_prior and a.labels == "gn" and not a.load_network:
         t0 = time.perf_counter()
-        gtr, label_conv = gn_labels(model, Vtr, lam, target=a.target, max_iters=4, options=gn_opts)
+        gtr, label_conv = gn_labels(model, Vtr, lam, target=a.target, max_iters=4, batch=128, options=train_opts)
         torch.cuda.synchronize()
         label_s = time.perf_counter() - t0
-    net = mp.MLP(L, a.hidden, a.hidden, round_up(E, 128), seed=17 + rank)
-    losses, train_s = train_warm_start(model, net, Vtr, gtr, epochs=a.epochs, batch=256, lr=1e-3,
-                                       snr_db=60.0, seed=rank, prior=use_prior)
+    if a.load_network:
+        net = mp.MLP.load(a.load_network, device=local)
+        losses, train_s = [float("nan")], float("nan")
+    else:
+        net = mp.MLP(L, a.hidden, a.hidden, round_up(E, 128), seed=17 + rank)
+        losses, train_s = train_warm_start(model, net, Vtr, gtr, epochs=a.epochs, batch=256, lr=1e-3,
+                                           snr_db=60.0, seed=rank, prior=use_prior)
+    if a.save_network and rank == 0:
+        net.save(a.save_network)
     net0 = zero_network(L, round_up(E, 128)) if use_prior else None
-    train_steps = a.epochs * max(1, a.train_pairs // 256)
+    train_steps = a.epochs * max(1, a.train_pairs // 256) if not a.load_network else 0
     del Vtr, gtr
 
     def barrier():
@@ -594,7 +610,8 @@ def run_gb300(a):
                     "train_pairs": a.train_pairs, "pair_generation_s": gen_s, "epochs": a.epochs,
                     "train_s": train_s, "train_steps": train_steps, "loss_first": losses[0],
                     "loss_last": losses[-1], "network": f"{L}-{a.hidden}-{a.hidden}-{round_up(E, 128)} GELU",
-                    "train_tflops": mlp_flops / train_s / 1e12,
+                    "train_tflops": (mlp_flops / train_s / 1e12) if train_steps else None,
+                    "train_cg_tol": a.train_tol, "loaded_network": a.load_network or None,
                     "labels": (("GN from the prior to the target (<= 4 updates; the prior where it does not "
                                 "converge)") if label_s is not None else "generating conductivity"),
                     "label_s": label_s, "label_converged_fraction": label_conv,

@@ -102,6 +102,46 @@ class MLP:
         """Flat FP32 gradients of the last backward, laid out as parameters()."""
         return self._params(2)
 
+    # checkpoint file: 8-byte magic, int64 inputs, hidden1, hidden2, outputs,
+    # parameter count, then the FP32 master parameters (little-endian, the
+    # layout of parameters()); the Adam state is not kept
+    MAGIC = b"MPFMLP01"
+
+    def save(self, path: str) -> None:
+        """Write the trained parameters to a binary checkpoint."""
+        flat = self.parameters().detach().cpu().numpy().astype("<f4")
+        head = np.array([self.inputs, self.hidden1, self.hidden2, self.outputs, self.param_count], dtype="<i8")
+        with open(path, "wb") as fh:
+            fh.write(self.MAGIC)
+            fh.write(head.tobytes())
+            fh.write(flat.tobytes())
+
+    @staticmethod
+    def read_checkpoint(path: str):
+        """(dims (inputs, hidden1, hidden2, outputs), FP32 parameters) of a
+        checkpoint written by save(); ValueError for a file of another kind
+        or of the wrong length."""
+        with open(path, "rb") as fh:
+            data = fh.read()
+        if len(data) < 48 or data[:8] != MLP.MAGIC:
+            raise ValueError(f"{path}: not a network checkpoint")
+        head = np.frombuffer(data[8:48], dtype="<i8")
+        count = int(head[4])
+        if len(data) != 48 + 4 * count:
+            raise ValueError(f"{path}: {len(data)} bytes, expected {48 + 4 * count} for {count} parameters")
+        return tuple(int(v) for v in head[:4]), np.frombuffer(data[48:], dtype="<f4")
+
+    @classmethod
+    def load(cls, path: str, device: int = 0) -> "MLP":
+        """A network with the dimensions and parameters of a checkpoint."""
+        import torch
+        dims, flat = cls.read_checkpoint(path)
+        net = cls(*dims, seed=0, device=device)
+        if flat.size != net.param_count:
+            raise ValueError(f"{path}: {flat.size} parameters, the network has {net.param_count}")
+        net.set_parameters(torch.tensor(flat, device=f"cuda:{device}"))
+        return net
+
     def unpack(self, flat):
         """Split a flat parameter (or gradient) vector into (W1, b1, W2, b2, W3, b3) numpy arrays."""
         f = flat.detach().cpu().numpy() if hasattr(flat, "detach") else np.asarray(flat)

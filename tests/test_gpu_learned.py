@@ -148,14 +148,16 @@ def test_learned_prior_is_the_first_gauss_newton_update():
 def test_learned_prior_and_network_save_gauss_newton_updates():
     """With the linear prior, the learned start (prior + a correction trained
     on where Gauss-Newton from the prior converges) needs fewer updates than
-    the homogeneous start, and the prior alone (zero network) is reported
-    beside it."""
+    the homogeneous start and than the prior alone (zero network) on 64
+    held-out frames.  The training set size decides it: at 20 rings the
+    network trained on 2048 pairs needed more updates than the prior alone
+    (1.03 against 0.89), on 8192 pairs fewer (0.72)."""
     from mpflow_gb300.learned import (generate_pairs, gn_labels, inclusion_frames, round_up, train_warm_start,
                                       zero_network)
-    mp, torch, model, mesh, cent, E, Vte, lam = _prior_setup(frames=32)
+    mp, torch, model, mesh, cent, E, Vte, lam = _prior_setup(frames=64)
     opts = mp.SolveOptions(tol=1e-6, max_iter=4000)
     model.learned_prior(lam)
-    Vtr, gtr = generate_pairs(model, inclusion_frames(cent, 2048, np.random.default_rng(11)), batch=128,
+    Vtr, gtr = generate_pairs(model, inclusion_frames(cent, 16384, np.random.default_rng(11)), batch=128,
                               options=opts)
     L = Vtr.shape[1] * Vtr.shape[2]
     labels, conv = gn_labels(model, Vtr, lam, target=1e-3, options=opts)
@@ -164,7 +166,8 @@ def test_learned_prior_and_network_save_gauss_newton_updates():
     losses, _ = train_warm_start(model, net, Vtr, labels, epochs=40, batch=256, lr=1e-3, snr_db=60.0, prior=True)
     assert losses[-1] < losses[0], losses
     target = 1e-3
-    g0 = torch.zeros((32, E), device="cuda")
+    F = Vte.shape[0]
+    g0 = torch.zeros((F, E), device="cuda")
     it_plain, _, st_plain = model.gn_solve(g0, Vte, lam, target=target, max_iters=15, options=opts)
     _, it_prior, _, acc_p, st_prior = model.gn_solve_learned(zero_network(L, round_up(E, 128)), Vte, lam,
                                                              target=target, max_iters=15, options=opts)
@@ -172,8 +175,25 @@ def test_learned_prior_and_network_save_gauss_newton_updates():
                                                            options=opts)
     print(f"GN updates: plain {it_plain.mean():.3f}, prior only {it_prior.mean():.3f} "
           f"(direct {np.mean(it_prior == 0):.2f}), prior + network {it_learn.mean():.3f} "
-          f"(direct {np.mean(it_learn == 0):.2f}, accepted {acc.sum()}/32); loss {losses[0]:.3g} -> {losses[-1]:.3g}")
-    assert st_plain.frames_converged == 32 and st_prior.frames_converged == 32 and st_learn.frames_converged == 32
-    assert acc_p.sum() >= 24 and acc.sum() >= 24
+          f"(direct {np.mean(it_learn == 0):.2f}, accepted {acc.sum()}/{F}); loss {losses[0]:.3g} -> {losses[-1]:.3g}")
+    assert st_plain.frames_converged == F and st_prior.frames_converged == F and st_learn.frames_converged == F
+    assert acc_p.sum() >= 0.75 * F and acc.sum() >= 0.75 * F
     assert it_prior.mean() < it_plain.mean()
-    assert it_learn.mean() < it_plain.mean()
+    # what the trained network gains over the method without it
+    assert it_learn.mean() < it_prior.mean(), (it_learn.mean(), it_prior.mean())
+
+
+def test_network_checkpoint_round_trip(tmp_path):
+    """MLP.save / MLP.load keep the parameters bit for bit, so a trained
+    warm start can be reused without training again."""
+    import mpflow_gb300 as mp
+    import torch
+    net = mp.MLP(256, 128, 128, 384, seed=3)
+    x = torch.randn((128, 256), device="cuda")
+    y0 = net.forward(x)
+    path = str(tmp_path / "net.mpf")
+    net.save(path)
+    back = mp.MLP.load(path)
+    assert (back.inputs, back.hidden1, back.hidden2, back.outputs) == (256, 128, 128, 384)
+    assert torch.equal(back.parameters(), net.parameters())
+    assert torch.equal(back.forward(x), y0)

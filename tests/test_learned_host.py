@@ -80,3 +80,24 @@ def test_inclusion_frames_family():
     # background 0 dB, inclusions within +-10 dB (contrast 0.1 .. 10), every frame has one
     assert np.all(np.abs(g) <= 10.0 + 1e-5)
     assert np.all((g != 0).sum(axis=1) > 0)
+
+
+def test_checkpoint_reader_rejects_foreign_and_truncated_files(tmp_path):
+    """The network checkpoint reader checks the magic and the length before
+    any parameter reaches a device."""
+    import numpy as np
+    import pytest
+    from mpflow_gb300.learned import MLP
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(b"not a checkpoint at all, just bytes........")
+    with pytest.raises(ValueError):
+        MLP.read_checkpoint(str(bad))
+    head = np.array([4, 128, 128, 8, 10], dtype="<i8").tobytes()
+    good = tmp_path / "good.bin"
+    good.write_bytes(MLP.MAGIC + head + np.arange(10, dtype="<f4").tobytes())
+    dims, flat = MLP.read_checkpoint(str(good))
+    assert dims == (4, 128, 128, 8) and np.array_equal(flat, np.arange(10, dtype=np.float32))
+    short = tmp_path / "short.bin"
+    short.write_bytes(MLP.MAGIC + head + np.arange(9, dtype="<f4").tobytes())
+    with pytest.raises(ValueError):
+        MLP.read_checkpoint(str(short))

@@ -151,6 +151,19 @@ typedef struct mpf_eit_desc {
      * 1: exact derivative of the 2.5D voltages (adds alpha_c * mass, weight beta_c).
      * Identical for a single harmonic. */
     int32_t jacobian_mode;
+    /* Electrode model.  0: the reference's gap model -- a port is a set of
+     * boundary edges, its current is spread as the integral of the basis
+     * functions over the port divided by the port length and its voltage is
+     * the mean potential over it (src/fem/equation.cpp:183-215,
+     * src/models/eit.cpp:85-94).  z > 0: the complete electrode model with
+     * contact impedance z on every port (Somersalo, Cheney and Isaacson,
+     * SIAM J. Appl. Math. 52 (1992) 1023-1040): one voltage unknown per
+     * electrode, the boundary term (1/z) int_e (u - U_l) v ds in every
+     * harmonic, the current injected into the electrode unknowns and the
+     * voltages read from them.  Current (open) sources, real parameters and
+     * single models only.  The two models are different physics and are
+     * never compared with each other. */
+    double contact_impedance;
 } mpf_eit_desc;
 
 /* Sizes a caller needs to shape its buffers. */

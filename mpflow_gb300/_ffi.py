@@ -39,6 +39,7 @@ class EitDesc(ctypes.Structure):
         ("reference_value", ctypes.c_double), ("logarithmic", ctypes.c_int32),
         ("components", ctypes.c_int32), ("height", ctypes.c_double), ("port_height", ctypes.c_double),
         ("device", ctypes.c_int32), ("jacobian_mode", ctypes.c_int32),
+        ("contact_impedance", ctypes.c_double),
     ]
 
 

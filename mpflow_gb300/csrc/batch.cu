@@ -173,6 +173,7 @@ int batch_create(mpf_eit* const* models, int count, mpf_batch** out) {
         MPF_CHECK(m, MPF_EINVAL, "mpf_batch_create: model %d == nullptr", i);
         MPF_CHECK(m->device == b->device, MPF_EINVAL, "mpf_batch_create: model %d is on another device", i);
         MPF_CHECK(!m->fixed, MPF_ENOTSUP, "mpf_batch_create: model %d has voltage (fixed) sources", i);
+        MPF_CHECK(!m->cem, MPF_ENOTSUP, "mpf_batch_create: model %d uses the complete electrode model", i);
         MPF_CHECK(m->Ca == b->Ca && m->anyDcFree == b->anyDcFree, MPF_EINVAL,
                   "mpf_batch_create: model %d has another harmonic set (components, height)", i);
         for (int c = 0; c < b->Ca; ++c)

@@ -10,7 +10,11 @@
 #include "model.h"
 
 struct mpf_eit {
-    // sizes
+    // sizes (n: rows of the system -- the mesh nodes, plus one electrode
+    // voltage per port in the complete electrode model; nNodes: mesh nodes)
+    int nNodes = 0;
+    int cem = 0;
+    double contactZ = 0.0;
     int n = 0, E = 0, dataRows = 0, npad = 0, nblk = 0, W = 0, levels = 0;
     int L = 0, Md = 0, Mm = 0, MdPad = 0, MmPad = 0, rowsJ = 0, Epad = 0;
     int K = 0, KP = 0, C = 0, Ca = 0;

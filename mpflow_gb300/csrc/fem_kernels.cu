@@ -39,12 +39,15 @@ __global__ void k_assemble(int W, int npad, int E, const int32_t* __restrict__ c
         double ds = 0.0, dr = 0.0;
         for (int c = c0; c < c1; ++c) {
             const int code = __ldg(&contrib[c]);
-            const float g = __ldg(&gf[code / 9]);
-            const float pg = mat_param(ref, g, logarithmic);
+            // elements past E are contact elements of the complete electrode
+            // model: parameter-free (weight 1)
+            const int el = code / 9;
+            const float g = el < E ? __ldg(&gf[el]) : 0.f;
+            const float pg = el < E ? mat_param(ref, g, logarithmic) : 1.f;
             vs = fmaf(__ldg(&Kf[code]), pg, vs);
             vr = fmaf(__ldg(&Mf[code]), pg, vr);
             if (S64) {
-                const double pg64 = mat_param64((double)ref, (double)g, logarithmic);
+                const double pg64 = el < E ? mat_param64((double)ref, (double)g, logarithmic) : 1.0;
                 ds = fma(Kd[code], pg64, ds);
                 dr = fma(Md[code], pg64, dr);
             }

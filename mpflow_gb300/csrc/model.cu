@@ -88,12 +88,20 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
               "mpf_eit_create: unknown source type %d", d->source_type);
     MPF_CHECK(!(d->source_type == MPF_SOURCE_FIXED && d->jacobian_mode == 1), MPF_ENOTSUP,
               "mpf_eit_create: the exact 2.5D Jacobian is implemented for current (open) sources only");
+    MPF_CHECK(d->contact_impedance >= 0.0 && std::isfinite(d->contact_impedance), MPF_EINVAL,
+              "mpf_eit_create: contact_impedance must be >= 0 (0: gap model)");
+    MPF_CHECK(!(d->contact_impedance > 0.0 && d->source_type == MPF_SOURCE_FIXED), MPF_ENOTSUP,
+              "mpf_eit_create: the complete electrode model is implemented for current (open) sources only");
     auto m = std::make_unique<mpf_eit>();
     m->device = d->device;
     MPF_TRY(check_device(m.get()));
-    m->n = d->n_nodes;
+    m->nNodes = d->n_nodes;
+    m->cem = d->contact_impedance > 0.0 ? 1 : 0;
+    m->contactZ = d->contact_impedance;
     m->E = d->n_elements;
     m->L = d->ports;
+    // complete electrode model: the electrode voltages are rows nNodes .. nNodes + L - 1
+    m->n = m->nNodes + (m->cem ? m->L : 0);
     m->Md = d->drive_count;
     m->Mm = d->meas_count;
     m->MdPad = (int)data_rows((uint32_t)m->Md);
@@ -107,7 +115,7 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     m->height = d->height;
     m->portHeight = d->port_height;
 
-    m->hostNodes.assign(d->nodes, d->nodes + (size_t)2 * m->n);
+    m->hostNodes.assign(d->nodes, d->nodes + (size_t)2 * m->nNodes);
     m->hostElements.assign(d->elements, d->elements + (size_t)3 * m->E);
 
     // ---- internal node order: Morton (Z-order) of the coordinates, so that
@@ -115,22 +123,58 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     // L1, and the two-level preconditioner's aggregates of consecutive rows
     // are compact).  Elements keep their order; every node-indexed export
     // maps back through rowOf.
-    std::vector<int32_t> perm(m->n), rowOf(m->n);
-    morton_order(m->n, d->nodes, perm.data());
-    for (int i = 0; i < m->n; ++i) rowOf[perm[i]] = i;
+    const int N = m->nNodes;
+    std::vector<int32_t> perm(N), rowOf(N);
+    morton_order(N, d->nodes, perm.data());
+    for (int i = 0; i < N; ++i) rowOf[perm[i]] = i;
     std::vector<int32_t> elems((size_t)3 * m->E);
     for (size_t k = 0; k < elems.size(); ++k) elems[k] = rowOf[d->elements[k]];
     std::vector<int32_t> edgesP((size_t)2 * d->n_edges);
     for (size_t k = 0; k < edgesP.size(); ++k) edgesP[k] = rowOf[d->edges[k]];
-    std::vector<double> nodesP((size_t)2 * m->n);
-    for (int i = 0; i < m->n; ++i) {
+    std::vector<double> nodesP((size_t)2 * N);
+    for (int i = 0; i < N; ++i) {
         nodesP[2 * i] = d->nodes[2 * (size_t)perm[i]];
         nodesP[2 * i + 1] = d->nodes[2 * (size_t)perm[i] + 1];
     }
 
+    // ---- complete electrode model: every boundary edge (a, b) of port l is a
+    // contact element on (a, b, U_l) with the element matrix of
+    //   (1/z) int_edge (u - U_l)(v - V_l) ds,
+    // 1/z [[h/3, h/6, -h/2], [h/6, h/3, -h/2], [-h/2, -h/2, h]] for an edge of
+    // length h (P1 on the edge); it enters the structure and the assembly like
+    // a triangle whose parameter is 1, so S carries it in every harmonic
+    std::vector<int32_t> elemsAll = elems;
+    std::vector<double> Kc, Mc;
+    if (m->cem) {
+        const double iz = 1.0 / m->contactZ;
+        for (int l = 0; l < m->L; ++l) {
+            int edgesOnPort = 0;
+            for (int k = 0; k < d->port_edges_cap; ++k) {
+                const int32_t eg = d->port_edges[(size_t)l * d->port_edges_cap + k];
+                if (eg < 0) continue;
+                MPF_CHECK(eg < d->n_edges, MPF_EINVAL, "mpf_eit_create: port %d names edge %d of %d", l, eg,
+                          d->n_edges);
+                const int32_t a = d->edges[2 * (size_t)eg], b = d->edges[2 * (size_t)eg + 1];
+                const double h = std::hypot(d->nodes[2 * (size_t)a] - d->nodes[2 * (size_t)b],
+                                            d->nodes[2 * (size_t)a + 1] - d->nodes[2 * (size_t)b + 1]);
+                elemsAll.push_back(rowOf[a]);
+                elemsAll.push_back(rowOf[b]);
+                elemsAll.push_back(N + l);
+                const double ke[9] = {h / 3, h / 6, -h / 2, h / 6, h / 3, -h / 2, -h / 2, -h / 2, h};
+                for (double v : ke) {
+                    Kc.push_back(iz * v);
+                    Mc.push_back(0.0);
+                }
+                ++edgesOnPort;
+            }
+            MPF_CHECK(edgesOnPort > 0, MPF_EINVAL, "mpf_eit_create: port %d has no boundary edge", l);
+        }
+    }
+    const int Eall = (int)(elemsAll.size() / 3);
+
     // ---- FEM structure and elemental integrals
-    MPF_TRY(build_structure(m->n, m->E, elems.data(), m->fs));
-    m->dataRows = m->fs.dataRows;
+    MPF_TRY(build_structure(m->n, Eall, elemsAll.data(), m->fs));
+    m->dataRows = (int)data_rows((uint32_t)m->nNodes);  // node-indexed exports (mesh nodes only)
     m->npad = m->fs.npad;
     m->nblk = m->npad / kRowTile;
     m->W = m->fs.density;
@@ -138,11 +182,19 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     for (uint32_t c : m->fs.refColIds) m->nnz += c != kInvalid;
     std::vector<double> K((size_t)m->E * 9), M((size_t)m->E * 9);
     p1_elemental(m->E, d->nodes, d->elements, K.data(), M.data());
+    K.insert(K.end(), Kc.begin(), Kc.end());  // contact elements follow the triangles
+    M.insert(M.end(), Mc.begin(), Mc.end());
     std::vector<float> Kf(K.begin(), K.end()), Mf(M.begin(), M.end());
 
     // ---- excitation matrix and unique right-hand sides
-    std::vector<double> exc((size_t)m->n * m->L);
-    excitation_matrix(m->n, nodesP.data(), edgesP.data(), m->L, d->port_edges, d->port_edges_cap, exc.data(), m->n);
+    std::vector<double> exc((size_t)m->n * m->L, 0.0);
+    if (m->cem) {
+        // the port current enters the electrode's voltage unknown
+        for (int l = 0; l < m->L; ++l) exc[(size_t)(N + l) + (size_t)l * m->n] = 1.0;
+    } else {
+        excitation_matrix(m->n, nodesP.data(), edgesP.data(), m->L, d->port_edges, d->port_edges_cap, exc.data(),
+                          m->n);
+    }
     m->fixed = d->source_type == MPF_SOURCE_FIXED ? 1 : 0;
     // voltage sources: binarised excitation (src/models/eit_kernel.cu:40-41)
     if (m->fixed)
@@ -614,6 +666,9 @@ int eit_assemble(mpf_eit* m, int F, const float* gamma, bool fp64, cudaStream_t 
 
 int eit_assemble_export(mpf_eit* m, int F, const float* gamma, float* sOut, float* rOut, cudaStream_t s) {
     MPF_TRY(check_device(m));
+    MPF_CHECK(!m->cem, MPF_ENOTSUP, "mpf_eit_assemble: the reference ELL layout has no electrode rows "
+              "(complete electrode model)");
+    
     MPF_CHECK(F >= 1 && gamma, MPF_EINVAL, "mpf_eit_assemble: bad arguments");
     MPF_TRY(ensure_workspace(m, F, false, false));
     MPF_TRY(eit_assemble(m, F, gamma, false, s));
@@ -769,6 +824,8 @@ int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, floa
                         mpf_solve_stats* stats, cudaStream_t s) {
     MPF_TRY(check_device(m));
     MPF_CHECK(F >= 1 && gamma && Vout, MPF_EINVAL, "mpf_eit_forward_complex: bad arguments");
+    MPF_CHECK(!m->cem, MPF_ENOTSUP, "mpf_eit_forward_complex: the complete electrode model is implemented for "
+              "real parameters only");
     MPF_CHECK(!m->fixed, MPF_ENOTSUP, "mpf_eit_forward_complex: voltage (fixed) sources are not implemented");
     MPF_CHECK(m->KP <= 64, MPF_ENOTSUP, "mpf_eit_forward_complex: at most 64 unique excitations");
     auto t0 = std::chrono::steady_clock::now();
@@ -844,7 +901,7 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
     MPF_CHECK(m->fieldsValid && F >= 1 && F <= m->lastFrames && out, MPF_EINVAL,
               "mpf_eit_fields: no forward solve with that many frames");
     MPF_TRY(fem_launch_fields_export(F, m->Ca, m->C, m->compOfD.ptr, m->npad, m->KP, m->dataRows, m->Md + m->Mm,
-                                     m->n, m->colU.ptr, m->colScale.ptr, m->betaC.ptr, m->X.ptr, m->rowOf.ptr, out,
+                                     m->nNodes, m->colU.ptr, m->colScale.ptr, m->betaC.ptr, m->X.ptr, m->rowOf.ptr, out,
                                      s));
     return MPF_OK;
 }
@@ -1427,7 +1484,7 @@ void eit_destroy(mpf_eit* m) {
 }
 
 void eit_info(const mpf_eit* m, mpf_eit_info* i) {
-    i->n_nodes = m->n;
+    i->n_nodes = m->nNodes;
     i->n_elements = m->E;
     i->data_rows = m->dataRows;
     i->ports = m->L;

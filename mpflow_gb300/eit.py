@@ -182,8 +182,10 @@ class EIT:
 
     def __init__(self, mesh: IrregularMesh, sources: Sources, referenceValue: float = 1.0,
                  components: int = 1, height: float = 1.0, portHeight: float = 1.0,
-                 logarithmic: bool = False, device: int = 0, exact_jacobian: bool = False):
+                 logarithmic: bool = False, device: int = 0, exact_jacobian: bool = False,
+                 contact_impedance: float = 0.0):
         self.mesh, self.sources = mesh, sources
+        self.contact_impedance = float(contact_impedance)
         self.referenceValue = float(referenceValue)
         self.components, self.height, self.portHeight = int(components), float(height), float(portHeight)
         self.logarithmic = bool(logarithmic)
@@ -197,7 +199,8 @@ class EIT:
             sources.drivePattern.shape[1], sources.measurementPattern.shape[1],
             ptr(sources.drivePattern).value, ptr(sources.measurementPattern).value,
             ptr(sources.values).value, sources.type, self.referenceValue, int(self.logarithmic),
-            self.components, self.height, self.portHeight, self.device, int(bool(exact_jacobian)))
+            self.components, self.height, self.portHeight, self.device, int(bool(exact_jacobian)),
+            self.contact_impedance)
         h = ctypes.c_void_p()
         check(lib().mpf_eit_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h

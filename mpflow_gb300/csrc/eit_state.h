@@ -38,6 +38,8 @@ struct mpf_eit {
     mpf::DevBuf<double> Bc64;
     mpf::DevBuf<float> alpha, beta, beta2, betaC, massCoef;
     int exactJacobian = 0;
+    int jacIdentity = 0;              // drive / measurement rows are the unique columns in order (JacPlan)
+    float jacUniformScale = 0.f;      // the common row scale of the Jacobian, or 0
     mpf::DevBuf<int32_t> dcFree, compOfD;
     mpf::DevBuf<int32_t> nzPtr, nzNode;
     mpf::DevBuf<double> nzVal;

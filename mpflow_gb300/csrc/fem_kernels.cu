@@ -116,91 +116,223 @@ __global__ void k_voltages(int F, int Ca, int KP, int Mm, int Md, const double* 
 // for all harmonics at once:
 //   J[d*MP + m][e] = -h p'(gamma_e) sd sm sum_c beta_c^2
 //                    sum_ij Y_c[n_i][ud] K_e[i+3j] Y_c[n_j][um]
-// A block owns 32 consecutive elements (one per lane); warp w owns drive rows
-// [w*DPT, (w+1)*DPT) and all MP measurement rows.  Fields of the 3 element
-// nodes are staged through shared memory per harmonic; the output rows of a
-// warp are 32 consecutive elements, i.e. coalesced 128-byte stores.
-template <int KP, int MP, int DPT>
-__global__ void __launch_bounds__(512) k_jacobian(JacPlan jp, int npad, const float* __restrict__ X,
-                                                  const float* __restrict__ gamma, float* __restrict__ J,
-                                                  __nv_bfloat16* __restrict__ Jhi,
-                                                  __nv_bfloat16* __restrict__ Jlo) {
-    extern __shared__ float jsm[];
-    float(*Ys)[KP][33] = reinterpret_cast<float(*)[KP][33]>(jsm);
-    float(*Ts)[KP][33] = reinterpret_cast<float(*)[KP][33]>(jsm + 3 * KP * 33);
-    float(*Ks)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33);
-    float(*Ms)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33 + 32 * 9);
-    float(*Ke)[9] = reinterpret_cast<float(*)[9]>(jsm + 6 * KP * 33 + 2 * 32 * 9);
+// i.e. per element a sum of 3 Ca outer products of a drive vector and a
+// measurement vector.  A block owns 32 consecutive elements (lane = element)
+// and 8 * DPT drive rows (grid z covers the rest); warp w owns drive rows
+// [w*DPT, (w+1)*DPT) of the block and all MP measurement rows, DPT x MP
+// accumulators per thread.  The field rows of the 96 element nodes (KP
+// floats each) are gathered per harmonic with cp.async into a double buffer,
+// one harmonic ahead of the arithmetic; they are then expanded in shared
+// memory into the block's drive rows (multiplied by the element matrix and
+// the harmonic weight) and the measurement rows, so the inner loop is DPT +
+// MP conflict-free shared-memory loads for DPT * MP FMAs with no index
+// lookups.  Output rows are 32 consecutive elements: coalesced stores.
+__device__ __forceinline__ void jac_cp16(float* dst, const float* src, bool valid) {
+    // 16 bytes, zero-filled when !valid (src-size 0)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+template <int KP, int MP, int DPT, bool ID>
+__global__ void __launch_bounds__(256, 1) k_jacobian(JacPlan jp, int npad, const float* __restrict__ X,
+                                                     const float* __restrict__ gamma, float* __restrict__ J,
+                                                     __nv_bfloat16* __restrict__ Jhi,
+                                                     __nv_bfloat16* __restrict__ Jlo) {
+    constexpr int DB = 8 * DPT;      // drive rows of a block
+    constexpr int RS = KP + 4;       // row stride of the gathered field rows (16-byte multiple)
+    constexpr int CH = KP / 4;       // 16-byte chunks per field row
+    constexpr int MS = MP + 4;       // element row stride of the measurement rows
+    constexpr int DS = DB + 4;       // element row stride of the drive rows
+    static_assert(MP % 4 == 0 && DPT % 2 == 0, "vector loads of the staged rows");
+    extern __shared__ __align__(16) float jsm[];
+    float* Yr = jsm;                                  // [2][96][RS] gathered field rows
+    float* Ym = jsm + 2 * 96 * RS;                    // [3][32][MS]: Ym[j][el][m] = Y[n_j][um(m)]
+    float* Td = Ym + 3 * 32 * MS;                     // [3][32][DS]: Td[j][el][d]
+    float(*Ks)[9] = reinterpret_cast<float(*)[9]>(Td + 3 * 32 * DS);
+    float(*Ms)[9] = Ks + 32;
+    float(*Ke)[9] = Ks + 64;
+    __shared__ int um[MP], ud[DB], nodeOf[96];
     const int f = blockIdx.y;
     if (jp.frameMask && !jp.frameMask[f]) return;
     const int e0 = blockIdx.x * 32;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nthreads = blockDim.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int e = e0 + lane;
-    for (int i = threadIdx.x; i < 32 * 9; i += nthreads) {
+    const int drives = jp.rowsJ / MP;
+    const int d0 = blockIdx.z * DB;
+    for (int i = threadIdx.x; i < 32 * 9; i += 256) {
         const int el = i / 9, k = i % 9;
         const bool in = e0 + el < jp.E;
         Ks[el][k] = in ? jp.Kf[(size_t)(e0 + el) * 9 + k] : 0.f;
         Ms[el][k] = (in && jp.exact) ? jp.Mf[(size_t)(e0 + el) * 9 + k] : 0.f;
     }
-    float acc[DPT][MP];
+    for (int i = threadIdx.x; i < MP; i += 256) um[i] = jp.rowM[i];
+    for (int i = threadIdx.x; i < DB; i += 256) ud[i] = d0 + i < drives ? jp.rowD[(size_t)(d0 + i) * MP] : -1;
+    for (int i = threadIdx.x; i < 96; i += 256) nodeOf[i] = e0 + i / 3 < jp.E ? jp.elements[(size_t)e0 * 3 + i] : -1;
+    __syncthreads();
+    // gather the field rows of harmonic ci into buffer b (row r = el * 3 + l)
+    auto gather = [&](int ci, int b) {
+        const float* Xg = X + ((size_t)f * jp.Ca + ci) * npad * KP;
+        for (int i = threadIdx.x; i < 96 * CH; i += 256) {
+            const int r = i / CH, c = i % CH;
+            const int nd = nodeOf[r];
+            jac_cp16(Yr + ((size_t)b * 96 + r) * RS + c * 4, Xg + (size_t)(nd < 0 ? 0 : nd) * KP + c * 4, nd >= 0);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    // accumulators as pairs of measurement rows: packed FP32x2 FMAs
+    float2 acc[DPT][MP / 2];
 #pragma unroll
     for (int a = 0; a < DPT; ++a)
 #pragma unroll
-        for (int m = 0; m < MP; ++m) acc[a][m] = 0.f;
-    const int dBase = warp * DPT;
-    const int drives = jp.rowsJ / MP;
+        for (int m = 0; m < MP / 2; ++m) acc[a][m] = make_float2(0.f, 0.f);
+    gather(0, 0);
+    if constexpr (ID) {
+        // identity maps: measurement row m is field column m and drive row d
+        // is column d, so each thread reads its element's rows directly and
+        // forms its own drive values from the element matrix in registers
+        for (int ci = 0; ci < jp.Ca; ++ci) {
+            if (ci + 1 < jp.Ca) {
+                gather(ci + 1, (ci + 1) & 1);
+                asm volatile("cp.async.wait_group 1;" ::: "memory");
+            } else {
+                asm volatile("cp.async.wait_group 0;" ::: "memory");
+            }
+            __syncthreads();  // harmonic ci's rows are in
+            const float* Yb = Yr + (size_t)(ci & 1) * 96 * RS;
+            const float mc = jp.massCoef[ci], b2 = jp.beta2[ci];
+            float kv[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) kv[k] = b2 * (Ks[lane][k] + mc * Ms[lane][k]);
+            const int dc = d0 + warp * DPT;  // first drive column of this warp
+#pragma unroll
+            for (int jj = 0; jj < 3; ++jj) {
+                float4 ym[MP / 4];
+                const float4* yrow = reinterpret_cast<const float4*>(Yb + (lane * 3 + jj) * RS);
+#pragma unroll
+                for (int k = 0; k < MP / 4; ++k) ym[k] = yrow[k];
+                float td[DPT];
+#pragma unroll
+                for (int a = 0; a < DPT; ++a) td[a] = 0.f;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const float* drow = Yb + (lane * 3 + q) * RS + dc;
+                    float yd[DPT];
+                    if constexpr (DPT % 4 == 0) {
+#pragma unroll
+                        for (int k = 0; k < DPT / 4; ++k) {
+                            const float4 t = reinterpret_cast<const float4*>(drow)[k];
+                            yd[4 * k] = t.x;
+                            yd[4 * k + 1] = t.y;
+                            yd[4 * k + 2] = t.z;
+                            yd[4 * k + 3] = t.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < DPT / 2; ++k) {
+                            const float2 t = reinterpret_cast<const float2*>(drow)[k];
+                            yd[2 * k] = t.x;
+                            yd[2 * k + 1] = t.y;
+                        }
+                    }
+#pragma unroll
+                    for (int a = 0; a < DPT; ++a) td[a] = fmaf(yd[a], kv[q * 3 + jj], td[a]);
+                }
+#pragma unroll
+                for (int a = 0; a < DPT; ++a) {
+                    const float2 t2 = make_float2(td[a], td[a]);
+#pragma unroll
+                    for (int k = 0; k < MP / 4; ++k) {
+                        acc[a][2 * k] = __ffma2_rn(t2, make_float2(ym[k].x, ym[k].y), acc[a][2 * k]);
+                        acc[a][2 * k + 1] = __ffma2_rn(t2, make_float2(ym[k].z, ym[k].w), acc[a][2 * k + 1]);
+                    }
+                }
+            }
+            __syncthreads();  // every thread is done with buffer ci & 1 before it is refilled
+        }
+    } else {
     for (int ci = 0; ci < jp.Ca; ++ci) {
-        const float* Xg = X + ((size_t)f * jp.Ca + ci) * npad * KP;
-        __syncthreads();
-        for (int i = threadIdx.x; i < 32 * 3 * KP; i += nthreads) {
-            const int u = i % KP, l = (i / KP) % 3, el = i / (3 * KP);
-            float v = 0.f;
-            if (e0 + el < jp.E) v = Xg[(size_t)jp.elements[(size_t)(e0 + el) * 3 + l] * KP + u];
-            Ys[l][u][el] = v;
+        // the buffer of harmonic ci + 1 was last read by the expansion of
+        // ci - 1, which every thread finished before the barrier ahead of its
+        // arithmetic
+        if (ci + 1 < jp.Ca) {
+            gather(ci + 1, (ci + 1) & 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         // element matrix of this harmonic: K (reference mode) or K + alpha_c M
-        // (exact derivative of the 2.5D system matrix)
-        const float mc = jp.massCoef[ci];
-        for (int i = threadIdx.x; i < 32 * 9; i += nthreads) {
+        // (exact derivative of the 2.5D system matrix); Ke was last read by
+        // the expansion of ci - 1, finished before the previous barrier
+        const float mc = jp.massCoef[ci], b2 = jp.beta2[ci];
+        for (int i = threadIdx.x; i < 32 * 9; i += 256) {
             const int el = i / 9, k = i % 9;
             Ke[el][k] = Ks[el][k] + mc * Ms[el][k];
         }
-        __syncthreads();
-        const float b2 = jp.beta2[ci];
-        for (int i = threadIdx.x; i < 32 * 3 * KP; i += nthreads) {
-            const int el = i % 32, u = (i / 32) % KP, jj = i / (32 * KP);
-            // T_j[u] = sum_i Y[n_i][u] K[i + 3j] (element matrices stored row-major [i][j])
-            Ts[jj][u][el] = b2 * (Ys[0][u][el] * Ke[el][0 * 3 + jj] + Ys[1][u][el] * Ke[el][1 * 3 + jj] +
-                                  Ys[2][u][el] * Ke[el][2 * 3 + jj]);
+        __syncthreads();  // harmonic ci's rows and Ke are in; Ym / Td are free
+        const float* Yb = Yr + (size_t)(ci & 1) * 96 * RS;
+        // measurement rows (lanes along m: contiguous reads and writes)
+        for (int i = threadIdx.x; i < 3 * MP * 32; i += 256) {
+            const int m = i % MP, el = (i / MP) % 32, jj = i / (MP * 32);
+            Ym[(jj * 32 + el) * MS + m] = um[m] >= 0 ? Yb[(el * 3 + jj) * RS + um[m]] : 0.f;
+        }
+        // drive rows: b2 sum_i Y[n_i][ud(d)] Ke[i + 3j] (lanes along d)
+        for (int i = threadIdx.x; i < 3 * DB * 32; i += 256) {
+            const int dl = i % DB, el = (i / DB) % 32, jj = i / (DB * 32);
+            const int u = ud[dl];
+            float v = 0.f;
+            if (u >= 0)
+                v = Yb[(el * 3 + 0) * RS + u] * Ke[el][jj] + Yb[(el * 3 + 1) * RS + u] * Ke[el][3 + jj] +
+                    Yb[(el * 3 + 2) * RS + u] * Ke[el][6 + jj];
+            Td[(jj * 32 + el) * DS + dl] = b2 * v;
         }
         __syncthreads();
 #pragma unroll
         for (int jj = 0; jj < 3; ++jj) {
-            float ym[MP];
+            float4 ym[MP / 4];
+            const float4* yrow = reinterpret_cast<const float4*>(Ym + (jj * 32 + lane) * MS);
 #pragma unroll
-            for (int m = 0; m < MP; ++m) {
-                const int um = jp.rowM[m];
-                ym[m] = um >= 0 ? Ys[jj][um][lane] : 0.f;
+            for (int k = 0; k < MP / 4; ++k) ym[k] = yrow[k];
+            float td[DPT];
+            const float4* trow = reinterpret_cast<const float4*>(Td + (jj * 32 + lane) * DS + warp * DPT);
+#pragma unroll
+            for (int k = 0; k < DPT / 4; ++k) {
+                const float4 t = trow[k];
+                td[4 * k] = t.x;
+                td[4 * k + 1] = t.y;
+                td[4 * k + 2] = t.z;
+                td[4 * k + 3] = t.w;
+            }
+            if constexpr (DPT % 4 != 0) {
+                const float2 t = reinterpret_cast<const float2*>(Td + (jj * 32 + lane) * DS + warp * DPT)[DPT / 2 - 1];
+                td[DPT - 2] = t.x;
+                td[DPT - 1] = t.y;
             }
 #pragma unroll
             for (int a = 0; a < DPT; ++a) {
-                const int ud = (dBase + a) < drives ? jp.rowD[(dBase + a) * MP] : -1;
-                const float td = ud >= 0 ? Ts[jj][ud][lane] : 0.f;
+                const float2 t2 = make_float2(td[a], td[a]);
 #pragma unroll
-                for (int m = 0; m < MP; ++m) acc[a][m] = fmaf(td, ym[m], acc[a][m]);
+                for (int k = 0; k < MP / 4; ++k) {
+                    acc[a][2 * k] = __ffma2_rn(t2, make_float2(ym[k].x, ym[k].y), acc[a][2 * k]);
+                    acc[a][2 * k + 1] = __ffma2_rn(t2, make_float2(ym[k].z, ym[k].w), acc[a][2 * k + 1]);
+                }
             }
         }
+    }
     }
     const bool valid = e < jp.E;
     const float deriv = valid ? -jp.height * mat_param_deriv(jp.ref, gamma[(size_t)f * jp.E + e], jp.logarithmic) : 0.f;
     const size_t base = (size_t)f * jp.rowsJ * jp.Epad;
 #pragma unroll
     for (int a = 0; a < DPT; ++a) {
+        const int d = d0 + warp * DPT + a;
+        if (d >= drives) continue;
 #pragma unroll
         for (int m = 0; m < MP; ++m) {
-            const int row = (dBase + a) * MP + m;
-            if (row >= jp.rowsJ) continue;
-            const float v = valid ? deriv * jp.rowScale[row] * acc[a][m] : 0.f;
+            const int row = d * MP + m;
+            const float am = (m & 1) ? acc[a][m / 2].y : acc[a][m / 2].x;
+            const float sc = (ID && jp.uniformScale > 0.f) ? jp.uniformScale : __ldg(&jp.rowScale[row]);
+            const float v = valid ? deriv * sc * am : 0.f;
             const size_t o = base + (size_t)row * jp.Epad + e;
             if (jp.writeF32) J[o] = v;
             if (Jhi) {
@@ -423,35 +555,45 @@ int fem_launch_voltages(int F, int Ca, int KP, int Mm, int Md, const double* Gm,
     return MPF_OK;
 }
 
+template <int KP, int MP, int DPT, bool ID>
+static int launch_jac_v(int F, const JacPlan& jp, int npad, const float* X, const float* gamma, float* J,
+                        __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s) {
+    const int drives = jp.rowsJ / MP;
+    dim3 grid(jp.Epad / 32, F, (drives + 8 * DPT - 1) / (8 * DPT));
+    const size_t smem = sizeof(float) * (2 * 96 * (KP + 4) + 3 * 32 * (MP + 4) + 3 * 32 * (8 * DPT + 4) + 3 * 32 * 9);
+    if (smem > 48 * 1024)
+        MPF_CUDA(cudaFuncSetAttribute(k_jacobian<KP, MP, DPT, ID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    k_jacobian<KP, MP, DPT, ID><<<grid, 256, smem, s>>>(jp, npad, X, gamma, J, Jhi, Jlo);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+// the direct path needs every drive and measurement row of the block to be a
+// field column: rows up to MP and to the block's drive range within KP
 template <int KP, int MP, int DPT>
 static int launch_jac(int F, const JacPlan& jp, int npad, const float* X, const float* gamma, float* J,
                       __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s) {
-    const int warps = (jp.rowsJ / MP + DPT - 1) / DPT;
-    MPF_CHECK(warps >= 1 && warps <= 16, MPF_ENOTSUP, "jacobian: %d drive rows not supported", jp.rowsJ / MP);
-    dim3 grid(jp.Epad / 32, F);
-    const size_t smem = sizeof(float) * (6 * KP * 33 + 3 * 32 * 9);
-    if (smem > 48 * 1024)
-        MPF_CUDA(cudaFuncSetAttribute(k_jacobian<KP, MP, DPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_jacobian<KP, MP, DPT><<<grid, warps * 32, smem, s>>>(jp, npad, X, gamma, J, Jhi, Jlo);
-    MPF_LAUNCHED(1);
-    return MPF_OK;
+    const int drives = jp.rowsJ / MP;
+    const int driveCols = (drives + 8 * DPT - 1) / (8 * DPT) * (8 * DPT);
+    if (jp.identity && MP <= KP && driveCols <= KP)
+        return launch_jac_v<KP, MP, DPT, true>(F, jp, npad, X, gamma, J, Jhi, Jlo, s);
+    return launch_jac_v<KP, MP, DPT, false>(F, jp, npad, X, gamma, J, Jhi, Jlo, s);
 }
 
 int fem_launch_jacobian(int F, const JacPlan& jp, int MP, int npad, const float* X, const float* gamma,
                                float* J, __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s) {
     const int drives = jp.rowsJ / MP;
+    // thread tile DPT x MP: DPT 4 up to 32 measurement rows, 2 for 64; fewer
+    // drive rows than a block covers only leave warps idle
 #define MPF_JAC(KPv, MPv, DPTv) \
-    if (jp.KP == KPv && MP == MPv && (drives + DPTv - 1) / DPTv <= 16 && (DPTv == 1 || drives > 16 * (DPTv / 2))) \
-        return launch_jac<KPv, MPv, DPTv>(F, jp, npad, X, gamma, J, Jhi, Jlo, s);
-    MPF_JAC(16, 16, 1)
-    MPF_JAC(32, 16, 1)
-    MPF_JAC(32, 32, 1)
-    MPF_JAC(32, 32, 2)
-    MPF_JAC(64, 32, 1)
-    MPF_JAC(64, 32, 2)
-    MPF_JAC(64, 64, 1)
+    if (jp.KP == KPv && MP == MPv) return launch_jac<KPv, MPv, DPTv>(F, jp, npad, X, gamma, J, Jhi, Jlo, s);
+    MPF_JAC(16, 16, 2)
+    MPF_JAC(32, 16, 2)
+    MPF_JAC(32, 32, 4)
+    MPF_JAC(64, 32, 4)
     MPF_JAC(64, 64, 2)
-    MPF_JAC(64, 64, 4)
+    MPF_JAC(128, 64, 2)
 #undef MPF_JAC
     return fail(MPF_ENOTSUP, "jacobian: unsupported shape KP=%d MP=%d drives=%d", jp.KP, MP, drives);
 }

@@ -235,6 +235,15 @@ int eit_create(const mpf_eit_desc* d, mpf_eit** out) {
     if (canon.empty()) canon.push_back(std::vector<double>(L, 0.0));
     for (auto& u : dU) u = u < 0 ? 0 : u;
     for (auto& u : mU) u = u < 0 ? 0 : u;
+    m->jacIdentity = 1;
+    for (int j = 0; j < Md; ++j) m->jacIdentity &= dU[j] == j;
+    for (int j = 0; j < Mm; ++j) m->jacIdentity &= mU[j] == j;
+    // one scale for every (drive, measurement) row (adjacent patterns)
+    m->jacUniformScale = dS[0] * mS[0];
+    for (int d = 0; d < Md; ++d)
+        for (int j = 0; j < Mm; ++j)
+            if (dS[d] * mS[j] != m->jacUniformScale) m->jacUniformScale = 0.f;
+    if (!(m->jacUniformScale > 0.f)) m->jacUniformScale = 0.f;
     m->K = (int)canon.size();
     m->KP = m->K <= 16 ? 16 : m->K <= 32 ? 32 : m->K <= 64 ? 64 : m->K <= 128 ? 128 : 0;
     MPF_CHECK(m->KP > 0, MPF_ENOTSUP, "mpf_eit_create: %d distinct excitation patterns (max 128)", m->K);
@@ -687,7 +696,8 @@ static int eit_jacobian(mpf_eit* m, int F, const float* gamma, const int* frameM
     if (f32) MPF_TRY(m->J.alloc((size_t)m->capFJ * m->rowsJ * m->Epad));
     JacPlan jp{m->rowsJ, m->Epad, m->E, m->KP, m->Ca, m->rowD.ptr, m->rowM.ptr, m->rowScale.ptr,
                m->beta2.ptr, m->massCoef.ptr, m->elements.ptr, m->Kf.ptr, m->Mf.ptr, m->exactJacobian,
-               m->ref, m->fixed ? -(float)m->height : (float)m->height, m->logarithmic, frameMask, f32 ? 1 : 0};
+               m->ref, m->fixed ? -(float)m->height : (float)m->height, m->logarithmic, frameMask, f32 ? 1 : 0,
+               m->jacIdentity, m->jacUniformScale};
     return fem_launch_jacobian(F, jp, m->MmPad, m->npad, m->X.ptr, gamma, f32 ? m->J.ptr : nullptr, m->Jhi.ptr,
                                m->Jlo.ptr, s);
 }

@@ -253,6 +253,12 @@ struct JacPlan {
     int logarithmic;
     const int* frameMask;    // [F] frames to compute, or null for all
     int writeF32;            // 0: only the BF16 hi/lo split (the Gauss-Newton path)
+    // 1: drive row d uses field column d and measurement row m column m (for
+    // every real row), so the kernel reads the staged field rows directly
+    int identity;
+    // > 0: every real row has this scale (rowScale is not read; with identity
+    // maps the padding rows come out zero on their own)
+    float uniformScale;
 };
 int fem_launch_jacobian(int F, const JacPlan& jp, int MP, int npad, const float* X, const float* gamma,
                         float* J, __nv_bfloat16* Jhi, __nv_bfloat16* Jlo, cudaStream_t s);

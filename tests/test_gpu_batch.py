@@ -137,3 +137,23 @@ def test_batch_rejects_refinement_and_warm_start():
         with pytest.raises(mp.MpfError) as e:
             batch.solve(g, opts)
         assert e.value.status == 8
+
+
+def test_batch_config4_largest_members_full_size():
+    """Configuration 4's largest members at full size in one batch: the
+    100-ring disk (30301 nodes) with 16 and with 32 electrodes, 4 harmonics
+    (height 4), beside a 20-ring one; every mesh's voltages against the FP64
+    oracle (the per-mesh solve of src/models/eit.cpp:139-213)."""
+    import oracle
+    import torch
+    import mpflow_gb300 as mp
+    cases = [(100, 16, 0.1), (100, 32, 0.1), (20, 16, 0.1)]
+    setups = _setups(cases=cases)
+    gammas = [torch.tensor(_frames(mesh, i)[:2], dtype=torch.float32, device="cuda")
+              for i, (mesh, _, _) in enumerate(setups)]
+    batch = mp.EITBatch([m for _, _, m in setups])
+    Vb = batch.solve(gammas, mp.SolveOptions(tol=1e-6, preconditioner="two-level"))
+    assert batch.last_stats.not_converged == 0
+    for i, (mesh, orc, _) in enumerate(setups):
+        Vo, _, _ = oracle.eit_forward(orc, _frames(mesh, i)[1], tol=1e-12, want_jacobian=False)
+        assert rel_err(Vb[i][1].cpu().numpy(), Vo) < 1e-4, (i, rel_err(Vb[i][1].cpu().numpy(), Vo))

@@ -74,16 +74,28 @@ def test_config3_regularised_updates(config2):
     Vg, Jg = model.solve(torch.ones((1, E), dtype=torch.float32, device="cuda"),
                          mp.SolveOptions(tol=1e-6, refine_tol=1e-10), jacobian=True)
     vm = torch.tensor(Vm[None], dtype=torch.float32, device="cuda")  # (frames, Mm, Md) as solve() returns
-    errors = {}
+    # the error split: the oracle's FP64 dual solve fed the GPU's own FP32
+    # Jacobian and forward voltages isolates the solve; its distance to the
+    # all-FP64 update is what the FP32 forward model contributes
+    Jgd = Jg[0].cpu().numpy().astype(np.float64)
+    yg = oracle.flatten_measurement(Vm, orc) - oracle.flatten_measurement(Vg[0].cpu().numpy().astype(np.float64), orc)
+    errors, solve_err, model_err = {}, {}, {}
     for lam_rel in (1e-4, 1e-3, 1e-2, 1e-1):
         lam = lam_rel * scale
         want = oracle.inverse_dual(J0, y, 1.0, lam)
+        want_g = oracle.inverse_dual(Jgd, yg, 1.0, lam)
         got = model.inverse(Jg[0], Vg, vm, lam, "identity")[0].cpu().numpy().astype(np.float64)
         errors[lam_rel] = rel_err(got, want)
-    print("regularised update error vs FP64 by lambda/rms-row-norm:", errors)
-    # bounded by the FP32 Jacobian (1e-5 relative) amplified by 1/mu
-    assert errors[1e-1] < 1e-3 and errors[1e-2] < 5e-3 and errors[1e-3] < 2e-2, errors
-    assert np.isfinite(errors[1e-4])
+        solve_err[lam_rel] = rel_err(got, want_g)
+        model_err[lam_rel] = rel_err(want_g, want)
+    print("update error vs FP64 by lambda/rms-row-norm:", errors, "solve part:", solve_err,
+          "FP32 forward-model part:", model_err)
+    # the solve itself (split-BF16 Gram refined in FP64) is accurate at every
+    # level; the total follows the FP32 Jacobian (1e-5 relative) amplified by 1/mu
+    assert all(v < 1e-3 for v in solve_err.values()), solve_err
+    assert errors[1e-1] < 1e-3 and errors[1e-2] < 5e-3 and errors[1e-3] < 2e-2 and errors[1e-4] < 0.1, errors
+    for lam_rel in (1e-4, 1e-3):
+        assert model_err[lam_rel] > 0.5 * errors[lam_rel], (lam_rel, model_err, errors)
 
 
 def test_config3_gn_step(config2):

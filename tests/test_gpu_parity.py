@@ -148,6 +148,34 @@ def test_gn_step_matches_oracle_dual():
     assert rel_err(d, d_ref) < 2e-3, rel_err(d, d_ref)
 
 
+def test_config1_gn_step_at_spec():
+    """Configuration 1 as specified: the 30-ring disk (2791 nodes, 5400
+    triangles), 16 electrodes 0.1 rad wide, adjacent drive (1 mA) and
+    measurement, 1 S/m with one 0.1 S/m inclusion of radius 0.2 centred in
+    r < 0.6 (seed 0), 2D, CG tolerance 1e-6, one Gauss-Newton step from the
+    homogeneous start with lambda = 1e-2, against the oracle's FP64 dual step
+    (src/solver/solver.cpp:196-225, src/solver/inverse.cpp:60-238)."""
+    import oracle
+    import mpflow_gb300 as mp
+    torch = _torch()
+    mesh, src, orc = make_setup(rings=30, ports=16, width=0.1)
+    assert mesh.nodes.shape[0] == 2791 and mesh.elements.shape[0] == 5400
+    g_true = inclusion_sigma(mesh, seed=0)
+    Vmeas, _, _ = oracle.eit_forward(orc, g_true, tol=1e-13, want_jacobian=False)
+    g0 = np.ones(mesh.elements.shape[0])
+    V0, J0, _ = oracle.eit_forward(orc, g0, tol=1e-13)
+    lam = 1e-2
+    y = oracle.flatten_measurement(Vmeas, orc) - oracle.flatten_measurement(V0, orc)
+    d_ref = oracle.inverse_dual(J0, y, 1.0, lam)
+    model = mp.EIT(mesh, src, 1.0)
+    gt = torch.ones((1, mesh.elements.shape[0]), dtype=torch.float32, device="cuda")
+    vm = torch.tensor(Vmeas[None], dtype=torch.float32, device="cuda")
+    res = model.gn_step(gt, vm, lam, mp.SolveOptions(tol=1e-6))
+    d = gt[0].cpu().numpy() - 1.0
+    assert abs(res[0] - np.linalg.norm(y) / np.linalg.norm(oracle.flatten_measurement(Vmeas, orc))) < 1e-4
+    assert rel_err(d, d_ref) < 2e-3, rel_err(d, d_ref)
+
+
 def test_exact_jacobian_2p5d_matches_oracle():
     import oracle
     import mpflow_gb300 as mp

@@ -389,7 +389,8 @@ def run_gb300(a):
                           "cg_shapes": model.cg_variants(F).tolist(),
                           "ms": dict(zip(names, ms.tolist())),
                           "gbs": dict(zip(names, (by / ms / 1e6).tolist())),
-                          "algorithmic_bytes": dict(zip(names, by.tolist()))}), flush=True)
+                          "algorithmic_bytes": dict(zip(names, by.tolist())),
+                          "cg_loop_overhead": model.profile_cg_loop(v, graphs=8)}), flush=True)
         return
     lib = mp.lib()
     # held-out frames and their noise-free measurements (untimed)
@@ -561,6 +562,11 @@ def run_gb300(a):
                       "dram_bytes": (traffic[i] * groups if traffic[i] is not None else None)}
                   for i, n in enumerate(names)}
 
+    # launch and graph overhead of the CG loop: per-iteration time of the loop
+    # as a solve runs it (graphs of 16 iterations, host convergence check
+    # between graphs) against the same kernels timed one launch at a time
+    cg_loop = model.profile_cg_loop(torch.tensor(truth[0], device=dev), graphs=8)
+
     # assembly and Jacobian kernels (HBM-bound), CUDA events on the launching stream
     fem_ms, fem_by = model.profile_fem(torch.tensor(truth[0], device=dev), reps=5)
     fem = {}
@@ -627,6 +633,7 @@ def run_gb300(a):
         "spmv_gbs": float(gbs[0]),
         "spmv": {"kernel": names[0], "gbs": float(gbs[0]), "frac_of_hbm": float(gbs[0] / peak), "target_frac": 0.70},
         "cg_kernels": cg_kernels,
+        "cg_loop_overhead": cg_loop,
         "phase_breakdown": {"learned": phase_learned, "plain_gn_batched": phase_plain},
         "roofline": roofline,
         "jjt_tensor_core": jjt,

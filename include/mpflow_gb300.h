@@ -355,6 +355,18 @@ int mpf_eit_profile_fem(mpf_eit_t model, int32_t frames, const float* gamma, int
 int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int32_t reps, double* ms,
                        double* bytes, mpf_stream_t stream);
 
+/* Launch and graph overhead of the CG loop on the systems of `gamma`
+ * (tolerance 0, every group iterating): ms[0] the per-iteration time of the
+ * loop as a solve runs it (CUDA graphs of 16 iterations with the host
+ * convergence check between graphs), timed by CUDA events around `graphs`
+ * graphs; ms[1] the per-iteration sum of the same kernels launched one at a
+ * time between CUDA events; ms[2] the host wall clock per iteration of the
+ * loop.  1 - ms[1] / ms[0] is the share of the loop spent outside the
+ * kernels.  The reference launches each iteration's kernels from the host
+ * (src/numeric/conjugate_gradient.cpp:111-157).  Synchronises. */
+int mpf_eit_profile_cg_loop(mpf_eit_t model, int32_t frames, const float* gamma, int32_t graphs, double* ms,
+                            mpf_stream_t stream);
+
 /* Device-time breakdown of the model's forward and Gauss-Newton calls by
  * phase.  While enabled, the library records a CUDA event on the call's
  * stream at every change of phase and attributes the time between
@@ -414,6 +426,14 @@ int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int
  * (C = A ./ B, 0 where B = 0).  C may alias A. */
 int mpf_matrix_elementwise(int32_t op, int32_t rows, int32_t cols, const float* A, const float* B, float* C,
                            int32_t ld, float scalar, mpf_stream_t stream);
+
+/* count scalars on the device between the reference's wider data types and
+ * the library's FP32 (direction 0: double -> float, 1: float -> double; a
+ * complex value is two scalars).  The C++ facade converts the material,
+ * voltages, Jacobian and fields of its double and complex<double>
+ * instantiations (src/models/eit.cpp:273-304 instantiates those natively)
+ * with this, stream-ordered and without host copies. */
+int mpf_convert_values(int32_t direction, int64_t count, const void* src, void* dst, mpf_stream_t stream);
 
 /* Column reductions into row 0 of each column of result (leading dimension
  * ldr), as Matrix::sum / vectorDotProduct / min / max leave them
@@ -521,7 +541,9 @@ int mpf_batch_cg_variants(mpf_batch_t batch, const int32_t* set, int32_t frames,
  * (hi.hi + hi.lo + lo.hi) on the tcgen05 tensor cores, FP32 accumulation;
  * C is rows x rows row-major (symmetric).  rows % 128 == 0, cols % 64 == 0.
  * The replaced reference product is the cuBLAS J^T J of
- * src/solver/inverse.cpp:136-156 (taken here in its dual orientation). */
+ * src/solver/inverse.cpp:136-156 (taken here in its dual orientation).
+ * Every pipeline wait inside the kernel is bounded (2 s); a wait that gives
+ * up makes the call return MPF_ETIMEOUT, and C is then undefined. */
 int mpf_gram_split_bf16(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda,
                         float* C, mpf_stream_t stream);
 
@@ -535,8 +557,9 @@ int mpf_gram_split_bf16(int32_t batch, int32_t rows, int32_t cols, const float* 
  * mpf_gram_split_bf16; limits batch*rows*lda <= 2,097,152 elements and a
  * split-K workspace <= 1,048,576 floats, larger requests return MPF_EINVAL.
  * All calls share the arrays: calls that overlap on the GPU race and corrupt
- * each other's results.  The first call on a device resolves the arrays'
- * addresses; make it before any stream capture.  Synchronises the stream. */
+ * each other's results.  Every call reads its abort flag back to the host
+ * and synchronises the stream, so the call cannot be captured into a CUDA
+ * graph: issue it on a stream that is not capturing. */
 int mpf_gram_split_bf16_noalloc(int32_t batch, int32_t rows, int32_t cols, const float* A, int32_t lda,
                                 float* C, mpf_stream_t stream);
 
@@ -594,6 +617,18 @@ int mpf_mlp_backward(mpf_mlp_t net, int32_t batch, const float* x, const float* 
  * applies to the weight matrices only. */
 int mpf_mlp_adam(mpf_mlp_t net, float lr, float beta1, float beta2, float eps, float weight_decay,
                  mpf_stream_t stream);
+
+/* One training step: mpf_mlp_backward on batch rows gathered by index
+ * (batch row b is row rows[b] of x, leading dimension ldx >= in, and of
+ * target, leading dimension ldt; rows = NULL takes rows 0..batch-1), then
+ * mpf_mlp_adam.  Same update, bit for bit, as the two calls on gathered
+ * copies, without the copies; the last layer's weight gradient is not
+ * stored (its Adam step runs in the epilogue of the tensor-core product that
+ * forms it), so the gradient array afterwards holds every gradient but that
+ * one.  rows is a device array of batch indices. */
+int mpf_mlp_train_step(mpf_mlp_t net, int32_t batch, const float* x, int32_t ldx, const int32_t* rows,
+                       const float* target, int32_t ldt, int32_t valid, float lr, float beta1, float beta2,
+                       float eps, float weight_decay, double* loss, mpf_stream_t stream);
 
 /* Device buffer of offsets[6] floats <-> network: which = 0 reads the
  * parameters, 1 writes them (and resets the Adam state), 2 reads the

@@ -86,17 +86,18 @@ To convert_value(From const& v) {
     if constexpr (is_complex<From>::value) return To(v.real(), v.imag());
     else return To(v);
 }
-// n values of type From on the device -> n values of type To on the device,
-// through the host
+// n values of type From on the device -> n values of type To on the device
+// (one of them FP32, the other FP64, real or complex alike), stream-ordered
+// on the device by mpf_convert_values
 template <class To, class From>
 void convert_device(To* dst, From const* src, size_t n, cudaStream_t s, const char* where) {
-    std::vector<From> h(n);
-    cuda(cudaMemcpyAsync(h.data(), src, sizeof(From) * n, cudaMemcpyDeviceToHost, s), where);
-    cuda(cudaStreamSynchronize(s), where);
-    std::vector<To> t(n);
-    for (size_t i = 0; i < n; ++i) t[i] = convert_value<To>(h[i]);
-    cuda(cudaMemcpyAsync(dst, t.data(), sizeof(To) * n, cudaMemcpyHostToDevice, s), where);
-    cuda(cudaStreamSynchronize(s), where);
+    static_assert(is_complex<To>::value == is_complex<From>::value, "convert_device: real <-> complex");
+    if constexpr (sizeof(To) == sizeof(From)) {
+        cuda(cudaMemcpyAsync(dst, src, sizeof(To) * n, cudaMemcpyDeviceToDevice, s), where);
+    } else {
+        const int64_t scalars = (int64_t)n * (is_complex<To>::value ? 2 : 1);
+        check(mpf_convert_values(sizeof(From) > sizeof(To) ? 0 : 1, scalars, src, dst, (mpf_stream_t)s), where);
+    }
 }
 }  // namespace detail
 
@@ -1150,8 +1151,14 @@ public:
         detail::cuda(cudaMallocAsync((void**)&buf, sizeof(float) * per * fields.size(), stream), "updateFields");
         const int st = mpf_eit_fields(model_, 1, buf, stream);
         if (st == MPF_OK)
-            for (size_t c = 0; c < fields.size(); ++c)
-                cudaMemcpyAsync(fields[c]->deviceData, buf + c * per, sizeof(float) * per, cudaMemcpyDeviceToDevice, stream);
+            for (size_t c = 0; c < fields.size(); ++c) {
+                if constexpr (detail::lib_native<dataType>())
+                    cudaMemcpyAsync(fields[c]->deviceData, buf + c * per, sizeof(float) * per, cudaMemcpyDeviceToDevice,
+                                    stream);
+                else if constexpr (!detail::is_complex<dataType>::value)  // double fields from FP32 potentials
+                    detail::convert_device(fields[c]->deviceData, buf + c * per, per, stream,
+                                           "mpFlow::models::EIT::updateFields");
+            }
         cudaFreeAsync(buf, stream);
         detail::check(st, "mpFlow::models::EIT::updateFields");
         detail::cuda(cudaStreamSynchronize(stream), "updateFields");
@@ -1213,16 +1220,16 @@ private:
             status = mpf_eit_forward(model_, 1, g, V, Jl, &options, st, stream);
         }
         if (status == MPF_OK || status == MPF_ENOCONV) {
-            std::vector<L> hv((size_t)Mm * Md);
-            detail::cuda(cudaMemcpyAsync(hv.data(), V, sizeof(L) * hv.size(), cudaMemcpyDeviceToHost, stream), where);
-            detail::cuda(cudaStreamSynchronize(stream), where);
-            std::vector<dataType> hd(hv.size());
-            for (size_t i = 0; i < hv.size(); ++i) hd[i] = detail::convert_value<dataType>(hv[i]);
-            detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, hd.data(),
-                                           sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md, cudaMemcpyHostToDevice,
+            dataType* Vd = nullptr;
+            detail::cuda(cudaMallocAsync((void**)&Vd, sizeof(dataType) * (size_t)Mm * Md, stream), where);
+            detail::convert_device(Vd, V, (size_t)Mm * Md, stream, where);
+            detail::cuda(cudaMemcpy2DAsync(result->deviceData, sizeof(dataType) * result->dataRows, Vd,
+                                           sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md, cudaMemcpyDeviceToDevice,
                                            stream),
                          where);
+            cudaFreeAsync(Vd, stream);
             detail::convert_device(jacobian->deviceData, Jl, nJ, stream, where);
+            fieldsValid_ = !detail::is_complex<dataType>::value;
         }
         cudaFreeAsync(V, stream);
         cudaFreeAsync(g, stream);

@@ -98,12 +98,14 @@ SIGNATURES = {
     "mpf_gn_solve": (_I, [_P, _I, _P, _P, _D, _D, _I, ctypes.POINTER(SolveOpts), _P, _P,
                           ctypes.POINTER(GnStats), _P]),
     "mpf_eit_profile_cg": (_I, [_P, _I, _P, _I, _P, _P, _P]),
+    "mpf_eit_profile_cg_loop": (_I, [_P, _I, _P, _I, _P, _P]),
     "mpf_eit_phase_times": (_I, [_P, _I, _P, _I, _P]),
     "mpf_eit_group_iterations": (_I, [_P, _P, _I, _P]),
     "mpf_eit_cg_variants": (_I, [_P, _P, _I, _P]),
     "mpf_inverse_solve": (_I, [_P, _I, _D, _I, _P, _P, _P, _P, _P]),
     "mpf_matrix_elementwise": (_I, [_I, _I, _I, _P, _P, _P, _I, ctypes.c_float, _P]),
     "mpf_matrix_column_reduce": (_I, [_I, _I, _I, _P, _P, _I, _P, _I, _P]),
+    "mpf_convert_values": (_I, [_I, ctypes.c_int64, _P, _P, _P]),
     "mpf_matrix_multiply": (_I, [_I, _I, _I, _I, _I, _P, _I, _P, _I, _P, _I, _P]),
     "mpf_sparse_create": (_I, [_I, _P, _P, ctypes.c_uint32, _P]),
     "mpf_sparse_destroy": (_I, [_P]),
@@ -124,6 +126,8 @@ SIGNATURES = {
     "mpf_mlp_forward": (_I, [_P, _I, _P, _P, _I, _P]),
     "mpf_mlp_backward": (_I, [_P, _I, _P, _P, _I, _I, _P, _P]),
     "mpf_mlp_adam": (_I, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P]),
+    "mpf_mlp_train_step": (_I, [_P, _I, _P, _I, _P, _P, _I, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                ctypes.c_float, ctypes.c_float, _P, _P]),
     "mpf_mlp_params": (_I, [_P, _P, _I, _P]),
     "mpf_eit_learned_input": (_I, [_P, _I, _P, _P, _P]),
     "mpf_eit_learned_prior": (_I, [_P, _D, _P]),

@@ -52,6 +52,7 @@ void eit_destroy(mpf_eit* m);
 int gn_solve(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, double target, int maxIters,
              const mpf_solve_opts* o, int32_t* itersOut, double* resOut, mpf_gn_stats* stats, cudaStream_t s);
 int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
+int profile_cg_loop(mpf_eit* m, int F, const float* gamma, int graphs, double* ms, cudaStream_t s);
 int phase_times(mpf_eit* m, int enable, double* ms, int cap, int64_t* calls);
 int profile_fem(mpf_eit* m, int F, const float* gamma, int reps, double* ms, double* bytes, cudaStream_t s);
 int group_iterations(mpf_eit* m, int32_t* out, int cap, int32_t* count);
@@ -84,6 +85,9 @@ int mlp_forward(mpf_mlp* n, int batch, const float* x, float* y, int ldy, cudaSt
 int mlp_backward(mpf_mlp* n, int batch, const float* x, const float* target, int ldt, int tvalid, double* loss,
                  cudaStream_t s);
 int mlp_adam(mpf_mlp* n, float lr, float beta1, float beta2, float eps, float weightDecay, cudaStream_t s);
+int mlp_train_step(mpf_mlp* n, int batch, const float* x, int ldx, const int* rows, const float* target, int ldt,
+                   int tvalid, float lr, float beta1, float beta2, float eps, float weightDecay, double* loss,
+                   cudaStream_t s);
 int mlp_params(mpf_mlp* n, float* buf, int which, cudaStream_t s);
 int learned_input(mpf_eit* m, int F, const float* vMeas, float* x, cudaStream_t s);
 int learned_prior(mpf_eit* m, double lambda, cudaStream_t s);
@@ -283,6 +287,14 @@ int mpf_eit_profile_cg(mpf_eit_t model, int32_t frames, const float* gamma, int3
     })
 }
 
+int mpf_eit_profile_cg_loop(mpf_eit_t model, int32_t frames, const float* gamma, int32_t graphs, double* ms,
+                            mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_profile_cg_loop: model == nullptr");
+        return mpf::profile_cg_loop(model, frames, gamma, graphs, ms, (cudaStream_t)stream);
+    })
+}
+
 int mpf_eit_phase_times(mpf_eit_t model, int32_t enable, double* ms, int32_t cap, int64_t* calls) {
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_phase_times: model == nullptr");
@@ -307,6 +319,10 @@ int mpf_eit_cg_variants(mpf_eit_t model, const int32_t* set, int32_t frames, int
 int mpf_matrix_elementwise(int32_t op, int32_t rows, int32_t cols, const float* A, const float* B, float* C,
                            int32_t ld, float scalar, mpf_stream_t stream) {
     MPF_GUARD({ return mpf::matrix_elementwise(op, rows, cols, A, B, C, ld, scalar, (cudaStream_t)stream); })
+}
+
+int mpf_convert_values(int32_t direction, int64_t count, const void* src, void* dst, mpf_stream_t stream) {
+    MPF_GUARD({ return mpf::convert_values(direction, (long long)count, src, dst, (cudaStream_t)stream); })
 }
 
 int mpf_matrix_column_reduce(int32_t op, int32_t rows, int32_t cols, const float* A, const float* B, int32_t ld,
@@ -475,6 +491,15 @@ int mpf_mlp_backward(mpf_mlp_t net, int32_t batch, const float* x, const float* 
 int mpf_mlp_adam(mpf_mlp_t net, float lr, float beta1, float beta2, float eps, float weight_decay,
                  mpf_stream_t stream) {
     MPF_GUARD({ return mpf::mlp_adam(net, lr, beta1, beta2, eps, weight_decay, (cudaStream_t)stream); })
+}
+
+int mpf_mlp_train_step(mpf_mlp_t net, int32_t batch, const float* x, int32_t ldx, const int32_t* rows,
+                       const float* target, int32_t ldt, int32_t valid, float lr, float beta1, float beta2,
+                       float eps, float weight_decay, double* loss, mpf_stream_t stream) {
+    MPF_GUARD({
+        return mpf::mlp_train_step(net, batch, x, ldx, rows, target, ldt, valid, lr, beta1, beta2, eps, weight_decay,
+                                   loss, (cudaStream_t)stream);
+    })
 }
 
 int mpf_mlp_params(mpf_mlp_t net, float* buffer, int32_t which, mpf_stream_t stream) {

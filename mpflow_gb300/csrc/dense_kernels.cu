@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
     uint64_t* bars = (uint64_t*)(smem + kStages * kStageBytes);
     __shared__ uint32_t tmemBase;
     __shared__ int localAbort;
+    __shared__ int issuedLoads;  // K blocks whose TMA loads the producer issued
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int b = blockIdx.z;
@@ -73,6 +74,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
 
     if (threadIdx.x == 0) {
         localAbort = 0;
+        issuedLoads = 0;
         for (int s = 0; s < kStages; ++s) {
             mbar_init(fullBar + 8 * s, 1);
             mbar_init(emptyBar + 8 * s, 1);
@@ -105,6 +107,7 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
             tma_load_2d(st + kTileBytes, &mapLo, fullBar + 8 * s, x, rowA);
             tma_load_2d(st + 2 * kTileBytes, &mapHi, fullBar + 8 * s, x, rowB);
             tma_load_2d(st + 3 * kTileBytes, &mapLo, fullBar + 8 * s, x, rowB);
+            issuedLoads = i + 1;
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
@@ -146,7 +149,27 @@ __global__ void __launch_bounds__(128, 1) k_gram_tc(const __grid_constant__ CUte
         if (threadIdx.x == 0 && nk > 0) atomicExch(ga.abortFlag, 1);
     }
     fence_before();
-    __syncthreads();
+    if (__syncthreads_or(!ok) && nk > 0) {
+        // A wait gave up: MMAs and TMA loads issued before the break may still
+        // be in flight.  Before TMEM is released and the CTA exits, wait (with
+        // the same limit, on a flag of its own) for the MMA issuer's final
+        // commit, which covers every MMA it issued, and for the last load
+        // issued into each stage (phases complete in order, and a stage's
+        // round r is issued only after its round r - 1 was consumed, so the
+        // parity of round r names that round).  TMEM is released even if
+        // these waits give up too: a CTA that exits holding TMEM would block
+        // every later allocation on its SM.  The result of a launch that
+        // raised the abort flag is undefined; the host reports MPF_ETIMEOUT.
+        if (threadIdx.x == 0) {
+            volatile int quiet = 0;
+            mbar_wait(doneBar, 0, &quiet);
+            for (int s = 0; s < kStages && s < issuedLoads; ++s) {
+                quiet = 0;
+                mbar_wait(fullBar + 8 * s, ((issuedLoads - 1 - s) / kStages) & 1, &quiet);
+            }
+        }
+        __syncthreads();
+    }
     if (warp == 1) {
         fence_after();
         tmem_dealloc(tmem, 128);
@@ -891,8 +914,8 @@ int dense_split_bf16(int batch, int rows, int cols, const float* A, int lda, __n
 // start of every call), and two calls that overlap on the GPU (different
 // streams, no ordering between them) race on the arrays and corrupt each
 // other's results.  The first call on a device resolves the arrays' device
-// addresses (cudaGetSymbolAddress); make that first call before any stream
-// capture on that device.
+// addresses (cudaGetSymbolAddress).  Every call copies the abort flag to the
+// host and synchronises the stream, so no call can be stream-captured.
 namespace {
 constexpr size_t kNoAllocElems = size_t(1) << 21;
 constexpr size_t kNoAllocWork = size_t(1) << 20;

@@ -111,7 +111,28 @@ __global__ void __launch_bounds__(256) k_mat_gemm(int transA, int transB, int m,
         }
 }
 
+// n scalars between FP64 and FP32 (direction 0: double -> float, 1: float ->
+// double); grid-stride, one value per thread per pass
+__global__ void k_convert(int direction, long long n, const void* __restrict__ src, void* __restrict__ dst) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (direction == 0) static_cast<float*>(dst)[i] = (float)static_cast<const double*>(src)[i];
+        else static_cast<double*>(dst)[i] = (double)static_cast<const float*>(src)[i];
+    }
+}
+
 }  // namespace
+
+int convert_values(int direction, long long count, const void* src, void* dst, cudaStream_t s) {
+    MPF_CHECK(direction == 0 || direction == 1, MPF_EINVAL, "mpf_convert_values: direction must be 0 or 1");
+    MPF_CHECK(count >= 0, MPF_EINVAL, "mpf_convert_values: count < 0");
+    if (count == 0) return MPF_OK;
+    MPF_CHECK(src && dst, MPF_EINVAL, "mpf_convert_values: null pointer");
+    const long long blocks = std::min<long long>((count + 255) / 256, 152LL * 16);
+    k_convert<<<(int)blocks, 256, 0, s>>>(direction, count, src, dst);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
 
 int matrix_elementwise(int op, int rows, int cols, const float* A, const float* B, float* C, int ld, float scalar,
                        cudaStream_t s) {

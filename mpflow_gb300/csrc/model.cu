@@ -1421,6 +1421,71 @@ int profile_cg(mpf_eit* m, int F, const float* gamma, int reps, double* ms, doub
     return MPF_OK;
 }
 
+// Launch and graph overhead of the CG loop.  ms[0]: per-iteration time of
+// the loop exactly as a solve runs it (graphs of 16 iterations, the active
+// flags and abort flag read back and the stream synchronised after each
+// graph), CUDA events around the whole loop; ms[1]: per-iteration sum of the
+// same kernels launched one at a time between CUDA events (the kernels'
+// own time); ms[2]: host wall clock of the loop per iteration.  Tolerance 0,
+// so no group retires and every iteration does the same work.
+int profile_cg_loop(mpf_eit* m, int F, const float* gamma, int graphs, double* ms, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(F >= 1 && gamma && graphs >= 1 && graphs <= 4096 && ms, MPF_EINVAL,
+              "mpf_eit_profile_cg_loop: bad arguments");
+    constexpr int kEvery = 16;
+    MPF_TRY(ensure_workspace(m, F, false, false));
+    MPF_TRY(eit_assemble(m, F, gamma, false, s));
+    MPF_TRY(tune_cg(m, F, s));
+    m->fieldsValid = false;  // the iteration vectors are overwritten below
+    CgProblem P = make_problem(m, F, 0.0);
+    MPF_TRY(cg_launch_init(P, true, s));
+    cudaEvent_t ev[2];
+    for (auto& e : ev) MPF_CUDA(cudaEventCreate(&e));
+    auto timed = [&](auto&& launch, double* acc) -> int {
+        MPF_CUDA(cudaEventRecord(ev[0], s));
+        MPF_TRY(launch());
+        MPF_CUDA(cudaEventRecord(ev[1], s));
+        MPF_CUDA(cudaEventSynchronize(ev[1]));
+        float t = 0.f;
+        MPF_CUDA(cudaEventElapsedTime(&t, ev[0], ev[1]));
+        *acc += t;
+        return MPF_OK;
+    };
+    double kernels = 0.0;
+    int st = MPF_OK;
+    for (int it = 0; it < kEvery && st == MPF_OK; ++it) {
+        st = timed([&] { return cg_launch_kernel(P, 0, s); }, &kernels);
+        if (st == MPF_OK) st = timed([&] { return cg_launch_kernel(P, 1, s); }, &kernels);
+        if (st == MPF_OK && P.coarse) st = timed([&] { return cg_launch_coarse(P, false, s); }, &kernels);
+        if (st == MPF_OK) st = timed([&] { return cg_launch_kernel(P, 2, s); }, &kernels);
+    }
+    double loop = 0.0, wall = 0.0;
+    if (st == MPF_OK) st = cg_launch_init(P, true, s);
+    if (st == MPF_OK) {
+        // one untimed graph so that capture and instantiation stay outside
+        int it = 0, nc = 0;
+        st = run_cg(m, P, kEvery, kEvery, s, &it, &nc);
+    }
+    if (st == MPF_OK) {
+        int it = 0, nc = 0;
+        const auto t0 = std::chrono::steady_clock::now();
+        MPF_CUDA(cudaEventRecord(ev[0], s));
+        st = run_cg(m, P, graphs * kEvery, kEvery, s, &it, &nc);
+        MPF_CUDA(cudaEventRecord(ev[1], s));
+        MPF_CUDA(cudaEventSynchronize(ev[1]));
+        wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        float t = 0.f;
+        MPF_CUDA(cudaEventElapsedTime(&t, ev[0], ev[1]));
+        loop = t;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    MPF_TRY(st);
+    ms[0] = loop / ((double)graphs * kEvery);
+    ms[1] = kernels / kEvery;
+    ms[2] = wall / ((double)graphs * kEvery);
+    return MPF_OK;
+}
+
 // Times the assembly and Jacobian kernels with CUDA events on `s`, on the
 // fields of a forward solve of gamma.  Algorithmic bytes per launch:
 //   assembly: E (12 connectivity + 36 K + 36 M) read once, and per frame

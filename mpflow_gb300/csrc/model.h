@@ -327,6 +327,7 @@ int dense_add_masked(int batch, int n, double* x, const double* d, cudaStream_t 
 // matrix_ops.cu: C = alpha op(A) op(B) + beta C, column-major FP32
 int matrix_multiply_scaled(int transA, int transB, int m, int n, int k, float alpha, const float* A, int lda,
                            const float* B, int ldb, float beta, float* C, int ldc, cudaStream_t s);
+int convert_values(int direction, long long count, const void* src, void* dst, cudaStream_t s);
 int matrix_elementwise(int op, int rows, int cols, const float* A, const float* B, float* C, int ld, float scalar,
                        cudaStream_t s);
 

@@ -489,6 +489,16 @@ class EIT:
         check(lib().mpf_eit_profile_cg(self._h, F, ptr(g), int(reps), ptr(ms), ptr(by), _stream()))
         return ms, by
 
+    def profile_cg_loop(self, gamma, graphs: int = 8):
+        """Per-iteration ms of the CG loop as a solve runs it (graphs of 16
+        iterations, host check between graphs), of its kernels launched one
+        at a time, and host wall per iteration (mpf_eit_profile_cg_loop)."""
+        g, F = self._frames(gamma)
+        ms = np.zeros(3)
+        check(lib().mpf_eit_profile_cg_loop(self._h, F, ptr(g), int(graphs), ptr(ms), _stream()))
+        return {"loop_ms": float(ms[0]), "kernels_ms": float(ms[1]), "wall_ms": float(ms[2]),
+                "outside_kernels_frac": float(1.0 - ms[1] / ms[0]) if ms[0] > 0 else None}
+
 
 class SparseMatrix:
     """numeric::SparseMatrix on the GPU (mpf_sparse_*): built from the

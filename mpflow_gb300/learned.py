@@ -83,6 +83,26 @@ class MLP:
         check(lib().mpf_mlp_adam(self._h, float(lr), float(beta1), float(beta2), float(eps), float(weight_decay),
                                  _stream()))
 
+    def train_step(self, x, target, rows=None, valid: int | None = None, lr: float = 1e-3, beta1: float = 0.9,
+                   beta2: float = 0.999, eps: float = 1e-8, weight_decay: float = 0.0, want_loss: bool = False):
+        """backward() + adam() on the batch rows `rows` (int32 CUDA tensor)
+        of x and target without gathering them (mpf_mlp_train_step); rows
+        None takes every row of x.  Returns the loss (host sync) or None."""
+        import torch
+        x = _f32(x, "x")
+        target = _f32(target, "target")
+        if rows is None:
+            batch, rp = x.shape[0], None
+        else:
+            rows = rows.to(device=x.device, dtype=torch.int32).contiguous()
+            batch, rp = rows.shape[0], ptr(rows)
+        valid = int(valid if valid is not None else target.shape[1])
+        loss = ctypes.c_double(0.0)
+        check(lib().mpf_mlp_train_step(self._h, batch, ptr(x), x.shape[1], rp, ptr(target), target.shape[1], valid,
+                                       float(lr), float(beta1), float(beta2), float(eps), float(weight_decay),
+                                       ctypes.byref(loss) if want_loss else None, _stream()))
+        return loss.value if want_loss else None
+
     def _params(self, which: int, buf=None):
         import torch
         if buf is None:
@@ -276,16 +296,15 @@ def train_warm_start(model, net: MLP, V, gamma, epochs: int = 60, batch: int = 2
         if prior:
             T.copy_(gamma)
             model.learned_prior_apply(X, T, mode=-1)
-        perm = torch.randperm(N, device=V.device, generator=gen)
+        perm = torch.randperm(N, device=V.device, generator=gen).to(torch.int32)
         acc = 0.0
         for b in range(steps_per_epoch):
             idx = perm[b * batch:(b + 1) * batch]
             want = b == steps_per_epoch - 1
-            loss = net.backward(X[idx], T[idx], valid=E, want_loss=want)
+            cur = lr * 0.5 * (1.0 + math.cos(math.pi * step / total))
+            loss = net.train_step(X, T, rows=idx, valid=E, lr=cur, weight_decay=weight_decay, want_loss=want)
             if want:
                 acc = loss
-            cur = lr * 0.5 * (1.0 + math.cos(math.pi * step / total))
-            net.adam(cur, weight_decay=weight_decay)
             step += 1
         losses.append(acc)
         if log:

@@ -4,6 +4,8 @@
 // every check holds.  Usage: facade_demo <rings> <electrodes>
 //        facade_demo complex <rings> <electrodes> <result file>: the complex
 //        (thrust::complex-style) model and differential reconstruction
+//        facade_demo wide <rings> <electrodes>: double and complex<double>
+//        instantiations against float and complex<float>
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
@@ -79,6 +81,104 @@ static int complex_case(unsigned rings, unsigned L, std::string const& file) {
     return 0;
 }
 
+// The double and complex<double> instantiations against float and
+// complex<float> on the same inputs: forward voltages, Jacobian, fields (real
+// only) and a differential reconstruction through solver::Solver.  Prints the
+// largest relative difference of each.
+template <class T>
+static std::vector<T> device_values(T const* p, size_t n) {
+    std::vector<T> h(n);
+    cudaMemcpy(h.data(), p, sizeof(T) * n, cudaMemcpyDeviceToHost);
+    return h;
+}
+template <class A, class B>
+static double rel_diff(std::vector<A> const& a, std::vector<B> const& b) {
+    double d = 0.0, m = 0.0;
+    for (size_t i = 0; i < a.size(); ++i) {
+        const std::complex<double> x(detail::real_part(a[i]), detail::imag_part(a[i]));
+        const std::complex<double> y(detail::real_part(b[i]), detail::imag_part(b[i]));
+        d = std::max(d, std::abs(x - y));
+        m = std::max(m, std::abs(y));
+    }
+    return d / std::max(m, 1e-300);
+}
+
+template <class T>
+static std::shared_ptr<solver::Solver<models::EIT<numeric::ConjugateGradient, FEM::Equation<T, FEM::basis::Linear, false>>>>
+wide_case(unsigned rings, unsigned L, T inclusion, T background, std::vector<T>* V, std::vector<T>* J,
+          std::vector<T>* F, std::vector<T>* S) {
+    typedef models::EIT<numeric::ConjugateGradient, FEM::Equation<T, FEM::basis::Linear, false>> M;
+    cudaStream_t stream = nullptr;
+    cublasHandle_t handle = nullptr;
+    auto mesh = numeric::IrregularMesh::ring(rings);
+    auto ports = FEM::Ports::circularBoundary(L, 0.1, mesh);
+    auto pattern = std::make_shared<numeric::Matrix<int>>(L, L, stream);
+    for (unsigned j = 0; j < L; ++j) {
+        (*pattern)(j, j) = 1;
+        (*pattern)((j + 1) % L, j) = -1;
+    }
+    pattern->copyToDevice(stream);
+    auto sources = std::make_shared<FEM::Sources<T>>(FEM::Sources<T>::Open, T(1e-3), ports, pattern, pattern, stream);
+    auto model = std::make_shared<M>(mesh, sources, T(1), handle, stream, 2, 1.0, 1.0);
+    model->options.tol = 1e-7;
+    const unsigned E = mesh->elements.rows();
+    auto target = std::make_shared<numeric::Matrix<T>>(E, 1, stream, background);
+    for (unsigned e = 0; e < E; ++e) {
+        auto xy = mesh->elementNodes(e);
+        const double cx = (xy(0, 0) + xy(1, 0) + xy(2, 0)) / 3.0, cy = (xy(0, 1) + xy(1, 1) + xy(2, 1)) / 3.0;
+        if ((cx - 0.3) * (cx - 0.3) + (cy - 0.2) * (cy - 0.2) < 0.0625) (*target)(e, 0) = inclusion;
+    }
+    target->copyToDevice(stream);
+    auto solver = std::make_shared<solver::Solver<M>>(model, 1, handle, stream);
+    solver->referenceDistribution->fill(background, stream);
+    solver->preSolve(handle, stream);
+    auto V0 = solver->calculation[0];
+    *V = device_values(V0->deviceData, (size_t)V0->dataRows * V0->cols);
+    *J = device_values(model->jacobian->deviceData, (size_t)model->jacobian->dataRows * E);
+    if (!detail::is_complex<T>::value) {
+        model->updateFields(stream);
+        F->clear();
+        for (auto const& f : model->fields) {
+            auto h = device_values(f->deviceData, (size_t)f->dataRows * f->cols);
+            F->insert(F->end(), h.begin(), h.end());
+        }
+    }
+    auto Vt = model->solve(target, handle, stream);
+    solver->measurement[0]->copy(Vt, stream);
+    model->solve(solver->referenceDistribution, handle, stream);
+    solver->inverseSolver->updateJacobian(model->jacobian, handle, stream);
+    solver->inverseSolver->setRegularizationParameter(T(2e-4), solver::Inverse<T>::identity, handle, stream);
+    auto sigma = solver->solveDifferential(handle, stream);
+    *S = device_values(sigma->deviceData, E);
+    return solver;
+}
+
+static int wide(unsigned rings, unsigned L) {
+    std::vector<float> Vf, Jf, Ff, Sf;
+    std::vector<double> Vd, Jd, Fd, Sd;
+    wide_case<float>(rings, L, 0.5f, 1.0f, &Vf, &Jf, &Ff, &Sf);
+    wide_case<double>(rings, L, 0.5, 1.0, &Vd, &Jd, &Fd, &Sd);
+    typedef std::complex<double> cdouble;
+    std::vector<cfloat> Vz, Jz, Fz, Sz;
+    std::vector<cdouble> Vw, Jw, Fw, Sw;
+    wide_case<cfloat>(rings, L, cfloat(0.5f, 0.3f), cfloat(1.f, 0.15f), &Vz, &Jz, &Fz, &Sz);
+    wide_case<cdouble>(rings, L, cdouble(0.5, 0.3), cdouble(1.0, 0.15), &Vw, &Jw, &Fw, &Sw);
+    const double dv = rel_diff(Vd, Vf), dj = rel_diff(Jd, Jf), df = rel_diff(Fd, Ff), ds = rel_diff(Sd, Sf);
+    const double zv = rel_diff(Vw, Vz), zj = rel_diff(Jw, Jz), zs = rel_diff(Sw, Sz);
+    double sMin = 1e300;
+    for (double v : Sd) sMin = std::min(sMin, v);
+    const bool sizes = Vd.size() == Vf.size() && Jd.size() == Jf.size() && Fd.size() == Ff.size() && !Fd.empty() &&
+                       Sd.size() == Sf.size() && Vw.size() == Vz.size() && Jw.size() == Jz.size() &&
+                       Sw.size() == Sz.size();
+    const bool ok = sizes && dv <= 1e-5 && dj <= 1e-5 && df <= 1e-5 && ds <= 1e-5 && zv <= 1e-5 && zj <= 1e-5 &&
+                    zs <= 1e-5 && sMin < 1.0;
+    printf("{\"double_v\": %.3e, \"double_j\": %.3e, \"double_fields\": %.3e, \"double_sigma\": %.3e, "
+           "\"cdouble_v\": %.3e, \"cdouble_j\": %.3e, \"cdouble_sigma\": %.3e, \"fields_values\": %zu, "
+           "\"sigma_min\": %.6f, \"ok\": %s}\n",
+           dv, dj, df, ds, zv, zj, zs, Fd.size(), sMin, ok ? "true" : "false");
+    return ok ? 0 : 1;
+}
+
 // json-selftest: parse a configuration without touching the GPU
 static int json_selftest() {
     auto v = json::parse(R"({"model": {"mesh": {"rings": 12, "radius": 1.5}, "ports": {"count": 8, "width": 0.2,
@@ -120,6 +220,14 @@ int main(int argc, char** argv) {
     if (argc > 4 && std::string(argv[1]) == "complex") {
         try {
             return complex_case((unsigned)atoi(argv[2]), (unsigned)atoi(argv[3]), argv[4]);
+        } catch (std::exception const& ex) {
+            printf("{\"error\": \"%s\", \"ok\": false}\n", ex.what());
+            return 2;
+        }
+    }
+    if (argc > 3 && std::string(argv[1]) == "wide") {
+        try {
+            return wide((unsigned)atoi(argv[2]), (unsigned)atoi(argv[3]));
         } catch (std::exception const& ex) {
             printf("{\"error\": \"%s\", \"ok\": false}\n", ex.what());
             return 2;

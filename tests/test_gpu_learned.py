@@ -53,6 +53,57 @@ def test_mlp_forward_and_gradients_match_oracle(batch):
         assert _rel(g, r) < 1e-2, (name, _rel(g, r))
 
 
+def test_mlp_adam_and_train_step():
+    """Adam (k_adam_flat / k_adam_wt) against an FP32 numpy Adam from the
+    kernels' own gradients; gradients after the step against the oracle at
+    the updated parameters (the backward products read the transposed BF16
+    copies that the Adam kernel writes); and mpf_mlp_train_step on rows
+    gathered by index equal to backward + adam on gathered copies, bit for
+    bit."""
+    from oracle import mlp_oracle as mo
+    import mpflow_gb300 as mp
+    import torch
+    dims = (128, 256, 128, 384)
+    rng = np.random.default_rng(11)
+    X = rng.standard_normal((300, dims[0])).astype(np.float32)
+    valid = 300
+    T = rng.standard_normal((300, 320)).astype(np.float32)
+    rows = rng.permutation(300)[:200].astype(np.int32)
+    Xt, Tt = torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda")
+    rt = torch.tensor(rows, device="cuda")
+    lr, wd, b1, b2, eps = 1e-3, 1e-2, 0.9, 0.999, 1e-8
+    a = _random_net(mp, torch, dims, seed=5)
+    b = _random_net(mp, torch, dims, seed=5)
+    p0 = a.parameters().cpu().numpy().astype(np.float64)
+    b.backward(Xt[rt.long()], Tt[rt.long()], valid=valid, want_loss=False)
+    g = b.gradients().cpu().numpy().astype(np.float64)
+    b.adam(lr, weight_decay=wd)
+    a.train_step(Xt, Tt, rows=rt, valid=valid, lr=lr, weight_decay=wd)
+    pa, pb = a.parameters().cpu().numpy(), b.parameters().cpu().numpy()
+    assert np.array_equal(pa, pb)
+    # FP64 Adam from the same gradients; weights decay, biases do not
+    o = a.offsets
+    decay = np.zeros(a.param_count, bool)
+    for k, (r, c) in enumerate(((dims[1], dims[0]), (dims[2], dims[1]), (dims[3], dims[2]))):
+        decay[o[2 * k]:o[2 * k] + r * c] = True
+    m, v = (1 - b1) * g, (1 - b2) * g * g
+    w = p0 - np.where(decay, lr * wd * p0, 0.0)
+    w = w - lr * (m / (1 - b1)) / (np.sqrt(v / (1 - b2)) + eps)
+    assert np.abs(pa - w).max() <= 1e-6 * max(np.abs(w).max(), 1.0), np.abs(pa - w).max()
+    # second step: gradients at the updated parameters against the oracle
+    a.backward(Xt[rt.long()], Tt[rt.long()], valid=valid, want_loss=False)
+    grads = a.unpack(a.gradients())
+    _, go = mo.loss_and_gradients(a.unpack(a.parameters()), X[rows], T[rows][:, :valid], valid)
+    for name, gg, r in zip(("dW1", "db1", "dW2", "db2", "dW3", "db3"), grads, go):
+        assert _rel(gg, r) < 1e-2, (name, _rel(gg, r))
+    # more train steps stay identical to backward + adam
+    for step in range(3):
+        a.train_step(Xt, Tt, rows=rt, valid=valid, lr=lr, weight_decay=wd)
+        b.backward(Xt[rt.long()], Tt[rt.long()], valid=valid, want_loss=False)
+        b.adam(lr, weight_decay=wd)
+    assert np.array_equal(a.parameters().cpu().numpy(), b.parameters().cpu().numpy())
+
+
 def test_mlp_training_reduces_loss():
     import mpflow_gb300 as mp
     import torch

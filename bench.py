@@ -79,6 +79,13 @@ def parse_args():
                    help="initial fields of each GN solve's first forward solve (and of the training-pair solves)")
     p.add_argument("--gn-factor", choices=["fp32-refined", "fp64"], default="fp64",
                    help="factor of J J^T + mu I in every Gauss-Newton update (mpf_solve_opts.gn_factor)")
+    p.add_argument("--accept-tol", type=float, default=0.0,
+                   help="CG tolerance of the learned start's acceptance solve in the timed steps "
+                        "(mpf_solve_opts.accept_tol; 0: the full tolerance)")
+    p.add_argument("--accept-study-tol", type=float, default=1e-4,
+                   help="untimed study after the timed steps: the learned path again with this acceptance "
+                        "tolerance, its decisions and step time against the timed run's (0: skip)")
+    p.add_argument("--accept-margin", type=float, default=0.1)
     p.add_argument("--cpu-threads", type=int, default=0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cg-shapes", type=str, default="",
@@ -404,6 +411,11 @@ def run_gb300(a):
     gn_opts = mp.SolveOptions(tol=a.tol, max_iter=6000, preconditioner=a.preconditioner,
                               warm_start="homogeneous" if a.gn_warm_start == "homogeneous" else 0,
                               gn_factor=a.gn_factor)
+    # the learned path: acceptance solve at accept_tol (the plain and
+    # prior-only paths have no acceptance solve; for them it changes nothing)
+    learned_opts = mp.SolveOptions(tol=a.tol, max_iter=6000, preconditioner=a.preconditioner,
+                                   warm_start="homogeneous" if a.gn_warm_start == "homogeneous" else 0,
+                                   gn_factor=a.gn_factor, accept_tol=a.accept_tol, accept_margin=a.accept_margin)
     lam = a.lam_rel * float(J0.norm() / np.sqrt(J0.shape[1]))
     del J0
 
@@ -442,6 +454,21 @@ def run_gb300(a):
         net.save(a.save_network)
     net0 = zero_network(L, round_up(E, 128)) if use_prior else None
     train_steps = a.epochs * max(1, a.train_pairs // 256) if not a.load_network else 0
+    # the training step alone (mpf_mlp_train_step, CUDA events; a throwaway
+    # network of the same shape on the same pairs): what the kernels sustain
+    # without the per-epoch work (noise, network inputs, prior targets)
+    probe = mp.MLP(L, a.hidden, a.hidden, round_up(E, 128), seed=99, device=local)
+    Xp = model.learned_input(Vtr)
+    batches = [torch.randint(0, Vtr.shape[0], (256,), device=dev, dtype=torch.int32) for _ in range(23)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for k, rows in enumerate(batches):
+        if k == 3:  # three untimed steps first
+            ev[0].record(torch.cuda.current_stream())
+        probe.train_step(Xp, gtr, rows=rows, valid=E, lr=1e-4)
+    ev[1].record(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    train_step_ms = ev[0].elapsed_time(ev[1]) / (len(batches) - 3)
+    del probe, Xp, batches
     del Vtr, gtr
 
     def barrier():
@@ -453,7 +480,7 @@ def run_gb300(a):
 
     def learned_step(s):
         _, it, res, acc, st = model.gn_solve_learned(net, vmeas[s], lam, target=a.target, max_iters=a.max_gn,
-                                                     options=gn_opts)
+                                                     options=learned_opts)
         return it, acc, st
 
     def prior_step(s):
@@ -514,6 +541,42 @@ def run_gb300(a):
     plain = summarise(t_p, r_p, F)
     accepted = float(np.mean(np.concatenate([r[1] for r in r_l])))
 
+    # the looser acceptance solve against the timed run's decisions on the same
+    # held-out frames (untimed by the step clock; CUDA events per call): the
+    # accepted flags and updates per frame, CG iterations and step time
+    accept_check = None
+    study_tol = a.accept_study_tol if a.accept_study_tol > a.tol else 0.0
+    if study_tol > 0.0 and study_tol != learned_opts.accept_tol:
+        study_opts = mp.SolveOptions(tol=a.tol, max_iter=6000, preconditioner=a.preconditioner,
+                                     warm_start="homogeneous" if a.gn_warm_start == "homogeneous" else 0,
+                                     gn_factor=a.gn_factor, accept_tol=study_tol, accept_margin=a.accept_margin)
+        same_acc = same_its = n_fr = 0
+        cg_study = cg_timed = study_decided = 0
+        study_ms = []
+        for i, s in enumerate(range(a.warmup, nsteps)):
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _, it_s, _, acc_s, st_s = model.gn_solve_learned(net, vmeas[s], lam, target=a.target,
+                                                             max_iters=a.max_gn, options=study_opts)
+            e1.record(stream)
+            barrier()
+            study_ms.append(e0.elapsed_time(e1))
+            it_t, acc_t, st_t = r_l[i]
+            same_acc += int(np.sum(np.asarray(acc_t) == acc_s))
+            same_its += int(np.sum(np.asarray(it_t) == it_s))
+            n_fr += F
+            cg_study += int(st_s.cg_iterations)
+            cg_timed += int(st_t.cg_iterations)
+            study_decided += int(st_s.accepted_loose)
+        k = max(1, nsteps - a.warmup)
+        accept_check = {"timed_accept_tol": learned_opts.accept_tol, "study_accept_tol": study_tol,
+                        "accept_margin": a.accept_margin, "cg_tol": a.tol, "frames": n_fr,
+                        "accepted_equal_fraction": same_acc / n_fr, "updates_equal_fraction": same_its / n_fr,
+                        "study_decided_on_loose_fraction": study_decided / n_fr,
+                        "cg_iterations_per_step": {"timed": cg_timed / k, "study": cg_study / k},
+                        "ms_per_step": {"timed": float(np.mean(t_l)), "study": float(np.mean(study_ms))}}
+
     # end to end through the public API: host V_meas in, host sigma out (learned path)
     host_v = [v.cpu().pin_memory() for v in vmeas]
     host_out = torch.empty((F, E), dtype=torch.float32).pin_memory()
@@ -522,7 +585,8 @@ def run_gb300(a):
         barrier()
         t0 = time.perf_counter()
         vm = host_v[s].to(dev, non_blocking=True)
-        g, _, _, _, st = model.gn_solve_learned(net, vm, lam, target=a.target, max_iters=a.max_gn, options=gn_opts)
+        g, _, _, _, st = model.gn_solve_learned(net, vm, lam, target=a.target, max_iters=a.max_gn,
+                                                options=learned_opts)
         host_out.copy_(g, non_blocking=True)
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) * 1e3
@@ -611,12 +675,18 @@ def run_gb300(a):
         "gn_first_solve_start": a.gn_warm_start,
         "gn_updates_mean": learned["gn_updates_mean"],
         "frames_converged_fraction": learned["frames_converged_fraction"],
+        "accept_check": accept_check,
         "learned": {"accepted_fraction": accepted,
                     "gn_updates_saved_per_frame": plain["gn_updates_mean"] - learned["gn_updates_mean"],
                     "train_pairs": a.train_pairs, "pair_generation_s": gen_s, "epochs": a.epochs,
                     "train_s": train_s, "train_steps": train_steps, "loss_first": losses[0],
                     "loss_last": losses[-1], "network": f"{L}-{a.hidden}-{a.hidden}-{round_up(E, 128)} GELU",
                     "train_tflops": (mlp_flops / train_s / 1e12) if train_steps else None,
+                    "train_step_ms": train_step_ms,
+                    "train_step_tflops": 6.0 * 256 * net.param_count / (train_step_ms * 1e-3) / 1e12,
+                    "train_tflops_what": "train_tflops: 6 x 256 x parameters x steps over the whole training "
+                                         "loop (per-epoch noise, inputs and prior targets included); "
+                                         "train_step_tflops: one mpf_mlp_train_step alone, CUDA events",
                     "train_cg_tol": a.train_tol, "loaded_network": a.load_network or None,
                     "labels": (("GN from the prior to the target (<= 4 updates; the prior where it does not "
                                 "converge)") if label_s is not None else "generating conductivity"),

@@ -219,6 +219,16 @@ typedef struct mpf_solve_opts {
      *    option 0.  The refinement's triangular solves (2.2 ms per step for 32
      *    frames) make it slower than option 0 on the 1024-row system. */
     int32_t gn_factor;
+    /* mpf_gn_solve_learned only: CG tolerance of the solve at the network's
+     * prediction, whose only use is the accept / reject decision (0 or <= tol:
+     * that solve runs at tol).  A frame whose data residual at accept_tol is
+     * <= target (1 - accept_margin) is accepted on it; every other frame
+     * continues from its fields to tol (the assembled systems and the coarse
+     * space are kept) and is decided on its full-tolerance residual, as
+     * without the option.  accept_margin (default 0.1 when 0) covers the
+     * difference between the two residuals. */
+    double accept_tol;
+    double accept_margin;
 } mpf_solve_opts;
 
 typedef struct mpf_solve_stats {
@@ -301,6 +311,7 @@ typedef struct mpf_gn_stats {
     double seconds;           /* host wall time of the call (synchronised) */
     int32_t solves_fp32;      /* frame updates solved by the FP32 factor with FP64 refinement */
     int32_t solves_fp64;      /* frame updates solved by the FP64 factor (gn_factor 1, or the fallback) */
+    int32_t accepted_loose;   /* mpf_gn_solve_learned: frames decided on the accept_tol solve */
 } mpf_gn_stats;
 
 /* Batched Gauss-Newton reconstruction: repeats mpf_gn_step on every frame
@@ -664,15 +675,18 @@ int mpf_inverse_solve_complex(mpf_eit_t model, int32_t regularization, double fa
  * mu = (referenceValue lambda)^2 as in mpf_gn_step, J0 the FP32 Jacobian at
  * gamma_h with the Gram and its Cholesky factor in FP64 (the fixed part of
  * Solver::solveAbsolute's first iteration, src/solver/solver.cpp:196-225,
- * taken once per model).  Held by the model as an n_elements x (meas_count
- * * drive_count) FP32 matrix; lambda = 0 removes it.  While a prior is set,
+ * taken once per model).  Held by the model as split-BF16 operands of an
+ * n_elements x (meas_count * drive_count) matrix (hi, lo parts), applied on
+ * the tensor cores as hi.hi + lo.hi + hi.lo with FP32 accumulation (about
+ * FP32 accuracy); lambda = 0 removes it.  While a prior is set,
  * mpf_gn_solve_learned starts from prior(x) + net(x), so the network learns
  * the correction to the linear step.  Synchronises. */
 int mpf_eit_learned_prior(mpf_eit_t model, double lambda, mpf_stream_t stream);
 
 /* out (device, frames x ldo, ldo >= n_elements) = prior(x) (mode 0),
  * out += prior(x) (mode 1) or out -= prior(x) (mode -1); x device, frames x
- * (meas_count * drive_count).  MPF_EINVAL when no prior is set. */
+ * (meas_count * drive_count).  MPF_EINVAL when no prior is set.
+ * Synchronises (reads the product's abort flag). */
 int mpf_eit_learned_prior_apply(mpf_eit_t model, int32_t frames, const float* x, float* out, int32_t ldo,
                                 int32_t mode, mpf_stream_t stream);
 

@@ -54,7 +54,7 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("refine_tol", ctypes.c_double),
                 ("max_refine", ctypes.c_int32), ("warm_start", ctypes.c_int32),
                 ("check_every", ctypes.c_int32), ("preconditioner", ctypes.c_int32), ("solver", ctypes.c_int32),
-                ("gn_factor", ctypes.c_int32)]
+                ("gn_factor", ctypes.c_int32), ("accept_tol", ctypes.c_double), ("accept_margin", ctypes.c_double)]
 
 
 class SolveStats(ctypes.Structure):
@@ -66,7 +66,8 @@ class SolveStats(ctypes.Structure):
 class GnStats(ctypes.Structure):
     _fields_ = [("gn_iterations", ctypes.c_int32), ("cg_iterations", ctypes.c_int32),
                 ("frames_converged", ctypes.c_int32), ("seconds", ctypes.c_double),
-                ("solves_fp32", ctypes.c_int32), ("solves_fp64", ctypes.c_int32)]
+                ("solves_fp32", ctypes.c_int32), ("solves_fp64", ctypes.c_int32),
+                ("accepted_loose", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p

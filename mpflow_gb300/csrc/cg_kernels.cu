@@ -1153,6 +1153,19 @@ int cg_iteration_launches(const CgProblem& P) { return P.solver >= 1 ? kBicgstab
 
 int cg_launch_kernel(const CgProblem& P, int which, cudaStream_t s) { return launch_one(P, which, s, true); }
 
+// Groups of the frames marked in frameSkip leave the iteration before it
+// starts (their x is kept as it is).  Launched after cg_launch_init.
+__global__ void k_skip_frames(int G, int M, int Ca, const int* __restrict__ frameSkip, int* __restrict__ active) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < G && frameSkip[(g / M) / Ca]) active[g] = 0;
+}
+
+int cg_launch_skip(const CgProblem& P, const int* frameSkip, cudaStream_t s) {
+    k_skip_frames<<<(P.G + 255) / 256, 256, 0, s>>>(P.G, P.M, P.Ca, frameSkip, P.active);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
 int cg_launch_finalize(const CgProblem& P, cudaStream_t s) {
     if (P.solver != 0) return MPF_OK;
     return dispatch_kp<FinalizeL>(P.KP, P, s);

@@ -71,7 +71,7 @@ struct mpf_eit {
     mpf::DevBuf<float> V, J, gramWork;
     mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
     mpf::DevBuf<double> A64, y, res;
-    mpf::DevBuf<int> info, frameMask, redoMask, fbMask, solveMask, upMask;
+    mpf::DevBuf<int> info, frameMask, redoMask, fbMask, solveMask, upMask, skipMask;
     // FP32 factor of the Gauss-Newton system with FP64 refinement (gn_update)
     mpf::DevBuf<double> cholL, cholX, cholR, cholY, cholRR, cholYY;
     mpf::DevBuf<int> info32, cholMask;
@@ -125,6 +125,11 @@ struct mpf_eit {
     bool priorReady = false;
     double priorLambda = 0.0;
     mpf::DevBuf<float> priorW;
+    // the prior as split-BF16 operands of the tensor-core product: W (E x L)
+    // as [priorN][3 priorLp] (hi, hi, lo) and the inputs of a call as
+    // [frames padded to 128][3 priorLp] (hi, lo, hi)
+    mpf::DevBuf<__nv_bfloat16> priorB, priorA;
+    int priorN = 0, priorLp = 0;
 
     // device-time breakdown by phase (mpf_eit_phase_times): while enabled,
     // phase_mark records an event on the stream at every change of phase;

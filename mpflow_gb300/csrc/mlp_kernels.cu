@@ -65,6 +65,10 @@ struct GemmArgs {
     __nv_bfloat16* wb;
     __nv_bfloat16* wt;
     int ldT;
+    // AXPBY form (one split): out = alpha D + beta out + add on rows <
+    // rowsValid and columns < colsValid
+    float alpha, beta, add;
+    int rowsValid, colsValid;
 };
 
 struct AdamArgs {
@@ -88,10 +92,13 @@ __device__ __forceinline__ float adam_one(float wi, float gi, float& m, float& v
 // One CTA = one 128x128 output tile and one K split.  Warp 0 lane 0 issues
 // the TMA loads, warp 1 lane 0 the MMAs; every warp drains TMEM (four warps,
 // or eight in the Adam form).
-template <bool ADAM>
-__global__ void __launch_bounds__(ADAM ? 256 : 128, 2) k_gemm_nt(const __grid_constant__ CUtensorMap mapA,
+enum GemmMode { kGemmStore = 0, kGemmAdam = 1, kGemmAxpby = 2 };
+
+template <int MODE>
+__global__ void __launch_bounds__(MODE == kGemmAdam ? 256 : 128, 2) k_gemm_nt(const __grid_constant__ CUtensorMap mapA,
                                                     const __grid_constant__ CUtensorMap mapB, GemmArgs ga,
                                                     AdamArgs adam) {
+    constexpr bool ADAM = MODE == kGemmAdam;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(smem + kStages * kStageBytes);
@@ -239,7 +246,8 @@ __global__ void __launch_bounds__(ADAM ? 256 : 128, 2) k_gemm_nt(const __grid_co
         // Every MMA has completed (doneBar), so the stage buffers are free:
         // each warp moves its 32 accumulator rows TMEM -> registers -> shared
         // memory (16-byte chunks XOR-swizzled by row, conflict-free), then
-        // writes them out one 512-byte row per instruction.
+        // writes them out one 512-byte row per instruction (the AXPBY form
+        // reads the old row and writes alpha D + beta out + add in bounds).
         float* stage = reinterpret_cast<float*>(smem) + warp * 32 * kTile;
 #pragma unroll 1
         for (int c = 0; c < kTile; c += 32) {
@@ -253,13 +261,30 @@ __global__ void __launch_bounds__(ADAM ? 256 : 128, 2) k_gemm_nt(const __grid_co
             }
         }
         __syncwarp();
+        if (MODE == kGemmStore) {
 #pragma unroll 4
-        for (int r = 0; r < 32; ++r) {
-            const int chunk = lane ^ (r & 7);
-            *reinterpret_cast<float4*>(tileOut + (size_t)(warp * 32 + r) * ga.ldOut + lane * 4) =
-                *reinterpret_cast<const float4*>(stage + r * kTile + chunk * 4);
+            for (int r = 0; r < 32; ++r) {
+                const int chunk = lane ^ (r & 7);
+                *reinterpret_cast<float4*>(tileOut + (size_t)(warp * 32 + r) * ga.ldOut + lane * 4) =
+                    *reinterpret_cast<const float4*>(stage + r * kTile + chunk * 4);
+            }
+        } else {
+            const int c0 = tn * kTile + lane * 4;
+#pragma unroll 2
+            for (int r = 0; r < 32; ++r) {
+                const int gr = tm * kTile + warp * 32 + r;
+                if (gr >= ga.rowsValid) break;
+                const float4 d = *reinterpret_cast<const float4*>(stage + r * kTile + ((lane ^ (r & 7)) * 4));
+                const float dv[4] = {d.x, d.y, d.z, d.w};
+                float* o = tileOut + (size_t)(warp * 32 + r) * ga.ldOut + lane * 4;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (c0 + k < ga.colsValid)
+                        o[k] = ga.beta != 0.f ? fmaf(ga.alpha, dv[k], fmaf(ga.beta, o[k], ga.add))
+                                              : fmaf(ga.alpha, dv[k], ga.add);
+            }
         }
-    } else if (!ADAM) {
+    } else if (MODE == kGemmStore) {
         float* out = tileOut + (size_t)(warp * 32 + lane) * ga.ldOut;
         for (int c = 0; c < kTile; ++c) out[c] = 0.f;
     }
@@ -639,11 +664,11 @@ static int gemm(mpf_mlp* n, const __nv_bfloat16* A, int M, int lda, const __nv_b
     const int kblocks = K / kBK, tiles = (M / kTile) * (N / kTile);
     const int splits = allowSplit ? gemm_splits(tiles, kblocks, n->slots) : 1;
     // per device and cheap: set on every call
-    MPF_CUDA(cudaFuncSetAttribute(k_gemm_nt<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
+    MPF_CUDA(cudaFuncSetAttribute(k_gemm_nt<kGemmStore>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
     GemmArgs ga{kblocks, splits, splits > 1 ? n->part.ptr : out, splits > 1 ? N : ldOut, (size_t)M * N,
                 n->flag.ptr};
     MPF_CHECK(splits == 1 || (size_t)splits * M * N <= n->part.count, MPF_EINVAL, "mlp gemm: split buffer too small");
-    k_gemm_nt<false><<<dim3(M / kTile, N / kTile, splits), 128, kGemmSmem, s>>>(mA, mB, ga, AdamArgs{});
+    k_gemm_nt<kGemmStore><<<dim3(M / kTile, N / kTile, splits), 128, kGemmSmem, s>>>(mA, mB, ga, AdamArgs{});
     MPF_LAUNCHED(1);
     *splitsOut = splits;
     return MPF_OK;
@@ -661,11 +686,11 @@ static int gemm_adam(mpf_mlp* n, const __nv_bfloat16* A, int M, int lda, const _
     CUtensorMap mA, mB;
     MPF_TRY(make_bf16_map(&mA, A, M, lda));
     MPF_TRY(make_bf16_map(&mB, Bm, N, ldb));
-    MPF_CUDA(cudaFuncSetAttribute(k_gemm_nt<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
+    MPF_CUDA(cudaFuncSetAttribute(k_gemm_nt<kGemmAdam>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
     GemmArgs ga{K / kBK, 1, n->g.ptr + off, N, (size_t)M * N, n->flag.ptr};
     ga.w = n->w.ptr + off, ga.m = n->m.ptr + off, ga.v = n->v.ptr + off, ga.wb = n->wb.ptr + off, ga.wt = wt;
     ga.ldT = M;
-    k_gemm_nt<true><<<dim3(N / kTile, M / kTile, 1), 256, kGemmSmem, s>>>(mA, mB, ga, adam);
+    k_gemm_nt<kGemmAdam><<<dim3(N / kTile, M / kTile, 1), 256, kGemmSmem, s>>>(mA, mB, ga, adam);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }
@@ -930,6 +955,56 @@ int mlp_train_step(mpf_mlp* n, int batch, const float* x, int ldx, const int* ro
     const AdamArgs a = next_adam(n, lr, beta1, beta2, eps, weightDecay);
     MPF_TRY(backward(n, batch, x, ldx, rows, target, ldt, tvalid, loss, &a, s));
     return adam(n, a, false, s);
+}
+
+// dst [rowsPad][3 Kp] BF16 from the rows x K FP32 matrix at src (element
+// (r, k) at src[r * srcRow + k * srcCol]): row r holds three K-segments of Kp
+// columns, the BF16 part hi = bf16(x) and the remainder lo = bf16(x - hi) in
+// the order hi, lo, hi (order 0) or hi, hi, lo (order 1); zero outside.  A
+// product of an order-0 and an order-1 matrix is hi.hi + lo.hi + hi.lo.
+__global__ void k_split3(int rows, int rowsPad, int K, int Kp, const float* __restrict__ src, size_t srcRow,
+                         size_t srcCol, int order, __nv_bfloat16* __restrict__ dst) {
+    const size_t total = (size_t)rowsPad * Kp;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / Kp), k = (int)(i % Kp);
+        const float x = (r < rows && k < K) ? src[r * srcRow + k * srcCol] : 0.f;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+        __nv_bfloat16* d = dst + (size_t)r * 3 * Kp + k;
+        d[0] = hi;
+        d[Kp] = order == 0 ? lo : hi;
+        d[2 * Kp] = order == 0 ? hi : lo;
+    }
+}
+
+int split3_bf16(int rows, int rowsPad, int K, int Kp, const float* src, size_t srcRow, size_t srcCol, int order,
+                __nv_bfloat16* dst, cudaStream_t s) {
+    const size_t total = (size_t)rowsPad * Kp;
+    const int blocks = (int)std::min<size_t>((total + 255) / 256, 152 * 16);
+    k_split3<<<blocks, 256, 0, s>>>(rows, rowsPad, K, Kp, src, srcRow, srcCol, order, dst);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+// out (rowsValid x colsValid of ld ldo) = alpha A B^T + beta out + add with
+// A: M x K and B: N x K BF16, both K-major (M, N multiples of 128, K of 64),
+// FP32 accumulation on the tensor cores, no K split.  Raises `flag` if a
+// pipeline wait gave up (the caller reads it).
+int tc_gemm_axpby(const __nv_bfloat16* A, int M, int lda, const __nv_bfloat16* B, int N, int ldb, int K,
+                  float* out, int ldo, int rowsValid, int colsValid, float alpha, float beta, float add, int* flag,
+                  cudaStream_t s) {
+    MPF_CHECK(M % kTile == 0 && N % kTile == 0 && K % kBK == 0 && lda % 8 == 0 && ldb % 8 == 0 &&
+                  rowsValid <= M && colsValid <= N && ldo >= colsValid && flag,
+              MPF_EINVAL, "tensor-core GEMM: M, N %% 128 and K %% 64 must be 0 (M=%d N=%d K=%d)", M, N, K);
+    CUtensorMap mA, mB;
+    MPF_TRY(make_bf16_map(&mA, A, M, lda));
+    MPF_TRY(make_bf16_map(&mB, B, N, ldb));
+    MPF_CUDA(cudaFuncSetAttribute(k_gemm_nt<kGemmAxpby>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
+    GemmArgs ga{K / kBK, 1, out, ldo, 0, flag};
+    ga.alpha = alpha, ga.beta = beta, ga.add = add, ga.rowsValid = rowsValid, ga.colsValid = colsValid;
+    k_gemm_nt<kGemmAxpby><<<dim3(M / kTile, N / kTile, 1), 128, kGemmSmem, s>>>(mA, mB, ga, AdamArgs{});
+    MPF_LAUNCHED(1);
+    return MPF_OK;
 }
 
 // Copy parameters or gradients between the network and a caller device

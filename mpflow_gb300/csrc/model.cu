@@ -656,6 +656,8 @@ static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
     o.preconditioner = 0;
     o.solver = 0;
     o.gn_factor = 0;
+    o.accept_tol = 0.0;
+    o.accept_margin = 0.1;
     if (in) o = *in;
     if (o.preconditioner != 1) o.preconditioner = 0;
     if (o.solver != 1) o.solver = 0;
@@ -665,6 +667,8 @@ static void fill_defaults(const mpf_solve_opts* in, mpf_solve_opts& o, int n) {
     if (o.max_iter <= 0) o.max_iter = 10 * n;
     if (o.max_refine <= 0) o.max_refine = 6;
     if (o.check_every <= 0) o.check_every = 16;
+    if (!(o.accept_tol > o.tol)) o.accept_tol = 0.0;  // only a looser acceptance solve is a saving
+    if (!(o.accept_margin > 0.0) || o.accept_margin >= 1.0) o.accept_margin = 0.1;
 }
 
 int eit_assemble(mpf_eit* m, int F, const float* gamma, bool fp64, cudaStream_t s) {
@@ -705,8 +709,13 @@ static int eit_jacobian(mpf_eit* m, int F, const float* gamma, const int* frameM
 static int ensure_v0(mpf_eit* m, cudaStream_t s);
 
 // Forward solve into the workspace (fields X, voltages V, optional J).
+// skipFrames (device, [F], optional): frames whose fields are kept as they
+// are (not iterated).  reuseSystems: the systems of gamma are already
+// assembled (and the coarse space set up) by the previous call with the same
+// frames, as in the continuation of a looser solve.
 int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_solve_opts* optsIn,
-                   mpf_solve_stats* stats, cudaStream_t s) {
+                   mpf_solve_stats* stats, cudaStream_t s, const int* skipFrames = nullptr,
+                   bool reuseSystems = false) {
     auto t0 = std::chrono::steady_clock::now();
     mpf_solve_opts o;
     fill_defaults(optsIn, o, m->n);
@@ -726,8 +735,9 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     const bool warm = o.warm_start && m->fieldsValid && m->lastFrames == F;
     MPF_CHECK(!(m->fixed && refine), MPF_ENOTSUP,
               "forward solve: FP64 refinement is implemented for current (open) sources only");
+    reuseSystems = reuseSystems && warm && !refine && !m->fixed;
     MPF_TRY(phase_mark(m, MPF_PHASE_ASSEMBLY, s));
-    MPF_TRY(eit_assemble(m, F, gamma, refine, s));
+    if (!reuseSystems) MPF_TRY(eit_assemble(m, F, gamma, refine, s));
     if (m->fixed) MPF_TRY(fixed_prepare(m, F, s));
     MPF_TRY(phase_mark(m, MPF_PHASE_CG_SETUP, s));
     const bool bicg = o.solver == 1;
@@ -736,7 +746,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     const bool coarse = o.preconditioner == 1 && m->coarseOK;
     if (coarse) MPF_TRY(ensure_coarse(m, F));
     CgProblem P = make_problem(m, F, o.tol, coarse, o.solver);
-    if (coarse) {
+    if (coarse && !reuseSystems) {
         CoarsePlan cp{m->nc, m->ncPad, m->cNnz, m->cPairI.ptr, m->cPairJ.ptr, m->cPairPtr.ptr, m->cSlots.ptr,
                       m->cAggSize.ptr};
         MPF_TRY(coarse_launch_setup(P, cp, m->Ac64.ptr, m->infoC.ptr, s, m->Lc.ptr, m->LinvD.ptr, m->Binv.ptr,
@@ -754,6 +764,7 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
             P.sumX0 = m->sumX.ptr;
         }
         MPF_TRY(cg_launch_init(P, !warm, s));
+        if (skipFrames && warm) MPF_TRY(cg_launch_skip(P, skipFrames, s));
         MPF_TRY(run_cg(m, P, o.max_iter, o.check_every, s, &totalIters, &notConv));
     } else {
         const size_t vec = (size_t)P.G * m->npad * m->KP;
@@ -1145,20 +1156,45 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
     int warm = o.warm_start, checkStart = fallback != nullptr;
     if (accepted)
         for (int f = 0; f < F; ++f) accepted[f] = 1;
+    // the acceptance solve at the start's prediction may run at a looser
+    // tolerance (o.accept_tol): frames that pass with the margin are decided
+    // on it, the others continue from their fields to o.tol
+    bool loosePass = checkStart && o.accept_tol > 0.0, reuse = false;
+    if (stats) stats->accepted_loose = 0;
+    // frames whose fields are final (decided, or finished) are not iterated again
+    std::vector<int> skip(F, 0);
+    MPF_TRY(m->skipMask.alloc((size_t)F));
     for (int it = 0;;) {
         mpf_solve_stats fs{};
         mpf_solve_opts oi = o;
         oi.warm_start = warm;
-        int st = eit_forward_ws(m, F, gamma, false, &oi, &fs, s);
+        if (loosePass) oi.tol = o.accept_tol;
+        const bool anySkip = std::find(skip.begin(), skip.end(), 1) != skip.end();
+        if (anySkip) MPF_CUDA(cudaMemcpyAsync(m->skipMask.ptr, skip.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+        int st = eit_forward_ws(m, F, gamma, false, &oi, &fs, s, anySkip ? m->skipMask.ptr : nullptr, reuse);
         if (st != MPF_OK && st != MPF_ENOCONV) return st;
         MPF_TRY(ensure_workspace(m, F, false, true));
         warm = 1;
+        reuse = false;
         cgTotal += fs.iterations;
         MPF_TRY(phase_mark(m, MPF_PHASE_VOLTAGES, s));
         MPF_TRY(fem_launch_residual(F, m->rowsJ, m->Mm, m->Md, vMeas, m->V.ptr, m->y.ptr, m->res.ptr, s));
         MPF_CUDA(cudaMemcpyAsync(res.data(), m->res.ptr, sizeof(double) * F, cudaMemcpyDeviceToHost, s));
         MPF_TRY(phase_mark(m, MPF_PHASE_HOST, s));
         MPF_CUDA(cudaStreamSynchronize(s));
+        if (loosePass) {
+            loosePass = false;
+            int undecided = 0;
+            for (int f = 0; f < F; ++f) {
+                skip[f] = res[f] <= target * (1.0 - o.accept_margin);
+                undecided += !skip[f];
+            }
+            if (stats) stats->accepted_loose = F - undecided;
+            if (undecided) {
+                reuse = true;  // same systems: continue from the fields to o.tol
+                continue;
+            }
+        }
         if (checkStart) {
             checkStart = false;
             std::vector<int> reject(F, 0);
@@ -1191,6 +1227,7 @@ static int gn_loop(mpf_eit* m, int F, float* gamma, const float* vMeas, double l
             live += mask[f];
         }
         if (live == 0 || it == maxIters) break;
+        for (int f = 0; f < F; ++f) skip[f] = !mask[f];
         for (int f = 0; f < F; ++f) iters[f] += mask[f];
         MPF_TRY(phase_mark(m, MPF_PHASE_JACOBIAN, s));
         MPF_CUDA(cudaMemcpyAsync(m->frameMask.ptr, mask.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
@@ -1298,6 +1335,8 @@ int learned_prior(mpf_eit* m, double lambda, cudaStream_t s) {
     m->priorReady = false;
     if (lambda == 0.0) {
         m->priorW.release();
+        m->priorB.release();
+        m->priorA.release();
         return MPF_OK;
     }
     MPF_TRY(ensure_v0(m, s));
@@ -1329,7 +1368,13 @@ int learned_prior(mpf_eit* m, double lambda, cudaStream_t s) {
     MPF_TRY(m->priorW.alloc((size_t)m->Epad * L));
     MPF_TRY(matrix_multiply_scaled(0, 0, m->E, L, R, 1.f, m->J.ptr, m->Epad, Q.ptr, R, 0.f, m->priorW.ptr, m->Epad,
                                    s));
+    // W (column-major E x L) as the B operand of the split-BF16 product
+    m->priorN = round_up(m->E, 128);
+    m->priorLp = round_up(L, 64);
+    MPF_TRY(m->priorB.alloc((size_t)m->priorN * 3 * m->priorLp));
+    MPF_TRY(split3_bf16(m->E, m->priorN, L, m->priorLp, m->priorW.ptr, 1, (size_t)m->Epad, 1, m->priorB.ptr, s));
     MPF_CUDA(cudaStreamSynchronize(s));
+    m->priorW.release();
     m->priorLambda = lambda;
     m->priorReady = true;
     return MPF_OK;
@@ -1341,11 +1386,22 @@ int learned_prior_apply(mpf_eit* m, int F, const float* x, float* out, int ldo, 
     MPF_CHECK(m->priorReady, MPF_EINVAL, "mpf_eit_learned_prior_apply: no prior (call mpf_eit_learned_prior first)");
     MPF_CHECK(F >= 1 && x && out && ldo >= m->E && mode >= -1 && mode <= 1, MPF_EINVAL,
               "mpf_eit_learned_prior_apply: bad arguments");
-    const int L = m->Mm * m->Md;
+    // out = alpha (W x + gamma_h) + beta out as one split-BF16 product on the
+    // tensor cores (hi.hi + lo.hi + hi.lo, FP32 accumulation: about FP32
+    // accuracy) with the update in its epilogue
+    const int L = m->Mm * m->Md, Fp = round_up(F, 128), Lp = m->priorLp;
     const float alpha = mode < 0 ? -1.f : 1.f, beta = mode == 0 ? 0.f : 1.f;
-    MPF_TRY(matrix_multiply_scaled(0, 0, m->E, F, L, alpha, m->priorW.ptr, m->Epad, x, L, beta, out, ldo, s));
-    const float gh = homogeneous_gamma(m);
-    if (gh != 0.f) MPF_TRY(matrix_elementwise(2, m->E, F, out, nullptr, out, ldo, alpha * gh, s));
+    MPF_TRY(m->priorA.alloc((size_t)Fp * 3 * Lp));
+    MPF_TRY(split3_bf16(F, Fp, L, Lp, x, (size_t)L, 1, 0, m->priorA.ptr, s));
+    int* flag = abort_flag_device();
+    MPF_CHECK(flag != nullptr, MPF_ENOMEM, "learned prior: abort flag allocation failed");
+    MPF_TRY(tc_gemm_axpby(m->priorA.ptr, Fp, 3 * Lp, m->priorB.ptr, m->priorN, 3 * Lp, 3 * Lp, out, ldo, F, m->E,
+                          alpha, beta, alpha * homogeneous_gamma(m), flag, s));
+    int aborted = 0;
+    MPF_CUDA(cudaMemcpyAsync(&aborted, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPF_CUDA(cudaStreamSynchronize(s));
+    if (aborted) MPF_CUDA(cudaMemset(flag, 0, sizeof(int)));
+    MPF_CHECK(!aborted, MPF_ETIMEOUT, "mpf_eit_learned_prior_apply: a tensor-core pipeline wait timed out");
     return MPF_OK;
 }
 

@@ -128,6 +128,13 @@ struct HaloPlan {
 void halo_plan(const std::vector<int32_t>& cols, int W, int npad, HaloPlan& out);
 // the pipeline abort flag of the current device (dense_kernels.cu)
 int* abort_flag_device();
+// mlp_kernels.cu: split-BF16 operands and the tensor-core GEMM with an
+// alpha / beta epilogue (used by the learned prior)
+int split3_bf16(int rows, int rowsPad, int K, int Kp, const float* src, size_t srcRow, size_t srcCol, int order,
+                __nv_bfloat16* dst, cudaStream_t s);
+int tc_gemm_axpby(const __nv_bfloat16* A, int M, int lda, const __nv_bfloat16* B, int N, int ldb, int K,
+                  float* out, int ldo, int rowsValid, int colsValid, float alpha, float beta, float add, int* flag,
+                  cudaStream_t s);
 
 // cg_kernels.cu
 // variant v = vecIdx * 3 + rbIdx, floats per lane {4, 2, 1}[vecIdx], row steps {1, 2, 4}[rbIdx]
@@ -176,6 +183,7 @@ int cg_iteration_launches(const CgProblem& P);
 int cg_launch_kernel(const CgProblem& P, int which /*0 spmm, 1 update, 2 direction*/, cudaStream_t s);
 // x += alphaX p on the groups whose last x update is still pending (end of a CG solve)
 int cg_launch_finalize(const CgProblem& P, cudaStream_t s);
+int cg_launch_skip(const CgProblem& P, const int* frameSkip /*[frames] device*/, cudaStream_t s);
 
 // cg_driver.cpp: host drivers shared by single models and batches of meshes.
 // Captured CUDA graphs of CG iteration chunks, keyed by the problems' bytes.

@@ -146,7 +146,7 @@ class SolveOptions:
 
     def __init__(self, tol=1e-6, max_iter=0, refine_tol=0.0, max_refine=6, warm_start=False,
                  check_every=16, preconditioner: str = "jacobi", solver: str = "cg",
-                 gn_factor: str = "fp64"):
+                 gn_factor: str = "fp64", accept_tol: float = 0.0, accept_margin: float = 0.1):
         self.tol, self.max_iter, self.refine_tol = tol, max_iter, refine_tol
         self.max_refine, self.warm_start, self.check_every = max_refine, warm_start, check_every
         if warm_start not in self.WARM_STARTS:
@@ -160,13 +160,16 @@ class SolveOptions:
         if gn_factor not in self.GN_FACTORS:
             raise ValueError(f"gn_factor must be one of {sorted(self.GN_FACTORS)}")
         self.gn_factor = gn_factor
+        # learned Gauss-Newton: tolerance of the acceptance solve and the
+        # margin below the target that decides on it
+        self.accept_tol, self.accept_margin = float(accept_tol), float(accept_margin)
 
     def c(self) -> _ffi.SolveOpts:
         """The options as the C ABI's mpf_solve_opts."""
         return _ffi.SolveOpts(float(self.tol), int(self.max_iter), float(self.refine_tol),
                               int(self.max_refine), self.WARM_STARTS[self.warm_start], int(self.check_every),
                               self.PRECONDITIONERS[self.preconditioner], self.SOLVERS[self.solver],
-                              self.GN_FACTORS[self.gn_factor])
+                              self.GN_FACTORS[self.gn_factor], self.accept_tol, self.accept_margin)
 
 
 def _stream():

@@ -196,6 +196,33 @@ def test_learned_prior_is_the_first_gauss_newton_update():
         model.learned_prior_apply(x)
 
 
+def test_looser_acceptance_solve_keeps_the_decisions():
+    """accept_tol: the solve at the start's prediction runs at a looser CG
+    tolerance, frames below target (1 - margin) are decided on it and skipped
+    afterwards, the others continue to the full tolerance.  On 64 held-out
+    frames from the linear prior (zero network) the accepted flags and the
+    updates per frame equal those of the full-tolerance run and the final
+    residuals stay below the target."""
+    from mpflow_gb300.learned import round_up, zero_network
+    mp, torch, model, mesh, cent, E, Vte, lam = _prior_setup(frames=64)
+    model.learned_prior(lam)
+    F = Vte.shape[0]
+    L = Vte.shape[1] * Vte.shape[2]
+    net0 = zero_network(L, round_up(E, 128))
+    target = 1e-3
+    full = mp.SolveOptions(tol=1e-6, max_iter=4000, warm_start="homogeneous")
+    loose = mp.SolveOptions(tol=1e-6, max_iter=4000, warm_start="homogeneous", accept_tol=1e-4, accept_margin=0.1)
+    _, it_f, res_f, acc_f, st_f = model.gn_solve_learned(net0, Vte, lam, target=target, max_iters=15, options=full)
+    g_l, it_l, res_l, acc_l, st_l = model.gn_solve_learned(net0, Vte, lam, target=target, max_iters=15,
+                                                           options=loose)
+    print(f"accepted {acc_f.sum()}/{F}, decided on the loose solve {st_l.accepted_loose}, "
+          f"CG iterations {st_l.cg_iterations} against {st_f.cg_iterations}")
+    assert np.array_equal(acc_l, acc_f) and np.array_equal(it_l, it_f)
+    assert st_l.frames_converged == st_f.frames_converged == F
+    assert (res_l <= target).all()
+    assert st_l.accepted_loose > 0 and st_f.accepted_loose == 0
+
+
 def test_learned_prior_and_network_save_gauss_newton_updates():
     """With the linear prior, the learned start (prior + a correction trained
     on where Gauss-Newton from the prior converges) needs fewer updates than

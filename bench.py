@@ -693,7 +693,7 @@ def run_gb300(a):
                     "label_s": label_s, "label_converged_fraction": label_conv,
                     "prior": ({"lambda": lam, "setup_s": prior_s,
                                "what": "J0^T (J0 J0^T + mu I)^-1 at the homogeneous point, FP64 Gram/Cholesky, "
-                                       "applied as an FP32 GEMM"} if use_prior else None),
+                                       "applied as a split-BF16 tensor-core product (hi.hi + lo.hi + hi.lo)"} if use_prior else None),
                     "no_update_fraction": learned["no_update_fraction"]},
         "prior_only_gn_batched": prior_only,
         "plain_gn_batched": plain,

@@ -504,44 +504,48 @@ __global__ void k_mirror_lower(int n, double* __restrict__ A, const int* __restr
         if (bi != bj || c > r) M[(size_t)(bj * 32 + r) + (size_t)(bi * 32 + c) * n] = t[c][r];
 }
 
-// r = y - A x for every active frame (A full symmetric, FP64, column-major),
-// and per-block partial sums of |r|^2 and |y|^2 (rr/yy[b][blockIdx.x]).
-// Grid (n / 128, batch), 128 threads, one row each.
-__global__ void __launch_bounds__(128) k_sym_residual(int n, const double* __restrict__ A, const double* __restrict__ x,
+// r = y - A x for the full symmetric FP64 matrices A (n x n per frame), one warp
+// per row (4 rows per warp, 32 per block: every SM keeps many rows' loads in
+// flight), and per block the partial sums of r.r and y.y (n / 32 per frame).
+__global__ void __launch_bounds__(256) k_sym_residual(int n, const double* __restrict__ A, const double* __restrict__ x,
                                                       const double* __restrict__ y, double* __restrict__ r,
                                                       double* __restrict__ rr, double* __restrict__ yy,
                                                       const int* __restrict__ frameMask) {
     const int b = blockIdx.y;
     if (frameMask && !frameMask[b]) return;
-    const int i = blockIdx.x * 128 + threadIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const double* M = A + (size_t)b * n * n;
     const double* xb = x + (size_t)b * n;
-    __shared__ double xs[128];
-    double acc = 0.0;
-    for (int j0 = 0; j0 < n; j0 += 128) {
-        __syncthreads();
-        xs[threadIdx.x] = xb[j0 + threadIdx.x];
-        __syncthreads();
-#pragma unroll 8
-        for (int j = 0; j < 128; ++j) acc = fma(M[(size_t)i + (size_t)(j0 + j) * n], xs[j], acc);
-    }
-    const double yi = y[(size_t)b * n + i];
-    const double ri = yi - acc;
-    r[(size_t)b * n + i] = ri;
-    __shared__ double red[2][128];
-    red[0][threadIdx.x] = ri * ri;
-    red[1][threadIdx.x] = yi * yi;
-    __syncthreads();
-    for (int w = 64; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            red[0][threadIdx.x] += red[0][threadIdx.x + w];
-            red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    __shared__ double red[2][8];
+    double r2 = 0.0, y2 = 0.0;
+    for (int q = 0; q < 4; ++q) {
+        const int i = blockIdx.x * 32 + warp * 4 + q;
+        const double* row = M + (size_t)i * n;
+        double acc = 0.0;
+#pragma unroll 4
+        for (int k = lane; k < n; k += 32) acc = fma(row[k], xb[k], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const double yi = y[(size_t)b * n + i], ri = yi - acc;
+            r[(size_t)b * n + i] = ri;
+            r2 += ri * ri;
+            y2 += yi * yi;
         }
-        __syncthreads();
     }
+    if (lane == 0) {
+        red[0][warp] = r2;
+        red[1][warp] = y2;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        rr[(size_t)b * gridDim.x + blockIdx.x] = red[0][0];
-        yy[(size_t)b * gridDim.x + blockIdx.x] = red[1][0];
+        double s0 = 0.0, s1 = 0.0;
+        for (int w = 0; w < 8; ++w) {
+            s0 += red[0][w];
+            s1 += red[1][w];
+        }
+        rr[(size_t)b * gridDim.x + blockIdx.x] = s0;
+        yy[(size_t)b * gridDim.x + blockIdx.x] = s1;
     }
 }
 
@@ -550,6 +554,134 @@ __global__ void k_add_masked(int n, int batch, double* __restrict__ x, const dou
                              const int* __restrict__ frameMask) {
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)n * batch; t += (size_t)gridDim.x * blockDim.x)
         if (!frameMask || frameMask[t / n]) x[t] += d[t];
+}
+
+// Inverse of the FP32 Cholesky factor, for refinement steps that are two
+// matrix-vector products instead of two latency-bound triangular solves.
+// L is the factor held in FP64 storage (values of the FP32 factor, lower
+// triangle, column-major n x n per frame: L(r, c) at c n + r, as the
+// triangular solves read it); the inverse X = L^-1 is computed in
+// FP32 in 32 x 32 blocks (NB): first the inverse D_b of every diagonal
+// block, then every block column j by forward substitution,
+// X_jj = D_j, X_ij = -D_i sum_{k=j}^{i-1} L_ik X_kj (i > j).
+//
+// One warp per (frame, diagonal block): lane c computes column c of D_b.
+__global__ void __launch_bounds__(32) k_trtri_diag(int n, const double* __restrict__ L, float* __restrict__ D,
+                                                   const int* __restrict__ frameMask) {
+    const int b = blockIdx.x, f = blockIdx.y;
+    if (frameMask && !frameMask[f]) return;
+    __shared__ float Lb[NB][NB + 1];
+    const double* M = L + (size_t)f * n * n + (size_t)(b * NB) * n + b * NB;
+    const int c = threadIdx.x;
+    for (int k = 0; k < NB; ++k) Lb[c][k] = (float)M[(size_t)k * n + c];  // L(c, k), column k coalesced
+    __syncwarp();
+    float x[NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+        float v = i == c ? 1.f : 0.f;
+#pragma unroll
+        for (int k = 0; k < i; ++k) v = fmaf(-Lb[i][k], x[k], v);
+        x[i] = v / Lb[i][i];
+    }
+    float* out = D + ((size_t)f * (n / NB) + b) * NB * NB;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) out[i * NB + c] = x[i];
+}
+
+// L in FP32 (column-major, as the FP64 storage) for the column kernel below.
+__global__ void k_to_f32(size_t count, const double* __restrict__ src, float* __restrict__ dst,
+                         const int* __restrict__ frameMask, size_t per) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count; t += (size_t)gridDim.x * blockDim.x)
+        if (!frameMask || frameMask[t / per]) dst[t] = (float)src[t];
+}
+
+// One block of 256 threads per (frame, block column j): the column's blocks
+// X_ij, i >= j, kept in shared memory as they are formed (the later ones
+// need the earlier), written to X (row-major) and to XT = X^T (row-major, so
+// that the transposed product is also a row-wise one).  X_jj = D_j,
+// X_ij = -D_i sum_{k=j}^{i-1} L_ik X_kj, the L_ik staged one 32 x 32 tile at
+// a time.  Thread t owns row t / 8 and columns 4 (t % 8) .. + 3 of the
+// block in progress.  Measured alternatives, 32 frames of 1024: this order
+// 2.8 ms; right-looking (each block column of L read once per step) 3.7 ms;
+// each thread streaming its row of L from memory without staging 8.4 ms.
+__global__ void __launch_bounds__(256) k_trtri_cols(int n, const float* __restrict__ L, const float* __restrict__ D,
+                                                    float* __restrict__ X, float* __restrict__ XT,
+                                                    const int* __restrict__ frameMask) {
+    const int j = blockIdx.x, f = blockIdx.y, nb = n / NB;
+    if (frameMask && !frameMask[f]) return;
+    extern __shared__ __align__(16) float col[];  // [nb - j][NB][NB]: X_ij, i = j ..
+    __shared__ float Lt[NB][NB + 1], Tt[NB][NB + 1];
+    const float* Lf = L + (size_t)f * n * n;
+    const float* Df = D + (size_t)f * nb * NB * NB;
+    float* Xf = X + (size_t)f * n * n;
+    float* XTf = XT + (size_t)f * n * n;
+    const int t = threadIdx.x, r = t >> 3, c0 = (t & 7) * 4;
+    for (int i = j; i < nb; ++i) {
+        float* Xi = col + (size_t)(i - j) * NB * NB;
+        if (i == j) {
+            for (int e = t; e < NB * NB; e += 256) Xi[e] = Df[(size_t)j * NB * NB + e];
+        } else {
+            // T = sum_k L_ik X_kj
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int k = j; k < i; ++k) {
+                __syncthreads();  // Lt free
+                for (int e = t; e < NB * NB; e += 256) {
+                    const int rr = e % NB, cc = e / NB;  // L(i NB + rr, k NB + cc), column-major
+                    Lt[rr][cc] = Lf[(size_t)(k * NB + cc) * n + i * NB + rr];
+                }
+                __syncthreads();
+                const float* Xk = col + (size_t)(k - j) * NB * NB;
+#pragma unroll 8
+                for (int q = 0; q < NB; ++q) {
+                    const float l = Lt[r][q];
+                    const float4 xv = *reinterpret_cast<const float4*>(Xk + q * NB + c0);
+                    acc[0] = fmaf(l, xv.x, acc[0]);
+                    acc[1] = fmaf(l, xv.y, acc[1]);
+                    acc[2] = fmaf(l, xv.z, acc[2]);
+                    acc[3] = fmaf(l, xv.w, acc[3]);
+                }
+            }
+            __syncthreads();  // Lt and Tt free
+            for (int e = 0; e < 4; ++e) Tt[r][c0 + e] = acc[e];
+            for (int e = t; e < NB * NB; e += 256) Lt[e / NB][e % NB] = Df[(size_t)i * NB * NB + e];  // D_i
+            __syncthreads();
+            // X_ij = -D_i T
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+            for (int q = 0; q < NB; ++q) {
+                const float d = Lt[r][q];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) v[e] = fmaf(d, Tt[q][c0 + e], v[e]);
+            }
+            for (int e = 0; e < 4; ++e) Xi[r * NB + c0 + e] = -v[e];
+        }
+        __syncthreads();  // X_ij complete
+        for (int e = t; e < NB * NB; e += 256) {
+            const int rr = e / NB, cc = e % NB;
+            Xf[(size_t)(i * NB + rr) * n + j * NB + cc] = Xi[rr * NB + cc];
+            XTf[(size_t)(j * NB + rr) * n + i * NB + cc] = Xi[cc * NB + rr];
+        }
+    }
+}
+
+// out[f][i] = sum_k M[f][i][k] v[f][k] over the lower (k <= i) or upper
+// (k >= i) triangle of row i; one warp per row, FP32 products of the FP32
+// matrix with v rounded to FP32, FP64 result.
+__global__ void __launch_bounds__(256) k_tri_rows(int n, const float* __restrict__ M, const double* __restrict__ v,
+                                                  double* __restrict__ out, int upper,
+                                                  const int* __restrict__ frameMask) {
+    const int f = blockIdx.y;
+    if (frameMask && !frameMask[f]) return;
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const float* row = M + (size_t)f * n * n + (size_t)i * n;
+    const double* vf = v + (size_t)f * n;
+    const int k0 = upper ? i : 0, k1 = upper ? n : i + 1;
+    float acc = 0.f;
+    for (int k = k0 + lane; k < k1; k += 32) acc = fmaf(row[k], (float)vf[k], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[(size_t)f * n + i] = (double)acc;
 }
 
 // L_ik = A_ik L_kk^-T for the block rows below the diagonal block k
@@ -1051,14 +1183,37 @@ int dense_mirror_lower(int batch, int n, double* A, cudaStream_t s, const int* f
 
 int dense_sym_residual(int batch, int n, const double* A, const double* x, const double* y, double* r, double* rr,
                        double* yy, cudaStream_t s, const int* frameMask) {
-    MPF_CHECK(n % 128 == 0, MPF_EINVAL, "FP64 residual: n must be a multiple of 128 (got %d)", n);
-    k_sym_residual<<<dim3(n / 128, batch), 128, 0, s>>>(n, A, x, y, r, rr, yy, frameMask);
+    MPF_CHECK(n % 32 == 0, MPF_EINVAL, "FP64 residual: n must be a multiple of 32 (got %d)", n);
+    k_sym_residual<<<dim3(n / 32, batch), 256, 0, s>>>(n, A, x, y, r, rr, yy, frameMask);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }
 
 int dense_add_masked(int batch, int n, double* x, const double* d, cudaStream_t s, const int* frameMask) {
     k_add_masked<<<std::min(1024, (n * batch + 255) / 256), 256, 0, s>>>(n, batch, x, d, frameMask);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
+int dense_trtri32(int batch, int n, const double* L, float* L32, float* D, float* X, float* XT, cudaStream_t s,
+                  const int* frameMask) {
+    MPF_CHECK(n % NB == 0 && n >= NB && n <= 1280, MPF_EINVAL,
+              "FP32 triangular inverse: n must be a multiple of %d in [32, 1280] (got %d)", NB, n);
+    const int nb = n / NB;
+    const size_t per = (size_t)n * n;
+    k_to_f32<<<(int)std::min<size_t>((per * batch + 255) / 256, 152 * 16), 256, 0, s>>>(per * batch, L, L32,
+                                                                                      frameMask, per);
+    k_trtri_diag<<<dim3(nb, batch), 32, 0, s>>>(n, L, D, frameMask);
+    const size_t smem = (size_t)nb * NB * NB * sizeof(float);
+    MPF_CUDA(cudaFuncSetAttribute(k_trtri_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_trtri_cols<<<dim3(nb, batch), 256, smem, s>>>(n, L32, D, X, XT, frameMask);
+    MPF_LAUNCHED(3);
+    return MPF_OK;
+}
+
+int dense_tri_rows(int batch, int n, const float* M, const double* v, double* out, bool upper, cudaStream_t s,
+                   const int* frameMask) {
+    k_tri_rows<<<dim3((n + 7) / 8, batch), 256, 0, s>>>(n, M, v, out, upper ? 1 : 0, frameMask);
     MPF_LAUNCHED(1);
     return MPF_OK;
 }

@@ -73,7 +73,8 @@ struct mpf_eit {
     mpf::DevBuf<double> A64, y, res;
     mpf::DevBuf<int> info, frameMask, redoMask, fbMask, solveMask, upMask, skipMask;
     // FP32 factor of the Gauss-Newton system with FP64 refinement (gn_update)
-    mpf::DevBuf<double> cholL, cholX, cholR, cholY, cholRR, cholYY;
+    mpf::DevBuf<double> cholL, cholX, cholR, cholY, cholRR, cholYY, cholW;
+    mpf::DevBuf<float> cholL32, cholD, cholInv, cholInvT;  // the FP32 factor, its inverse and transpose
     mpf::DevBuf<int> info32, cholMask;
     long long nnz = 0;                // used ELL slots (matrix nonzeros)
     std::vector<int> activeHost, itersHost;

@@ -933,13 +933,18 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
 // instead (FP32 breakdown, stalled or unconverged refinement).  A64's lower
 // triangle is left intact (its upper triangle becomes the mirror image).
 static int gn_solve_fp32(mpf_eit* m, int F, const std::vector<int>& act, std::vector<int>& fb, cudaStream_t s) {
-    const int n = m->rowsJ, nbk = n / 128;
+    const int n = m->rowsJ, nbk = n / 32;  // residual partial sums per 32 rows
     MPF_TRY(m->cholL.alloc((size_t)F * n * n));
     MPF_TRY(m->cholX.alloc((size_t)F * n));
     MPF_TRY(m->cholR.alloc((size_t)F * n));
     MPF_TRY(m->cholY.alloc((size_t)F * n));
     MPF_TRY(m->cholRR.alloc((size_t)F * nbk));
     MPF_TRY(m->cholYY.alloc((size_t)F * nbk));
+    MPF_TRY(m->cholW.alloc((size_t)F * n));
+    MPF_TRY(m->cholD.alloc((size_t)F * n * 32));
+    MPF_TRY(m->cholL32.alloc((size_t)F * n * n));
+    MPF_TRY(m->cholInv.alloc((size_t)F * n * n));
+    MPF_TRY(m->cholInvT.alloc((size_t)F * n * n));
     MPF_TRY(m->info32.alloc((size_t)F));
     MPF_TRY(m->cholMask.alloc((size_t)F));
     MPF_CUDA(cudaMemcpyAsync(m->cholMask.ptr, act.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
@@ -964,6 +969,11 @@ static int gn_solve_fp32(mpf_eit* m, int F, const std::vector<int>& act, std::ve
     }
     if (!any) return MPF_OK;
     MPF_CUDA(cudaMemcpyAsync(m->cholMask.ptr, live.data(), sizeof(int) * F, cudaMemcpyHostToDevice, s));
+    // L^-1 and L^-T in FP32 once, so that every refinement step is two
+    // row-parallel matrix-vector products instead of two triangular solves
+    // (a chain of n / 32 dependent block steps each)
+    MPF_TRY(dense_trtri32(F, n, m->cholL.ptr, m->cholL32.ptr, m->cholD.ptr, m->cholInv.ptr, m->cholInvT.ptr, s,
+                          m->cholMask.ptr));
     // refinement: x += L^-T L^-1 r, r = y - A x, until |r| <= 1e-10 |y| (the
     // split-BF16 Gram itself is accurate to ~1e-5) or the residual stops
     // shrinking; the first check comes after two steps (each step gains
@@ -973,7 +983,8 @@ static int gn_solve_fp32(mpf_eit* m, int F, const std::vector<int>& act, std::ve
     std::vector<double> rr((size_t)F * nbk), yy((size_t)F * nbk), prev(F, 1e300);
     std::vector<int> done(F, 0);
     for (int it = 0; it < kMaxRefine; ++it) {
-        MPF_TRY(dense_cholesky_solve_f64(F, n, m->cholL.ptr, m->cholR.ptr, 1, s, m->cholMask.ptr));
+        MPF_TRY(dense_tri_rows(F, n, m->cholInv.ptr, m->cholR.ptr, m->cholW.ptr, false, s, m->cholMask.ptr));
+        MPF_TRY(dense_tri_rows(F, n, m->cholInvT.ptr, m->cholW.ptr, m->cholR.ptr, true, s, m->cholMask.ptr));
         MPF_TRY(dense_add_masked(F, n, m->cholX.ptr, m->cholR.ptr, s, m->cholMask.ptr));
         MPF_TRY(dense_sym_residual(F, n, m->A64.ptr, m->cholX.ptr, m->cholY.ptr, m->cholR.ptr, m->cholRR.ptr,
                                    m->cholYY.ptr, s, m->cholMask.ptr));
@@ -1040,7 +1051,7 @@ static int gn_update(mpf_eit* m, int F, float* gamma, double lambda, const int* 
     // frames for the FP64 factor: all (gnFactor 0, or n outside the FP32
     // kernel's range) or the FP32 path's fallbacks
     std::vector<int> fb = act;
-    const bool fp32 = gnFactor == 1 && m->rowsJ % 128 == 0 && m->rowsJ <= 1536;
+    const bool fp32 = gnFactor == 1 && m->rowsJ % 128 == 0 && m->rowsJ <= 1280;
     if (fp32) MPF_TRY(gn_solve_fp32(m, F, act, fb, s));
     int nfb = 0;
     for (int f = 0; f < F; ++f) nfb += fb[f];

@@ -331,6 +331,15 @@ int dense_sym_residual(int batch, int n, const double* A, const double* x, const
                        double* yy, cudaStream_t s, const int* frameMask = nullptr);
 // x += d on the masked frames ([batch][n])
 int dense_add_masked(int batch, int n, double* x, const double* d, cudaStream_t s, const int* frameMask = nullptr);
+// X = L^-1 and XT = X^T in FP32 from the FP32 factor L (FP64 storage,
+// column-major lower); L32 receives L in FP32, D the inverted 32 x 32
+// diagonal blocks (batch x n / 32 x 1024); n <= 1280
+int dense_trtri32(int batch, int n, const double* L, float* L32, float* D, float* X, float* XT, cudaStream_t s,
+                  const int* frameMask = nullptr);
+// out = tril(M) v (upper = false) or triu(M) v (upper = true), M FP32 n x n
+// row-major per frame, v and out FP64
+int dense_tri_rows(int batch, int n, const float* M, const double* v, double* out, bool upper, cudaStream_t s,
+                   const int* frameMask = nullptr);
 
 // matrix_ops.cu: C = alpha op(A) op(B) + beta C, column-major FP32
 int matrix_multiply_scaled(int transA, int transB, int m, int n, int k, float alpha, const float* A, int lda,

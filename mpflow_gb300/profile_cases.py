@@ -4,10 +4,11 @@
         assembly (k_assemble) and Jacobian (k_jacobian) of F frames of the
         80-ring, 32-electrode, 8-harmonic model (log conductivity, 1-3
         inclusions), timed with CUDA events (mpf_eit_profile_fem);
-    python -m mpflow_gb300.profile_cases gn --frames 4
-        one Gauss-Newton step from the homogeneous start on F frames of that
-        model (split-BF16 Gram, FP64 Cholesky k_potrf_diag / k_trsm / k_syrk,
-        triangular solves k_chol_solve);
+    python -m mpflow_gb300.profile_cases gn --frames 4 [--gn-factor fp32-refined]
+        Gauss-Newton steps from the homogeneous start on F frames of that
+        model (split-BF16 Gram, FP64 Cholesky k_potrf_diag / k_trsm / k_syrk
+        and triangular solves k_chol_solve, or the FP32 factor with FP64
+        refinement), with the device time per phase;
     python -m mpflow_gb300.profile_cases mlp --steps 20
         training steps (mpf_mlp_train_step) of the 1024-2048-2048-38400
         network on batches of 256 rows gathered from 16384 pairs, timed with
@@ -45,7 +46,7 @@ def case_fem(frames: int, reps: int) -> dict:
             "algorithmic_bytes": [float(by[0]), float(by[1])]}
 
 
-def case_gn(frames: int) -> dict:
+def case_gn(frames: int, gn_factor: str, reps: int) -> dict:
     import torch
     import mpflow_gb300 as mp
     from mpflow_gb300.learned import inclusion_frames
@@ -56,9 +57,20 @@ def case_gn(frames: int) -> dict:
     Vm = model.solve(vt, mp.SolveOptions(tol=1e-6, refine_tol=1e-9)).contiguous()
     _, J0 = model.solve(torch.zeros((1, E), device="cuda"), mp.SolveOptions(tol=1e-6), jacobian=True)
     lam = 2e-2 * float(J0.norm() / np.sqrt(J0.shape[1]))
+    opts = mp.SolveOptions(tol=1e-5, gn_factor=gn_factor)
     g = torch.zeros((frames, E), device="cuda")
-    res = model.gn_step(g, Vm, lam, mp.SolveOptions(tol=1e-5))
-    return {"case": "gn", "frames": frames, "residuals": [float(r) for r in np.asarray(res).ravel()]}
+    res = model.gn_step(g, Vm, lam, opts)  # first step: autotuning and buffers
+    phases = {}
+    for _ in range(reps):
+        g = torch.zeros((frames, E), device="cuda")
+        model.phase_times(True)
+        res = model.gn_step(g, Vm, lam, opts)
+        ph, _ = model.phase_times(False)
+        for k, v in ph.items():
+            phases[k] = phases.get(k, 0.0) + v / reps
+    return {"case": "gn", "frames": frames, "gn_factor": gn_factor,
+            "residuals": [float(r) for r in np.asarray(res).ravel()][:8],
+            "phase_ms": {k: round(v, 3) for k, v in phases.items() if v > 0}}
 
 
 def case_mlp(steps: int) -> dict:
@@ -88,11 +100,12 @@ def main(argv=None) -> None:
     p.add_argument("--frames", type=int, default=4)
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--gn-factor", choices=["fp64", "fp32-refined"], default="fp64")
     a = p.parse_args(argv)
     if a.case == "fem":
         out = case_fem(a.frames, a.reps)
     elif a.case == "gn":
-        out = case_gn(a.frames)
+        out = case_gn(a.frames, a.gn_factor, a.reps)
     else:
         out = case_mlp(a.steps)
     print(json.dumps(out), flush=True)

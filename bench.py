@@ -77,8 +77,9 @@ def parse_args():
                    help="CG preconditioner of every GPU solve (jacobi = the reference's)")
     p.add_argument("--gn-warm-start", choices=["homogeneous", "cold"], default="homogeneous",
                    help="initial fields of each GN solve's first forward solve (and of the training-pair solves)")
-    p.add_argument("--gn-factor", choices=["fp32-refined", "fp64"], default="fp64",
-                   help="factor of J J^T + mu I in every Gauss-Newton update (mpf_solve_opts.gn_factor)")
+    p.add_argument("--gn-factor", choices=["fp32-refined", "fp64"], default="fp32-refined",
+                   help="factor of J J^T + mu I in every Gauss-Newton update (mpf_solve_opts.gn_factor): the FP32 "
+                        "factor with FP64 refinement (FP64 factor where it fails), or the FP64 factor")
     p.add_argument("--accept-tol", type=float, default=0.0,
                    help="CG tolerance of the learned start's acceptance solve in the timed steps "
                         "(mpf_solve_opts.accept_tol; 0: the full tolerance)")
@@ -322,6 +323,7 @@ def workload_config(a, frames):
             "frames_per_step_per_gpu": frames, "target_rel_residual": a.target,
             "target_data": "noise-free held-out frames (60 dB noise only on the training pairs)",
             "lambda_rel": a.lam_rel, "cg_tol": a.tol, "jacobian": "exact 2.5D derivative",
+            "gn_factor": a.gn_factor,
             "l2": "CG working set > L2 (129 MB) at >= 8 frames per step"}
 
 
@@ -662,7 +664,7 @@ def run_gb300(a):
     line = {
         "metric": METRIC, "value": learned["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": learned["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 inner products / refinement / Cholesky, split-BF16 J J^T, "
+        "vs_baseline": None, "dtype": "f32 (FP64 inner products and refinement, FP32 Cholesky refined in FP64, split-BF16 J J^T, "
                                       "BF16 network)",
         "data": "synthetic (seeded inclusion frames; V_meas noise-free from the FP64-refined forward model; "
                 "training pairs from the forward model with 60 dB noise)",

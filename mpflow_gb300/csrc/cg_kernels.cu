@@ -1160,6 +1160,18 @@ __global__ void k_skip_frames(int G, int M, int Ca, const int* __restrict__ fram
     if (g < G && frameSkip[(g / M) / Ca]) active[g] = 0;
 }
 
+// groupMask[g] = 1 for the groups of frames not in frameSkip
+__global__ void k_group_mask(int G, int M, int Ca, const int* __restrict__ frameSkip, int* __restrict__ groupMask) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < G) groupMask[g] = !frameSkip[(g / M) / Ca];
+}
+
+int cg_launch_group_mask(const CgProblem& P, const int* frameSkip, int* groupMask, cudaStream_t s) {
+    k_group_mask<<<(P.G + 255) / 256, 256, 0, s>>>(P.G, P.M, P.Ca, frameSkip, groupMask);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
 int cg_launch_skip(const CgProblem& P, const int* frameSkip, cudaStream_t s) {
     k_skip_frames<<<(P.G + 255) / 256, 256, 0, s>>>(P.G, P.M, P.Ca, frameSkip, P.active);
     MPF_LAUNCHED(1);

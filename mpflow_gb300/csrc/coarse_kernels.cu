@@ -32,8 +32,17 @@ constexpr int kCT = 256;  // threads of k_coarse
 
 // A_c[g][I][J] = sum over the slots of rows in aggregate I whose column lies
 // in aggregate J of (S + alpha R), FP64, fixed order.
-__global__ void k_coarse_assemble(CgProblem P, CoarsePlan cp, double* __restrict__ Ac) {
+// Zero the coarse matrices of the groups in groupMask.
+__global__ void k_zero_groups(size_t per, double* __restrict__ Ac, const int* __restrict__ groupMask) {
     const int g = blockIdx.y;
+    if (!groupMask[g]) return;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < per; t += (size_t)gridDim.x * blockDim.x)
+        Ac[(size_t)g * per + t] = 0.0;
+}
+
+__global__ void k_coarse_assemble(CgProblem P, CoarsePlan cp, double* __restrict__ Ac, const int* __restrict__ groupMask) {
+    const int g = blockIdx.y;
+    if (groupMask && !groupMask[g]) return;
     const int slice = g / P.M, mesh = g - slice * P.M;
     const int f = slice / P.Ca, ci = slice % P.Ca;
     const double alpha = (double)P.alpha[ci];
@@ -53,8 +62,9 @@ __global__ void k_coarse_assemble(CgProblem P, CoarsePlan cp, double* __restrict
 
 // Neumann groups: + c' |I| |J| (the coarse image of c' 1 1^T); padding
 // aggregates get an identity block.
-__global__ void k_coarse_fixup(CgProblem P, CoarsePlan cp, double* __restrict__ Ac) {
+__global__ void k_coarse_fixup(CgProblem P, CoarsePlan cp, double* __restrict__ Ac, const int* __restrict__ groupMask) {
     const int g = blockIdx.y;
+    if (groupMask && !groupMask[g]) return;
     const int slice = g / P.M, mesh = g - slice * P.M;
     const bool dc = P.dcFree[slice % P.Ca] != 0;
     const int nc = cp.meshNc ? cp.meshNc[mesh] : cp.nc;
@@ -76,8 +86,10 @@ __global__ void k_coarse_fixup(CgProblem P, CoarsePlan cp, double* __restrict__ 
 // and the inverses of its 32x32 diagonal blocks.  One warp per (block row,
 // group); lane c inverts column c by forward substitution.
 __global__ void __launch_bounds__(32) k_coarse_prep(int ncPad, const double* __restrict__ L64,
-                                                    float* __restrict__ Lc, float* __restrict__ LinvD) {
+                                                    float* __restrict__ Lc, float* __restrict__ LinvD,
+                                                    const int* __restrict__ groupMask) {
     const int bi = blockIdx.x, g = blockIdx.y, lane = threadIdx.x;
+    if (groupMask && !groupMask[g]) return;
     const double* L = L64 + (size_t)g * ncPad * ncPad;
     float* Lf = Lc + (size_t)g * ncPad * ncPad;
     for (int r = 0; r < 32; ++r) {
@@ -171,13 +183,15 @@ __device__ void coarse_solve(const float* __restrict__ L, const float* __restric
 // Setup: columns [32 * blockIdx.x, +32) of (P^T A P)^-1 by triangular solves
 // on identity columns; Binv is row-major and symmetric up to rounding.
 __global__ void __launch_bounds__(kCT) k_coarse_inverse(int ncPad, const float* __restrict__ Lc,
-                                                        const float* __restrict__ LinvD, float* __restrict__ Binv) {
+                                                        const float* __restrict__ LinvD, float* __restrict__ Binv,
+                                                        const int* __restrict__ groupMask) {
     constexpr int YS = 33;
     extern __shared__ float smc[];
     float* y = smc;
     float* tmp = y + (size_t)ncPad * YS;
     float(*Ls)[33] = reinterpret_cast<float(*)[33]>(tmp + 32 * YS);
     const int g = blockIdx.y, col0 = blockIdx.x * 32;
+    if (groupMask && !groupMask[g]) return;
     for (int t = threadIdx.x; t < ncPad * 32; t += kCT) y[(t / 32) * YS + t % 32] = (t / 32 == col0 + t % 32) ? 1.f : 0.f;
     __syncthreads();
     coarse_solve<32>(Lc + (size_t)g * ncPad * ncPad, LinvD + (size_t)g * (ncPad / 32) * 1024, ncPad, y, tmp, Ls);
@@ -377,11 +391,17 @@ int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count) 
 }
 
 int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,
-                        float* Lc, float* LinvD, float* Binv, double* L64) {
+                        float* Lc, float* LinvD, float* Binv, double* L64, const int* groupMask) {
     const size_t per = (size_t)cp.ncPad * cp.ncPad;
-    MPF_CUDA(cudaMemsetAsync(Ac64, 0, sizeof(double) * per * P.G, s));
-    k_coarse_assemble<<<dim3(std::min((cp.nnz + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64);
-    k_coarse_fixup<<<dim3((int)std::min<size_t>((per + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64);
+    if (!groupMask) {
+        MPF_CUDA(cudaMemsetAsync(Ac64, 0, sizeof(double) * per * P.G, s));
+    } else {
+        k_zero_groups<<<dim3((int)std::min<size_t>((per + 255) / 256, 1024), P.G), 256, 0, s>>>(per, Ac64, groupMask);
+        MPF_LAUNCHED(1);
+    }
+    k_coarse_assemble<<<dim3(std::min((cp.nnz + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64, groupMask);
+    k_coarse_fixup<<<dim3((int)std::min<size_t>((per + 255) / 256, 1024), P.G), 256, 0, s>>>(P, cp, Ac64,
+                                                                                           groupMask);
     MPF_LAUNCHED(2);
     // The coarse operator is applied in FP32 (Binv), so its factor is taken
     // in FP32 arithmetic, one CTA per group, into L64; a group whose FP32
@@ -393,7 +413,7 @@ int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, 
     const double* Lsrc = Ac64;
     std::vector<int> jacobiOnly;
     if (L64) {
-        MPF_TRY(dense_potrf32(P.G, cp.ncPad, Ac64, L64, info, s));
+        MPF_TRY(dense_potrf32(P.G, cp.ncPad, Ac64, L64, info, s, groupMask));
         std::vector<int> h(P.G), redo(P.G, 0);
         MPF_CUDA(cudaMemcpyAsync(h.data(), info, sizeof(int) * P.G, cudaMemcpyDeviceToHost, s));
         MPF_CUDA(cudaStreamSynchronize(s));
@@ -414,9 +434,9 @@ int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, 
         }
         Lsrc = L64;
     } else {
-        MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s));
+        MPF_TRY(dense_cholesky_f64(P.G, cp.ncPad, Ac64, info, s, groupMask));
     }
-    k_coarse_prep<<<dim3(cp.ncPad / 32, P.G), 32, 0, s>>>(cp.ncPad, Lsrc, Lc, LinvD);
+    k_coarse_prep<<<dim3(cp.ncPad / 32, P.G), 32, 0, s>>>(cp.ncPad, Lsrc, Lc, LinvD, groupMask);
     const size_t smem = coarse_solve_smem(cp.ncPad);
     static std::atomic<size_t> configured[64];
     int dev = 0;
@@ -426,7 +446,7 @@ int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, 
         MPF_CUDA(cudaFuncSetAttribute(k_coarse_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured[dev].store(smem);
     }
-    k_coarse_inverse<<<dim3(cp.ncPad / 32, P.G), kCT, smem, s>>>(cp.ncPad, Lc, LinvD, Binv);
+    k_coarse_inverse<<<dim3(cp.ncPad / 32, P.G), kCT, smem, s>>>(cp.ncPad, Lc, LinvD, Binv, groupMask);
     MPF_LAUNCHED(2);
     for (int g : jacobiOnly) {
         MPF_CUDA(cudaMemsetAsync(Binv + per * g, 0, sizeof(float) * per, s));

@@ -71,7 +71,7 @@ struct mpf_eit {
     mpf::DevBuf<float> V, J, gramWork;
     mpf::DevBuf<__nv_bfloat16> Jhi, Jlo;
     mpf::DevBuf<double> A64, y, res;
-    mpf::DevBuf<int> info, frameMask, redoMask, fbMask, solveMask, upMask, skipMask;
+    mpf::DevBuf<int> info, frameMask, redoMask, fbMask, solveMask, upMask, skipMask, groupMask;
     // FP32 factor of the Gauss-Newton system with FP64 refinement (gn_update)
     mpf::DevBuf<double> cholL, cholX, cholR, cholY, cholRR, cholYY, cholW;
     mpf::DevBuf<float> cholL32, cholD, cholInv, cholInvT;  // the FP32 factor, its inverse and transpose

@@ -749,8 +749,16 @@ int eit_forward_ws(mpf_eit* m, int F, const float* gamma, bool wantJ, const mpf_
     if (coarse && !reuseSystems) {
         CoarsePlan cp{m->nc, m->ncPad, m->cNnz, m->cPairI.ptr, m->cPairJ.ptr, m->cPairPtr.ptr, m->cSlots.ptr,
                       m->cAggSize.ptr};
+        // frames left out of the solve keep the coarse space of their
+        // previous (warm) solve
+        const int* groupMask = nullptr;
+        if (skipFrames && warm && !refine) {
+            MPF_TRY(m->groupMask.alloc((size_t)P.G));
+            MPF_TRY(cg_launch_group_mask(P, skipFrames, m->groupMask.ptr, s));
+            groupMask = m->groupMask.ptr;
+        }
         MPF_TRY(coarse_launch_setup(P, cp, m->Ac64.ptr, m->infoC.ptr, s, m->Lc.ptr, m->LinvD.ptr, m->Binv.ptr,
-                                    m->Lc64.ptr));
+                                    m->Lc64.ptr, groupMask));
     }
     MPF_TRY(phase_mark(m, MPF_PHASE_CG, s));
     int totalIters = 0, notConv = 0, refinements = 0;

@@ -169,9 +169,11 @@ struct CoarsePlan {
 };
 // Lc [G][ncPad][ncPad], LinvD [G][ncPad/32][1024]: FP32 factor scratch; Binv: the inverse (P.Binv);
 // L64 [G][ncPad][ncPad]: the factor taken in FP32 arithmetic (FP64 factor in
-// place of Ac64 where it breaks down; null: FP64 only); info: 2 * G ints
+// place of Ac64 where it breaks down; null: FP64 only); info: 2 * G ints;
+// groupMask (device, [G], optional): only these groups are set up (the
+// others keep their coarse space, e.g. frames left out of a solve)
 int coarse_launch_setup(const CgProblem& P, const CoarsePlan& cp, double* Ac64, int* info, cudaStream_t s,
-                        float* Lc, float* LinvD, float* Binv, double* L64);
+                        float* Lc, float* LinvD, float* Binv, double* L64, const int* groupMask = nullptr);
 // `count`: false while recording a CUDA graph (replays are counted by the caller)
 int cg_launch_coarse(const CgProblem& P, bool init, cudaStream_t s, bool count = true);
 bool coarse_supported(int KP, int ncPad);
@@ -184,6 +186,7 @@ int cg_launch_kernel(const CgProblem& P, int which /*0 spmm, 1 update, 2 directi
 // x += alphaX p on the groups whose last x update is still pending (end of a CG solve)
 int cg_launch_finalize(const CgProblem& P, cudaStream_t s);
 int cg_launch_skip(const CgProblem& P, const int* frameSkip /*[frames] device*/, cudaStream_t s);
+int cg_launch_group_mask(const CgProblem& P, const int* frameSkip, int* groupMask /*[G] device*/, cudaStream_t s);
 
 // cg_driver.cpp: host drivers shared by single models and batches of meshes.
 // Captured CUDA graphs of CG iteration chunks, keyed by the problems' bytes.

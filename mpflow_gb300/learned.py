@@ -287,11 +287,14 @@ def train_warm_start(model, net: MLP, V, gamma, epochs: int = 60, batch: int = 2
     if prior and getattr(model, "prior_lambda", None) is None:
         raise ValueError("prior=True needs the model's linear prior (EIT.learned_prior)")
     losses = []
-    # first use of the random-number and permutation kernels loads them
-    # (seconds on a fresh process): outside the timed loop
+    # the first use of the random-number and permutation kernels at these
+    # sizes loads them (seconds on a fresh process): outside the timed loop,
+    # with a generator of its own so the training draws are unchanged
     warm = torch.Generator(device=V.device)
-    torch.randn(16, device=V.device, generator=warm)
-    torch.randperm(16, device=V.device, generator=warm)
+    warm.manual_seed(seed + 1)
+    if snr_db is not None:
+        add_noise(V, snr_db, warm)
+    torch.randperm(N, device=V.device, generator=warm)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     step = 0

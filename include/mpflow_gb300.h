@@ -266,6 +266,13 @@ int mpf_eit_forward(mpf_eit_t model, int32_t frames, const float* gamma, float* 
  * (drive_count + meas_count). */
 int mpf_eit_fields(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t stream);
 
+/* Complex potential fields of the last mpf_eit_forward_complex call, same
+ * layout as mpf_eit_fields with interleaved (re, im) float pairs: fields
+ * holds frames x components x data_rows x (drive_count + meas_count)
+ * complex values (the reference's EIT::fields of its complex
+ * instantiations, src/models/eit.cpp:152-180). */
+int mpf_eit_fields_complex(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t stream);
+
 /* EIT::solve for complex material values: the reference's
  * models::EIT<..., FEM::Equation<thrust::complex<float>, ...>> instantiations
  * (src/models/eit.cpp:289-304).  p(gamma) = ref * gamma or

@@ -1128,7 +1128,7 @@ public:
                                                sizeof(dataType) * Mm, sizeof(dataType) * Mm, Md,
                                                cudaMemcpyDeviceToDevice, stream),
                              "mpFlow::models::EIT::solve");
-                fieldsValid_ = !detail::is_complex<dataType>::value;
+                fieldsValid_ = true;
             }
             cudaFreeAsync(V, stream);
         } else {
@@ -1141,24 +1141,23 @@ public:
         return result;
     }
 
-    // potentials of the last solve, one matrix per 2.5D component
+    // potentials of the last solve, one matrix per 2.5D component (complex
+    // for the complex instantiations)
     void updateFields(cudaStream_t const stream) {
-        if (detail::is_complex<dataType>::value)
-            throw std::logic_error("mpFlow::models::EIT::updateFields: not available for complex models");
         if (!fieldsValid_) throw std::logic_error("mpFlow::models::EIT::updateFields: no solve yet");
+        typedef detail::lib_type<dataType> L;
         const size_t per = (size_t)fields[0]->dataRows * fields[0]->cols;  // export layout: dataRows x cols per component
-        float* buf = nullptr;
-        detail::cuda(cudaMallocAsync((void**)&buf, sizeof(float) * per * fields.size(), stream), "updateFields");
-        const int st = mpf_eit_fields(model_, 1, buf, stream);
+        L* buf = nullptr;
+        detail::cuda(cudaMallocAsync((void**)&buf, sizeof(L) * per * fields.size(), stream), "updateFields");
+        int st;
+        if constexpr (detail::is_complex<dataType>::value)
+            st = mpf_eit_fields_complex(model_, 1, reinterpret_cast<float*>(buf), stream);
+        else
+            st = mpf_eit_fields(model_, 1, buf, stream);
         if (st == MPF_OK)
-            for (size_t c = 0; c < fields.size(); ++c) {
-                if constexpr (detail::lib_native<dataType>())
-                    cudaMemcpyAsync(fields[c]->deviceData, buf + c * per, sizeof(float) * per, cudaMemcpyDeviceToDevice,
-                                    stream);
-                else if constexpr (!detail::is_complex<dataType>::value)  // double fields from FP32 potentials
-                    detail::convert_device(fields[c]->deviceData, buf + c * per, per, stream,
-                                           "mpFlow::models::EIT::updateFields");
-            }
+            for (size_t c = 0; c < fields.size(); ++c)  // double / complex<double>: from the FP32 potentials
+                detail::convert_device(fields[c]->deviceData, buf + c * per, per, stream,
+                                       "mpFlow::models::EIT::updateFields");
         cudaFreeAsync(buf, stream);
         detail::check(st, "mpFlow::models::EIT::updateFields");
         detail::cuda(cudaStreamSynchronize(stream), "updateFields");
@@ -1229,7 +1228,7 @@ private:
                          where);
             cudaFreeAsync(Vd, stream);
             detail::convert_device(jacobian->deviceData, Jl, nJ, stream, where);
-            fieldsValid_ = !detail::is_complex<dataType>::value;
+            fieldsValid_ = true;
         }
         cudaFreeAsync(V, stream);
         cudaFreeAsync(g, stream);

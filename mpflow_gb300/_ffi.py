@@ -94,6 +94,7 @@ SIGNATURES = {
     "mpf_eit_assemble": (_I, [_P, _I, _P, _P, _P, _P]),
     "mpf_eit_forward": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P]),
     "mpf_eit_fields": (_I, [_P, _I, _P, _P]),
+    "mpf_eit_fields_complex": (_I, [_P, _I, _P, _P]),
     "mpf_eit_forward_complex": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _P]),
     "mpf_gn_step": (_I, [_P, _I, _P, _P, _D, ctypes.POINTER(SolveOpts), _P, ctypes.POINTER(SolveStats), _P]),
     "mpf_gn_solve": (_I, [_P, _I, _P, _P, _D, _D, _I, ctypes.POINTER(SolveOpts), _P, _P,

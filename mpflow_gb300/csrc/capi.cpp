@@ -43,6 +43,7 @@ int eit_assemble_export(mpf_eit* m, int F, const float* gamma, float* sOut, floa
 int eit_forward(mpf_eit* m, int F, const float* gamma, float* V, float* Jref, const mpf_solve_opts* o,
                 mpf_solve_stats* stats, cudaStream_t s);
 int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s);
+int eit_fields_complex(mpf_eit* m, int F, float* out, cudaStream_t s);
 int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, float* Jref, const mpf_solve_opts* optsIn,
                         mpf_solve_stats* stats, cudaStream_t s);
 int gn_step(mpf_eit* m, int F, float* gamma, const float* vMeas, double lambda, const mpf_solve_opts* o,
@@ -248,6 +249,13 @@ int mpf_eit_fields(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t 
     MPF_GUARD({
         MPF_CHECK(model, MPF_EINVAL, "mpf_eit_fields: model == nullptr");
         return mpf::eit_fields(model, frames, fields, (cudaStream_t)stream);
+    })
+}
+
+int mpf_eit_fields_complex(mpf_eit_t model, int32_t frames, float* fields, mpf_stream_t stream) {
+    MPF_GUARD({
+        MPF_CHECK(model, MPF_EINVAL, "mpf_eit_fields_complex: model == nullptr");
+        return mpf::eit_fields_complex(model, frames, fields, (cudaStream_t)stream);
     })
 }
 

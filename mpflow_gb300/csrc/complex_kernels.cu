@@ -694,6 +694,41 @@ int cg_launch_zdc_shift(const CgProblem& P, const double* shift, float sign, cud
     return MPF_OK;
 }
 
+// Complex potentials in the reference layout (EIT::fields): as
+// k_fields_export, with interleaved (re, im) pairs.
+__global__ void k_zfields_export(int F, int Ca, int C, const int32_t* __restrict__ compOf, int npad, int KP,
+                                 int dataRows, int cols, const int32_t* __restrict__ colU,
+                                 const float* __restrict__ colScale, const float* __restrict__ betaC,
+                                 const float* __restrict__ Xz, const int32_t* __restrict__ rowOf,
+                                 float* __restrict__ out, int n) {
+    const size_t per = (size_t)dataRows * cols;
+    const size_t total = (size_t)F * C * per;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int f = (int)(i / ((size_t)C * per));
+        const int c = (int)((i / per) % C);
+        const size_t r = i % per;
+        const int node = (int)(r % dataRows), col = (int)(r / dataRows);
+        const int ci = compOf[c];
+        float2 v = make_float2(0.f, 0.f);
+        if (ci >= 0 && node < n) {
+            const float sc = betaC[c] * colScale[col];
+            const float2 x = *reinterpret_cast<const float2*>(
+                Xz + 2 * ((((size_t)f * Ca + ci) * npad + rowOf[node]) * KP + colU[col]));
+            v = make_float2(sc * x.x, sc * x.y);
+        }
+        *reinterpret_cast<float2*>(out + 2 * i) = v;
+    }
+}
+
+int fem_launch_zfields_export(int F, int Ca, int C, const int32_t* compOf, int npad, int KP, int dataRows, int cols,
+                              int n, const int32_t* colU, const float* colScale, const float* betaC, const float* Xz,
+                              const int32_t* rowOf, float* out, cudaStream_t s) {
+    k_zfields_export<<<2048, 256, 0, s>>>(F, Ca, C, compOf, npad, KP, dataRows, cols, colU, colScale, betaC, Xz,
+                                          rowOf, out, n);
+    MPF_LAUNCHED(1);
+    return MPF_OK;
+}
+
 int fem_launch_zgram_meas(int G, int KP, int npad, const int32_t* nzPtr, const int32_t* nzNode, const double* nzVal,
                           const float* Xz, double* Gmz, cudaStream_t s) {
     k_zgram_meas<<<G, 256, 0, s>>>(KP, npad, nzPtr, nzNode, nzVal, Xz, Gmz);

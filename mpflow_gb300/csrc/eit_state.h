@@ -81,6 +81,8 @@ struct mpf_eit {
     int* pinnedActive = nullptr;
     bool fieldsValid = false;
     int lastFrames = 0;
+    bool zFieldsValid = false;  // complex fields of the last complex solve
+    int zLastFrames = 0;
     // captured CG iteration chunks keyed by the problem bytes
     std::map<std::string, cudaGraphExec_t> graphs;
     // CG kernel variants {spmm, update, direction}: autotuned per frame count,

@@ -888,6 +888,8 @@ int eit_forward_complex(mpf_eit* m, int F, const float* gamma, float* Vout, floa
     MPF_TRY(cg_launch_init(P, true, s));
     MPF_TRY(run_cg(m, P, o.max_iter, o.check_every, s, &iters, &notConv));
     if (m->anyDcFree) MPF_TRY(cg_launch_zdc_shift(P, m->dcShift.ptr, 1.f, s));
+    m->zFieldsValid = true;
+    m->zLastFrames = F;
     MPF_TRY(fem_launch_zgram_meas(P.G, m->KP, m->npad, m->nzPtr.ptr, m->nzNode.ptr, m->nzVal.ptr, m->Xz.ptr,
                                   m->Gmz.ptr, s));
     MPF_TRY(fem_launch_zvoltages(F, m->Ca, m->KP, m->Mm, m->Md, m->Gmz.ptr, m->beta.ptr, m->measU.ptr,
@@ -932,6 +934,16 @@ int eit_fields(mpf_eit* m, int F, float* out, cudaStream_t s) {
     MPF_TRY(fem_launch_fields_export(F, m->Ca, m->C, m->compOfD.ptr, m->npad, m->KP, m->dataRows, m->Md + m->Mm,
                                      m->nNodes, m->colU.ptr, m->colScale.ptr, m->betaC.ptr, m->X.ptr, m->rowOf.ptr, out,
                                      s));
+    return MPF_OK;
+}
+
+int eit_fields_complex(mpf_eit* m, int F, float* out, cudaStream_t s) {
+    MPF_TRY(check_device(m));
+    MPF_CHECK(m->zFieldsValid && F >= 1 && F <= m->zLastFrames && out, MPF_EINVAL,
+              "mpf_eit_fields_complex: no complex forward solve with that many frames");
+    MPF_TRY(fem_launch_zfields_export(F, m->Ca, m->C, m->compOfD.ptr, m->npad, m->KP, m->dataRows, m->Md + m->Mm,
+                                      m->nNodes, m->colU.ptr, m->colScale.ptr, m->betaC.ptr, m->Xz.ptr,
+                                      m->rowOf.ptr, out, s));
     return MPF_OK;
 }
 

@@ -222,6 +222,9 @@ int zbicgstab_launch_iteration(const CgProblem& P, cudaStream_t s);
 int fem_launch_zassemble(int F, int W, int npad, int E, const int32_t* cptr, const int32_t* contrib, const float* Kf,
                          const float* Mf, const float* gamma2, float ref, int logarithmic, float4* SRz, cudaStream_t s);
 int cg_launch_zdc_shift(const CgProblem& P, const double* shift, float sign, cudaStream_t s);
+int fem_launch_zfields_export(int F, int Ca, int C, const int32_t* compOf, int npad, int KP, int dataRows, int cols,
+                              int n, const int32_t* colU, const float* colScale, const float* betaC, const float* Xz,
+                              const int32_t* rowOf, float* out, cudaStream_t s);
 int fem_launch_zgram_meas(int G, int KP, int npad, const int32_t* nzPtr, const int32_t* nzNode, const double* nzVal,
                           const float* Xz, double* Gmz, cudaStream_t s);
 int fem_launch_zvoltages(int F, int Ca, int KP, int Mm, int Md, const double* Gmz, const float* beta,

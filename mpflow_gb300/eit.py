@@ -314,6 +314,16 @@ class EIT:
         check(lib().mpf_eit_fields(self._h, frames, ptr(out), _stream()))
         return out
 
+    def fields_complex(self, frames: int):
+        """Complex potentials of the last solve_complex: (frames, components,
+        Md+Mm, data_rows) complex64 (mpf_eit_fields_complex)."""
+        import torch
+        dr = self.info["data_rows"]
+        cols = self.info["drive_count"] + self.info["meas_count"]
+        out = torch.empty((frames, self.components, cols, dr), dtype=torch.complex64, device="cuda")
+        check(lib().mpf_eit_fields_complex(self._h, frames, ptr(out), _stream()))
+        return out
+
     def gn_step(self, gamma, v_meas, lam: float, options: SolveOptions | None = None):
         """One regularised Gauss-Newton step in place on gamma; returns the
         relative data residual of each frame before the step."""

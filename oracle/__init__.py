@@ -581,14 +581,16 @@ def calc_jacobian_complex(s: Setup, phi: np.ndarray, gamma: np.ndarray) -> np.nd
     return J
 
 
-def eit_forward_complex(s: Setup, gamma: np.ndarray, want_jacobian: bool = False):
+def eit_forward_complex(s: Setup, gamma: np.ndarray, want_jacobian: bool = False, want_fields: bool = False):
     """Restatement of EIT::solve for complex material values (the
     Equation<thrust::complex<T>> instantiations, src/models/eit.cpp:139-245
     and :289-304; p(gamma) of src/fem/equation_kernel.cu:35-43 with complex
     gamma), current sources.  The complex systems are solved directly in FP64
     (the reference iterates to the same solution); the Neumann harmonic is
     (A + 1 1^T) x = b as in the reference's CG.  Returns V (Mm x Md, complex)
-    and, with want_jacobian, (V, J) with J = -h sum_c J_c (rowsJ x E)."""
+    and, with want_jacobian, (V, J) with J = -h sum_c J_c (rowsJ x E); with
+    want_fields the list of n x (Md + Mm) complex fields per component is
+    appended to the returned tuple."""
     g = np.asarray(gamma, np.complex128)
     p = s.ref * (np.exp(math.log(10.0) * g / 10.0) if s.logarithmic else g)
     S = (update_matrix(s.layout, s.layout.elemS, p.real, 1.0, False) +
@@ -600,6 +602,7 @@ def eit_forward_complex(s: Setup, gamma: np.ndarray, want_jacobian: bool = False
     att = s.meas.T @ s.exc.T
     V = np.zeros((s.Mm, s.Md), np.complex128)
     J = np.zeros((s.rowsJ, s.elements.shape[0]), np.complex128) if want_jacobian else None
+    fields = []
     for c in range(s.components):
         alpha, beta = s.alpha_beta(c)
         sys_re = update_system_matrix(s.layout, S.real.copy(), R.real.copy(), alpha)
@@ -608,9 +611,11 @@ def eit_forward_complex(s: Setup, gamma: np.ndarray, want_jacobian: bool = False
         if c == 0:
             A = A + 1.0
         x = np.linalg.solve(A, (s.exc @ pattern) * beta)
+        fields.append(x)
         V += att @ x[:, :s.Md]
         if want_jacobian:
             J += calc_jacobian_complex(s, x, g)
-    if want_jacobian:
-        return V, -s.height * J
-    return V
+    out = (V, -s.height * J) if want_jacobian else (V,)
+    if want_fields:
+        out = out + (fields,)
+    return out if len(out) > 1 else out[0]

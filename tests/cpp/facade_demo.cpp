@@ -135,13 +135,11 @@ wide_case(unsigned rings, unsigned L, T inclusion, T background, std::vector<T>*
     auto V0 = solver->calculation[0];
     *V = device_values(V0->deviceData, (size_t)V0->dataRows * V0->cols);
     *J = device_values(model->jacobian->deviceData, (size_t)model->jacobian->dataRows * E);
-    if (!detail::is_complex<T>::value) {
-        model->updateFields(stream);
-        F->clear();
-        for (auto const& f : model->fields) {
-            auto h = device_values(f->deviceData, (size_t)f->dataRows * f->cols);
-            F->insert(F->end(), h.begin(), h.end());
-        }
+    model->updateFields(stream);
+    F->clear();
+    for (auto const& f : model->fields) {
+        auto h = device_values(f->deviceData, (size_t)f->dataRows * f->cols);
+        F->insert(F->end(), h.begin(), h.end());
     }
     auto Vt = model->solve(target, handle, stream);
     solver->measurement[0]->copy(Vt, stream);
@@ -164,18 +162,19 @@ static int wide(unsigned rings, unsigned L) {
     wide_case<cfloat>(rings, L, cfloat(0.5f, 0.3f), cfloat(1.f, 0.15f), &Vz, &Jz, &Fz, &Sz);
     wide_case<cdouble>(rings, L, cdouble(0.5, 0.3), cdouble(1.0, 0.15), &Vw, &Jw, &Fw, &Sw);
     const double dv = rel_diff(Vd, Vf), dj = rel_diff(Jd, Jf), df = rel_diff(Fd, Ff), ds = rel_diff(Sd, Sf);
-    const double zv = rel_diff(Vw, Vz), zj = rel_diff(Jw, Jz), zs = rel_diff(Sw, Sz);
+    const double zv = rel_diff(Vw, Vz), zj = rel_diff(Jw, Jz), zs = rel_diff(Sw, Sz), zf = rel_diff(Fw, Fz);
     double sMin = 1e300;
     for (double v : Sd) sMin = std::min(sMin, v);
     const bool sizes = Vd.size() == Vf.size() && Jd.size() == Jf.size() && Fd.size() == Ff.size() && !Fd.empty() &&
                        Sd.size() == Sf.size() && Vw.size() == Vz.size() && Jw.size() == Jz.size() &&
-                       Sw.size() == Sz.size();
+                       Sw.size() == Sz.size() && Fw.size() == Fz.size() && !Fz.empty();
     const bool ok = sizes && dv <= 1e-5 && dj <= 1e-5 && df <= 1e-5 && ds <= 1e-5 && zv <= 1e-5 && zj <= 1e-5 &&
-                    zs <= 1e-5 && sMin < 1.0;
+                    zs <= 1e-5 && zf <= 1e-5 && sMin < 1.0;
     printf("{\"double_v\": %.3e, \"double_j\": %.3e, \"double_fields\": %.3e, \"double_sigma\": %.3e, "
-           "\"cdouble_v\": %.3e, \"cdouble_j\": %.3e, \"cdouble_sigma\": %.3e, \"fields_values\": %zu, "
+           "\"cdouble_v\": %.3e, \"cdouble_j\": %.3e, \"cdouble_sigma\": %.3e, \"cdouble_fields\": %.3e, "
+           "\"fields_values\": %zu, "
            "\"sigma_min\": %.6f, \"ok\": %s}\n",
-           dv, dj, df, ds, zv, zj, zs, Fd.size(), sMin, ok ? "true" : "false");
+           dv, dj, df, ds, zv, zj, zs, zf, Fd.size(), sMin, ok ? "true" : "false");
     return ok ? 0 : 1;
 }
 

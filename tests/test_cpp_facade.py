@@ -189,12 +189,14 @@ def test_facade_double_and_complex_double_match_float(tmp_path):
     complex<double> (the reference instantiates both natively,
     src/models/eit.cpp:273-304) against float and complex<float> on the same
     mesh and inputs: voltages (padded result layout), Jacobian (dataRows x
-    E), fields after updateFields (two 2.5D components) and a
-    solveDifferential reconstruction agree within 1e-5 relative."""
+    E), fields after updateFields (two 2.5D components, complex for the
+    complex types) and a solveDifferential reconstruction agree within 1e-5
+    relative."""
     exe = _build(tmp_path)
     r = subprocess.run([exe, "wide", "16", "16"], capture_output=True, text=True, timeout=300)
     out = json.loads(r.stdout.strip().splitlines()[-1])
     assert r.returncode == 0 and out["ok"], (r.stdout, r.stderr)
-    for k in ("double_v", "double_j", "double_fields", "double_sigma", "cdouble_v", "cdouble_j", "cdouble_sigma"):
+    for k in ("double_v", "double_j", "double_fields", "double_sigma", "cdouble_v", "cdouble_j", "cdouble_sigma",
+              "cdouble_fields"):
         assert out[k] <= 1e-5, (k, out)
     assert out["fields_values"] > 0 and out["sigma_min"] < 1.0

@@ -44,6 +44,30 @@ def test_complex_forward_matches_oracle(logarithmic):
         assert rel_err(J[f].cpu().numpy(), Jo) < 1e-4, f
 
 
+def test_complex_fields_match_oracle():
+    """mpf_eit_fields_complex (EIT::fields of the complex instantiations):
+    every component's complex potentials, in the reference's convention for
+    the Neumann harmonic, against the oracle's FP64 fields."""
+    import oracle
+    import torch
+    import mpflow_gb300 as mp
+    mesh, src, orc = make_setup(rings=16, ports=16, components=3, height=2.0)
+    g = _complex_frames(mesh, 2, seed=5, logarithmic=False)
+    model = mp.EIT(mesh, src, 1.0, components=3, height=2.0)
+    with pytest.raises(mp.MpfError):
+        model.fields_complex(1)  # no complex solve yet
+    model.solve_complex(torch.tensor(g, dtype=torch.complex64, device="cuda"),
+                        mp.SolveOptions(tol=1e-7, solver="bicgstab"))
+    Fz = model.fields_complex(2).cpu().numpy()  # (frames, C, Md+Mm, data_rows)
+    n = mesh.nodes.shape[0]
+    for f in range(2):
+        _, Fo = oracle.eit_forward_complex(orc, g[f], want_fields=True)
+        scale = np.abs(Fo[0]).max()
+        for c in range(3):
+            err = np.abs(Fz[f, c][:, :n].T - Fo[c]).max() / scale
+            assert err < 1e-5, (f, c, err)
+
+
 def test_complex_with_real_values_equals_real_solve():
     import torch
     import mpflow_gb300 as mp

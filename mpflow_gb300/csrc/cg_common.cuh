@@ -77,7 +77,7 @@ __device__ __forceinline__ float diag_inv(const float2* SR, const int32_t* diagS
     const int ds = __ldg(&diagSlot[row]);
     const float2 e = __ldg(&SR[(size_t)ds * npad + row]);
     const float d = e.x + alpha * e.y;
-    return d != 0.f ? 1.f / d : 0.f;
+    return d != 0.f ? __frcp_rn(d) : 0.f;  // correctly rounded: the same value as 1.f / d
 }
 
 // Rows of one mesh: a single mesh covers tiles [0, nblk) and rows < n; a

@@ -628,6 +628,10 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
     }
     DotAcc acc[1][VEC];
     float rsum[VEC] = {};
+    // r.D^-1 r: its terms are never negative, so each thread sums a tile's
+    // terms in FP32 (no cancellation) and folds that sum into the
+    // compensated pair once per tile
+    float rz[VEC] = {};
     __shared__ float red[kWarps * 32 * VEC];
     const int tile0 = sg.tile0 + blockIdx.x * T;
     const int nsteps = (min(sg.tile0 + sg.nblk, tile0 + T) - tile0) * Sh::STEPS;
@@ -649,10 +653,17 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
                 rv[i][v] = fmaf(-a[v], qv[i][v], rv[i][v]);
-                acc[0][v].add(rv[i][v], di[i] * rv[i][v]);
+                rz[v] = fmaf(rv[i][v], di[i] * rv[i][v], rz[v]);
                 rsum[v] += rv[i][v];  // padding rows keep r = 0
             }
             stv<VEC>(P.r + o[i], rv[i]);
+        }
+        if ((st % Sh::STEPS) + RB == Sh::STEPS) {  // end of a tile
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                acc[0][v].addf(rz[v]);
+                rz[v] = 0.f;
+            }
         }
         if (P.coarse && (st % Sh::STEPS) + RB == Sh::STEPS) {
             restrict_tile<KP, VEC>(rsum, tile0 - sg.tile0 + st / Sh::STEPS, seg_aggregates(sg),
@@ -661,6 +672,8 @@ __global__ void __launch_bounds__(kThreads) k_update(CgProblem P) {
             for (int v = 0; v < VEC; ++v) rsum[v] = 0.f;
         }
     }
+#pragma unroll
+    for (int v = 0; v < VEC; ++v) acc[0][v].addf(rz[v]);  // terms after the last tile end (if any)
     double* const parts[1] = {P.partA};
     if (block_partials<KP, VEC, 1>(acc, parts, g, P.counter, nb)) {
         // the step length of this iteration, for the deferred x update

@@ -600,10 +600,12 @@ __global__ void k_to_f32(size_t count, const double* __restrict__ src, float* __
 // need the earlier), written to X (row-major) and to XT = X^T (row-major, so
 // that the transposed product is also a row-wise one).  X_jj = D_j,
 // X_ij = -D_i sum_{k=j}^{i-1} L_ik X_kj, the L_ik staged one 32 x 32 tile at
-// a time.  Thread t owns row t / 8 and columns 4 (t % 8) .. + 3 of the
-// block in progress.  Measured alternatives, 32 frames of 1024: this order
-// 2.8 ms; right-looking (each block column of L read once per step) 3.7 ms;
-// each thread streaming its row of L from memory without staging 8.4 ms.
+// a time (the next tile's loads in flight while the current one is used).
+// Thread t owns row t / 8 and columns 4 (t % 8) .. + 3 of the block in
+// progress.  Measured alternatives, 32 frames of 1024: this order without
+// the prefetch 2.8 ms; right-looking (each block column of L read once per
+// step) 3.7 ms; each thread streaming its row of L from memory without
+// staging 8.4 ms.
 __global__ void __launch_bounds__(256) k_trtri_cols(int n, const float* __restrict__ L, const float* __restrict__ D,
                                                     float* __restrict__ X, float* __restrict__ XT,
                                                     const int* __restrict__ frameMask) {
@@ -621,13 +623,25 @@ __global__ void __launch_bounds__(256) k_trtri_cols(int n, const float* __restri
         if (i == j) {
             for (int e = t; e < NB * NB; e += 256) Xi[e] = Df[(size_t)j * NB * NB + e];
         } else {
-            // T = sum_k L_ik X_kj
+            // T = sum_k L_ik X_kj; the next tile of L is loaded into registers
+            // while the current one is used (4 elements per thread)
             float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            // element q of this thread: L(i NB + t % 32, k NB + t / 32 + 8 q), column-major
+            const float* Lp = Lf + (size_t)(t / NB) * n + i * NB + (t % NB);
+            float n0 = Lp[(size_t)(j * NB) * n], n1 = Lp[(size_t)(j * NB + 8) * n];
+            float n2 = Lp[(size_t)(j * NB + 16) * n], n3 = Lp[(size_t)(j * NB + 24) * n];
             for (int k = j; k < i; ++k) {
                 __syncthreads();  // Lt free
-                for (int e = t; e < NB * NB; e += 256) {
-                    const int rr = e % NB, cc = e / NB;  // L(i NB + rr, k NB + cc), column-major
-                    Lt[rr][cc] = Lf[(size_t)(k * NB + cc) * n + i * NB + rr];
+                Lt[t % NB][t / NB] = n0;
+                Lt[t % NB][t / NB + 8] = n1;
+                Lt[t % NB][t / NB + 16] = n2;
+                Lt[t % NB][t / NB + 24] = n3;
+                if (k + 1 < i) {
+                    const float* Lk = Lp + (size_t)((k + 1) * NB) * n;
+                    n0 = Lk[0];
+                    n1 = Lk[(size_t)8 * n];
+                    n2 = Lk[(size_t)16 * n];
+                    n3 = Lk[(size_t)24 * n];
                 }
                 __syncthreads();
                 const float* Xk = col + (size_t)(k - j) * NB * NB;

@@ -74,3 +74,25 @@ def test_new_entry_points_reject_bad_arguments_without_gpu():
     assert L.mpf_profile_gram(1, 100, 64, 1, ctypes.byref(ms), None) == 1
     assert b"rows" in L.mpf_last_error()
     assert L.mpf_profile_gram(0, 128, 64, 1, ctypes.byref(ms), None) == 1
+
+
+def test_entry_points_of_this_build_reject_bad_arguments_without_gpu():
+    """Argument checks of the device conversion, the training step, the
+    complex field export and the CG loop hook run before any device work;
+    the solve options carry the acceptance-solve fields in header order."""
+    L = mpflow_gb300.lib()
+    assert L.mpf_convert_values(2, 4, None, None, None) == 1
+    assert b"direction" in L.mpf_last_error()
+    assert L.mpf_convert_values(0, -1, None, None, None) == 1
+    assert L.mpf_convert_values(0, 0, None, None, None) == 0  # nothing to convert
+    assert L.mpf_mlp_train_step(None, 1, None, 0, None, None, 0, 1, 1e-3, 0.9, 0.999, 1e-8, 0.0, None, None) == 1
+    assert L.mpf_eit_fields_complex(None, 1, None, None) == 1
+    assert b"model == nullptr" in L.mpf_last_error()
+    assert L.mpf_eit_profile_cg_loop(None, 1, None, 1, None, None) == 1
+    from mpflow_gb300 import _ffi
+    from mpflow_gb300.eit import SolveOptions
+    o = SolveOptions(tol=1e-5, gn_factor="fp32-refined", accept_tol=1e-4, accept_margin=0.2).c()
+    assert (o.gn_factor, o.accept_tol, o.accept_margin) == (1, 1e-4, 0.2)
+    names = [f[0] for f in _ffi.SolveOpts._fields_]
+    assert names[-3:] == ["gn_factor", "accept_tol", "accept_margin"]
+    assert [f[0] for f in _ffi.GnStats._fields_][-1] == "accepted_loose"

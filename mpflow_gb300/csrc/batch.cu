@@ -377,7 +377,10 @@ int batch_forward(mpf_batch* b, int F, const float* const* gamma, float* const* 
     MPF_CHECK(F >= 1 && gamma && V, MPF_EINVAL, "mpf_batch_forward: bad arguments");
     for (int i = 0; i < b->M; ++i)
         MPF_CHECK(gamma[i] && V[i], MPF_EINVAL, "mpf_batch_forward: gamma[%d] or voltages[%d] == nullptr", i, i);
-    mpf_solve_opts o{1e-6, 0, 0.0, 6, 0, 16, 0};
+    mpf_solve_opts o{};
+    o.tol = 1e-6;
+    o.max_refine = 6;
+    o.check_every = 16;
     if (in) o = *in;
     MPF_CHECK(o.refine_tol <= 0.0 && o.warm_start == 0, MPF_ENOTSUP,
               "mpf_batch_forward: batches solve cold without FP64 refinement");

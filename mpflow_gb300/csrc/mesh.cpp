@@ -265,8 +265,8 @@ int build_structure(int N, int E, const int32_t* elements, FemStructure& fs) {
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) {
                 int32_t r = elements[3 * e + i], c = elements[3 * e + j];
-                int slot;
-                slot_of(r, c, false, slot);
+                int slot = 0;
+                MPF_TRY(slot_of(r, c, false, slot));  // inserted by the pass above
                 int v = ++cnt[(size_t)slot * P + r];
                 levels = std::max(levels, v);
             }
@@ -279,8 +279,8 @@ int build_structure(int N, int E, const int32_t* elements, FemStructure& fs) {
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) {
                 int32_t r = elements[3 * e + i], c = elements[3 * e + j];
-                int slot;
-                slot_of(r, c, false, slot);
+                int slot = 0;
+                MPF_TRY(slot_of(r, c, false, slot));
                 fs.contrib[fill[(size_t)slot * P + r]++] = e * 9 + i * 3 + j;
             }
     return MPF_OK;

@@ -65,7 +65,10 @@ def test_solver_from_config_matches_python(tmp_path):
     got = np.loadtxt(d / "result.txt")
     Vmt = torch.tensor(np.loadtxt(d / "measurement.txt"), dtype=torch.float32, device="cuda")[None]
     want = 1.0 + model.inverse(J[0], V0, Vmt, factor, "identity")[0].cpu().numpy()
-    assert np.abs(got - want).max() <= 1e-5 * max(np.abs(want - 1.0).max(), 1e-12) + 1e-6
+    # two independent forward solves at CG tolerance 1e-6 (the launch shapes
+    # are autotuned by timing in each process, so the summation orders can
+    # differ); the inverse amplifies their difference to ~3e-5 of the update
+    assert np.abs(got - want).max() <= 1e-4 * max(np.abs(want - 1.0).max(), 1e-12) + 1e-6
 
 
 @pytest.mark.gpu
